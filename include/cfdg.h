@@ -1,0 +1,210 @@
+/* cfdg — GB300 (sm_103a) residual-and-Newton path for a 2D unstructured
+ * cell-centred finite-volume compressible-flow solver.
+ *
+ * C ABI of libcfdgpu.so.  Plain pointers and sizes only.  It replaces the C++ class
+ * surface of the reference solver (AmberMond/mycode): Mesh (include/Mesh.hpp),
+ * Solver (include/Solver.hpp) and the flux library (include/Flux.hpp).  Each entry
+ * point names the reference interface it stands in for.
+ *
+ * Conventions
+ *  - Every call returns a cfdg_status (0 = ok).  cfdg_last_error() gives the
+ *    message of the calling thread's last failure.
+ *  - States, residuals and vectors cross the ABI in the reference's layout and
+ *    numbering: AoS, 6 doubles per cell {rho, rhou, rhov, rhoE, rhok, rhow}
+ *    (struct State, include/Types.hpp:55-82), cells in the order they were given.
+ *    The library renumbers the mesh internally and permutes on entry and exit.
+ *  - A cfdg_mesh must outlive the solvers made from it (the reference's Solver
+ *    holds a const Mesh&, include/Solver.hpp:117).
+ *  - One CUDA stream per solver.  A solver is not thread-safe; distinct solvers are
+ *    independent.
+ *  - There is no CPU fallback: every compute entry point runs on the GPU and
+ *    returns CFDG_ERR_CUDA when no usable device exists.
+ */
+#ifndef CFDG_H
+#define CFDG_H
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef enum cfdg_status {
+    CFDG_OK = 0,
+    CFDG_ERR_ARG = 1,           /* bad argument or size */
+    CFDG_ERR_CUDA = 2,          /* CUDA runtime failure or no device */
+    CFDG_ERR_NAN = 3,           /* non-finite or non-positive density/pressure found */
+    CFDG_ERR_NOT_CONVERGED = 4, /* solve stopped at max_steps above tolerance */
+    CFDG_ERR_TIMEOUT = 5,       /* a bounded device-side wait gave up */
+    CFDG_ERR_MESH = 6,          /* mesh file or connectivity error */
+    CFDG_ERR_UNSUPPORTED = 7,   /* option combination not available */
+    CFDG_ERR_BREAKDOWN = 8      /* GMRES breakdown (zero Krylov direction) */
+} cfdg_status;
+
+/* FluxScheme (include/Types.hpp:38-43); AUSM evaluates LLF as in include/Flux.hpp:225 */
+enum { CFDG_FLUX_LLF = 0, CFDG_FLUX_ROE = 1, CFDG_FLUX_HLLC = 2, CFDG_FLUX_AUSM = 3 };
+/* SpatialScheme (include/Types.hpp:45-49) */
+enum { CFDG_FIRST_ORDER = 0, CFDG_SECOND_ORDER_CENTRAL = 1, CFDG_SECOND_ORDER_LIMITED = 2 };
+/* boundary-condition sets: the reference's getBoundaryGhostState variants
+ * bump (src/Solver.cpp:806-863), supersonic (:973-1011), flat plate / SWBLI (:1088-1139) */
+enum { CFDG_BC_BUMP = 0, CFDG_BC_SUPERSONIC = 1, CFDG_BC_PLATE = 2 };
+/* initialize variants: bump (src/Solver.cpp:46-65), free stream (:905-920) */
+enum { CFDG_INIT_BUMP = 0, CFDG_INIT_FREESTREAM = 1 };
+/* arithmetic of the Newton-Krylov loop */
+enum { CFDG_FP64 = 0, CFDG_MIXED = 1 };
+/* Jacobian-vector product: one-sided finite difference (src/Solver.cpp:1331-1386) or
+ * exact forward linearisation (no reference counterpart) */
+enum { CFDG_JV_FD = 0, CFDG_JV_EXACT = 1 };
+enum { CFDG_RENUMBER_NONE = 0, CFDG_RENUMBER_HILBERT = 1, CFDG_RENUMBER_RCM = 2 };
+enum { CFDG_TURB_NONE = 0, CFDG_TURB_SST = 1 };
+
+typedef struct cfdg_config {
+    int flux;              /* CFDG_FLUX_*; reference default HLLC (include/Solver.hpp:33) */
+    int spatial;           /* CFDG_*_ORDER; reference default SECOND_ORDER_LIMITED (:34) */
+    int bcset;             /* CFDG_BC_* */
+    int init;              /* CFDG_INIT_* */
+    int viscous;           /* 1: subtract the viscous flux (src/Solver.cpp:787 instead of :792) */
+    int turbulence;        /* CFDG_TURB_*; SST adds rhok, rhow (no reference counterpart) */
+    int precision;         /* CFDG_FP64 or CFDG_MIXED (FP32 Krylov, Jv and preconditioner) */
+    int jv;                /* CFDG_JV_FD or CFDG_JV_EXACT */
+    int gmres_m;           /* Krylov dimension; reference 40 (src/Solver.cpp:1479) */
+    double gmres_tol;      /* relative tolerance; reference 1e-2 (src/Solver.cpp:1587) */
+    double gamma;          /* 1.4 (include/Flux.hpp:9, include/Solver.hpp:91) */
+    double R_gas;          /* 287 (include/Solver.hpp:92) */
+    double Pr;             /* 0.72 (src/Solver.cpp:541) */
+    double nu;             /* 0.01 until setKinematicViscosity (include/Solver.hpp:42) */
+    double cfl0;           /* 0.1 (src/Solver.cpp:1701) */
+    double cfl_max;        /* 1e4 (src/Solver.cpp:1790) */
+    int limiter_freeze_step;   /* 150 (src/Solver.cpp:1714) */
+    double limiter_freeze_cfl; /* 10 (src/Solver.cpp:1714) */
+    /* SST free stream (no reference counterpart) */
+    double turb_intensity; /* Tu, e.g. 0.001 */
+    double mut_ratio;      /* mu_t / mu in the free stream, e.g. 0.01 */
+    double shock_deflection_deg; /* tag-6 post-shock inflow; 0 = unused */
+    int renumber;          /* CFDG_RENUMBER_* */
+    int device;            /* CUDA device ordinal */
+} cfdg_config;
+
+/* per-step record of a Newton solve (the reference prints these, src/Solver.cpp:1725-1727, :1746) */
+typedef struct cfdg_step {
+    double res_vm;         /* volume-weighted L2 of all components (norm_L2_VolumeWeighted) */
+    double res_abs;        /* plain L2 (norm_L2) */
+    double res_rho;        /* volume-weighted L2 of the density component */
+    double cfl;
+    int gmres_iters;
+    int limiter_updated;
+    double seconds;        /* wall time of the step */
+} cfdg_step;
+
+typedef struct cfdg_mesh cfdg_mesh;
+typedef struct cfdg_solver cfdg_solver;
+
+const char* cfdg_version(void);
+const char* cfdg_last_error(void);
+/* number of visible CUDA devices (0 when none) */
+cfdg_status cfdg_device_count(int* n);
+void cfdg_config_default(cfdg_config* cfg);
+
+/* ---- mesh: Mesh::load / buildConnectivity / computeGeometry (src/Mesh.cpp:10-201) */
+
+/* From arrays: xy[2*n_nodes]; cells[4*n_cells] 0-based node ids, -1 in the fourth
+ * slot for a triangle; bedges[3*n_bedges] = (node a, node b, physical tag). */
+cfdg_status cfdg_mesh_create(int n_nodes, const double* xy, int n_cells, const int* cells,
+                             int n_bedges, const int* bedges, int renumber, cfdg_mesh** out);
+/* Mesh::load (src/Mesh.cpp:10-26) on a Gmsh 2.2 ASCII file; LF and CRLF both accepted */
+cfdg_status cfdg_mesh_load_gmsh(const char* path, int renumber, cfdg_mesh** out);
+/* Mesh::getNumCells / getNumFaces (include/Mesh.hpp:25-27) */
+cfdg_status cfdg_mesh_sizes(const cfdg_mesh* m, int* n_cells, int* n_faces, int* n_boundary_faces);
+/* public Mesh::faces in reference order: ints5 = node1, node2, owner, neighbor, bcTag
+ * (0-based nodes); dbl5 = nx, ny, area, x_mid, y_mid (struct Face, include/Types.hpp:16-27) */
+cfdg_status cfdg_mesh_faces(const cfdg_mesh* m, int* ints5, double* dbl5);
+/* public Mesh::cells: volume, x_c, y_c per cell (struct Cell, include/Types.hpp:30-35) */
+cfdg_status cfdg_mesh_cells(const cfdg_mesh* m, double* vol_xc_yc);
+/* internal numbering: cell_perm[new] = reference cell, face_perm[new] = reference face */
+cfdg_status cfdg_mesh_permutation(const cfdg_mesh* m, int* cell_perm, int* face_perm);
+void cfdg_mesh_destroy(cfdg_mesh* m);
+
+/* ---- solver: Solver(const Mesh&) (src/Solver.cpp:7-10) */
+cfdg_status cfdg_solver_create(const cfdg_mesh* m, const cfdg_config* cfg, cfdg_solver** out);
+void cfdg_solver_destroy(cfdg_solver* s);
+/* Solver::setNumericalMethod (include/Solver.hpp:33-36) */
+cfdg_status cfdg_set_numerical_method(cfdg_solver* s, int flux, int spatial);
+/* Solver::setFlowConditions (src/Solver.cpp:12-32) */
+cfdg_status cfdg_set_flow_conditions(cfdg_solver* s, double mach, double p_ref, double t_ref);
+/* Solver::setFreestreamStatic (src/Solver.cpp:2017-2025) */
+cfdg_status cfdg_set_freestream_static(cfdg_solver* s, double mach, double p_static, double t_static);
+/* Solver::setKinematicViscosity (src/Solver.cpp:34-43) */
+cfdg_status cfdg_set_kinematic_viscosity(cfdg_solver* s, double reynolds, double l_ref);
+/* Solver::initialize (src/Solver.cpp:46-65 / :905-920, chosen by cfg.init) */
+cfdg_status cfdg_initialize(cfdg_solver* s);
+/* M_inf, P_total_inlet, T_total_inlet, P_static_exit, nu, R_gas (include/Solver.hpp:37-39, :93-95) */
+cfdg_status cfdg_get_params(const cfdg_solver* s, double* out6);
+
+/* Solver::getSolution (include/Solver.hpp:58) and its setter */
+cfdg_status cfdg_set_state(cfdg_solver* s, const double* U);
+cfdg_status cfdg_get_state(cfdg_solver* s, double* U);
+
+/* Solver::computeResiduals (src/Solver.cpp:529-801).  U = NULL uses the current state.
+ * update_limiters = 0 keeps the last limiter values (the frozen limiter of JFNK). */
+cfdg_status cfdg_residual(cfdg_solver* s, const double* U, double* R, int update_limiters);
+/* Solver::computeGradients (src/Solver.cpp:81-149): 10 per cell in CellGradient order
+ * drho/dx, drho/dy, du/dx, du/dy, dv/dx, dv/dy, dp/dx, dp/dy, dT/dx, dT/dy */
+cfdg_status cfdg_gradients(cfdg_solver* s, const double* U, double* grad10);
+/* Solver::computeLimiters (src/Solver.cpp:152-253) after computeGradients on U */
+cfdg_status cfdg_limiters(cfdg_solver* s, const double* U, double* phi);
+cfdg_status cfdg_get_limiters(cfdg_solver* s, double* phi);
+cfdg_status cfdg_set_limiters(cfdg_solver* s, const double* phi);
+/* Solver::computeLocalTimeStep (src/Solver.cpp:1388-1422) on the current state;
+ * keeps dt for cfdg_jv / cfdg_preconditioner / cfdg_gmres */
+cfdg_status cfdg_local_timestep(cfdg_solver* s, double cfl, double* dt);
+cfdg_status cfdg_set_timestep(cfdg_solver* s, const double* dt);
+/* Solver::computeDiagonalPreconditioner (src/Solver.cpp:1424-1465) on the current state */
+cfdg_status cfdg_preconditioner(cfdg_solver* s, double* D);
+/* Solver::applyJacobian (src/Solver.cpp:1331-1386): Jv = dR/dU v + (vol/dt) v with the
+ * limiter frozen.  mode CFDG_JV_FD reproduces the reference's one-sided difference
+ * about (U_base, R_base); CFDG_JV_EXACT is the exact linearisation (R_base unused). */
+cfdg_status cfdg_jv(cfdg_solver* s, const double* U_base, const double* R_base, const double* v,
+                    double* Jv, int mode);
+/* Solver::solveGMRES (src/Solver.cpp:1472-1618): one right-preconditioned MGS-GMRES
+ * cycle from x0 = 0 for (vol/dt + dR/dU) x = rhs at U_base. */
+cfdg_status cfdg_gmres(cfdg_solver* s, const double* U_base, const double* R_base, const double* rhs,
+                       double* x, int* iters);
+/* Solver::norm_L2_VolumeWeighted (src/Solver.cpp:1280-1303) */
+cfdg_status cfdg_norm_vm(cfdg_solver* s, const double* R, double* out);
+/* Solver::solveImplicit (src/Solver.cpp:1696-1799) on the device-resident state.
+ * trace (may be NULL) receives up to max_steps records; *n_steps the count.
+ * Returns CFDG_ERR_NOT_CONVERGED when max_steps ran out above tol. */
+cfdg_status cfdg_solve_implicit(cfdg_solver* s, double tol, int max_steps, cfdg_step* trace, int* n_steps);
+/* one pseudo-transient Newton step of solveImplicit; *converged set when the
+ * step's residual was already below tol (no update made) */
+cfdg_status cfdg_newton_step(cfdg_solver* s, double tol, cfdg_step* info, int* converged);
+/* Newton driver state (CFL, step counter) */
+cfdg_status cfdg_reset_newton(cfdg_solver* s);
+
+/* Adjoint: gU = (dR/dU)^T lambda for the full residual at U, gradients and limiter
+ * recomputed and differentiated along the branches the forward pass took (no
+ * reference counterpart).  U = NULL uses the current state. */
+cfdg_status cfdg_vjp(cfdg_solver* s, const double* U, const double* lambda, double* gU);
+
+/* Wall quantities (src/Solver.cpp:1307-1325 calculateDrag, :1899-1979
+ * extractSkinFriction): per boundary face of the given tag in reference face order,
+ * x_mid, Cp (p - p_inf)/q_inf and Cf (one-sided wall shear / q_inf).  *n gets the count;
+ * buffers may be NULL to query it. */
+cfdg_status cfdg_wall_coefficients(cfdg_solver* s, int tag, double* x_mid, double* cp, double* cf, int* n);
+/* calculateDrag (src/Solver.cpp:1307-1325): sum of -p A n_x over tag-3 faces */
+cfdg_status cfdg_drag(cfdg_solver* s, double* drag);
+/* calculateEntropyError (src/Solver.cpp:1620-1646) */
+cfdg_status cfdg_entropy_error(cfdg_solver* s, double* err);
+
+/* ---- device-resident entry points (no host copies): the benchmark's kernel path */
+/* R(U_current) into the solver's device residual */
+cfdg_status cfdg_residual_device(cfdg_solver* s, int update_limiters);
+cfdg_status cfdg_synchronize(cfdg_solver* s);
+/* per-kernel CUDA-event timings of the last cfdg_residual_device with timing on */
+cfdg_status cfdg_set_timing(cfdg_solver* s, int on);
+cfdg_status cfdg_kernel_times(cfdg_solver* s, double* ms_prim, double* ms_grad, double* ms_flux, double* ms_gather);
+/* kernel launches issued by this solver since creation (all of them are this library's) */
+cfdg_status cfdg_launch_count(cfdg_solver* s, long long* n);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* CFDG_H */

@@ -1,0 +1,398 @@
+"""Python front-end of libcfdgpu (ctypes over the C ABI in include/cfdg.h).
+
+Mirrors the reference's class surface so drivers and tests read like the
+reference's own code: ``Mesh.load`` / faces / cells (include/Mesh.hpp) and
+``Solver`` with setNumericalMethod, setFlowConditions, setFreestreamStatic,
+setKinematicViscosity, initialize, computeResiduals, solveImplicit, getSolution
+(include/Solver.hpp).  States and residuals are numpy arrays in the reference's
+AoS layout: shape (n_cells, 6), columns rho, rhou, rhov, rhoE, rhok, rhow, cells in
+the order the mesh was given.
+
+There is no CPU path: every compute call runs the CUDA kernels and raises
+:class:`CfdgError` when the library or a GPU is missing.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+
+import numpy as np
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(_HERE, "_lib", "libcfdgpu.so")
+
+FLUX = {"LLF": 0, "ROE": 1, "HLLC": 2, "AUSM": 3}
+SPATIAL = {"FIRST_ORDER": 0, "SECOND_ORDER_CENTRAL": 1, "SECOND_ORDER_LIMITED": 2}
+BCSET = {"bump": 0, "supersonic": 1, "plate": 2}
+INIT = {"bump": 0, "freestream": 1}
+PRECISION = {"fp64": 0, "mixed": 1}
+JV = {"fd": 0, "exact": 1}
+RENUMBER = {"none": 0, "hilbert": 1, "rcm": 2}
+STATUS = {0: "OK", 1: "ERR_ARG", 2: "ERR_CUDA", 3: "ERR_NAN", 4: "ERR_NOT_CONVERGED", 5: "ERR_TIMEOUT",
+          6: "ERR_MESH", 7: "ERR_UNSUPPORTED", 8: "ERR_BREAKDOWN"}
+
+
+class CfdgError(RuntimeError):
+    def __init__(self, status: int, msg: str):
+        super().__init__(f"{STATUS.get(status, status)}: {msg}")
+        self.status = status
+
+
+class Config(C.Structure):
+    _fields_ = [
+        ("flux", C.c_int), ("spatial", C.c_int), ("bcset", C.c_int), ("init", C.c_int),
+        ("viscous", C.c_int), ("turbulence", C.c_int), ("precision", C.c_int), ("jv", C.c_int),
+        ("gmres_m", C.c_int), ("gmres_tol", C.c_double), ("gamma", C.c_double), ("R_gas", C.c_double),
+        ("Pr", C.c_double), ("nu", C.c_double), ("cfl0", C.c_double), ("cfl_max", C.c_double),
+        ("limiter_freeze_step", C.c_int), ("limiter_freeze_cfl", C.c_double),
+        ("turb_intensity", C.c_double), ("mut_ratio", C.c_double), ("shock_deflection_deg", C.c_double),
+        ("renumber", C.c_int), ("device", C.c_int),
+    ]
+
+
+class Step(C.Structure):
+    _fields_ = [("res_vm", C.c_double), ("res_abs", C.c_double), ("res_rho", C.c_double),
+                ("cfl", C.c_double), ("gmres_iters", C.c_int), ("limiter_updated", C.c_int),
+                ("seconds", C.c_double)]
+
+
+_lib = None
+_dp = np.ctypeslib.ndpointer(dtype=np.float64, flags="C_CONTIGUOUS")
+_ip = np.ctypeslib.ndpointer(dtype=np.int32, flags="C_CONTIGUOUS")
+_vp = C.c_void_p
+
+
+def _opt_dp(a):
+    return None if a is None else np.ascontiguousarray(a, dtype=np.float64).ctypes.data_as(C.POINTER(C.c_double))
+
+
+SIGNATURES = {
+    "cfdg_version": (C.c_char_p, []),
+    "cfdg_last_error": (C.c_char_p, []),
+    "cfdg_device_count": (C.c_int, [C.POINTER(C.c_int)]),
+    "cfdg_config_default": (None, [C.POINTER(Config)]),
+    "cfdg_mesh_create": (C.c_int, [C.c_int, _dp, C.c_int, _ip, C.c_int, _vp, C.c_int, C.POINTER(_vp)]),
+    "cfdg_mesh_load_gmsh": (C.c_int, [C.c_char_p, C.c_int, C.POINTER(_vp)]),
+    "cfdg_mesh_sizes": (C.c_int, [_vp, C.POINTER(C.c_int), C.POINTER(C.c_int), C.POINTER(C.c_int)]),
+    "cfdg_mesh_faces": (C.c_int, [_vp, _ip, _dp]),
+    "cfdg_mesh_cells": (C.c_int, [_vp, _dp]),
+    "cfdg_mesh_permutation": (C.c_int, [_vp, _ip, _ip]),
+    "cfdg_mesh_destroy": (None, [_vp]),
+    "cfdg_solver_create": (C.c_int, [_vp, C.POINTER(Config), C.POINTER(_vp)]),
+    "cfdg_solver_destroy": (None, [_vp]),
+    "cfdg_set_numerical_method": (C.c_int, [_vp, C.c_int, C.c_int]),
+    "cfdg_set_flow_conditions": (C.c_int, [_vp, C.c_double, C.c_double, C.c_double]),
+    "cfdg_set_freestream_static": (C.c_int, [_vp, C.c_double, C.c_double, C.c_double]),
+    "cfdg_set_kinematic_viscosity": (C.c_int, [_vp, C.c_double, C.c_double]),
+    "cfdg_initialize": (C.c_int, [_vp]),
+    "cfdg_get_params": (C.c_int, [_vp, _dp]),
+    "cfdg_set_state": (C.c_int, [_vp, _dp]),
+    "cfdg_get_state": (C.c_int, [_vp, _dp]),
+    "cfdg_residual": (C.c_int, [_vp, C.c_void_p, _dp, C.c_int]),
+    "cfdg_gradients": (C.c_int, [_vp, C.c_void_p, _dp]),
+    "cfdg_limiters": (C.c_int, [_vp, C.c_void_p, _dp]),
+    "cfdg_get_limiters": (C.c_int, [_vp, _dp]),
+    "cfdg_set_limiters": (C.c_int, [_vp, _dp]),
+    "cfdg_local_timestep": (C.c_int, [_vp, C.c_double, C.c_void_p]),
+    "cfdg_set_timestep": (C.c_int, [_vp, _dp]),
+    "cfdg_preconditioner": (C.c_int, [_vp, _dp]),
+    "cfdg_jv": (C.c_int, [_vp, _dp, C.c_void_p, _dp, _dp, C.c_int]),
+    "cfdg_gmres": (C.c_int, [_vp, C.c_void_p, C.c_void_p, _dp, _dp, C.POINTER(C.c_int)]),
+    "cfdg_norm_vm": (C.c_int, [_vp, _dp, C.POINTER(C.c_double)]),
+    "cfdg_solve_implicit": (C.c_int, [_vp, C.c_double, C.c_int, C.POINTER(Step), C.POINTER(C.c_int)]),
+    "cfdg_newton_step": (C.c_int, [_vp, C.c_double, C.POINTER(Step), C.POINTER(C.c_int)]),
+    "cfdg_reset_newton": (C.c_int, [_vp]),
+    "cfdg_vjp": (C.c_int, [_vp, C.c_void_p, _dp, _dp]),
+    "cfdg_wall_coefficients": (C.c_int, [_vp, C.c_int, C.c_void_p, C.c_void_p, C.c_void_p, C.POINTER(C.c_int)]),
+    "cfdg_drag": (C.c_int, [_vp, C.POINTER(C.c_double)]),
+    "cfdg_entropy_error": (C.c_int, [_vp, C.POINTER(C.c_double)]),
+    "cfdg_residual_device": (C.c_int, [_vp, C.c_int]),
+    "cfdg_synchronize": (C.c_int, [_vp]),
+    "cfdg_set_timing": (C.c_int, [_vp, C.c_int]),
+    "cfdg_kernel_times": (C.c_int, [_vp] + [C.POINTER(C.c_double)] * 4),
+    "cfdg_launch_count": (C.c_int, [_vp, C.POINTER(C.c_longlong)]),
+}
+
+
+def lib():
+    """The loaded libcfdgpu.so; raises when it has not been built."""
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIB_PATH):
+            raise CfdgError(2, f"{LIB_PATH} is missing: build it with mycode_gb300.build.build() "
+                               "(this package has no CPU fallback)")
+        L = C.CDLL(LIB_PATH)
+        for name, (res, args) in SIGNATURES.items():
+            fn = getattr(L, name)
+            fn.restype = res
+            fn.argtypes = args
+        _lib = L
+    return _lib
+
+
+def _check(st: int):
+    if st != 0:
+        raise CfdgError(st, lib().cfdg_last_error().decode())
+
+
+def device_count() -> int:
+    n = C.c_int(0)
+    _check(lib().cfdg_device_count(C.byref(n)))
+    return n.value
+
+
+def default_config(**overrides) -> Config:
+    c = Config()
+    lib().cfdg_config_default(C.byref(c))
+    for k, v in overrides.items():
+        if k == "flux" and isinstance(v, str):
+            v = FLUX[v]
+        elif k == "spatial" and isinstance(v, str):
+            v = SPATIAL[v]
+        elif k == "bcset" and isinstance(v, str):
+            v = BCSET[v]
+        elif k == "init" and isinstance(v, str):
+            v = INIT[v]
+        elif k == "precision" and isinstance(v, str):
+            v = PRECISION[v]
+        elif k == "jv" and isinstance(v, str):
+            v = JV[v]
+        elif k == "renumber" and isinstance(v, str):
+            v = RENUMBER[v]
+        elif k == "turbulence" and isinstance(v, str):
+            v = {"none": 0, "sst": 1}[v]
+        if not hasattr(c, k):
+            raise KeyError(k)
+        setattr(c, k, v)
+    return c
+
+
+class Mesh:
+    """Mesh::load / buildConnectivity / computeGeometry (src/Mesh.cpp:10-201), renumbered for the GPU."""
+
+    def __init__(self, handle):
+        self._h = handle
+        nc, nf, nb = C.c_int(), C.c_int(), C.c_int()
+        _check(lib().cfdg_mesh_sizes(self._h, C.byref(nc), C.byref(nf), C.byref(nb)))
+        self.n_cells, self.n_faces, self.n_boundary_faces = nc.value, nf.value, nb.value
+
+    @classmethod
+    def from_spec(cls, spec, renumber="hilbert") -> "Mesh":
+        xy = np.ascontiguousarray(spec.nodes, dtype=np.float64).ravel()
+        cells = np.ascontiguousarray(spec.cells, dtype=np.int32).ravel()
+        bed = np.ascontiguousarray(spec.bedges, dtype=np.int32).ravel()
+        h = _vp()
+        _check(lib().cfdg_mesh_create(spec.n_nodes, xy, spec.n_cells, cells, spec.bedges.shape[0],
+                                      bed.ctypes.data_as(_vp) if bed.size else None,
+                                      RENUMBER[renumber] if isinstance(renumber, str) else int(renumber),
+                                      C.byref(h)))
+        m = cls(h)
+        m._keep = (xy, cells, bed)
+        return m
+
+    @classmethod
+    def load(cls, path: str, renumber="hilbert") -> "Mesh":
+        h = _vp()
+        _check(lib().cfdg_mesh_load_gmsh(path.encode(), RENUMBER[renumber] if isinstance(renumber, str)
+                                         else int(renumber), C.byref(h)))
+        return cls(h)
+
+    def faces(self):
+        i5 = np.zeros(5 * self.n_faces, np.int32)
+        d5 = np.zeros(5 * self.n_faces)
+        _check(lib().cfdg_mesh_faces(self._h, i5, d5))
+        return i5.reshape(-1, 5), d5.reshape(-1, 5)
+
+    def cells(self):
+        d = np.zeros(3 * self.n_cells)
+        _check(lib().cfdg_mesh_cells(self._h, d))
+        return d.reshape(-1, 3)
+
+    def permutation(self):
+        cp = np.zeros(self.n_cells, np.int32)
+        fp = np.zeros(self.n_faces, np.int32)
+        _check(lib().cfdg_mesh_permutation(self._h, cp, fp))
+        return cp, fp
+
+    def __del__(self):
+        try:
+            lib().cfdg_mesh_destroy(self._h)
+        except Exception:
+            pass
+
+
+class Solver:
+    """The GPU solver with the reference Solver's method names (include/Solver.hpp:26-66)."""
+
+    def __init__(self, mesh: Mesh, config: Config | None = None, **overrides):
+        self.mesh = mesh
+        cfg = config if config is not None else default_config(**overrides)
+        if config is not None:
+            for k, v in overrides.items():
+                setattr(cfg, k, v)
+        self.config = cfg
+        h = _vp()
+        _check(lib().cfdg_solver_create(mesh._h, C.byref(cfg), C.byref(h)))
+        self._h = h
+        self.n_cells = mesh.n_cells
+
+    def __del__(self):
+        try:
+            if getattr(self, "_h", None):
+                lib().cfdg_solver_destroy(self._h)
+                self._h = None
+        except Exception:
+            pass
+
+    def close(self):
+        self.__del__()
+
+    # ---- configuration (Solver setters)
+    def setNumericalMethod(self, flux, spatial):
+        _check(lib().cfdg_set_numerical_method(self._h, FLUX[flux] if isinstance(flux, str) else flux,
+                                               SPATIAL[spatial] if isinstance(spatial, str) else spatial))
+
+    def setFlowConditions(self, M, P, T):
+        _check(lib().cfdg_set_flow_conditions(self._h, M, P, T))
+
+    def setFreestreamStatic(self, M, P, T):
+        _check(lib().cfdg_set_freestream_static(self._h, M, P, T))
+
+    def setKinematicViscosity(self, Re, L):
+        _check(lib().cfdg_set_kinematic_viscosity(self._h, Re, L))
+
+    def initialize(self):
+        _check(lib().cfdg_initialize(self._h))
+
+    def params(self):
+        o = np.zeros(6)
+        _check(lib().cfdg_get_params(self._h, o))
+        return dict(zip(["M_inf", "P0", "T0", "Pexit", "nu", "R_gas"], o))
+
+    # ---- state
+    def set_state(self, U):
+        _check(lib().cfdg_set_state(self._h, np.ascontiguousarray(U, np.float64).ravel()))
+
+    def getSolution(self):
+        U = np.zeros(6 * self.n_cells)
+        _check(lib().cfdg_get_state(self._h, U))
+        return U.reshape(-1, 6)
+
+    get_state = getSolution
+
+    # ---- residual path
+    def computeResiduals(self, U=None, update_limiters=True):
+        R = np.zeros(6 * self.n_cells)
+        u = None if U is None else np.ascontiguousarray(U, np.float64).ravel()
+        _check(lib().cfdg_residual(self._h, None if u is None else u.ctypes.data_as(_vp), R, int(update_limiters)))
+        return R.reshape(-1, 6)
+
+    residual = computeResiduals
+
+    def gradients(self, U=None):
+        g = np.zeros(10 * self.n_cells)
+        u = None if U is None else np.ascontiguousarray(U, np.float64).ravel()
+        _check(lib().cfdg_gradients(self._h, None if u is None else u.ctypes.data_as(_vp), g))
+        return g.reshape(-1, 10)
+
+    def limiters(self, U=None):
+        p = np.zeros(self.n_cells)
+        u = None if U is None else np.ascontiguousarray(U, np.float64).ravel()
+        _check(lib().cfdg_limiters(self._h, None if u is None else u.ctypes.data_as(_vp), p))
+        return p
+
+    def get_limiters(self):
+        p = np.zeros(self.n_cells)
+        _check(lib().cfdg_get_limiters(self._h, p))
+        return p
+
+    def set_limiters(self, phi):
+        _check(lib().cfdg_set_limiters(self._h, np.ascontiguousarray(phi, np.float64)))
+
+    def local_timestep(self, cfl):
+        dt = np.zeros(self.n_cells)
+        _check(lib().cfdg_local_timestep(self._h, float(cfl), dt.ctypes.data_as(_vp)))
+        return dt
+
+    def set_dt(self, dt):
+        _check(lib().cfdg_set_timestep(self._h, np.ascontiguousarray(dt, np.float64)))
+
+    def preconditioner(self):
+        D = np.zeros(self.n_cells)
+        _check(lib().cfdg_preconditioner(self._h, D))
+        return D
+
+    def apply_jacobian(self, Ub, Rb, v, mode="fd"):
+        J = np.zeros(6 * self.n_cells)
+        c = lambda a: np.ascontiguousarray(a, np.float64).ravel()
+        rb = None if Rb is None else c(Rb)
+        _check(lib().cfdg_jv(self._h, c(Ub), None if rb is None else rb.ctypes.data_as(_vp), c(v), J,
+                             JV[mode] if isinstance(mode, str) else mode))
+        return J.reshape(-1, 6)
+
+    def gmres(self, Ub, Rb, rhs):
+        x = np.zeros(6 * self.n_cells)
+        c = lambda a: None if a is None else np.ascontiguousarray(a, np.float64).ravel()
+        ub, rb = c(Ub), c(Rb)
+        it = C.c_int(0)
+        _check(lib().cfdg_gmres(self._h, None if ub is None else ub.ctypes.data_as(_vp),
+                                None if rb is None else rb.ctypes.data_as(_vp), c(rhs), x, C.byref(it)))
+        return it.value, x.reshape(-1, 6)
+
+    def norm_vm(self, R):
+        o = C.c_double()
+        _check(lib().cfdg_norm_vm(self._h, np.ascontiguousarray(R, np.float64).ravel(), C.byref(o)))
+        return o.value
+
+    def solveImplicit(self, tol=1e-6, max_steps=50, raise_on_nonconvergence=False):
+        tr = (Step * max(max_steps, 1))()
+        n = C.c_int(0)
+        st = lib().cfdg_solve_implicit(self._h, float(tol), int(max_steps), tr, C.byref(n))
+        if st != 0 and not (st == 4 and not raise_on_nonconvergence):
+            _check(st)
+        recs = tr[: n.value]
+        return {
+            "res_vm": np.array([r.res_vm for r in recs]),
+            "res_abs": np.array([r.res_abs for r in recs]),
+            "res_rho": np.array([r.res_rho for r in recs]),
+            "cfl": np.array([r.cfl for r in recs]),
+            "gmres_iters": np.array([r.gmres_iters for r in recs], dtype=np.int32),
+            "seconds": np.array([r.seconds for r in recs]),
+            "converged": st == 0,
+        }
+
+    def newton_step(self, tol=0.0):
+        s = Step()
+        cv = C.c_int(0)
+        _check(lib().cfdg_newton_step(self._h, float(tol), C.byref(s), C.byref(cv)))
+        return s, bool(cv.value)
+
+    def reset_newton(self):
+        _check(lib().cfdg_reset_newton(self._h))
+
+    def vjp(self, lam, U=None):
+        g = np.zeros(6 * self.n_cells)
+        u = None if U is None else np.ascontiguousarray(U, np.float64).ravel()
+        _check(lib().cfdg_vjp(self._h, None if u is None else u.ctypes.data_as(_vp),
+                              np.ascontiguousarray(lam, np.float64).ravel(), g))
+        return g.reshape(-1, 6)
+
+    # ---- device-resident path and instrumentation
+    def residual_device(self, update_limiters=True):
+        _check(lib().cfdg_residual_device(self._h, int(update_limiters)))
+
+    def synchronize(self):
+        _check(lib().cfdg_synchronize(self._h))
+
+    def set_timing(self, on=True):
+        _check(lib().cfdg_set_timing(self._h, int(on)))
+
+    def kernel_times(self):
+        v = [C.c_double() for _ in range(4)]
+        _check(lib().cfdg_kernel_times(self._h, *[C.byref(x) for x in v]))
+        return dict(zip(["prim", "grad", "flux", "gather"], [x.value for x in v]))
+
+    def launch_count(self):
+        n = C.c_longlong()
+        _check(lib().cfdg_launch_count(self._h, C.byref(n)))
+        return n.value

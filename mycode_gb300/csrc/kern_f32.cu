@@ -1,0 +1,79 @@
+// FP32 residual and FP32-vector Krylov kernels (mixed precision: FP32 Krylov basis,
+// FP64 reductions).  FMA contraction on.
+#include "launch.hpp"
+
+namespace cfdg {
+
+template <int NV>
+static void residual_nv(const ResArgs<float>& a) {
+    long nc = a.m.nc, nf = a.m.nf;
+    if (a.ev) cudaEventRecord(a.ev[0], a.stream);
+    k_prim<float, NV><<<grid_for(nc), 256, 0, a.stream>>>((int)nc, a.F, a.U, a.W);
+    if (a.ev) cudaEventRecord(a.ev[1], a.stream);
+    k_grad<float, NV><<<grid_for(nc), 256, 0, a.stream>>>(a.m, a.F, a.U, a.W, a.G, a.phi, a.do_limiter);
+    if (a.ev) cudaEventRecord(a.ev[2], a.stream);
+    k_flux<float, NV><<<grid_for(nf), 256, 0, a.stream>>>(a.m, a.F, a.U, a.W, a.G, a.phi, a.FA);
+    if (a.ev) cudaEventRecord(a.ev[3], a.stream);
+    k_gather<float, NV><<<grid_for(nc), 256, 0, a.stream>>>(a.m, a.FA.v, a.FA.n, a.out, nc, a.diag_v, a.dt);
+    if (a.ev) cudaEventRecord(a.ev[4], a.stream);
+}
+
+template <>
+void launch_residual<float>(const ResArgs<float>& a) {
+    if (a.nv == 6) residual_nv<6>(a);
+    else residual_nv<4>(a);
+}
+
+#define NV_SWITCH(nv, ...) \
+    do {                                 \
+        if ((nv) == 6) { constexpr int NVC = 6; __VA_ARGS__; } \
+        else { constexpr int NVC = 4; __VA_ARGS__; }           \
+    } while (0)
+
+template <>
+void launch_dot<float>(int nv, long nc, const float* a, const float* b, RedScratch rs, double* out, cudaStream_t s) {
+    NV_SWITCH(nv, (k_dot<float, float, NVC><<<red_grid(nc), RED_THREADS, 0, s>>>(nc, a, b, rs, out)));
+}
+template <>
+void launch_mgs<float>(int nv, long nc, float* w, const float* vprev, const double* hprev, const float* vnext,
+                       RedScratch rs, double* out, cudaStream_t s) {
+    NV_SWITCH(nv, (k_mgs<float, NVC><<<red_grid(nc), RED_THREADS, 0, s>>>(nc, w, vprev, hprev, vnext, rs, out)));
+}
+template <>
+void launch_scale_guard<float>(long n, float* x, const double* h, double thresh, cudaStream_t s) {
+    k_scale_guard<float><<<red_grid(n), RED_THREADS, 0, s>>>(n, x, h, thresh);
+}
+template <>
+void launch_scale_from<float>(long n, float* x, const double* a, const double* sc, int invert, cudaStream_t s) {
+    k_scale_from<float, double><<<red_grid(n), RED_THREADS, 0, s>>>(n, x, a, sc, invert);
+}
+template <>
+void launch_precond_apply<float>(int nv, long nc, const float* V, const double* D, float* z, RedScratch rs,
+                                 double* out_sq, cudaStream_t s) {
+    NV_SWITCH(nv, (k_precond_apply<float, float, NVC><<<red_grid(nc), RED_THREADS, 0, s>>>(nc, V, D, z, rs, out_sq)));
+}
+template <>
+void launch_gmres_solution<float>(int nv, long nc, const float* V, long vstride, const double* y, int k,
+                                  const double* D, double* x, cudaStream_t s) {
+    NV_SWITCH(nv, (k_gmres_solution<float, NVC><<<grid_for(nc), 256, 0, s>>>(nc, V, vstride, y, k, D, x)));
+}
+template <>
+void launch_aos_to_soa<float>(long nc, int np, int stride, const double* aos, const int* perm, float* soa,
+                                 cudaStream_t s) {
+    k_aos_to_soa<float><<<grid_for(nc), 256, 0, s>>>(nc, np, stride, aos, perm, soa);
+}
+template <>
+void launch_soa_to_aos<float>(long nc, int np, int stride, const float* soa, const int* perm, double* aos,
+                                 cudaStream_t s) {
+    k_soa_to_aos<float><<<grid_for(nc), 256, 0, s>>>(nc, np, stride, soa, perm, aos);
+}
+
+__global__ void k_convert_f32(long n, const double* __restrict__ in, float* __restrict__ out) {
+    for (long q = (long)blockIdx.x * blockDim.x + threadIdx.x; q < n; q += (long)gridDim.x * blockDim.x) out[q] = (float)in[q];
+}
+template <>
+void launch_convert<float>(long n, const double* in, float* out, cudaStream_t s) {
+    k_convert_f32<<<red_grid(n), RED_THREADS, 0, s>>>(n, in, out);
+}
+
+}  // namespace cfdg

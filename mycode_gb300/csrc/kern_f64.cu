@@ -1,0 +1,100 @@
+// FP64 kernels, compiled with --fmad=false: the residual, the pseudo-time kernels and
+// the FP64 Krylov vector kernels reproduce the reference's CPU arithmetic.
+#include "launch.hpp"
+
+namespace cfdg {
+
+template <int NV>
+static void residual_nv(const ResArgs<double>& a) {
+    long nc = a.m.nc, nf = a.m.nf;
+    if (a.ev) cudaEventRecord(a.ev[0], a.stream);
+    k_prim<double, NV><<<grid_for(nc), 256, 0, a.stream>>>((int)nc, a.F, a.U, a.W);
+    if (a.ev) cudaEventRecord(a.ev[1], a.stream);
+    k_grad<double, NV><<<grid_for(nc), 256, 0, a.stream>>>(a.m, a.F, a.U, a.W, a.G, a.phi, a.do_limiter);
+    if (a.ev) cudaEventRecord(a.ev[2], a.stream);
+    k_flux<double, NV><<<grid_for(nf), 256, 0, a.stream>>>(a.m, a.F, a.U, a.W, a.G, a.phi, a.FA);
+    if (a.ev) cudaEventRecord(a.ev[3], a.stream);
+    k_gather<double, NV><<<grid_for(nc), 256, 0, a.stream>>>(a.m, a.FA.v, a.FA.n, a.out, nc, a.diag_v, a.dt);
+    if (a.ev) cudaEventRecord(a.ev[4], a.stream);
+}
+
+template <>
+void launch_residual<double>(const ResArgs<double>& a) {
+    if (a.nv == 6) residual_nv<6>(a);
+    else residual_nv<4>(a);
+}
+
+void launch_prim64(int nv, long nc, const Flow<double>& F, Field<double> U, Field<double> W, cudaStream_t s) {
+    if (nv == 6) k_prim<double, 6><<<grid_for(nc), 256, 0, s>>>((int)nc, F, U, W);
+    else k_prim<double, 4><<<grid_for(nc), 256, 0, s>>>((int)nc, F, U, W);
+}
+
+#define NV_SWITCH(nv, ...) \
+    do {                                 \
+        if ((nv) == 6) { constexpr int NVC = 6; __VA_ARGS__; } \
+        else { constexpr int NVC = 4; __VA_ARGS__; }           \
+    } while (0)
+
+template <>
+void launch_dot<double>(int nv, long nc, const double* a, const double* b, RedScratch rs, double* out, cudaStream_t s) {
+    NV_SWITCH(nv, (k_dot<double, double, NVC><<<red_grid(nc), RED_THREADS, 0, s>>>(nc, a, b, rs, out)));
+}
+template <>
+void launch_mgs<double>(int nv, long nc, double* w, const double* vprev, const double* hprev, const double* vnext,
+                        RedScratch rs, double* out, cudaStream_t s) {
+    NV_SWITCH(nv, (k_mgs<double, NVC><<<red_grid(nc), RED_THREADS, 0, s>>>(nc, w, vprev, hprev, vnext, rs, out)));
+}
+template <>
+void launch_scale_guard<double>(long n, double* x, const double* h, double thresh, cudaStream_t s) {
+    k_scale_guard<double><<<red_grid(n), RED_THREADS, 0, s>>>(n, x, h, thresh);
+}
+template <>
+void launch_scale_from<double>(long n, double* x, const double* a, const double* sc, int invert, cudaStream_t s) {
+    k_scale_from<double, double><<<red_grid(n), RED_THREADS, 0, s>>>(n, x, a, sc, invert);
+}
+template <>
+void launch_precond_apply<double>(int nv, long nc, const double* V, const double* D, double* z, RedScratch rs,
+                                  double* out_sq, cudaStream_t s) {
+    NV_SWITCH(nv, (k_precond_apply<double, double, NVC><<<red_grid(nc), RED_THREADS, 0, s>>>(nc, V, D, z, rs, out_sq)));
+}
+template <>
+void launch_gmres_solution<double>(int nv, long nc, const double* V, long vstride, const double* y, int k,
+                                   const double* D, double* x, cudaStream_t s) {
+    NV_SWITCH(nv, (k_gmres_solution<double, NVC><<<grid_for(nc), 256, 0, s>>>(nc, V, vstride, y, k, D, x)));
+}
+template <>
+void launch_aos_to_soa<double>(long nc, int np, int stride, const double* aos, const int* perm, double* soa,
+                                 cudaStream_t s) {
+    k_aos_to_soa<double><<<grid_for(nc), 256, 0, s>>>(nc, np, stride, aos, perm, soa);
+}
+template <>
+void launch_soa_to_aos<double>(long nc, int np, int stride, const double* soa, const int* perm, double* aos,
+                                 cudaStream_t s) {
+    k_soa_to_aos<double><<<grid_for(nc), 256, 0, s>>>(nc, np, stride, soa, perm, aos);
+}
+
+void launch_fd_perturb(long n, const double* U, const double* v, const double* u_sq, const double* v_sq, double* Up,
+                       double* eps, cudaStream_t s) {
+    k_fd_perturb<<<red_grid(n), RED_THREADS, 0, s>>>(n, U, v, u_sq, v_sq, Up, eps);
+}
+void launch_fd_combine(int nv, long nc, const double* Rp, const double* Rb, const double* v, const double* eps,
+                       const double* vol, const double* dt, double* Jv, cudaStream_t s) {
+    NV_SWITCH(nv, (k_fd_combine<NVC><<<red_grid(nc), RED_THREADS, 0, s>>>(nc, Rp, Rb, v, eps, vol, dt, Jv)));
+}
+void launch_norm_vm(int nv, long nc, const double* R, const double* vol, RedScratch rs, double* out3, cudaStream_t s) {
+    NV_SWITCH(nv, (k_norm_vm<NVC><<<red_grid(nc), RED_THREADS, 0, s>>>(nc, R, vol, rs, out3)));
+}
+void launch_local_dt(int nv, const MeshView<double>& m, const Flow<double>& F, const double* U, const double* W,
+                     double cfl, double* dt, cudaStream_t s) {
+    NV_SWITCH(nv, (k_local_dt<NVC><<<grid_for(m.nc), 256, 0, s>>>(m, F, U, W, cfl, dt)));
+}
+void launch_precond(int nv, const MeshView<double>& m, const Flow<double>& F, const double* U, const double* W,
+                    const double* dt, double* D, cudaStream_t s) {
+    NV_SWITCH(nv, (k_precond<NVC><<<grid_for(m.nc), 256, 0, s>>>(m, F, U, W, dt, D)));
+}
+void launch_newton_update(int nv, long nc, double* U, const double* dU, double relax, double gam, int* bad,
+                          cudaStream_t s) {
+    NV_SWITCH(nv, (k_newton_update<NVC><<<grid_for(nc), 256, 0, s>>>(nc, U, dU, relax, gam, bad)));
+}
+
+}  // namespace cfdg

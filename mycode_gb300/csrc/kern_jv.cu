@@ -1,0 +1,36 @@
+// Exact Jacobian-vector products: the residual kernels instantiated on Dual<R>, so the
+// derivative follows the primal operation sequence and branch decisions exactly.  The
+// limiter is frozen (phi read, zero derivative), as in the reference's applyJacobian
+// (src/Solver.cpp:1366).  The gather adds the time term v * vol/(dt + 1e-30).
+#include "launch.hpp"
+
+namespace cfdg {
+
+template <class R, int NV>
+static void jv_nv(const ResArgs<R>& a) {
+    typedef Dual<R> S;
+    long nc = a.m.nc, nf = a.m.nf;
+    if (a.ev) cudaEventRecord(a.ev[0], a.stream);
+    k_prim<S, NV><<<grid_for(nc), 256, 0, a.stream>>>((int)nc, a.F, a.U, a.W);
+    if (a.ev) cudaEventRecord(a.ev[1], a.stream);
+    k_grad<S, NV><<<grid_for(nc), 256, 0, a.stream>>>(a.m, a.F, a.U, a.W, a.G, a.phi, 0);
+    if (a.ev) cudaEventRecord(a.ev[2], a.stream);
+    k_flux<S, NV><<<grid_for(nf), 256, 0, a.stream>>>(a.m, a.F, a.U, a.W, a.G, a.phi, a.FA);
+    if (a.ev) cudaEventRecord(a.ev[3], a.stream);
+    k_gather<R, NV><<<grid_for(nc), 256, 0, a.stream>>>(a.m, a.FA.d, a.FA.n, a.out, nc, a.diag_v, a.dt);
+    if (a.ev) cudaEventRecord(a.ev[4], a.stream);
+}
+
+template <>
+void launch_jv<double>(const ResArgs<double>& a) {
+    if (a.nv == 6) jv_nv<double, 6>(a);
+    else jv_nv<double, 4>(a);
+}
+
+template <>
+void launch_jv<float>(const ResArgs<float>& a) {
+    if (a.nv == 6) jv_nv<float, 6>(a);
+    else jv_nv<float, 4>(a);
+}
+
+}  // namespace cfdg

@@ -1,0 +1,69 @@
+// Host-side launchers.  The kernels live in three translation units so each gets its
+// own floating-point contract:
+//   kern_f64.cu  FP64 residual, pseudo-time and Krylov kernels, built with --fmad=false
+//                so the arithmetic matches the reference's CPU code bit for bit
+//   kern_f32.cu  FP32 residual and FP32-vector Krylov kernels (mixed precision), FMA on
+//   kern_jv.cu   Dual-number (exact J v) kernels in FP64 and FP32, FMA on
+#pragma once
+#include <cuda_runtime.h>
+#include "linalg.cuh"
+
+namespace cfdg {
+
+template <class R>
+struct ResArgs {
+    MeshView<R> m;
+    Flow<R> F;
+    int nv;
+    Field<R> U, W, G, FA;   // for the Dual launch .d holds the derivative planes
+    R* phi;
+    R* out;                 // residual (or J v) planes, stride m.nc
+    int do_limiter;
+    const R* diag_v;        // optional: adds diag_v * vol / (dt + 1e-30)
+    const R* dt;
+    cudaStream_t stream;
+    cudaEvent_t* ev;        // optional 5 events around the four kernels
+};
+
+// R(U) (kern_f64.cu for double, kern_f32.cu for float)
+template <class R> void launch_residual(const ResArgs<R>& a);
+// J v by forward linearisation with the limiter frozen (kern_jv.cu)
+template <class R> void launch_jv(const ResArgs<R>& a);
+
+// ---- vectors (T = double in kern_f64.cu, T = float in kern_f32.cu)
+template <class T> void launch_dot(int nv, long nc, const T* a, const T* b, RedScratch rs, double* out, cudaStream_t s);
+template <class T> void launch_mgs(int nv, long nc, T* w, const T* vprev, const double* hprev, const T* vnext,
+                                   RedScratch rs, double* out, cudaStream_t s);
+template <class T> void launch_scale_guard(long n, T* x, const double* h_sq, double thresh, cudaStream_t s);
+template <class T> void launch_scale_from(long n, T* x, const double* a, const double* sc, int invert, cudaStream_t s);
+template <class T> void launch_precond_apply(int nv, long nc, const T* V, const double* D, T* z, RedScratch rs,
+                                             double* out_sq, cudaStream_t s);
+template <class T> void launch_gmres_solution(int nv, long nc, const T* V, long vstride, const double* y, int k,
+                                              const double* D, double* x, cudaStream_t s);
+template <class T> void launch_aos_to_soa(long nc, int np, int stride, const double* aos, const int* perm, T* soa,
+                                          cudaStream_t s);
+template <class T> void launch_soa_to_aos(long nc, int np, int stride, const T* soa, const int* perm, double* aos,
+                                          cudaStream_t s);
+template <class T> void launch_convert(long n, const double* in, T* out, cudaStream_t s);
+
+// ---- FP64 only (kern_f64.cu)
+void launch_prim64(int nv, long nc, const Flow<double>& F, Field<double> U, Field<double> W, cudaStream_t s);
+void launch_fd_perturb(long n, const double* U, const double* v, const double* u_sq, const double* v_sq, double* Up,
+                       double* eps, cudaStream_t s);
+void launch_fd_combine(int nv, long nc, const double* Rp, const double* Rb, const double* v, const double* eps,
+                       const double* vol, const double* dt, double* Jv, cudaStream_t s);
+void launch_norm_vm(int nv, long nc, const double* R, const double* vol, RedScratch rs, double* out3, cudaStream_t s);
+void launch_local_dt(int nv, const MeshView<double>& m, const Flow<double>& F, const double* U, const double* W,
+                     double cfl, double* dt, cudaStream_t s);
+void launch_precond(int nv, const MeshView<double>& m, const Flow<double>& F, const double* U, const double* W,
+                    const double* dt, double* D, cudaStream_t s);
+void launch_newton_update(int nv, long nc, double* U, const double* dU, double relax, double gam, int* bad,
+                          cudaStream_t s);
+
+inline unsigned grid_for(long n, int threads = 256) { return (unsigned)((n + threads - 1) / threads); }
+inline unsigned red_grid(long n) {
+    long b = (n + RED_THREADS - 1) / RED_THREADS;
+    return (unsigned)(b < RED_BLOCKS ? (b < 1 ? 1 : b) : RED_BLOCKS);
+}
+
+}  // namespace cfdg

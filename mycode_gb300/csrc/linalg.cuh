@@ -1,0 +1,327 @@
+// Vector kernels of the Newton-Krylov loop and the per-cell pseudo-time kernels.
+//
+// Reductions accumulate in FP64 whatever the vector type, with a fixed grid and a
+// fixed combination order (per-block partials, then the last block to finish sums
+// the partials in index order), so every result is run-to-run deterministic.
+// Vectors are flat arrays of nv*nc entries (SoA planes of the state).
+#pragma once
+#include <cuda_runtime.h>
+#include "residual.cuh"
+
+namespace cfdg {
+
+constexpr int RED_THREADS = 256;
+constexpr int RED_BLOCKS = 608;  // 4 blocks per SM on a 152-SM part
+
+struct RedScratch {
+    double* partial;     // [RED_BLOCKS * 2]
+    unsigned* counter;   // one ticket counter, left at 0 after each reduction
+};
+
+__device__ __forceinline__ double warp_sum(double v) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+    return v;
+}
+
+// Block sum of up to two values; result valid in thread 0.
+template <int K>
+__device__ __forceinline__ void block_sum(double (&v)[K]) {
+    __shared__ double sm[K][RED_THREADS / 32];
+    int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+#pragma unroll
+    for (int k = 0; k < K; ++k) {
+        double s = warp_sum(v[k]);
+        if (lane == 0) sm[k][w] = s;
+    }
+    __syncthreads();
+    if (w == 0) {
+#pragma unroll
+        for (int k = 0; k < K; ++k) {
+            double s = lane < (int)(blockDim.x >> 5) ? sm[k][lane] : 0.0;
+            v[k] = warp_sum(s);
+        }
+    }
+}
+
+// Finishes a grid reduction of K values: block partials, then the last block sums
+// them in a fixed order and writes out[0..K).  Returns true in the thread that wrote.
+template <int K>
+__device__ __forceinline__ bool grid_finish(double (&v)[K], RedScratch rs, double* out) {
+    __shared__ bool last;
+    block_sum<K>(v);
+    if (threadIdx.x == 0) {
+#pragma unroll
+        for (int k = 0; k < K; ++k) rs.partial[k * RED_BLOCKS + blockIdx.x] = v[k];
+        __threadfence();
+        unsigned t = atomicAdd(rs.counter, 1u);
+        last = (t == gridDim.x - 1);
+    }
+    __syncthreads();
+    if (!last) return false;
+    __threadfence();
+    double s[K];
+#pragma unroll
+    for (int k = 0; k < K; ++k) {
+        s[k] = 0.0;
+        for (int b = threadIdx.x; b < (int)gridDim.x; b += blockDim.x)
+            s[k] += ((volatile double*)rs.partial)[k * RED_BLOCKS + b];
+    }
+    block_sum<K>(s);
+    if (threadIdx.x == 0) {
+#pragma unroll
+        for (int k = 0; k < K; ++k) out[k] = s[k];
+        *rs.counter = 0u;
+    }
+    return threadIdx.x == 0;
+}
+
+// sum over cells of sum_c a_c b_c (planes in component order, as Solver::dot_product
+// src/Solver.cpp:1258-1264); a == b gives the squared norm (norm_L2, :1250-1256)
+template <class TA, class TB, int NV>
+__global__ void __launch_bounds__(RED_THREADS) k_dot(long nc, const TA* __restrict__ a, const TB* __restrict__ b,
+                                                     RedScratch rs, double* out) {
+    double v[1] = {0.0};
+    for (long i = (long)blockIdx.x * blockDim.x + threadIdx.x; i < nc; i += (long)gridDim.x * blockDim.x) {
+        double s = (double)a[i] * (double)b[i];
+#pragma unroll
+        for (int c = 1; c < NV; ++c) s = s + (double)a[c * nc + i] * (double)b[c * nc + i];
+        v[0] += s;
+    }
+    grid_finish<1>(v, rs, out);
+}
+
+// Fused modified Gram-Schmidt step: w -= h_prev * v_prev (when v_prev != null), then
+// out = <w, v_next> (when v_next != null) else out = <w, w>.  The update keeps the
+// reference's expression V[j+1] - V[i] * H[i][j] (src/Solver.cpp:1546).
+template <class T, int NV>
+__global__ void __launch_bounds__(RED_THREADS) k_mgs(long nc, T* __restrict__ w, const T* __restrict__ v_prev,
+                                                     const double* h_prev, const T* __restrict__ v_next,
+                                                     RedScratch rs, double* out) {
+    double v[1] = {0.0};
+    T h = v_prev ? (T)(*h_prev) : T(0);
+    for (long i = (long)blockIdx.x * blockDim.x + threadIdx.x; i < nc; i += (long)gridDim.x * blockDim.x) {
+        double s = 0.0;
+#pragma unroll
+        for (int c = 0; c < NV; ++c) {
+            long q = c * nc + i;
+            T x = w[q];
+            if (v_prev) {
+                x = x - v_prev[q] * h;
+                w[q] = x;
+            }
+            T y = v_next ? v_next[q] : x;
+            s = (c == 0) ? (double)x * (double)y : s + (double)x * (double)y;
+        }
+        v[0] += s;
+    }
+    grid_finish<1>(v, rs, out);
+}
+
+// x *= 1/h with h = sqrt(*h_sq) when h > thresh (the breakdown guard of
+// src/Solver.cpp:1550-1558)
+template <class T>
+__global__ void k_scale_guard(long n, T* x, const double* h_sq, double thresh) {
+    double hv = sqrt(*h_sq);
+    if (!(hv > thresh)) return;
+    T ih = (T)(1.0 / hv);
+    for (long q = (long)blockIdx.x * blockDim.x + threadIdx.x; q < n; q += (long)gridDim.x * blockDim.x) x[q] = x[q] * ih;
+}
+
+// x = a * s (s a device scalar, inverted when invert != 0)
+template <class TO, class TI>
+__global__ void k_scale_from(long n, TO* x, const TI* a, const double* s, int invert) {
+    double sv = invert ? 1.0 / *s : *s;
+    for (long q = (long)blockIdx.x * blockDim.x + threadIdx.x; q < n; q += (long)gridDim.x * blockDim.x)
+        x[q] = (TO)(a[q] * (TI)sv);
+}
+
+// z = V * (1 / D) per cell (src/Solver.cpp:1536-1538), with sum of squares of z
+template <class TV, class TZ, int NV>
+__global__ void __launch_bounds__(RED_THREADS) k_precond_apply(long nc, const TV* __restrict__ V,
+                                                               const double* __restrict__ D, TZ* __restrict__ z,
+                                                               RedScratch rs, double* out_sq) {
+    double v[1] = {0.0};
+    for (long i = (long)blockIdx.x * blockDim.x + threadIdx.x; i < nc; i += (long)gridDim.x * blockDim.x) {
+        TV id = (TV)(1.0 / D[i]);
+        double s = 0.0;
+#pragma unroll
+        for (int c = 0; c < NV; ++c) {
+            TZ zz = (TZ)(V[c * nc + i] * id);
+            z[c * nc + i] = zz;
+            s = (c == 0) ? (double)zz * (double)zz : s + (double)zz * (double)zz;
+        }
+        v[0] += s;
+    }
+    if (out_sq) grid_finish<1>(v, rs, out_sq);
+}
+
+// FD perturbation: Up = U + v * eps with eps = 1e-7 (1 + |U|) / (|v| + 1e-30)
+// (src/Solver.cpp:1342-1362); norms given as squared sums
+static __global__ void k_fd_perturb(long n, const double* __restrict__ U, const double* __restrict__ v,
+                             const double* u_sq, const double* v_sq, double* __restrict__ Up, double* eps_out) {
+    double eps = 1e-7 * (1.0 + sqrt(*u_sq)) / (sqrt(*v_sq) + 1e-30);
+    if (blockIdx.x == 0 && threadIdx.x == 0) *eps_out = eps;
+    for (long q = (long)blockIdx.x * blockDim.x + threadIdx.x; q < n; q += (long)gridDim.x * blockDim.x) Up[q] = U[q] + v[q] * eps;
+}
+
+// Jv = (Rp - Rb) * (1/eps) + v * (vol / (dt + 1e-30)) (src/Solver.cpp:1378-1385)
+template <int NV>
+__global__ void k_fd_combine(long nc, const double* __restrict__ Rp, const double* __restrict__ Rb,
+                             const double* __restrict__ v, const double* eps, const double* __restrict__ vol,
+                             const double* __restrict__ dt, double* __restrict__ Jv) {
+    double ie = 1.0 / *eps;
+    for (long i = (long)blockIdx.x * blockDim.x + threadIdx.x; i < nc; i += (long)gridDim.x * blockDim.x) {
+        double tc = vol[i] / (dt[i] + 1e-30);
+#pragma unroll
+        for (int c = 0; c < NV; ++c) {
+            long q = c * nc + i;
+            Jv[q] = (Rp[q] - Rb[q]) * ie + v[q] * tc;
+        }
+    }
+}
+
+// x = sum_i (V_i * y_i) * (1/D) accumulated in i order (src/Solver.cpp:1610-1615)
+template <class TV, int NV>
+__global__ void k_gmres_solution(long nc, const TV* __restrict__ V, long vstride, const double* y, int k,
+                                 const double* __restrict__ D, double* __restrict__ x) {
+    for (long i = (long)blockIdx.x * blockDim.x + threadIdx.x; i < nc; i += (long)gridDim.x * blockDim.x) {
+        double id = 1.0 / D[i];
+#pragma unroll
+        for (int c = 0; c < NV; ++c) {
+            long q = c * nc + i;
+            double acc = 0.0;
+            for (int j = 0; j <= k; ++j) acc = acc + (double)V[j * vstride + q] * y[j] * id;
+            x[q] = acc;
+        }
+    }
+}
+
+// Volume-weighted residual norm pieces (src/Solver.cpp:1280-1303): sum of
+// (sum_c (R_c/vol)^2) * vol, sum of vol, and the density-only sum
+template <int NV>
+__global__ void __launch_bounds__(RED_THREADS) k_norm_vm(long nc, const double* __restrict__ R,
+                                                         const double* __restrict__ vol, RedScratch rs, double* out3) {
+    double v[3] = {0.0, 0.0, 0.0};
+    for (long i = (long)blockIdx.x * blockDim.x + threadIdx.x; i < nc; i += (long)gridDim.x * blockDim.x) {
+        double vv = vol[i];
+        double s = 0.0;
+#pragma unroll
+        for (int c = 0; c < NV; ++c) {
+            double r = R[c * nc + i] / vv;
+            s = (c == 0) ? r * r : s + r * r;
+        }
+        double r0 = R[i] / vv;
+        v[0] += s * vv;
+        v[1] += vv;
+        v[2] += r0 * r0 * vv;
+    }
+    grid_finish<3>(v, rs, out3);
+}
+
+// computeLocalTimeStep (src/Solver.cpp:1388-1422) as a per-cell gather: each face
+// adds (|u_n| + c) A from the cell's own state, owner and neighbour with their own
+// expressions, summed in reference face order from 1e-12.
+template <int NV>
+__global__ void k_local_dt(MeshView<double> m, Flow<double> F, const double* __restrict__ U,
+                           const double* __restrict__ W, double cfl, double* __restrict__ dt) {
+    long i = (long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= m.nc) return;
+    long nc = m.nc;
+    double r = U[i], ru = U[nc + i], rv = U[2 * nc + i];
+    double p = W[3 * nc + i];
+    double c = sqrt(F.gam * p / r);
+    double lam = 1e-12;
+    for (int k = 0; k < 4; ++k) {
+        int e = m.cf[(long)k * nc + i];
+        if (e < 0) break;
+        int f = e >> 1;
+        double un = (e & 1) ? (ru * (-m.nx[f]) + rv * (-m.ny[f])) / r : (ru * m.nx[f] + rv * m.ny[f]) / r;
+        lam += (fabs(un) + c) * m.area[f];
+    }
+    dt[i] = cfl * m.vol[i] / lam;
+}
+
+// computeDiagonalPreconditioner (src/Solver.cpp:1424-1465) as a per-cell gather; each
+// face term is evaluated with the owner as L exactly as the reference's face loop.
+template <int NV>
+__global__ void k_precond(MeshView<double> m, Flow<double> F, const double* __restrict__ U,
+                          const double* __restrict__ W, const double* __restrict__ dt, double* __restrict__ D) {
+    long i = (long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= m.nc) return;
+    long nc = m.nc;
+    double acc = 0.0;
+    for (int k = 0; k < 4; ++k) {
+        int e = m.cf[(long)k * nc + i];
+        if (e < 0) break;
+        int f = e >> 1;
+        int o = m.fo[f], n = m.fn[f];
+        CS<double> L = load_cs<double, NV>(Field<double>{(double*)U, nullptr, nc}, Field<double>{(double*)W, nullptr, nc}, o);
+        CS<double> Rr = n >= 0 ? load_cs<double, NV>(Field<double>{(double*)U, nullptr, nc}, Field<double>{(double*)W, nullptr, nc}, n)
+                               : ghost_state(F, L, m.ftag[f], m.nx[f], m.ny[f]);
+        double g = F.gam;
+        double cL = sqrt(g * L.p / L.r);
+        double cR = sqrt(g * (Rr.p > 0 ? Rr.p : 1e-3) / (Rr.r > 0 ? Rr.r : 1e-3));
+        double cf = 0.5 * (cL + cR);
+        double uf = 0.5 * (L.u + Rr.u);
+        double vf = 0.5 * (L.v + Rr.v);
+        double vn = fabs(uf * m.nx[f] + vf * m.ny[f]);
+        double li = vn + cf;
+        double dx = sqrt(m.vol[o]);
+        double mu = 0.5 * (L.r + Rr.r) * F.nu;
+        double lv = 2.0 * mu / (0.5 * (L.r + Rr.r) * dx + 1e-12);
+        double lt = (li + lv) * m.area[f];
+        acc += lt * 0.5;
+    }
+    double v = m.vol[i];
+    double d = (v / (dt[i] + 1e-30)) + acc;
+    if (d < 1e-12) d = 1e-12;
+    D[i] = d;
+}
+
+// Newton update with the positivity clamps of src/Solver.cpp:1760-1778; flags a
+// non-finite state in *bad (bit 0) without stopping.
+template <int NV>
+__global__ void k_newton_update(long nc, double* __restrict__ U, const double* __restrict__ dU, double relax,
+                                double gam, int* bad) {
+    long i = (long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= nc) return;
+    double u[NV];
+#pragma unroll
+    for (int c = 0; c < NV; ++c) u[c] = U[c * nc + i] + dU[c * nc + i] * relax;
+    double ke = 0.5 * (u[1] * u[1] + u[2] * u[2]) / (u[0] + 1e-12);
+    double pn = (gam - 1.0) * (u[3] - ke);
+    if (u[0] < 1e-5) u[0] = 1e-5;
+    if (pn < 1e-5) {
+        pn = 1e-5;
+        u[3] = pn / (gam - 1.0) + ke;
+    }
+    bool ok = true;
+#pragma unroll
+    for (int c = 0; c < NV; ++c) {
+        ok = ok && isfinite(u[c]);
+        U[c * nc + i] = u[c];
+    }
+    if (!ok) atomicOr(bad, 1);
+}
+
+// AoS (stride doubles per cell, reference numbering) <-> SoA (np planes, internal
+// numbering); AoS slots np..stride-1 are written as zero
+template <class T>
+__global__ void k_aos_to_soa(long nc, int np, int stride, const double* __restrict__ aos, const int* __restrict__ perm,
+                             T* __restrict__ soa) {
+    long i = (long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= nc) return;
+    long src = (long)perm[i] * stride;
+    for (int c = 0; c < np; ++c) soa[c * nc + i] = (T)aos[src + c];
+}
+template <class T>
+__global__ void k_soa_to_aos(long nc, int np, int stride, const T* __restrict__ soa, const int* __restrict__ perm,
+                             double* __restrict__ aos) {
+    long i = (long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= nc) return;
+    long dst = (long)perm[i] * stride;
+    for (int c = 0; c < stride; ++c) aos[dst + c] = c < np ? (double)soa[c * nc + i] : 0.0;
+}
+
+}  // namespace cfdg

@@ -1,0 +1,266 @@
+// Point-wise physics of the residual: pressure, normal flux, the LLF / Roe / HLLC
+// Riemann fluxes, ghost states, prim->cons and the viscous face flux.
+//
+// Every function is templated on the scalar S (double, float, or Dual<double|float>
+// for the exact linearisation) and keeps the reference's floating-point operation
+// order, so the double instantiation compiled without FMA contraction reproduces the
+// reference's CPU arithmetic bit for bit.  Citations are to AmberMond/mycode.
+#pragma once
+#include "dual.cuh"
+
+namespace cfdg {
+
+using ::sqrt;
+using ::fabs;
+using ::pow;
+
+enum FluxScheme { FLUX_LLF = 0, FLUX_ROE = 1, FLUX_HLLC = 2, FLUX_AUSM = 3 };
+enum SpatialScheme { SP_FIRST = 0, SP_CENTRAL = 1, SP_LIMITED = 2 };
+enum BcSet { BC_BUMP = 0, BC_SUPERSONIC = 1, BC_PLATE = 2 };
+
+// libstdc++'s std::max / std::min selection rule (NaN behaviour included)
+template <class S> CFD_HD S smax(S a, S b) { return (val(a) < val(b)) ? b : a; }
+template <class S> CFD_HD S smin(S a, S b) { return (val(b) < val(a)) ? b : a; }
+
+// Flow constants seen by the kernels (set on the host from the Solver setters).
+template <class R>
+struct Flow {
+    R gam;      // ratio of specific heats (include/Flux.hpp:9, include/Solver.hpp:91)
+    R Rgas;     // gas constant (include/Solver.hpp:92)
+    R Pr;       // Prandtl number (src/Solver.cpp:541)
+    R nu;       // kinematic viscosity (include/Solver.hpp:42)
+    R Minf, P0, T0, Pexit;   // setFlowConditions (src/Solver.cpp:12-32)
+    R fs[4];    // frozen free-stream state (src/Solver.cpp:979-985); exact host copy
+    R shock[4]; // post-shock inflow state for tag 6 (no reference counterpart)
+    // SST (no reference counterpart; parity unpinned)
+    R k_inf, w_inf, Pr_t;
+    int bcset, flux, spatial, viscous;
+};
+
+// Conservative state with its derived primitives u, v, p (reference formulas).
+template <class S>
+struct CS {
+    S r, ru, rv, rE, rk, rw;
+    S u, v, p;
+};
+
+// getPressure (include/Flux.hpp:12-15)
+template <class S, class R>
+CFD_HD S pressure(const Flow<R>& F, S r, S ru, S rv, S rE) {
+    S V2 = (ru * ru + rv * rv) / (r * r);
+    return (F.gam - R(1.0)) * (rE - R(0.5) * r * V2);
+}
+
+template <class S, class R>
+CFD_HD CS<S> make_cs(const Flow<R>& F, S r, S ru, S rv, S rE, S rk, S rw) {
+    CS<S> c;
+    c.r = r; c.ru = ru; c.rv = rv; c.rE = rE; c.rk = rk; c.rw = rw;
+    c.u = ru / r;
+    c.v = rv / r;
+    c.p = pressure(F, r, ru, rv, rE);
+    return c;
+}
+
+// primitiveToConservative (src/Solver.cpp:498-501)
+template <class S, class R>
+CFD_HD CS<S> p2c(const Flow<R>& F, S r, S u, S v, S p, S k, S w) {
+    S rE = p / (F.gam - R(1.0)) + R(0.5) * r * (u * u + v * v);
+    return make_cs(F, r, r * u, r * v, rE, r * k, r * w);
+}
+
+template <class S>
+struct Flux6 { S f[6]; };
+
+// computeNormalFlux (include/Flux.hpp:23-34); k and w components are zero
+template <class S, class R>
+CFD_HD Flux6<S> normal_flux(const CS<S>& U, R nx, R ny) {
+    S un = U.u * nx + U.v * ny;
+    Flux6<S> o;
+    o.f[0] = U.r * un;
+    o.f[1] = U.ru * un + U.p * nx;
+    o.f[2] = U.rv * un + U.p * ny;
+    o.f[3] = (U.rE + U.p) * un;
+    o.f[4] = S(R(0));
+    o.f[5] = S(R(0));
+    return o;
+}
+
+// computeFluxLLF (include/Flux.hpp:81-108)
+template <class S, class R>
+CFD_HD Flux6<S> flux_llf(const Flow<R>& F, const CS<S>& L, const CS<S>& Rt, R nx, R ny) {
+    Flux6<S> FL = normal_flux(L, nx, ny), FR = normal_flux(Rt, nx, ny);
+    S unL = L.u * nx + L.v * ny;
+    S cL = sqrt(F.gam * L.p / L.r);
+    S unR = Rt.u * nx + Rt.v * ny;
+    S cR = sqrt(F.gam * Rt.p / Rt.r);
+    S a = smax(fabs(unL) + cL, fabs(unR) + cR);
+    S ha = R(0.5) * a;
+    S UL[6] = {L.r, L.ru, L.rv, L.rE, L.rk, L.rw};
+    S UR[6] = {Rt.r, Rt.ru, Rt.rv, Rt.rE, Rt.rk, Rt.rw};
+    Flux6<S> o;
+#pragma unroll
+    for (int c = 0; c < 6; ++c) o.f[c] = (FL.f[c] + FR.f[c]) * R(0.5) - (UR[c] - UL[c]) * ha;
+    return o;
+}
+
+// computeFluxROE with Harten's entropy fix (include/Flux.hpp:112-213)
+template <class S, class R>
+CFD_HD Flux6<S> flux_roe(const Flow<R>& F, const CS<S>& L, const CS<S>& Rt, R nx, R ny) {
+    S hL = (L.rE + L.p) / L.r;
+    S hR = (Rt.rE + Rt.p) / Rt.r;
+    S sL = sqrt(L.r), sR = sqrt(Rt.r);
+    S inv = R(1.0) / (sL + sR);
+    S ut = (sL * L.u + sR * Rt.u) * inv;
+    S vt = (sL * L.v + sR * Rt.v) * inv;
+    S ht = (sL * hL + sR * hR) * inv;
+    S V2 = ut * ut + vt * vt;
+    S c2 = (F.gam - R(1.0)) * (ht - R(0.5) * V2);
+    S ct = sqrt(smax(c2, S(R(1e-8))));
+    S unt = ut * nx + vt * ny;
+    S utt = -ut * ny + vt * nx;
+    S lam[4] = {unt - ct, unt, unt, unt + ct};
+    S eps = R(0.1) * ct;
+#pragma unroll
+    for (int i = 0; i < 4; ++i) {
+        if (val(fabs(lam[i])) < val(eps)) lam[i] = R(0.5) * (lam[i] * lam[i] / eps + eps);
+        lam[i] = fabs(lam[i]);
+    }
+    S dr = Rt.r - L.r, du = Rt.u - L.u, dv = Rt.v - L.v, dp = Rt.p - L.p;
+    S dun = du * nx + dv * ny;
+    S dut = -du * ny + dv * nx;
+    S rt = sL * sR;
+    S al0 = R(0.5) / c2 * (dp - rt * ct * dun);
+    S al1 = dr - dp / c2;
+    S al2 = rt * dut;
+    S al3 = R(0.5) / c2 * (dp + rt * ct * dun);
+    S w1 = lam[0] * al0, w2 = lam[1] * al1, w3 = lam[2] * al2, w4 = lam[3] * al3;
+    S D[6];
+    D[0] = w1 * R(1.0) + w2 * R(1.0) + w3 * R(0.0) + w4 * R(1.0);
+    D[1] = w1 * (ut - ct * nx) + w2 * ut + w3 * (-ny) + w4 * (ut + ct * nx);
+    D[2] = w1 * (vt - ct * ny) + w2 * vt + w3 * nx + w4 * (vt + ct * ny);
+    D[3] = w1 * (ht - unt * ct) + w2 * (R(0.5) * V2) + w3 * utt + w4 * (ht + unt * ct);
+    D[4] = fabs(unt) * (Rt.rk / Rt.r - L.rk / L.r) * rt;
+    D[5] = fabs(unt) * (Rt.rw / Rt.r - L.rw / L.r) * rt;
+    Flux6<S> FL = normal_flux(L, nx, ny), FR = normal_flux(Rt, nx, ny);
+    Flux6<S> o;
+#pragma unroll
+    for (int c = 0; c < 6; ++c) o.f[c] = (FL.f[c] + FR.f[c]) * R(0.5) - D[c] * R(0.5);
+    return o;
+}
+
+// computeFluxHLLC with Roe-averaged (Einfeldt) wave speeds (include/Flux.hpp:36-76).
+// The star state is built with the 4-argument State constructor, so its k and w are 0.
+template <class S, class R>
+CFD_HD Flux6<S> flux_hllc(const Flow<R>& F, const CS<S>& L, const CS<S>& Rt, R nx, R ny) {
+    S unL = L.u * nx + L.v * ny, unR = Rt.u * nx + Rt.v * ny;
+    S cL = sqrt(F.gam * L.p / L.r), cR = sqrt(F.gam * Rt.p / Rt.r);
+    S hL = (L.rE + L.p) / L.r, hR = (Rt.rE + Rt.p) / Rt.r;
+    S sL = sqrt(L.r), sR = sqrt(Rt.r);
+    S ut = (sL * L.u + sR * Rt.u) / (sL + sR);
+    S vt = (sL * L.v + sR * Rt.v) / (sL + sR);
+    S ht = (sL * hL + sR * hR) / (sL + sR);
+    S unt = ut * nx + vt * ny;
+    S ct = sqrt((F.gam - R(1.0)) * (ht - R(0.5) * (ut * ut + vt * vt)));
+    S SL = smin(unL - cL, unt - ct);
+    S SR = smax(unR + cR, unt + ct);
+    S Ss = (Rt.p - L.p + L.r * unL * (SL - unL) - Rt.r * unR * (SR - unR)) /
+           (L.r * (SL - unL) - Rt.r * (SR - unR));
+    if (val(SL) >= R(0.0)) return normal_flux(L, nx, ny);
+    if (val(SR) <= R(0.0)) return normal_flux(Rt, nx, ny);
+    const CS<S>& K = (val(Ss) >= R(0.0)) ? L : Rt;
+    S SK = (val(Ss) >= R(0.0)) ? SL : SR;
+    S unK = (val(Ss) >= R(0.0)) ? unL : unR;
+    S coef = K.r * (SK - unK) / (SK - Ss);
+    S Us[6];
+    Us[0] = coef;
+    Us[1] = coef * (K.u + (Ss - unK) * nx);
+    Us[2] = coef * (K.v + (Ss - unK) * ny);
+    Us[3] = coef * (K.rE / K.r + (Ss - unK) * (Ss + K.p / (K.r * (SK - unK))));
+    Us[4] = S(R(0));
+    Us[5] = S(R(0));
+    S UK[6] = {K.r, K.ru, K.rv, K.rE, K.rk, K.rw};
+    Flux6<S> FK = normal_flux(K, nx, ny);
+    Flux6<S> o;
+#pragma unroll
+    for (int c = 0; c < 6; ++c) o.f[c] = FK.f[c] + (Us[c] - UK[c]) * SK;
+    return o;
+}
+
+// computeInviscidFlux (include/Flux.hpp:216-227): AUSM falls through to LLF
+template <class S, class R>
+CFD_HD Flux6<S> inviscid_flux(const Flow<R>& F, const CS<S>& L, const CS<S>& Rt, R nx, R ny) {
+    if (F.flux == FLUX_ROE) return flux_roe(F, L, Rt, nx, ny);
+    if (F.flux == FLUX_HLLC) return flux_hllc(F, L, Rt, nx, ny);
+    return flux_llf(F, L, Rt, nx, ny);
+}
+
+// slip-wall reflection (src/Solver.cpp:845-860): k and w copied from the interior
+template <class S, class R>
+CFD_HD CS<S> slip_ghost(const Flow<R>& F, const CS<S>& U, R nx, R ny) {
+    S vn = U.u * nx + U.v * ny;
+    S ug = U.u - R(2.0) * vn * nx;
+    S vg = U.v - R(2.0) * vn * ny;
+    return make_cs(F, U.r, U.r * ug, U.r * vg, U.rE, U.rk, U.rw);
+}
+
+template <class S, class R>
+CFD_HD CS<S> const_state(const Flow<R>& F, const R* s4) {
+    return make_cs(F, S(s4[0]), S(s4[1]), S(s4[2]), S(s4[3]), S(R(0)), S(R(0)));
+}
+
+// getBoundaryGhostState: bump set (src/Solver.cpp:806-863), supersonic set
+// (:973-1011), laminar-plate / SWBLI set (:1088-1139).  Tag 6 (post-shock inflow)
+// has no reference counterpart.  For the SST variables the turbulent far field and
+// wall values follow the SST model's boundary rules (parity unpinned).
+template <class S, class R>
+CFD_HD CS<S> ghost_state(const Flow<R>& F, const CS<S>& U, int tag, R nx, R ny) {
+    const R g = F.gam;
+    if (F.bcset == BC_BUMP) {
+        if (tag == 1) {
+            S pu = smin(U.p, S(F.P0 - R(1e-4)));
+            S Tg = F.T0 * pow(pu / F.P0, (g - R(1.0)) / g);
+            S rg = pu / (F.Rgas * Tg);
+            R Cp = g * F.Rgas / (g - R(1.0));
+            S V2 = R(2.0) * Cp * (F.T0 - Tg);
+            S V = (val(V2) > R(0)) ? sqrt(V2) : S(R(0.0));
+            return p2c(F, rg, V, S(R(0.0)), pu, S(R(0)), S(R(0)));
+        } else if (tag == 2) {
+            return p2c(F, U.r, U.u, U.v, S(F.Pexit), S(R(0)), S(R(0)));
+        } else if (tag == 3) {
+            return slip_ghost(F, U, nx, ny);
+        }
+        return U;
+    } else if (F.bcset == BC_SUPERSONIC) {
+        if (tag == 1) return const_state<S>(F, F.fs);
+        if (tag == 2) return U;
+        if (tag == 3) return slip_ghost(F, U, nx, ny);
+        if (tag == 6) return const_state<S>(F, F.shock);
+        return U;
+    } else {
+        if (tag == 1 || tag == 5) {
+            CS<S> c = const_state<S>(F, F.fs);
+            c.rk = S(c.r * F.k_inf);
+            c.rw = S(c.r * F.w_inf);
+            return c;
+        }
+        if (tag == 6) {
+            CS<S> c = const_state<S>(F, F.shock);
+            c.rk = S(c.r * F.k_inf);
+            c.rw = S(c.r * F.w_inf);
+            return c;
+        }
+        if (tag == 2) return U;
+        if (tag == 3) return slip_ghost(F, U, nx, ny);
+        if (tag == 4) {
+            S ug = -(U.ru / U.r), vg = -(U.rv / U.r);
+            S ek = R(0.5) * (U.ru * U.ru + U.rv * U.rv) / U.r;
+            S pin = (g - R(1.0)) * (U.rE - ek);
+            S Tin = pin / (U.r * F.Rgas);
+            S rg = pin / (F.Rgas * Tin);
+            return p2c(F, rg, ug, vg, pin, S(R(0)), S(R(0)));
+        }
+        return U;
+    }
+}
+
+}  // namespace cfdg

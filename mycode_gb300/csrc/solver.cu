@@ -1,0 +1,1013 @@
+// Host side of libcfdgpu: the solver handle, device buffers, the GMRES and
+// pseudo-transient Newton drivers, and the C ABI declared in include/cfdg.h.
+//
+// All arithmetic on vectors and states runs in the CUDA kernels (kern_*.cu).  The host
+// keeps only what the reference keeps in scalars: the Hessenberg matrix, the Givens
+// rotations and the CFL / relaxation logic of solveGMRES and solveImplicit
+// (AmberMond/mycode src/Solver.cpp:1472-1618, :1696-1799), evaluated with the same
+// expressions so the Newton trace follows the reference.
+#include <cuda_runtime.h>
+
+#include <chrono>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "../../include/cfdg.h"
+#include "launch.hpp"
+#include "mesh.hpp"
+
+using namespace cfdg;
+
+struct cfdg_mesh {
+    HostMesh h;
+};
+
+namespace {
+
+thread_local std::string g_err;
+
+cfdg_status fail(cfdg_status st, const std::string& msg) {
+    g_err = msg;
+    return st;
+}
+
+#define CK(call)                                                                                   \
+    do {                                                                                           \
+        cudaError_t e_ = (call);                                                                   \
+        if (e_ != cudaSuccess) return fail(CFDG_ERR_CUDA, std::string(#call) + ": " + cudaGetErrorString(e_)); \
+    } while (0)
+
+#define TRY(expr)                          \
+    do {                                   \
+        cfdg_status st_ = (expr);          \
+        if (st_ != CFDG_OK) return st_;    \
+    } while (0)
+
+template <class T>
+cfdg_status dalloc(T** p, size_t n) {
+    *p = nullptr;
+    if (n == 0) n = 1;
+    CK(cudaMalloc((void**)p, n * sizeof(T)));
+    CK(cudaMemset(*p, 0, n * sizeof(T)));
+    return CFDG_OK;
+}
+
+template <class R>
+struct GeoBuf {
+    R *nx = nullptr, *ny = nullptr, *area = nullptr, *dxo = nullptr, *dyo = nullptr, *dxn = nullptr, *dyn = nullptr,
+      *dxlr = nullptr, *dylr = nullptr, *vol = nullptr;
+    void release() {
+        R* a[] = {nx, ny, area, dxo, dyo, dxn, dyn, dxlr, dylr, vol};
+        for (R* p : a) cudaFree(p);
+    }
+};
+
+template <class R>
+cfdg_status upload_geo(GeoBuf<R>& g, const HostMesh& h) {
+    const std::vector<double>* src[] = {&h.nx, &h.ny, &h.area, &h.dxo, &h.dyo, &h.dxn, &h.dyn, &h.dxlr, &h.dylr, &h.vol};
+    R** dst[] = {&g.nx, &g.ny, &g.area, &g.dxo, &g.dyo, &g.dxn, &g.dyn, &g.dxlr, &g.dylr, &g.vol};
+    for (int k = 0; k < 10; ++k) {
+        std::vector<R> tmp(src[k]->begin(), src[k]->end());
+        TRY(dalloc(dst[k], tmp.size()));
+        CK(cudaMemcpy(*dst[k], tmp.data(), tmp.size() * sizeof(R), cudaMemcpyHostToDevice));
+    }
+    return CFDG_OK;
+}
+
+double now_s() {
+    return std::chrono::duration<double>(std::chrono::steady_clock::now().time_since_epoch()).count();
+}
+
+}  // namespace
+
+struct cfdg_solver {
+    const cfdg_mesh* mesh = nullptr;
+    cfdg_config cfg;
+    int nv = 4, nc = 0, nf = 0;
+    long L = 0;  // nv * nc
+    cudaStream_t st = nullptr;
+    // flow parameters (Solver members, include/Solver.hpp:37-39, :93-95)
+    double M_inf = 0, P0 = 0, T0 = 0, Pexit = 0, nu = 0.01;
+    Flow<double> F;
+    Flow<float> Ff;
+    // device mesh
+    int *cf = nullptr, *fo = nullptr, *fn = nullptr, *ftag = nullptr, *perm = nullptr;
+    GeoBuf<double> g64;
+    GeoBuf<float> g32;
+    MeshView<double> mv;
+    MeshView<float> mvf;
+    // FP64 state and work
+    double *U = nullptr, *W = nullptr, *G = nullptr, *phi = nullptr, *FA = nullptr, *R = nullptr, *dt = nullptr,
+           *D = nullptr;
+    double *stage = nullptr;   // AoS staging, 14 doubles per cell
+    double *Ub = nullptr, *Rb = nullptr, *Up = nullptr, *Rp = nullptr, *vtmp = nullptr, *x = nullptr, *rhs = nullptr;
+    // dual (exact J v) work, FP64
+    double *Wj = nullptr, *Wjd = nullptr, *Gj = nullptr, *Gjd = nullptr, *FAjd = nullptr;
+    // FP32 (mixed precision) work
+    float *U32 = nullptr, *W32 = nullptr, *W32d = nullptr, *G32 = nullptr, *G32d = nullptr, *FA32d = nullptr,
+          *phi32 = nullptr, *dt32 = nullptr, *V32 = nullptr, *z32 = nullptr;
+    // Krylov basis FP64
+    double *V = nullptr, *z = nullptr;
+    int m_alloc = 0;
+    // reductions
+    RedScratch rs{nullptr, nullptr};
+    double* scal = nullptr;  // [0] |U|^2 [1] |z|^2 [2] eps [3] beta^2 [4..6] vm [8..] H columns, y
+    int* bad = nullptr;
+    // Newton driver state
+    double cfl = 0.1;
+    int step = 0;
+    bool limiter_valid = false;
+    // instrumentation
+    int timing = 0;
+    cudaEvent_t ev[5] = {};
+    float kms[4] = {0, 0, 0, 0};
+    long long launches = 0;
+
+    double* hcol(int j) { return scal + 16 + (size_t)j * (cfg.gmres_m + 2); }
+    double* ydev() { return scal + 16 + (size_t)(cfg.gmres_m + 1) * (cfg.gmres_m + 2); }
+
+    Field<double> f64(double* v, double* d = nullptr) { return Field<double>{v, d, nc}; }
+    Field<double> ff64(double* v, double* d = nullptr) { return Field<double>{v, d, nf}; }
+    Field<float> f32(float* v, float* d = nullptr) { return Field<float>{v, d, nc}; }
+    Field<float> ff32(float* v, float* d = nullptr) { return Field<float>{v, d, nf}; }
+
+    void set_flow() {
+        F.gam = cfg.gamma;
+        F.Rgas = cfg.R_gas;
+        F.Pr = cfg.Pr;
+        F.nu = nu;
+        F.Minf = M_inf;
+        F.P0 = P0;
+        F.T0 = T0;
+        F.Pexit = Pexit;
+        F.bcset = cfg.bcset;
+        F.flux = cfg.flux;
+        F.spatial = cfg.spatial;
+        F.viscous = cfg.viscous;
+        // frozen free stream, same expressions as src/Solver.cpp:979-985 (host IEEE
+        // arithmetic without contraction gives the device's values)
+        double g = cfg.gamma, M = M_inf;
+        double fT = 1.0 + 0.5 * (g - 1.0) * M * M;
+        double Ts = T0 / fT;
+        double rho = Pexit / (cfg.R_gas * Ts);
+        double c = std::sqrt(g * cfg.R_gas * Ts);
+        double u = M * c;
+        double rE = Pexit / (g - 1.0) + 0.5 * rho * (u * u + 0.0 * 0.0);
+        F.fs[0] = rho;
+        F.fs[1] = rho * u;
+        F.fs[2] = rho * 0.0;
+        F.fs[3] = rE;
+        for (int k = 0; k < 4; ++k) F.shock[k] = F.fs[k];
+        if (cfg.shock_deflection_deg > 0.0 && M > 1.0) post_shock(F.shock, rho, u, Pexit, g);
+        F.k_inf = 0;
+        F.w_inf = 0;
+        F.Pr_t = 0.9;
+        Ff.gam = (float)F.gam; Ff.Rgas = (float)F.Rgas; Ff.Pr = (float)F.Pr; Ff.nu = (float)F.nu;
+        Ff.Minf = (float)F.Minf; Ff.P0 = (float)F.P0; Ff.T0 = (float)F.T0; Ff.Pexit = (float)F.Pexit;
+        for (int k = 0; k < 4; ++k) { Ff.fs[k] = (float)F.fs[k]; Ff.shock[k] = (float)F.shock[k]; }
+        Ff.k_inf = (float)F.k_inf; Ff.w_inf = (float)F.w_inf; Ff.Pr_t = (float)F.Pr_t;
+        Ff.bcset = F.bcset; Ff.flux = F.flux; Ff.spatial = F.spatial; Ff.viscous = F.viscous;
+    }
+
+    // state behind an oblique shock of deflection theta (theta-beta-M relation, weak branch)
+    void post_shock(double* out, double rho1, double u1, double p1, double g) {
+        double M1 = M_inf, th = cfg.shock_deflection_deg * M_PI / 180.0;
+        double beta = std::asin(1.0 / M1) + 1e-6, best = beta;
+        for (int it = 0; it < 200000; ++it) {
+            double b = std::asin(1.0 / M1) + it * (M_PI / 2 - std::asin(1.0 / M1)) / 200000.0;
+            double t = std::atan(2.0 / std::tan(b) * (M1 * M1 * std::sin(b) * std::sin(b) - 1.0) /
+                                 (M1 * M1 * (g + std::cos(2 * b)) + 2.0));
+            if (t >= th) { best = b; break; }
+        }
+        beta = best;
+        double Mn1 = M1 * std::sin(beta);
+        double r2 = rho1 * (g + 1) * Mn1 * Mn1 / ((g - 1) * Mn1 * Mn1 + 2);
+        double p2 = p1 * (1 + 2 * g / (g + 1) * (Mn1 * Mn1 - 1));
+        double un1 = u1 * std::sin(beta), ut = u1 * std::cos(beta);
+        double un2 = un1 * rho1 / r2;
+        // flow turned by -theta (downwards) behind a shock from the upper boundary
+        double V2 = std::sqrt(un2 * un2 + ut * ut);
+        double ux = V2 * std::cos(th), uy = -V2 * std::sin(th);
+        out[0] = r2;
+        out[1] = r2 * ux;
+        out[2] = r2 * uy;
+        out[3] = p2 / (g - 1) + 0.5 * r2 * (ux * ux + uy * uy);
+    }
+
+    ResArgs<double> res64(double* Uin, double* out, int do_lim) {
+        ResArgs<double> a;
+        a.m = mv;
+        a.F = F;
+        a.nv = nv;
+        a.U = f64(Uin);
+        a.W = f64(W);
+        a.G = f64(G);
+        a.FA = ff64(FA);
+        a.phi = phi;
+        a.out = out;
+        a.do_limiter = do_lim;
+        a.diag_v = nullptr;
+        a.dt = nullptr;
+        a.stream = st;
+        a.ev = timing ? ev : nullptr;
+        return a;
+    }
+
+    cfdg_status residual_dev(double* Uin, double* out, int update_limiters) {
+        int do_lim = (cfg.spatial == CFDG_SECOND_ORDER_LIMITED && update_limiters) ? 1 : 0;
+        ResArgs<double> a = res64(Uin, out, do_lim);
+        launch_residual<double>(a);
+        launches += 4;
+        if (do_lim) limiter_valid = true;
+        CK(cudaGetLastError());
+        if (timing) {
+            CK(cudaEventSynchronize(ev[4]));
+            for (int k = 0; k < 4; ++k) cudaEventElapsedTime(&kms[k], ev[k], ev[k + 1]);
+        }
+        return CFDG_OK;
+    }
+
+    cfdg_status upload_aos(const double* host, double* dev_soa, int np = -1) {
+        if (np < 0) np = nv;
+        CK(cudaMemcpyAsync(stage, host, sizeof(double) * 6 * (size_t)nc, cudaMemcpyHostToDevice, st));
+        launch_aos_to_soa<double>(nc, np, 6, stage, perm, dev_soa, st);
+        ++launches;
+        CK(cudaGetLastError());
+        return CFDG_OK;
+    }
+
+    cfdg_status download_aos(const double* dev_soa, double* host, int np, int stride) {
+        launch_soa_to_aos<double>(nc, np, stride, dev_soa, perm, stage, st);
+        ++launches;
+        CK(cudaGetLastError());
+        CK(cudaMemcpyAsync(host, stage, sizeof(double) * stride * (size_t)nc, cudaMemcpyDeviceToHost, st));
+        CK(cudaStreamSynchronize(st));
+        return CFDG_OK;
+    }
+
+    cfdg_status read_scalars(int first, int n, double* out) {
+        CK(cudaMemcpyAsync(out, scal + first, sizeof(double) * n, cudaMemcpyDeviceToHost, st));
+        CK(cudaStreamSynchronize(st));
+        return CFDG_OK;
+    }
+
+    // J v at Ub (FD about (Ub, Rb), or exact).  v, out FP64 device vectors.
+    cfdg_status jv64(double* Ubase, double* Rbase, double* v, double* out, int mode, bool have_usq) {
+        if (mode == CFDG_JV_FD) {
+            if (!have_usq) { launch_dot<double>(nv, nc, Ubase, Ubase, rs, scal + 0, st); ++launches; }
+            launch_dot<double>(nv, nc, v, v, rs, scal + 1, st);
+            launch_fd_perturb(L, Ubase, v, scal + 0, scal + 1, Up, scal + 2, st);
+            launches += 2;
+            TRY(residual_dev(Up, Rp, 0));
+            launch_fd_combine(nv, nc, Rp, Rbase, v, scal + 2, g64.vol, dt, out, st);
+            ++launches;
+        } else {
+            ResArgs<double> a;
+            a.m = mv;
+            a.F = F;
+            a.nv = nv;
+            a.U = f64(Ubase, v);
+            a.W = f64(Wj, Wjd);
+            a.G = f64(Gj, Gjd);
+            a.FA = ff64(nullptr, FAjd);
+            a.phi = phi;
+            a.out = out;
+            a.do_limiter = 0;
+            a.diag_v = v;
+            a.dt = dt;
+            a.stream = st;
+            a.ev = nullptr;
+            launch_jv<double>(a);
+            launches += 4;
+        }
+        CK(cudaGetLastError());
+        return CFDG_OK;
+    }
+
+    cfdg_status ensure_krylov() {
+        int m = cfg.gmres_m;
+        if (m_alloc >= m) return CFDG_OK;
+        cudaFree(V); cudaFree(z); cudaFree(V32); cudaFree(z32);
+        V = nullptr; z = nullptr; V32 = nullptr; z32 = nullptr;
+        if (cfg.precision == CFDG_MIXED) {
+            TRY(dalloc(&V32, (size_t)(m + 1) * L));
+            TRY(dalloc(&z32, (size_t)L));
+        } else {
+            TRY(dalloc(&V, (size_t)(m + 1) * L));
+            TRY(dalloc(&z, (size_t)L));
+        }
+        m_alloc = m;
+        return CFDG_OK;
+    }
+
+    // solveGMRES (src/Solver.cpp:1472-1618) about Ubase with the preconditioner of the
+    // current state; rhs and xout are FP64 device vectors.
+    cfdg_status gmres(double* Ubase, double* Rbase, double* rhsd, double* xout, int* iters) {
+        const int m = cfg.gmres_m;
+        const bool mixed = cfg.precision == CFDG_MIXED;
+        const int mode = mixed ? CFDG_JV_EXACT : cfg.jv;
+        TRY(ensure_krylov());
+        // preconditioner on the current state (computeDiagonalPreconditioner uses U_current)
+        launch_prim64(nv, nc, F, f64(U), f64(W), st);
+        launch_precond(nv, mv, F, U, W, dt, D, st);
+        launches += 2;
+        launch_dot<double>(nv, nc, rhsd, rhsd, rs, scal + 3, st);
+        ++launches;
+        double beta2;
+        TRY(read_scalars(3, 1, &beta2));
+        double beta = std::sqrt(beta2);
+        *iters = 0;
+        if (beta < 1e-12) {
+            CK(cudaMemsetAsync(xout, 0, sizeof(double) * L, st));
+            return CFDG_OK;
+        }
+        if (mixed) {
+            // linearisation point and frozen limiter in FP32
+            launch_convert<float>(L, Ubase, U32, st);
+            launch_convert<float>(nc, phi, phi32, st);
+            launch_convert<float>(nc, dt, dt32, st);
+            launches += 3;
+            // V0 = rhs * (1/beta) in FP32: scale by 1/beta computed on the device
+            CK(cudaMemcpyAsync(scal + 5, &beta, sizeof(double), cudaMemcpyHostToDevice, st));
+            launch_scale_from<float>(L, V32, rhsd, scal + 5, 1, st);
+            ++launches;
+        } else {
+            CK(cudaMemcpyAsync(scal + 5, &beta, sizeof(double), cudaMemcpyHostToDevice, st));
+            launch_scale_from<double>(L, V, rhsd, scal + 5, 1, st);
+            ++launches;
+            if (mode == CFDG_JV_FD) { launch_dot<double>(nv, nc, Ubase, Ubase, rs, scal + 0, st); ++launches; }
+        }
+        std::vector<double> H((size_t)(m + 1) * m, 0.0), sn(m, 0.0), cs(m, 0.0), g(m + 1, 0.0), col(m + 2);
+        auto HH = [&](int i, int j) -> double& { return H[(size_t)i * m + j]; };
+        g[0] = beta;
+        int k = 0;
+        for (int j = 0; j < m; ++j) {
+            k = j;
+            double* hc = hcol(j);
+            if (mixed) {
+                float* Vj = V32 + (size_t)j * L;
+                float* Vj1 = V32 + (size_t)(j + 1) * L;
+                launch_precond_apply<float>(nv, nc, Vj, D, z32, rs, nullptr, st);
+                ResArgs<float> a;
+                a.m = mvf;
+                a.F = Ff;
+                a.nv = nv;
+                a.U = f32(U32, z32);
+                a.W = f32(W32, W32d);
+                a.G = f32(G32, G32d);
+                a.FA = ff32(nullptr, FA32d);
+                a.phi = phi32;
+                a.out = Vj1;
+                a.do_limiter = 0;
+                a.diag_v = z32;
+                a.dt = dt32;
+                a.stream = st;
+                a.ev = nullptr;
+                launch_jv<float>(a);
+                launches += 5;
+                for (int i = 0; i <= j; ++i) {
+                    launch_mgs<float>(nv, nc, Vj1, i > 0 ? V32 + (size_t)(i - 1) * L : nullptr, hc + i - 1,
+                                      V32 + (size_t)i * L, rs, hc + i, st);
+                }
+                launch_mgs<float>(nv, nc, Vj1, V32 + (size_t)j * L, hc + j, nullptr, rs, hc + j + 1, st);
+                launch_scale_guard<float>(L, Vj1, hc + j + 1, 1e-12, st);
+                launches += j + 3;
+            } else {
+                double* Vj = V + (size_t)j * L;
+                double* Vj1 = V + (size_t)(j + 1) * L;
+                launch_precond_apply<double>(nv, nc, Vj, D, z, rs, nullptr, st);
+                ++launches;
+                TRY(jv64(Ubase, Rbase, z, Vj1, mode, true));
+                for (int i = 0; i <= j; ++i) {
+                    launch_mgs<double>(nv, nc, Vj1, i > 0 ? V + (size_t)(i - 1) * L : nullptr, hc + i - 1,
+                                       V + (size_t)i * L, rs, hc + i, st);
+                }
+                launch_mgs<double>(nv, nc, Vj1, V + (size_t)j * L, hc + j, nullptr, rs, hc + j + 1, st);
+                launch_scale_guard<double>(L, Vj1, hc + j + 1, 1e-12, st);
+                launches += j + 3;
+            }
+            CK(cudaGetLastError());
+            CK(cudaMemcpyAsync(col.data(), hc, sizeof(double) * (j + 2), cudaMemcpyDeviceToHost, st));
+            CK(cudaStreamSynchronize(st));
+            for (int i = 0; i <= j; ++i) HH(i, j) = col[i];
+            HH(j + 1, j) = std::sqrt(col[j + 1]);
+            // Givens rotations (src/Solver.cpp:1562-1584)
+            for (int i = 0; i < j; ++i) {
+                double t = cs[i] * HH(i, j) + sn[i] * HH(i + 1, j);
+                HH(i + 1, j) = -sn[i] * HH(i, j) + cs[i] * HH(i + 1, j);
+                HH(i, j) = t;
+            }
+            double a = HH(j, j), b = HH(j + 1, j);
+            if (std::fabs(b) < 1e-14) {
+                cs[j] = 1.0;
+                sn[j] = 0.0;
+            } else {
+                double t = std::sqrt(a * a + b * b);
+                cs[j] = a / t;
+                sn[j] = b / t;
+            }
+            HH(j, j) = cs[j] * a + sn[j] * b;
+            HH(j + 1, j) = 0.0;
+            g[j + 1] = -sn[j] * g[j];
+            g[j] = cs[j] * g[j];
+            if (std::fabs(g[j + 1]) < cfg.gmres_tol * beta) break;
+        }
+        // back substitution (src/Solver.cpp:1592-1599)
+        std::vector<double> y(k + 1);
+        for (int i = k; i >= 0; --i) {
+            y[i] = g[i];
+            for (int l = i + 1; l <= k; ++l) y[i] -= HH(i, l) * y[l];
+            y[i] /= HH(i, i);
+        }
+        CK(cudaMemcpyAsync(ydev(), y.data(), sizeof(double) * (k + 1), cudaMemcpyHostToDevice, st));
+        if (mixed) launch_gmres_solution<float>(nv, nc, V32, L, ydev(), k, D, xout, st);
+        else launch_gmres_solution<double>(nv, nc, V, L, ydev(), k, D, xout, st);
+        ++launches;
+        CK(cudaGetLastError());
+        CK(cudaStreamSynchronize(st));
+        *iters = k + 1;
+        return CFDG_OK;
+    }
+
+    // one step of solveImplicit (src/Solver.cpp:1705-1797)
+    cfdg_status newton_step(double tol, cfdg_step* info, int* converged) {
+        double t0 = now_s();
+        *converged = 0;
+        launch_prim64(nv, nc, F, f64(U), f64(W), st);
+        launch_local_dt(nv, mv, F, U, W, cfl, dt, st);
+        launches += 2;
+        bool upd = !(step > cfg.limiter_freeze_step || cfl > cfg.limiter_freeze_cfl);
+        TRY(residual_dev(U, R, upd ? 1 : 0));
+        launch_norm_vm(nv, nc, R, g64.vol, rs, scal + 8, st);
+        launch_dot<double>(nv, nc, R, R, rs, scal + 11, st);
+        launches += 2;
+        double s[4];
+        TRY(read_scalars(8, 4, s));
+        double resVM = s[1] == 0 ? 0.0 : std::sqrt(s[0] / s[1]);
+        double resRho = s[1] == 0 ? 0.0 : std::sqrt(s[2] / s[1]);
+        double resAbs = std::sqrt(s[3]);
+        cfdg_step rec;
+        rec.res_vm = resVM;
+        rec.res_abs = resAbs;
+        rec.res_rho = resRho;
+        rec.cfl = cfl;
+        rec.gmres_iters = 0;
+        rec.limiter_updated = upd ? 1 : 0;
+        rec.seconds = 0;
+        if (!std::isfinite(resVM)) {
+            if (info) *info = rec;
+            return fail(CFDG_ERR_NAN, "non-finite residual at Newton step " + std::to_string(step));
+        }
+        if (resVM < tol) {
+            *converged = 1;
+            rec.seconds = now_s() - t0;
+            if (info) *info = rec;
+            return CFDG_OK;
+        }
+        // RHS = -R
+        double m1 = -1.0;
+        CK(cudaMemcpyAsync(scal + 6, &m1, sizeof(double), cudaMemcpyHostToDevice, st));
+        launch_scale_from<double>(L, rhs, R, scal + 6, 0, st);
+        ++launches;
+        int it = 0;
+        TRY(gmres(U, R, rhs, x, &it));
+        rec.gmres_iters = it;
+        if (it >= 29) {
+            cfl *= 0.5;
+            if (cfl < 0.05) cfl = 0.05;
+        }
+        double relax = 1.0;
+        if (resVM > 1e6) relax = 0.5;
+        else if (resVM > 2e3 && resVM < 1e2) relax = 0.9;
+        CK(cudaMemsetAsync(bad, 0, sizeof(int), st));
+        launch_newton_update(nv, nc, U, x, relax, cfg.gamma, bad, st);
+        ++launches;
+        int hbad = 0;
+        CK(cudaMemcpyAsync(&hbad, bad, sizeof(int), cudaMemcpyDeviceToHost, st));
+        CK(cudaStreamSynchronize(st));
+        if (step > 5) {
+            if (resVM > 1e6) cfl *= 1.2;
+            else cfl *= 1.5;
+            if (it >= 25) cfl *= 0.5;
+            if (cfl > cfg.cfl_max) cfl = cfg.cfl_max;
+            if (cfl < 0.1) cfl = 0.1;
+        }
+        ++step;
+        rec.seconds = now_s() - t0;
+        if (info) *info = rec;
+        if (hbad) return fail(CFDG_ERR_NAN, "non-finite state after the Newton update at step " + std::to_string(step - 1));
+        return CFDG_OK;
+    }
+
+    void release() {
+        void* ps[] = {cf, fo, fn, ftag, perm, U, W, G, phi, FA, R, dt, D, stage, Ub, Rb, Up, Rp, vtmp, x, rhs,
+                      Wj, Wjd, Gj, Gjd, FAjd, U32, W32, W32d, G32, G32d, FA32d, phi32, dt32, V32, z32, V, z,
+                      rs.partial, rs.counter, scal, bad};
+        for (void* p : ps) cudaFree(p);
+        g64.release();
+        g32.release();
+        for (auto& e : ev) if (e) cudaEventDestroy(e);
+        if (st) cudaStreamDestroy(st);
+    }
+};
+
+// ------------------------------------------------------------------ C ABI
+
+extern "C" {
+
+const char* cfdg_version(void) { return "cfdg 0.1 (sm_103a)"; }
+
+const char* cfdg_last_error(void) { return g_err.c_str(); }
+
+cfdg_status cfdg_device_count(int* n) {
+    if (!n) return fail(CFDG_ERR_ARG, "null pointer");
+    int c = 0;
+    cudaError_t e = cudaGetDeviceCount(&c);
+    if (e != cudaSuccess) {
+        cudaGetLastError();
+        c = 0;
+    }
+    *n = c;
+    return CFDG_OK;
+}
+
+void cfdg_config_default(cfdg_config* c) {
+    if (!c) return;
+    std::memset(c, 0, sizeof(*c));
+    c->flux = CFDG_FLUX_HLLC;
+    c->spatial = CFDG_SECOND_ORDER_LIMITED;
+    c->bcset = CFDG_BC_BUMP;
+    c->init = CFDG_INIT_BUMP;
+    c->viscous = 0;
+    c->turbulence = CFDG_TURB_NONE;
+    c->precision = CFDG_FP64;
+    c->jv = CFDG_JV_FD;
+    c->gmres_m = 40;
+    c->gmres_tol = 1e-2;
+    c->gamma = 1.4;
+    c->R_gas = 287.0;
+    c->Pr = 0.72;
+    c->nu = 0.01;
+    c->cfl0 = 0.1;
+    c->cfl_max = 10000.0;
+    c->limiter_freeze_step = 150;
+    c->limiter_freeze_cfl = 10.0;
+    c->turb_intensity = 0.001;
+    c->mut_ratio = 0.01;
+    c->shock_deflection_deg = 0.0;
+    c->renumber = CFDG_RENUMBER_HILBERT;
+    c->device = 0;
+}
+
+cfdg_status cfdg_mesh_create(int n_nodes, const double* xy, int n_cells, const int* cells, int n_bedges,
+                             const int* bedges, int renumber, cfdg_mesh** out) {
+    if (!out || !xy || !cells || (n_bedges > 0 && !bedges) || n_nodes <= 0 || n_cells <= 0 || n_bedges < 0)
+        return fail(CFDG_ERR_ARG, "cfdg_mesh_create: bad arguments");
+    cfdg_mesh* m = new cfdg_mesh();
+    std::string e = build_mesh(m->h, n_nodes, xy, n_cells, cells, n_bedges, bedges, renumber);
+    if (!e.empty()) {
+        delete m;
+        return fail(CFDG_ERR_MESH, e);
+    }
+    *out = m;
+    return CFDG_OK;
+}
+
+cfdg_status cfdg_mesh_load_gmsh(const char* path, int renumber, cfdg_mesh** out) {
+    if (!path || !out) return fail(CFDG_ERR_ARG, "cfdg_mesh_load_gmsh: null argument");
+    std::vector<double> xy;
+    std::vector<int> cells, bed;
+    std::string e = read_gmsh(path, xy, cells, bed);
+    if (!e.empty()) return fail(CFDG_ERR_MESH, e);
+    if (cells.empty()) return fail(CFDG_ERR_MESH, std::string("no cells in ") + path);
+    return cfdg_mesh_create((int)(xy.size() / 2), xy.data(), (int)(cells.size() / 4), cells.data(),
+                            (int)(bed.size() / 3), bed.empty() ? nullptr : bed.data(), renumber, out);
+}
+
+cfdg_status cfdg_mesh_sizes(const cfdg_mesh* m, int* n_cells, int* n_faces, int* n_boundary_faces) {
+    if (!m) return fail(CFDG_ERR_ARG, "null mesh");
+    if (n_cells) *n_cells = m->h.n_cells;
+    if (n_faces) *n_faces = m->h.n_faces;
+    if (n_boundary_faces) *n_boundary_faces = m->h.n_faces - m->h.n_interior;
+    return CFDG_OK;
+}
+
+cfdg_status cfdg_mesh_faces(const cfdg_mesh* m, int* i5, double* d5) {
+    if (!m || !i5 || !d5) return fail(CFDG_ERR_ARG, "null argument");
+    const HostMesh& h = m->h;
+    for (int f = 0; f < h.n_faces; ++f) {
+        i5[5 * f] = h.f_n1[f]; i5[5 * f + 1] = h.f_n2[f]; i5[5 * f + 2] = h.f_o[f];
+        i5[5 * f + 3] = h.f_n[f]; i5[5 * f + 4] = h.f_tag[f];
+        d5[5 * f] = h.f_nx[f]; d5[5 * f + 1] = h.f_ny[f]; d5[5 * f + 2] = h.f_area[f];
+        d5[5 * f + 3] = h.f_xm[f]; d5[5 * f + 4] = h.f_ym[f];
+    }
+    return CFDG_OK;
+}
+
+cfdg_status cfdg_mesh_cells(const cfdg_mesh* m, double* d3) {
+    if (!m || !d3) return fail(CFDG_ERR_ARG, "null argument");
+    for (int c = 0; c < m->h.n_cells; ++c) {
+        d3[3 * c] = m->h.c_vol[c]; d3[3 * c + 1] = m->h.c_xc[c]; d3[3 * c + 2] = m->h.c_yc[c];
+    }
+    return CFDG_OK;
+}
+
+cfdg_status cfdg_mesh_permutation(const cfdg_mesh* m, int* cell_perm, int* face_perm) {
+    if (!m) return fail(CFDG_ERR_ARG, "null mesh");
+    if (cell_perm) std::memcpy(cell_perm, m->h.cell_perm.data(), sizeof(int) * m->h.n_cells);
+    if (face_perm) std::memcpy(face_perm, m->h.face_perm.data(), sizeof(int) * m->h.n_faces);
+    return CFDG_OK;
+}
+
+void cfdg_mesh_destroy(cfdg_mesh* m) { delete m; }
+
+cfdg_status cfdg_solver_create(const cfdg_mesh* m, const cfdg_config* cfg, cfdg_solver** out) {
+    if (!m || !out) return fail(CFDG_ERR_ARG, "cfdg_solver_create: null argument");
+    cfdg_config c;
+    if (cfg) c = *cfg;
+    else cfdg_config_default(&c);
+    if (c.gmres_m < 1 || c.gmres_m > 400) return fail(CFDG_ERR_ARG, "gmres_m must be in [1, 400]");
+    if (c.flux < 0 || c.flux > 3 || c.spatial < 0 || c.spatial > 2 || c.bcset < 0 || c.bcset > 2)
+        return fail(CFDG_ERR_ARG, "unknown flux, spatial scheme or boundary-condition set");
+    if (c.turbulence != CFDG_TURB_NONE) return fail(CFDG_ERR_UNSUPPORTED, "SST is not built into this library yet");
+    int ndev = 0;
+    if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) {
+        cudaGetLastError();
+        return fail(CFDG_ERR_CUDA, "no CUDA device available (this library has no CPU path)");
+    }
+    if (c.device < 0 || c.device >= ndev) return fail(CFDG_ERR_ARG, "device ordinal out of range");
+    CK(cudaSetDevice(c.device));
+    cfdg_solver* s = new cfdg_solver();
+    s->mesh = m;
+    s->cfg = c;
+    s->nv = c.turbulence == CFDG_TURB_SST ? 6 : 4;
+    s->nc = m->h.n_cells;
+    s->nf = m->h.n_faces;
+    s->L = (long)s->nv * s->nc;
+    s->nu = c.nu;
+    s->cfl = c.cfl0;
+    auto bail = [&](cfdg_status st) {
+        s->release();
+        delete s;
+        return st;
+    };
+#define TRYS(expr)                       \
+    do {                                 \
+        cfdg_status st_ = (expr);        \
+        if (st_ != CFDG_OK) return bail(st_); \
+    } while (0)
+    if (cudaStreamCreateWithFlags(&s->st, cudaStreamNonBlocking) != cudaSuccess) return bail(fail(CFDG_ERR_CUDA, "stream"));
+    for (auto& e : s->ev) cudaEventCreate(&e);
+    const HostMesh& h = m->h;
+    int nc = s->nc, nf = s->nf, nv = s->nv;
+    long L = s->L;
+    TRYS(dalloc(&s->cf, 4 * (size_t)nc));
+    TRYS(dalloc(&s->fo, nf));
+    TRYS(dalloc(&s->fn, nf));
+    TRYS(dalloc(&s->ftag, nf));
+    TRYS(dalloc(&s->perm, nc));
+    if (cudaMemcpy(s->cf, h.cf.data(), sizeof(int) * 4 * (size_t)nc, cudaMemcpyHostToDevice) != cudaSuccess ||
+        cudaMemcpy(s->fo, h.fo.data(), sizeof(int) * nf, cudaMemcpyHostToDevice) != cudaSuccess ||
+        cudaMemcpy(s->fn, h.fn.data(), sizeof(int) * nf, cudaMemcpyHostToDevice) != cudaSuccess ||
+        cudaMemcpy(s->ftag, h.ftag.data(), sizeof(int) * nf, cudaMemcpyHostToDevice) != cudaSuccess ||
+        cudaMemcpy(s->perm, h.cell_perm.data(), sizeof(int) * nc, cudaMemcpyHostToDevice) != cudaSuccess)
+        return bail(fail(CFDG_ERR_CUDA, "mesh upload failed"));
+    TRYS(upload_geo(s->g64, h));
+    TRYS(upload_geo(s->g32, h));
+    auto view = [&](auto& g, auto& mvx) {
+        mvx.nc = nc; mvx.nf = nf; mvx.nfi = h.n_interior;
+        mvx.cf = s->cf; mvx.fo = s->fo; mvx.fn = s->fn; mvx.ftag = s->ftag;
+        mvx.nx = g.nx; mvx.ny = g.ny; mvx.area = g.area; mvx.dxo = g.dxo; mvx.dyo = g.dyo;
+        mvx.dxn = g.dxn; mvx.dyn = g.dyn; mvx.dxlr = g.dxlr; mvx.dylr = g.dylr; mvx.vol = g.vol;
+    };
+    view(s->g64, s->mv);
+    view(s->g32, s->mvf);
+    int NW = nv == 6 ? 7 : 5, NG = nv == 6 ? 14 : 10;
+    TRYS(dalloc(&s->U, L)); TRYS(dalloc(&s->W, (size_t)NW * nc)); TRYS(dalloc(&s->G, (size_t)NG * nc));
+    TRYS(dalloc(&s->phi, nc)); TRYS(dalloc(&s->FA, (size_t)nv * nf)); TRYS(dalloc(&s->R, L));
+    TRYS(dalloc(&s->dt, nc)); TRYS(dalloc(&s->D, nc)); TRYS(dalloc(&s->stage, 14 * (size_t)nc));
+    TRYS(dalloc(&s->Ub, L)); TRYS(dalloc(&s->Rb, L)); TRYS(dalloc(&s->Up, L)); TRYS(dalloc(&s->Rp, L));
+    TRYS(dalloc(&s->vtmp, L)); TRYS(dalloc(&s->x, L)); TRYS(dalloc(&s->rhs, L));
+    TRYS(dalloc(&s->Wj, (size_t)NW * nc)); TRYS(dalloc(&s->Wjd, (size_t)NW * nc));
+    TRYS(dalloc(&s->Gj, (size_t)NG * nc)); TRYS(dalloc(&s->Gjd, (size_t)NG * nc));
+    TRYS(dalloc(&s->FAjd, (size_t)nv * nf));
+    if (c.precision == CFDG_MIXED) {
+        TRYS(dalloc(&s->U32, L)); TRYS(dalloc(&s->W32, (size_t)NW * nc)); TRYS(dalloc(&s->W32d, (size_t)NW * nc));
+        TRYS(dalloc(&s->G32, (size_t)NG * nc)); TRYS(dalloc(&s->G32d, (size_t)NG * nc));
+        TRYS(dalloc(&s->FA32d, (size_t)nv * nf)); TRYS(dalloc(&s->phi32, nc)); TRYS(dalloc(&s->dt32, nc));
+    }
+    TRYS(dalloc(&s->rs.partial, 3 * (size_t)RED_BLOCKS));
+    TRYS(dalloc(&s->rs.counter, 1));
+    TRYS(dalloc(&s->scal, 16 + (size_t)(c.gmres_m + 2) * (c.gmres_m + 2) + 8));
+    TRYS(dalloc(&s->bad, 1));
+    // limiter starts at 1 (no limiting) until the first limited evaluation
+    std::vector<double> ones(nc, 1.0);
+    if (cudaMemcpy(s->phi, ones.data(), sizeof(double) * nc, cudaMemcpyHostToDevice) != cudaSuccess)
+        return bail(fail(CFDG_ERR_CUDA, "limiter init failed"));
+    s->set_flow();
+#undef TRYS
+    *out = s;
+    return CFDG_OK;
+}
+
+void cfdg_solver_destroy(cfdg_solver* s) {
+    if (!s) return;
+    cudaStreamSynchronize(s->st);
+    s->release();
+    delete s;
+}
+
+cfdg_status cfdg_set_numerical_method(cfdg_solver* s, int flux, int spatial) {
+    if (!s || flux < 0 || flux > 3 || spatial < 0 || spatial > 2) return fail(CFDG_ERR_ARG, "bad scheme");
+    s->cfg.flux = flux;
+    s->cfg.spatial = spatial;
+    s->set_flow();
+    return CFDG_OK;
+}
+
+cfdg_status cfdg_set_flow_conditions(cfdg_solver* s, double M, double P, double T) {
+    if (!s) return fail(CFDG_ERR_ARG, "null solver");
+    double g = s->cfg.gamma;
+    s->M_inf = M;
+    double fT = 1.0 + 0.5 * (g - 1.0) * M * M;
+    double fP = std::pow(fT, g / (g - 1.0));
+    s->T0 = T * fT;
+    s->P0 = P * fP;
+    s->Pexit = P;
+    s->set_flow();
+    return CFDG_OK;
+}
+
+cfdg_status cfdg_set_freestream_static(cfdg_solver* s, double M, double P, double T) {
+    return cfdg_set_flow_conditions(s, M, P, T);
+}
+
+cfdg_status cfdg_set_kinematic_viscosity(cfdg_solver* s, double Re, double Lref) {
+    if (!s || !(Re > 0)) return fail(CFDG_ERR_ARG, "bad Reynolds number");
+    double g = s->cfg.gamma;
+    double fT = 1.0 + 0.5 * (g - 1.0) * s->M_inf * s->M_inf;
+    double Ts = s->T0 / fT;
+    double c = std::sqrt(g * s->cfg.R_gas * Ts);
+    double u = s->M_inf * c;
+    s->nu = (u * Lref) / Re;
+    s->set_flow();
+    return CFDG_OK;
+}
+
+cfdg_status cfdg_get_params(const cfdg_solver* s, double* o) {
+    if (!s || !o) return fail(CFDG_ERR_ARG, "null argument");
+    o[0] = s->M_inf; o[1] = s->P0; o[2] = s->T0; o[3] = s->Pexit; o[4] = s->nu; o[5] = s->cfg.R_gas;
+    return CFDG_OK;
+}
+
+cfdg_status cfdg_initialize(cfdg_solver* s) {
+    if (!s) return fail(CFDG_ERR_ARG, "null solver");
+    double g = s->cfg.gamma, Rg = s->cfg.R_gas;
+    double st4[4];
+    if (s->cfg.init == CFDG_INIT_BUMP) {
+        // src/Solver.cpp:46-65
+        double p = s->Pexit;
+        double fT = std::pow(s->P0 / p, (g - 1.0) / g);
+        double T = s->T0 / fT;
+        double rho = p / (Rg * T);
+        double V = std::sqrt(2.0 * (g * Rg / (g - 1.0)) * (s->T0 - T));
+        st4[0] = rho; st4[1] = rho * V; st4[2] = rho * 0.0;
+        st4[3] = p / (g - 1.0) + 0.5 * rho * (V * V + 0.0 * 0.0);
+    } else {
+        for (int k = 0; k < 4; ++k) st4[k] = s->F.fs[k];
+    }
+    std::vector<double> U(6 * (size_t)s->nc, 0.0);
+    for (int i = 0; i < s->nc; ++i)
+        for (int k = 0; k < 4; ++k) U[6 * (size_t)i + k] = st4[k];
+    return cfdg_set_state(s, U.data());
+}
+
+cfdg_status cfdg_set_state(cfdg_solver* s, const double* U) {
+    if (!s || !U) return fail(CFDG_ERR_ARG, "null argument");
+    TRY(s->upload_aos(U, s->U));
+    CK(cudaStreamSynchronize(s->st));
+    return CFDG_OK;
+}
+
+cfdg_status cfdg_get_state(cfdg_solver* s, double* U) {
+    if (!s || !U) return fail(CFDG_ERR_ARG, "null argument");
+    return s->download_aos(s->U, U, s->nv, 6);
+}
+
+cfdg_status cfdg_residual(cfdg_solver* s, const double* U, double* R, int update_limiters) {
+    if (!s || !R) return fail(CFDG_ERR_ARG, "null argument");
+    double* Uin = s->U;
+    if (U) {
+        TRY(s->upload_aos(U, s->Ub));
+        Uin = s->Ub;
+    }
+    TRY(s->residual_dev(Uin, s->R, update_limiters));
+    return s->download_aos(s->R, R, s->nv, 6);
+}
+
+cfdg_status cfdg_residual_device(cfdg_solver* s, int update_limiters) {
+    if (!s) return fail(CFDG_ERR_ARG, "null solver");
+    return s->residual_dev(s->U, s->R, update_limiters);
+}
+
+cfdg_status cfdg_gradients(cfdg_solver* s, const double* U, double* g10) {
+    if (!s || !g10) return fail(CFDG_ERR_ARG, "null argument");
+    double* Uin = s->U;
+    if (U) {
+        TRY(s->upload_aos(U, s->Ub));
+        Uin = s->Ub;
+    }
+    // the residual's gradient stage (no limiter update) leaves the gradients in G
+    ResArgs<double> a = s->res64(Uin, s->R, 0);
+    launch_residual<double>(a);
+    s->launches += 4;
+    CK(cudaGetLastError());
+    return s->download_aos(s->G, g10, 10, 10);
+}
+
+cfdg_status cfdg_limiters(cfdg_solver* s, const double* U, double* phi) {
+    if (!s || !phi) return fail(CFDG_ERR_ARG, "null argument");
+    double* Uin = s->U;
+    if (U) {
+        TRY(s->upload_aos(U, s->Ub));
+        Uin = s->Ub;
+    }
+    ResArgs<double> a = s->res64(Uin, s->R, 1);
+    launch_residual<double>(a);
+    s->launches += 4;
+    s->limiter_valid = true;
+    CK(cudaGetLastError());
+    return s->download_aos(s->phi, phi, 1, 1);
+}
+
+cfdg_status cfdg_get_limiters(cfdg_solver* s, double* phi) {
+    if (!s || !phi) return fail(CFDG_ERR_ARG, "null argument");
+    return s->download_aos(s->phi, phi, 1, 1);
+}
+
+cfdg_status cfdg_set_limiters(cfdg_solver* s, const double* phi) {
+    if (!s || !phi) return fail(CFDG_ERR_ARG, "null argument");
+    CK(cudaMemcpyAsync(s->stage, phi, sizeof(double) * s->nc, cudaMemcpyHostToDevice, s->st));
+    launch_aos_to_soa<double>(s->nc, 1, 1, s->stage, s->perm, s->phi, s->st);
+    s->launches += 1;
+    CK(cudaGetLastError());
+    CK(cudaStreamSynchronize(s->st));
+    s->limiter_valid = true;
+    return CFDG_OK;
+}
+
+cfdg_status cfdg_local_timestep(cfdg_solver* s, double cfl, double* dt) {
+    if (!s) return fail(CFDG_ERR_ARG, "null solver");
+    launch_prim64(s->nv, s->nc, s->F, s->f64(s->U), s->f64(s->W), s->st);
+    launch_local_dt(s->nv, s->mv, s->F, s->U, s->W, cfl, s->dt, s->st);
+    s->launches += 2;
+    CK(cudaGetLastError());
+    if (dt) return s->download_aos(s->dt, dt, 1, 1);
+    CK(cudaStreamSynchronize(s->st));
+    return CFDG_OK;
+}
+
+cfdg_status cfdg_set_timestep(cfdg_solver* s, const double* dt) {
+    if (!s || !dt) return fail(CFDG_ERR_ARG, "null argument");
+    CK(cudaMemcpyAsync(s->stage, dt, sizeof(double) * s->nc, cudaMemcpyHostToDevice, s->st));
+    launch_aos_to_soa<double>(s->nc, 1, 1, s->stage, s->perm, s->dt, s->st);
+    s->launches += 1;
+    CK(cudaGetLastError());
+    CK(cudaStreamSynchronize(s->st));
+    return CFDG_OK;
+}
+
+cfdg_status cfdg_preconditioner(cfdg_solver* s, double* D) {
+    if (!s || !D) return fail(CFDG_ERR_ARG, "null argument");
+    launch_prim64(s->nv, s->nc, s->F, s->f64(s->U), s->f64(s->W), s->st);
+    launch_precond(s->nv, s->mv, s->F, s->U, s->W, s->dt, s->D, s->st);
+    s->launches += 2;
+    CK(cudaGetLastError());
+    return s->download_aos(s->D, D, 1, 1);
+}
+
+cfdg_status cfdg_jv(cfdg_solver* s, const double* Ubase, const double* Rbase, const double* v, double* Jv, int mode) {
+    if (!s || !Ubase || !v || !Jv || (mode == CFDG_JV_FD && !Rbase) || mode < 0 || mode > 1)
+        return fail(CFDG_ERR_ARG, "cfdg_jv: bad arguments");
+    TRY(s->upload_aos(Ubase, s->Ub));
+    if (Rbase) TRY(s->upload_aos(Rbase, s->Rb));
+    TRY(s->upload_aos(v, s->vtmp));
+    TRY(s->jv64(s->Ub, s->Rb, s->vtmp, s->x, mode, false));
+    return s->download_aos(s->x, Jv, s->nv, 6);
+}
+
+cfdg_status cfdg_gmres(cfdg_solver* s, const double* Ubase, const double* Rbase, const double* rhs, double* x,
+                       int* iters) {
+    if (!s || !rhs || !x) return fail(CFDG_ERR_ARG, "cfdg_gmres: bad arguments");
+    double* Ud = s->U;
+    if (Ubase) {
+        TRY(s->upload_aos(Ubase, s->Ub));
+        Ud = s->Ub;
+    }
+    double* Rd = s->R;
+    if (Rbase) {
+        TRY(s->upload_aos(Rbase, s->Rb));
+        Rd = s->Rb;
+    }
+    TRY(s->upload_aos(rhs, s->rhs));
+    int it = 0;
+    TRY(s->gmres(Ud, Rd, s->rhs, s->x, &it));
+    if (iters) *iters = it;
+    return s->download_aos(s->x, x, s->nv, 6);
+}
+
+cfdg_status cfdg_norm_vm(cfdg_solver* s, const double* R, double* out) {
+    if (!s || !R || !out) return fail(CFDG_ERR_ARG, "null argument");
+    TRY(s->upload_aos(R, s->vtmp));
+    launch_norm_vm(s->nv, s->nc, s->vtmp, s->g64.vol, s->rs, s->scal + 8, s->st);
+    s->launches += 1;
+    double v[3];
+    TRY(s->read_scalars(8, 3, v));
+    *out = v[1] == 0 ? 0.0 : std::sqrt(v[0] / v[1]);
+    return CFDG_OK;
+}
+
+cfdg_status cfdg_reset_newton(cfdg_solver* s) {
+    if (!s) return fail(CFDG_ERR_ARG, "null solver");
+    s->cfl = s->cfg.cfl0;
+    s->step = 0;
+    return CFDG_OK;
+}
+
+cfdg_status cfdg_newton_step(cfdg_solver* s, double tol, cfdg_step* info, int* converged) {
+    if (!s) return fail(CFDG_ERR_ARG, "null solver");
+    int cv = 0;
+    cfdg_status st = s->newton_step(tol, info, &cv);
+    if (converged) *converged = cv;
+    return st;
+}
+
+cfdg_status cfdg_solve_implicit(cfdg_solver* s, double tol, int max_steps, cfdg_step* trace, int* n_steps) {
+    if (!s || max_steps < 0) return fail(CFDG_ERR_ARG, "bad arguments");
+    TRY(cfdg_reset_newton(s));
+    int n = 0;
+    for (int k = 0; k < max_steps; ++k) {
+        cfdg_step rec;
+        int cv = 0;
+        cfdg_status st = s->newton_step(tol, &rec, &cv);
+        if (trace) trace[n] = rec;
+        ++n;
+        if (n_steps) *n_steps = n;
+        if (st != CFDG_OK) return st;
+        if (cv) return CFDG_OK;
+    }
+    if (n_steps) *n_steps = n;
+    return fail(CFDG_ERR_NOT_CONVERGED, "solveImplicit reached max_steps above the tolerance");
+}
+
+cfdg_status cfdg_vjp(cfdg_solver* s, const double*, const double*, double*) {
+    if (!s) return fail(CFDG_ERR_ARG, "null solver");
+    return fail(CFDG_ERR_UNSUPPORTED, "the adjoint kernel is not built into this library yet");
+}
+
+cfdg_status cfdg_wall_coefficients(cfdg_solver* s, int, double*, double*, double*, int*) {
+    if (!s) return fail(CFDG_ERR_ARG, "null solver");
+    return fail(CFDG_ERR_UNSUPPORTED, "wall coefficients are not built into this library yet");
+}
+
+cfdg_status cfdg_drag(cfdg_solver* s, double*) {
+    if (!s) return fail(CFDG_ERR_ARG, "null solver");
+    return fail(CFDG_ERR_UNSUPPORTED, "drag is not built into this library yet");
+}
+
+cfdg_status cfdg_entropy_error(cfdg_solver* s, double*) {
+    if (!s) return fail(CFDG_ERR_ARG, "null solver");
+    return fail(CFDG_ERR_UNSUPPORTED, "entropy error is not built into this library yet");
+}
+
+cfdg_status cfdg_synchronize(cfdg_solver* s) {
+    if (!s) return fail(CFDG_ERR_ARG, "null solver");
+    CK(cudaStreamSynchronize(s->st));
+    return CFDG_OK;
+}
+
+cfdg_status cfdg_set_timing(cfdg_solver* s, int on) {
+    if (!s) return fail(CFDG_ERR_ARG, "null solver");
+    s->timing = on;
+    return CFDG_OK;
+}
+
+cfdg_status cfdg_kernel_times(cfdg_solver* s, double* a, double* b, double* c, double* d) {
+    if (!s) return fail(CFDG_ERR_ARG, "null solver");
+    if (a) *a = s->kms[0];
+    if (b) *b = s->kms[1];
+    if (c) *c = s->kms[2];
+    if (d) *d = s->kms[3];
+    return CFDG_OK;
+}
+
+cfdg_status cfdg_launch_count(cfdg_solver* s, long long* n) {
+    if (!s || !n) return fail(CFDG_ERR_ARG, "null argument");
+    *n = s->launches;
+    return CFDG_OK;
+}
+
+}  // extern "C"

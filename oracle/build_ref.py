@@ -1,0 +1,147 @@
+"""Build the reference solver as shared-library oracles: oracle/_ref/libref_<variant>.so.
+
+Test infrastructure only.  The reference (AmberMond/mycode) selects its boundary
+condition set, initial condition and the viscous term by commenting whole function
+bodies in and out of src/Solver.cpp (see the variants at src/Solver.cpp:806-863,
+:973-1011, :1088-1139 and the initialisers at :46-65, :905-920; the viscous toggle
+is :787 vs :792).  This script writes one source variant per case into a temporary
+directory OUTSIDE the repository (checking every edited line's text first), compiles
+it with the reference's own flags (``g++ -O2 -std=c++17``, makefile:2) together with
+oracle/ref_harness.cpp, and keeps only the shared objects in oracle/_ref/.
+
+The one edit that is not a variant switch: with the viscous term enabled, a boundary
+face that is not a no-slip wall reads ``mesh.cells[f.neighbor]`` with neighbor = -1
+(src/Solver.cpp:729-730), which is undefined behaviour.  The variants with the viscous
+term replace that index by the owner, which makes the non-orthogonal correction
+vanish (dist2 = 0) on those faces; the CPU restatement and the CUDA kernels define
+the same behaviour.
+
+Usage: python oracle/build_ref.py [--src /root/reference]
+"""
+from __future__ import annotations
+
+import argparse
+import os
+import shutil
+import subprocess
+import sys
+import tempfile
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+OUT = os.path.join(HERE, "_ref")
+
+# (first line, last line) ranges of src/Solver.cpp, 1-based inclusive
+ACTIVE_INIT = (46, 65)
+ACTIVE_BC = (806, 863)
+BC_SUPERSONIC = (973, 1011)
+BC_PLATE = (1088, 1139)
+INIT_FREESTREAM = (905, 920)
+
+VARIANTS = {
+    # name: (bc range to enable or None, init range to enable or None, viscous)
+    "bump": (None, None, False),
+    "bump_visc": (None, None, True),
+    "supersonic": (BC_SUPERSONIC, INIT_FREESTREAM, False),
+    "plate": (BC_PLATE, INIT_FREESTREAM, False),
+    "plate_visc": (BC_PLATE, INIT_FREESTREAM, True),
+}
+
+
+def _expect(lines, no, needle):
+    got = lines[no - 1]
+    if needle not in got:
+        raise SystemExit(f"src/Solver.cpp:{no}: expected {needle!r}, found {got!r}")
+
+
+def _comment(lines, rng):
+    a, b = rng
+    for i in range(a - 1, b):
+        lines[i] = "// " + lines[i]
+
+
+def _uncomment(lines, rng):
+    a, b = rng
+    for i in range(a - 1, b):
+        s = lines[i]
+        k = s.find("//")
+        if k < 0 or s[:k].strip():
+            if s.strip():
+                raise SystemExit(f"src/Solver.cpp:{i + 1}: not a comment line: {s!r}")
+            continue
+        lines[i] = s[:k] + s[k + 2:]
+
+
+def make_variant(src_lines, bc, init, viscous):
+    lines = list(src_lines)
+    _expect(lines, 46, "void Solver::initialize()")
+    _expect(lines, 806, "State Solver::getBoundaryGhostState")
+    _expect(lines, 863, "}")
+    _expect(lines, 787, "// State TotalFlux = FluxEuler - FluxVisc;")
+    _expect(lines, 792, "State TotalFlux = FluxEuler;")
+    _expect(lines, 729, "double dx_LR = mesh.cells[f.neighbor].x_c - mesh.cells[f.owner].x_c;")
+    _expect(lines, 730, "double dy_LR = mesh.cells[f.neighbor].y_c - mesh.cells[f.owner].y_c;")
+    if bc is not None:
+        _expect(lines, bc[0], "State Solver::getBoundaryGhostState")
+        _comment(lines, ACTIVE_BC)
+        _uncomment(lines, bc)
+    if init is not None:
+        _expect(lines, init[0], "void Solver::initialize()")
+        _comment(lines, ACTIVE_INIT)
+        _uncomment(lines, init)
+    if viscous:
+        lines[786] = lines[786].replace("// State TotalFlux", "State TotalFlux")
+        lines[791] = lines[791].replace("State TotalFlux = FluxEuler;", "// State TotalFlux = FluxEuler;")
+        nb = "mesh.cells[f.neighbor >= 0 ? f.neighbor : f.owner]"
+        lines[728] = lines[728].replace("mesh.cells[f.neighbor]", nb)
+        lines[729] = lines[729].replace("mesh.cells[f.neighbor]", nb)
+    return lines
+
+
+def build(src_root: str, jobs: int = 4) -> list[str]:
+    solver = os.path.join(src_root, "src", "Solver.cpp")
+    mesh = os.path.join(src_root, "src", "Mesh.cpp")
+    inc = os.path.join(src_root, "include")
+    if not (os.path.isfile(solver) and os.path.isfile(mesh)):
+        raise FileNotFoundError(f"reference sources not found under {src_root}")
+    with open(solver, "r", newline="") as fh:
+        src_lines = fh.read().split("\n")
+    os.makedirs(OUT, exist_ok=True)
+    tmp = tempfile.mkdtemp(prefix="cfd_ref_")
+    procs, outs = [], []
+    try:
+        for name, (bc, init, visc) in VARIANTS.items():
+            gen = os.path.join(tmp, f"Solver_{name}.cpp")
+            with open(gen, "w", newline="") as fh:
+                fh.write("\n".join(make_variant(src_lines, bc, init, visc)))
+            so = os.path.join(OUT, f"libref_{name}.so")
+            cmd = ["g++", "-O2", "-std=c++17", "-fPIC", "-shared", "-ffp-contract=off",
+                   f"-I{inc}", f'-DREF_SOLVER_CPP="{gen}"', f'-DREF_MESH_CPP="{mesh}"',
+                   os.path.join(HERE, "ref_harness.cpp"), "-o", so]
+            procs.append((name, subprocess.Popen(cmd, stderr=subprocess.PIPE, text=True)))
+            outs.append(so)
+            if len(procs) >= jobs:
+                _wait(procs.pop(0))
+        for p in procs:
+            _wait(p)
+    finally:
+        shutil.rmtree(tmp, ignore_errors=True)
+    return outs
+
+
+def _wait(item):
+    name, p = item
+    _, err = p.communicate()
+    if p.returncode != 0:
+        raise SystemExit(f"building reference variant {name} failed:\n{err}")
+
+
+def main(argv=None):
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--src", default="/root/reference")
+    a = ap.parse_args(argv)
+    for so in build(a.src):
+        print(so)
+
+
+if __name__ == "__main__":
+    sys.exit(main())

@@ -1,0 +1,990 @@
+/* CPU oracle for the residual-and-Newton path — TEST INFRASTRUCTURE ONLY.
+ *
+ * A plain-C restatement of the reference solver's algorithm (AmberMond/mycode,
+ * src/Solver.cpp, src/Mesh.cpp, include/Flux.hpp), written to reproduce the
+ * reference's floating-point operation order so it can be pinned bit-for-bit
+ * against the reference itself (oracle/_ref, built by oracle/build_ref.py).
+ * Only tests/, the smoke check and the benchmark's CPU-baseline leg load it, and
+ * only as the checker; the CUDA library never links or calls it.
+ *
+ * Build with -ffp-contract=off so that no a*b+c is fused (x86-64 g++ -O2 does not
+ * fuse; an aarch64 build would unless told not to).
+ *
+ * Layout: states are AoS, 6 doubles per cell {rho, rhou, rhov, rhoE, rhok, rhow},
+ * cells and faces in the reference's own numbering.
+ *
+ * Parts with no reference counterpart (SST sources) are marked "parity unpinned".
+ */
+#include <math.h>
+#include <stdint.h>
+#include <stdlib.h>
+#include <string.h>
+
+#define NV 6
+
+typedef struct { double r, ru, rv, rE, rk, rw; } st_t;
+
+static inline st_t st(double r, double ru, double rv, double rE, double rk, double rw) {
+    st_t s = {r, ru, rv, rE, rk, rw};
+    return s;
+}
+/* State::operator+, -, *scalar (include/Types.hpp:71-81) */
+static inline st_t st_add(st_t a, st_t b) { return st(a.r + b.r, a.ru + b.ru, a.rv + b.rv, a.rE + b.rE, a.rk + b.rk, a.rw + b.rw); }
+static inline st_t st_sub(st_t a, st_t b) { return st(a.r - b.r, a.ru - b.ru, a.rv - b.rv, a.rE - b.rE, a.rk - b.rk, a.rw - b.rw); }
+static inline st_t st_mul(st_t a, double s) { return st(a.r * s, a.ru * s, a.rv * s, a.rE * s, a.rk * s, a.rw * s); }
+static inline st_t st_load(const double* p) { return st(p[0], p[1], p[2], p[3], p[4], p[5]); }
+static inline void st_store(double* p, st_t s) { p[0] = s.r; p[1] = s.ru; p[2] = s.rv; p[3] = s.rE; p[4] = s.rk; p[5] = s.rw; }
+/* std::max / std::min as libstdc++ defines them: max(a,b) = a<b ? b : a; min(a,b) = b<a ? b : a */
+static inline double smax(double a, double b) { return (a < b) ? b : a; }
+static inline double smin(double a, double b) { return (b < a) ? b : a; }
+
+enum { FLUX_LLF = 0, FLUX_ROE = 1, FLUX_HLLC = 2, FLUX_AUSM = 3 };
+enum { SP_FIRST = 0, SP_CENTRAL = 1, SP_LIMITED = 2 };
+enum { BC_BUMP = 0, BC_SUPERSONIC = 1, BC_PLATE = 2 };
+enum { INIT_BUMP = 0, INIT_FREESTREAM = 1 };
+
+/* ------------------------------------------------------------------ mesh */
+
+typedef struct {
+    int n_nodes, n_cells, n_faces;
+    const double* xy;
+    int* cell_nodes; /* n_cells x 4, -1 pads */
+    /* faces, in creation order (src/Mesh.cpp:107-141) */
+    int *node1, *node2, *owner, *neighbor, *tag;
+    double *nx, *ny, *area, *xm, *ym;
+    double *vol, *xc, *yc;
+} om_mesh;
+
+typedef struct { int64_t key; int val; } hslot;
+
+static uint64_t hmix(uint64_t x) {
+    x ^= x >> 33; x *= 0xff51afd7ed558ccdULL; x ^= x >> 33; x *= 0xc4ceb9fe1a85ec53ULL; x ^= x >> 33;
+    return x;
+}
+
+typedef struct { hslot* s; int64_t mask; } htab;
+
+static void ht_init(htab* h, int64_t n) {
+    int64_t cap = 16;
+    while (cap < 2 * n + 16) cap <<= 1;
+    h->s = (hslot*)malloc(sizeof(hslot) * cap);
+    for (int64_t i = 0; i < cap; ++i) h->s[i].key = -1;
+    h->mask = cap - 1;
+}
+static hslot* ht_find(htab* h, int64_t key) {
+    int64_t i = (int64_t)(hmix((uint64_t)key) & (uint64_t)h->mask);
+    while (h->s[i].key != -1 && h->s[i].key != key) i = (i + 1) & h->mask;
+    return &h->s[i];
+}
+static inline int64_t edge_key(int a, int b) {
+    int lo = a < b ? a : b, hi = a < b ? b : a;
+    return ((int64_t)lo << 32) | (int64_t)(uint32_t)hi;
+}
+
+/* Mesh::buildConnectivity (src/Mesh.cpp:102-143) + Mesh::computeGeometry (:148-201).
+ * cells: n_cells x 4 node ids (0-based, -1 pads triangles); bedges: n x 3 (a, b, tag),
+ * later duplicates overwrite earlier ones as in the std::map of src/Mesh.cpp:72. */
+om_mesh* om_mesh_build(int n_nodes, const double* xy, int n_cells, const int* cells,
+                       int n_bedges, const int* bedges) {
+    om_mesh* m = (om_mesh*)calloc(1, sizeof(om_mesh));
+    m->n_nodes = n_nodes;
+    m->n_cells = n_cells;
+    m->xy = xy;
+    m->cell_nodes = (int*)malloc(sizeof(int) * 4 * (size_t)n_cells);
+    memcpy(m->cell_nodes, cells, sizeof(int) * 4 * (size_t)n_cells);
+    htab bt, et;
+    ht_init(&bt, n_bedges);
+    for (int e = 0; e < n_bedges; ++e) {
+        hslot* s = ht_find(&bt, edge_key(bedges[3 * e], bedges[3 * e + 1]));
+        s->key = edge_key(bedges[3 * e], bedges[3 * e + 1]);
+        s->val = bedges[3 * e + 2];
+    }
+    int cap = 4 * n_cells + 4;
+    m->node1 = (int*)malloc(sizeof(int) * cap);
+    m->node2 = (int*)malloc(sizeof(int) * cap);
+    m->owner = (int*)malloc(sizeof(int) * cap);
+    m->neighbor = (int*)malloc(sizeof(int) * cap);
+    m->tag = (int*)malloc(sizeof(int) * cap);
+    ht_init(&et, cap);
+    int nf = 0;
+    for (int i = 0; i < n_cells; ++i) {
+        const int* c = cells + 4 * i;
+        int n = c[3] >= 0 ? 4 : 3;
+        for (int j = 0; j < n; ++j) {
+            int a = c[j], b = c[(j + 1) % n];
+            int64_t k = edge_key(a, b);
+            hslot* s = ht_find(&et, k);
+            if (s->key == k) {
+                m->neighbor[s->val] = i;
+            } else {
+                s->key = k;
+                s->val = nf;
+                m->node1[nf] = a < b ? a : b;
+                m->node2[nf] = a < b ? b : a;
+                m->owner[nf] = i;
+                m->neighbor[nf] = -1;
+                hslot* bs = ht_find(&bt, k);
+                m->tag[nf] = (bs->key == k) ? bs->val : 0;
+                ++nf;
+            }
+        }
+    }
+    free(bt.s);
+    free(et.s);
+    m->n_faces = nf;
+    m->nx = (double*)malloc(sizeof(double) * nf);
+    m->ny = (double*)malloc(sizeof(double) * nf);
+    m->area = (double*)malloc(sizeof(double) * nf);
+    m->xm = (double*)malloc(sizeof(double) * nf);
+    m->ym = (double*)malloc(sizeof(double) * nf);
+    m->vol = (double*)malloc(sizeof(double) * n_cells);
+    m->xc = (double*)malloc(sizeof(double) * n_cells);
+    m->yc = (double*)malloc(sizeof(double) * n_cells);
+#define X(k) xy[2 * (k)]
+#define Y(k) xy[2 * (k) + 1]
+    for (int i = 0; i < n_cells; ++i) {
+        const int* c = cells + 4 * i;
+        if (c[3] < 0) {
+            double x1 = X(c[0]), y1 = Y(c[0]), x2 = X(c[1]), y2 = Y(c[1]), x3 = X(c[2]), y3 = Y(c[2]);
+            m->vol[i] = 0.5 * fabs((x2 - x1) * (y3 - y1) - (x3 - x1) * (y2 - y1));
+            m->xc[i] = (x1 + x2 + x3) / 3.0;
+            m->yc[i] = (y1 + y2 + y3) / 3.0;
+        } else {
+            double sx = 0, sy = 0, a = 0.0;
+            for (int k = 0; k < 4; ++k) { sx += X(c[k]); sy += Y(c[k]); }
+            m->xc[i] = sx / 4.0;
+            m->yc[i] = sy / 4.0;
+            for (int k = 0; k < 4; ++k) {
+                int n1 = c[k], n2 = c[(k + 1) % 4];
+                a += (X(n1) * Y(n2) - X(n2) * Y(n1));
+            }
+            m->vol[i] = 0.5 * fabs(a);
+        }
+    }
+    for (int f = 0; f < nf; ++f) {
+        double dx = X(m->node2[f]) - X(m->node1[f]);
+        double dy = Y(m->node2[f]) - Y(m->node1[f]);
+        double A = sqrt(dx * dx + dy * dy);
+        m->area[f] = A;
+        m->xm[f] = 0.5 * (X(m->node1[f]) + X(m->node2[f]));
+        m->ym[f] = 0.5 * (Y(m->node1[f]) + Y(m->node2[f]));
+        double nx = dy / A, ny = -dx / A;
+        double vx = m->xm[f] - m->xc[m->owner[f]];
+        double vy = m->ym[f] - m->yc[m->owner[f]];
+        if (vx * nx + vy * ny < 0) { nx = -nx; ny = -ny; }
+        m->nx[f] = nx;
+        m->ny[f] = ny;
+    }
+#undef X
+#undef Y
+    return m;
+}
+
+void om_mesh_free(om_mesh* m) {
+    if (!m) return;
+    free(m->cell_nodes); free(m->node1); free(m->node2); free(m->owner); free(m->neighbor); free(m->tag);
+    free(m->nx); free(m->ny); free(m->area); free(m->xm); free(m->ym);
+    free(m->vol); free(m->xc); free(m->yc);
+    free(m);
+}
+
+int om_mesh_n_cells(const om_mesh* m) { return m->n_cells; }
+int om_mesh_n_faces(const om_mesh* m) { return m->n_faces; }
+
+void om_mesh_faces(const om_mesh* m, int* ints5, double* dbl5) {
+    for (int f = 0; f < m->n_faces; ++f) {
+        ints5[5 * f] = m->node1[f]; ints5[5 * f + 1] = m->node2[f];
+        ints5[5 * f + 2] = m->owner[f]; ints5[5 * f + 3] = m->neighbor[f]; ints5[5 * f + 4] = m->tag[f];
+        dbl5[5 * f] = m->nx[f]; dbl5[5 * f + 1] = m->ny[f]; dbl5[5 * f + 2] = m->area[f];
+        dbl5[5 * f + 3] = m->xm[f]; dbl5[5 * f + 4] = m->ym[f];
+    }
+}
+
+void om_mesh_cells(const om_mesh* m, double* vol_xc_yc) {
+    for (int c = 0; c < m->n_cells; ++c) {
+        vol_xc_yc[3 * c] = m->vol[c]; vol_xc_yc[3 * c + 1] = m->xc[c]; vol_xc_yc[3 * c + 2] = m->yc[c];
+    }
+}
+
+/* ------------------------------------------------------------------ flux library */
+
+static const double G = 1.4; /* include/Flux.hpp:9 */
+
+/* getPressure, getSoundSpeed, computeNormalFlux (include/Flux.hpp:12-34) */
+static inline double pressure(st_t U) {
+    double V2 = (U.ru * U.ru + U.rv * U.rv) / (U.r * U.r);
+    return (G - 1.0) * (U.rE - 0.5 * U.r * V2);
+}
+static inline st_t normal_flux(st_t U, double nx, double ny) {
+    double p = pressure(U);
+    double u = U.ru / U.r, v = U.rv / U.r;
+    double un = u * nx + v * ny;
+    return st(U.r * un, U.ru * un + p * nx, U.rv * un + p * ny, (U.rE + p) * un, 0, 0);
+}
+
+/* computeFluxHLLC (include/Flux.hpp:36-76) */
+static st_t flux_hllc(st_t L, st_t R, double nx, double ny) {
+    double pL = pressure(L), pR = pressure(R);
+    double uL = L.ru / L.r, uR = R.ru / R.r;
+    double vL = L.rv / L.r, vR = R.rv / R.r;
+    double unL = uL * nx + vL * ny, unR = uR * nx + vR * ny;
+    double cL = sqrt(G * pL / L.r), cR = sqrt(G * pR / R.r);
+    double hL = (L.rE + pL) / L.r, hR = (R.rE + pR) / R.r;
+    double sL = sqrt(L.r), sR = sqrt(R.r);
+    double ut = (sL * uL + sR * uR) / (sL + sR);
+    double vt = (sL * vL + sR * vR) / (sL + sR);
+    double ht = (sL * hL + sR * hR) / (sL + sR);
+    double unt = ut * nx + vt * ny;
+    double ct = sqrt((G - 1.0) * (ht - 0.5 * (ut * ut + vt * vt)));
+    double SL = smin(unL - cL, unt - ct);
+    double SR = smax(unR + cR, unt + ct);
+    double Ss = (pR - pL + L.r * unL * (SL - unL) - R.r * unR * (SR - unR)) /
+                (L.r * (SL - unL) - R.r * (SR - unR));
+    if (SL >= 0.0) return normal_flux(L, nx, ny);
+    if (SR <= 0.0) return normal_flux(R, nx, ny);
+    if (Ss >= 0.0) {
+        double coef = L.r * (SL - unL) / (SL - Ss);
+        st_t Us = st(coef, coef * (uL + (Ss - unL) * nx), coef * (vL + (Ss - unL) * ny),
+                     coef * (L.rE / L.r + (Ss - unL) * (Ss + pL / (L.r * (SL - unL)))), 0, 0);
+        return st_add(normal_flux(L, nx, ny), st_mul(st_sub(Us, L), SL));
+    } else {
+        double coef = R.r * (SR - unR) / (SR - Ss);
+        st_t Us = st(coef, coef * (uR + (Ss - unR) * nx), coef * (vR + (Ss - unR) * ny),
+                     coef * (R.rE / R.r + (Ss - unR) * (Ss + pR / (R.r * (SR - unR)))), 0, 0);
+        return st_add(normal_flux(R, nx, ny), st_mul(st_sub(Us, R), SR));
+    }
+}
+
+/* computeFluxLLF (include/Flux.hpp:81-108) */
+static st_t flux_llf(st_t L, st_t R, double nx, double ny) {
+    st_t FL = normal_flux(L, nx, ny), FR = normal_flux(R, nx, ny);
+    double pL = pressure(L);
+    double uL = L.ru / L.r, vL = L.rv / L.r;
+    double unL = uL * nx + vL * ny;
+    double cL = sqrt(G * pL / L.r);
+    double pR = pressure(R);
+    double uR = R.ru / R.r, vR = R.rv / R.r;
+    double unR = uR * nx + vR * ny;
+    double cR = sqrt(G * pR / R.r);
+    double a = smax(fabs(unL) + cL, fabs(unR) + cR);
+    st_t D = st_mul(st_sub(R, L), 0.5 * a);
+    st_t A = st_mul(st_add(FL, FR), 0.5);
+    return st_sub(A, D);
+}
+
+/* computeFluxROE with Harten's entropy fix (include/Flux.hpp:112-213) */
+static st_t flux_roe(st_t L, st_t R, double nx, double ny) {
+    double pL = pressure(L);
+    double uL = L.ru / L.r, vL = L.rv / L.r;
+    double hL = (L.rE + pL) / L.r;
+    double pR = pressure(R);
+    double uR = R.ru / R.r, vR = R.rv / R.r;
+    double hR = (R.rE + pR) / R.r;
+    double sL = sqrt(L.r), sR = sqrt(R.r);
+    double inv = 1.0 / (sL + sR);
+    double ut = (sL * uL + sR * uR) * inv;
+    double vt = (sL * vL + sR * vR) * inv;
+    double ht = (sL * hL + sR * hR) * inv;
+    double V2 = ut * ut + vt * vt;
+    double c2 = (G - 1.0) * (ht - 0.5 * V2);
+    double ct = sqrt(smax(c2, 1e-8));
+    double unt = ut * nx + vt * ny;
+    double utt = -ut * ny + vt * nx;
+    double lam[4] = {unt - ct, unt, unt, unt + ct};
+    double eps = 0.1 * ct;
+    for (int i = 0; i < 4; ++i) {
+        if (fabs(lam[i]) < eps) lam[i] = 0.5 * (lam[i] * lam[i] / eps + eps);
+        lam[i] = fabs(lam[i]);
+    }
+    double dr = R.r - L.r, du = uR - uL, dv = vR - vL, dp = pR - pL;
+    double dun = du * nx + dv * ny;
+    double dut = -du * ny + dv * nx;
+    double rt = sL * sR;
+    double al0 = 0.5 / c2 * (dp - rt * ct * dun);
+    double al1 = dr - dp / c2;
+    double al2 = rt * dut;
+    double al3 = 0.5 / c2 * (dp + rt * ct * dun);
+    double w1 = lam[0] * al0, w2 = lam[1] * al1, w3 = lam[2] * al2, w4 = lam[3] * al3;
+    st_t D;
+    D.r = w1 * 1.0 + w2 * 1.0 + w3 * 0.0 + w4 * 1.0;
+    D.ru = w1 * (ut - ct * nx) + w2 * ut + w3 * (-ny) + w4 * (ut + ct * nx);
+    D.rv = w1 * (vt - ct * ny) + w2 * vt + w3 * nx + w4 * (vt + ct * ny);
+    D.rE = w1 * (ht - unt * ct) + w2 * (0.5 * V2) + w3 * utt + w4 * (ht + unt * ct);
+    D.rk = fabs(unt) * (R.rk / R.r - L.rk / L.r) * rt;
+    D.rw = fabs(unt) * (R.rw / R.r - L.rw / L.r) * rt;
+    st_t FL = normal_flux(L, nx, ny), FR = normal_flux(R, nx, ny);
+    return st_sub(st_mul(st_add(FL, FR), 0.5), st_mul(D, 0.5));
+}
+
+/* computeInviscidFlux (include/Flux.hpp:216-227); AUSM falls to LLF */
+static st_t inviscid_flux(st_t L, st_t R, double nx, double ny, int scheme) {
+    switch (scheme) {
+        case FLUX_ROE: return flux_roe(L, R, nx, ny);
+        case FLUX_HLLC: return flux_hllc(L, R, nx, ny);
+        default: return flux_llf(L, R, nx, ny);
+    }
+}
+
+/* ------------------------------------------------------------------ solver */
+
+typedef struct {
+    const om_mesh* m;
+    int flux, spatial, bcset, viscous, init_mode;
+    double gamma, R_gas, Pr, nu;
+    double M_inf, P0, T0, Pexit;
+    double* grad; /* 10 per cell: rho, u, v, p, T gradients, (x, y) pairs */
+    double* phi;  /* limiter per cell */
+    double* dt;   /* local time step */
+    double* U;    /* current state, 6 per cell */
+    double* pc;   /* scratch */
+    double* pmax;
+    double* pmin;
+    int gmres_m;
+    double gmres_tol;
+} om_solver;
+
+enum { GR_RHO = 0, GR_U = 2, GR_V = 4, GR_P = 6, GR_T = 8 };
+
+om_solver* om_solver_create(const om_mesh* m) {
+    om_solver* s = (om_solver*)calloc(1, sizeof(om_solver));
+    s->m = m;
+    s->flux = FLUX_HLLC;      /* include/Solver.hpp:33-34 defaults */
+    s->spatial = SP_LIMITED;
+    s->bcset = BC_BUMP;
+    s->init_mode = INIT_BUMP;
+    s->gamma = 1.4;           /* include/Solver.hpp:91-92 */
+    s->R_gas = 287.0;
+    s->Pr = 0.72;             /* src/Solver.cpp:541 */
+    s->nu = 0.01;             /* include/Solver.hpp:42 */
+    s->gmres_m = 40;          /* src/Solver.cpp:1479 */
+    s->gmres_tol = 1e-2;      /* src/Solver.cpp:1587 */
+    int n = m->n_cells;
+    s->grad = (double*)calloc((size_t)10 * n, sizeof(double));
+    s->phi = (double*)malloc(sizeof(double) * n);
+    for (int i = 0; i < n; ++i) s->phi[i] = 1.0;
+    s->dt = (double*)calloc(n, sizeof(double));
+    s->U = (double*)calloc((size_t)NV * n, sizeof(double));
+    s->pc = (double*)malloc(sizeof(double) * n);
+    s->pmax = (double*)malloc(sizeof(double) * n);
+    s->pmin = (double*)malloc(sizeof(double) * n);
+    return s;
+}
+
+void om_solver_free(om_solver* s) {
+    if (!s) return;
+    free(s->grad); free(s->phi); free(s->dt); free(s->U); free(s->pc); free(s->pmax); free(s->pmin);
+    free(s);
+}
+
+void om_set_method(om_solver* s, int flux, int spatial) { s->flux = flux; s->spatial = spatial; }
+void om_set_case(om_solver* s, int bcset, int viscous, int init_mode) {
+    s->bcset = bcset; s->viscous = viscous; s->init_mode = init_mode;
+}
+void om_set_gmres(om_solver* s, int m, double tol) { s->gmres_m = m; s->gmres_tol = tol; }
+void om_set_nu(om_solver* s, double nu) { s->nu = nu; }
+
+/* setFlowConditions (src/Solver.cpp:12-32) */
+void om_set_flow_conditions(om_solver* s, double M, double P, double T) {
+    s->M_inf = M;
+    double fT = 1.0 + 0.5 * (s->gamma - 1.0) * M * M;
+    double fP = pow(fT, s->gamma / (s->gamma - 1.0));
+    s->T0 = T * fT;
+    s->P0 = P * fP;
+    s->Pexit = P;
+}
+/* setFreestreamStatic (src/Solver.cpp:2017-2025): same arithmetic */
+void om_set_freestream_static(om_solver* s, double M, double P, double T) { om_set_flow_conditions(s, M, P, T); }
+
+/* setKinematicViscosity (src/Solver.cpp:34-43) */
+void om_set_kinematic_viscosity(om_solver* s, double Re, double L) {
+    double fT = 1.0 + 0.5 * (s->gamma - 1.0) * s->M_inf * s->M_inf;
+    double Ts = s->T0 / fT;
+    double c = sqrt(s->gamma * s->R_gas * Ts);
+    double u = s->M_inf * c;
+    s->nu = (u * L) / Re;
+}
+
+void om_get_params(const om_solver* s, double* out6) {
+    out6[0] = s->M_inf; out6[1] = s->P0; out6[2] = s->T0; out6[3] = s->Pexit; out6[4] = s->nu; out6[5] = s->R_gas;
+}
+
+/* primitiveToConservative (src/Solver.cpp:498-501) */
+static inline st_t p2c(const om_solver* s, double r, double u, double v, double p, double k, double w) {
+    double rE = p / (s->gamma - 1.0) + 0.5 * r * (u * u + v * v);
+    return st(r, r * u, r * v, rE, r * k, r * w);
+}
+
+/* free-stream state used by the frozen inflow / far-field tags (src/Solver.cpp:979-985, :1094-1100)
+ * and by the free-stream initialiser (:905-920) */
+static st_t freestream(const om_solver* s) {
+    double g = s->gamma, M = s->M_inf;
+    double fT = 1.0 + 0.5 * (g - 1.0) * M * M;
+    double Ts = s->T0 / fT;
+    double rho = s->Pexit / (s->R_gas * Ts);
+    double c = sqrt(g * s->R_gas * Ts);
+    double u = M * c;
+    return p2c(s, rho, u, 0.0, s->Pexit, 0.0, 0.0);
+}
+
+static st_t slip_ghost(st_t U, double nx, double ny) {
+    double u = U.ru / U.r, v = U.rv / U.r;
+    double vn = u * nx + v * ny;
+    double ug = u - 2.0 * vn * nx, vg = v - 2.0 * vn * ny;
+    st_t g = U;
+    g.r = U.r; g.ru = U.r * ug; g.rv = U.r * vg; g.rE = U.rE;
+    return g;
+}
+
+/* getBoundaryGhostState: the bump set (src/Solver.cpp:806-863), the supersonic set
+ * (:973-1011) and the laminar-plate / SWBLI set (:1088-1139) */
+static st_t ghost(const om_solver* s, st_t U, int f) {
+    const om_mesh* m = s->m;
+    int tag = m->tag[f];
+    double nx = m->nx[f], ny = m->ny[f];
+    double g = s->gamma;
+    if (s->bcset == BC_BUMP) {
+        if (tag == 1) {
+            double pin = pressure(U);
+            double pu = smin(pin, s->P0 - 1e-4);
+            double Tg = s->T0 * pow(pu / s->P0, (g - 1.0) / g);
+            double rg = pu / (s->R_gas * Tg);
+            double Cp = g * s->R_gas / (g - 1.0);
+            double V2 = 2.0 * Cp * (s->T0 - Tg);
+            double V = (V2 > 0) ? sqrt(V2) : 0.0;
+            return p2c(s, rg, V, 0.0, pu, 0.0, 0.0);
+        } else if (tag == 2) {
+            double r = U.r, u = U.ru / U.r, v = U.rv / U.r;
+            return p2c(s, r, u, v, s->Pexit, 0.0, 0.0);
+        } else if (tag == 3) {
+            return slip_ghost(U, nx, ny);
+        }
+        return U;
+    } else if (s->bcset == BC_SUPERSONIC) {
+        if (tag == 1) return freestream(s);
+        if (tag == 2) return U;
+        if (tag == 3) return slip_ghost(U, nx, ny);
+        return U;
+    } else {
+        if (tag == 1 || tag == 5) return freestream(s);
+        if (tag == 2) return U;
+        if (tag == 3) return slip_ghost(U, nx, ny);
+        if (tag == 4) {
+            double ug = -(U.ru / U.r), vg = -(U.rv / U.r);
+            double ek = 0.5 * (U.ru * U.ru + U.rv * U.rv) / U.r;
+            double pin = (g - 1.0) * (U.rE - ek);
+            double Tin = pin / (U.r * s->R_gas);
+            double Tg = Tin;
+            double rg = pin / (s->R_gas * Tg);
+            return p2c(s, rg, ug, vg, pin, 0.0, 0.0);
+        }
+        return U;
+    }
+}
+
+/* initialize: the bump variant (src/Solver.cpp:46-65) or free stream (:905-920) */
+void om_initialize(om_solver* s) {
+    st_t init;
+    if (s->init_mode == INIT_BUMP) {
+        double g = s->gamma, p = s->Pexit;
+        double fT = pow(s->P0 / p, (g - 1.0) / g);
+        double T = s->T0 / fT;
+        double rho = p / (s->R_gas * T);
+        double V = sqrt(2.0 * (g * s->R_gas / (g - 1.0)) * (s->T0 - T));
+        init = p2c(s, rho, V, 0.0, p, 0.0, 0.0);
+    } else {
+        init = freestream(s);
+    }
+    for (int i = 0; i < s->m->n_cells; ++i) st_store(s->U + NV * i, init);
+}
+
+void om_set_state(om_solver* s, const double* U) { memcpy(s->U, U, sizeof(double) * NV * s->m->n_cells); }
+void om_get_state(const om_solver* s, double* U) { memcpy(U, s->U, sizeof(double) * NV * s->m->n_cells); }
+
+/* computeGradients (src/Solver.cpp:81-149) */
+void om_gradients(om_solver* s, const double* Uin) {
+    const om_mesh* m = s->m;
+    int n = m->n_cells;
+    double R = s->R_gas;
+    memset(s->grad, 0, sizeof(double) * 10 * (size_t)n);
+    for (int f = 0; f < m->n_faces; ++f) {
+        int o = m->owner[f], nb = m->neighbor[f];
+        st_t L = st_load(Uin + NV * o);
+        st_t Rs = nb >= 0 ? st_load(Uin + NV * nb) : ghost(s, L, f);
+        double uL = L.ru / L.r, vL = L.rv / L.r, pL = pressure(L), TL = pL / (L.r * R);
+        double uR = Rs.ru / Rs.r, vR = Rs.rv / Rs.r, pR = pressure(Rs), TR = pR / (Rs.r * R);
+        double ph[5];
+        ph[0] = 0.5 * (L.r + Rs.r);
+        ph[1] = 0.5 * (uL + uR);
+        ph[2] = 0.5 * (vL + vR);
+        ph[3] = 0.5 * (pL + pR);
+        ph[4] = 0.5 * (TL + TR);
+        double nx = m->nx[f], ny = m->ny[f], A = m->area[f];
+        double* go = s->grad + 10 * o;
+        for (int q = 0; q < 5; ++q) {
+            go[2 * q] += ph[q] * nx * A;
+            go[2 * q + 1] += ph[q] * ny * A;
+        }
+        if (nb >= 0) {
+            double* gn = s->grad + 10 * nb;
+            for (int q = 0; q < 5; ++q) {
+                gn[2 * q] -= ph[q] * nx * A;
+                gn[2 * q + 1] -= ph[q] * ny * A;
+            }
+        }
+    }
+    for (int i = 0; i < n; ++i) {
+        double v = m->vol[i];
+        for (int q = 0; q < 10; ++q) s->grad[10 * i + q] /= v;
+    }
+}
+
+/* computeLimiters: Barth-Jespersen on pressure reconstructed through T
+ * (src/Solver.cpp:152-253) */
+void om_limiters(om_solver* s, const double* Uin) {
+    const om_mesh* m = s->m;
+    int n = m->n_cells;
+    double R = s->R_gas;
+    for (int i = 0; i < n; ++i) {
+        s->phi[i] = 1.0;
+        s->pc[i] = pressure(st_load(Uin + NV * i));
+        s->pmax[i] = s->pc[i];
+        s->pmin[i] = s->pc[i];
+    }
+    for (int f = 0; f < m->n_faces; ++f) {
+        int o = m->owner[f], nb = m->neighbor[f];
+        double pg = 0.0;
+        if (nb >= 0) pg = s->pc[nb];
+        else pg = pressure(ghost(s, st_load(Uin + NV * o), f));
+        s->pmax[o] = smax(s->pmax[o], pg);
+        s->pmin[o] = smin(s->pmin[o], pg);
+        if (nb >= 0) {
+            s->pmax[nb] = smax(s->pmax[nb], s->pc[o]);
+            s->pmin[nb] = smin(s->pmin[nb], s->pc[o]);
+        }
+    }
+    const double eps = 1e-12;
+    for (int f = 0; f < m->n_faces; ++f) {
+        int o = m->owner[f], nb = m->neighbor[f];
+        for (int side = 0; side < 2; ++side) {
+            int c = side == 0 ? o : nb;
+            if (c < 0) break;
+            double dx = m->xm[f] - m->xc[c], dy = m->ym[f] - m->yc[c];
+            const double* g = s->grad + 10 * c;
+            double rho = Uin[NV * c];
+            double Tc = s->pc[c] / (rho * R);
+            double Tf = Tc + 1.0 * (g[GR_T] * dx + g[GR_T + 1] * dy);
+            double Pf = rho * R * Tf;
+            double d2 = Pf - s->pc[c];
+            double a = 1.0;
+            if (d2 > 0.0) {
+                a = (s->pmax[c] - s->pc[c]) / (d2 + eps);
+                a = smin(1.0, a);
+            } else if (d2 < 0.0) {
+                a = (s->pmin[c] - s->pc[c]) / (d2 - eps);
+                a = smin(1.0, a);
+            }
+            s->phi[c] = smin(s->phi[c], a);
+        }
+    }
+}
+
+void om_get_gradients(const om_solver* s, double* G10) { memcpy(G10, s->grad, sizeof(double) * 10 * s->m->n_cells); }
+void om_get_limiters(const om_solver* s, double* phi) { memcpy(phi, s->phi, sizeof(double) * s->m->n_cells); }
+void om_set_limiters(om_solver* s, const double* phi) { memcpy(s->phi, phi, sizeof(double) * s->m->n_cells); }
+
+/* computeResiduals (src/Solver.cpp:529-801); the viscous flux is subtracted when
+ * s->viscous is set (the reference's commented line :787 instead of :792) */
+void om_residual(om_solver* s, const double* Uin, double* Rout, int update_limiters) {
+    const om_mesh* m = s->m;
+    int n = m->n_cells;
+    double g = s->gamma, R = s->R_gas;
+    memset(Rout, 0, sizeof(double) * NV * (size_t)n);
+    om_gradients(s, Uin);
+    if (s->spatial == SP_LIMITED && update_limiters) om_limiters(s, Uin);
+    double Cp = g * R / (g - 1.0);
+    double Pr = s->Pr;
+    for (int f = 0; f < m->n_faces; ++f) {
+        int o = m->owner[f], nb = m->neighbor[f];
+        double nx = m->nx[f], ny = m->ny[f];
+        st_t L = st_load(Uin + NV * o);
+        st_t Rs = nb >= 0 ? st_load(Uin + NV * nb) : ghost(s, L, f);
+        st_t Lr, Rr;
+        if (s->spatial == SP_FIRST || nb < 0) {
+            Lr = L;
+            Rr = Rs;
+        } else {
+            double dxL = m->xm[f] - m->xc[o], dyL = m->ym[f] - m->yc[o];
+            double dxR = m->xm[f] - m->xc[nb], dyR = m->ym[f] - m->yc[nb];
+            const double* gL = s->grad + 10 * o;
+            const double* gR = s->grad + 10 * nb;
+            double phL = s->spatial == SP_LIMITED ? s->phi[o] : 0.5;
+            double phR = s->spatial == SP_LIMITED ? s->phi[nb] : 0.5;
+            double uL = L.ru / L.r, vL = L.rv / L.r;
+            double pL = pressure(L);
+            double rLf = L.r + phL * (gL[GR_RHO] * dxL + gL[GR_RHO + 1] * dyL);
+            double pLf = pL + phL * (gL[GR_P] * dxL + gL[GR_P + 1] * dyL);
+            double uLf = uL + phL * (gL[GR_U] * dxL + gL[GR_U + 1] * dyL);
+            double vLf = vL + phL * (gL[GR_V] * dxL + gL[GR_V + 1] * dyL);
+            if (rLf < 1e-4) rLf = L.r;
+            if (pLf < 1e-4) pLf = pL;
+            Lr = p2c(s, rLf, uLf, vLf, pLf, 0.0, 0.0);
+            double uR = Rs.ru / Rs.r, vR = Rs.rv / Rs.r;
+            double pR = pressure(Rs);
+            double rRf = Rs.r + phR * (gR[GR_RHO] * dxR + gR[GR_RHO + 1] * dyR);
+            double pRf = pR + phR * (gR[GR_P] * dxR + gR[GR_P + 1] * dyR);
+            double uRf = uR + phR * (gR[GR_U] * dxR + gR[GR_U + 1] * dyR);
+            double vRf = vR + phR * (gR[GR_V] * dxR + gR[GR_V + 1] * dyR);
+            if (rRf < 1e-4) rRf = Rs.r;
+            if (pRf < 1e-4) pRf = pR;
+            Rr = p2c(s, rRf, uRf, vRf, pRf, 0.0, 0.0);
+        }
+        st_t FE;
+        if (nb < 0 && (m->tag[f] == 3 || m->tag[f] == 4)) {
+            double pw = pressure(Lr);
+            FE = st(0.0, pw * nx, pw * ny, 0.0, 0.0, 0.0);
+        } else {
+            FE = inviscid_flux(Lr, Rr, nx, ny, s->flux);
+        }
+        st_t TF = FE;
+        if (s->viscous) {
+            double rf = 0.5 * (L.r + Rs.r);
+            double uf = 0.5 * (L.ru / L.r + Rs.ru / Rs.r);
+            double vf = 0.5 * (L.rv / L.r + Rs.rv / Rs.r);
+            const double* gL = s->grad + 10 * o;
+            const double* gR = nb >= 0 ? s->grad + 10 * nb : gL;
+            double dudx, dudy, dvdx, dvdy, dTdx, dTdy;
+            if (nb < 0 && m->tag[f] == 4) {
+                double dx = m->xm[f] - m->xc[o], dy = m->ym[f] - m->yc[o];
+                double d2 = dx * dx + dy * dy;
+                double uc = L.ru / L.r, vc = L.rv / L.r;
+                dudx = -uc * dx / d2;
+                dudy = -uc * dy / d2;
+                dvdx = -vc * dx / d2;
+                dvdy = -vc * dy / d2;
+                dTdx = 0.0;
+                dTdy = 0.0;
+            } else {
+                dudx = 0.5 * (gL[GR_U] + gR[GR_U]);
+                dudy = 0.5 * (gL[GR_U + 1] + gR[GR_U + 1]);
+                dvdx = 0.5 * (gL[GR_V] + gR[GR_V]);
+                dvdy = 0.5 * (gL[GR_V + 1] + gR[GR_V + 1]);
+                dTdx = 0.5 * (gL[GR_T] + gR[GR_T]);
+                dTdy = 0.5 * (gL[GR_T + 1] + gR[GR_T + 1]);
+                /* boundary faces use the owner's centroid for the missing neighbour,
+                 * so dist2 = 0 and no correction (defined in place of the reference's
+                 * out-of-range read at src/Solver.cpp:729-730) */
+                int c2 = nb >= 0 ? nb : o;
+                double dxLR = m->xc[c2] - m->xc[o], dyLR = m->yc[c2] - m->yc[o];
+                double d2 = dxLR * dxLR + dyLR * dyLR;
+                if (d2 > 1e-14) {
+                    double du = (Rs.ru / Rs.r) - (L.ru / L.r);
+                    double dv = (Rs.rv / Rs.r) - (L.rv / L.r);
+                    double a0 = dudx, b0 = dudy, c0 = dvdx, e0 = dvdy;
+                    dudx = a0 - (a0 * dxLR + b0 * dyLR - du) * dxLR / d2;
+                    dudy = b0 - (a0 * dxLR + b0 * dyLR - du) * dyLR / d2;
+                    dvdx = c0 - (c0 * dxLR + e0 * dyLR - dv) * dxLR / d2;
+                    dvdy = e0 - (c0 * dxLR + e0 * dyLR - dv) * dyLR / d2;
+                }
+            }
+            double mu = rf * s->nu;
+            double k = mu * Cp / Pr;
+            double div = dudx + dvdy;
+            double txx = mu * (2.0 * dudx - (2.0 / 3.0) * div);
+            double tyy = mu * (2.0 * dvdy - (2.0 / 3.0) * div);
+            double txy = mu * (dudy + dvdx);
+            double qx = -k * dTdx, qy = -k * dTdy;
+            st_t FV;
+            FV.r = 0.0;
+            FV.ru = txx * nx + txy * ny;
+            FV.rv = txy * nx + tyy * ny;
+            double wx = uf * txx + vf * txy - qx;
+            double wy = uf * txy + vf * tyy - qy;
+            FV.rE = wx * nx + wy * ny;
+            FV.rk = 0.0;
+            FV.rw = 0.0;
+            TF = st_sub(FE, FV);
+        }
+        double A = m->area[f];
+        st_store(Rout + NV * o, st_add(st_load(Rout + NV * o), st_mul(TF, A)));
+        if (nb >= 0) st_store(Rout + NV * nb, st_sub(st_load(Rout + NV * nb), st_mul(TF, A)));
+    }
+}
+
+/* norm_L2, dot_product, norm_L2_VolumeWeighted (src/Solver.cpp:1250-1303) */
+double om_norm(int n, const double* v) {
+    double sum = 0.0;
+    for (int i = 0; i < n; ++i) {
+        const double* s = v + NV * i;
+        sum += s[0] * s[0] + s[1] * s[1] + s[2] * s[2] + s[3] * s[3] + s[4] * s[4] + s[5] * s[5];
+    }
+    return sqrt(sum);
+}
+double om_dot(int n, const double* a, const double* b) {
+    double sum = 0.0;
+    for (int i = 0; i < n; ++i) {
+        const double* x = a + NV * i;
+        const double* y = b + NV * i;
+        sum += x[0] * y[0] + x[1] * y[1] + x[2] * y[2] + x[3] * y[3] + x[4] * y[4] + x[5] * y[5];
+    }
+    return sum;
+}
+double om_norm_vm(const om_solver* s, const double* R) {
+    double sq = 0.0, tv = 0.0;
+    for (int i = 0; i < s->m->n_cells; ++i) {
+        double v = s->m->vol[i];
+        const double* r = R + NV * i;
+        double a = r[0] / v, b = r[1] / v, c = r[2] / v, d = r[3] / v, e = r[4] / v, f = r[5] / v;
+        double l = a * a + b * b + c * c + d * d + e * e + f * f;
+        sq += l * v;
+        tv += v;
+    }
+    if (tv == 0) return 0.0;
+    return sqrt(sq / tv);
+}
+
+/* computeLocalTimeStep (src/Solver.cpp:1388-1422), on the current state */
+void om_local_timestep(om_solver* s, double CFL) {
+    const om_mesh* m = s->m;
+    int n = m->n_cells;
+    double g = s->gamma;
+    double* lam = s->pc;
+    for (int i = 0; i < n; ++i) lam[i] = 1e-12;
+    for (int f = 0; f < m->n_faces; ++f) {
+        int o = m->owner[f], nb = m->neighbor[f];
+        st_t L = st_load(s->U + NV * o);
+        double pL = pressure(L);
+        double cL = sqrt(g * pL / L.r);
+        double unL = (L.ru * m->nx[f] + L.rv * m->ny[f]) / L.r;
+        lam[o] += (fabs(unL) + cL) * m->area[f];
+        if (nb >= 0) {
+            st_t Rr = st_load(s->U + NV * nb);
+            double pR = pressure(Rr);
+            double cR = sqrt(g * pR / Rr.r);
+            double unR = (Rr.ru * (-m->nx[f]) + Rr.rv * (-m->ny[f])) / Rr.r;
+            lam[nb] += (fabs(unR) + cR) * m->area[f];
+        }
+    }
+    for (int i = 0; i < n; ++i) s->dt[i] = CFL * m->vol[i] / lam[i];
+}
+void om_get_dt(const om_solver* s, double* dt) { memcpy(dt, s->dt, sizeof(double) * s->m->n_cells); }
+void om_set_dt(om_solver* s, const double* dt) { memcpy(s->dt, dt, sizeof(double) * s->m->n_cells); }
+
+/* computeDiagonalPreconditioner (src/Solver.cpp:1424-1465), on the current state */
+void om_preconditioner(om_solver* s, double* D) {
+    const om_mesh* m = s->m;
+    int n = m->n_cells;
+    double g = s->gamma;
+    for (int i = 0; i < n; ++i) D[i] = 0.0;
+    for (int f = 0; f < m->n_faces; ++f) {
+        int o = m->owner[f], nb = m->neighbor[f];
+        st_t L = st_load(s->U + NV * o);
+        st_t Rr = nb >= 0 ? st_load(s->U + NV * nb) : ghost(s, L, f);
+        double cL = sqrt(g * pressure(L) / L.r);
+        double cR = sqrt(g * (pressure(Rr) > 0 ? pressure(Rr) : 1e-3) / (Rr.r > 0 ? Rr.r : 1e-3));
+        double cf = 0.5 * (cL + cR);
+        double uf = 0.5 * (L.ru / L.r + Rr.ru / Rr.r);
+        double vf = 0.5 * (L.rv / L.r + Rr.rv / Rr.r);
+        double vn = fabs(uf * m->nx[f] + vf * m->ny[f]);
+        double li = vn + cf;
+        double dx = sqrt(m->vol[o]);
+        double mu = 0.5 * (L.r + Rr.r) * s->nu;
+        double lv = 2.0 * mu / (0.5 * (L.r + Rr.r) * dx + 1e-12);
+        double lt = (li + lv) * m->area[f];
+        D[o] += lt * 0.5;
+        if (nb >= 0) D[nb] += lt * 0.5;
+    }
+    for (int i = 0; i < n; ++i) {
+        double v = m->vol[i];
+        D[i] = (v / (s->dt[i] + 1e-30)) + D[i];
+        if (D[i] < 1e-12) D[i] = 1e-12;
+    }
+}
+
+/* applyJacobian: one-sided finite difference with the limiter frozen
+ * (src/Solver.cpp:1331-1386) */
+void om_apply_jacobian(om_solver* s, const double* Ub, const double* Rb, const double* v, double* Jv) {
+    int n = s->m->n_cells;
+    double un = om_norm(n, Ub), vn = om_norm(n, v);
+    double eps = 1e-7 * (1.0 + un) / (vn + 1e-30);
+    double* Up = (double*)malloc(sizeof(double) * NV * (size_t)n);
+    double* Rp = (double*)malloc(sizeof(double) * NV * (size_t)n);
+    for (int i = 0; i < n; ++i)
+        st_store(Up + NV * i, st_add(st_load(Ub + NV * i), st_mul(st_load(v + NV * i), eps)));
+    om_residual(s, Up, Rp, 0);
+    for (int i = 0; i < n; ++i) {
+        st_t t1 = st_mul(st_sub(st_load(Rp + NV * i), st_load(Rb + NV * i)), 1.0 / eps);
+        double tc = s->m->vol[i] / (s->dt[i] + 1e-30);
+        st_t t2 = st_mul(st_load(v + NV * i), tc);
+        st_store(Jv + NV * i, st_add(t1, t2));
+    }
+    free(Up);
+    free(Rp);
+}
+
+/* solveGMRES: one right-preconditioned MGS-GMRES cycle from x0 = 0
+ * (src/Solver.cpp:1472-1618).  Returns the iteration count k+1. */
+int om_gmres(om_solver* s, const double* Ub, const double* Rb, const double* rhs, double* x) {
+    int n = s->m->n_cells, m = s->gmres_m;
+    size_t len = (size_t)NV * n;
+    double* D = (double*)malloc(sizeof(double) * n);
+    om_preconditioner(s, D);
+    double* V = (double*)calloc((size_t)(m + 1) * len, sizeof(double));
+    double* H = (double*)calloc((size_t)(m + 1) * m, sizeof(double));
+    double* sn = (double*)calloc(m, sizeof(double));
+    double* cs = (double*)calloc(m, sizeof(double));
+    double* gv = (double*)calloc(m + 1, sizeof(double));
+    double* z = (double*)malloc(sizeof(double) * len);
+#define HH(i, j) H[(size_t)(i) * m + (j)]
+    for (size_t q = 0; q < len; ++q) x[q] = 0.0;
+    double beta = om_norm(n, rhs);
+    int k = 0;
+    if (beta < 1e-12) { k = -1; goto done; }
+    {
+        double ib = 1.0 / beta;
+        for (int i = 0; i < n; ++i) st_store(V + NV * i, st_mul(st_load(rhs + NV * i), ib));
+    }
+    gv[0] = beta;
+    for (int j = 0; j < m; ++j) {
+        k = j;
+        double* Vj = V + (size_t)j * len;
+        double* Vj1 = V + (size_t)(j + 1) * len;
+        for (int i = 0; i < n; ++i) st_store(z + NV * i, st_mul(st_load(Vj + NV * i), 1.0 / D[i]));
+        om_apply_jacobian(s, Ub, Rb, z, Vj1);
+        for (int i = 0; i <= j; ++i) {
+            double* Vi = V + (size_t)i * len;
+            HH(i, j) = om_dot(n, Vj1, Vi);
+            for (int c = 0; c < n; ++c)
+                st_store(Vj1 + NV * c, st_sub(st_load(Vj1 + NV * c), st_mul(st_load(Vi + NV * c), HH(i, j))));
+        }
+        HH(j + 1, j) = om_norm(n, Vj1);
+        if (HH(j + 1, j) > 1e-12) {
+            double ih = 1.0 / HH(j + 1, j);
+            for (int c = 0; c < n; ++c) st_store(Vj1 + NV * c, st_mul(st_load(Vj1 + NV * c), ih));
+        }
+        for (int i = 0; i < j; ++i) {
+            double t = cs[i] * HH(i, j) + sn[i] * HH(i + 1, j);
+            HH(i + 1, j) = -sn[i] * HH(i, j) + cs[i] * HH(i + 1, j);
+            HH(i, j) = t;
+        }
+        double a = HH(j, j), b = HH(j + 1, j);
+        if (fabs(b) < 1e-14) { cs[j] = 1.0; sn[j] = 0.0; }
+        else {
+            double t = sqrt(a * a + b * b);
+            cs[j] = a / t;
+            sn[j] = b / t;
+        }
+        HH(j, j) = cs[j] * a + sn[j] * b;
+        HH(j + 1, j) = 0.0;
+        gv[j + 1] = -sn[j] * gv[j];
+        gv[j] = cs[j] * gv[j];
+        if (fabs(gv[j + 1]) < s->gmres_tol * beta) break;
+    }
+    {
+        double* y = (double*)malloc(sizeof(double) * (k + 1));
+        for (int i = k; i >= 0; --i) {
+            y[i] = gv[i];
+            for (int l = i + 1; l <= k; ++l) y[i] -= HH(i, l) * y[l];
+            y[i] /= HH(i, i);
+        }
+        for (size_t q = 0; q < len; ++q) x[q] = 0.0;
+        for (int i = 0; i <= k; ++i) {
+            const double* Vi = V + (size_t)i * len;
+            for (int c = 0; c < n; ++c)
+                st_store(x + NV * c, st_add(st_load(x + NV * c), st_mul(st_mul(st_load(Vi + NV * c), y[i]), 1.0 / D[c])));
+        }
+        free(y);
+    }
+done:
+#undef HH
+    free(D); free(V); free(H); free(sn); free(cs); free(gv); free(z);
+    return k + 1;
+}
+
+/* solveImplicit: pseudo-transient Newton with the reference CFL schedule, limiter
+ * freeze, relaxation and positivity clamps (src/Solver.cpp:1696-1799).  Writes, per
+ * step, the volume-weighted and plain residual norms, the CFL and the GMRES count;
+ * returns the number of steps logged. */
+int om_solve_implicit(om_solver* s, double tol, int max_steps, double* res_vm, double* res_abs,
+                      double* cfl_out, int* iters_out) {
+    int n = s->m->n_cells;
+    size_t len = (size_t)NV * n;
+    double g = s->gamma;
+    double CFL = 0.1;
+    double* R = (double*)malloc(sizeof(double) * len);
+    double* rhs = (double*)malloc(sizeof(double) * len);
+    double* dU = (double*)malloc(sizeof(double) * len);
+    int logged = 0;
+    for (int step = 0; step < max_steps; ++step) {
+        om_local_timestep(s, CFL);
+        int upd = 1;
+        if (step > 150 || CFL > 10.0) upd = 0;
+        om_residual(s, s->U, R, upd);
+        double rvm = om_norm_vm(s, R);
+        double rn = om_norm(n, R);
+        res_vm[step] = rvm; res_abs[step] = rn; cfl_out[step] = CFL; iters_out[step] = 0;
+        logged = step + 1;
+        if (rvm < tol) break;
+        for (int i = 0; i < n; ++i) st_store(rhs + NV * i, st_mul(st_load(R + NV * i), -1.0));
+        int it = om_gmres(s, s->U, R, rhs, dU);
+        iters_out[step] = it;
+        if (it >= 29) {
+            CFL *= 0.5;
+            if (CFL < 0.05) CFL = 0.05;
+        }
+        double relax = 1.0;
+        if (rvm > 1e6) relax = 0.5;
+        else if (rvm > 2e3 && rvm < 1e2) relax = 0.9;
+        for (int i = 0; i < n; ++i) {
+            st_t Un = st_add(st_load(s->U + NV * i), st_mul(st_load(dU + NV * i), relax));
+            double ke = 0.5 * (Un.ru * Un.ru + Un.rv * Un.rv) / (Un.r + 1e-12);
+            double pn = (g - 1.0) * (Un.rE - ke);
+            if (Un.r < 1e-5) Un.r = 1e-5;
+            if (pn < 1e-5) {
+                pn = 1e-5;
+                Un.rE = pn / (g - 1.0) + ke;
+            }
+            st_store(s->U + NV * i, Un);
+        }
+        if (step > 5) {
+            if (rvm > 1e6) CFL *= 1.2;
+            else CFL *= 1.5;
+            if (it >= 25) CFL *= 0.5;
+            if (CFL > 10000) CFL = 10000;
+            if (CFL < 0.1) CFL = 0.1;
+        }
+    }
+    free(R); free(rhs); free(dU);
+    return logged;
+}
+
+/* calculateDrag: pressure force on tag-3 faces (src/Solver.cpp:1307-1325) */
+double om_drag(const om_solver* s) {
+    const om_mesh* m = s->m;
+    double d = 0.0;
+    for (int f = 0; f < m->n_faces; ++f)
+        if (m->tag[f] == 3) {
+            double p = pressure(st_load(s->U + NV * m->owner[f]));
+            d += -p * m->area[f] * m->nx[f];
+        }
+    return d;
+}
+
+/* calculateEntropyError (src/Solver.cpp:1620-1646) */
+double om_entropy_error(const om_solver* s) {
+    double g = s->gamma, M = s->M_inf;
+    double Tinf = s->T0 / (1.0 + 0.5 * (g - 1.0) * M * M);
+    double Pinf = s->P0 / pow(1.0 + 0.5 * (g - 1.0) * M * M, g / (g - 1.0));
+    double rinf = Pinf / (s->R_gas * Tinf);
+    double Sref = Pinf / pow(rinf, g);
+    double se = 0.0, tv = 0.0;
+    for (int i = 0; i < s->m->n_cells; ++i) {
+        st_t U = st_load(s->U + NV * i);
+        double p = pressure(U), r = U.r;
+        if (p <= 0 || r <= 0) continue;
+        double Sl = p / pow(r, g);
+        double e = (Sl - Sref) / Sref;
+        se += (e * e) * s->m->vol[i];
+        tv += s->m->vol[i];
+    }
+    return sqrt(se / tv);
+}

@@ -1,0 +1,88 @@
+"""libcfdgpu on the host: it loads, exports every entry point include/cfdg.h declares,
+ingests meshes with the reference's face order and geometry bit for bit, and refuses to
+compute without a GPU (there is no CPU path)."""
+import ctypes
+import os
+import re
+
+import numpy as np
+import pytest
+
+import cases as C
+from mycode_gb300 import api, meshgen as mg
+from oracle.oracle import OracleSolver
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+def declared_symbols():
+    text = open(os.path.join(ROOT, "include", "cfdg.h")).read()
+    decl = r"^\s*(?:cfdg_status|void|const char\s*\*)\s+(cfdg_[a-z0-9_]+)\s*\("
+    return sorted(set(re.findall(decl, text, flags=re.M)))
+
+
+def test_library_exports_every_declared_symbol():
+    lib = api.lib()
+    names = declared_symbols()
+    assert len(names) >= 40
+    for n in names:
+        assert hasattr(lib, n), n
+    assert set(api.SIGNATURES) == set(names)
+
+
+def test_config_defaults_follow_reference():
+    c = api.default_config()
+    assert c.flux == api.FLUX["HLLC"] and c.spatial == api.SPATIAL["SECOND_ORDER_LIMITED"]
+    assert c.gmres_m == 40 and c.gmres_tol == 1e-2
+    assert c.gamma == 1.4 and c.R_gas == 287.0 and c.Pr == 0.72 and c.nu == 0.01
+    assert c.cfl0 == 0.1 and c.cfl_max == 1e4 and c.limiter_freeze_step == 150 and c.limiter_freeze_cfl == 10.0
+
+
+@pytest.mark.parametrize("spec_fn", [lambda: mg.mixed_box(8, 6), lambda: mg.wedge(12, 8),
+                                     lambda: mg.laminar_plate(12, 8, ratio=1.2), lambda: mg.bump(3000, seed=1)])
+@pytest.mark.parametrize("renumber", ["none", "hilbert", "rcm"])
+def test_mesh_ingest_bit_exact_with_oracle(spec_fn, renumber):
+    spec = spec_fn()
+    m = api.Mesh.from_spec(spec, renumber=renumber)
+    o = OracleSolver(spec)
+    assert (m.n_cells, m.n_faces) == (o.n_cells, o.n_faces) == (spec.n_cells, spec.expected_faces())
+    mi, md = m.faces()
+    oi, od = o.faces()
+    np.testing.assert_array_equal(mi, oi)
+    np.testing.assert_array_equal(md, od)
+    np.testing.assert_array_equal(m.cells(), o.cells())
+    cp, fp = m.permutation()
+    assert sorted(cp) == list(range(m.n_cells)) and sorted(fp) == list(range(m.n_faces))
+    if renumber == "none":
+        np.testing.assert_array_equal(cp, np.arange(m.n_cells))
+
+
+def test_gmsh_loader_accepts_crlf_and_lf(tmp_path):
+    spec = mg.mixed_box(5, 4)
+    a, b = tmp_path / "lf.msh", tmp_path / "crlf.msh"
+    mg.write_gmsh(spec, str(a))
+    mg.write_gmsh(spec, str(b), crlf=True)
+    ma, mb = api.Mesh.load(str(a)), api.Mesh.load(str(b))
+    ms = api.Mesh.from_spec(spec)
+    for m in (ma, mb):
+        np.testing.assert_array_equal(m.faces()[0], ms.faces()[0])
+        np.testing.assert_array_equal(m.faces()[1], ms.faces()[1])
+
+
+def test_mesh_errors_are_reported(tmp_path):
+    with pytest.raises(api.CfdgError) as e:
+        api.Mesh.load(str(tmp_path / "missing.msh"))
+    assert e.value.status == 6
+    spec = mg.mixed_box(3, 2)
+    bad = spec.cells.copy()
+    bad[0, 0] = 10 ** 6
+    with pytest.raises(api.CfdgError):
+        api.Mesh.from_spec(mg.MeshSpec("bad", spec.nodes, bad, spec.bedges))
+
+
+@pytest.mark.skipif(api.device_count() > 0, reason="a GPU is visible")
+def test_no_cpu_fallback_without_gpu():
+    m = api.Mesh.from_spec(mg.mixed_box(3, 2))
+    with pytest.raises(api.CfdgError) as e:
+        api.Solver(m)
+    assert e.value.status == 2 and "no CUDA device" in str(e.value)
