@@ -1,0 +1,437 @@
+#!/usr/bin/env python3
+"""Benchmark of the residual-and-Newton path: cell-residuals per second.
+
+Workload (one GPU): the laminar flat plate — Navier-Stokes, M = 0.2, Re_L = 1e5,
+Pr = 0.72, adiabatic no-slip plate from x = 0 behind a 0.2 symmetry lead-in, 240 x 120
+quads (28,800 cells, 57,960 faces) with wall-normal stretching 1.08; Roe flux plus the
+viscous flux, second-order central reconstruction; pseudo-transient JFNK.  Synthetic
+mesh and state (seeded recipe, no dataset).
+
+A step is one pseudo-transient Newton step of the solve: local time step, residual,
+one right-preconditioned GMRES solve (each Krylov iteration one J v product) and the
+clamped update.  The unit of work is one cell-residual: one cell of one residual or
+J v evaluation, so a step processes n_cells * (1 + GMRES iterations) cell-residuals.
+
+  value  mixed precision (FP32 Krylov basis, FP32 exact J v and preconditioner; FP64
+         residual, update, Hessenberg/Givens and norms), state resident in HBM; device
+         time from CUDA events on the solver's stream; L2 flushed between steps
+  e2e    the same step through the C ABI with the state uploaded from pinned host
+         memory before and read back after every step (wall clock)
+  fp64   the plain FP64 path (FD J v as the reference) on the same workload
+
+``--impl reference`` times the reference's algorithm on the host cores instead: the
+reference built from its sources (oracle/_ref) when present, else the plain-C
+restatement (oracle/), one independent copy per host core.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import math
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "cell-residuals/s; JFNK time-to-1e-10 mixed vs FP64 GPU; adjoint/primal cost"
+UNIT = "cell-residuals/s"
+L2_FLUSH_BYTES = 256 << 20
+
+
+def workload_spec():
+    from mycode_gb300 import meshgen
+    return meshgen.laminar_plate(240, 120, ratio=1.08)
+
+
+WORKLOAD = {
+    "workload": "laminar flat plate 240x120 quads (28,800 cells, 57,960 faces), stretching 1.08, "
+                "Navier-Stokes M=0.2 Re_L=1e5 Pr=0.72, Roe + viscous flux, 2nd-order central, "
+                "pseudo-transient JFNK-GMRES(40), one Newton step per step",
+    "n_cells": 28800,
+    "n_faces": 57960,
+}
+
+
+def setup_flow(s):
+    s.setFreestreamStatic(0.2, 101325.0, 300.0)
+    s.setKinematicViscosity(1e5, 1.0)
+    s.initialize()
+    s.setNumericalMethod("ROE", "SECOND_ORDER_CENTRAL")
+
+
+# ---------------------------------------------------------------- roofline helpers
+
+def algorithmic_bytes(kind: str, nc: int, nf: int, nv: int, s: int, spatial: str, viscous: bool, dual: bool) -> float:
+    """Compulsory DRAM bytes of one launch: every distinct input read once and every
+    output written once.  s = bytes per real; dual kernels move value + derivative."""
+    k = 2 if dual else 1
+    second = spatial != "FIRST_ORDER"
+    limited = spatial == "SECOND_ORDER_LIMITED"
+    if kind == "prim":
+        return nc * (nv * s * k + 5 * s * k)
+    if kind == "grad":
+        # U (ghost faces) is negligible; W of every cell, gradients written, limiter written
+        return nc * (5 * s * k + 10 * s * k + (s if limited and not dual else 0)) + nc * 4 * 4
+    if kind == "flux":
+        per_face = 8 + 9 * s + nv * s * (1 if dual else 1)  # indices, geometry, F*A (derivative only for dual)
+        per_cell = nv * s * k + 3 * s * k
+        if second or viscous:
+            per_cell += 10 * s * k
+        if limited:
+            per_cell += s
+        return nf * per_face + nc * per_cell
+    if kind == "gather":
+        return nc * 16 + nf * nv * s + nc * nv * s + (nc * (nv * s + s + s) if dual else 0)
+    raise ValueError(kind)
+
+
+def measured_peak():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    try:
+        with open(p) as fh:
+            j = json.load(fh)
+        return float(j["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+def profile_traffic(kernel_class: str):
+    """DRAM bytes per launch of a kernel class from the committed ncu summary, if any."""
+    path = os.path.join(ROOT, "profiles", "traffic.txt")
+    if not os.path.exists(path):
+        return None
+    with open(path) as fh:
+        for line in fh:
+            parts = line.split()
+            if len(parts) >= 2 and parts[0] == kernel_class:
+                try:
+                    return float(parts[1])
+                except ValueError:
+                    return None
+    return None
+
+
+# ---------------------------------------------------------------- clocks
+
+class ClockSampler:
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device: int):
+        self.device = device
+        self.lines = []
+        self.proc = None
+        self.thread = None
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits",
+                                          "-i", str(self.device), "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+        except Exception:
+            self.proc = None
+            return
+        self.thread = threading.Thread(target=self._read, daemon=True)
+        self.thread.start()
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self):
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        if self.thread:
+            self.thread.join(timeout=2)
+        sm, smax, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            p = [x.strip() for x in ln.split(",")]
+            if len(p) < 9:
+                continue
+            try:
+                sm.append(float(p[1]))
+                smax = float(p[2])
+            except ValueError:
+                continue
+            for n, v in zip(names, p[5:9]):
+                if v.lower() == "active":
+                    reasons.add(n)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": smax,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+# ---------------------------------------------------------------- distributed
+
+def dist_setup(gpus: int):
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if world > 1:
+        import torch.distributed as dist
+        import torch
+        torch.cuda.set_device(local)
+        dist.init_process_group("nccl")
+    return world, rank, local
+
+
+def barrier(world):
+    if world > 1:
+        import torch.distributed as dist
+        dist.barrier()
+
+
+def all_max(world, x: float) -> float:
+    if world == 1:
+        return x
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([x], dtype=torch.float64, device="cuda")
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def all_sum(world, x: float) -> float:
+    if world == 1:
+        return x
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([x], dtype=torch.float64, device="cuda")
+    dist.all_reduce(t, op=dist.ReduceOp.SUM)
+    return float(t.item())
+
+
+# ---------------------------------------------------------------- our arm
+
+def run_steps(s, steps, flush=True):
+    """Timed Newton steps; returns (device seconds, cell-residual evaluations, per-step records)."""
+    tot_ms, evals, recs = 0.0, 0, []
+    for _ in range(steps):
+        if flush:
+            s.flush_l2(L2_FLUSH_BYTES)
+        rec, _ = s.newton_step(0.0)
+        tot_ms += rec.device_ms
+        evals += 1 + rec.gmres_iters
+        recs.append((rec.res_vm, rec.gmres_iters, rec.device_ms, rec.cfl))
+    return tot_ms / 1e3, evals, recs
+
+
+def make_solver(api, mesh, device, precision):
+    cfg = dict(bcset="plate", init="freestream", viscous=1, flux="ROE", spatial="SECOND_ORDER_CENTRAL",
+               device=device)
+    if precision == "mixed":
+        cfg.update(precision="mixed", jv="exact")
+    else:
+        cfg.update(precision="fp64", jv="fd")
+    s = api.Solver(mesh, **cfg)
+    setup_flow(s)
+    return s
+
+
+def ours(args):
+    world, rank, local = dist_setup(args.gpus)
+    from mycode_gb300 import api
+    import numpy as np
+    spec = workload_spec()
+    mesh = api.Mesh.from_spec(spec)
+    nc, nf = mesh.n_cells, mesh.n_faces
+
+    # ---- primary: mixed precision, state resident in HBM
+    s = make_solver(api, mesh, local, "mixed")
+    s.set_timing(True)
+    for _ in range(args.warmup):
+        s.newton_step(0.0)
+    s.kernel_stats(reset=True)
+    l0 = s.launch_count()
+    s.synchronize()
+    barrier(world)
+    clk = ClockSampler(local)
+    clk.start()
+    t_dev, evals, recs = run_steps(s, args.steps)
+    s.synchronize()
+    barrier(world)
+    clocks = clk.stop()
+    launches = s.launch_count() - l0
+    stats = s.kernel_stats(reset=True)
+    t_max = all_max(world, t_dev)
+    units = all_sum(world, float(evals * nc))
+    value = units / t_max
+
+    # ---- roofline of the dominant kernel class
+    peak, peak_kind = measured_peak()
+    kern = {}
+    for k, (ms, n) in stats.items():
+        if n == 0:
+            continue
+        grp, name = k.split(".")
+        dual = grp == "jv"
+        b = algorithmic_bytes(name, nc, nf, 4, 4 if dual else 8, "SECOND_ORDER_CENTRAL", True, dual)
+        avg = ms / n
+        kern[k] = {"launches": n, "total_ms": round(ms, 4), "avg_us": round(avg * 1e3, 3),
+                   "algorithmic_bytes": int(b), "achieved_gbs": round(b / (avg * 1e-3) / 1e9, 1),
+                   "share_of_step": round(ms / (t_dev * 1e3), 4)}
+    dom = max(kern, key=lambda k: kern[k]["total_ms"])
+    d = kern[dom]
+    traffic = profile_traffic(dom)
+    roofline = {"bound": "hbm", "kernel": dom, "achieved": d["achieved_gbs"], "peak": peak, "unit": "GB/s",
+                "frac": round(d["achieved_gbs"] / peak, 4), "peak_source": f"{peak_kind} (MEASURED_PEAKS.json hbm_gbs)"
+                if peak_kind == "measured" else "fallback 6.8 TB/s",
+                "traffic": traffic}
+
+    # ---- e2e through the C ABI with pinned host buffers
+    import torch
+    Uh = torch.empty((nc, 6), dtype=torch.float64, pin_memory=True).numpy()
+    Uh[:] = s.getSolution()
+    s.synchronize()
+    barrier(world)
+    t0 = time.perf_counter()
+    e_evals = 0
+    for _ in range(args.steps):
+        s.set_state(Uh)
+        rec, _ = s.newton_step(0.0)
+        Uh[:] = s.getSolution()
+        e_evals += 1 + rec.gmres_iters
+    s.synchronize()
+    barrier(world)
+    t_e2e = all_max(world, time.perf_counter() - t0)
+    e_units = all_sum(world, float(e_evals * nc))
+    e2e = {"value": e_units / t_e2e, "unit": UNIT, "h2d_bytes_per_step": nc * 6 * 8, "d2h_bytes_per_step": nc * 6 * 8,
+           "api": "cfdg_set_state + cfdg_newton_step + cfdg_get_state"}
+
+    # ---- the plain FP64 path (FD J v), same protocol
+    s64 = make_solver(api, mesh, local, "fp64")
+    s64.set_timing(True)
+    for _ in range(args.warmup):
+        s64.newton_step(0.0)
+    s64.synchronize()
+    t64, ev64, recs64 = run_steps(s64, args.steps)
+    fp64 = {"value": ev64 * nc / t64, "unit": UNIT, "ms_per_step": 1e3 * t64 / args.steps,
+            "gmres_iters": [r[1] for r in recs64], "jv": "one-sided FD (reference)"}
+
+    # ---- CPU baseline: the oracle port on this host, bounded sample
+    cpu = None
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        cpu = cpu_baseline_sample(args.cpu_seconds)
+
+    if rank == 0:
+        line = {
+            "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": 1e3 * t_max / args.steps, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32 Krylov/J v + f64 residual/update",
+            "data": "synthetic (seeded mesh recipe, free-stream start)",
+            "config": dict(WORKLOAD, precision="mixed", jv="exact (dual numbers, FP32)",
+                           l2="flushed between timed steps (256 MiB write)", parallelism="replicas" if world > 1 else "1 GPU"),
+            "gmres_iters": [r[1] for r in recs],
+            "res_vm": [r[0] for r in recs],
+            "gpu_launches": launches,
+            "roofline": roofline,
+            "kernels": kern,
+            "e2e": e2e,
+            "fp64": fp64,
+            "clocks": clocks,
+            "cpu_baseline": cpu,
+        }
+        print(json.dumps(line))
+
+
+# ---------------------------------------------------------------- CPU side
+
+def _cpu_worker(args):
+    """One independent copy of the CPU path: untimed warm-up Newton steps, then a timed
+    solveImplicit of `steps` steps continuing from that state."""
+    warm, steps, kind = args
+    sys.path.insert(0, ROOT)
+    from oracle.oracle import OracleSolver, RefSolver
+    spec = workload_spec()
+    if kind == "reference":
+        s = RefSolver(spec, "plate_visc")
+    else:
+        s = OracleSolver(spec, bcset="plate", viscous=True, init="freestream")
+    setup_flow(s)
+    if warm:
+        s.solveImplicit(0.0, warm)
+    t0 = time.perf_counter()
+    tr = s.solveImplicit(0.0, steps)
+    t = time.perf_counter() - t0
+    evals = int(len(tr["res_vm"]) + tr["gmres_iters"].sum())
+    return evals, t, len(tr["res_vm"])
+
+
+def cpu_kind():
+    from oracle.oracle import ref_available
+    return "reference" if ref_available("plate_visc") else "port"
+
+
+def cpu_baseline_sample(seconds: float):
+    from oracle.oracle import build_oracle
+    build_oracle()
+    kind = cpu_kind()
+    e1, t1, _ = _cpu_worker((0, 2, kind))
+    steps = max(2, int(seconds / max(t1 / 2, 1e-3)))
+    evals, t, n = _cpu_worker((0, steps, kind))
+    nc = WORKLOAD["n_cells"]
+    return {"value": evals * nc / t, "unit": UNIT, "cores": 1, "kind": kind,
+            "sample": f"{n} Newton steps ({evals} residual/J v evaluations, FD J v, FP64) of the same workload "
+                      f"from the free-stream start on 1 host core, {t:.1f} s"}
+
+
+def reference_arm(args):
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return
+    from oracle.oracle import build_oracle
+    build_oracle()
+    kind = cpu_kind()
+    cores = os.cpu_count() or 1
+    import multiprocessing as mp
+    ctx = mp.get_context("spawn")
+    with ctx.Pool(cores) as pool:
+        res = pool.map(_cpu_worker, [(args.warmup, args.steps, kind)] * cores)
+    nc = WORKLOAD["n_cells"]
+    evals = sum(r[0] for r in res)
+    t = max(r[1] for r in res)
+    value = evals * nc / t
+    line = {
+        "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": 1e3 * t / args.steps, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded mesh recipe, free-stream start)",
+        "config": dict(WORKLOAD, precision="fp64", jv="one-sided FD (reference)"),
+        "cpu_baseline": {"value": value, "unit": UNIT, "cores": cores, "kind": kind,
+                         "sample": f"{cores} independent copies x {args.steps} Newton steps after {args.warmup} "
+                                   f"warm-up steps ({evals} evaluations in {t:.1f} s)"},
+        "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line))
+
+
+def main():
+    ap = argparse.ArgumentParser(description=__doc__.split("\n")[0])
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--cpu-seconds", type=float, default=15.0)
+    args = ap.parse_args()
+    if args.warmup < 3:
+        ap.error("--warmup must be at least 3")
+    if args.impl == "reference":
+        reference_arm(args)
+    else:
+        ours(args)
+
+
+if __name__ == "__main__":
+    main()

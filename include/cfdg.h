@@ -23,6 +23,8 @@
 #ifndef CFDG_H
 #define CFDG_H
 
+#include <stddef.h>
+
 #ifdef __cplusplus
 extern "C" {
 #endif
@@ -92,6 +94,7 @@ typedef struct cfdg_step {
     int gmres_iters;
     int limiter_updated;
     double seconds;        /* wall time of the step */
+    double device_ms;      /* CUDA-event time of the step on the solver's stream (timing on) */
 } cfdg_step;
 
 typedef struct cfdg_mesh cfdg_mesh;
@@ -198,9 +201,16 @@ cfdg_status cfdg_entropy_error(cfdg_solver* s, double* err);
 /* R(U_current) into the solver's device residual */
 cfdg_status cfdg_residual_device(cfdg_solver* s, int update_limiters);
 cfdg_status cfdg_synchronize(cfdg_solver* s);
-/* per-kernel CUDA-event timings of the last cfdg_residual_device with timing on */
+/* timing on: CUDA events around every kernel of every residual and exact-J v
+ * evaluation and around each Newton step (cfdg_step.device_ms) */
 cfdg_status cfdg_set_timing(cfdg_solver* s, int on);
+/* per-kernel times of the last timed residual evaluation */
 cfdg_status cfdg_kernel_times(cfdg_solver* s, double* ms_prim, double* ms_grad, double* ms_flux, double* ms_gather);
+/* accumulated per-kernel time and launch count since the last reset: classes 0-3 are the
+ * residual's prim, grad, flux, gather kernels, 4-7 the same kernels of the exact J v */
+cfdg_status cfdg_kernel_stats(cfdg_solver* s, double* ms8, long long* n8, int reset);
+/* writes `bytes` of device memory on the solver's stream (evicts L2 between timed steps) */
+cfdg_status cfdg_flush_l2(cfdg_solver* s, size_t bytes);
 /* kernel launches issued by this solver since creation (all of them are this library's) */
 cfdg_status cfdg_launch_count(cfdg_solver* s, long long* n);
 

@@ -53,7 +53,7 @@ class Config(C.Structure):
 class Step(C.Structure):
     _fields_ = [("res_vm", C.c_double), ("res_abs", C.c_double), ("res_rho", C.c_double),
                 ("cfl", C.c_double), ("gmres_iters", C.c_int), ("limiter_updated", C.c_int),
-                ("seconds", C.c_double)]
+                ("seconds", C.c_double), ("device_ms", C.c_double)]
 
 
 _lib = None
@@ -110,6 +110,8 @@ SIGNATURES = {
     "cfdg_synchronize": (C.c_int, [_vp]),
     "cfdg_set_timing": (C.c_int, [_vp, C.c_int]),
     "cfdg_kernel_times": (C.c_int, [_vp] + [C.POINTER(C.c_double)] * 4),
+    "cfdg_kernel_stats": (C.c_int, [_vp, _dp, np.ctypeslib.ndpointer(dtype=np.int64, flags="C_CONTIGUOUS"), C.c_int]),
+    "cfdg_flush_l2": (C.c_int, [_vp, C.c_size_t]),
     "cfdg_launch_count": (C.c_int, [_vp, C.POINTER(C.c_longlong)]),
 }
 
@@ -358,6 +360,7 @@ class Solver:
             "cfl": np.array([r.cfl for r in recs]),
             "gmres_iters": np.array([r.gmres_iters for r in recs], dtype=np.int32),
             "seconds": np.array([r.seconds for r in recs]),
+            "device_ms": np.array([r.device_ms for r in recs]),
             "converged": st == 0,
         }
 
@@ -391,6 +394,18 @@ class Solver:
         v = [C.c_double() for _ in range(4)]
         _check(lib().cfdg_kernel_times(self._h, *[C.byref(x) for x in v]))
         return dict(zip(["prim", "grad", "flux", "gather"], [x.value for x in v]))
+
+    KERNEL_CLASSES = ["residual.prim", "residual.grad", "residual.flux", "residual.gather",
+                      "jv.prim", "jv.grad", "jv.flux", "jv.gather"]
+
+    def kernel_stats(self, reset=False):
+        ms = np.zeros(8)
+        n = np.zeros(8, np.int64)
+        _check(lib().cfdg_kernel_stats(self._h, ms, n, int(reset)))
+        return {k: (float(ms[i]), int(n[i])) for i, k in enumerate(self.KERNEL_CLASSES)}
+
+    def flush_l2(self, nbytes=256 << 20):
+        _check(lib().cfdg_flush_l2(self._h, int(nbytes)))
 
     def launch_count(self):
         n = C.c_longlong()

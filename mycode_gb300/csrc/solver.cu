@@ -120,11 +120,49 @@ struct cfdg_solver {
     double cfl = 0.1;
     int step = 0;
     bool limiter_valid = false;
-    // instrumentation
+    // instrumentation: CUDA events around the four kernels of every residual (stat
+    // classes 0-3) and exact J v (4-7) evaluation, resolved at the next stream sync
     int timing = 0;
-    cudaEvent_t ev[5] = {};
+    std::vector<cudaEvent_t> pool;
+    size_t pool_used = 0;
+    std::vector<std::pair<int, size_t>> pending;
+    double kstat_ms[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+    long long kstat_n[8] = {0, 0, 0, 0, 0, 0, 0, 0};
     float kms[4] = {0, 0, 0, 0};
+    cudaEvent_t step_ev[2] = {nullptr, nullptr};
     long long launches = 0;
+    unsigned char* l2buf = nullptr;
+    size_t l2bytes = 0;
+    int l2fill = 0;
+
+    cudaEvent_t* take_events(int base) {
+        if (!timing) return nullptr;
+        while (pool_used + 5 > pool.size()) {
+            cudaEvent_t e;
+            if (cudaEventCreate(&e) != cudaSuccess) return nullptr;
+            pool.push_back(e);
+        }
+        pending.push_back({base, pool_used});
+        cudaEvent_t* e = &pool[pool_used];
+        pool_used += 5;
+        return e;
+    }
+
+    // call only after the stream has been synchronised
+    void collect() {
+        for (auto& p : pending) {
+            float ms[4];
+            for (int k = 0; k < 4; ++k) {
+                cudaEventElapsedTime(&ms[k], pool[p.second + k], pool[p.second + k + 1]);
+                kstat_ms[p.first + k] += ms[k];
+                ++kstat_n[p.first + k];
+            }
+            if (p.first == 0)
+                for (int k = 0; k < 4; ++k) kms[k] = ms[k];
+        }
+        pending.clear();
+        pool_used = 0;
+    }
 
     double* hcol(int j) { return scal + 16 + (size_t)j * (cfg.gmres_m + 2); }
     double* ydev() { return scal + 16 + (size_t)(cfg.gmres_m + 1) * (cfg.gmres_m + 2); }
@@ -212,21 +250,18 @@ struct cfdg_solver {
         a.diag_v = nullptr;
         a.dt = nullptr;
         a.stream = st;
-        a.ev = timing ? ev : nullptr;
+        a.ev = nullptr;
         return a;
     }
 
     cfdg_status residual_dev(double* Uin, double* out, int update_limiters) {
         int do_lim = (cfg.spatial == CFDG_SECOND_ORDER_LIMITED && update_limiters) ? 1 : 0;
         ResArgs<double> a = res64(Uin, out, do_lim);
+        a.ev = take_events(0);
         launch_residual<double>(a);
         launches += 4;
         if (do_lim) limiter_valid = true;
         CK(cudaGetLastError());
-        if (timing) {
-            CK(cudaEventSynchronize(ev[4]));
-            for (int k = 0; k < 4; ++k) cudaEventElapsedTime(&kms[k], ev[k], ev[k + 1]);
-        }
         return CFDG_OK;
     }
 
@@ -245,12 +280,14 @@ struct cfdg_solver {
         CK(cudaGetLastError());
         CK(cudaMemcpyAsync(host, stage, sizeof(double) * stride * (size_t)nc, cudaMemcpyDeviceToHost, st));
         CK(cudaStreamSynchronize(st));
+        collect();
         return CFDG_OK;
     }
 
     cfdg_status read_scalars(int first, int n, double* out) {
         CK(cudaMemcpyAsync(out, scal + first, sizeof(double) * n, cudaMemcpyDeviceToHost, st));
         CK(cudaStreamSynchronize(st));
+        collect();
         return CFDG_OK;
     }
 
@@ -279,7 +316,7 @@ struct cfdg_solver {
             a.diag_v = v;
             a.dt = dt;
             a.stream = st;
-            a.ev = nullptr;
+            a.ev = take_events(4);
             launch_jv<double>(a);
             launches += 4;
         }
@@ -365,7 +402,7 @@ struct cfdg_solver {
                 a.diag_v = z32;
                 a.dt = dt32;
                 a.stream = st;
-                a.ev = nullptr;
+                a.ev = take_events(4);
                 launch_jv<float>(a);
                 launches += 5;
                 for (int i = 0; i <= j; ++i) {
@@ -392,6 +429,7 @@ struct cfdg_solver {
             CK(cudaGetLastError());
             CK(cudaMemcpyAsync(col.data(), hc, sizeof(double) * (j + 2), cudaMemcpyDeviceToHost, st));
             CK(cudaStreamSynchronize(st));
+            collect();
             for (int i = 0; i <= j; ++i) HH(i, j) = col[i];
             HH(j + 1, j) = std::sqrt(col[j + 1]);
             // Givens rotations (src/Solver.cpp:1562-1584)
@@ -428,7 +466,21 @@ struct cfdg_solver {
         ++launches;
         CK(cudaGetLastError());
         CK(cudaStreamSynchronize(st));
+        collect();
         *iters = k + 1;
+        return CFDG_OK;
+    }
+
+    cfdg_status step_time(cfdg_step& rec, double t0) {
+        if (timing) CK(cudaEventRecord(step_ev[1], st));
+        CK(cudaStreamSynchronize(st));
+        collect();
+        rec.seconds = now_s() - t0;
+        if (timing) {
+            float ms = 0;
+            CK(cudaEventElapsedTime(&ms, step_ev[0], step_ev[1]));
+            rec.device_ms = ms;
+        }
         return CFDG_OK;
     }
 
@@ -436,6 +488,7 @@ struct cfdg_solver {
     cfdg_status newton_step(double tol, cfdg_step* info, int* converged) {
         double t0 = now_s();
         *converged = 0;
+        if (timing) CK(cudaEventRecord(step_ev[0], st));
         launch_prim64(nv, nc, F, f64(U), f64(W), st);
         launch_local_dt(nv, mv, F, U, W, cfl, dt, st);
         launches += 2;
@@ -457,13 +510,14 @@ struct cfdg_solver {
         rec.gmres_iters = 0;
         rec.limiter_updated = upd ? 1 : 0;
         rec.seconds = 0;
+        rec.device_ms = 0;
         if (!std::isfinite(resVM)) {
             if (info) *info = rec;
             return fail(CFDG_ERR_NAN, "non-finite residual at Newton step " + std::to_string(step));
         }
         if (resVM < tol) {
             *converged = 1;
-            rec.seconds = now_s() - t0;
+            TRY(step_time(rec, t0));
             if (info) *info = rec;
             return CFDG_OK;
         }
@@ -487,7 +541,7 @@ struct cfdg_solver {
         ++launches;
         int hbad = 0;
         CK(cudaMemcpyAsync(&hbad, bad, sizeof(int), cudaMemcpyDeviceToHost, st));
-        CK(cudaStreamSynchronize(st));
+        TRY(step_time(rec, t0));
         if (step > 5) {
             if (resVM > 1e6) cfl *= 1.2;
             else cfl *= 1.5;
@@ -496,7 +550,6 @@ struct cfdg_solver {
             if (cfl < 0.1) cfl = 0.1;
         }
         ++step;
-        rec.seconds = now_s() - t0;
         if (info) *info = rec;
         if (hbad) return fail(CFDG_ERR_NAN, "non-finite state after the Newton update at step " + std::to_string(step - 1));
         return CFDG_OK;
@@ -509,7 +562,9 @@ struct cfdg_solver {
         for (void* p : ps) cudaFree(p);
         g64.release();
         g32.release();
-        for (auto& e : ev) if (e) cudaEventDestroy(e);
+        cudaFree(l2buf);
+        for (auto& e : pool) cudaEventDestroy(e);
+        for (auto& e : step_ev) if (e) cudaEventDestroy(e);
         if (st) cudaStreamDestroy(st);
     }
 };
@@ -660,7 +715,7 @@ cfdg_status cfdg_solver_create(const cfdg_mesh* m, const cfdg_config* cfg, cfdg_
         if (st_ != CFDG_OK) return bail(st_); \
     } while (0)
     if (cudaStreamCreateWithFlags(&s->st, cudaStreamNonBlocking) != cudaSuccess) return bail(fail(CFDG_ERR_CUDA, "stream"));
-    for (auto& e : s->ev) cudaEventCreate(&e);
+    for (auto& e : s->step_ev) cudaEventCreate(&e);
     const HostMesh& h = m->h;
     int nc = s->nc, nf = s->nf, nv = s->nv;
     long L = s->L;
@@ -810,7 +865,12 @@ cfdg_status cfdg_residual(cfdg_solver* s, const double* U, double* R, int update
 
 cfdg_status cfdg_residual_device(cfdg_solver* s, int update_limiters) {
     if (!s) return fail(CFDG_ERR_ARG, "null solver");
-    return s->residual_dev(s->U, s->R, update_limiters);
+    TRY(s->residual_dev(s->U, s->R, update_limiters));
+    if (s->timing) {
+        CK(cudaStreamSynchronize(s->st));
+        s->collect();
+    }
+    return CFDG_OK;
 }
 
 cfdg_status cfdg_gradients(cfdg_solver* s, const double* U, double* g10) {
@@ -1001,6 +1061,32 @@ cfdg_status cfdg_kernel_times(cfdg_solver* s, double* a, double* b, double* c, d
     if (b) *b = s->kms[1];
     if (c) *c = s->kms[2];
     if (d) *d = s->kms[3];
+    return CFDG_OK;
+}
+
+cfdg_status cfdg_kernel_stats(cfdg_solver* s, double* ms8, long long* n8, int reset) {
+    if (!s) return fail(CFDG_ERR_ARG, "null solver");
+    for (int k = 0; k < 8; ++k) {
+        if (ms8) ms8[k] = s->kstat_ms[k];
+        if (n8) n8[k] = s->kstat_n[k];
+        if (reset) {
+            s->kstat_ms[k] = 0;
+            s->kstat_n[k] = 0;
+        }
+    }
+    return CFDG_OK;
+}
+
+cfdg_status cfdg_flush_l2(cfdg_solver* s, size_t bytes) {
+    if (!s) return fail(CFDG_ERR_ARG, "null solver");
+    if (bytes > s->l2bytes) {
+        cudaFree(s->l2buf);
+        s->l2buf = nullptr;
+        s->l2bytes = 0;
+        CK(cudaMalloc((void**)&s->l2buf, bytes));
+        s->l2bytes = bytes;
+    }
+    CK(cudaMemsetAsync(s->l2buf, ++s->l2fill & 0xff, bytes, s->st));
     return CFDG_OK;
 }
 

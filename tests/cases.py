@@ -63,3 +63,8 @@ def random_direction(n_cells, seed, nv=4):
     v = np.random.default_rng(seed).standard_normal((n_cells, 6))
     v[:, nv:] = 0.0
     return v
+
+
+def golden_spec(gold, name):
+    """The case's mesh exactly as stored with the reference fixtures."""
+    return mg.MeshSpec(name, gold[f"{name}/nodes"], gold[f"{name}/cells"], gold[f"{name}/bedges"])

@@ -41,6 +41,11 @@ def gen_cases():
     out = {}
     for name, case in C.CASES.items():
         spec = case["spec"]()
+        # the mesh itself is stored: regenerating it elsewhere can differ in the last bit
+        # (numpy's pow and cumsum are not the same on every machine)
+        out[f"{name}/nodes"] = spec.nodes
+        out[f"{name}/cells"] = spec.cells
+        out[f"{name}/bedges"] = spec.bedges
         variant = ref_variant(case["bcset"], case["viscous"])
         r = RefSolver(spec, variant)
         C.setup(r, case)

@@ -18,9 +18,9 @@ pytestmark = pytest.mark.gpu
 REL = 1e-12  # bar for the FP64 residual path
 
 
-def _make(api, name, renumber="hilbert", **cfg):
+def _make(api, name, renumber="hilbert", spec=None, **cfg):
     case = C.CASES[name]
-    spec = case["spec"]()
+    spec = case["spec"]() if spec is None else spec
     m = api.Mesh.from_spec(spec, renumber=renumber)
     s = api.Solver(m, bcset=case["bcset"], viscous=int(case["viscous"]), init=case["init"], **cfg)
     C.setup(s, case)
@@ -66,7 +66,7 @@ def test_residual_all_schemes(cuda_lib, name, renumber):
 def test_against_reference_fixtures(cuda_lib, name):
     import os
     gold = np.load(os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden", "ref_cases.npz"))
-    case, s, o = _make(cuda_lib, name)
+    case, s, o = _make(cuda_lib, name, spec=C.golden_spec(gold, name))
     exact = case["bcset"] != "bump"
     U = np.zeros((s.n_cells, 6))
     U[:, :4] = gold[f"{name}/U"]
@@ -122,7 +122,7 @@ def test_newton_trace_against_reference(cuda_lib, name):
     import os
     from golden.make_golden import TRACE_METHOD
     gold = np.load(os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden", "ref_cases.npz"))
-    case, s, o = _make(cuda_lib, name)
+    case, s, o = _make(cuda_lib, name, spec=C.golden_spec(gold, name))
     s.setNumericalMethod(*TRACE_METHOD[name])
     tr = s.solveImplicit(0.0, 25)
     g = gold[f"{name}/trace_res_vm"]

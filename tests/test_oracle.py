@@ -25,9 +25,9 @@ def gold():
     return np.load(os.path.join(GOLD, "ref_cases.npz"))
 
 
-def _oracle(name):
+def _oracle(name, gold):
     case = C.CASES[name]
-    o = OracleSolver(case["spec"](), bcset=case["bcset"], viscous=case["viscous"], init=case["init"])
+    o = OracleSolver(C.golden_spec(gold, name), bcset=case["bcset"], viscous=case["viscous"], init=case["init"])
     C.setup(o, case)
     return o
 
@@ -40,7 +40,7 @@ def _full(U4):
 
 @pytest.mark.parametrize("name", list(C.CASES))
 def test_oracle_matches_reference_fixtures(gold, name):
-    o = _oracle(name)
+    o = _oracle(name, gold)
     U = _full(gold[f"{name}/U"])
     np.testing.assert_array_equal(o.gradients(U), gold[f"{name}/G"])
     np.testing.assert_array_equal(o.limiters(U), gold[f"{name}/phi"])
@@ -63,7 +63,7 @@ def test_oracle_matches_reference_fixtures(gold, name):
 @pytest.mark.parametrize("name", list(C.CASES))
 def test_oracle_newton_trace_matches_reference(gold, name):
     from golden.make_golden import TRACE_METHOD  # noqa: E402
-    o = _oracle(name)
+    o = _oracle(name, gold)
     o.setNumericalMethod(*TRACE_METHOD[name])
     tr = o.solveImplicit(0.0, 25)
     np.testing.assert_array_equal(tr["res_vm"], gold[f"{name}/trace_res_vm"])
