@@ -211,6 +211,20 @@ cfdg_status cfdg_kernel_times(cfdg_solver* s, double* ms_prim, double* ms_grad, 
 cfdg_status cfdg_kernel_stats(cfdg_solver* s, double* ms8, long long* n8, int reset);
 /* writes `bytes` of device memory on the solver's stream (evicts L2 between timed steps) */
 cfdg_status cfdg_flush_l2(cfdg_solver* s, size_t bytes);
+/* The volume-weighted residual norm of cfdg_norm_vm for callers that cannot allocate
+ * device memory: applications whose GPU memory belongs to their own pool (a library's
+ * cudaMalloc would fail or fragment it) and callers on latency-bound paths that cannot
+ * afford cudaMalloc's device synchronisation.  No counterpart in the reference.
+ * R: device SoA residual, nv planes of n_cells doubles; vol: device cell volumes;
+ * out: one device double, receives sqrt(sum_i (sum_c (R_c,i/vol_i)^2) vol_i / sum_i vol_i).
+ * stream: a cudaStream_t (NULL = default stream); the call only enqueues work.
+ * Allocates nothing: its reduction scratch is a static device array sized for at most
+ * 8,388,608 cells (larger n_cells is rejected with CFDG_ERR_ARG).  The first call on a
+ * device looks that array's address up (cudaGetSymbolAddress) with the device current;
+ * make that first call before any stream capture.  All calls share the array: calls
+ * that overlap on the GPU race and must be serialised by the caller. */
+cfdg_status cfdg_norm_vm_noalloc(const double* R, const double* vol, long n_cells, int nv, double* out,
+                                 void* stream);
 /* kernel launches issued by this solver since creation (all of them are this library's) */
 cfdg_status cfdg_launch_count(cfdg_solver* s, long long* n);
 

@@ -113,6 +113,7 @@ SIGNATURES = {
     "cfdg_kernel_stats": (C.c_int, [_vp, _dp, np.ctypeslib.ndpointer(dtype=np.int64, flags="C_CONTIGUOUS"), C.c_int]),
     "cfdg_flush_l2": (C.c_int, [_vp, C.c_size_t]),
     "cfdg_launch_count": (C.c_int, [_vp, C.POINTER(C.c_longlong)]),
+    "cfdg_norm_vm_noalloc": (C.c_int, [C.c_void_p, C.c_void_p, C.c_long, C.c_int, C.c_void_p, C.c_void_p]),
 }
 
 

@@ -5,6 +5,7 @@ Translation units and their floating-point contracts:
   kern_f32.cu  nvcc               (FP32 residual and mixed-precision vectors)
   kern_jv.cu   nvcc               (dual-number exact J v)
   solver.cu    nvcc               (host driver and C ABI; host code without contraction)
+  noalloc.cu   nvcc --fmad=false  (residual norm with static scratch, no allocation)
   mesh.cpp     g++ -ffp-contract=off (host geometry bit-exact on x86 and Arm)
 Compiles in parallel, links with nvcc (static cudart).
 """
@@ -26,6 +27,7 @@ CU = {
     "kern_f32.cu": [],
     "kern_jv.cu": [],
     "solver.cu": [],
+    "noalloc.cu": ["--fmad=false"],
 }
 CPP = ["mesh.cpp"]
 

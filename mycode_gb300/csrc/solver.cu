@@ -83,6 +83,11 @@ double now_s() {
 
 }  // namespace
 
+namespace cfdg {
+// lets other translation units of the library report through cfdg_last_error()
+void set_error_message(const std::string& msg) { g_err = msg; }
+}  // namespace cfdg
+
 struct cfdg_solver {
     const cfdg_mesh* mesh = nullptr;
     cfdg_config cfg;
