@@ -266,6 +266,19 @@ def ours(args):
     clocks = clk.stop()
     launches = s.launch_count() - l0
     stats = s.kernel_stats(reset=True)
+    # Event nodes are not allowed inside the graph's WHILE body, so the J v kernels of the
+    # timed steps carry no per-kernel events: replay a few steps with the host-driven
+    # Krylov loop (same kernels, launched one by one between events) to time them.
+    Usnap = s.getSolution()
+    s.set_krylov("host")
+    run_steps(s, min(args.steps, 10))
+    s.synchronize()
+    replay = s.kernel_stats(reset=True)
+    s.set_krylov("graph")
+    s.set_state(Usnap)
+    for k in list(replay):
+        if k.startswith("jv."):
+            stats[k] = replay[k]
     t_max = all_max(world, t_dev)
     units = all_sum(world, float(evals * nc))
     value = units / t_max
@@ -281,9 +294,14 @@ def ours(args):
         b = algorithmic_bytes(name, nc, nf, 4, 4 if dual else 8, "SECOND_ORDER_CENTRAL", True, dual)
         avg = ms / n
         kern[k] = {"launches": n, "total_ms": round(ms, 4), "avg_us": round(avg * 1e3, 3),
-                   "algorithmic_bytes": int(b), "achieved_gbs": round(b / (avg * 1e-3) / 1e9, 1),
-                   "share_of_step": round(ms / (t_dev * 1e3), 4)}
-    dom = max(kern, key=lambda k: kern[k]["total_ms"])
+                   "algorithmic_bytes": int(b), "achieved_gbs": round(b / (avg * 1e-3) / 1e9, 1)}
+        if grp == "jv":
+            # replayed launches: scale their average to the J v products of the timed steps
+            kern[k]["timed_launches"] = evals - args.steps
+            kern[k]["est_total_ms"] = round(avg * (evals - args.steps), 4)
+            kern[k]["source"] = "instrumented replay (host-driven Krylov loop)"
+        kern[k]["share_of_step"] = round(kern[k].get("est_total_ms", ms) / (t_dev * 1e3), 4)
+    dom = max(kern, key=lambda k: kern[k].get("est_total_ms", kern[k]["total_ms"]))
     d = kern[dom]
     traffic = profile_traffic(dom)
     roofline = {"bound": "hbm", "kernel": dom, "achieved": d["achieved_gbs"], "peak": peak, "unit": "GB/s",

@@ -83,7 +83,14 @@ typedef struct cfdg_config {
     double shock_deflection_deg; /* tag-6 post-shock inflow; 0 = unused */
     int renumber;          /* CFDG_RENUMBER_* */
     int device;            /* CUDA device ordinal */
+    /* Krylov driver: CFDG_KRYLOV_HOST runs the reference's modified Gram-Schmidt loop with
+     * the Hessenberg on the host (one sync per iteration); CFDG_KRYLOV_GRAPH runs the whole
+     * solve as one CUDA graph (WHILE node, device Givens, CGS2 orthogonalisation);
+     * CFDG_KRYLOV_AUTO picks GRAPH for mixed precision or exact J v, else HOST. */
+    int krylov;
 } cfdg_config;
+
+enum { CFDG_KRYLOV_AUTO = -1, CFDG_KRYLOV_HOST = 0, CFDG_KRYLOV_GRAPH = 1 };
 
 /* per-step record of a Newton solve (the reference prints these, src/Solver.cpp:1725-1727, :1746) */
 typedef struct cfdg_step {
@@ -179,6 +186,8 @@ cfdg_status cfdg_solve_implicit(cfdg_solver* s, double tol, int max_steps, cfdg_
 /* one pseudo-transient Newton step of solveImplicit; *converged set when the
  * step's residual was already below tol (no update made) */
 cfdg_status cfdg_newton_step(cfdg_solver* s, double tol, cfdg_step* info, int* converged);
+/* switch the Krylov driver (CFDG_KRYLOV_HOST or CFDG_KRYLOV_GRAPH) between solves */
+cfdg_status cfdg_set_krylov(cfdg_solver* s, int mode);
 /* Newton driver state (CFL, step counter) */
 cfdg_status cfdg_reset_newton(cfdg_solver* s);
 

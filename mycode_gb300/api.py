@@ -46,7 +46,7 @@ class Config(C.Structure):
         ("Pr", C.c_double), ("nu", C.c_double), ("cfl0", C.c_double), ("cfl_max", C.c_double),
         ("limiter_freeze_step", C.c_int), ("limiter_freeze_cfl", C.c_double),
         ("turb_intensity", C.c_double), ("mut_ratio", C.c_double), ("shock_deflection_deg", C.c_double),
-        ("renumber", C.c_int), ("device", C.c_int),
+        ("renumber", C.c_int), ("device", C.c_int), ("krylov", C.c_int),
     ]
 
 
@@ -102,6 +102,7 @@ SIGNATURES = {
     "cfdg_solve_implicit": (C.c_int, [_vp, C.c_double, C.c_int, C.POINTER(Step), C.POINTER(C.c_int)]),
     "cfdg_newton_step": (C.c_int, [_vp, C.c_double, C.POINTER(Step), C.POINTER(C.c_int)]),
     "cfdg_reset_newton": (C.c_int, [_vp]),
+    "cfdg_set_krylov": (C.c_int, [_vp, C.c_int]),
     "cfdg_vjp": (C.c_int, [_vp, C.c_void_p, _dp, _dp]),
     "cfdg_wall_coefficients": (C.c_int, [_vp, C.c_int, C.c_void_p, C.c_void_p, C.c_void_p, C.POINTER(C.c_int)]),
     "cfdg_drag": (C.c_int, [_vp, C.POINTER(C.c_double)]),
@@ -370,6 +371,9 @@ class Solver:
         cv = C.c_int(0)
         _check(lib().cfdg_newton_step(self._h, float(tol), C.byref(s), C.byref(cv)))
         return s, bool(cv.value)
+
+    def set_krylov(self, mode):
+        _check(lib().cfdg_set_krylov(self._h, {"host": 0, "graph": 1}.get(mode, mode)))
 
     def reset_newton(self):
         _check(lib().cfdg_reset_newton(self._h))

@@ -76,4 +76,33 @@ void launch_convert<float>(long n, const double* in, float* out, cudaStream_t s)
     k_convert_f32<<<red_grid(n), RED_THREADS, 0, s>>>(n, in, out);
 }
 
+// ---- device-resident GMRES
+template <>
+void launch_gmres_v0<float>(long n, float* V0, const double* rhs, const GmresDev& d, cudaStream_t s) {
+    k_gmres_v0<float><<<red_grid(n), RED_THREADS, 0, s>>>(n, V0, rhs, d);
+}
+template <>
+void launch_gmres_z<float>(int nv, long nc, const float* V, long L, const double* D, float* z, const GmresDev& d,
+                        cudaStream_t s) {
+    NV_SWITCH(nv, (k_gmres_z<float, NVC><<<red_grid(nc), RED_THREADS, 0, s>>>(nc, V, L, D, z, d)));
+}
+template <>
+void launch_gmres_multidot<float>(long L, const float* w, const float* V, const GmresDev& d, double* h, cudaStream_t s) {
+    k_gmres_multidot<float><<<red_grid(L), RED_THREADS, 0, s>>>(L, w, V, d, h);
+}
+template <>
+void launch_gmres_update<float>(long L, float* w, const float* V, const GmresDev& d, const double* h, double* hsq,
+                             cudaStream_t s) {
+    k_gmres_update<float><<<red_grid(L), RED_THREADS, 0, s>>>(L, w, V, d, h, hsq);
+}
+template <>
+void launch_gmres_store<float>(long L, const float* w, float* V, const GmresDev& d, cudaStream_t s) {
+    k_gmres_store<float><<<red_grid(L), RED_THREADS, 0, s>>>(L, w, V, d);
+}
+template <>
+void launch_gmres_solution_dev<float>(int nv, long nc, const float* V, long L, const GmresDev& d, const double* D,
+                                   double* x, cudaStream_t s) {
+    NV_SWITCH(nv, (k_gmres_solution_dev<float, NVC><<<grid_for(nc), 256, 0, s>>>(nc, V, L, d, D, x)));
+}
+
 }  // namespace cfdg

@@ -97,4 +97,40 @@ void launch_newton_update(int nv, long nc, double* U, const double* dU, double r
     NV_SWITCH(nv, (k_newton_update<NVC><<<grid_for(nc), 256, 0, s>>>(nc, U, dU, relax, gam, bad)));
 }
 
+// ---- device-resident GMRES
+void launch_gmres_init(const GmresDev& d, int m, double tol, cudaGraphConditionalHandle h, cudaStream_t s) {
+    k_gmres_init<<<1, 1, 0, s>>>(d, m, tol, h);
+}
+void launch_gmres_givens(const GmresDev& d, cudaGraphConditionalHandle h, cudaStream_t s) {
+    k_gmres_givens<<<1, 1, 0, s>>>(d, h);
+}
+void launch_gmres_backsub(const GmresDev& d, cudaStream_t s) { k_gmres_backsub<<<1, 1, 0, s>>>(d); }
+template <>
+void launch_gmres_v0<double>(long n, double* V0, const double* rhs, const GmresDev& d, cudaStream_t s) {
+    k_gmres_v0<double><<<red_grid(n), RED_THREADS, 0, s>>>(n, V0, rhs, d);
+}
+template <>
+void launch_gmres_z<double>(int nv, long nc, const double* V, long L, const double* D, double* z, const GmresDev& d,
+                        cudaStream_t s) {
+    NV_SWITCH(nv, (k_gmres_z<double, NVC><<<red_grid(nc), RED_THREADS, 0, s>>>(nc, V, L, D, z, d)));
+}
+template <>
+void launch_gmres_multidot<double>(long L, const double* w, const double* V, const GmresDev& d, double* h, cudaStream_t s) {
+    k_gmres_multidot<double><<<red_grid(L), RED_THREADS, 0, s>>>(L, w, V, d, h);
+}
+template <>
+void launch_gmres_update<double>(long L, double* w, const double* V, const GmresDev& d, const double* h, double* hsq,
+                             cudaStream_t s) {
+    k_gmres_update<double><<<red_grid(L), RED_THREADS, 0, s>>>(L, w, V, d, h, hsq);
+}
+template <>
+void launch_gmres_store<double>(long L, const double* w, double* V, const GmresDev& d, cudaStream_t s) {
+    k_gmres_store<double><<<red_grid(L), RED_THREADS, 0, s>>>(L, w, V, d);
+}
+template <>
+void launch_gmres_solution_dev<double>(int nv, long nc, const double* V, long L, const GmresDev& d, const double* D,
+                                   double* x, cudaStream_t s) {
+    NV_SWITCH(nv, (k_gmres_solution_dev<double, NVC><<<grid_for(nc), 256, 0, s>>>(nc, V, L, d, D, x)));
+}
+
 }  // namespace cfdg

@@ -1,0 +1,219 @@
+// Device-resident GMRES: the Arnoldi iteration runs as the body of a CUDA-graph WHILE
+// node, with the Hessenberg column, the Givens rotations and the convergence test on the
+// device, so a whole Krylov solve is one graph launch with no host round trip.
+//
+// Orthogonalisation is classical Gram-Schmidt applied twice (CGS2): two multi-dot
+// kernels and two update kernels per iteration whatever the iteration index, against
+// j+2 launches for modified Gram-Schmidt.  The Givens/least-squares arithmetic is the
+// reference's (src/Solver.cpp:1562-1599) in FP64.
+//
+// Termination: k_gmres_givens is the only kernel that advances j, it runs once per body
+// execution, and it clears the loop condition when j + 1 reaches m (or on convergence),
+// so the loop runs at most m times.
+#pragma once
+#include <cuda_runtime.h>
+#include "linalg.cuh"
+
+namespace cfdg {
+
+constexpr int KRY_MAXM = 128;  // largest Krylov dimension of the device solver
+
+struct GmresDev {
+    int* gi;          // [0] j, [1] k (last iteration), [2] done, [3] m
+    double* beta;     // [0] beta, [1] tol, [2] beta^2
+    double* g;        // [m+1]
+    double* cs;       // [m]
+    double* sn;       // [m]
+    double* H;        // [(m+1) * m], column j at H + j*(m+1)
+    double* y;        // [m]
+    double* h1;       // [m+1] first CGS pass
+    double* h2;       // [m+1] second CGS pass
+    double* hsq;      // [2] squared norms after each pass
+    double* partial;  // [(KRY_MAXM+1) * RED_BLOCKS]
+    unsigned* counter;
+};
+
+// beta = sqrt(|rhs|^2); empty solve when beta < 1e-12 (src/Solver.cpp:1514-1516)
+static __global__ void k_gmres_init(GmresDev d, int m, double tol, cudaGraphConditionalHandle h) {
+    double b = sqrt(d.beta[2]);
+    d.beta[0] = b;
+    d.beta[1] = tol;
+    d.gi[0] = 0;
+    d.gi[3] = m;
+    for (int i = 0; i <= m; ++i) d.g[i] = 0.0;
+    for (int i = 0; i < m; ++i) { d.cs[i] = 0.0; d.sn[i] = 0.0; }
+    d.g[0] = b;
+    if (b < 1e-12) {
+        d.gi[1] = -1;
+        d.gi[2] = 1;
+        cudaGraphSetConditional(h, 0);
+    } else {
+        d.gi[1] = 0;
+        d.gi[2] = 0;
+    }
+}
+
+// V0 = rhs * (1/beta)
+template <class T>
+__global__ void k_gmres_v0(long n, T* V0, const double* rhs, GmresDev d) {
+    if (d.gi[2]) return;
+    double ib = 1.0 / d.beta[0];
+    for (long q = (long)blockIdx.x * blockDim.x + threadIdx.x; q < n; q += (long)gridDim.x * blockDim.x)
+        V0[q] = (T)(rhs[q] * ib);
+}
+
+// z = V_j * (1/D) per cell (src/Solver.cpp:1536-1538)
+template <class T, int NV>
+__global__ void k_gmres_z(long nc, const T* V, long L, const double* D, T* z, GmresDev d) {
+    const T* Vj = V + (long)d.gi[0] * L;
+    for (long i = (long)blockIdx.x * blockDim.x + threadIdx.x; i < nc; i += (long)gridDim.x * blockDim.x) {
+        T id = (T)(1.0 / D[i]);
+#pragma unroll
+        for (int c = 0; c < NV; ++c) z[c * nc + i] = Vj[c * nc + i] * id;
+    }
+}
+
+// h[i] = <w, V_i>, i = 0..j.  Each block owns a contiguous slice of the vectors and
+// accumulates the dot products eight basis vectors at a time (one block reduction per
+// tile of eight); the last block to finish sums each h[i] over the blocks in block order,
+// one warp per basis vector.
+constexpr int KRY_TILE = 8;
+
+template <class T>
+__global__ void __launch_bounds__(RED_THREADS) k_gmres_multidot(long L, const T* __restrict__ w,
+                                                                const T* __restrict__ V, GmresDev d, double* h) {
+    const int j = d.gi[0];
+    long per = (L + gridDim.x - 1) / gridDim.x;
+    long lo = (long)blockIdx.x * per;
+    long hi = lo + per < L ? lo + per : L;
+    for (int i0 = 0; i0 <= j; i0 += KRY_TILE) {
+        double v[KRY_TILE];
+#pragma unroll
+        for (int t = 0; t < KRY_TILE; ++t) v[t] = 0.0;
+        const int nt = (j + 1 - i0) < KRY_TILE ? (j + 1 - i0) : KRY_TILE;
+        for (long q = lo + threadIdx.x; q < hi; q += blockDim.x) {
+            double wq = (double)w[q];
+#pragma unroll
+            for (int t = 0; t < KRY_TILE; ++t)
+                if (t < nt) v[t] += wq * (double)V[(long)(i0 + t) * L + q];
+        }
+        block_sum<KRY_TILE>(v);
+        if (threadIdx.x == 0)
+            for (int t = 0; t < nt; ++t) d.partial[(long)(i0 + t) * RED_BLOCKS + blockIdx.x] = v[t];
+        __syncthreads();
+    }
+    __shared__ bool last;
+    if (threadIdx.x == 0) {
+        __threadfence();
+        last = atomicAdd(d.counter, 1u) == gridDim.x - 1;
+    }
+    __syncthreads();
+    if (!last) return;
+    __threadfence();
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+    for (int i = warp; i <= j; i += nw) {
+        double s = 0.0;
+        for (int b = lane; b < (int)gridDim.x; b += 32) s += ((volatile double*)d.partial)[(long)i * RED_BLOCKS + b];
+        s = warp_sum(s);
+        if (lane == 0) h[i] = s;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) *d.counter = 0u;
+}
+
+// w -= sum_{i<=j} h[i] V_i, then |w|^2 into *hsq
+template <class T>
+__global__ void __launch_bounds__(RED_THREADS) k_gmres_update(long L, T* __restrict__ w, const T* __restrict__ V,
+                                                              GmresDev d, const double* h, double* hsq) {
+    const int j = d.gi[0];
+    __shared__ double hs[KRY_MAXM + 1];
+    for (int i = threadIdx.x; i <= j; i += blockDim.x) hs[i] = h[i];
+    __syncthreads();
+    double v[1] = {0.0};
+    for (long q = (long)blockIdx.x * blockDim.x + threadIdx.x; q < L; q += (long)gridDim.x * blockDim.x) {
+        double a = (double)w[q];
+        for (int i = 0; i <= j; ++i) a -= hs[i] * (double)V[(long)i * L + q];
+        T t = (T)a;
+        w[q] = t;
+        v[0] += (double)t * (double)t;
+    }
+    grid_finish<1>(v, RedScratch{d.partial, d.counter}, hsq);
+}
+
+// V_{j+1} = w / |w| when |w| > 1e-12 (the breakdown guard of src/Solver.cpp:1553-1558)
+template <class T>
+__global__ void k_gmres_store(long L, const T* w, T* V, GmresDev d) {
+    const int j = d.gi[0];
+    double hv = sqrt(d.hsq[1]);
+    double inv = hv > 1e-12 ? 1.0 / hv : 1.0;
+    T* Vn = V + (long)(j + 1) * L;
+    T s = (T)inv;
+    for (long q = (long)blockIdx.x * blockDim.x + threadIdx.x; q < L; q += (long)gridDim.x * blockDim.x)
+        Vn[q] = hv > 1e-12 ? w[q] * s : w[q];
+}
+
+// Hessenberg column, Givens rotations and the convergence test (src/Solver.cpp:1550-1588);
+// advances j or ends the loop.  One thread.
+static __global__ void k_gmres_givens(GmresDev d, cudaGraphConditionalHandle hnd) {
+    if (threadIdx.x != 0 || blockIdx.x != 0) return;
+    const int j = d.gi[0], m = d.gi[3];
+    double* col = d.H + (long)j * (m + 1);
+    for (int i = 0; i <= j; ++i) col[i] = d.h1[i] + d.h2[i];
+    col[j + 1] = sqrt(d.hsq[1]);
+    for (int i = 0; i < j; ++i) {
+        double t = d.cs[i] * col[i] + d.sn[i] * col[i + 1];
+        col[i + 1] = -d.sn[i] * col[i] + d.cs[i] * col[i + 1];
+        col[i] = t;
+    }
+    double a = col[j], b = col[j + 1];
+    if (fabs(b) < 1e-14) {
+        d.cs[j] = 1.0;
+        d.sn[j] = 0.0;
+    } else {
+        double t = sqrt(a * a + b * b);
+        d.cs[j] = a / t;
+        d.sn[j] = b / t;
+    }
+    col[j] = d.cs[j] * a + d.sn[j] * b;
+    col[j + 1] = 0.0;
+    d.g[j + 1] = -d.sn[j] * d.g[j];
+    d.g[j] = d.cs[j] * d.g[j];
+    bool conv = fabs(d.g[j + 1]) < d.beta[1] * d.beta[0];
+    if (conv || j + 1 >= m) {
+        d.gi[1] = j;
+        d.gi[2] = 1;
+        cudaGraphSetConditional(hnd, 0);
+    } else {
+        d.gi[0] = j + 1;
+    }
+}
+
+// back substitution H y = g over the k+1 leading columns (src/Solver.cpp:1592-1599)
+static __global__ void k_gmres_backsub(GmresDev d) {
+    if (threadIdx.x != 0 || blockIdx.x != 0) return;
+    const int k = d.gi[1], m = d.gi[3];
+    for (int i = k; i >= 0; --i) {
+        double yi = d.g[i];
+        for (int l = i + 1; l <= k; ++l) yi -= d.H[(long)l * (m + 1) + i] * d.y[l];
+        d.y[i] = yi / d.H[(long)i * (m + 1) + i];
+    }
+}
+
+// x = sum_{i<=k} V_i y_i / D (src/Solver.cpp:1610-1615); zero when the solve was empty
+template <class T, int NV>
+__global__ void k_gmres_solution_dev(long nc, const T* __restrict__ V, long L, GmresDev d,
+                                     const double* __restrict__ D, double* __restrict__ x) {
+    const int k = d.gi[1];
+    for (long i = (long)blockIdx.x * blockDim.x + threadIdx.x; i < nc; i += (long)gridDim.x * blockDim.x) {
+        double id = 1.0 / D[i];
+#pragma unroll
+        for (int c = 0; c < NV; ++c) {
+            long q = c * nc + i;
+            double acc = 0.0;
+            for (int j = 0; j <= k; ++j) acc = acc + (double)V[j * L + q] * d.y[j] * id;
+            x[q] = acc;
+        }
+    }
+}
+
+}  // namespace cfdg

@@ -61,9 +61,28 @@ void launch_newton_update(int nv, long nc, double* U, const double* dU, double r
                           cudaStream_t s);
 
 inline unsigned grid_for(long n, int threads = 256) { return (unsigned)((n + threads - 1) / threads); }
+// reduction / streaming grids: one entry per thread up to RED_BLOCKS blocks (enough warps
+// in flight to hide latency), grid-stride beyond
 inline unsigned red_grid(long n) {
     long b = (n + RED_THREADS - 1) / RED_THREADS;
     return (unsigned)(b < RED_BLOCKS ? (b < 1 ? 1 : b) : RED_BLOCKS);
 }
 
+}  // namespace cfdg
+
+// ---- device-resident GMRES (krylov.cuh); T = float in kern_f32.cu, double in kern_f64.cu
+#include "krylov.cuh"
+namespace cfdg {
+void launch_gmres_init(const GmresDev& d, int m, double tol, cudaGraphConditionalHandle h, cudaStream_t s);
+void launch_gmres_givens(const GmresDev& d, cudaGraphConditionalHandle h, cudaStream_t s);
+void launch_gmres_backsub(const GmresDev& d, cudaStream_t s);
+template <class T> void launch_gmres_v0(long n, T* V0, const double* rhs, const GmresDev& d, cudaStream_t s);
+template <class T> void launch_gmres_z(int nv, long nc, const T* V, long L, const double* D, T* z, const GmresDev& d,
+                                       cudaStream_t s);
+template <class T> void launch_gmres_multidot(long L, const T* w, const T* V, const GmresDev& d, double* h, cudaStream_t s);
+template <class T> void launch_gmres_update(long L, T* w, const T* V, const GmresDev& d, const double* h, double* hsq,
+                                            cudaStream_t s);
+template <class T> void launch_gmres_store(long L, const T* w, T* V, const GmresDev& d, cudaStream_t s);
+template <class T> void launch_gmres_solution_dev(int nv, long nc, const T* V, long L, const GmresDev& d,
+                                                  const double* D, double* x, cudaStream_t s);
 }  // namespace cfdg

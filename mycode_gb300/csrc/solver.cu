@@ -117,6 +117,17 @@ struct cfdg_solver {
     // Krylov basis FP64
     double *V = nullptr, *z = nullptr;
     int m_alloc = 0;
+    // device-resident GMRES (graph with a WHILE node)
+    GmresDev gd{};
+    int* gdi = nullptr;
+    double* gdd = nullptr;
+    float* w32 = nullptr;
+    double* w64 = nullptr;
+    cudaGraphExec_t gexec = nullptr;
+    const void* gkey[4] = {nullptr, nullptr, nullptr, nullptr};
+    int flow_version = 0, graph_version = -1;
+    bool capturing = false;
+    long long graph_pre = 0, graph_body = 0, graph_post = 0;
     // reductions
     RedScratch rs{nullptr, nullptr};
     double* scal = nullptr;  // [0] |U|^2 [1] |z|^2 [2] eps [3] beta^2 [4..6] vm [8..] H columns, y
@@ -141,7 +152,7 @@ struct cfdg_solver {
     int l2fill = 0;
 
     cudaEvent_t* take_events(int base) {
-        if (!timing) return nullptr;
+        if (!timing || capturing) return nullptr;  // event nodes are not allowed in graph bodies
         while (pool_used + 5 > pool.size()) {
             cudaEvent_t e;
             if (cudaEventCreate(&e) != cudaSuccess) return nullptr;
@@ -190,6 +201,7 @@ struct cfdg_solver {
         F.flux = cfg.flux;
         F.spatial = cfg.spatial;
         F.viscous = cfg.viscous;
+        ++flow_version;
         // frozen free stream, same expressions as src/Solver.cpp:979-985 (host IEEE
         // arithmetic without contraction gives the device's values)
         double g = cfg.gamma, M = M_inf;
@@ -345,9 +357,178 @@ struct cfdg_solver {
         return CFDG_OK;
     }
 
+    // ---- device-resident GMRES: one graph per (Ubase, Rbase, rhs, x, flow parameters)
+
+    // preconditioner, FP32 copies, beta and V0 (graph prologue)
+    void enqueue_gmres_pre(double* Ubase, double* rhsd, cudaGraphConditionalHandle h) {
+        const bool mixed = cfg.precision == CFDG_MIXED;
+        launch_prim64(nv, nc, F, f64(U), f64(W), st);
+        launch_precond(nv, mv, F, U, W, dt, D, st);
+        launches += 2;
+        if (mixed) {
+            launch_convert<float>(L, Ubase, U32, st);
+            launch_convert<float>(nc, phi, phi32, st);
+            launch_convert<float>(nc, dt, dt32, st);
+            launches += 3;
+        } else if (cfg.jv == CFDG_JV_FD) {
+            launch_dot<double>(nv, nc, Ubase, Ubase, rs, scal + 0, st);
+            ++launches;
+        }
+        launch_dot<double>(nv, nc, rhsd, rhsd, rs, gd.beta + 2, st);
+        launch_gmres_init(gd, cfg.gmres_m, cfg.gmres_tol, h, st);
+        if (mixed) launch_gmres_v0<float>(L, V32, rhsd, gd, st);
+        else launch_gmres_v0<double>(L, V, rhsd, gd, st);
+        launches += 3;
+    }
+
+    // one Arnoldi iteration (graph WHILE body)
+    cfdg_status enqueue_gmres_body(double* Ubase, double* Rbase, cudaGraphConditionalHandle h) {
+        const bool mixed = cfg.precision == CFDG_MIXED;
+        if (mixed) {
+            launch_gmres_z<float>(nv, nc, V32, L, D, z32, gd, st);
+            ResArgs<float> a;
+            a.m = mvf;
+            a.F = Ff;
+            a.nv = nv;
+            a.U = f32(U32, z32);
+            a.W = f32(W32, W32d);
+            a.G = f32(G32, G32d);
+            a.FA = ff32(nullptr, FA32d);
+            a.phi = phi32;
+            a.out = w32;
+            a.do_limiter = 0;
+            a.diag_v = z32;
+            a.dt = dt32;
+            a.stream = st;
+            a.ev = nullptr;
+            launch_jv<float>(a);
+            launch_gmres_multidot<float>(L, w32, V32, gd, gd.h1, st);
+            launch_gmres_update<float>(L, w32, V32, gd, gd.h1, gd.hsq, st);
+            launch_gmres_multidot<float>(L, w32, V32, gd, gd.h2, st);
+            launch_gmres_update<float>(L, w32, V32, gd, gd.h2, gd.hsq + 1, st);
+            launch_gmres_store<float>(L, w32, V32, gd, st);
+            launches += 10;
+        } else {
+            launch_gmres_z<double>(nv, nc, V, L, D, z, gd, st);
+            ++launches;
+            TRY(jv64(Ubase, Rbase, z, w64, cfg.jv, true));
+            launch_gmres_multidot<double>(L, w64, V, gd, gd.h1, st);
+            launch_gmres_update<double>(L, w64, V, gd, gd.h1, gd.hsq, st);
+            launch_gmres_multidot<double>(L, w64, V, gd, gd.h2, st);
+            launch_gmres_update<double>(L, w64, V, gd, gd.h2, gd.hsq + 1, st);
+            launch_gmres_store<double>(L, w64, V, gd, st);
+            launches += 5;
+        }
+        launch_gmres_givens(gd, h, st);
+        ++launches;
+        CK(cudaGetLastError());
+        return CFDG_OK;
+    }
+
+    void enqueue_gmres_post(double* xout) {
+        launch_gmres_backsub(gd, st);
+        if (cfg.precision == CFDG_MIXED) launch_gmres_solution_dev<float>(nv, nc, V32, L, gd, D, xout, st);
+        else launch_gmres_solution_dev<double>(nv, nc, V, L, gd, D, xout, st);
+        launches += 2;
+    }
+
+    cfdg_status build_gmres_graph(double* Ubase, double* Rbase, double* rhsd, double* xout) {
+        if (gexec) {
+            cudaGraphExecDestroy(gexec);
+            gexec = nullptr;
+        }
+        cudaGraph_t G = nullptr;
+        CK(cudaGraphCreate(&G, 0));
+        cudaGraphConditionalHandle h;
+        cfdg_status st_ = CFDG_OK;
+        long long l0 = launches;
+        std::vector<cudaGraphNode_t> leaf;
+        cudaGraphNode_t cnode = nullptr;
+        cudaGraph_t body = nullptr;
+        const cudaGraphNode_t* deps = nullptr;
+        size_t nd = 0;
+        cudaStreamCaptureStatus cs;
+        cudaGraphNodeParams p = {};
+        cudaError_t e = cudaGraphConditionalHandleCreate(&h, G, 1, cudaGraphCondAssignDefault);
+        if (e != cudaSuccess) goto cuda_fail;
+        capturing = true;
+        e = cudaStreamBeginCaptureToGraph(st, G, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal);
+        if (e != cudaSuccess) goto cuda_fail;
+        enqueue_gmres_pre(Ubase, rhsd, h);
+        e = cudaStreamGetCaptureInfo(st, &cs, nullptr, nullptr, &deps, nullptr, &nd);
+        if (e == cudaSuccess) leaf.assign(deps, deps + nd);
+        {
+            cudaError_t e2 = cudaStreamEndCapture(st, &G);
+            if (e == cudaSuccess) e = e2;
+        }
+        if (e != cudaSuccess) goto cuda_fail;
+        graph_pre = launches - l0;
+        p.type = cudaGraphNodeTypeConditional;
+        p.conditional.handle = h;
+        p.conditional.type = cudaGraphCondTypeWhile;
+        p.conditional.size = 1;
+        e = cudaGraphAddNode(&cnode, G, leaf.data(), nullptr, leaf.size(), &p);
+        if (e != cudaSuccess) goto cuda_fail;
+        body = p.conditional.phGraph_out[0];
+        l0 = launches;
+        e = cudaStreamBeginCaptureToGraph(st, body, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal);
+        if (e != cudaSuccess) goto cuda_fail;
+        st_ = enqueue_gmres_body(Ubase, Rbase, h);
+        {
+            cudaError_t e2 = cudaStreamEndCapture(st, &body);
+            if (st_ != CFDG_OK) {
+                capturing = false;
+                cudaGraphDestroy(G);
+                return st_;
+            }
+            e = e2;
+        }
+        if (e != cudaSuccess) goto cuda_fail;
+        graph_body = launches - l0;
+        l0 = launches;
+        e = cudaStreamBeginCaptureToGraph(st, G, &cnode, nullptr, 1, cudaStreamCaptureModeThreadLocal);
+        if (e != cudaSuccess) goto cuda_fail;
+        enqueue_gmres_post(xout);
+        e = cudaStreamEndCapture(st, &G);
+        if (e != cudaSuccess) goto cuda_fail;
+        graph_post = launches - l0;
+        launches = l0 - graph_pre - graph_body;
+        capturing = false;
+        e = cudaGraphInstantiate(&gexec, G, 0);
+        cudaGraphDestroy(G);
+        if (e != cudaSuccess) {
+            gexec = nullptr;
+            return fail(CFDG_ERR_CUDA, std::string("GMRES graph instantiation: ") + cudaGetErrorString(e));
+        }
+        gkey[0] = Ubase; gkey[1] = Rbase; gkey[2] = rhsd; gkey[3] = xout;
+        graph_version = flow_version;
+        return CFDG_OK;
+    cuda_fail:
+        capturing = false;
+        cudaGetLastError();
+        if (G) cudaGraphDestroy(G);
+        return fail(CFDG_ERR_CUDA, std::string("building the GMRES graph: ") + cudaGetErrorString(e));
+    }
+
+    cfdg_status gmres_graph(double* Ubase, double* Rbase, double* rhsd, double* xout, int* iters) {
+        TRY(ensure_krylov());
+        if (!gexec || graph_version != flow_version || gkey[0] != Ubase || gkey[1] != Rbase || gkey[2] != rhsd ||
+            gkey[3] != xout)
+            TRY(build_gmres_graph(Ubase, Rbase, rhsd, xout));
+        CK(cudaGraphLaunch(gexec, st));
+        int k = -1;
+        CK(cudaMemcpyAsync(&k, gd.gi + 1, sizeof(int), cudaMemcpyDeviceToHost, st));
+        CK(cudaStreamSynchronize(st));
+        collect();
+        *iters = k + 1;
+        launches += graph_pre + (long long)(k + 1) * graph_body + graph_post;
+        return CFDG_OK;
+    }
+
     // solveGMRES (src/Solver.cpp:1472-1618) about Ubase with the preconditioner of the
     // current state; rhs and xout are FP64 device vectors.
     cfdg_status gmres(double* Ubase, double* Rbase, double* rhsd, double* xout, int* iters) {
+        if (cfg.krylov == CFDG_KRYLOV_GRAPH) return gmres_graph(Ubase, Rbase, rhsd, xout, iters);
         const int m = cfg.gmres_m;
         const bool mixed = cfg.precision == CFDG_MIXED;
         const int mode = mixed ? CFDG_JV_EXACT : cfg.jv;
@@ -568,6 +749,11 @@ struct cfdg_solver {
         g64.release();
         g32.release();
         cudaFree(l2buf);
+        cudaFree(gdi);
+        cudaFree(gdd);
+        cudaFree(w32);
+        cudaFree(w64);
+        if (gexec) cudaGraphExecDestroy(gexec);
         for (auto& e : pool) cudaEventDestroy(e);
         for (auto& e : step_ev) if (e) cudaEventDestroy(e);
         if (st) cudaStreamDestroy(st);
@@ -620,6 +806,7 @@ void cfdg_config_default(cfdg_config* c) {
     c->shock_deflection_deg = 0.0;
     c->renumber = CFDG_RENUMBER_HILBERT;
     c->device = 0;
+    c->krylov = CFDG_KRYLOV_AUTO;
 }
 
 cfdg_status cfdg_mesh_create(int n_nodes, const double* xy, int n_cells, const int* cells, int n_bedges,
@@ -690,6 +877,9 @@ cfdg_status cfdg_solver_create(const cfdg_mesh* m, const cfdg_config* cfg, cfdg_
     if (cfg) c = *cfg;
     else cfdg_config_default(&c);
     if (c.gmres_m < 1 || c.gmres_m > 400) return fail(CFDG_ERR_ARG, "gmres_m must be in [1, 400]");
+    if (c.krylov < CFDG_KRYLOV_AUTO || c.krylov > CFDG_KRYLOV_GRAPH) return fail(CFDG_ERR_ARG, "unknown krylov driver");
+    if (c.krylov != CFDG_KRYLOV_HOST && c.gmres_m > KRY_MAXM)
+        return fail(CFDG_ERR_ARG, "the graph Krylov driver supports gmres_m <= 128");
     if (c.flux < 0 || c.flux > 3 || c.spatial < 0 || c.spatial > 2 || c.bcset < 0 || c.bcset > 2)
         return fail(CFDG_ERR_ARG, "unknown flux, spatial scheme or boundary-condition set");
     if (c.turbulence != CFDG_TURB_NONE) return fail(CFDG_ERR_UNSUPPORTED, "SST is not built into this library yet");
@@ -709,6 +899,8 @@ cfdg_status cfdg_solver_create(const cfdg_mesh* m, const cfdg_config* cfg, cfdg_
     s->L = (long)s->nv * s->nc;
     s->nu = c.nu;
     s->cfl = c.cfl0;
+    if (s->cfg.krylov == CFDG_KRYLOV_AUTO)
+        s->cfg.krylov = (c.precision == CFDG_MIXED || c.jv == CFDG_JV_EXACT) ? CFDG_KRYLOV_GRAPH : CFDG_KRYLOV_HOST;
     auto bail = [&](cfdg_status st) {
         s->release();
         delete s;
@@ -763,6 +955,29 @@ cfdg_status cfdg_solver_create(const cfdg_mesh* m, const cfdg_config* cfg, cfdg_
     TRYS(dalloc(&s->rs.counter, 1));
     TRYS(dalloc(&s->scal, 16 + (size_t)(c.gmres_m + 2) * (c.gmres_m + 2) + 8));
     TRYS(dalloc(&s->bad, 1));
+    if (c.gmres_m <= KRY_MAXM) {  // device-GMRES state, so the driver can be switched at run time
+        int m = c.gmres_m;
+        TRYS(dalloc(&s->gdi, 4));
+        size_t nd = 3 + (size_t)(m + 1) + 2 * (size_t)m + (size_t)(m + 1) * m + m + 2 * (size_t)(m + 1) + 2 +
+                    (size_t)(KRY_MAXM + 1) * RED_BLOCKS + 4;
+        TRYS(dalloc(&s->gdd, nd));
+        double* q = s->gdd;
+        GmresDev& d = s->gd;
+        d.gi = s->gdi;
+        d.beta = q; q += 3;
+        d.g = q; q += m + 1;
+        d.cs = q; q += m;
+        d.sn = q; q += m;
+        d.H = q; q += (size_t)(m + 1) * m;
+        d.y = q; q += m;
+        d.h1 = q; q += m + 1;
+        d.h2 = q; q += m + 1;
+        d.hsq = q; q += 2;
+        d.partial = q; q += (size_t)(KRY_MAXM + 1) * RED_BLOCKS;
+        d.counter = reinterpret_cast<unsigned*>(q);
+        if (c.precision == CFDG_MIXED) TRYS(dalloc(&s->w32, (size_t)L));
+        else TRYS(dalloc(&s->w64, (size_t)L));
+    }
     // limiter starts at 1 (no limiting) until the first limited evaluation
     std::vector<double> ones(nc, 1.0);
     if (cudaMemcpy(s->phi, ones.data(), sizeof(double) * nc, cudaMemcpyHostToDevice) != cudaSuccess)
@@ -992,6 +1207,13 @@ cfdg_status cfdg_norm_vm(cfdg_solver* s, const double* R, double* out) {
     double v[3];
     TRY(s->read_scalars(8, 3, v));
     *out = v[1] == 0 ? 0.0 : std::sqrt(v[0] / v[1]);
+    return CFDG_OK;
+}
+
+cfdg_status cfdg_set_krylov(cfdg_solver* s, int mode) {
+    if (!s || (mode != CFDG_KRYLOV_HOST && mode != CFDG_KRYLOV_GRAPH)) return fail(CFDG_ERR_ARG, "bad krylov mode");
+    if (mode == CFDG_KRYLOV_GRAPH && !s->gdi) return fail(CFDG_ERR_ARG, "the graph driver needs gmres_m <= 128");
+    s->cfg.krylov = mode;
     return CFDG_OK;
 }
 
