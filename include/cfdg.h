@@ -215,9 +215,12 @@ cfdg_status cfdg_synchronize(cfdg_solver* s);
 cfdg_status cfdg_set_timing(cfdg_solver* s, int on);
 /* per-kernel times of the last timed residual evaluation */
 cfdg_status cfdg_kernel_times(cfdg_solver* s, double* ms_prim, double* ms_grad, double* ms_flux, double* ms_gather);
-/* accumulated per-kernel time and launch count since the last reset: classes 0-3 are the
- * residual's prim, grad, flux, gather kernels, 4-7 the same kernels of the exact J v */
-cfdg_status cfdg_kernel_stats(cfdg_solver* s, double* ms8, long long* n8, int reset);
+/* accumulated per-kernel time and launch count since the last reset (12 classes): 0-3 the
+ * residual's prim, grad, flux, gather kernels, 4-7 the same kernels of the exact J v,
+ * 8-11 the VJP's forward recomputation, face adjoint and its two cell gathers */
+cfdg_status cfdg_kernel_stats(cfdg_solver* s, double* ms12, long long* n12, int reset);
+/* VJP at the device-resident state with the device residual as lambda (timing path) */
+cfdg_status cfdg_vjp_device(cfdg_solver* s);
 /* writes `bytes` of device memory on the solver's stream (evicts L2 between timed steps) */
 cfdg_status cfdg_flush_l2(cfdg_solver* s, size_t bytes);
 /* The volume-weighted residual norm of cfdg_norm_vm for callers that cannot allocate

@@ -108,6 +108,7 @@ SIGNATURES = {
     "cfdg_drag": (C.c_int, [_vp, C.POINTER(C.c_double)]),
     "cfdg_entropy_error": (C.c_int, [_vp, C.POINTER(C.c_double)]),
     "cfdg_residual_device": (C.c_int, [_vp, C.c_int]),
+    "cfdg_vjp_device": (C.c_int, [_vp]),
     "cfdg_synchronize": (C.c_int, [_vp]),
     "cfdg_set_timing": (C.c_int, [_vp, C.c_int]),
     "cfdg_kernel_times": (C.c_int, [_vp] + [C.POINTER(C.c_double)] * 4),
@@ -401,11 +402,12 @@ class Solver:
         return dict(zip(["prim", "grad", "flux", "gather"], [x.value for x in v]))
 
     KERNEL_CLASSES = ["residual.prim", "residual.grad", "residual.flux", "residual.gather",
-                      "jv.prim", "jv.grad", "jv.flux", "jv.gather"]
+                      "jv.prim", "jv.grad", "jv.flux", "jv.gather",
+                      "vjp.forward", "vjp.flux_adj", "vjp.cell1", "vjp.cell2"]
 
     def kernel_stats(self, reset=False):
-        ms = np.zeros(8)
-        n = np.zeros(8, np.int64)
+        ms = np.zeros(12)
+        n = np.zeros(12, np.int64)
         _check(lib().cfdg_kernel_stats(self._h, ms, n, int(reset)))
         return {k: (float(ms[i]), int(n[i])) for i, k in enumerate(self.KERNEL_CLASSES)}
 

@@ -6,6 +6,7 @@ Translation units and their floating-point contracts:
   kern_jv.cu   nvcc               (dual-number exact J v)
   solver.cu    nvcc               (host driver and C ABI; host code without contraction)
   noalloc.cu   nvcc --fmad=false  (residual norm with static scratch, no allocation)
+  kern_adj.cu  nvcc               (adjoint / VJP of the FP64 residual)
   mesh.cpp     g++ -ffp-contract=off (host geometry bit-exact on x86 and Arm)
 Compiles in parallel, links with nvcc (static cudart).
 """
@@ -28,6 +29,7 @@ CU = {
     "kern_jv.cu": [],
     "solver.cu": [],
     "noalloc.cu": ["--fmad=false"],
+    "kern_adj.cu": [],
 }
 CPP = ["mesh.cpp"]
 

@@ -1,0 +1,120 @@
+// The residual's face function: F*A for one face from the two cell states, their
+// gradients and limiters (the body of the face loop of computeResiduals,
+// src/Solver.cpp:543-800).  Shared by the residual kernel (any scalar type) and by the
+// adjoint, which differentiates exactly this sequence of operations.
+#pragma once
+#include "physics.cuh"
+
+namespace cfdg {
+
+template <class R>
+struct FaceGeo {
+    R nx, ny, A;
+    R dxL, dyL, dxR, dyR;  // face midpoint minus owner / neighbour centroid
+    R dxlr, dylr;          // neighbour minus owner centroid (0 on the boundary)
+};
+
+// gradient layout per cell: (x, y) pairs of rho, u, v, p, T
+enum { FG_R = 0, FG_U = 2, FG_V = 4, FG_P = 6, FG_T = 8 };
+
+// Ghost or neighbour state of the face: the neighbour when interior, else the ghost of L.
+template <class S, class R>
+CFD_HD CS<S> face_right(const Flow<R>& F, const CS<S>& L, const CS<S>& Rn, bool interior, int tag, R nx, R ny) {
+    return interior ? Rn : ghost_state(F, L, tag, nx, ny);
+}
+
+// Second-order reconstruction of one side (src/Solver.cpp:596-623)
+template <class S, class R>
+CFD_HD CS<S> reconstruct(const Flow<R>& F, const CS<S>& C, const S* g, S ph, R dx, R dy) {
+    S rf = C.r + ph * (g[FG_R] * dx + g[FG_R + 1] * dy);
+    S pf = C.p + ph * (g[FG_P] * dx + g[FG_P + 1] * dy);
+    S uf = C.u + ph * (g[FG_U] * dx + g[FG_U + 1] * dy);
+    S vf = C.v + ph * (g[FG_V] * dx + g[FG_V + 1] * dy);
+    if (val(rf) < R(1e-4)) rf = C.r;
+    if (val(pf) < R(1e-4)) pf = C.p;
+    return p2c(F, rf, uf, vf, pf, S(R(0)), S(R(0)));
+}
+
+// F*A of one face.  L: owner state; Rn: neighbour state (ignored on the boundary);
+// gL/gR: the owner's / neighbour's 10 gradient values (gR ignored on the boundary);
+// phL/phR: limiter values (used by the limited scheme).
+template <class S, class R>
+CFD_HD Flux6<S> face_flux(const Flow<R>& F, const CS<S>& L, const CS<S>& Rn, bool interior, int tag,
+                          const FaceGeo<R>& g, const S* gL, const S* gR, S phL, S phR) {
+    const R nx = g.nx, ny = g.ny;
+    CS<S> Rt = face_right(F, L, Rn, interior, tag, nx, ny);
+    CS<S> Lr = L, Rr = Rt;
+    if (F.spatial != SP_FIRST && interior) {
+        S pl = F.spatial == SP_LIMITED ? phL : S(R(0.5));
+        S pr = F.spatial == SP_LIMITED ? phR : S(R(0.5));
+        Lr = reconstruct(F, L, gL, pl, g.dxL, g.dyL);
+        Rr = reconstruct(F, Rt, gR, pr, g.dxR, g.dyR);
+    }
+    Flux6<S> TF;
+    if (!interior && (tag == 3 || tag == 4)) {
+        S pw = Lr.p;
+        TF.f[0] = S(R(0.0));
+        TF.f[1] = pw * nx;
+        TF.f[2] = pw * ny;
+        TF.f[3] = S(R(0.0));
+        TF.f[4] = S(R(0.0));
+        TF.f[5] = S(R(0.0));
+    } else {
+        TF = inviscid_flux(F, Lr, Rr, nx, ny);
+    }
+    if (F.viscous) {
+        const S* gRv = interior ? gR : gL;
+        S rf = R(0.5) * (L.r + Rt.r);
+        S uf = R(0.5) * (L.u + Rt.u);
+        S vf = R(0.5) * (L.v + Rt.v);
+        S dudx, dudy, dvdx, dvdy, dTdx, dTdy;
+        if (!interior && tag == 4) {
+            R dx = g.dxL, dy = g.dyL;
+            R d2 = dx * dx + dy * dy;
+            S uc = L.u, vc = L.v;
+            dudx = -uc * dx / d2;
+            dudy = -uc * dy / d2;
+            dvdx = -vc * dx / d2;
+            dvdy = -vc * dy / d2;
+            dTdx = S(R(0.0));
+            dTdy = S(R(0.0));
+        } else {
+            dudx = R(0.5) * (gL[FG_U] + gRv[FG_U]);
+            dudy = R(0.5) * (gL[FG_U + 1] + gRv[FG_U + 1]);
+            dvdx = R(0.5) * (gL[FG_V] + gRv[FG_V]);
+            dvdy = R(0.5) * (gL[FG_V + 1] + gRv[FG_V + 1]);
+            dTdx = R(0.5) * (gL[FG_T] + gRv[FG_T]);
+            dTdy = R(0.5) * (gL[FG_T + 1] + gRv[FG_T + 1]);
+            R d2 = g.dxlr * g.dxlr + g.dylr * g.dylr;
+            if (d2 > R(1e-14)) {
+                S du = Rt.u - L.u;
+                S dv = Rt.v - L.v;
+                S a0 = dudx, b0 = dudy, c0 = dvdx, e0 = dvdy;
+                dudx = a0 - (a0 * g.dxlr + b0 * g.dylr - du) * g.dxlr / d2;
+                dudy = b0 - (a0 * g.dxlr + b0 * g.dylr - du) * g.dylr / d2;
+                dvdx = c0 - (c0 * g.dxlr + e0 * g.dylr - dv) * g.dxlr / d2;
+                dvdy = e0 - (c0 * g.dxlr + e0 * g.dylr - dv) * g.dylr / d2;
+            }
+        }
+        R Cp = F.gam * F.Rgas / (F.gam - R(1.0));
+        S mu = rf * F.nu;
+        S kc = mu * Cp / F.Pr;
+        S div = dudx + dvdy;
+        S txx = mu * (R(2.0) * dudx - (R(2.0) / R(3.0)) * div);
+        S tyy = mu * (R(2.0) * dvdy - (R(2.0) / R(3.0)) * div);
+        S txy = mu * (dudy + dvdx);
+        S qx = -kc * dTdx, qy = -kc * dTdy;
+        S wx = uf * txx + vf * txy - qx;
+        S wy = uf * txy + vf * tyy - qy;
+        TF.f[0] = TF.f[0] - S(R(0.0));
+        TF.f[1] = TF.f[1] - (txx * nx + txy * ny);
+        TF.f[2] = TF.f[2] - (txy * nx + tyy * ny);
+        TF.f[3] = TF.f[3] - (wx * nx + wy * ny);
+    }
+    Flux6<S> out;
+#pragma unroll
+    for (int c = 0; c < 6; ++c) out.f[c] = TF.f[c] * g.A;
+    return out;
+}
+
+}  // namespace cfdg

@@ -1,0 +1,29 @@
+// Adjoint (VJP) kernels of the FP64 residual: forward recomputation of the primitives,
+// gradients and limiter, then the reverse face and cell kernels of adjoint_kernels.cuh.
+#include "adjoint_kernels.cuh"
+#include "launch.hpp"
+
+namespace cfdg {
+
+template <int NV>
+static void vjp_nv(const ResArgs<double>& a, const double* lam, const AdjBufs& b, double* gU) {
+    long nc = a.m.nc, nf = a.m.nf;
+    int limited = a.F.spatial == SP_LIMITED ? 1 : 0;
+    if (a.ev) cudaEventRecord(a.ev[0], a.stream);
+    k_prim<double, NV><<<grid_for(nc), 256, 0, a.stream>>>((int)nc, a.F, a.U, a.W);
+    k_grad<double, NV><<<grid_for(nc), 256, 0, a.stream>>>(a.m, a.F, a.U, a.W, a.G, a.phi, limited);
+    if (a.ev) cudaEventRecord(a.ev[1], a.stream);
+    k_flux_adj<NV><<<grid_for(nf, 128), 128, 0, a.stream>>>(a.m, a.F, a.U, a.W, a.G, a.phi, lam, b);
+    if (a.ev) cudaEventRecord(a.ev[2], a.stream);
+    k_adj_cell1<NV><<<grid_for(nc, 128), 128, 0, a.stream>>>(a.m, a.F, a.U, a.W, a.G, a.phi, limited, b);
+    if (a.ev) cudaEventRecord(a.ev[3], a.stream);
+    k_adj_cell2<NV><<<grid_for(nc, 128), 128, 0, a.stream>>>(a.m, a.F, a.U, a.W, b, gU);
+    if (a.ev) cudaEventRecord(a.ev[4], a.stream);
+}
+
+void launch_vjp64(const ResArgs<double>& a, const double* lam, const AdjBufs& b, double* gU) {
+    if (a.nv == 6) vjp_nv<6>(a, lam, b, gU);
+    else vjp_nv<4>(a, lam, b, gU);
+}
+
+}  // namespace cfdg

@@ -86,3 +86,9 @@ template <class T> void launch_gmres_store(long L, const T* w, T* V, const Gmres
 template <class T> void launch_gmres_solution_dev(int nv, long nc, const T* V, long L, const GmresDev& d,
                                                   const double* D, double* x, cudaStream_t s);
 }  // namespace cfdg
+
+// ---- adjoint of the FP64 residual (kern_adj.cu); a.phi receives the recomputed limiter
+namespace cfdg {
+struct AdjBufs;
+void launch_vjp64(const ResArgs<double>& a, const double* lam, const AdjBufs& b, double* gU);
+}  // namespace cfdg

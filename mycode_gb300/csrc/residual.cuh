@@ -14,7 +14,7 @@
 // frozen), where every array has a value plane and a derivative plane.
 #pragma once
 #include <cuda_runtime.h>
-#include "physics.cuh"
+#include "face.cuh"
 
 namespace cfdg {
 
@@ -212,103 +212,57 @@ __global__ void __launch_bounds__(256) k_grad(MeshView<R> m, Flow<R> F, Field<R>
 }
 
 // ---------------------------------------------------------------- k_flux
-// The face loop of computeResiduals (src/Solver.cpp:543-800): reconstruction, the
-// wall pressure flux or the Riemann flux, and (viscous) the Navier-Stokes flux from
-// averaged and corrected cell gradients.  Writes F*A per face.
+// The face loop of computeResiduals (src/Solver.cpp:543-800) through face_flux:
+// reconstruction, the wall pressure flux or the Riemann flux, and (viscous) the
+// Navier-Stokes flux from averaged and corrected cell gradients.  Writes F*A per face.
+template <class S, int NV, class R>
+__device__ __forceinline__ void load_grad(const Field<R>& G, long i, S* g) {
+#pragma unroll
+    for (int q = 0; q < 10; ++q) g[q] = Acc<S>::ld(G, q, i);
+}
+
+template <class R>
+__device__ __forceinline__ FaceGeo<R> load_geo(const MeshView<R>& m, long f) {
+    FaceGeo<R> g;
+    g.nx = m.nx[f];
+    g.ny = m.ny[f];
+    g.A = m.area[f];
+    g.dxL = m.dxo[f];
+    g.dyL = m.dyo[f];
+    g.dxR = m.dxn[f];
+    g.dyR = m.dyn[f];
+    g.dxlr = m.dxlr[f];
+    g.dylr = m.dylr[f];
+    return g;
+}
+
 template <class S, int NV, class R>
 __global__ void __launch_bounds__(256) k_flux(MeshView<R> m, Flow<R> F, Field<R> U, Field<R> W, Field<R> G,
                                               const R* __restrict__ phi, Field<R> FA) {
     long f = (long)blockIdx.x * blockDim.x + threadIdx.x;
     if (f >= m.nf) return;
     int o = m.fo[f], n = m.fn[f];
-    R nx = m.nx[f], ny = m.ny[f], A = m.area[f];
-    int tag = n >= 0 ? 0 : m.ftag[f];
+    bool interior = n >= 0;
+    int tag = interior ? 0 : m.ftag[f];
+    FaceGeo<R> g = load_geo(m, f);
     CS<S> L = load_cs<S, NV>(U, W, o);
-    CS<S> Rt = n >= 0 ? load_cs<S, NV>(U, W, n) : ghost_state(F, L, tag, nx, ny);
-    CS<S> Lr = L, Rr = Rt;
-    if (F.spatial != SP_FIRST && n >= 0) {
-        R dxL = m.dxo[f], dyL = m.dyo[f], dxR = m.dxn[f], dyR = m.dyn[f];
-        S phL = F.spatial == SP_LIMITED ? S(phi[o]) : S(R(0.5));
-        S phR = F.spatial == SP_LIMITED ? S(phi[n]) : S(R(0.5));
-        S rLf = L.r + phL * (Acc<S>::ld(G, G_R, o) * dxL + Acc<S>::ld(G, G_R + 1, o) * dyL);
-        S pLf = L.p + phL * (Acc<S>::ld(G, G_P, o) * dxL + Acc<S>::ld(G, G_P + 1, o) * dyL);
-        S uLf = L.u + phL * (Acc<S>::ld(G, G_U, o) * dxL + Acc<S>::ld(G, G_U + 1, o) * dyL);
-        S vLf = L.v + phL * (Acc<S>::ld(G, G_V, o) * dxL + Acc<S>::ld(G, G_V + 1, o) * dyL);
-        if (val(rLf) < R(1e-4)) rLf = L.r;
-        if (val(pLf) < R(1e-4)) pLf = L.p;
-        Lr = p2c(F, rLf, uLf, vLf, pLf, S(R(0)), S(R(0)));
-        S rRf = Rt.r + phR * (Acc<S>::ld(G, G_R, n) * dxR + Acc<S>::ld(G, G_R + 1, n) * dyR);
-        S pRf = Rt.p + phR * (Acc<S>::ld(G, G_P, n) * dxR + Acc<S>::ld(G, G_P + 1, n) * dyR);
-        S uRf = Rt.u + phR * (Acc<S>::ld(G, G_U, n) * dxR + Acc<S>::ld(G, G_U + 1, n) * dyR);
-        S vRf = Rt.v + phR * (Acc<S>::ld(G, G_V, n) * dxR + Acc<S>::ld(G, G_V + 1, n) * dyR);
-        if (val(rRf) < R(1e-4)) rRf = Rt.r;
-        if (val(pRf) < R(1e-4)) pRf = Rt.p;
-        Rr = p2c(F, rRf, uRf, vRf, pRf, S(R(0)), S(R(0)));
-    }
-    Flux6<S> TF;
-    if (n < 0 && (tag == 3 || tag == 4)) {
-        S pw = Lr.p;
-        TF.f[0] = S(R(0.0));
-        TF.f[1] = pw * nx;
-        TF.f[2] = pw * ny;
-        TF.f[3] = S(R(0.0));
-        TF.f[4] = S(R(0.0));
-        TF.f[5] = S(R(0.0));
-    } else {
-        TF = inviscid_flux(F, Lr, Rr, nx, ny);
-    }
-    if (F.viscous) {
-        S rf = R(0.5) * (L.r + Rt.r);
-        S uf = R(0.5) * (L.u + Rt.u);
-        S vf = R(0.5) * (L.v + Rt.v);
-        S dudx, dudy, dvdx, dvdy, dTdx, dTdy;
-        if (n < 0 && tag == 4) {
-            R dx = m.dxo[f], dy = m.dyo[f];
-            R d2 = dx * dx + dy * dy;
-            S uc = L.u, vc = L.v;
-            dudx = -uc * dx / d2;
-            dudy = -uc * dy / d2;
-            dvdx = -vc * dx / d2;
-            dvdy = -vc * dy / d2;
-            dTdx = S(R(0.0));
-            dTdy = S(R(0.0));
-        } else {
-            int nn = n >= 0 ? n : o;
-            dudx = R(0.5) * (Acc<S>::ld(G, G_U, o) + Acc<S>::ld(G, G_U, nn));
-            dudy = R(0.5) * (Acc<S>::ld(G, G_U + 1, o) + Acc<S>::ld(G, G_U + 1, nn));
-            dvdx = R(0.5) * (Acc<S>::ld(G, G_V, o) + Acc<S>::ld(G, G_V, nn));
-            dvdy = R(0.5) * (Acc<S>::ld(G, G_V + 1, o) + Acc<S>::ld(G, G_V + 1, nn));
-            dTdx = R(0.5) * (Acc<S>::ld(G, G_T, o) + Acc<S>::ld(G, G_T, nn));
-            dTdy = R(0.5) * (Acc<S>::ld(G, G_T + 1, o) + Acc<S>::ld(G, G_T + 1, nn));
-            R dxLR = m.dxlr[f], dyLR = m.dylr[f];
-            R d2 = dxLR * dxLR + dyLR * dyLR;
-            if (d2 > R(1e-14)) {
-                S du = Rt.u - L.u;
-                S dv = Rt.v - L.v;
-                S a0 = dudx, b0 = dudy, c0 = dvdx, e0 = dvdy;
-                dudx = a0 - (a0 * dxLR + b0 * dyLR - du) * dxLR / d2;
-                dudy = b0 - (a0 * dxLR + b0 * dyLR - du) * dyLR / d2;
-                dvdx = c0 - (c0 * dxLR + e0 * dyLR - dv) * dxLR / d2;
-                dvdy = e0 - (c0 * dxLR + e0 * dyLR - dv) * dyLR / d2;
-            }
-        }
-        R Cp = F.gam * F.Rgas / (F.gam - R(1.0));
-        S mu = rf * F.nu;
-        S kc = mu * Cp / F.Pr;
-        S div = dudx + dvdy;
-        S txx = mu * (R(2.0) * dudx - (R(2.0) / R(3.0)) * div);
-        S tyy = mu * (R(2.0) * dvdy - (R(2.0) / R(3.0)) * div);
-        S txy = mu * (dudy + dvdx);
-        S qx = -kc * dTdx, qy = -kc * dTdy;
-        S wx = uf * txx + vf * txy - qx;
-        S wy = uf * txy + vf * tyy - qy;
-        TF.f[0] = TF.f[0] - S(R(0.0));
-        TF.f[1] = TF.f[1] - (txx * nx + txy * ny);
-        TF.f[2] = TF.f[2] - (txy * nx + tyy * ny);
-        TF.f[3] = TF.f[3] - (wx * nx + wy * ny);
-    }
+    CS<S> Rn = interior ? load_cs<S, NV>(U, W, n) : L;
+    S gL[10], gR[10];
 #pragma unroll
-    for (int c = 0; c < NV; ++c) Acc<S>::st(FA, c, f, TF.f[c] * A);
+    for (int q = 0; q < 10; ++q) { gL[q] = S(R(0)); gR[q] = S(R(0)); }
+    const bool second = F.spatial != SP_FIRST;
+    if ((second && interior) || F.viscous) {
+        load_grad<S, NV>(G, o, gL);
+        if (interior) load_grad<S, NV>(G, n, gR);
+    }
+    S phL = S(R(1)), phR = S(R(1));
+    if (F.spatial == SP_LIMITED && interior) {
+        phL = S(phi[o]);
+        phR = S(phi[n]);
+    }
+    Flux6<S> out = face_flux(F, L, Rn, interior, tag, g, gL, gR, phL, phR);
+#pragma unroll
+    for (int c = 0; c < NV; ++c) Acc<S>::st(FA, c, f, out.f[c]);
 }
 
 // ---------------------------------------------------------------- k_gather

@@ -16,6 +16,7 @@
 #include <vector>
 
 #include "../../include/cfdg.h"
+#include "adjoint_kernels.cuh"
 #include "launch.hpp"
 #include "mesh.hpp"
 
@@ -142,8 +143,14 @@ struct cfdg_solver {
     std::vector<cudaEvent_t> pool;
     size_t pool_used = 0;
     std::vector<std::pair<int, size_t>> pending;
-    double kstat_ms[8] = {0, 0, 0, 0, 0, 0, 0, 0};
-    long long kstat_n[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+    // classes 8-11: the VJP's forward recomputation, face adjoint, cell gathers 1 and 2
+    double kstat_ms[12] = {0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0};
+    long long kstat_n[12] = {0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0};
+    // adjoint work buffers (allocated on the first VJP)
+    AdjBufs ab{};
+    double* adj_mem = nullptr;
+    int* adj_imem = nullptr;
+    double* phi_adj = nullptr;
     float kms[4] = {0, 0, 0, 0};
     cudaEvent_t step_ev[2] = {nullptr, nullptr};
     long long launches = 0;
@@ -354,6 +361,37 @@ struct cfdg_solver {
             TRY(dalloc(&z, (size_t)L));
         }
         m_alloc = m;
+        return CFDG_OK;
+    }
+
+    // ---- adjoint: gU = (dR/dU)^T lam at Uin, limiter recomputed into a scratch buffer
+    cfdg_status ensure_adj() {
+        if (adj_mem) return CFDG_OK;
+        const int N = nv + 11;
+        size_t nd = 2 * (size_t)N * nf + (size_t)nv * nc + 10 * (size_t)nc + 2 * (size_t)nc;
+        TRY(dalloc(&adj_mem, nd));
+        TRY(dalloc(&adj_imem, 2 * (size_t)nc));
+        TRY(dalloc(&phi_adj, (size_t)nc));
+        double* q = adj_mem;
+        ab.fb0 = q; q += (size_t)N * nf;
+        ab.fb1 = q; q += (size_t)N * nf;
+        ab.gpart = q; q += (size_t)nv * nc;
+        ab.accb = q; q += 10 * (size_t)nc;
+        ab.pmaxb = q; q += nc;
+        ab.pminb = q;
+        ab.pmax_face = adj_imem;
+        ab.pmin_face = adj_imem + nc;
+        return CFDG_OK;
+    }
+
+    cfdg_status vjp_dev(double* Uin, double* lam, double* gout) {
+        TRY(ensure_adj());
+        ResArgs<double> a = res64(Uin, nullptr, 0);
+        a.phi = phi_adj;
+        a.ev = take_events(8);
+        launch_vjp64(a, lam, ab, gout);
+        launches += 5;
+        CK(cudaGetLastError());
         return CFDG_OK;
     }
 
@@ -753,6 +791,9 @@ struct cfdg_solver {
         cudaFree(gdd);
         cudaFree(w32);
         cudaFree(w64);
+        cudaFree(adj_mem);
+        cudaFree(adj_imem);
+        cudaFree(phi_adj);
         if (gexec) cudaGraphExecDestroy(gexec);
         for (auto& e : pool) cudaEventDestroy(e);
         for (auto& e : step_ev) if (e) cudaEventDestroy(e);
@@ -1250,9 +1291,26 @@ cfdg_status cfdg_solve_implicit(cfdg_solver* s, double tol, int max_steps, cfdg_
     return fail(CFDG_ERR_NOT_CONVERGED, "solveImplicit reached max_steps above the tolerance");
 }
 
-cfdg_status cfdg_vjp(cfdg_solver* s, const double*, const double*, double*) {
+cfdg_status cfdg_vjp(cfdg_solver* s, const double* U, const double* lambda, double* gU) {
+    if (!s || !lambda || !gU) return fail(CFDG_ERR_ARG, "cfdg_vjp: null argument");
+    double* Uin = s->U;
+    if (U) {
+        TRY(s->upload_aos(U, s->Ub));
+        Uin = s->Ub;
+    }
+    TRY(s->upload_aos(lambda, s->vtmp));
+    TRY(s->vjp_dev(Uin, s->vtmp, s->x));
+    return s->download_aos(s->x, gU, s->nv, 6);
+}
+
+cfdg_status cfdg_vjp_device(cfdg_solver* s) {
     if (!s) return fail(CFDG_ERR_ARG, "null solver");
-    return fail(CFDG_ERR_UNSUPPORTED, "the adjoint kernel is not built into this library yet");
+    TRY(s->vjp_dev(s->U, s->R, s->x));
+    if (s->timing) {
+        CK(cudaStreamSynchronize(s->st));
+        s->collect();
+    }
+    return CFDG_OK;
 }
 
 cfdg_status cfdg_wall_coefficients(cfdg_solver* s, int, double*, double*, double*, int*) {
@@ -1293,7 +1351,7 @@ cfdg_status cfdg_kernel_times(cfdg_solver* s, double* a, double* b, double* c, d
 
 cfdg_status cfdg_kernel_stats(cfdg_solver* s, double* ms8, long long* n8, int reset) {
     if (!s) return fail(CFDG_ERR_ARG, "null solver");
-    for (int k = 0; k < 8; ++k) {
+    for (int k = 0; k < 12; ++k) {
         if (ms8) ms8[k] = s->kstat_ms[k];
         if (n8) n8[k] = s->kstat_n[k];
         if (reset) {

@@ -1,0 +1,50 @@
+// Test-only host build of the residual's face function (face.cuh) and its hand-written
+// adjoint (adjoint.cuh), so the adjoint can be checked against finite differences of the
+// same operation sequence on the CPU.  Not part of the library.
+#include "../../mycode_gb300/csrc/adjoint.cuh"
+
+using namespace cfdg;
+
+namespace {
+Flow<double> flow(const double* p, const int* fl) {
+    Flow<double> F;
+    F.gam = p[0]; F.Rgas = p[1]; F.Pr = p[2]; F.nu = p[3]; F.Minf = p[4]; F.P0 = p[5]; F.T0 = p[6]; F.Pexit = p[7];
+    for (int k = 0; k < 4; ++k) { F.fs[k] = p[8 + k]; F.shock[k] = p[12 + k]; }
+    F.k_inf = 0; F.w_inf = 0; F.Pr_t = 0.9;
+    F.bcset = fl[0]; F.flux = fl[1]; F.spatial = fl[2]; F.viscous = fl[3];
+    return F;
+}
+FaceGeo<double> geo(const double* g) {
+    FaceGeo<double> G;
+    G.nx = g[0]; G.ny = g[1]; G.A = g[2]; G.dxL = g[3]; G.dyL = g[4]; G.dxR = g[5]; G.dyR = g[6];
+    G.dxlr = g[7]; G.dylr = g[8];
+    return G;
+}
+CS<double> cs(const Flow<double>& F, const double* U) { return make_cs(F, U[0], U[1], U[2], U[3], U[4], U[5]); }
+}  // namespace
+
+extern "C" {
+
+// fl: bcset, flux, spatial, viscous, interior, tag
+void face_eval(const double* p, const int* fl, const double* g, const double* UL, const double* UR, const double* gL,
+               const double* gR, double phL, double phR, double* out) {
+    Flow<double> F = flow(p, fl);
+    Flux6<double> o = face_flux(F, cs(F, UL), cs(F, UR), fl[4] != 0, fl[5], geo(g), gL, gR, phL, phR);
+    for (int c = 0; c < 6; ++c) out[c] = o.f[c];
+}
+
+void face_adj(const double* p, const int* fl, const double* g, const double* UL, const double* UR, const double* gL,
+              const double* gR, double phL, double phR, const double* FAb, double* ULb, double* URb, double* gLb,
+              double* gRb, double* phb) {
+    Flow<double> F = flow(p, fl);
+    CS<double> L = cs(F, UL), Rn = cs(F, UR);
+    CSb<double> Lb = csb_zero<double>(), Rb = csb_zero<double>();
+    for (int q = 0; q < 10; ++q) { gLb[q] = 0; gRb[q] = 0; }
+    phb[0] = phb[1] = 0;
+    face_flux_b(F, L, Rn, fl[4] != 0, fl[5], geo(g), gL, gR, phL, phR, FAb, Lb, Rb, gLb, gRb, phb[0], phb[1]);
+    for (int c = 0; c < 6; ++c) { ULb[c] = 0; URb[c] = 0; }
+    cs_back(F, L, Lb, ULb);
+    cs_back(F, Rn, Rb, URb);
+}
+
+}  // extern "C"

@@ -1,0 +1,121 @@
+"""The hand-written adjoint of the face function (mycode_gb300/csrc/adjoint.cuh) against
+central differences of the forward face function (face.cuh), both built for the host
+from the library's own headers by a test-only harness: every flux scheme, spatial order,
+boundary-condition set and tag, with and without the viscous term."""
+import ctypes as C
+import os
+import subprocess
+
+import numpy as np
+import pytest
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+SRC = os.path.join(ROOT, "tests", "adjoint_harness", "face_harness.cpp")
+
+_dp = np.ctypeslib.ndpointer(dtype=np.float64, flags="C_CONTIGUOUS")
+_ip = np.ctypeslib.ndpointer(dtype=np.int32, flags="C_CONTIGUOUS")
+
+
+@pytest.fixture(scope="module")
+def harness(tmp_path_factory):
+    so = str(tmp_path_factory.mktemp("adj") / "face_harness.so")
+    subprocess.check_call(["g++", "-O2", "-std=c++17", "-fPIC", "-shared", "-ffp-contract=off", SRC, "-o", so])
+    lib = C.CDLL(so)
+    lib.face_eval.argtypes = [_dp, _ip, _dp, _dp, _dp, _dp, _dp, C.c_double, C.c_double, _dp]
+    lib.face_adj.argtypes = [_dp, _ip, _dp, _dp, _dp, _dp, _dp, C.c_double, C.c_double, _dp, _dp, _dp, _dp, _dp, _dp]
+    return lib
+
+
+def flow_params(M=0.5, P=101325.0, T=300.0, nu=1.5e-3):
+    g, Rg = 1.4, 287.0
+    fT = 1 + 0.5 * (g - 1) * M * M
+    T0, P0 = T * fT, P * fT ** (g / (g - 1))
+    rho = P / (Rg * T)
+    u = M * np.sqrt(g * Rg * T)
+    fs = [rho, rho * u, 0.0, P / (g - 1) + 0.5 * rho * u * u]
+    return np.array([g, Rg, 0.72, nu, M, P0, T0, P] + fs + fs, dtype=np.float64)
+
+
+def state(rng, rho=1.2, u=170.0, v=20.0, p=101325.0, amp=0.1):
+    r = rho * (1 + amp * rng.uniform(-1, 1))
+    uu = u * (1 + amp * rng.uniform(-1, 1))
+    vv = v + amp * u * rng.uniform(-1, 1)
+    pp = p * (1 + amp * rng.uniform(-1, 1))
+    return np.array([r, r * uu, r * vv, pp / 0.4 + 0.5 * r * (uu * uu + vv * vv), 0.0, 0.0])
+
+
+def check(lib, p, fl, seed, u=170.0, v=20.0):
+    rng = np.random.default_rng(seed)
+    th = rng.uniform(0, 2 * np.pi)
+    g = np.array([np.cos(th), np.sin(th), 0.013, 0.004, -0.003, -0.005, 0.002, -0.009, 0.005])
+    UL, UR = state(rng, u=u, v=v), state(rng, u=u, v=v)
+    scale = np.array([1.0, 100.0, 100.0, 1e5, 1, 1, 1e3, 1e3, 1e3, 1e3])
+    gL = rng.standard_normal(10) * np.array([1, 1, 100, 100, 100, 100, 1e4, 1e4, 10, 10])
+    gR = rng.standard_normal(10) * np.array([1, 1, 100, 100, 100, 100, 1e4, 1e4, 10, 10])
+    phL, phR = rng.uniform(0.2, 0.9), rng.uniform(0.2, 0.9)
+    fl = np.asarray(fl, dtype=np.int32)
+    lam = rng.standard_normal(6)
+    lam[4:] = 0
+    out = np.zeros(6)
+
+    def f(UL_, UR_, gL_, gR_, a, b):
+        lib.face_eval(p, fl, g, UL_, UR_, gL_, gR_, a, b, out)
+        return float(lam @ out)
+
+    ULb, URb, gLb, gRb, phb = np.zeros(6), np.zeros(6), np.zeros(10), np.zeros(10), np.zeros(2)
+    lib.face_adj(p, fl, g, UL, UR, gL, gR, phL, phR, lam.copy(), ULb, URb, gLb, gRb, phb)
+    base = abs(f(UL, UR, gL, gR, phL, phR)) + 1.0
+    gscale = np.array([1, 1, 100, 100, 100, 100, 1e4, 1e4, 10, 10], dtype=float)
+
+    def deriv(fun, x0, h):
+        # central differences at h and h/2 combined by Richardson extrapolation
+        d1 = (fun(x0 + h) - fun(x0 - h)) / (2 * h)
+        d2 = (fun(x0 + h / 2) - fun(x0 - h / 2)) / h
+        return (4 * d2 - d1) / 3
+
+    checks = []
+    for name, vec, adj, n in (("UL", UL, ULb, 4), ("UR", UR, URb, 4), ("gL", gL, gLb, 10), ("gR", gR, gRb, 10)):
+        for k in range(n):
+            h = 1e-4 * (abs(vec[k]) + 1e-3) if name.startswith("U") else 1e-3 * gscale[k]
+
+            def fun(x, name=name, k=k):
+                v = {"UL": UL, "UR": UR, "gL": gL, "gR": gR}
+                w = v[name].copy()
+                w[k] = x
+                v[name] = w
+                return f(v["UL"], v["UR"], v["gL"], v["gR"], phL, phR)
+
+            checks.append((name, k, deriv(fun, vec[k], h), adj[k]))
+    checks.append(("phL", 0, deriv(lambda x: f(UL, UR, gL, gR, x, phR), phL, 1e-3), phb[0]))
+    checks.append(("phR", 0, deriv(lambda x: f(UL, UR, gL, gR, phL, x), phR, 1e-3), phb[1]))
+    for name, k, d, a in checks:
+        tol = 1e-6 * (abs(d) + abs(a)) + 1e-10 * base
+        assert abs(d - a) <= tol, f"{name}[{k}]: fd {d:.10e} adjoint {a:.10e}"
+
+
+FLUXES = [0, 1, 2]
+
+
+@pytest.mark.parametrize("flux", FLUXES)
+@pytest.mark.parametrize("spatial", [0, 1, 2])
+@pytest.mark.parametrize("viscous", [0, 1])
+@pytest.mark.parametrize("seed", [1, 2, 3])
+def test_interior_face_adjoint(harness, flux, spatial, viscous, seed):
+    check(harness, flow_params(), [0, flux, spatial, viscous, 1, 0], seed)
+
+
+@pytest.mark.parametrize("flux", FLUXES)
+@pytest.mark.parametrize("seed", [4, 5])
+def test_supersonic_and_reversed_flow(harness, flux, seed):
+    # wave-speed branches of HLLC / Roe: supersonic both ways and subsonic reversed
+    for u, v in ((600.0, 10.0), (-600.0, 30.0), (-150.0, 60.0), (5.0, 3.0)):
+        check(harness, flow_params(M=2.0), [1, flux, 2, 1, 1, 0], seed, u=u, v=v)
+
+
+@pytest.mark.parametrize("bcset,tags", [(0, [1, 2, 3, 7]), (1, [1, 2, 3, 6, 7]), (2, [1, 2, 3, 4, 5, 7])])
+@pytest.mark.parametrize("flux", FLUXES)
+@pytest.mark.parametrize("viscous", [0, 1])
+def test_boundary_face_adjoint(harness, bcset, tags, flux, viscous):
+    for tag in tags:
+        for seed in (7, 8):
+            check(harness, flow_params(), [bcset, flux, 2, viscous, 0, tag], seed)
