@@ -339,6 +339,22 @@ def ours(args):
     fp64 = {"value": ev64 * nc / t64, "unit": UNIT, "ms_per_step": 1e3 * t64 / args.steps,
             "gmres_iters": [r[1] for r in recs64], "jv": "one-sided FD (reference)"}
 
+    # ---- adjoint / primal cost: FP64 VJP (gradients and limiter recomputed) over one FP64
+    # residual, CUDA-event kernel time on the same state, L2 flushed before each
+    s64.set_timing(True)
+    s64.kernel_stats(reset=True)
+    reps = 20
+    for _ in range(reps):
+        s64.flush_l2(L2_FLUSH_BYTES)
+        s64.residual_device(True)
+        s64.flush_l2(L2_FLUSH_BYTES)
+        s64.vjp_device()
+    st64 = s64.kernel_stats(reset=True)
+    t_res = sum(st64[k][0] for k in st64 if k.startswith("residual.")) / reps
+    t_vjp = sum(st64[k][0] for k in st64 if k.startswith("vjp.")) / reps
+    adjoint = {"ratio": t_vjp / t_res, "residual_ms": t_res, "vjp_ms": t_vjp,
+               "note": "FP64 VJP of the full residual (forward recomputation included) / FP64 residual"}
+
     # ---- CPU baseline: the oracle port on this host, bounded sample
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
@@ -359,6 +375,7 @@ def ours(args):
             "kernels": kern,
             "e2e": e2e,
             "fp64": fp64,
+            "adjoint_over_primal": adjoint,
             "clocks": clocks,
             "cpu_baseline": cpu,
         }

@@ -390,6 +390,9 @@ class Solver:
     def residual_device(self, update_limiters=True):
         _check(lib().cfdg_residual_device(self._h, int(update_limiters)))
 
+    def vjp_device(self):
+        _check(lib().cfdg_vjp_device(self._h))
+
     def synchronize(self):
         _check(lib().cfdg_synchronize(self._h))
 
