@@ -19,8 +19,16 @@ enum { FG_R = 0, FG_U = 2, FG_V = 4, FG_P = 6, FG_T = 8 };
 
 // Ghost or neighbour state of the face: the neighbour when interior, else the ghost of L.
 template <class S, class R>
-CFD_HD CS<S> face_right(const Flow<R>& F, const CS<S>& L, const CS<S>& Rn, bool interior, int tag, R nx, R ny) {
-    return interior ? Rn : ghost_state(F, L, tag, nx, ny);
+CFD_HD CS<S> face_right(const Flow<R>& F, const CS<S>& L, const CS<S>& Rn, bool interior, int tag, R nx, R ny,
+                        R dwall = R(0)) {
+    return interior ? Rn : ghost_state(F, L, tag, nx, ny, dwall);
+}
+
+// normal distance from the owner's centroid to a boundary face (SST wall value of w)
+template <class R>
+CFD_HD R wall_normal_distance(const FaceGeo<R>& g) {
+    R d = g.dxL * g.nx + g.dyL * g.ny;
+    return d < R(0) ? -d : d;
 }
 
 // Second-order reconstruction of one side (src/Solver.cpp:596-623)
@@ -37,12 +45,13 @@ CFD_HD CS<S> reconstruct(const Flow<R>& F, const CS<S>& C, const S* g, S ph, R d
 
 // F*A of one face.  L: owner state; Rn: neighbour state (ignored on the boundary);
 // gL/gR: the owner's / neighbour's 10 gradient values (gR ignored on the boundary);
-// phL/phR: limiter values (used by the limited scheme).
+// phL/phR: limiter values (used by the limited scheme); mutf: face eddy viscosity
+// (SST only; it adds to mu in the stresses and as mu_t Cp / Pr_t to the conductivity).
 template <class S, class R>
 CFD_HD Flux6<S> face_flux(const Flow<R>& F, const CS<S>& L, const CS<S>& Rn, bool interior, int tag,
-                          const FaceGeo<R>& g, const S* gL, const S* gR, S phL, S phR) {
+                          const FaceGeo<R>& g, const S* gL, const S* gR, S phL, S phR, S mutf = S(R(0))) {
     const R nx = g.nx, ny = g.ny;
-    CS<S> Rt = face_right(F, L, Rn, interior, tag, nx, ny);
+    CS<S> Rt = face_right(F, L, Rn, interior, tag, nx, ny, wall_normal_distance(g));
     CS<S> Lr = L, Rr = Rt;
     if (F.spatial != SP_FIRST && interior) {
         S pl = F.spatial == SP_LIMITED ? phL : S(R(0.5));
@@ -99,6 +108,10 @@ CFD_HD Flux6<S> face_flux(const Flow<R>& F, const CS<S>& L, const CS<S>& Rn, boo
         R Cp = F.gam * F.Rgas / (F.gam - R(1.0));
         S mu = rf * F.nu;
         S kc = mu * Cp / F.Pr;
+        if (F.sst) {
+            kc = kc + mutf * Cp / F.Pr_t;
+            mu = mu + mutf;
+        }
         S div = dudx + dvdy;
         S txx = mu * (R(2.0) * dudx - (R(2.0) / R(3.0)) * div);
         S tyy = mu * (R(2.0) * dvdy - (R(2.0) / R(3.0)) * div);

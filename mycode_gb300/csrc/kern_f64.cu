@@ -11,10 +11,12 @@ static void residual_nv(const ResArgs<double>& a) {
     k_prim<double, NV><<<grid_for(nc), 256, 0, a.stream>>>((int)nc, a.F, a.U, a.W);
     if (a.ev) cudaEventRecord(a.ev[1], a.stream);
     k_grad<double, NV><<<grid_for(nc), 256, 0, a.stream>>>(a.m, a.F, a.U, a.W, a.G, a.phi, a.do_limiter);
+    if (NV == 6) k_sst_cell<double, NV><<<grid_for(nc), 256, 0, a.stream>>>(a.m, a.F, a.W, a.G, a.dwall, a.T);
     if (a.ev) cudaEventRecord(a.ev[2], a.stream);
-    k_flux<double, NV><<<grid_for(nf), 256, 0, a.stream>>>(a.m, a.F, a.U, a.W, a.G, a.phi, a.FA);
+    k_flux<double, NV><<<grid_for(nf), 256, 0, a.stream>>>(a.m, a.F, a.U, a.W, a.G, a.phi, a.FA, a.T);
     if (a.ev) cudaEventRecord(a.ev[3], a.stream);
-    k_gather<double, NV><<<grid_for(nc), 256, 0, a.stream>>>(a.m, a.FA.v, a.FA.n, a.out, nc, a.diag_v, a.dt);
+    k_gather<double, NV><<<grid_for(nc), 256, 0, a.stream>>>(a.m, a.FA.v, a.FA.n, a.out, nc, a.diag_v, a.dt,
+                                                           NV == 6 ? a.T.v + 2 * nc : nullptr);
     if (a.ev) cudaEventRecord(a.ev[4], a.stream);
 }
 
@@ -92,9 +94,9 @@ void launch_precond(int nv, const MeshView<double>& m, const Flow<double>& F, co
                     const double* dt, double* D, cudaStream_t s) {
     NV_SWITCH(nv, (k_precond<NVC><<<grid_for(m.nc), 256, 0, s>>>(m, F, U, W, dt, D)));
 }
-void launch_newton_update(int nv, long nc, double* U, const double* dU, double relax, double gam, int* bad,
+void launch_newton_update(int nv, long nc, double* U, const double* dU, double relax, double gam, double wmin, int* bad,
                           cudaStream_t s) {
-    NV_SWITCH(nv, (k_newton_update<NVC><<<grid_for(nc), 256, 0, s>>>(nc, U, dU, relax, gam, bad)));
+    NV_SWITCH(nv, (k_newton_update<NVC><<<grid_for(nc), 256, 0, s>>>(nc, U, dU, relax, gam, wmin, bad)));
 }
 
 // ---- device-resident GMRES

@@ -14,10 +14,12 @@ static void jv_nv(const ResArgs<R>& a) {
     k_prim<S, NV><<<grid_for(nc), 256, 0, a.stream>>>((int)nc, a.F, a.U, a.W);
     if (a.ev) cudaEventRecord(a.ev[1], a.stream);
     k_grad<S, NV><<<grid_for(nc), 256, 0, a.stream>>>(a.m, a.F, a.U, a.W, a.G, a.phi, 0);
+    if (NV == 6) k_sst_cell<S, NV><<<grid_for(nc), 256, 0, a.stream>>>(a.m, a.F, a.W, a.G, a.dwall, a.T);
     if (a.ev) cudaEventRecord(a.ev[2], a.stream);
-    k_flux<S, NV><<<grid_for(nf), 256, 0, a.stream>>>(a.m, a.F, a.U, a.W, a.G, a.phi, a.FA);
+    k_flux<S, NV><<<grid_for(nf), 256, 0, a.stream>>>(a.m, a.F, a.U, a.W, a.G, a.phi, a.FA, a.T);
     if (a.ev) cudaEventRecord(a.ev[3], a.stream);
-    k_gather<R, NV><<<grid_for(nc), 256, 0, a.stream>>>(a.m, a.FA.d, a.FA.n, a.out, nc, a.diag_v, a.dt);
+    k_gather<R, NV><<<grid_for(nc), 256, 0, a.stream>>>(a.m, a.FA.d, a.FA.n, a.out, nc, a.diag_v, a.dt,
+                                                         NV == 6 ? a.T.d + 2 * nc : nullptr);
     if (a.ev) cudaEventRecord(a.ev[4], a.stream);
 }
 

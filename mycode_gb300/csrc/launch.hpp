@@ -23,6 +23,8 @@ struct ResArgs {
     const R* dt;
     cudaStream_t stream;
     cudaEvent_t* ev;        // optional 5 events around the four kernels
+    Field<R> T{nullptr, nullptr, 0};  // SST cell terms (mu_t, F1, S_k vol, S_w vol); nv = 6 only
+    const R* dwall = nullptr;         // wall distance per cell; nv = 6 only
 };
 
 // R(U) (kern_f64.cu for double, kern_f32.cu for float)
@@ -57,7 +59,7 @@ void launch_local_dt(int nv, const MeshView<double>& m, const Flow<double>& F, c
                      double cfl, double* dt, cudaStream_t s);
 void launch_precond(int nv, const MeshView<double>& m, const Flow<double>& F, const double* U, const double* W,
                     const double* dt, double* D, cudaStream_t s);
-void launch_newton_update(int nv, long nc, double* U, const double* dU, double relax, double gam, int* bad,
+void launch_newton_update(int nv, long nc, double* U, const double* dU, double relax, double gam, double wmin, int* bad,
                           cudaStream_t s);
 
 inline unsigned grid_for(long n, int threads = 256) { return (unsigned)((n + threads - 1) / threads); }

@@ -279,11 +279,11 @@ __global__ void k_precond(MeshView<double> m, Flow<double> F, const double* __re
     D[i] = d;
 }
 
-// Newton update with the positivity clamps of src/Solver.cpp:1760-1778; flags a
-// non-finite state in *bad (bit 0) without stopping.
+// Newton update with the positivity clamps of src/Solver.cpp:1760-1778 (and, for SST,
+// k >= 0 and w >= wmin); flags a non-finite state in *bad (bit 0) without stopping.
 template <int NV>
 __global__ void k_newton_update(long nc, double* __restrict__ U, const double* __restrict__ dU, double relax,
-                                double gam, int* bad) {
+                                double gam, double wmin, int* bad) {
     long i = (long)blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= nc) return;
     double u[NV];
@@ -295,6 +295,10 @@ __global__ void k_newton_update(long nc, double* __restrict__ U, const double* _
     if (pn < 1e-5) {
         pn = 1e-5;
         u[3] = pn / (gam - 1.0) + ke;
+    }
+    if constexpr (NV == 6) {
+        if (u[4] < 0.0) u[4] = 0.0;
+        if (u[5] < u[0] * wmin) u[5] = u[0] * wmin;
     }
     bool ok = true;
 #pragma unroll

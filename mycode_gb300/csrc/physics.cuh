@@ -13,6 +13,7 @@ namespace cfdg {
 using ::sqrt;
 using ::fabs;
 using ::pow;
+using ::tanh;
 
 enum FluxScheme { FLUX_LLF = 0, FLUX_ROE = 1, FLUX_HLLC = 2, FLUX_AUSM = 3 };
 enum SpatialScheme { SP_FIRST = 0, SP_CENTRAL = 1, SP_LIMITED = 2 };
@@ -35,6 +36,7 @@ struct Flow {
     // SST (no reference counterpart; parity unpinned)
     R k_inf, w_inf, Pr_t;
     int bcset, flux, spatial, viscous;
+    int sst;    // 1: the state carries rhok, rhow (SST)
 };
 
 // Conservative state with its derived primitives u, v, p (reference formulas).
@@ -212,8 +214,30 @@ CFD_HD CS<S> const_state(const Flow<R>& F, const R* s4) {
 // (:973-1011), laminar-plate / SWBLI set (:1088-1139).  Tag 6 (post-shock inflow)
 // has no reference counterpart.  For the SST variables the turbulent far field and
 // wall values follow the SST model's boundary rules (parity unpinned).
+// With SST (F.sst) the turbulence variables of the ghost are set by the model's rules
+// instead of the reference's zeros: free stream at inflow and far-field tags,
+// extrapolation at the pressure outlet, and at a no-slip wall k_face = 0 and
+// w_face = 60 nu / (beta1 d^2) with d = dwall, the normal distance of the wall face.
 template <class S, class R>
-CFD_HD CS<S> ghost_state(const Flow<R>& F, const CS<S>& U, int tag, R nx, R ny) {
+CFD_HD CS<S> sst_ghost(const Flow<R>& F, CS<S> g, const CS<S>& U, int kind, R dwall) {
+    if (!F.sst) return g;
+    if (kind == 0) {          // free stream
+        g.rk = g.r * F.k_inf;
+        g.rw = g.r * F.w_inf;
+    } else if (kind == 1) {   // extrapolate the specific values
+        g.rk = g.r * (U.rk / U.r);
+        g.rw = g.r * (U.rw / U.r);
+    } else {                  // no-slip wall
+        R d = dwall > R(1e-30) ? dwall : R(1e-30);
+        R ww = R(60.0) * F.nu / (R(0.075) * d * d);
+        g.rk = -g.r * (U.rk / U.r);
+        g.rw = g.r * (R(2.0) * ww - U.rw / U.r);
+    }
+    return g;
+}
+
+template <class S, class R>
+CFD_HD CS<S> ghost_state(const Flow<R>& F, const CS<S>& U, int tag, R nx, R ny, R dwall = R(0)) {
     const R g = F.gam;
     if (F.bcset == BC_BUMP) {
         if (tag == 1) {
@@ -223,18 +247,18 @@ CFD_HD CS<S> ghost_state(const Flow<R>& F, const CS<S>& U, int tag, R nx, R ny) 
             R Cp = g * F.Rgas / (g - R(1.0));
             S V2 = R(2.0) * Cp * (F.T0 - Tg);
             S V = (val(V2) > R(0)) ? sqrt(V2) : S(R(0.0));
-            return p2c(F, rg, V, S(R(0.0)), pu, S(R(0)), S(R(0)));
+            return sst_ghost(F, p2c(F, rg, V, S(R(0.0)), pu, S(R(0)), S(R(0))), U, 0, dwall);
         } else if (tag == 2) {
-            return p2c(F, U.r, U.u, U.v, S(F.Pexit), S(R(0)), S(R(0)));
+            return sst_ghost(F, p2c(F, U.r, U.u, U.v, S(F.Pexit), S(R(0)), S(R(0))), U, 1, dwall);
         } else if (tag == 3) {
             return slip_ghost(F, U, nx, ny);
         }
         return U;
     } else if (F.bcset == BC_SUPERSONIC) {
-        if (tag == 1) return const_state<S>(F, F.fs);
+        if (tag == 1) return sst_ghost(F, const_state<S>(F, F.fs), U, 0, dwall);
         if (tag == 2) return U;
         if (tag == 3) return slip_ghost(F, U, nx, ny);
-        if (tag == 6) return const_state<S>(F, F.shock);
+        if (tag == 6) return sst_ghost(F, const_state<S>(F, F.shock), U, 0, dwall);
         return U;
     } else {
         if (tag == 1 || tag == 5) {
@@ -257,7 +281,7 @@ CFD_HD CS<S> ghost_state(const Flow<R>& F, const CS<S>& U, int tag, R nx, R ny) 
             S pin = (g - R(1.0)) * (U.rE - ek);
             S Tin = pin / (U.r * F.Rgas);
             S rg = pin / (F.Rgas * Tin);
-            return p2c(F, rg, ug, vg, pin, S(R(0)), S(R(0)));
+            return sst_ghost(F, p2c(F, rg, ug, vg, pin, S(R(0)), S(R(0))), U, 2, dwall);
         }
         return U;
     }

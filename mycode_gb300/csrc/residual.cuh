@@ -15,6 +15,7 @@
 #pragma once
 #include <cuda_runtime.h>
 #include "face.cuh"
+#include "sst.cuh"
 
 namespace cfdg {
 
@@ -147,7 +148,8 @@ __global__ void __launch_bounds__(256) k_grad(MeshView<R> m, Flow<R> F, Field<R>
             for (int q = 0; q < NQ; ++q) wj[q] = Acc<S>::ld(W, q, j);
         } else {
             CS<S> Ui = load_cs<S, NV>(U, W, i);
-            CS<S> g = ghost_state(F, Ui, m.ftag[f], nx, ny);
+            R dn = m.dxo[f] * nx + m.dyo[f] * ny;
+            CS<S> g = ghost_state(F, Ui, m.ftag[f], nx, ny, dn < R(0) ? -dn : dn);
             wj[W_R] = g.r;
             wj[W_U] = g.u;
             wj[W_V] = g.v;
@@ -236,9 +238,26 @@ __device__ __forceinline__ FaceGeo<R> load_geo(const MeshView<R>& m, long f) {
     return g;
 }
 
+// SST cell terms (sst.cuh): T planes 0 mu_t, 1 F1, 2 S_k vol, 3 S_w vol
+template <class S, int NV, class R>
+__global__ void __launch_bounds__(256) k_sst_cell(MeshView<R> m, Flow<R> F, Field<R> W, Field<R> G,
+                                                  const R* __restrict__ dwall, Field<R> T) {
+    long i = (long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= m.nc) return;
+    SstCell<S> c = sst_cell(F, Acc<S>::ld(W, W_R, i), Acc<S>::ld(W, W_K, i), Acc<S>::ld(W, W_W, i),
+                            Acc<S>::ld(G, G_U, i), Acc<S>::ld(G, G_U + 1, i), Acc<S>::ld(G, G_V, i),
+                            Acc<S>::ld(G, G_V + 1, i), Acc<S>::ld(G, G_K, i), Acc<S>::ld(G, G_K + 1, i),
+                            Acc<S>::ld(G, G_W, i), Acc<S>::ld(G, G_W + 1, i), dwall[i]);
+    R vol = m.vol[i];
+    Acc<S>::st(T, 0, i, c.mut);
+    Acc<S>::st(T, 1, i, c.F1);
+    Acc<S>::st(T, 2, i, c.Sk * vol);
+    Acc<S>::st(T, 3, i, c.Sw * vol);
+}
+
 template <class S, int NV, class R>
 __global__ void __launch_bounds__(256) k_flux(MeshView<R> m, Flow<R> F, Field<R> U, Field<R> W, Field<R> G,
-                                              const R* __restrict__ phi, Field<R> FA) {
+                                              const R* __restrict__ phi, Field<R> FA, Field<R> T) {
     long f = (long)blockIdx.x * blockDim.x + threadIdx.x;
     if (f >= m.nf) return;
     int o = m.fo[f], n = m.fn[f];
@@ -260,6 +279,32 @@ __global__ void __launch_bounds__(256) k_flux(MeshView<R> m, Flow<R> F, Field<R>
         phL = S(phi[o]);
         phR = S(phi[n]);
     }
+    if (NV == 6) {
+        // SST: face eddy viscosity in the mean-flow stresses, then the k and w fluxes
+        bool wall = !interior && tag == 4;
+        S mutL = Acc<S>::ld(T, 0, o), F1L = Acc<S>::ld(T, 1, o);
+        S mutR = interior ? Acc<S>::ld(T, 0, n) : mutL, F1R = interior ? Acc<S>::ld(T, 1, n) : F1L;
+        S mutf = wall ? S(R(0)) : R(0.5) * (mutL + mutR);
+        S F1f = R(0.5) * (F1L + F1R);
+        Flux6<S> out = face_flux(F, L, Rn, interior, tag, g, gL, gR, phL, phR, mutf);
+        CS<S> Rt = face_right(F, L, Rn, interior, tag, g.nx, g.ny, wall_normal_distance(g));
+        S gkL[4] = {Acc<S>::ld(G, G_K, o), Acc<S>::ld(G, G_K + 1, o), Acc<S>::ld(G, G_W, o), Acc<S>::ld(G, G_W + 1, o)};
+        S gkR[4] = {gkL[0], gkL[1], gkL[2], gkL[3]};
+        if (interior) {
+            gkR[0] = Acc<S>::ld(G, G_K, n);
+            gkR[1] = Acc<S>::ld(G, G_K + 1, n);
+            gkR[2] = Acc<S>::ld(G, G_W, n);
+            gkR[3] = Acc<S>::ld(G, G_W + 1, n);
+        }
+        S Fk, Fw;
+        sst_face_flux(F, out.f[0], L.rk / L.r, L.rw / L.r, Rt.rk / Rt.r, Rt.rw / Rt.r, R(0.5) * (L.r + Rt.r), mutf,
+                      F1f, gkL, gkR, wall, g.nx, g.ny, g.A, g.dxL, g.dyL, g.dxlr, g.dylr, Fk, Fw);
+        out.f[4] = Fk;
+        out.f[5] = Fw;
+#pragma unroll
+        for (int c = 0; c < 6; ++c) Acc<S>::st(FA, c, f, out.f[c]);
+        return;
+    }
     Flux6<S> out = face_flux(F, L, Rn, interior, tag, g, gL, gR, phL, phR);
 #pragma unroll
     for (int c = 0; c < NV; ++c) Acc<S>::st(FA, c, f, out.f[c]);
@@ -272,7 +317,8 @@ __global__ void __launch_bounds__(256) k_flux(MeshView<R> m, Flow<R> F, Field<R>
 template <class R, int NV>
 __global__ void __launch_bounds__(256) k_gather(MeshView<R> m, const R* __restrict__ FA, long fa_stride,
                                                 R* __restrict__ Rout, long r_stride,
-                                                const R* __restrict__ diag_v, const R* __restrict__ dt) {
+                                                const R* __restrict__ diag_v, const R* __restrict__ dt,
+                                                const R* __restrict__ src) {
     long i = (long)blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= m.nc) return;
     R acc[NV];
@@ -289,6 +335,13 @@ __global__ void __launch_bounds__(256) k_gather(MeshView<R> m, const R* __restri
         } else {
 #pragma unroll
             for (int c = 0; c < NV; ++c) acc[c] = acc[c] + FA[c * fa_stride + f];
+        }
+    }
+    if constexpr (NV == 6) {
+        // SST sources (times the cell volume): R = sum of fluxes - S vol
+        if (src) {
+            acc[4] = acc[4] - src[i];
+            acc[5] = acc[5] - src[r_stride + i];
         }
     }
     if (diag_v) {

@@ -112,6 +112,9 @@ struct cfdg_solver {
     double *Ub = nullptr, *Rb = nullptr, *Up = nullptr, *Rp = nullptr, *vtmp = nullptr, *x = nullptr, *rhs = nullptr;
     // dual (exact J v) work, FP64
     double *Wj = nullptr, *Wjd = nullptr, *Gj = nullptr, *Gjd = nullptr, *FAjd = nullptr;
+    // SST (nv = 6): cell terms (mu_t, F1, S_k vol, S_w vol) and the wall distance
+    double *Tt = nullptr, *Tj = nullptr, *Tjd = nullptr, *dwall = nullptr;
+    float *T32 = nullptr, *T32d = nullptr, *dwall32 = nullptr;
     // FP32 (mixed precision) work
     float *U32 = nullptr, *W32 = nullptr, *W32d = nullptr, *G32 = nullptr, *G32d = nullptr, *FA32d = nullptr,
           *phi32 = nullptr, *dt32 = nullptr, *V32 = nullptr, *z32 = nullptr;
@@ -224,14 +227,22 @@ struct cfdg_solver {
         F.fs[3] = rE;
         for (int k = 0; k < 4; ++k) F.shock[k] = F.fs[k];
         if (cfg.shock_deflection_deg > 0.0 && M > 1.0) post_shock(F.shock, rho, u, Pexit, g);
+        F.sst = nv == 6 ? 1 : 0;
         F.k_inf = 0;
         F.w_inf = 0;
+        if (F.sst) {
+            // k = 1.5 (Tu U)^2, w = k / (nu mu_t/mu) from the configured intensity and ratio
+            double kk, ww;
+            sst_freestream(cfg.turb_intensity, cfg.mut_ratio, u, nu, kk, ww);
+            F.k_inf = kk;
+            F.w_inf = ww;
+        }
         F.Pr_t = 0.9;
         Ff.gam = (float)F.gam; Ff.Rgas = (float)F.Rgas; Ff.Pr = (float)F.Pr; Ff.nu = (float)F.nu;
         Ff.Minf = (float)F.Minf; Ff.P0 = (float)F.P0; Ff.T0 = (float)F.T0; Ff.Pexit = (float)F.Pexit;
         for (int k = 0; k < 4; ++k) { Ff.fs[k] = (float)F.fs[k]; Ff.shock[k] = (float)F.shock[k]; }
         Ff.k_inf = (float)F.k_inf; Ff.w_inf = (float)F.w_inf; Ff.Pr_t = (float)F.Pr_t;
-        Ff.bcset = F.bcset; Ff.flux = F.flux; Ff.spatial = F.spatial; Ff.viscous = F.viscous;
+        Ff.bcset = F.bcset; Ff.flux = F.flux; Ff.spatial = F.spatial; Ff.viscous = F.viscous; Ff.sst = F.sst;
     }
 
     // state behind an oblique shock of deflection theta (theta-beta-M relation, weak branch)
@@ -268,6 +279,8 @@ struct cfdg_solver {
         a.W = f64(W);
         a.G = f64(G);
         a.FA = ff64(FA);
+        a.T = f64(Tt);
+        a.dwall = dwall;
         a.phi = phi;
         a.out = out;
         a.do_limiter = do_lim;
@@ -334,6 +347,8 @@ struct cfdg_solver {
             a.W = f64(Wj, Wjd);
             a.G = f64(Gj, Gjd);
             a.FA = ff64(nullptr, FAjd);
+            a.T = f64(Tj, Tjd);
+            a.dwall = dwall;
             a.phi = phi;
             a.out = out;
             a.do_limiter = 0;
@@ -385,6 +400,7 @@ struct cfdg_solver {
     }
 
     cfdg_status vjp_dev(double* Uin, double* lam, double* gout) {
+        if (nv == 6) return fail(CFDG_ERR_UNSUPPORTED, "the adjoint does not cover the SST terms yet");
         TRY(ensure_adj());
         ResArgs<double> a = res64(Uin, nullptr, 0);
         a.phi = phi_adj;
@@ -432,6 +448,8 @@ struct cfdg_solver {
             a.W = f32(W32, W32d);
             a.G = f32(G32, G32d);
             a.FA = ff32(nullptr, FA32d);
+            a.T = f32(T32, T32d);
+            a.dwall = dwall32;
             a.phi = phi32;
             a.out = w32;
             a.do_limiter = 0;
@@ -620,6 +638,8 @@ struct cfdg_solver {
                 a.W = f32(W32, W32d);
                 a.G = f32(G32, G32d);
                 a.FA = ff32(nullptr, FA32d);
+                a.T = f32(T32, T32d);
+                a.dwall = dwall32;
                 a.phi = phi32;
                 a.out = Vj1;
                 a.do_limiter = 0;
@@ -761,7 +781,7 @@ struct cfdg_solver {
         if (resVM > 1e6) relax = 0.5;
         else if (resVM > 2e3 && resVM < 1e2) relax = 0.9;
         CK(cudaMemsetAsync(bad, 0, sizeof(int), st));
-        launch_newton_update(nv, nc, U, x, relax, cfg.gamma, bad, st);
+        launch_newton_update(nv, nc, U, x, relax, cfg.gamma, F.w_inf * SstConst::w_min_frac, bad, st);
         ++launches;
         int hbad = 0;
         CK(cudaMemcpyAsync(&hbad, bad, sizeof(int), cudaMemcpyDeviceToHost, st));
@@ -780,6 +800,8 @@ struct cfdg_solver {
     }
 
     void release() {
+        void* pt[] = {Tt, Tj, Tjd, dwall, T32, T32d, dwall32};
+        for (void* p : pt) cudaFree(p);
         void* ps[] = {cf, fo, fn, ftag, perm, U, W, G, phi, FA, R, dt, D, stage, Ub, Rb, Up, Rp, vtmp, x, rhs,
                       Wj, Wjd, Gj, Gjd, FAjd, U32, W32, W32d, G32, G32d, FA32d, phi32, dt32, V32, z32, V, z,
                       rs.partial, rs.counter, scal, bad};
@@ -923,7 +945,8 @@ cfdg_status cfdg_solver_create(const cfdg_mesh* m, const cfdg_config* cfg, cfdg_
         return fail(CFDG_ERR_ARG, "the graph Krylov driver supports gmres_m <= 128");
     if (c.flux < 0 || c.flux > 3 || c.spatial < 0 || c.spatial > 2 || c.bcset < 0 || c.bcset > 2)
         return fail(CFDG_ERR_ARG, "unknown flux, spatial scheme or boundary-condition set");
-    if (c.turbulence != CFDG_TURB_NONE) return fail(CFDG_ERR_UNSUPPORTED, "SST is not built into this library yet");
+    if (c.turbulence != CFDG_TURB_NONE && c.turbulence != CFDG_TURB_SST) return fail(CFDG_ERR_ARG, "unknown turbulence model");
+    if (c.turbulence == CFDG_TURB_SST && !c.viscous) return fail(CFDG_ERR_ARG, "SST needs the viscous term (viscous = 1)");
     int ndev = 0;
     if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) {
         cudaGetLastError();
@@ -987,6 +1010,31 @@ cfdg_status cfdg_solver_create(const cfdg_mesh* m, const cfdg_config* cfg, cfdg_
     TRYS(dalloc(&s->Wj, (size_t)NW * nc)); TRYS(dalloc(&s->Wjd, (size_t)NW * nc));
     TRYS(dalloc(&s->Gj, (size_t)NG * nc)); TRYS(dalloc(&s->Gjd, (size_t)NG * nc));
     TRYS(dalloc(&s->FAjd, (size_t)nv * nf));
+    if (nv == 6) {
+        TRYS(dalloc(&s->Tt, 4 * (size_t)nc)); TRYS(dalloc(&s->Tj, 4 * (size_t)nc)); TRYS(dalloc(&s->Tjd, 4 * (size_t)nc));
+        TRYS(dalloc(&s->dwall, (size_t)nc)); TRYS(dalloc(&s->dwall32, (size_t)nc));
+        TRYS(dalloc(&s->T32, 4 * (size_t)nc)); TRYS(dalloc(&s->T32d, 4 * (size_t)nc));
+        // distance from each cell centroid to the nearest no-slip wall face midpoint
+        // (computeWallDistances, src/Solver.cpp:1981-2015); 1e10 without walls
+        std::vector<double> wx, wy;
+        for (int f = 0; f < h.n_faces; ++f)
+            if (h.f_n[f] < 0 && h.f_tag[f] == 4) { wx.push_back(h.f_xm[f]); wy.push_back(h.f_ym[f]); }
+        std::vector<double> d(nc, 1e10);
+        std::vector<float> d32(nc);
+        for (int i = 0; i < nc; ++i) {
+            double best = 1e20;
+            for (size_t w = 0; w < wx.size(); ++w) {
+                double dx = h.xc[i] - wx[w], dy = h.yc[i] - wy[w];
+                double d2 = dx * dx + dy * dy;
+                if (d2 < best) best = d2;
+            }
+            if (!wx.empty()) d[i] = std::sqrt(best);
+            d32[i] = (float)d[i];
+        }
+        if (cudaMemcpy(s->dwall, d.data(), sizeof(double) * nc, cudaMemcpyHostToDevice) != cudaSuccess ||
+            cudaMemcpy(s->dwall32, d32.data(), sizeof(float) * nc, cudaMemcpyHostToDevice) != cudaSuccess)
+            return bail(fail(CFDG_ERR_CUDA, "wall distance upload failed"));
+    }
     if (c.precision == CFDG_MIXED) {
         TRYS(dalloc(&s->U32, L)); TRYS(dalloc(&s->W32, (size_t)NW * nc)); TRYS(dalloc(&s->W32d, (size_t)NW * nc));
         TRYS(dalloc(&s->G32, (size_t)NG * nc)); TRYS(dalloc(&s->G32d, (size_t)NG * nc));
@@ -1096,8 +1144,13 @@ cfdg_status cfdg_initialize(cfdg_solver* s) {
         for (int k = 0; k < 4; ++k) st4[k] = s->F.fs[k];
     }
     std::vector<double> U(6 * (size_t)s->nc, 0.0);
-    for (int i = 0; i < s->nc; ++i)
+    for (int i = 0; i < s->nc; ++i) {
         for (int k = 0; k < 4; ++k) U[6 * (size_t)i + k] = st4[k];
+        if (s->nv == 6) {
+            U[6 * (size_t)i + 4] = st4[0] * s->F.k_inf;
+            U[6 * (size_t)i + 5] = st4[0] * s->F.w_inf;
+        }
+    }
     return cfdg_set_state(s, U.data());
 }
 

@@ -988,3 +988,302 @@ double om_entropy_error(const om_solver* s) {
     }
     return sqrt(se / tv);
 }
+
+/* ------------------------------------------------------------------ SST (parity unpinned)
+ * Menter SST, 2003 variant, as restated from the published model (Menter, Kuntz & Langtry
+ * 2003; the "SST-2003" form of the NASA Turbulence Modeling Resource).  The reference has
+ * only scaffolding for it (include/Types.hpp:63-68, src/Solver.cpp:1981-2015), so these
+ * functions follow the model, not reference code:
+ *   mu_t = rho a1 k / max(a1 w, S F2);  P = min(mu_t S^2, 10 beta* rho k w)
+ *   S_k = P - beta* rho w k
+ *   S_w = gamma rho / mu_t P - beta rho w^2 + 2 (1 - F1) rho sigma_w2 grad k . grad w / w
+ * k and w are advected first-order upwind with the Riemann mass flux and diffused with
+ * (mu + sigma mu_t); mu_t enters the mean-flow stresses and, over Pr_t = 0.9, the heat flux.
+ * Boundary values: free stream at inflow / far field, extrapolation at the pressure outlet
+ * and the slip wall, k = 0 and w = 60 nu / (0.075 d^2) at a no-slip wall face. */
+
+static const double SST_BS = 0.09, SST_A1 = 0.31;
+static const double SST_SK1 = 0.85, SST_SW1 = 0.5, SST_B1 = 0.075, SST_G1 = 5.0 / 9.0;
+static const double SST_SK2 = 1.0, SST_SW2 = 0.856, SST_B2 = 0.0828, SST_G2 = 0.44;
+
+typedef struct {
+    const om_mesh* mesh; /* the mesh and settings the arrays below were built for */
+    double Tu, ratio, nu;
+    double k_inf, w_inf, w_min;
+    double* dwall; /* per cell */
+    double* g14;   /* gradients of rho, u, v, p, T, k, w */
+    double* mut;
+    double* F1;
+    double* Sk;
+    double* Sw;
+} om_sst;
+
+static om_sst g_sst;
+
+/* distance from each centroid to the nearest no-slip wall face midpoint (the brute force
+ * of computeWallDistances, src/Solver.cpp:1981-2015) */
+static void sst_setup(om_solver* s, double Tu, double ratio) {
+    const om_mesh* m = s->m;
+    int n = m->n_cells;
+    free(g_sst.dwall); free(g_sst.g14); free(g_sst.mut); free(g_sst.F1); free(g_sst.Sk); free(g_sst.Sw);
+    g_sst.mesh = m;
+    g_sst.Tu = Tu;
+    g_sst.ratio = ratio;
+    g_sst.nu = s->nu;
+    g_sst.dwall = (double*)malloc(sizeof(double) * n);
+    g_sst.g14 = (double*)calloc((size_t)14 * n, sizeof(double));
+    g_sst.mut = (double*)malloc(sizeof(double) * n);
+    g_sst.F1 = (double*)malloc(sizeof(double) * n);
+    g_sst.Sk = (double*)malloc(sizeof(double) * n);
+    g_sst.Sw = (double*)malloc(sizeof(double) * n);
+    for (int i = 0; i < n; ++i) {
+        double best = 1e20;
+        int any = 0;
+        for (int f = 0; f < m->n_faces; ++f)
+            if (m->neighbor[f] < 0 && m->tag[f] == 4) {
+                double dx = m->xc[i] - m->xm[f], dy = m->yc[i] - m->ym[f];
+                double d2 = dx * dx + dy * dy;
+                if (d2 < best) best = d2;
+                any = 1;
+            }
+        g_sst.dwall[i] = any ? sqrt(best) : 1e10;
+    }
+    double g = s->gamma, M = s->M_inf;
+    double fT = 1.0 + 0.5 * (g - 1.0) * M * M;
+    double Ts = s->T0 / fT;
+    double U = M * sqrt(g * s->R_gas * Ts);
+    g_sst.k_inf = 1.5 * (Tu * U) * (Tu * U);
+    g_sst.w_inf = g_sst.k_inf / (ratio * s->nu);
+    g_sst.w_min = g_sst.w_inf * 1e-6;
+}
+
+static st_t ghost_sst(const om_solver* s, st_t U, int f) {
+    const om_mesh* m = s->m;
+    st_t gs = ghost(s, U, f);
+    int tag = m->tag[f];
+    int kind = -1; /* 0 free stream, 1 extrapolate, 2 no-slip wall, -1 keep */
+    if (s->bcset == BC_BUMP) kind = tag == 1 ? 0 : tag == 2 ? 1 : -1;
+    else if (s->bcset == BC_SUPERSONIC) kind = (tag == 1 || tag == 6) ? 0 : -1;
+    else kind = (tag == 1 || tag == 5 || tag == 6) ? 0 : tag == 4 ? 2 : -1;
+    if (kind == 0) {
+        gs.rk = gs.r * g_sst.k_inf;
+        gs.rw = gs.r * g_sst.w_inf;
+    } else if (kind == 1) {
+        gs.rk = gs.r * (U.rk / U.r);
+        gs.rw = gs.r * (U.rw / U.r);
+    } else if (kind == 2) {
+        int o = m->owner[f];
+        double dn = fabs((m->xm[f] - m->xc[o]) * m->nx[f] + (m->ym[f] - m->yc[o]) * m->ny[f]);
+        if (dn < 1e-30) dn = 1e-30;
+        double ww = 60.0 * s->nu / (0.075 * dn * dn);
+        gs.rk = -gs.r * (U.rk / U.r);
+        gs.rw = gs.r * (2.0 * ww - U.rw / U.r);
+    }
+    return gs;
+}
+
+/* face averages of rho, u, v, p, T, k, w summed Green-Gauss style */
+static void sst_gradients(om_solver* s, const double* Uin) {
+    const om_mesh* m = s->m;
+    int n = m->n_cells;
+    double* G = g_sst.g14;
+    memset(G, 0, sizeof(double) * 14 * (size_t)n);
+    for (int f = 0; f < m->n_faces; ++f) {
+        int o = m->owner[f], nb = m->neighbor[f];
+        st_t L = st_load(Uin + NV * o);
+        st_t Rs = nb >= 0 ? st_load(Uin + NV * nb) : ghost_sst(s, L, f);
+        double wl[7] = {L.r, L.ru / L.r, L.rv / L.r, pressure(L), 0, L.rk / L.r, L.rw / L.r};
+        double wr[7] = {Rs.r, Rs.ru / Rs.r, Rs.rv / Rs.r, pressure(Rs), 0, Rs.rk / Rs.r, Rs.rw / Rs.r};
+        wl[4] = wl[3] / (L.r * s->R_gas);
+        wr[4] = wr[3] / (Rs.r * s->R_gas);
+        double nx = m->nx[f], ny = m->ny[f], A = m->area[f];
+        for (int q = 0; q < 7; ++q) {
+            double ph = 0.5 * (wl[q] + wr[q]);
+            G[14 * o + 2 * q] += ph * nx * A;
+            G[14 * o + 2 * q + 1] += ph * ny * A;
+            if (nb >= 0) {
+                G[14 * nb + 2 * q] -= ph * nx * A;
+                G[14 * nb + 2 * q + 1] -= ph * ny * A;
+            }
+        }
+    }
+    for (int i = 0; i < n; ++i)
+        for (int q = 0; q < 14; ++q) G[14 * i + q] /= m->vol[i];
+}
+
+static void sst_cells(om_solver* s, const double* Uin) {
+    int n = s->m->n_cells;
+    for (int i = 0; i < n; ++i) {
+        const double* g = g_sst.g14 + 14 * i;
+        double r = Uin[NV * i];
+        double k = Uin[NV * i + 4] / r, w = Uin[NV * i + 5] / r;
+        double kp = k > 0 ? k : 0.0;
+        double wp = w > g_sst.w_min ? w : g_sst.w_min;
+        double ux = g[2], uy = g[3], vx = g[4], vy = g[5];
+        double kx = g[10], ky = g[11], wx = g[12], wy = g[13];
+        double Sxy = 0.5 * (uy + vx);
+        double S2 = 2.0 * (ux * ux + vy * vy + 2.0 * Sxy * Sxy);
+        double Smag = sqrt(S2 + 1e-30);
+        double d = g_sst.dwall[i] > 1e-30 ? g_sst.dwall[i] : 1e-30;
+        double gkgw = kx * wx + ky * wy;
+        double CD = 2.0 * r * SST_SW2 * gkgw / wp;
+        if (CD < 1e-10) CD = 1e-10;
+        double sk = sqrt(kp + 1e-30);
+        double t1 = sk / (SST_BS * wp * d);
+        double t2 = 500.0 * s->nu / (d * d * wp);
+        double t3 = 4.0 * r * SST_SW2 * kp / (CD * d * d);
+        double arg1 = t1 > t2 ? t1 : t2;
+        if (t3 < arg1) arg1 = t3;
+        double F1 = tanh(arg1 * arg1 * arg1 * arg1);
+        double arg2 = 2.0 * t1 > t2 ? 2.0 * t1 : t2;
+        double F2 = tanh(arg2 * arg2);
+        double den = SST_A1 * wp > Smag * F2 ? SST_A1 * wp : Smag * F2;
+        double mut = r * SST_A1 * kp / den;
+        double beta = F1 * SST_B1 + (1.0 - F1) * SST_B2;
+        double gam = F1 * SST_G1 + (1.0 - F1) * SST_G2;
+        double P = mut * S2;
+        double Pl = 10.0 * SST_BS * r * kp * wp;
+        if (Pl < P) P = Pl;
+        g_sst.mut[i] = mut;
+        g_sst.F1[i] = F1;
+        g_sst.Sk[i] = P - SST_BS * r * wp * kp;
+        g_sst.Sw[i] = gam * r / (mut + 1e-30) * P - beta * r * wp * wp + 2.0 * (1.0 - F1) * r * SST_SW2 * gkgw / wp;
+    }
+}
+
+/* The residual with the SST model (nv = 6).  The mean-flow face flux is the reference's
+ * (reconstruction, Riemann or wall flux, viscous flux) with mu_t added to the viscosity. */
+void om_residual_sst(om_solver* s, const double* Uin, double* Rout, double Tu, double ratio) {
+    const om_mesh* m = s->m;
+    int n = m->n_cells;
+    double g = s->gamma, R = s->R_gas;
+    if (!g_sst.dwall || g_sst.mesh != s->m || g_sst.Tu != Tu || g_sst.ratio != ratio || g_sst.nu != s->nu)
+        sst_setup(s, Tu, ratio);
+    memset(Rout, 0, sizeof(double) * NV * (size_t)n);
+    if (s->spatial == SP_LIMITED) {
+        om_gradients(s, Uin);
+        om_limiters(s, Uin);
+    }
+    sst_gradients(s, Uin);
+    sst_cells(s, Uin);
+    double Cp = g * R / (g - 1.0);
+    const double* G = g_sst.g14;
+    for (int f = 0; f < m->n_faces; ++f) {
+        int o = m->owner[f], nb = m->neighbor[f];
+        double nx = m->nx[f], ny = m->ny[f], A = m->area[f];
+        int tag = m->tag[f];
+        int wall = nb < 0 && tag == 4;
+        st_t L = st_load(Uin + NV * o);
+        st_t Rs = nb >= 0 ? st_load(Uin + NV * nb) : ghost_sst(s, L, f);
+        st_t Lr = L, Rr = Rs;
+        if (s->spatial != SP_FIRST && nb >= 0) {
+            double dxL = m->xm[f] - m->xc[o], dyL = m->ym[f] - m->yc[o];
+            double dxR = m->xm[f] - m->xc[nb], dyR = m->ym[f] - m->yc[nb];
+            const double* gL = G + 14 * o;
+            const double* gR = G + 14 * nb;
+            double phL = s->spatial == SP_LIMITED ? s->phi[o] : 0.5;
+            double phR = s->spatial == SP_LIMITED ? s->phi[nb] : 0.5;
+            double pL = pressure(L), pR = pressure(Rs);
+            double rLf = L.r + phL * (gL[0] * dxL + gL[1] * dyL), pLf = pL + phL * (gL[6] * dxL + gL[7] * dyL);
+            double uLf = L.ru / L.r + phL * (gL[2] * dxL + gL[3] * dyL), vLf = L.rv / L.r + phL * (gL[4] * dxL + gL[5] * dyL);
+            if (rLf < 1e-4) rLf = L.r;
+            if (pLf < 1e-4) pLf = pL;
+            Lr = p2c(s, rLf, uLf, vLf, pLf, 0.0, 0.0);
+            double rRf = Rs.r + phR * (gR[0] * dxR + gR[1] * dyR), pRf = pR + phR * (gR[6] * dxR + gR[7] * dyR);
+            double uRf = Rs.ru / Rs.r + phR * (gR[2] * dxR + gR[3] * dyR), vRf = Rs.rv / Rs.r + phR * (gR[4] * dxR + gR[5] * dyR);
+            if (rRf < 1e-4) rRf = Rs.r;
+            if (pRf < 1e-4) pRf = pR;
+            Rr = p2c(s, rRf, uRf, vRf, pRf, 0.0, 0.0);
+        }
+        st_t FE;
+        if (nb < 0 && (tag == 3 || tag == 4)) {
+            double pw = pressure(Lr);
+            FE = st(0.0, pw * nx, pw * ny, 0.0, 0.0, 0.0);
+        } else {
+            FE = inviscid_flux(Lr, Rr, nx, ny, s->flux);
+        }
+        /* mean-flow viscous flux with mu + mu_t */
+        double mutL = g_sst.mut[o], mutR = nb >= 0 ? g_sst.mut[nb] : mutL;
+        double mutf = wall ? 0.0 : 0.5 * (mutL + mutR);
+        double F1f = 0.5 * (g_sst.F1[o] + (nb >= 0 ? g_sst.F1[nb] : g_sst.F1[o]));
+        const double* gL = G + 14 * o;
+        const double* gR = nb >= 0 ? G + 14 * nb : gL;
+        double rf = 0.5 * (L.r + Rs.r);
+        double uL = L.ru / L.r, vL = L.rv / L.r, uR = Rs.ru / Rs.r, vR = Rs.rv / Rs.r;
+        double uf = 0.5 * (uL + uR), vf = 0.5 * (vL + vR);
+        double dudx, dudy, dvdx, dvdy, dTdx, dTdy;
+        double dxo = m->xm[f] - m->xc[o], dyo = m->ym[f] - m->yc[o];
+        double dxlr = nb >= 0 ? m->xc[nb] - m->xc[o] : 0.0, dylr = nb >= 0 ? m->yc[nb] - m->yc[o] : 0.0;
+        double d2lr = dxlr * dxlr + dylr * dylr;
+        if (wall) {
+            double d2 = dxo * dxo + dyo * dyo;
+            dudx = -uL * dxo / d2; dudy = -uL * dyo / d2; dvdx = -vL * dxo / d2; dvdy = -vL * dyo / d2;
+            dTdx = 0.0; dTdy = 0.0;
+        } else {
+            dudx = 0.5 * (gL[2] + gR[2]); dudy = 0.5 * (gL[3] + gR[3]);
+            dvdx = 0.5 * (gL[4] + gR[4]); dvdy = 0.5 * (gL[5] + gR[5]);
+            dTdx = 0.5 * (gL[8] + gR[8]); dTdy = 0.5 * (gL[9] + gR[9]);
+            if (d2lr > 1e-14) {
+                double cu = (dudx * dxlr + dudy * dylr - (uR - uL)) / d2lr;
+                double cv = (dvdx * dxlr + dvdy * dylr - (vR - vL)) / d2lr;
+                dudx -= cu * dxlr; dudy -= cu * dylr; dvdx -= cv * dxlr; dvdy -= cv * dylr;
+            }
+        }
+        double mu = rf * s->nu + mutf;
+        double kc = rf * s->nu * Cp / s->Pr + mutf * Cp / 0.9;
+        double div = dudx + dvdy;
+        double txx = mu * (2.0 * dudx - (2.0 / 3.0) * div);
+        double tyy = mu * (2.0 * dvdy - (2.0 / 3.0) * div);
+        double txy = mu * (dudy + dvdx);
+        double wx = uf * txx + vf * txy + kc * dTdx, wy = uf * txy + vf * tyy + kc * dTdy;
+        double TF[6];
+        TF[0] = FE.r;
+        TF[1] = FE.ru - (txx * nx + txy * ny);
+        TF[2] = FE.rv - (txy * nx + tyy * ny);
+        TF[3] = FE.rE - (wx * nx + wy * ny);
+        /* k and w: upwind advection with the mass flux, diffusion with mu + sigma mu_t */
+        double mdot = TF[0];
+        double kL = L.rk / L.r, wL = L.rw / L.r, kR = Rs.rk / Rs.r, wR = Rs.rw / Rs.r;
+        double Fk = (mdot > 0 ? mdot * kL : mdot * kR);
+        double Fw = (mdot > 0 ? mdot * wL : mdot * wR);
+        double sk = F1f * SST_SK1 + (1.0 - F1f) * SST_SK2, sw = F1f * SST_SW1 + (1.0 - F1f) * SST_SW2;
+        double dkn, dwn;
+        if (wall) {
+            double d2 = dxo * dxo + dyo * dyo, dn = dxo * nx + dyo * ny;
+            dkn = (0.0 - kL) * dn / d2;
+            dwn = (0.5 * (wL + wR) - wL) * dn / d2;
+        } else {
+            double kx = 0.5 * (gL[10] + gR[10]), ky = 0.5 * (gL[11] + gR[11]);
+            double wxg = 0.5 * (gL[12] + gR[12]), wyg = 0.5 * (gL[13] + gR[13]);
+            if (d2lr > 1e-14) {
+                double ck = (kx * dxlr + ky * dylr - (kR - kL)) / d2lr;
+                double cw = (wxg * dxlr + wyg * dylr - (wR - wL)) / d2lr;
+                kx -= ck * dxlr; ky -= ck * dylr; wxg -= cw * dxlr; wyg -= cw * dylr;
+            }
+            dkn = kx * nx + ky * ny;
+            dwn = wxg * nx + wyg * ny;
+        }
+        double mul = rf * s->nu;
+        TF[4] = Fk - (mul + sk * mutf) * dkn;
+        TF[5] = Fw - (mul + sw * mutf) * dwn;
+        for (int c = 0; c < 6; ++c) {
+            Rout[NV * o + c] += TF[c] * A;
+            if (nb >= 0) Rout[NV * nb + c] -= TF[c] * A;
+        }
+    }
+    for (int i = 0; i < n; ++i) {
+        Rout[NV * i + 4] -= g_sst.Sk[i] * m->vol[i];
+        Rout[NV * i + 5] -= g_sst.Sw[i] * m->vol[i];
+    }
+}
+
+void om_sst_reset(void) {
+    free(g_sst.dwall); free(g_sst.g14); free(g_sst.mut); free(g_sst.F1); free(g_sst.Sk); free(g_sst.Sw);
+    memset(&g_sst, 0, sizeof g_sst);
+}
+
+void om_sst_freestream(om_solver* s, double Tu, double ratio, double* kw) {
+    sst_setup(s, Tu, ratio);
+    kw[0] = g_sst.k_inf;
+    kw[1] = g_sst.w_inf;
+}

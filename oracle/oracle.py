@@ -92,6 +92,9 @@ def _oracle_lib():
             "om_solve_implicit": (C.c_int, [vp, C.c_double, C.c_int, _dp, _dp, _dp, _ip]),
             "om_drag": (C.c_double, [vp]),
             "om_entropy_error": (C.c_double, [vp]),
+            "om_residual_sst": (None, [vp, _dp, _dp, C.c_double, C.c_double]),
+            "om_sst_freestream": (None, [vp, C.c_double, C.c_double, _dp]),
+            "om_sst_reset": (None, []),
         }
         for name, (res, args) in sig.items():
             fn = getattr(lib, name)
@@ -254,6 +257,18 @@ class OracleSolver(_Base):
 
     def entropy_error(self):
         return self._L.om_entropy_error(self._s)
+
+    def residual_sst(self, U, turb_intensity=0.001, mut_ratio=0.01):
+        """Residual of the mean flow plus the SST k and w equations (nv = 6, AoS)."""
+        R = np.zeros(6 * self.n_cells)
+        self._L.om_residual_sst(self._s, np.ascontiguousarray(U, np.float64).ravel(), R, float(turb_intensity),
+                                float(mut_ratio))
+        return R.reshape(-1, 6)
+
+    def sst_freestream(self, turb_intensity=0.001, mut_ratio=0.01):
+        kw = np.zeros(2)
+        self._L.om_sst_freestream(self._s, float(turb_intensity), float(mut_ratio), kw)
+        return float(kw[0]), float(kw[1])
 
 
 def ref_available(variant: str = "bump") -> bool:

@@ -1,0 +1,118 @@
+"""SST residual (nv = 6) on the GPU against the oracle's SST restatement, the exact
+(dual-number) J v of the SST residual against central differences, and a short
+mixed-precision solve of a turbulent plate.
+
+The SST terms have no reference counterpart, so their parity is to the oracle's
+independent restatement of the model, within round-off (the two order their
+floating-point operations differently): 1e-10 of each row's largest entry.
+"""
+import numpy as np
+import pytest
+
+import cases as C
+from mycode_gb300 import meshgen as mg
+from oracle.oracle import OracleSolver
+
+pytestmark = pytest.mark.gpu
+
+REL_SST = 1e-10
+
+SST_CASES = {
+    "plate": dict(C.CASES["plate_visc"]),
+    "bump": dict(C.CASES["bump_visc"]),
+    "supersonic": dict(C.CASES["supersonic"], viscous=True, re=(1e5, 1.0)),
+}
+
+
+def _make(api, name, **cfg):
+    case = SST_CASES[name]
+    spec = case["spec"]()
+    m = api.Mesh.from_spec(spec)
+    s = api.Solver(m, bcset=case["bcset"], viscous=1, init=case["init"], turbulence="sst", **cfg)
+    C.setup(s, case)
+    o = OracleSolver(spec, bcset=case["bcset"], viscous=True, init=case["init"])
+    C.setup(o, case)
+    return spec, s, o
+
+
+def _turbulent_state(o, seed):
+    """Perturbed mean flow with k of a few percent turbulence and nu_t of 5-25 nu."""
+    U = C.perturbed_state(o.get_state(), o.cells(), seed=seed, amplitude=0.06)
+    xc = o.cells()[:, 1:]
+    pert = mg.smooth_perturbation(xc, seed + 101, 1.0)
+    r = U[:, 0]
+    speed = np.sqrt(U[:, 1] ** 2 + U[:, 2] ** 2) / r
+    nu = o.params()["nu"]
+    k = (0.03 * speed.mean()) ** 2 * (1.0 + 0.5 * pert[:, 0])
+    nut = nu * (15.0 + 10.0 * pert[:, 1])
+    U[:, 4] = r * k
+    U[:, 5] = r * k / nut
+    return U
+
+
+def _rows_match(got, want, what):
+    for c in range(6):
+        scale = max(np.abs(want[:, c]).max(), 1e-300)
+        err = np.abs(got[:, c] - want[:, c]).max()
+        assert err <= REL_SST * scale, f"{what} row {c}: rel err {err / scale:.3e}"
+
+
+@pytest.mark.parametrize("name", list(SST_CASES))
+def test_sst_residual_against_oracle(cuda_lib, name):
+    spec, s, o = _make(cuda_lib, name)
+    U = _turbulent_state(o, seed=5)
+    for fl in C.FLUXES:
+        for sp in C.SPATIALS:
+            s.setNumericalMethod(fl, sp)
+            o.setNumericalMethod(fl, sp)
+            _rows_match(s.computeResiduals(U), o.residual_sst(U), f"{name} {fl} {sp}")
+
+
+def test_sst_initial_state_is_freestream_k_w(cuda_lib):
+    spec, s, o = _make(cuda_lib, "plate")
+    k_inf, w_inf = o.sst_freestream()
+    U = s.getSolution()
+    np.testing.assert_allclose(U[:, 4], U[:, 0] * k_inf, rtol=1e-15)
+    np.testing.assert_allclose(U[:, 5], U[:, 0] * w_inf, rtol=1e-15)
+
+
+@pytest.mark.parametrize("flux", ["ROE", "HLLC"])
+def test_sst_exact_jv_matches_central_differences(cuda_lib, flux):
+    spec, s, o = _make(cuda_lib, "plate")
+    s.setNumericalMethod(flux, "SECOND_ORDER_CENTRAL")
+    U = _turbulent_state(o, seed=7)
+    n = U.shape[0]
+    s.set_dt(np.full(n, 1e300))  # time term vol / dt vanishes
+    rng = np.random.default_rng(3)
+    v = rng.standard_normal(U.shape) * np.abs(U).mean(axis=0)
+    J = s.apply_jacobian(U, None, v, mode="exact")
+    h = 1e-6
+    Jfd = (s.computeResiduals(U + h * v) - s.computeResiduals(U - h * v)) / (2 * h)
+    for c in range(6):
+        err = np.linalg.norm(J[:, c] - Jfd[:, c])
+        assert err <= 1e-6 * np.linalg.norm(Jfd[:, c]), f"row {c}: {err / np.linalg.norm(Jfd[:, c]):.3e}"
+
+
+def test_sst_vjp_is_refused(cuda_lib):
+    spec, s, o = _make(cuda_lib, "plate")
+    U = _turbulent_state(o, seed=9)
+    with pytest.raises(cuda_lib.CfdgError):
+        s.vjp(np.ones_like(U), U)
+
+
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+def test_turbulent_plate_solve_reduces_residual(cuda_lib, precision):
+    spec = mg.turb_plate(48, 40)
+    m = cuda_lib.Mesh.from_spec(spec)
+    s = cuda_lib.Solver(m, bcset="plate", viscous=1, init="freestream", turbulence="sst", precision=precision,
+                        jv="exact", gmres_m=30)
+    s.setNumericalMethod("ROE", "SECOND_ORDER_CENTRAL")
+    s.setFreestreamStatic(0.2, 101325.0, 300.0)
+    s.setKinematicViscosity(5e6, 1.0)
+    s.initialize()
+    h = s.solveImplicit(tol=1e-8, max_steps=300)
+    U = s.getSolution()
+    assert np.isfinite(U).all()
+    assert (U[:, 4] >= 0).all() and (U[:, 5] > 0).all()
+    r = h["res_vm"]
+    assert r[-1] <= 1e-4 * r[0], r[-10:]
