@@ -201,6 +201,10 @@ cfdg_status cfdg_vjp(cfdg_solver* s, const double* U, const double* lambda, doub
  * x_mid, Cp (p - p_inf)/q_inf and Cf (one-sided wall shear / q_inf).  *n gets the count;
  * buffers may be NULL to query it. */
 cfdg_status cfdg_wall_coefficients(cfdg_solver* s, int tag, double* x_mid, double* cp, double* cf, int* n);
+/* computeWallDistances (src/Solver.cpp:1981-2015): per cell (reference numbering), the
+ * distance from its centroid to the nearest no-slip (tag 4) face midpoint, 1e10 without
+ * such faces.  Computed on the GPU; with SST the same array feeds the model. */
+cfdg_status cfdg_wall_distance(cfdg_solver* s, double* d);
 /* calculateDrag (src/Solver.cpp:1307-1325): sum of -p A n_x over tag-3 faces */
 cfdg_status cfdg_drag(cfdg_solver* s, double* drag);
 /* calculateEntropyError (src/Solver.cpp:1620-1646) */

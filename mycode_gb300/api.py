@@ -105,6 +105,7 @@ SIGNATURES = {
     "cfdg_set_krylov": (C.c_int, [_vp, C.c_int]),
     "cfdg_vjp": (C.c_int, [_vp, C.c_void_p, _dp, _dp]),
     "cfdg_wall_coefficients": (C.c_int, [_vp, C.c_int, C.c_void_p, C.c_void_p, C.c_void_p, C.POINTER(C.c_int)]),
+    "cfdg_wall_distance": (C.c_int, [_vp, C.c_void_p]),
     "cfdg_drag": (C.c_int, [_vp, C.POINTER(C.c_double)]),
     "cfdg_entropy_error": (C.c_int, [_vp, C.POINTER(C.c_double)]),
     "cfdg_residual_device": (C.c_int, [_vp, C.c_int]),
@@ -416,6 +417,32 @@ class Solver:
 
     def flush_l2(self, nbytes=256 << 20):
         _check(lib().cfdg_flush_l2(self._h, int(nbytes)))
+
+    # ---- wall quantities (calculateDrag, extractSkinFriction, calculateEntropyError)
+    def wall_coefficients(self, tag=4):
+        """x_mid, Cp and Cf of the boundary faces with ``tag``, in reference face order."""
+        n = C.c_int(0)
+        _check(lib().cfdg_wall_coefficients(self._h, int(tag), None, None, None, C.byref(n)))
+        x, cp, cf = np.zeros(n.value), np.zeros(n.value), np.zeros(n.value)
+        if n.value:
+            _check(lib().cfdg_wall_coefficients(self._h, int(tag), x.ctypes.data_as(_vp), cp.ctypes.data_as(_vp),
+                                                cf.ctypes.data_as(_vp), C.byref(n)))
+        return x, cp, cf
+
+    def wall_distance(self):
+        d = np.zeros(self.n_cells)
+        _check(lib().cfdg_wall_distance(self._h, d.ctypes.data_as(_vp)))
+        return d
+
+    def drag(self):
+        d = C.c_double()
+        _check(lib().cfdg_drag(self._h, C.byref(d)))
+        return d.value
+
+    def entropy_error(self):
+        e = C.c_double()
+        _check(lib().cfdg_entropy_error(self._h, C.byref(e)))
+        return e.value
 
     def launch_count(self):
         n = C.c_longlong()

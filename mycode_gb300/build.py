@@ -7,6 +7,7 @@ Translation units and their floating-point contracts:
   solver.cu    nvcc               (host driver and C ABI; host code without contraction)
   noalloc.cu   nvcc --fmad=false  (residual norm with static scratch, no allocation)
   kern_adj.cu  nvcc               (adjoint / VJP of the FP64 residual)
+  kern_qoi.cu  nvcc --fmad=false  (wall distance, Cp/Cf, drag, entropy error)
   mesh.cpp     g++ -ffp-contract=off (host geometry bit-exact on x86 and Arm)
 Compiles in parallel, links with nvcc (static cudart).
 """
@@ -30,6 +31,7 @@ CU = {
     "solver.cu": [],
     "noalloc.cu": ["--fmad=false"],
     "kern_adj.cu": [],
+    "kern_qoi.cu": ["--fmad=false"],
 }
 CPP = ["mesh.cpp"]
 

@@ -26,11 +26,6 @@ void launch_residual<float>(const ResArgs<float>& a) {
     else residual_nv<4>(a);
 }
 
-#define NV_SWITCH(nv, ...) \
-    do {                                 \
-        if ((nv) == 6) { constexpr int NVC = 6; __VA_ARGS__; } \
-        else { constexpr int NVC = 4; __VA_ARGS__; }           \
-    } while (0)
 
 template <>
 void launch_dot<float>(int nv, long nc, const float* a, const float* b, RedScratch rs, double* out, cudaStream_t s) {

@@ -31,11 +31,6 @@ void launch_prim64(int nv, long nc, const Flow<double>& F, Field<double> U, Fiel
     else k_prim<double, 4><<<grid_for(nc), 256, 0, s>>>((int)nc, F, U, W);
 }
 
-#define NV_SWITCH(nv, ...) \
-    do {                                 \
-        if ((nv) == 6) { constexpr int NVC = 6; __VA_ARGS__; } \
-        else { constexpr int NVC = 4; __VA_ARGS__; }           \
-    } while (0)
 
 template <>
 void launch_dot<double>(int nv, long nc, const double* a, const double* b, RedScratch rs, double* out, cudaStream_t s) {
@@ -91,8 +86,8 @@ void launch_local_dt(int nv, const MeshView<double>& m, const Flow<double>& F, c
     NV_SWITCH(nv, (k_local_dt<NVC><<<grid_for(m.nc), 256, 0, s>>>(m, F, U, W, cfl, dt)));
 }
 void launch_precond(int nv, const MeshView<double>& m, const Flow<double>& F, const double* U, const double* W,
-                    const double* dt, double* D, cudaStream_t s) {
-    NV_SWITCH(nv, (k_precond<NVC><<<grid_for(m.nc), 256, 0, s>>>(m, F, U, W, dt, D)));
+                    const double* dt, double* D, const double* mut, cudaStream_t s) {
+    NV_SWITCH(nv, (k_precond<NVC><<<grid_for(m.nc), 256, 0, s>>>(m, F, U, W, dt, D, mut)));
 }
 void launch_newton_update(int nv, long nc, double* U, const double* dU, double relax, double gam, double wmin, int* bad,
                           cudaStream_t s) {

@@ -67,9 +67,10 @@ template <class T, int NV>
 __global__ void k_gmres_z(long nc, const T* V, long L, const double* D, T* z, GmresDev d) {
     const T* Vj = V + (long)d.gi[0] * L;
     for (long i = (long)blockIdx.x * blockDim.x + threadIdx.x; i < nc; i += (long)gridDim.x * blockDim.x) {
-        T id = (T)(1.0 / D[i]);
+        double id[NV];
+        d_inv<NV>(D, nc, i, id);
 #pragma unroll
-        for (int c = 0; c < NV; ++c) z[c * nc + i] = Vj[c * nc + i] * id;
+        for (int c = 0; c < NV; ++c) z[c * nc + i] = Vj[c * nc + i] * (T)id[c];
     }
 }
 
@@ -205,12 +206,13 @@ __global__ void k_gmres_solution_dev(long nc, const T* __restrict__ V, long L, G
                                      const double* __restrict__ D, double* __restrict__ x) {
     const int k = d.gi[1];
     for (long i = (long)blockIdx.x * blockDim.x + threadIdx.x; i < nc; i += (long)gridDim.x * blockDim.x) {
-        double id = 1.0 / D[i];
+        double id[NV];
+        d_inv<NV>(D, nc, i, id);
 #pragma unroll
         for (int c = 0; c < NV; ++c) {
             long q = c * nc + i;
             double acc = 0.0;
-            for (int j = 0; j <= k; ++j) acc = acc + (double)V[j * L + q] * d.y[j] * id;
+            for (int j = 0; j <= k; ++j) acc = acc + (double)V[j * L + q] * d.y[j] * id[c];
             x[q] = acc;
         }
     }

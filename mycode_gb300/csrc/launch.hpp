@@ -57,8 +57,9 @@ void launch_fd_combine(int nv, long nc, const double* Rp, const double* Rb, cons
 void launch_norm_vm(int nv, long nc, const double* R, const double* vol, RedScratch rs, double* out3, cudaStream_t s);
 void launch_local_dt(int nv, const MeshView<double>& m, const Flow<double>& F, const double* U, const double* W,
                      double cfl, double* dt, cudaStream_t s);
+// D: one plane per cell, three with SST (mean flow, k, w); mut: SST eddy viscosity or null
 void launch_precond(int nv, const MeshView<double>& m, const Flow<double>& F, const double* U, const double* W,
-                    const double* dt, double* D, cudaStream_t s);
+                    const double* dt, double* D, const double* mut, cudaStream_t s);
 void launch_newton_update(int nv, long nc, double* U, const double* dU, double relax, double gam, double wmin, int* bad,
                           cudaStream_t s);
 
@@ -69,6 +70,23 @@ inline unsigned red_grid(long n) {
     long b = (n + RED_THREADS - 1) / RED_THREADS;
     return (unsigned)(b < RED_BLOCKS ? (b < 1 ? 1 : b) : RED_BLOCKS);
 }
+
+// instantiate a launch for nv = 4 or 6 (NVC is the compile-time count in __VA_ARGS__)
+#define NV_SWITCH(nv, ...)                                      \
+    do {                                                        \
+        if ((nv) == 6) { constexpr int NVC = 6; __VA_ARGS__; } \
+        else { constexpr int NVC = 4; __VA_ARGS__; }           \
+    } while (0)
+
+// ---- wall quantities and wall distance (kern_qoi.cu)
+void launch_wall_distance(long nc, const double* xc, const double* yc, int nw, const double* wx, const double* wy,
+                          double* d, float* d32, cudaStream_t s);
+void launch_wall_coeff(int nv, int n, const int* slots, const MeshView<double>& m, const Flow<double>& F,
+                       const double* U, double q_inf, double p_inf, double* cp, double* cf, double* drag,
+                       cudaStream_t s);
+void launch_sum_in_order(int n, const double* terms, double* out, cudaStream_t s);
+void launch_entropy(int nv, long nc, const Flow<double>& F, const double* U, const double* vol, double s_ref,
+                    RedScratch rs, double* out2, cudaStream_t s);
 
 }  // namespace cfdg
 

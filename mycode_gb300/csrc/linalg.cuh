@@ -136,6 +136,19 @@ __global__ void k_scale_from(long n, TO* x, const TI* a, const double* s, int in
         x[q] = (TO)(a[q] * (TI)sv);
 }
 
+// The preconditioner holds one value per cell for the mean flow (plane 0 of D); with SST
+// (NV = 6) planes 1 and 2 hold the k and w values, which add the destruction terms.
+template <int NV>
+__device__ __forceinline__ void d_inv(const double* __restrict__ D, long nc, long i, double* id) {
+    id[0] = 1.0 / D[i];
+#pragma unroll
+    for (int c = 1; c < NV; ++c) id[c] = id[0];
+    if (NV == 6) {
+        id[4] = 1.0 / D[nc + i];
+        id[5] = 1.0 / D[2 * nc + i];
+    }
+}
+
 // z = V * (1 / D) per cell (src/Solver.cpp:1536-1538), with sum of squares of z
 template <class TV, class TZ, int NV>
 __global__ void __launch_bounds__(RED_THREADS) k_precond_apply(long nc, const TV* __restrict__ V,
@@ -143,11 +156,12 @@ __global__ void __launch_bounds__(RED_THREADS) k_precond_apply(long nc, const TV
                                                                RedScratch rs, double* out_sq) {
     double v[1] = {0.0};
     for (long i = (long)blockIdx.x * blockDim.x + threadIdx.x; i < nc; i += (long)gridDim.x * blockDim.x) {
-        TV id = (TV)(1.0 / D[i]);
+        double idd[NV];
+        d_inv<NV>(D, nc, i, idd);
         double s = 0.0;
 #pragma unroll
         for (int c = 0; c < NV; ++c) {
-            TZ zz = (TZ)(V[c * nc + i] * id);
+            TZ zz = (TZ)(V[c * nc + i] * (TV)idd[c]);
             z[c * nc + i] = zz;
             s = (c == 0) ? (double)zz * (double)zz : s + (double)zz * (double)zz;
         }
@@ -186,12 +200,13 @@ template <class TV, int NV>
 __global__ void k_gmres_solution(long nc, const TV* __restrict__ V, long vstride, const double* y, int k,
                                  const double* __restrict__ D, double* __restrict__ x) {
     for (long i = (long)blockIdx.x * blockDim.x + threadIdx.x; i < nc; i += (long)gridDim.x * blockDim.x) {
-        double id = 1.0 / D[i];
+        double id[NV];
+        d_inv<NV>(D, nc, i, id);
 #pragma unroll
         for (int c = 0; c < NV; ++c) {
             long q = c * nc + i;
             double acc = 0.0;
-            for (int j = 0; j <= k; ++j) acc = acc + (double)V[j * vstride + q] * y[j] * id;
+            for (int j = 0; j <= k; ++j) acc = acc + (double)V[j * vstride + q] * y[j] * id[c];
             x[q] = acc;
         }
     }
@@ -244,9 +259,13 @@ __global__ void k_local_dt(MeshView<double> m, Flow<double> F, const double* __r
 
 // computeDiagonalPreconditioner (src/Solver.cpp:1424-1465) as a per-cell gather; each
 // face term is evaluated with the owner as L exactly as the reference's face loop.
+// With SST (NV = 6, mut = the cell eddy viscosity) the viscous eigenvalue uses mu + mu_t,
+// and planes 1 and 2 of D add the linearised destruction of k (beta* w vol) and of w
+// (2 beta1 w vol) to the k and w diagonals.
 template <int NV>
 __global__ void k_precond(MeshView<double> m, Flow<double> F, const double* __restrict__ U,
-                          const double* __restrict__ W, const double* __restrict__ dt, double* __restrict__ D) {
+                          const double* __restrict__ W, const double* __restrict__ dt, double* __restrict__ D,
+                          const double* __restrict__ mut) {
     long i = (long)blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= m.nc) return;
     long nc = m.nc;
@@ -269,6 +288,7 @@ __global__ void k_precond(MeshView<double> m, Flow<double> F, const double* __re
         double li = vn + cf;
         double dx = sqrt(m.vol[o]);
         double mu = 0.5 * (L.r + Rr.r) * F.nu;
+        if (NV == 6 && mut) mu = mu + 0.5 * (mut[o] + mut[n >= 0 ? n : o]);
         double lv = 2.0 * mu / (0.5 * (L.r + Rr.r) * dx + 1e-12);
         double lt = (li + lv) * m.area[f];
         acc += lt * 0.5;
@@ -277,6 +297,11 @@ __global__ void k_precond(MeshView<double> m, Flow<double> F, const double* __re
     double d = (v / (dt[i] + 1e-30)) + acc;
     if (d < 1e-12) d = 1e-12;
     D[i] = d;
+    if (NV == 6) {
+        double w = W[W_W * nc + i];
+        D[nc + i] = d + SstConst::beta_s * w * v;
+        D[2 * nc + i] = d + 2.0 * SstConst::b1 * w * v;
+    }
 }
 
 // Newton update with the positivity clamps of src/Solver.cpp:1760-1778 (and, for SST,

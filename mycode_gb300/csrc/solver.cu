@@ -417,7 +417,7 @@ struct cfdg_solver {
     void enqueue_gmres_pre(double* Ubase, double* rhsd, cudaGraphConditionalHandle h) {
         const bool mixed = cfg.precision == CFDG_MIXED;
         launch_prim64(nv, nc, F, f64(U), f64(W), st);
-        launch_precond(nv, mv, F, U, W, dt, D, st);
+        launch_precond(nv, mv, F, U, W, dt, D, Tt, st);
         launches += 2;
         if (mixed) {
             launch_convert<float>(L, Ubase, U32, st);
@@ -591,7 +591,7 @@ struct cfdg_solver {
         TRY(ensure_krylov());
         // preconditioner on the current state (computeDiagonalPreconditioner uses U_current)
         launch_prim64(nv, nc, F, f64(U), f64(W), st);
-        launch_precond(nv, mv, F, U, W, dt, D, st);
+        launch_precond(nv, mv, F, U, W, dt, D, Tt, st);
         launches += 2;
         launch_dot<double>(nv, nc, rhsd, rhsd, rs, scal + 3, st);
         ++launches;
@@ -799,7 +799,88 @@ struct cfdg_solver {
         return CFDG_OK;
     }
 
+    // distance from each cell centroid to the nearest no-slip wall face midpoint
+    // (computeWallDistances, src/Solver.cpp:1981-2015), 1e10 without walls, into dwall
+    // (and dwall32 when allocated); dwall is allocated here when the model has none
+    cfdg_status wall_distance() {
+        const HostMesh& h = mesh->h;
+        if (!dwall) TRY(dalloc(&dwall, (size_t)nc));
+        std::vector<double> wxy;
+        for (int f = 0; f < h.n_faces; ++f)
+            if (h.f_n[f] < 0 && h.f_tag[f] == 4) wxy.push_back(h.f_xm[f]);
+        size_t nw = wxy.size();
+        for (int f = 0; f < h.n_faces; ++f)
+            if (h.f_n[f] < 0 && h.f_tag[f] == 4) wxy.push_back(h.f_ym[f]);
+        double* tmp = nullptr;
+        TRY(dalloc(&tmp, 2 * (size_t)nc + 2 * nw));
+        bool ok = cudaMemcpy(tmp, h.xc.data(), sizeof(double) * nc, cudaMemcpyHostToDevice) == cudaSuccess &&
+                  cudaMemcpy(tmp + nc, h.yc.data(), sizeof(double) * nc, cudaMemcpyHostToDevice) == cudaSuccess &&
+                  (nw == 0 || cudaMemcpy(tmp + 2 * nc, wxy.data(), sizeof(double) * 2 * nw,
+                                         cudaMemcpyHostToDevice) == cudaSuccess);
+        if (ok) {
+            launch_wall_distance(nc, tmp, tmp + nc, (int)nw, tmp + 2 * nc, tmp + 2 * nc + nw, dwall, dwall32, st);
+            ++launches;
+            ok = cudaStreamSynchronize(st) == cudaSuccess && cudaGetLastError() == cudaSuccess;
+        }
+        cudaFree(tmp);
+        if (!ok) return fail(CFDG_ERR_CUDA, "wall distance failed");
+        return CFDG_OK;
+    }
+
+    // wall quantities: boundary faces of one tag in reference face order, as device slots,
+    // and the per-face outputs (cp, cf, drag terms) plus the drag sum
+    int* qslots = nullptr;
+    double* qbuf = nullptr;
+    int qcap = 0;
+
+    // the device slots of the boundary faces with this tag, in reference face order
+    std::vector<int> tagged_faces(int tag) const {
+        const HostMesh& h = mesh->h;
+        std::vector<int> out;
+        for (int f = 0; f < h.n_faces; ++f)
+            if (h.f_n[f] < 0 && h.f_tag[f] == tag) out.push_back(h.face_inv[f]);
+        return out;
+    }
+
+    // free-stream q and p of extractSkinFriction (src/Solver.cpp:1904-1911)
+    void freestream_q(double& q_inf, double& p_inf) const {
+        double g = cfg.gamma;
+        double factor_T = 1.0 + 0.5 * (g - 1.0) * M_inf * M_inf;
+        double T_static = T0 / factor_T;
+        double c_inf = std::sqrt(g * cfg.R_gas * T_static);
+        double u_inf = M_inf * c_inf;
+        double rho_inf = Pexit / (cfg.R_gas * T_static);
+        q_inf = 0.5 * rho_inf * u_inf * u_inf;
+        p_inf = Pexit;
+    }
+
+    // Cp, Cf and drag terms of the listed faces into qbuf (3 planes of qcap) and the
+    // in-order drag sum into qbuf[3 * qcap]
+    cfdg_status wall_terms(const std::vector<int>& faces) {
+        int n = (int)faces.size();
+        if (n > qcap) {
+            cudaFree(qslots);
+            cudaFree(qbuf);
+            qslots = nullptr;
+            qbuf = nullptr;
+            qcap = 0;
+            TRY(dalloc(&qslots, (size_t)n));
+            TRY(dalloc(&qbuf, 3 * (size_t)n + 1));
+            qcap = n;
+        }
+        if (n) CK(cudaMemcpyAsync(qslots, faces.data(), sizeof(int) * n, cudaMemcpyHostToDevice, st));
+        double q_inf, p_inf;
+        freestream_q(q_inf, p_inf);
+        launch_wall_coeff(nv, n, qslots, mv, F, U, q_inf, p_inf, qbuf, qbuf + qcap, qbuf + 2 * (size_t)qcap, st);
+        launch_sum_in_order(n, qbuf + 2 * (size_t)qcap, qbuf + 3 * (size_t)qcap, st);
+        launches += 2;
+        CK(cudaGetLastError());
+        return CFDG_OK;
+    }
+
     void release() {
+        cudaFree(qslots);
+        cudaFree(qbuf);
         void* pt[] = {Tt, Tj, Tjd, dwall, T32, T32d, dwall32};
         for (void* p : pt) cudaFree(p);
         void* ps[] = {cf, fo, fn, ftag, perm, U, W, G, phi, FA, R, dt, D, stage, Ub, Rb, Up, Rp, vtmp, x, rhs,
@@ -1004,7 +1085,7 @@ cfdg_status cfdg_solver_create(const cfdg_mesh* m, const cfdg_config* cfg, cfdg_
     int NW = nv == 6 ? 7 : 5, NG = nv == 6 ? 14 : 10;
     TRYS(dalloc(&s->U, L)); TRYS(dalloc(&s->W, (size_t)NW * nc)); TRYS(dalloc(&s->G, (size_t)NG * nc));
     TRYS(dalloc(&s->phi, nc)); TRYS(dalloc(&s->FA, (size_t)nv * nf)); TRYS(dalloc(&s->R, L));
-    TRYS(dalloc(&s->dt, nc)); TRYS(dalloc(&s->D, nc)); TRYS(dalloc(&s->stage, 14 * (size_t)nc));
+    TRYS(dalloc(&s->dt, nc)); TRYS(dalloc(&s->D, (size_t)(nv == 6 ? 3 : 1) * nc)); TRYS(dalloc(&s->stage, 14 * (size_t)nc));
     TRYS(dalloc(&s->Ub, L)); TRYS(dalloc(&s->Rb, L)); TRYS(dalloc(&s->Up, L)); TRYS(dalloc(&s->Rp, L));
     TRYS(dalloc(&s->vtmp, L)); TRYS(dalloc(&s->x, L)); TRYS(dalloc(&s->rhs, L));
     TRYS(dalloc(&s->Wj, (size_t)NW * nc)); TRYS(dalloc(&s->Wjd, (size_t)NW * nc));
@@ -1014,26 +1095,7 @@ cfdg_status cfdg_solver_create(const cfdg_mesh* m, const cfdg_config* cfg, cfdg_
         TRYS(dalloc(&s->Tt, 4 * (size_t)nc)); TRYS(dalloc(&s->Tj, 4 * (size_t)nc)); TRYS(dalloc(&s->Tjd, 4 * (size_t)nc));
         TRYS(dalloc(&s->dwall, (size_t)nc)); TRYS(dalloc(&s->dwall32, (size_t)nc));
         TRYS(dalloc(&s->T32, 4 * (size_t)nc)); TRYS(dalloc(&s->T32d, 4 * (size_t)nc));
-        // distance from each cell centroid to the nearest no-slip wall face midpoint
-        // (computeWallDistances, src/Solver.cpp:1981-2015); 1e10 without walls
-        std::vector<double> wx, wy;
-        for (int f = 0; f < h.n_faces; ++f)
-            if (h.f_n[f] < 0 && h.f_tag[f] == 4) { wx.push_back(h.f_xm[f]); wy.push_back(h.f_ym[f]); }
-        std::vector<double> d(nc, 1e10);
-        std::vector<float> d32(nc);
-        for (int i = 0; i < nc; ++i) {
-            double best = 1e20;
-            for (size_t w = 0; w < wx.size(); ++w) {
-                double dx = h.xc[i] - wx[w], dy = h.yc[i] - wy[w];
-                double d2 = dx * dx + dy * dy;
-                if (d2 < best) best = d2;
-            }
-            if (!wx.empty()) d[i] = std::sqrt(best);
-            d32[i] = (float)d[i];
-        }
-        if (cudaMemcpy(s->dwall, d.data(), sizeof(double) * nc, cudaMemcpyHostToDevice) != cudaSuccess ||
-            cudaMemcpy(s->dwall32, d32.data(), sizeof(float) * nc, cudaMemcpyHostToDevice) != cudaSuccess)
-            return bail(fail(CFDG_ERR_CUDA, "wall distance upload failed"));
+        TRYS(s->wall_distance());
     }
     if (c.precision == CFDG_MIXED) {
         TRYS(dalloc(&s->U32, L)); TRYS(dalloc(&s->W32, (size_t)NW * nc)); TRYS(dalloc(&s->W32d, (size_t)NW * nc));
@@ -1257,7 +1319,7 @@ cfdg_status cfdg_set_timestep(cfdg_solver* s, const double* dt) {
 cfdg_status cfdg_preconditioner(cfdg_solver* s, double* D) {
     if (!s || !D) return fail(CFDG_ERR_ARG, "null argument");
     launch_prim64(s->nv, s->nc, s->F, s->f64(s->U), s->f64(s->W), s->st);
-    launch_precond(s->nv, s->mv, s->F, s->U, s->W, s->dt, s->D, s->st);
+    launch_precond(s->nv, s->mv, s->F, s->U, s->W, s->dt, s->D, s->Tt, s->st);
     s->launches += 2;
     CK(cudaGetLastError());
     return s->download_aos(s->D, D, 1, 1);
@@ -1366,19 +1428,58 @@ cfdg_status cfdg_vjp_device(cfdg_solver* s) {
     return CFDG_OK;
 }
 
-cfdg_status cfdg_wall_coefficients(cfdg_solver* s, int, double*, double*, double*, int*) {
-    if (!s) return fail(CFDG_ERR_ARG, "null solver");
-    return fail(CFDG_ERR_UNSUPPORTED, "wall coefficients are not built into this library yet");
+cfdg_status cfdg_wall_coefficients(cfdg_solver* s, int tag, double* x_mid, double* cp, double* cf, int* n) {
+    if (!s || !n) return fail(CFDG_ERR_ARG, "null solver or count");
+    std::vector<int> faces = s->tagged_faces(tag);
+    int nw = (int)faces.size();
+    *n = nw;
+    if (!x_mid && !cp && !cf) return CFDG_OK;
+    if (x_mid) {
+        const HostMesh& h = s->mesh->h;
+        for (int k = 0; k < nw; ++k) x_mid[k] = h.f_xm[h.face_perm[faces[k]]];
+    }
+    if (!cp && !cf) return CFDG_OK;
+    TRY(s->wall_terms(faces));
+    if (nw && cp) CK(cudaMemcpyAsync(cp, s->qbuf, sizeof(double) * nw, cudaMemcpyDeviceToHost, s->st));
+    if (nw && cf) CK(cudaMemcpyAsync(cf, s->qbuf + s->qcap, sizeof(double) * nw, cudaMemcpyDeviceToHost, s->st));
+    CK(cudaStreamSynchronize(s->st));
+    return CFDG_OK;
 }
 
-cfdg_status cfdg_drag(cfdg_solver* s, double*) {
-    if (!s) return fail(CFDG_ERR_ARG, "null solver");
-    return fail(CFDG_ERR_UNSUPPORTED, "drag is not built into this library yet");
+cfdg_status cfdg_wall_distance(cfdg_solver* s, double* d) {
+    if (!s || !d) return fail(CFDG_ERR_ARG, "null solver or output");
+    TRY(s->wall_distance());
+    std::vector<double> dd(s->nc);
+    CK(cudaMemcpy(dd.data(), s->dwall, sizeof(double) * s->nc, cudaMemcpyDeviceToHost));
+    const std::vector<int>& perm = s->mesh->h.cell_perm;
+    for (int i = 0; i < s->nc; ++i) d[perm[i]] = dd[i];
+    return CFDG_OK;
 }
 
-cfdg_status cfdg_entropy_error(cfdg_solver* s, double*) {
-    if (!s) return fail(CFDG_ERR_ARG, "null solver");
-    return fail(CFDG_ERR_UNSUPPORTED, "entropy error is not built into this library yet");
+cfdg_status cfdg_drag(cfdg_solver* s, double* drag) {
+    if (!s || !drag) return fail(CFDG_ERR_ARG, "null solver or output");
+    TRY(s->wall_terms(s->tagged_faces(3)));
+    CK(cudaMemcpyAsync(drag, s->qbuf + 3 * (size_t)s->qcap, sizeof(double), cudaMemcpyDeviceToHost, s->st));
+    CK(cudaStreamSynchronize(s->st));
+    return CFDG_OK;
+}
+
+cfdg_status cfdg_entropy_error(cfdg_solver* s, double* err) {
+    if (!s || !err) return fail(CFDG_ERR_ARG, "null solver or output");
+    // free-stream entropy (src/Solver.cpp:1621-1625), host IEEE arithmetic
+    double g = s->cfg.gamma, M = s->M_inf;
+    double T_inf = s->T0 / (1.0 + 0.5 * (g - 1.0) * M * M);
+    double P_inf = s->P0 / std::pow(1.0 + 0.5 * (g - 1.0) * M * M, g / (g - 1.0));
+    double rho_inf = P_inf / (s->cfg.R_gas * T_inf);
+    double S_ref = P_inf / std::pow(rho_inf, g);
+    launch_entropy(s->nv, s->nc, s->F, s->U, s->g64.vol, S_ref, s->rs, s->scal + 8, s->st);
+    ++s->launches;
+    CK(cudaGetLastError());
+    double h2[2];
+    CK(cudaMemcpyAsync(h2, s->scal + 8, sizeof(h2), cudaMemcpyDeviceToHost, s->st));
+    CK(cudaStreamSynchronize(s->st));
+    *err = std::sqrt(h2[0] / h2[1]);
+    return CFDG_OK;
 }
 
 cfdg_status cfdg_synchronize(cfdg_solver* s) {

@@ -957,6 +957,60 @@ int om_solve_implicit(om_solver* s, double tol, int max_steps, double* res_vm, d
     return logged;
 }
 
+/* extractSkinFriction (src/Solver.cpp:1899-1979) before its sort by x: per boundary face
+ * of the tag, in face order, x_mid, Cp = (p - p_exit) / q_inf and Cf = rho nu u_t / dn / q_inf
+ * from the owner cell.  Returns the face count; the arrays may be NULL. */
+int om_wall_coefficients(const om_solver* s, int tag, double* x, double* cp, double* cf) {
+    const om_mesh* m = s->m;
+    double g = s->gamma;
+    double factor_T = 1.0 + 0.5 * (g - 1.0) * s->M_inf * s->M_inf;
+    double T_static = s->T0 / factor_T;
+    double c_inf = sqrt(g * s->R_gas * T_static);
+    double u_inf = s->M_inf * c_inf;
+    double rho_inf = s->Pexit / (s->R_gas * T_static);
+    double q_inf = 0.5 * rho_inf * u_inf * u_inf;
+    int n = 0;
+    for (int f = 0; f < m->n_faces; ++f) {
+        if (m->neighbor[f] >= 0 || m->tag[f] != tag) continue;
+        if (x) {
+            int o = m->owner[f];
+            st_t U = st_load(s->U + NV * o);
+            double uc = U.ru / U.r, vc = U.rv / U.r;
+            double tx = -m->ny[f], ty = m->nx[f];
+            if (tx < 0) { tx = -tx; ty = -ty; }
+            double ut = uc * tx + vc * ty;
+            double dx = m->xm[f] - m->xc[o], dy = m->ym[f] - m->yc[o];
+            double dn = fabs(dx * m->nx[f] + dy * m->ny[f]);
+            if (dn < 1e-12) dn = 1e-12;
+            double dudn = ut / dn;
+            double mu = U.r * s->nu;
+            double tau = mu * dudn;
+            x[n] = m->xm[f];
+            cf[n] = tau / q_inf;
+            cp[n] = (pressure(U) - s->Pexit) / q_inf;
+        }
+        ++n;
+    }
+    return n;
+}
+
+/* computeWallDistances (src/Solver.cpp:1981-2015): nearest tag-4 face midpoint, 1e10 without walls */
+void om_wall_distance(const om_solver* s, double* d) {
+    const om_mesh* m = s->m;
+    for (int i = 0; i < m->n_cells; ++i) {
+        double best = 1e20;
+        int any = 0;
+        for (int f = 0; f < m->n_faces; ++f)
+            if (m->neighbor[f] < 0 && m->tag[f] == 4) {
+                double dx = m->xc[i] - m->xm[f], dy = m->yc[i] - m->ym[f];
+                double d2 = dx * dx + dy * dy;
+                if (d2 < best) best = d2;
+                any = 1;
+            }
+        d[i] = any ? sqrt(best) : 1e10;
+    }
+}
+
 /* calculateDrag: pressure force on tag-3 faces (src/Solver.cpp:1307-1325) */
 double om_drag(const om_solver* s) {
     const om_mesh* m = s->m;

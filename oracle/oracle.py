@@ -95,6 +95,8 @@ def _oracle_lib():
             "om_residual_sst": (None, [vp, _dp, _dp, C.c_double, C.c_double]),
             "om_sst_freestream": (None, [vp, C.c_double, C.c_double, _dp]),
             "om_sst_reset": (None, []),
+            "om_wall_coefficients": (C.c_int, [vp, C.c_int, C.c_void_p, C.c_void_p, C.c_void_p]),
+            "om_wall_distance": (None, [vp, _dp]),
         }
         for name, (res, args) in sig.items():
             fn = getattr(lib, name)
@@ -258,6 +260,19 @@ class OracleSolver(_Base):
     def entropy_error(self):
         return self._L.om_entropy_error(self._s)
 
+    def wall_coefficients(self, tag=4):
+        """x_mid, Cp, Cf of the boundary faces with ``tag`` in face order (current state)."""
+        n = self._L.om_wall_coefficients(self._s, int(tag), None, None, None)
+        x, cp, cf = np.zeros(n), np.zeros(n), np.zeros(n)
+        if n:
+            self._L.om_wall_coefficients(self._s, int(tag), x.ctypes.data, cp.ctypes.data, cf.ctypes.data)
+        return x, cp, cf
+
+    def wall_distance(self):
+        d = np.zeros(self.n_cells)
+        self._L.om_wall_distance(self._s, d)
+        return d
+
     def residual_sst(self, U, turb_intensity=0.001, mut_ratio=0.01):
         """Residual of the mean flow plus the SST k and w equations (nv = 6, AoS)."""
         R = np.zeros(6 * self.n_cells)
@@ -318,6 +333,10 @@ class RefSolver(_Base):
                 "ref_gmres": (C.c_int, [vp, _dp, _dp, _dp, _dp]),
                 "ref_norm_vm": (C.c_double, [vp, _dp]),
                 "ref_solve_implicit": (C.c_int, [vp, C.c_double, C.c_int, _dp, _dp, _dp, _ip]),
+                "ref_wall_distance": (None, [vp, _dp]),
+                "ref_drag": (C.c_double, [vp]),
+                "ref_entropy_error": (C.c_double, [vp]),
+                "ref_skin_friction": (C.c_int, [vp, C.c_char_p, _dp, _dp, C.c_int]),
             }
             for name, (res, args) in sig.items():
                 fn = getattr(lib, name)
@@ -431,3 +450,21 @@ class RefSolver(_Base):
         it = np.zeros(max_steps, np.int32)
         n = self._L.ref_solve_implicit(self._h, float(tol), int(max_steps), a, b, c, it)
         return {"res_vm": a[:n], "res_abs": b[:n], "cfl": c[:n], "gmres_iters": it[:n]}
+
+    def wall_distance(self):
+        d = np.zeros(self.n_cells)
+        self._L.ref_wall_distance(self._h, d)
+        return d
+
+    def drag(self):
+        return self._L.ref_drag(self._h)
+
+    def entropy_error(self):
+        return self._L.ref_entropy_error(self._h)
+
+    def skin_friction(self, path):
+        """(x, Cf) rows of the reference's skin-friction CSV (sorted by x, 6 digits)."""
+        cap = self.n_faces
+        x, cf = np.zeros(cap), np.zeros(cap)
+        n = self._L.ref_skin_friction(self._h, str(path).encode(), x, cf, cap)
+        return x[:n], cf[:n]

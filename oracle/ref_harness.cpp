@@ -262,3 +262,67 @@ int ref_solve_implicit(void* p, double tol, int max_steps, double* res_vm, doubl
 }
 
 }  // extern "C"
+
+namespace {
+// runs f with std::cout captured at 17 significant digits; returns what it printed
+template <class Fn>
+std::string captured(Fn f) {
+    std::ostringstream cap;
+    std::streambuf* old = std::cout.rdbuf(cap.rdbuf());
+    std::streamsize prec = std::cout.precision(17);
+    f();
+    std::cout.precision(prec);
+    std::cout.rdbuf(old);
+    return cap.str();
+}
+}  // namespace
+
+extern "C" {
+
+// computeWallDistances (src/Solver.cpp:1981-2015)
+void ref_wall_distance(void* p, double* d) {
+    Solver* s = ((Handle*)p)->solver;
+    captured([&] { s->computeWallDistances(); });
+    for (size_t i = 0; i < s->wallDistances.size(); ++i) d[i] = s->wallDistances[i];
+}
+
+// calculateDrag (src/Solver.cpp:1307-1325) on the current state, parsed from its output
+double ref_drag(void* p) {
+    Solver* s = ((Handle*)p)->solver;
+    std::string out = captured([&] { s->calculateDrag(); });
+    double d = 0.0;
+    std::sscanf(out.c_str(), " Drag :%lf", &d);
+    return d;
+}
+
+// calculateEntropyError (src/Solver.cpp:1620-1646), parsed from its output
+double ref_entropy_error(void* p) {
+    Solver* s = ((Handle*)p)->solver;
+    std::string out = captured([&] { s->calculateEntropyError(); });
+    size_t k = out.find("L2 Entropy Error:");
+    double e = -1.0;
+    if (k != std::string::npos) std::sscanf(out.c_str() + k, "L2 Entropy Error: %lf", &e);
+    return e;
+}
+
+// extractSkinFriction (src/Solver.cpp:1899-1979) into the CSV at path (sorted by x, six
+// significant digits); returns the number of rows read back into x, cf (at most cap)
+int ref_skin_friction(void* p, const char* path, double* x, double* cf, int cap) {
+    Solver* s = ((Handle*)p)->solver;
+    captured([&] { s->extractSkinFriction(path); });
+    std::ifstream in(path);
+    std::string line;
+    std::getline(in, line);
+    int n = 0;
+    while (std::getline(in, line) && n < cap) {
+        double a, b, c;
+        if (std::sscanf(line.c_str(), "%lf,%lf,%lf", &a, &b, &c) == 3) {
+            x[n] = a;
+            cf[n] = b;
+            ++n;
+        }
+    }
+    return n;
+}
+
+}  // extern "C"
