@@ -205,6 +205,15 @@ cfdg_status cfdg_wall_coefficients(cfdg_solver* s, int tag, double* x_mid, doubl
  * distance from its centroid to the nearest no-slip (tag 4) face midpoint, 1e10 without
  * such faces.  Computed on the GPU; with SST the same array feeds the model. */
 cfdg_status cfdg_wall_distance(cfdg_solver* s, double* d);
+/* Wall objectives J(U) of the owner states of boundary faces, summed in reference face
+ * order (no reference counterpart except the pressure drag): the adjoint's objectives.
+ *   CFDG_OBJ_PRESSURE_DRAG        sum over tag-3 faces of -p A n_x (calculateDrag)
+ *   CFDG_OBJ_SKIN_FRICTION_DRAG   sum over tag-4 faces of tau_w A t_x, tau_w = rho nu u_t / dn
+ *                                 and t the wall tangent with t_x >= 0 (extractSkinFriction)
+ *   CFDG_OBJ_WALL_PRESSURE        sum over tag-4 faces with x0 <= x_mid <= x1 of p A
+ * J gets the value; dJdU (AoS, 6 per cell, reference numbering; may be NULL) dJ/dU. */
+enum { CFDG_OBJ_PRESSURE_DRAG = 0, CFDG_OBJ_SKIN_FRICTION_DRAG = 1, CFDG_OBJ_WALL_PRESSURE = 2 };
+cfdg_status cfdg_objective(cfdg_solver* s, int kind, double x0, double x1, double* J, double* dJdU);
 /* calculateDrag (src/Solver.cpp:1307-1325): sum of -p A n_x over tag-3 faces */
 cfdg_status cfdg_drag(cfdg_solver* s, double* drag);
 /* calculateEntropyError (src/Solver.cpp:1620-1646) */

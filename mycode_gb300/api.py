@@ -106,6 +106,7 @@ SIGNATURES = {
     "cfdg_vjp": (C.c_int, [_vp, C.c_void_p, _dp, _dp]),
     "cfdg_wall_coefficients": (C.c_int, [_vp, C.c_int, C.c_void_p, C.c_void_p, C.c_void_p, C.POINTER(C.c_int)]),
     "cfdg_wall_distance": (C.c_int, [_vp, C.c_void_p]),
+    "cfdg_objective": (C.c_int, [_vp, C.c_int, C.c_double, C.c_double, C.POINTER(C.c_double), C.c_void_p]),
     "cfdg_drag": (C.c_int, [_vp, C.POINTER(C.c_double)]),
     "cfdg_entropy_error": (C.c_int, [_vp, C.POINTER(C.c_double)]),
     "cfdg_residual_device": (C.c_int, [_vp, C.c_int]),
@@ -433,6 +434,18 @@ class Solver:
         d = np.zeros(self.n_cells)
         _check(lib().cfdg_wall_distance(self._h, d.ctypes.data_as(_vp)))
         return d
+
+    OBJECTIVES = {"pressure_drag": 0, "skin_friction_drag": 1, "wall_pressure": 2}
+
+    def objective(self, kind, x0=-1e300, x1=1e300, gradient=True):
+        """J (and dJ/dU, AoS) of a wall objective: pressure_drag, skin_friction_drag or
+        wall_pressure (over tag-4 faces with x0 <= x_mid <= x1)."""
+        k = self.OBJECTIVES[kind] if isinstance(kind, str) else int(kind)
+        J = C.c_double()
+        g = np.zeros(6 * self.n_cells) if gradient else None
+        _check(lib().cfdg_objective(self._h, k, float(x0), float(x1), C.byref(J),
+                                    g.ctypes.data_as(_vp) if gradient else None))
+        return (J.value, g.reshape(-1, 6)) if gradient else J.value
 
     def drag(self):
         d = C.c_double()

@@ -436,14 +436,48 @@ CFD_HD void inviscid_flux_b(const Flow<R>& F, const CS<R>& L, const CS<R>& Rt, R
     else flux_llf_b(F, L, Rt, nx, ny, Fb, Lb, Rb);
 }
 
-// Adjoint of ghost_state: accumulates into the interior state's field adjoints.
+// Adjoint of ghost_state: accumulates into the interior state's field adjoints.  With
+// SST the ghost's rho k and rho w follow sst_ghost (free stream, extrapolated, or the
+// no-slip wall values at the normal distance dwall).
 template <class R>
-CFD_HD void ghost_state_b(const Flow<R>& F, const CS<R>& U, int tag, R nx, R ny, const CSb<R>& gb_in, CSb<R>& Ub) {
+CFD_HD void ghost_state_b(const Flow<R>& F, const CS<R>& U, int tag, R nx, R ny, const CSb<R>& gb_in, CSb<R>& Ub,
+                          R dwall = R(0)) {
     const R g = F.gam;
-    CS<R> gs = ghost_state(F, U, tag, nx, ny);
+    CS<R> gs = ghost_state(F, U, tag, nx, ny, dwall);
     // adjoints of the ghost's conservative variables
     R cb[6] = {R(0), R(0), R(0), R(0), R(0), R(0)};
     cs_back(F, gs, gb_in, cb);
+    if (F.sst) {
+        // 0 free stream, 1 extrapolated, 2 no-slip wall, -1 copied with the state
+        int kind = -1;
+        if (F.bcset == BC_BUMP) kind = tag == 1 ? 0 : tag == 2 ? 1 : -1;
+        else if (F.bcset == BC_SUPERSONIC) kind = (tag == 1 || tag == 6) ? 0 : -1;
+        else kind = tag == 4 ? 2 : -1;
+        if (kind >= 0) {
+            R kb = cb[4], wb = cb[5];
+            cb[4] = cb[5] = R(0);
+            if (kind == 0) {
+                cb[0] += kb * F.k_inf + wb * F.w_inf;
+            } else {
+                R ku = U.rk / U.r, wu = U.rw / U.r;
+                R kub, wub;
+                if (kind == 1) {
+                    cb[0] += kb * ku + wb * wu;
+                    kub = kb * gs.r;
+                    wub = wb * gs.r;
+                } else {
+                    R d = dwall > R(1e-30) ? dwall : R(1e-30);
+                    R ww = R(60.0) * F.nu / (R(0.075) * d * d);
+                    cb[0] += -kb * ku + wb * (R(2.0) * ww - wu);
+                    kub = -kb * gs.r;
+                    wub = -wb * gs.r;
+                }
+                Ub.rk += kub / U.r;
+                Ub.rw += wub / U.r;
+                Ub.r -= (kub * ku + wub * wu) / U.r;
+            }
+        }
+    }
     auto slip = [&]() {
         R vn = U.u * nx + U.v * ny;
         R ug = U.u - R(2.0) * vn * nx, vg = U.v - R(2.0) * vn * ny;
@@ -571,7 +605,7 @@ CFD_HD void reconstruct_b(const Flow<R>& F, const CS<R>& C, const R* g, R ph, R 
 template <class R>
 CFD_HD void face_flux_b(const Flow<R>& F, const CS<R>& L, const CS<R>& Rn, bool interior, int tag,
                         const FaceGeo<R>& g, const R* gL, const R* gR, R phL, R phR, const R* FAb, CSb<R>& Lb,
-                        CSb<R>& Rnb, R* gLb, R* gRb, R& phLb, R& phRb) {
+                        CSb<R>& Rnb, R* gLb, R* gRb, R& phLb, R& phRb, R mutf = R(0), R* mutfb = nullptr) {
     const R nx = g.nx, ny = g.ny;
     R TFb[6];
     for (int c = 0; c < 6; ++c) TFb[c] = FAb[c] * g.A;
@@ -616,6 +650,10 @@ CFD_HD void face_flux_b(const Flow<R>& F, const CS<R>& L, const CS<R>& Rn, bool 
         R Cp = F.gam * F.Rgas / (F.gam - R(1.0));
         R mu = rf * F.nu;
         R kc = mu * Cp / F.Pr;
+        if (F.sst) {
+            kc = kc + mutf * Cp / F.Pr_t;
+            mu = mu + mutf;
+        }
         R div = dudx + dvdy;
         R txx = mu * (R(2.0) * dudx - (R(2.0) / R(3.0)) * div);
         R tyy = mu * (R(2.0) * dvdy - (R(2.0) / R(3.0)) * div);
@@ -631,8 +669,11 @@ CFD_HD void face_flux_b(const Flow<R>& F, const CS<R>& L, const CS<R>& Rn, bool 
         R qxb = -wxb, qyb = -wyb;
         R kcb = -qxb * dTdx - qyb * dTdy;
         R dTdxb = -qxb * kc, dTdyb = -qyb * kc;
-        R mub = kcb * Cp / F.Pr + txxb * (R(2.0) * dudx - (R(2.0) / R(3.0)) * div) +
-                tyyb * (R(2.0) * dvdy - (R(2.0) / R(3.0)) * div) + txyb * (dudy + dvdx);
+        // mu (and kc) of the stresses include mu_t with SST; the laminar part is rf nu
+        R mufb = txxb * (R(2.0) * dudx - (R(2.0) / R(3.0)) * div) + tyyb * (R(2.0) * dvdy - (R(2.0) / R(3.0)) * div) +
+                 txyb * (dudy + dvdx);
+        R mub = kcb * Cp / F.Pr + mufb;
+        if (F.sst && mutfb) *mutfb += mufb + kcb * Cp / F.Pr_t;
         R divb = -(R(2.0) / R(3.0)) * mu * (txxb + tyyb);
         R dudxb = R(2.0) * mu * txxb + divb;
         R dvdyb = R(2.0) * mu * tyyb + divb;
@@ -710,6 +751,64 @@ CFD_HD void face_flux_b(const Flow<R>& F, const CS<R>& L, const CS<R>& Rn, bool 
         Rnb.u += Rtb.u; Rnb.v += Rtb.v; Rnb.p += Rtb.p;
     } else {
         ghost_state_b(F, L, tag, nx, ny, Rtb, Lb);
+    }
+}
+
+// Adjoint of face_flux_sst.  Besides face_flux_b's outputs: the adjoints of each side's
+// k, w gradients (gkLb, gkRb: k_x, k_y, w_x, w_y), mu_t and F1.  On the boundary all of
+// the right-hand ones are folded into the owner's.
+template <class R>
+CFD_HD void face_flux_sst_b(const Flow<R>& F, const CS<R>& L, const CS<R>& Rn, bool interior, int tag,
+                            const FaceGeo<R>& g, const R* gL, const R* gR, const R* gkL, const R* gkR, R phL, R phR,
+                            R mutL, R mutR, R F1L, R F1R, const R* FAb_in, CSb<R>& Lb, CSb<R>& Rnb, R* gLb, R* gRb,
+                            R* gkLb, R* gkRb, R& phLb, R& phRb, R& mutLb, R& mutRb, R& F1Lb, R& F1Rb) {
+    bool wall = !interior && tag == 4;
+    if (!interior) {
+        mutR = mutL;
+        F1R = F1L;
+    }
+    R mutf = wall ? R(0) : R(0.5) * (mutL + mutR);
+    R F1f = R(0.5) * (F1L + F1R);
+    R dwl = wall_normal_distance(g);
+    Flux6<R> out = face_flux(F, L, Rn, interior, tag, g, gL, gR, phL, phR, mutf);
+    CS<R> Rt = face_right(F, L, Rn, interior, tag, g.nx, g.ny, dwl);
+    const R* gkRv = interior ? gkR : gkL;
+    R gkRvb[4] = {R(0), R(0), R(0), R(0)};
+    R kL = L.rk / L.r, wL = L.rw / L.r, kR = Rt.rk / Rt.r, wR = Rt.rw / Rt.r;
+    R mdotAb = 0, kLb = 0, wLb = 0, kRb = 0, wRb = 0, rfb = 0, mutfb = 0, F1fb = 0;
+    sst_face_flux_b(F, out.f[0], kL, wL, kR, wR, R(0.5) * (L.r + Rt.r), mutf, F1f, gkL, gkRv, wall, g.nx, g.ny, g.A,
+                    g.dxL, g.dyL, g.dxlr, g.dylr, FAb_in[4], FAb_in[5], mdotAb, kLb, wLb, kRb, wRb, rfb, mutfb, F1fb,
+                    gkLb, gkRvb);
+    // the mean flow, with the k and w rows' mass-flux adjoint added to row 0
+    R FAb[6] = {FAb_in[0] + mdotAb, FAb_in[1], FAb_in[2], FAb_in[3], R(0), R(0)};
+    face_flux_b(F, L, Rn, interior, tag, g, gL, gR, phL, phR, FAb, Lb, Rnb, gLb, gRb, phLb, phRb, mutf, &mutfb);
+    // k = rho k / rho of both sides, and rf = (rho_L + rho_R) / 2
+    Lb.rk += kLb / L.r;
+    Lb.rw += wLb / L.r;
+    Lb.r += R(0.5) * rfb - (kLb * kL + wLb * wL) / L.r;
+    CSb<R> RtSb = csb_zero<R>();
+    RtSb.rk = kRb / Rt.r;
+    RtSb.rw = wRb / Rt.r;
+    RtSb.r = R(0.5) * rfb - (kRb * kR + wRb * wR) / Rt.r;
+    if (interior) {
+        Rnb.r += RtSb.r;
+        Rnb.rk += RtSb.rk;
+        Rnb.rw += RtSb.rw;
+    } else {
+        ghost_state_b(F, L, tag, g.nx, g.ny, RtSb, Lb, dwl);
+    }
+    R mb = wall ? R(0) : R(0.5) * mutfb;
+    R fb = R(0.5) * F1fb;
+    if (interior) {
+        mutLb += mb;
+        mutRb += mb;
+        F1Lb += fb;
+        F1Rb += fb;
+        for (int q = 0; q < 4; ++q) gkRb[q] += gkRvb[q];
+    } else {
+        mutLb += mb + mb;
+        F1Lb += fb + fb;
+        for (int q = 0; q < 4; ++q) gkLb[q] += gkRvb[q];
     }
 }
 

@@ -4,6 +4,7 @@
 // adjoint, which differentiates exactly this sequence of operations.
 #pragma once
 #include "physics.cuh"
+#include "sst.cuh"
 
 namespace cfdg {
 
@@ -127,6 +128,32 @@ CFD_HD Flux6<S> face_flux(const Flow<R>& F, const CS<S>& L, const CS<S>& Rn, boo
     Flux6<S> out;
 #pragma unroll
     for (int c = 0; c < 6; ++c) out.f[c] = TF.f[c] * g.A;
+    return out;
+}
+
+// F*A of one face with the SST model: the mean-flow rows with the face eddy viscosity
+// mu_t,f = (mu_t,L + mu_t,R) / 2 (zero at a no-slip wall), then the k and w rows
+// (sst_face_flux) from the mean flow's mass flux.  gkL/gkR: k_x, k_y, w_x, w_y of each
+// side.  On the boundary the right-hand mu_t, F1 and k, w gradients are the owner's.
+template <class S, class R>
+CFD_HD Flux6<S> face_flux_sst(const Flow<R>& F, const CS<S>& L, const CS<S>& Rn, bool interior, int tag,
+                              const FaceGeo<R>& g, const S* gL, const S* gR, const S* gkL, const S* gkR, S phL,
+                              S phR, S mutL, S mutR, S F1L, S F1R) {
+    bool wall = !interior && tag == 4;
+    if (!interior) {
+        mutR = mutL;
+        F1R = F1L;
+    }
+    S mutf = wall ? S(R(0)) : R(0.5) * (mutL + mutR);
+    S F1f = R(0.5) * (F1L + F1R);
+    Flux6<S> out = face_flux(F, L, Rn, interior, tag, g, gL, gR, phL, phR, mutf);
+    CS<S> Rt = face_right(F, L, Rn, interior, tag, g.nx, g.ny, wall_normal_distance(g));
+    const S* gkRv = interior ? gkR : gkL;
+    S Fk, Fw;
+    sst_face_flux(F, out.f[0], L.rk / L.r, L.rw / L.r, Rt.rk / Rt.r, Rt.rw / Rt.r, R(0.5) * (L.r + Rt.r), mutf, F1f,
+                  gkL, gkRv, wall, g.nx, g.ny, g.A, g.dxL, g.dyL, g.dxlr, g.dylr, Fk, Fw);
+    out.f[4] = Fk;
+    out.f[5] = Fw;
     return out;
 }
 

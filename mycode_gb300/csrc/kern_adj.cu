@@ -1,5 +1,6 @@
 // Adjoint (VJP) kernels of the FP64 residual: forward recomputation of the primitives,
-// gradients and limiter, then the reverse face and cell kernels of adjoint_kernels.cuh.
+// gradients and limiter (and the SST cell terms), then the reverse face and cell kernels
+// of adjoint_kernels.cuh.
 #include "adjoint_kernels.cuh"
 #include "launch.hpp"
 
@@ -12,10 +13,12 @@ static void vjp_nv(const ResArgs<double>& a, const double* lam, const AdjBufs& b
     if (a.ev) cudaEventRecord(a.ev[0], a.stream);
     k_prim<double, NV><<<grid_for(nc), 256, 0, a.stream>>>((int)nc, a.F, a.U, a.W);
     k_grad<double, NV><<<grid_for(nc), 256, 0, a.stream>>>(a.m, a.F, a.U, a.W, a.G, a.phi, limited);
+    if (NV == 6) k_sst_cell<double, NV><<<grid_for(nc), 256, 0, a.stream>>>(a.m, a.F, a.W, a.G, a.dwall, a.T);
     if (a.ev) cudaEventRecord(a.ev[1], a.stream);
-    k_flux_adj<NV><<<grid_for(nf, 128), 128, 0, a.stream>>>(a.m, a.F, a.U, a.W, a.G, a.phi, lam, b);
+    k_flux_adj<NV><<<grid_for(nf, 128), 128, 0, a.stream>>>(a.m, a.F, a.U, a.W, a.G, a.phi, lam, b, a.T);
     if (a.ev) cudaEventRecord(a.ev[2], a.stream);
-    k_adj_cell1<NV><<<grid_for(nc, 128), 128, 0, a.stream>>>(a.m, a.F, a.U, a.W, a.G, a.phi, limited, b);
+    k_adj_cell1<NV><<<grid_for(nc, 128), 128, 0, a.stream>>>(a.m, a.F, a.U, a.W, a.G, a.phi, limited, b, lam,
+                                                            a.dwall);
     if (a.ev) cudaEventRecord(a.ev[3], a.stream);
     k_adj_cell2<NV><<<grid_for(nc, 128), 128, 0, a.stream>>>(a.m, a.F, a.U, a.W, b, gU);
     if (a.ev) cudaEventRecord(a.ev[4], a.stream);

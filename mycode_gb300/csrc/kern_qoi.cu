@@ -4,6 +4,8 @@
 //   Cp, Cf          extractSkinFriction (src/Solver.cpp:1899-1979); Cp = (p - p_inf) / q_inf
 //   drag            calculateDrag (src/Solver.cpp:1307-1325), summed in reference face order
 //   entropy error   calculateEntropyError (src/Solver.cpp:1620-1646)
+//   objectives      the pressure drag, the skin-friction drag and a wall-pressure
+//                   integral, with their gradients dJ/dU (the adjoint's right-hand side)
 #include "launch.hpp"
 
 namespace cfdg {
@@ -94,6 +96,93 @@ __global__ void __launch_bounds__(RED_THREADS) k_entropy(long nc, Flow<double> F
         v[1] += vol[i];
     }
     grid_finish<2>(v, rs, out2);
+}
+
+// Wall objectives, per listed boundary face of the owner state (the adjoint's right-hand
+// sides): 0 pressure drag -p A n_x (calculateDrag), 1 skin-friction drag tau_w A t_x with
+// tau_w = rho nu u_t / dn (extractSkinFriction's shear), 2 wall-pressure integral p A.
+// Face weights scale each face's term (0 drops it).
+template <int NV>
+__device__ __forceinline__ double objective_term(int kind, long f, const MeshView<double>& m,
+                                                 const Flow<double>& F, const double* __restrict__ U, double* gb) {
+    long o = m.fo[f], nc = m.nc;
+    double r = U[o], ru = U[nc + o], rv = U[2 * nc + o], rE = U[3 * nc + o];
+    double nx = m.nx[f], ny = m.ny[f], A = m.area[f];
+    if (kind == 1) {
+        double tx = -ny, ty = nx;
+        if (tx < 0) {
+            tx = -tx;
+            ty = -ty;
+        }
+        double dn = fabs(m.dxo[f] * nx + m.dyo[f] * ny);
+        if (dn < 1e-12) dn = 1e-12;
+        double uc = ru / r, vc = rv / r;
+        double ut = uc * tx + vc * ty;
+        double tau = (r * F.nu) * (ut / dn);
+        if (gb) {
+            // tau = nu (ru t_x + rv t_y) / dn exactly: no dependence on rho
+            double c = F.nu / dn * A * tx;
+            gb[0] = 0.0;
+            gb[1] = c * tx;
+            gb[2] = c * ty;
+            gb[3] = 0.0;
+        }
+        return tau * A * tx;
+    }
+    double p = pressure(F, r, ru, rv, rE);
+    double s = kind == 0 ? -A * nx : A;
+    if (gb) {
+        double gm = F.gam - 1.0, u = ru / r, v = rv / r;
+        gb[0] = s * gm * 0.5 * (u * u + v * v);
+        gb[1] = -s * gm * u;
+        gb[2] = -s * gm * v;
+        gb[3] = s * gm;
+    }
+    return kind == 0 ? -p * A * nx : p * A;
+}
+
+template <int NV>
+__global__ void k_objective_terms(int n, const int* __restrict__ slots, const double* __restrict__ w, int kind,
+                                  MeshView<double> m, Flow<double> F, const double* __restrict__ U,
+                                  double* __restrict__ terms) {
+    int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= n) return;
+    terms[k] = w[k] * objective_term<NV>(kind, slots[k], m, F, U, nullptr);
+}
+
+// dJ/dU per cell (SoA planes), gathered over the cell's boundary faces with their weights
+// (wslot: weight per boundary slot, slots [nfi, nf))
+template <int NV>
+__global__ void k_objective_grad(int kind, MeshView<double> m, Flow<double> F, const double* __restrict__ U,
+                                 const double* __restrict__ wslot, double* __restrict__ g) {
+    long i = (long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= m.nc) return;
+    long nc = m.nc;
+    double acc[NV];
+#pragma unroll
+    for (int c = 0; c < NV; ++c) acc[c] = 0.0;
+    for (int k = 0; k < 4; ++k) {
+        int e = m.cf[(long)k * nc + i];
+        if (e < 0) break;
+        long f = e >> 1;
+        if (f < m.nfi) continue;
+        double wf = wslot[f - m.nfi];
+        if (wf == 0.0) continue;
+        double gb[4];
+        objective_term<NV>(kind, f, m, F, U, gb);
+        for (int c = 0; c < 4; ++c) acc[c] += wf * gb[c];
+    }
+#pragma unroll
+    for (int c = 0; c < NV; ++c) g[c * nc + i] = acc[c];
+}
+
+void launch_objective(int nv, int kind, int n, const int* slots, const double* w, const double* wslot,
+                      const MeshView<double>& m, const Flow<double>& F, const double* U, double* terms, double* J,
+                      double* grad, cudaStream_t s) {
+    if (n > 0)
+        NV_SWITCH(nv, (k_objective_terms<NVC><<<grid_for(n, 128), 128, 0, s>>>(n, slots, w, kind, m, F, U, terms)));
+    k_sum_in_order<<<1, 32, 0, s>>>(n, terms, J);
+    if (grad) NV_SWITCH(nv, (k_objective_grad<NVC><<<grid_for(m.nc), 256, 0, s>>>(kind, m, F, U, wslot, grad)));
 }
 
 void launch_wall_distance(long nc, const double* xc, const double* yc, int nw, const double* wx, const double* wy,

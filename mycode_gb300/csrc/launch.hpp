@@ -87,6 +87,11 @@ void launch_wall_coeff(int nv, int n, const int* slots, const MeshView<double>& 
 void launch_sum_in_order(int n, const double* terms, double* out, cudaStream_t s);
 void launch_entropy(int nv, long nc, const Flow<double>& F, const double* U, const double* vol, double s_ref,
                     RedScratch rs, double* out2, cudaStream_t s);
+// J = sum in list order of w_k * term(face slots[k]); grad (SoA, may be null) = dJ/dU with
+// the per-boundary-slot weights wslot
+void launch_objective(int nv, int kind, int n, const int* slots, const double* w, const double* wslot,
+                      const MeshView<double>& m, const Flow<double>& F, const double* U, double* terms, double* J,
+                      double* grad, cudaStream_t s);
 
 }  // namespace cfdg
 

@@ -279,28 +279,24 @@ __global__ void __launch_bounds__(256) k_flux(MeshView<R> m, Flow<R> F, Field<R>
         phL = S(phi[o]);
         phR = S(phi[n]);
     }
-    if (NV == 6) {
-        // SST: face eddy viscosity in the mean-flow stresses, then the k and w fluxes
-        bool wall = !interior && tag == 4;
-        S mutL = Acc<S>::ld(T, 0, o), F1L = Acc<S>::ld(T, 1, o);
-        S mutR = interior ? Acc<S>::ld(T, 0, n) : mutL, F1R = interior ? Acc<S>::ld(T, 1, n) : F1L;
-        S mutf = wall ? S(R(0)) : R(0.5) * (mutL + mutR);
-        S F1f = R(0.5) * (F1L + F1R);
-        Flux6<S> out = face_flux(F, L, Rn, interior, tag, g, gL, gR, phL, phR, mutf);
-        CS<S> Rt = face_right(F, L, Rn, interior, tag, g.nx, g.ny, wall_normal_distance(g));
-        S gkL[4] = {Acc<S>::ld(G, G_K, o), Acc<S>::ld(G, G_K + 1, o), Acc<S>::ld(G, G_W, o), Acc<S>::ld(G, G_W + 1, o)};
-        S gkR[4] = {gkL[0], gkL[1], gkL[2], gkL[3]};
+    if constexpr (NV == 6) {
+        S gk[8];
+        gk[0] = Acc<S>::ld(G, G_K, o);
+        gk[1] = Acc<S>::ld(G, G_K + 1, o);
+        gk[2] = Acc<S>::ld(G, G_W, o);
+        gk[3] = Acc<S>::ld(G, G_W + 1, o);
+        gk[4] = gk[0], gk[5] = gk[1], gk[6] = gk[2], gk[7] = gk[3];
+        S mutR = S(R(0)), F1R = S(R(0));
         if (interior) {
-            gkR[0] = Acc<S>::ld(G, G_K, n);
-            gkR[1] = Acc<S>::ld(G, G_K + 1, n);
-            gkR[2] = Acc<S>::ld(G, G_W, n);
-            gkR[3] = Acc<S>::ld(G, G_W + 1, n);
+            gk[4] = Acc<S>::ld(G, G_K, n);
+            gk[5] = Acc<S>::ld(G, G_K + 1, n);
+            gk[6] = Acc<S>::ld(G, G_W, n);
+            gk[7] = Acc<S>::ld(G, G_W + 1, n);
+            mutR = Acc<S>::ld(T, 0, n);
+            F1R = Acc<S>::ld(T, 1, n);
         }
-        S Fk, Fw;
-        sst_face_flux(F, out.f[0], L.rk / L.r, L.rw / L.r, Rt.rk / Rt.r, Rt.rw / Rt.r, R(0.5) * (L.r + Rt.r), mutf,
-                      F1f, gkL, gkR, wall, g.nx, g.ny, g.A, g.dxL, g.dyL, g.dxlr, g.dylr, Fk, Fw);
-        out.f[4] = Fk;
-        out.f[5] = Fw;
+        Flux6<S> out = face_flux_sst(F, L, Rn, interior, tag, g, gL, gR, gk, gk + 4, phL, phR, Acc<S>::ld(T, 0, o),
+                                     mutR, Acc<S>::ld(T, 1, o), F1R);
 #pragma unroll
         for (int c = 0; c < 6; ++c) Acc<S>::st(FA, c, f, out.f[c]);
         return;

@@ -296,7 +296,7 @@ struct cfdg_solver {
         ResArgs<double> a = res64(Uin, out, do_lim);
         a.ev = take_events(0);
         launch_residual<double>(a);
-        launches += 4;
+        launches += nv == 6 ? 5 : 4;
         if (do_lim) limiter_valid = true;
         CK(cudaGetLastError());
         return CFDG_OK;
@@ -357,7 +357,7 @@ struct cfdg_solver {
             a.stream = st;
             a.ev = take_events(4);
             launch_jv<double>(a);
-            launches += 4;
+            launches += nv == 6 ? 5 : 4;
         }
         CK(cudaGetLastError());
         return CFDG_OK;
@@ -382,8 +382,9 @@ struct cfdg_solver {
     // ---- adjoint: gU = (dR/dU)^T lam at Uin, limiter recomputed into a scratch buffer
     cfdg_status ensure_adj() {
         if (adj_mem) return CFDG_OK;
-        const int N = nv + 11;
-        size_t nd = 2 * (size_t)N * nf + (size_t)nv * nc + 10 * (size_t)nc + 2 * (size_t)nc;
+        const int N = nv == 6 ? AdjSlot<6>::N : AdjSlot<4>::N;
+        const int NG = nv == 6 ? 14 : 10;
+        size_t nd = 2 * (size_t)N * nf + (size_t)nv * nc + (size_t)NG * nc + 2 * (size_t)nc;
         TRY(dalloc(&adj_mem, nd));
         TRY(dalloc(&adj_imem, 2 * (size_t)nc));
         TRY(dalloc(&phi_adj, (size_t)nc));
@@ -391,7 +392,7 @@ struct cfdg_solver {
         ab.fb0 = q; q += (size_t)N * nf;
         ab.fb1 = q; q += (size_t)N * nf;
         ab.gpart = q; q += (size_t)nv * nc;
-        ab.accb = q; q += 10 * (size_t)nc;
+        ab.accb = q; q += (size_t)NG * nc;
         ab.pmaxb = q; q += nc;
         ab.pminb = q;
         ab.pmax_face = adj_imem;
@@ -400,13 +401,12 @@ struct cfdg_solver {
     }
 
     cfdg_status vjp_dev(double* Uin, double* lam, double* gout) {
-        if (nv == 6) return fail(CFDG_ERR_UNSUPPORTED, "the adjoint does not cover the SST terms yet");
         TRY(ensure_adj());
         ResArgs<double> a = res64(Uin, nullptr, 0);
         a.phi = phi_adj;
         a.ev = take_events(8);
         launch_vjp64(a, lam, ab, gout);
-        launches += 5;
+        launches += nv == 6 ? 6 : 5;
         CK(cudaGetLastError());
         return CFDG_OK;
     }
@@ -463,7 +463,7 @@ struct cfdg_solver {
             launch_gmres_multidot<float>(L, w32, V32, gd, gd.h2, st);
             launch_gmres_update<float>(L, w32, V32, gd, gd.h2, gd.hsq + 1, st);
             launch_gmres_store<float>(L, w32, V32, gd, st);
-            launches += 10;
+            launches += nv == 6 ? 11 : 10;
         } else {
             launch_gmres_z<double>(nv, nc, V, L, D, z, gd, st);
             ++launches;
@@ -648,7 +648,7 @@ struct cfdg_solver {
                 a.stream = st;
                 a.ev = take_events(4);
                 launch_jv<float>(a);
-                launches += 5;
+                launches += nv == 6 ? 6 : 5;
                 for (int i = 0; i <= j; ++i) {
                     launch_mgs<float>(nv, nc, Vj1, i > 0 ? V32 + (size_t)(i - 1) * L : nullptr, hc + i - 1,
                                       V32 + (size_t)i * L, rs, hc + i, st);
@@ -832,6 +832,49 @@ struct cfdg_solver {
     int* qslots = nullptr;
     double* qbuf = nullptr;
     int qcap = 0;
+    // objectives: listed faces, their weights, the per-boundary-slot weights, terms and J
+    int* oslots = nullptr;
+    double* obuf = nullptr;
+    int ocap = 0;
+
+    // J and (grad != null) dJ/dU into grad (device SoA) for objective kind; see cfdg.h
+    cfdg_status objective(int kind, double x0, double x1, double* grad) {
+        const HostMesh& h = mesh->h;
+        int tag = kind == CFDG_OBJ_PRESSURE_DRAG ? 3 : 4;
+        std::vector<int> faces = tagged_faces(tag);
+        int n = (int)faces.size(), nb = nf - h.n_interior;
+        std::vector<double> w(n, 1.0), wslot(nb, 0.0);
+        for (int k = 0; k < n; ++k) {
+            if (kind == CFDG_OBJ_WALL_PRESSURE) {
+                double xm = h.f_xm[h.face_perm[faces[k]]];
+                w[k] = (xm >= x0 && xm <= x1) ? 1.0 : 0.0;
+            }
+            wslot[faces[k] - h.n_interior] = w[k];
+        }
+        if (n + 1 > ocap || ocap == 0) {
+            cudaFree(oslots);
+            cudaFree(obuf);
+            oslots = nullptr;
+            obuf = nullptr;
+            ocap = 0;
+            TRY(dalloc(&oslots, (size_t)n + 1));
+            TRY(dalloc(&obuf, 2 * ((size_t)n + 1) + (size_t)nb + 1));
+            ocap = n + 1;
+        }
+        double* dw = obuf;
+        double* dterms = obuf + ocap;
+        double* dwslot = obuf + 2 * (size_t)ocap;
+        double* dJ = dwslot + nb;
+        if (n) {
+            CK(cudaMemcpyAsync(oslots, faces.data(), sizeof(int) * n, cudaMemcpyHostToDevice, st));
+            CK(cudaMemcpyAsync(dw, w.data(), sizeof(double) * n, cudaMemcpyHostToDevice, st));
+        }
+        if (nb) CK(cudaMemcpyAsync(dwslot, wslot.data(), sizeof(double) * nb, cudaMemcpyHostToDevice, st));
+        launch_objective(nv, kind, n, oslots, dw, dwslot, mv, F, U, dterms, dJ, grad, st);
+        launches += (n > 0) + 1 + (grad != nullptr);
+        CK(cudaGetLastError());
+        return CFDG_OK;
+    }
 
     // the device slots of the boundary faces with this tag, in reference face order
     std::vector<int> tagged_faces(int tag) const {
@@ -881,6 +924,8 @@ struct cfdg_solver {
     void release() {
         cudaFree(qslots);
         cudaFree(qbuf);
+        cudaFree(oslots);
+        cudaFree(obuf);
         void* pt[] = {Tt, Tj, Tjd, dwall, T32, T32d, dwall32};
         for (void* p : pt) cudaFree(p);
         void* ps[] = {cf, fo, fn, ftag, perm, U, W, G, phi, FA, R, dt, D, stage, Ub, Rb, Up, Rp, vtmp, x, rhs,
@@ -1259,7 +1304,7 @@ cfdg_status cfdg_gradients(cfdg_solver* s, const double* U, double* g10) {
     // the residual's gradient stage (no limiter update) leaves the gradients in G
     ResArgs<double> a = s->res64(Uin, s->R, 0);
     launch_residual<double>(a);
-    s->launches += 4;
+    s->launches += s->nv == 6 ? 5 : 4;
     CK(cudaGetLastError());
     return s->download_aos(s->G, g10, 10, 10);
 }
@@ -1273,7 +1318,7 @@ cfdg_status cfdg_limiters(cfdg_solver* s, const double* U, double* phi) {
     }
     ResArgs<double> a = s->res64(Uin, s->R, 1);
     launch_residual<double>(a);
-    s->launches += 4;
+    s->launches += s->nv == 6 ? 5 : 4;
     s->limiter_valid = true;
     CK(cudaGetLastError());
     return s->download_aos(s->phi, phi, 1, 1);
@@ -1453,6 +1498,17 @@ cfdg_status cfdg_wall_distance(cfdg_solver* s, double* d) {
     CK(cudaMemcpy(dd.data(), s->dwall, sizeof(double) * s->nc, cudaMemcpyDeviceToHost));
     const std::vector<int>& perm = s->mesh->h.cell_perm;
     for (int i = 0; i < s->nc; ++i) d[perm[i]] = dd[i];
+    return CFDG_OK;
+}
+
+cfdg_status cfdg_objective(cfdg_solver* s, int kind, double x0, double x1, double* J, double* dJdU) {
+    if (!s || !J) return fail(CFDG_ERR_ARG, "null solver or output");
+    if (kind < CFDG_OBJ_PRESSURE_DRAG || kind > CFDG_OBJ_WALL_PRESSURE) return fail(CFDG_ERR_ARG, "unknown objective");
+    TRY(s->objective(kind, x0, x1, dJdU ? s->x : nullptr));
+    CK(cudaMemcpyAsync(J, s->obuf + 2 * (size_t)s->ocap + (s->nf - s->mesh->h.n_interior), sizeof(double),
+                       cudaMemcpyDeviceToHost, s->st));
+    if (dJdU) return s->download_aos(s->x, dJdU, s->nv, 6);
+    CK(cudaStreamSynchronize(s->st));
     return CFDG_OK;
 }
 

@@ -112,6 +112,212 @@ CFD_HD void sst_face_flux(const Flow<R>& F, S mdotA, S kL, S wL, S kR, S wR, S r
     Fw = Fw - (mu + sw * mutf) * dwn * A;
 }
 
+// ---------------------------------------------------------------- reverse mode
+// Adjoints of sst_cell's inputs from the adjoints of (mu_t, F1, S_k, S_w), along the
+// branches the forward takes at the same point (the same selections as the Dual forward,
+// so the VJP is the exact transpose of the J v).  Accumulates into the *b outputs.
+template <class R>
+CFD_HD void sst_cell_b(const Flow<R>& F, R r, R k, R w, R ux, R uy, R vx, R vy, R kx, R ky, R wx, R wy, R d,
+                       R mutb, R F1b, R Skb, R Swb, R& rb, R& kb, R& wb, R& uxb, R& uyb, R& vxb, R& vyb, R& kxb,
+                       R& kyb, R& wxb, R& wyb) {
+    typedef SstConst C;
+    const R bs = R(C::beta_s), a1 = R(C::a1), sw2 = R(C::sw2);
+    // forward
+    const R wmin = F.w_inf * R(C::w_min_frac);
+    bool kneg = k < R(0), wlow = w < wmin;
+    R kp = kneg ? R(0) : k;
+    R wp = wlow ? wmin : w;
+    R Sxy = R(0.5) * (uy + vx);
+    R S2 = R(2) * (ux * ux + vy * vy + R(2) * Sxy * Sxy);
+    R Smag = sqrt(S2 + R(1e-30));
+    R nu = F.nu;
+    R dd = d > R(1e-30) ? d : R(1e-30);
+    R gkgw = kx * wx + ky * wy;
+    R CDa = R(2) * r * sw2 * gkgw / wp;
+    bool cdclip = CDa < R(1e-10);
+    R CDkw = cdclip ? R(1e-10) : CDa;
+    R sk = sqrt(kp + R(1e-30));
+    R t1 = sk / (bs * wp * dd);
+    R t2 = R(500) * nu / (dd * dd * wp);
+    bool m1t2 = t1 < t2;
+    R m1 = m1t2 ? t2 : t1;
+    R t3 = R(4) * r * sw2 * kp / (CDkw * dd * dd);
+    bool a1t3 = t3 < m1;
+    R arg1 = a1t3 ? t3 : m1;
+    R a14 = arg1 * arg1 * arg1 * arg1;
+    R F1 = tanh(a14);
+    bool a2t2 = R(2) * t1 < t2;
+    R arg2 = a2t2 ? t2 : R(2) * t1;
+    R F2 = tanh(arg2 * arg2);
+    R da = a1 * wp, ds = Smag * F2;
+    bool dens = da < ds;
+    R den = dens ? ds : da;
+    R mut = r * a1 * kp / den;
+    R beta = F1 * R(C::b1) + (R(1) - F1) * R(C::b2);
+    R gam = F1 * R(C::g1) + (R(1) - F1) * R(C::g2);
+    R Pu = mut * S2, Pl = R(10) * bs * r * kp * wp;
+    bool plim = Pl < Pu;
+    R P = plim ? Pl : Pu;
+    R me = mut + R(1e-30);
+    // reverse
+    R rb_ = 0, kpb = 0, wpb = 0, Pb = 0, gamb = 0, betab = 0, gkgwb = 0;
+    R mutb_ = mutb, F1b_ = F1b;
+    gamb += Swb * r / me * P;
+    rb_ += Swb * gam / me * P;
+    mutb_ -= Swb * gam * r * P / (me * me);
+    Pb += Swb * gam * r / me;
+    betab -= Swb * r * wp * wp;
+    rb_ -= Swb * beta * wp * wp;
+    wpb -= Swb * R(2) * beta * r * wp;
+    F1b_ -= Swb * R(2) * r * sw2 * gkgw / wp;
+    rb_ += Swb * R(2) * (R(1) - F1) * sw2 * gkgw / wp;
+    gkgwb += Swb * R(2) * (R(1) - F1) * r * sw2 / wp;
+    wpb -= Swb * R(2) * (R(1) - F1) * r * sw2 * gkgw / (wp * wp);
+    Pb += Skb;
+    rb_ -= Skb * bs * wp * kp;
+    wpb -= Skb * bs * r * kp;
+    kpb -= Skb * bs * r * wp;
+    R S2b = 0;
+    if (plim) {
+        rb_ += Pb * R(10) * bs * kp * wp;
+        kpb += Pb * R(10) * bs * r * wp;
+        wpb += Pb * R(10) * bs * r * kp;
+    } else {
+        mutb_ += Pb * S2;
+        S2b += Pb * mut;
+    }
+    F1b_ += betab * (R(C::b1) - R(C::b2)) + gamb * (R(C::g1) - R(C::g2));
+    rb_ += mutb_ * a1 * kp / den;
+    kpb += mutb_ * r * a1 / den;
+    R denb = -mutb_ * mut / den;
+    R Smagb = 0, F2b = 0;
+    if (dens) {
+        Smagb += denb * F2;
+        F2b += denb * Smag;
+    } else {
+        wpb += denb * a1;
+    }
+    R arg2b = F2b * (R(1) - F2 * F2) * R(2) * arg2;
+    R t1b = 0, t2b = 0;
+    if (a2t2) t2b += arg2b;
+    else t1b += R(2) * arg2b;
+    R a14b = F1b_ * (R(1) - F1 * F1);
+    R arg1b = a14b * R(4) * arg1 * arg1 * arg1;
+    R t3b = 0, m1b = 0;
+    if (a1t3) t3b += arg1b;
+    else m1b += arg1b;
+    R CDkwb = 0;
+    rb_ += t3b * R(4) * sw2 * kp / (CDkw * dd * dd);
+    kpb += t3b * R(4) * r * sw2 / (CDkw * dd * dd);
+    CDkwb -= t3b * t3 / CDkw;
+    if (m1t2) t2b += m1b;
+    else t1b += m1b;
+    wpb -= t2b * t2 / wp;
+    R skb = t1b / (bs * wp * dd);
+    wpb -= t1b * t1 / wp;
+    kpb += skb / (sk + sk);
+    if (!cdclip) {
+        rb_ += CDkwb * R(2) * sw2 * gkgw / wp;
+        gkgwb += CDkwb * R(2) * r * sw2 / wp;
+        wpb -= CDkwb * CDa / wp;
+    }
+    kxb += gkgwb * wx;
+    wxb += gkgwb * kx;
+    kyb += gkgwb * wy;
+    wyb += gkgwb * ky;
+    S2b += Smagb / (Smag + Smag);
+    uxb += S2b * R(4) * ux;
+    vyb += S2b * R(4) * vy;
+    R Sxyb = S2b * R(8) * Sxy;
+    uyb += R(0.5) * Sxyb;
+    vxb += R(0.5) * Sxyb;
+    if (!wlow) wb += wpb;
+    if (!kneg) kb += kpb;
+    rb += rb_;
+}
+
+// Adjoints of sst_face_flux's inputs from (Fkb, Fwb).  gkLb / gkRb: k_x, k_y, w_x, w_y.
+template <class R>
+CFD_HD void sst_face_flux_b(const Flow<R>& F, R mdotA, R kL, R wL, R kR, R wR, R rf, R mutf, R F1f, const R* gkL,
+                            const R* gkR, bool wall, R nx, R ny, R A, R dxL, R dyL, R dxlr, R dylr, R Fkb, R Fwb,
+                            R& mdotAb, R& kLb, R& wLb, R& kRb, R& wRb, R& rfb, R& mutfb, R& F1fb, R* gkLb,
+                            R* gkRb) {
+    typedef SstConst C;
+    // forward
+    bool mneg = mdotA < R(0), mpos = R(0) < mdotA;
+    R mp = mneg ? R(0) : mdotA, mm = mpos ? R(0) : mdotA;
+    R mu = rf * F.nu;
+    R sk = F1f * R(C::sk1) + (R(1) - F1f) * R(C::sk2);
+    R sw = F1f * R(C::sw1) + (R(1) - F1f) * R(C::sw2);
+    R Dk = mu + sk * mutf, Dw = mu + sw * mutf;
+    R dkn, dwn;
+    R d2w = dxL * dxL + dyL * dyL, dnw = dxL * nx + dyL * ny;
+    R kx = 0, ky = 0, wx = 0, wy = 0, d2 = dxlr * dxlr + dylr * dylr;
+    bool corr = !wall && d2 > R(1e-14);
+    if (wall) {
+        dkn = (R(0) - kL) * dnw / d2w;
+        dwn = (R(0.5) * (wL + wR) - wL) * dnw / d2w;
+    } else {
+        kx = R(0.5) * (gkL[0] + gkR[0]);
+        ky = R(0.5) * (gkL[1] + gkR[1]);
+        wx = R(0.5) * (gkL[2] + gkR[2]);
+        wy = R(0.5) * (gkL[3] + gkR[3]);
+        R kxc = kx, kyc = ky, wxc = wx, wyc = wy;
+        if (corr) {
+            R ck = (kx * dxlr + ky * dylr - (kR - kL)) / d2;
+            R cw = (wx * dxlr + wy * dylr - (wR - wL)) / d2;
+            kxc = kx - ck * dxlr;
+            kyc = ky - ck * dylr;
+            wxc = wx - cw * dxlr;
+            wyc = wy - cw * dylr;
+        }
+        dkn = kxc * nx + kyc * ny;
+        dwn = wxc * nx + wyc * ny;
+    }
+    // reverse of Fk = mp kL + mm kR - Dk dkn A (and w)
+    R mpb = Fkb * kL + Fwb * wL, mmb = Fkb * kR + Fwb * wR;
+    kLb += Fkb * mp;
+    kRb += Fkb * mm;
+    wLb += Fwb * mp;
+    wRb += Fwb * mm;
+    R Dkb = -Fkb * dkn * A, Dwb = -Fwb * dwn * A;
+    R dknb = -Fkb * Dk * A, dwnb = -Fwb * Dw * A;
+    R mub = Dkb + Dwb;
+    R skb = Dkb * mutf, swb = Dwb * mutf;
+    mutfb += Dkb * sk + Dwb * sw;
+    F1fb += skb * (R(C::sk1) - R(C::sk2)) + swb * (R(C::sw1) - R(C::sw2));
+    rfb += mub * F.nu;
+    if (!mneg) mdotAb += mpb;
+    if (!mpos) mdotAb += mmb;
+    if (wall) {
+        kLb -= dknb * dnw / d2w;
+        R t = dwnb * dnw / d2w;
+        wLb += t * (R(0.5) - R(1));
+        wRb += t * R(0.5);
+    } else {
+        R kxb = dknb * nx, kyb = dknb * ny, wxb = dwnb * nx, wyb = dwnb * ny;
+        if (corr) {
+            R ckb = -(kxb * dxlr + kyb * dylr), cwb = -(wxb * dxlr + wyb * dylr);
+            kxb += ckb * dxlr / d2;
+            kyb += ckb * dylr / d2;
+            kRb -= ckb / d2;
+            kLb += ckb / d2;
+            wxb += cwb * dxlr / d2;
+            wyb += cwb * dylr / d2;
+            wRb -= cwb / d2;
+            wLb += cwb / d2;
+        }
+        gkLb[0] += R(0.5) * kxb;
+        gkRb[0] += R(0.5) * kxb;
+        gkLb[1] += R(0.5) * kyb;
+        gkRb[1] += R(0.5) * kyb;
+        gkLb[2] += R(0.5) * wxb;
+        gkRb[2] += R(0.5) * wxb;
+        gkLb[3] += R(0.5) * wyb;
+        gkRb[3] += R(0.5) * wyb;
+    }
+}
+
 // free-stream k and w from turbulence intensity and eddy-viscosity ratio
 inline void sst_freestream(double Tu, double ratio, double U, double nu, double& k, double& w) {
     k = 1.5 * (Tu * U) * (Tu * U);

@@ -994,6 +994,50 @@ int om_wall_coefficients(const om_solver* s, int tag, double* x, double* cp, dou
     return n;
 }
 
+/* Wall objectives over the owner states, summed in face order, and dJ/dU (AoS, may be
+ * NULL): 0 pressure drag -p A n_x over tag 3 (calculateDrag), 1 skin-friction drag
+ * tau_w A t_x over tag 4 (tau_w as extractSkinFriction), 2 p A over tag-4 faces with
+ * x0 <= x_mid <= x1.  No reference counterpart beyond the pressure drag. */
+double om_objective(const om_solver* s, int kind, double x0, double x1, double* grad) {
+    const om_mesh* m = s->m;
+    int tag = kind == 0 ? 3 : 4;
+    double J = 0.0, gm = s->gamma - 1.0;
+    if (grad) memset(grad, 0, sizeof(double) * NV * (size_t)m->n_cells);
+    for (int f = 0; f < m->n_faces; ++f) {
+        if (m->neighbor[f] >= 0 || m->tag[f] != tag) continue;
+        double w = 1.0;
+        if (kind == 2) w = (m->xm[f] >= x0 && m->xm[f] <= x1) ? 1.0 : 0.0;
+        int o = m->owner[f];
+        st_t U = st_load(s->U + NV * o);
+        double nx = m->nx[f], ny = m->ny[f], A = m->area[f];
+        double t, gb[4];
+        if (kind == 1) {
+            double tx = -ny, ty = nx;
+            if (tx < 0) { tx = -tx; ty = -ty; }
+            double dx = m->xm[f] - m->xc[o], dy = m->ym[f] - m->yc[o];
+            double dn = fabs(dx * nx + dy * ny);
+            if (dn < 1e-12) dn = 1e-12;
+            double ut = (U.ru / U.r) * tx + (U.rv / U.r) * ty;
+            double tau = (U.r * s->nu) * (ut / dn);
+            t = tau * A * tx;
+            double c = s->nu / dn * A * tx;
+            gb[0] = 0.0; gb[1] = c * tx; gb[2] = c * ty; gb[3] = 0.0;
+        } else {
+            double p = pressure(U), sc = kind == 0 ? -A * nx : A;
+            double u = U.ru / U.r, v = U.rv / U.r;
+            t = kind == 0 ? -p * A * nx : p * A;
+            gb[0] = sc * gm * 0.5 * (u * u + v * v);
+            gb[1] = -sc * gm * u;
+            gb[2] = -sc * gm * v;
+            gb[3] = sc * gm;
+        }
+        J += w * t;
+        if (grad && w != 0.0)
+            for (int c = 0; c < 4; ++c) grad[NV * o + c] += w * gb[c];
+    }
+    return J;
+}
+
 /* computeWallDistances (src/Solver.cpp:1981-2015): nearest tag-4 face midpoint, 1e10 without walls */
 void om_wall_distance(const om_solver* s, double* d) {
     const om_mesh* m = s->m;

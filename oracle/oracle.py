@@ -97,6 +97,7 @@ def _oracle_lib():
             "om_sst_reset": (None, []),
             "om_wall_coefficients": (C.c_int, [vp, C.c_int, C.c_void_p, C.c_void_p, C.c_void_p]),
             "om_wall_distance": (None, [vp, _dp]),
+            "om_objective": (C.c_double, [vp, C.c_int, C.c_double, C.c_double, C.c_void_p]),
         }
         for name, (res, args) in sig.items():
             fn = getattr(lib, name)
@@ -272,6 +273,14 @@ class OracleSolver(_Base):
         d = np.zeros(self.n_cells)
         self._L.om_wall_distance(self._s, d)
         return d
+
+    OBJECTIVES = {"pressure_drag": 0, "skin_friction_drag": 1, "wall_pressure": 2}
+
+    def objective(self, kind, x0=-1e300, x1=1e300, gradient=True):
+        k = self.OBJECTIVES[kind] if isinstance(kind, str) else int(kind)
+        g = np.zeros(6 * self.n_cells) if gradient else None
+        J = self._L.om_objective(self._s, k, float(x0), float(x1), g.ctypes.data if gradient else None)
+        return (J, g.reshape(-1, 6)) if gradient else J
 
     def residual_sst(self, U, turb_intensity=0.001, mut_ratio=0.01):
         """Residual of the mean flow plus the SST k and w equations (nv = 6, AoS)."""

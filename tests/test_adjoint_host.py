@@ -119,3 +119,141 @@ def test_boundary_face_adjoint(harness, bcset, tags, flux, viscous):
     for tag in tags:
         for seed in (7, 8):
             check(harness, flow_params(), [bcset, flux, 2, viscous, 0, tag], seed)
+
+
+# ---------------------------------------------------------------- SST (nv = 6)
+def _sst_lib(lib):
+    if not getattr(lib, "_sst_ready", False):
+        lib.sst_face_eval.argtypes = [_dp, _ip, _dp, _dp, _dp, _dp, _dp, _dp, _dp, C.c_double, C.c_double, _dp, _dp]
+        lib.sst_face_adj.argtypes = [_dp, _ip, _dp, _dp, _dp, _dp, _dp, _dp, _dp, C.c_double, C.c_double, _dp, _dp,
+                                     _dp, _dp, _dp, _dp, _dp, _dp, _dp, _dp]
+        lib.sst_cell_eval.argtypes = [_dp, _dp, _dp]
+        lib.sst_cell_adj.argtypes = [_dp, _dp, _dp, _dp]
+        lib._sst_ready = True
+    return lib
+
+
+def sst_params(M=0.5, nu=1.5e-3, k_inf=0.2, w_inf=300.0):
+    return np.concatenate([flow_params(M=M, nu=nu), [k_inf, w_inf]])
+
+
+def _deriv(fun, x0, h):
+    d1 = (fun(x0 + h) - fun(x0 - h)) / (2 * h)
+    d2 = (fun(x0 + h / 2) - fun(x0 - h / 2)) / h
+    return (4 * d2 - d1) / 3
+
+
+def check_sst_cell(lib, seed):
+    lib = _sst_lib(lib)
+    rng = np.random.default_rng(seed)
+    p = sst_params()
+    r = 1.2 * (1 + 0.1 * rng.uniform(-1, 1))
+    k = 4.0 * (1 + 0.5 * rng.uniform(-1, 1))
+    w = 300.0 * (1 + 0.5 * rng.uniform(-1, 1))
+    grads = rng.standard_normal(8) * np.array([3e3, 3e3, 3e3, 3e3, 400, 400, 3e4, 3e4])
+    d = rng.uniform(0.03, 0.3)
+    x = np.concatenate([[r, k, w], grads, [d]])
+    lam = rng.standard_normal(4) * np.array([1e3, 1.0, 1e-3, 1e-5])
+    out = np.zeros(4)
+
+    def f(xx):
+        lib.sst_cell_eval(p, xx, out)
+        return float(lam @ out)
+
+    xb = np.zeros(11)
+    lib.sst_cell_adj(p, x, lam.copy(), xb)
+    base = abs(f(x)) + 1e-300
+    for q in range(11):
+        h = 1e-4 * (abs(x[q]) + 1e-3)
+
+        def fun(v, q=q):
+            y = x.copy()
+            y[q] = v
+            return f(y)
+
+        dfd = _deriv(fun, x[q], h)
+        tol = 1e-6 * (abs(dfd) + abs(xb[q])) + 1e-10 * base / (abs(x[q]) + 1e-3)
+        assert abs(dfd - xb[q]) <= tol, f"input {q}: fd {dfd:.10e} adjoint {xb[q]:.10e}"
+
+
+@pytest.mark.parametrize("seed", range(12))
+def test_sst_cell_adjoint(harness, seed):
+    check_sst_cell(harness, seed)
+
+
+def check_sst_face(lib, fl, seed, M=0.5, u=170.0, v=20.0):
+    lib = _sst_lib(lib)
+    rng = np.random.default_rng(seed)
+    p = sst_params(M=M)
+    th = rng.uniform(0, 2 * np.pi)
+    g = np.array([np.cos(th), np.sin(th), 0.013, 0.004, -0.003, -0.005, 0.002, -0.009, 0.005])
+    if not fl[4]:
+        g[5:] = 0.0
+
+    def turb(U):
+        U = U.copy()
+        U[4] = U[0] * 4.0 * (1 + 0.5 * rng.uniform(-1, 1))
+        U[5] = U[0] * 300.0 * (1 + 0.5 * rng.uniform(-1, 1))
+        return U
+
+    UL, UR = turb(state(rng, u=u, v=v)), turb(state(rng, u=u, v=v))
+    gsc = np.array([1, 1, 100, 100, 100, 100, 1e4, 1e4, 10, 10], dtype=float)
+    gksc = np.array([400, 400, 3e4, 3e4], dtype=float)
+    gL, gR = rng.standard_normal(10) * gsc, rng.standard_normal(10) * gsc
+    gkL, gkR = rng.standard_normal(4) * gksc, rng.standard_normal(4) * gksc
+    phL, phR = rng.uniform(0.2, 0.9), rng.uniform(0.2, 0.9)
+    t = np.array([0.02 * rng.uniform(0.5, 1.5), 0.02 * rng.uniform(0.5, 1.5), rng.uniform(0.2, 0.8),
+                  rng.uniform(0.2, 0.8)])
+    fl = np.asarray(fl, dtype=np.int32)
+    lam = rng.standard_normal(6)
+    out = np.zeros(6)
+    names = ["UL", "UR", "gL", "gR", "gkL", "gkR", "t"]
+    vals = dict(UL=UL, UR=UR, gL=gL, gR=gR, gkL=gkL, gkR=gkR, t=t)
+
+    def f(vv, a=phL, b=phR):
+        lib.sst_face_eval(p, fl, g, vv["UL"], vv["UR"], vv["gL"], vv["gR"], vv["gkL"], vv["gkR"], a, b, vv["t"], out)
+        return float(lam @ out)
+
+    adj = {k: np.zeros(len(vals[k])) for k in names}
+    phb = np.zeros(2)
+    lib.sst_face_adj(p, fl, g, UL, UR, gL, gR, gkL, gkR, phL, phR, t, lam.copy(), adj["UL"], adj["UR"], adj["gL"],
+                     adj["gR"], adj["gkL"], adj["gkR"], phb, adj["t"])
+    base = abs(f(vals)) + 1.0
+    scales = dict(gL=gsc, gR=gsc, gkL=gksc, gkR=gksc)
+    for name in names:
+        for q in range(len(vals[name])):
+            x0 = vals[name][q]
+            if name in scales:
+                h = 1e-3 * scales[name][q]
+            elif name == "t":  # the flux is linear in mu_t and F1: a wide step keeps round-off out
+                h = 1e-2 * (abs(x0) + 1e-3)
+            else:
+                h = 1e-4 * (abs(x0) + 1e-3)
+
+            def fun(x, name=name, q=q):
+                vv = {k: a.copy() for k, a in vals.items()}
+                vv[name][q] = x
+                return f(vv)
+
+            dfd = _deriv(fun, x0, h)
+            a = adj[name][q]
+            tol = 1e-6 * (abs(dfd) + abs(a)) + 1e-10 * base
+            assert abs(dfd - a) <= tol, f"{name}[{q}]: fd {dfd:.10e} adjoint {a:.10e}"
+    for s_, (dfd, a) in enumerate(((_deriv(lambda x: f(vals, x, phR), phL, 1e-3), phb[0]),
+                                   (_deriv(lambda x: f(vals, phL, x), phR, 1e-3), phb[1]))):
+        assert abs(dfd - a) <= 1e-6 * (abs(dfd) + abs(a)) + 1e-10 * base, f"phi[{s_}]"
+
+
+@pytest.mark.parametrize("flux", FLUXES)
+@pytest.mark.parametrize("spatial", [0, 1, 2])
+@pytest.mark.parametrize("seed", [1, 2])
+def test_sst_interior_face_adjoint(harness, flux, spatial, seed):
+    check_sst_face(harness, [2, flux, spatial, 1, 1, 0], seed)
+
+
+@pytest.mark.parametrize("bcset,tags", [(0, [1, 2, 3]), (1, [1, 2, 3, 6]), (2, [1, 2, 3, 4, 5])])
+@pytest.mark.parametrize("flux", FLUXES)
+def test_sst_boundary_face_adjoint(harness, bcset, tags, flux):
+    for tag in tags:
+        for seed in (7, 8):
+            check_sst_face(harness, [bcset, flux, 2, 1, 0, tag], seed)

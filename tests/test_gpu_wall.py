@@ -75,3 +75,15 @@ def test_wall_quantities_follow_the_solve(cuda_lib):
     s.solveImplicit(tol=1e-30, max_steps=5)
     o.set_state(s.getSolution())
     np.testing.assert_array_equal(s.wall_coefficients(4)[2], o.wall_coefficients(4)[2])
+
+
+@pytest.mark.parametrize("kind,name", [("pressure_drag", "supersonic"), ("skin_friction_drag", "plate_visc"),
+                                       ("wall_pressure", "plate_visc")])
+def test_objective_and_gradient_bit_exact(cuda_lib, kind, name):
+    s, o = _pair(cuda_lib, name)
+    Js, gs = s.objective(kind, 0.1, 0.6)
+    Jo, go = o.objective(kind, 0.1, 0.6)
+    assert Js == Jo and Js != 0.0
+    np.testing.assert_array_equal(gs, go)
+    if kind == "pressure_drag":
+        assert Js == s.drag()

@@ -70,3 +70,32 @@ def test_wall_coefficients_count_and_cp_definition():
     assert (cf > 0).all()
     assert len(o.wall_coefficients(1)[0]) > 0
     assert len(o.wall_coefficients(7)[0]) == 0
+
+
+@pytest.mark.parametrize("kind", ["pressure_drag", "skin_friction_drag", "wall_pressure"])
+def test_objective_gradient_matches_central_differences(kind):
+    name = "supersonic" if kind == "pressure_drag" else "plate_visc"
+    case = C.CASES[name]
+    o = OracleSolver(case["spec"](), bcset=case["bcset"], viscous=case["viscous"], init=case["init"])
+    C.setup(o, case)
+    U = C.perturbed_state(o.get_state(), o.cells(), seed=4, amplitude=0.08)
+    o.set_state(U)
+    J, g = o.objective(kind, 0.1, 0.6)
+    assert J != 0.0 and np.abs(g).max() > 0
+    rng = np.random.default_rng(1)
+    for _ in range(4):
+        v = rng.standard_normal(U.shape) * np.abs(U).mean(axis=0)
+        v[:, 4:] = 0
+        h = 1e-6
+        o.set_state(U + h * v)
+        jp = o.objective(kind, 0.1, 0.6, gradient=False)
+        o.set_state(U - h * v)
+        jm = o.objective(kind, 0.1, 0.6, gradient=False)
+        fd = (jp - jm) / (2 * h)
+        assert fd == pytest.approx(float(np.sum(g * v)), rel=1e-6, abs=1e-12 * abs(J))
+
+
+@needs_ref
+def test_pressure_drag_objective_is_calculate_drag():
+    o, r, _ = _pair("supersonic")
+    assert o.objective("pressure_drag", gradient=False) == r.drag()
