@@ -68,26 +68,54 @@ def setup_flow(s):
 
 def algorithmic_bytes(kind: str, nc: int, nf: int, nv: int, s: int, spatial: str, viscous: bool, dual: bool) -> float:
     """Compulsory DRAM bytes of one launch: every distinct input read once and every
-    output written once.  s = bytes per real; dual kernels move value + derivative."""
+    output written once.  s = bytes per real; dual kernels move value + derivative.
+    With SST (nv = 6) the primitives carry k, w (7 planes), the gradients 14 planes, and
+    the cell terms (mu_t, F1, S_k vol, S_w vol) are written by the gradient stage (its
+    SST kernel, which also reads the wall distance) and read by the flux and gather."""
     k = 2 if dual else 1
+    sst = nv == 6
+    nq = 7 if sst else 5
+    ng = 2 * nq
     second = spatial != "FIRST_ORDER"
     limited = spatial == "SECOND_ORDER_LIMITED"
     if kind == "prim":
-        return nc * (nv * s * k + 5 * s * k)
+        return nc * (nv * s * k + nq * s * k)
     if kind == "grad":
         # U (ghost faces) is negligible; W of every cell, gradients written, limiter written
-        return nc * (5 * s * k + 10 * s * k + (s if limited and not dual else 0)) + nc * 4 * 4
+        b = nc * (nq * s * k + ng * s * k + (s if limited and not dual else 0)) + nc * 4 * 4
+        if sst:
+            b += nc * (nq * s * k + ng * s * k + s + 4 * s * k)  # the SST cell kernel: W, G, d in, T out
+        return b
     if kind == "flux":
-        per_face = 8 + 9 * s + nv * s * (1 if dual else 1)  # indices, geometry, F*A (derivative only for dual)
+        per_face = 8 + 9 * s + nv * s  # indices, geometry, F*A (derivative only for dual)
         per_cell = nv * s * k + 3 * s * k
         if second or viscous:
-            per_cell += 10 * s * k
+            per_cell += ng * s * k
         if limited:
             per_cell += s
+        if sst:
+            per_cell += 2 * s * k  # mu_t, F1
         return nf * per_face + nc * per_cell
     if kind == "gather":
-        return nc * 16 + nf * nv * s + nc * nv * s + (nc * (nv * s + s + s) if dual else 0)
+        b = nc * 16 + nf * nv * s + nc * nv * s + (nc * (nv * s + s + s) if dual else 0)
+        if sst:
+            b += nc * 2 * s  # the source planes
+        return b
     raise ValueError(kind)
+
+
+def vjp_algorithmic_bytes(nc: int, nf: int, nv: int, spatial: str) -> float:
+    """Compulsory FP64 bytes of one VJP: the forward recomputation (prim, gradients,
+    limiter, SST terms), then the face kernel (state, primitives, gradients, limiter of
+    both cells, lambda, geometry in; 2 x slots out) and the two cell kernels (slots in,
+    gU out).  Slots per face side: nv + gradients + phi (+ mu_t, F1 with SST)."""
+    s = 8
+    ng = 14 if nv == 6 else 10
+    slots = nv + ng + 1 + (2 if nv == 6 else 0)
+    fwd = sum(algorithmic_bytes(kd, nc, nf, nv, s, spatial, True, False) for kd in ("prim", "grad"))
+    face = nf * (8 + 9 * s + 2 * slots * s) + nc * (nv * s + (ng + 7) * s + s + nv * s)
+    cells = nf * 2 * slots * s + nc * (ng * s + 2 * s + 8 + nv * s) + nc * (ng * s + nv * s + nv * s)
+    return fwd + face + cells
 
 
 def measured_peak():
@@ -453,6 +481,120 @@ def reference_arm(args):
     print(json.dumps(line))
 
 
+# ---------------------------------------------------------------- bandwidth sweep
+
+SWEEP_SIZES = (64_000, 256_000, 1_000_000, 4_000_000)
+
+
+def sweep(args):
+    """Per-kernel throughput of the residual, the exact J v and the VJP in FP64 and FP32
+    on the Gaussian-bump channel (3 x 1, height 0.05, width 0.2, triangles, 10 % seeded
+    jitter) at M = 0.5, Re = 3e6 with SST, HLLC, second-order limited; one JSON line."""
+    from mycode_gb300 import api, meshgen
+    import numpy as np
+    peak, peak_kind = measured_peak()
+    sizes = [int(x) for x in args.sweep_sizes.split(",")] if args.sweep_sizes else SWEEP_SIZES
+    out = []
+    for target in sizes:
+        spec = meshgen.bump(target, jitter=0.10, seed=0)
+        mesh = api.Mesh.from_spec(spec)
+        nc, nf = mesh.n_cells, mesh.n_faces
+        s = api.Solver(mesh, bcset="bump", init="bump", viscous=1, turbulence="sst", precision="mixed", jv="exact",
+                       flux="HLLC", spatial="SECOND_ORDER_LIMITED")
+        s.setFlowConditions(0.5, 101325.0, 300.0)
+        s.setKinematicViscosity(3e6, 1.0)
+        s.initialize()
+        U0 = s.getSolution()
+        cells = mesh.cells()
+        pert = meshgen.smooth_perturbation(cells[:, 1:], 7, 0.05)
+        U = U0.copy()
+        for c in range(4):
+            U[:, c] *= 1.0 + pert[:, c]
+        U[:, 4] *= 1.0 + 0.5 * pert[:, 0]
+        U[:, 5] *= 1.0 + 0.5 * pert[:, 1]
+        s.set_state(U)
+        s.residual_device(True)
+        s.set_dt(s.local_timestep(10.0))
+        v = np.random.default_rng(1).standard_normal(U.shape) * np.abs(U).mean(axis=0)
+        lam = np.random.default_rng(2).standard_normal(U.shape)
+        s.set_timing(True)
+        ops = {
+            "residual_fp64": (lambda: s.residual_device(True), "residual.", 8, False),
+            "residual_fp32": (lambda: s.residual32(), "residual.", 4, False),
+            "jv_fp64": (lambda: s.apply_jacobian(U, None, v, mode="exact"), "jv.", 8, True),
+            "jv_fp32": (lambda: s.apply_jacobian32(U, v), "jv.", 4, True),
+            "vjp_fp64": (lambda: s.vjp(lam, U), "vjp.", 8, None),
+        }
+        res = {"n_cells": nc, "n_faces": nf}
+        for name, (fn, cls, sz, dual) in ops.items():
+            for _ in range(2):
+                fn()
+            s.synchronize()
+            s.kernel_stats(reset=True)
+            for _ in range(args.sweep_reps):
+                s.flush_l2(L2_FLUSH_BYTES)
+                fn()
+            s.synchronize()
+            st = s.kernel_stats(reset=True)
+            kern, tot = {}, 0.0
+            for k, (ms, n) in st.items():
+                if not k.startswith(cls) or n == 0:
+                    continue
+                avg = ms / n
+                tot += avg
+                entry = {"avg_us": round(avg * 1e3, 2)}
+                if dual is not None:
+                    b = algorithmic_bytes(k.split(".")[1], nc, nf, 6, sz, "SECOND_ORDER_LIMITED", True, dual)
+                    entry.update(algorithmic_bytes=int(b), gbs=round(b / (avg * 1e-3) / 1e9, 1),
+                                 hbm_frac=round(b / (avg * 1e-3) / 1e9 / peak, 4))
+                kern[k.split(".")[1]] = entry
+            r = {"ms": round(tot, 4), "cell_residuals_per_s": nc / (tot * 1e-3), "kernels": kern}
+            if dual is None:
+                b = vjp_algorithmic_bytes(nc, nf, 6, "SECOND_ORDER_LIMITED")
+                r.update(algorithmic_bytes=int(b), gbs=round(b / (tot * 1e-3) / 1e9, 1),
+                         hbm_frac=round(b / (tot * 1e-3) / 1e9 / peak, 4))
+            res[name] = r
+        res["vjp_fp32"] = None  # the adjoint runs in FP64 only
+        res["vjp_over_residual_fp64"] = res["vjp_fp64"]["ms"] / res["residual_fp64"]["ms"]
+        out.append(res)
+        s.close()
+        del mesh
+    cpu = None
+    if not args.no_cpu_baseline:
+        cpu = sweep_cpu_sample(SWEEP_SIZES[0])
+    line = {"metric": "bandwidth sweep: cell-residuals/s per kernel", "unit": UNIT,
+            "config": {"workload": "Gaussian bump channel 3x1 (height 0.05, width 0.2), triangles, 10% seeded jitter, "
+                                   "M=0.5 Re=3e6, SST, HLLC, 2nd-order limited; seeded smooth perturbation of the "
+                                   "initial state", "l2": "flushed before every evaluation"},
+            "peak_gbs": peak, "peak_source": peak_kind, "sizes": out, "cpu_baseline": cpu}
+    print(json.dumps(line))
+
+
+def sweep_cpu_sample(target: int):
+    """The oracle's FP64 SST residual on one host core at the smallest sweep size."""
+    from oracle.oracle import build_oracle, OracleSolver
+    from mycode_gb300 import meshgen
+    build_oracle()
+    spec = meshgen.bump(target, jitter=0.10, seed=0)
+    o = OracleSolver(spec, bcset="bump", viscous=True, init="bump")
+    o.setNumericalMethod("HLLC", "SECOND_ORDER_LIMITED")
+    o.setFlowConditions(0.5, 101325.0, 300.0)
+    o.setKinematicViscosity(3e6, 1.0)
+    o.initialize()
+    U = o.get_state()
+    k, w = o.sst_freestream()
+    U[:, 4] = U[:, 0] * k
+    U[:, 5] = U[:, 0] * w
+    o.residual_sst(U)
+    n, t0 = 0, time.perf_counter()
+    while time.perf_counter() - t0 < 5.0:
+        o.residual_sst(U)
+        n += 1
+    t = time.perf_counter() - t0
+    return {"value": n * o.n_cells / t, "unit": UNIT, "cores": 1, "kind": "port",
+            "sample": f"{n} FP64 SST residual evaluations of the {o.n_cells}-cell bump on 1 host core, {t:.1f} s"}
+
+
 def main():
     ap = argparse.ArgumentParser(description=__doc__.split("\n")[0])
     ap.add_argument("--gpus", type=int, default=1)
@@ -461,10 +603,15 @@ def main():
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--cpu-seconds", type=float, default=15.0)
+    ap.add_argument("--sweep", action="store_true", help="bandwidth sweep on the bump channel instead")
+    ap.add_argument("--sweep-sizes", default="", help="comma-separated target cell counts")
+    ap.add_argument("--sweep-reps", type=int, default=10)
     args = ap.parse_args()
     if args.warmup < 3:
         ap.error("--warmup must be at least 3")
-    if args.impl == "reference":
+    if args.sweep:
+        sweep(args)
+    elif args.impl == "reference":
         reference_arm(args)
     else:
         ours(args)

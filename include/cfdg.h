@@ -152,6 +152,13 @@ cfdg_status cfdg_get_params(const cfdg_solver* s, double* out6);
 cfdg_status cfdg_set_state(cfdg_solver* s, const double* U);
 cfdg_status cfdg_get_state(cfdg_solver* s, double* U);
 
+/* The mixed-precision kernels on their own (solvers created with precision = mixed):
+ * the FP32 residual of U (AoS, NULL = current state; the limiter recomputed in FP32 for
+ * the limited scheme) and the FP32 exact J v (dual numbers; limiter frozen at the current
+ * FP64 limiter, plus v vol / dt with the current dt).  Outputs widened to FP64 AoS. */
+cfdg_status cfdg_residual32(cfdg_solver* s, const double* U, double* R);
+cfdg_status cfdg_jv32(cfdg_solver* s, const double* Ubase, const double* v, double* Jv);
+
 /* Solver::computeResiduals (src/Solver.cpp:529-801).  U = NULL uses the current state.
  * update_limiters = 0 keeps the last limiter values (the frozen limiter of JFNK). */
 cfdg_status cfdg_residual(cfdg_solver* s, const double* U, double* R, int update_limiters);

@@ -106,6 +106,8 @@ SIGNATURES = {
     "cfdg_vjp": (C.c_int, [_vp, C.c_void_p, _dp, _dp]),
     "cfdg_wall_coefficients": (C.c_int, [_vp, C.c_int, C.c_void_p, C.c_void_p, C.c_void_p, C.POINTER(C.c_int)]),
     "cfdg_wall_distance": (C.c_int, [_vp, C.c_void_p]),
+    "cfdg_residual32": (C.c_int, [_vp, C.c_void_p, _dp]),
+    "cfdg_jv32": (C.c_int, [_vp, _dp, _dp, _dp]),
     "cfdg_objective": (C.c_int, [_vp, C.c_int, C.c_double, C.c_double, C.POINTER(C.c_double), C.c_void_p]),
     "cfdg_drag": (C.c_int, [_vp, C.POINTER(C.c_double)]),
     "cfdg_entropy_error": (C.c_int, [_vp, C.POINTER(C.c_double)]),
@@ -335,6 +337,20 @@ class Solver:
         rb = None if Rb is None else c(Rb)
         _check(lib().cfdg_jv(self._h, c(Ub), None if rb is None else rb.ctypes.data_as(_vp), c(v), J,
                              JV[mode] if isinstance(mode, str) else mode))
+        return J.reshape(-1, 6)
+
+    def residual32(self, U=None):
+        """FP32 residual (mixed-precision solvers), widened to FP64 AoS."""
+        R = np.zeros(6 * self.n_cells)
+        u = None if U is None else np.ascontiguousarray(U, np.float64).ravel()
+        _check(lib().cfdg_residual32(self._h, None if u is None else u.ctypes.data_as(_vp), R))
+        return R.reshape(-1, 6)
+
+    def apply_jacobian32(self, Ub, v):
+        """FP32 exact J v (mixed-precision solvers), widened to FP64 AoS."""
+        J = np.zeros(6 * self.n_cells)
+        c = lambda a: np.ascontiguousarray(a, np.float64).ravel()
+        _check(lib().cfdg_jv32(self._h, c(Ub), c(v), J))
         return J.reshape(-1, 6)
 
     def gmres(self, Ub, Rb, rhs):

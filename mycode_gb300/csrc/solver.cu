@@ -321,6 +321,87 @@ struct cfdg_solver {
         return CFDG_OK;
     }
 
+    cfdg_status download_aos32(const float* dev_soa, double* host) {
+        launch_soa_to_aos<float>(nc, nv, 6, dev_soa, perm, stage, st);
+        ++launches;
+        CK(cudaGetLastError());
+        CK(cudaMemcpyAsync(host, stage, sizeof(double) * 6 * (size_t)nc, cudaMemcpyDeviceToHost, st));
+        CK(cudaStreamSynchronize(st));
+        collect();
+        return CFDG_OK;
+    }
+
+    // ---- FP32 entry points (the mixed-precision kernels on their own; mixed solvers only)
+    // own FP32 direction and output vectors (the Krylov basis and its z are allocated
+    // only with the first GMRES solve)
+    float* f32out = nullptr;
+    float* f32dir = nullptr;
+
+    cfdg_status need_f32() {
+        if (cfg.precision != CFDG_MIXED) return fail(CFDG_ERR_UNSUPPORTED, "FP32 entry points need precision = mixed");
+        if (!f32out) TRY(dalloc(&f32out, (size_t)L));
+        if (!f32dir) TRY(dalloc(&f32dir, (size_t)L));
+        return CFDG_OK;
+    }
+
+    // FP32 residual of Ubase (limiter recomputed in FP32 for the limited scheme) into f32out
+    cfdg_status residual32_dev(double* Ubase) {
+        TRY(need_f32());
+        launch_convert<float>(L, Ubase, U32, st);
+        ResArgs<float> a;
+        a.m = mvf;
+        a.F = Ff;
+        a.nv = nv;
+        a.U = f32(U32);
+        a.W = f32(W32);
+        a.G = f32(G32);
+        a.FA = ff32(FA32d);
+        a.T = f32(T32);
+        a.dwall = dwall32;
+        a.phi = phi32;
+        a.out = f32out;
+        a.do_limiter = cfg.spatial == CFDG_SECOND_ORDER_LIMITED ? 1 : 0;
+        a.diag_v = nullptr;
+        a.dt = nullptr;
+        a.stream = st;
+        a.ev = take_events(0);
+        launch_residual<float>(a);
+        launches += 1 + (nv == 6 ? 5 : 4);
+        CK(cudaGetLastError());
+        return CFDG_OK;
+    }
+
+    // FP32 exact J v (dual numbers, limiter frozen at the FP64 phi, time term with dt) of
+    // direction vdev about Ubase into f32out
+    cfdg_status jv32_dev(double* Ubase, double* vdev) {
+        TRY(need_f32());
+        launch_convert<float>(L, Ubase, U32, st);
+        launch_convert<float>(nc, phi, phi32, st);
+        launch_convert<float>(nc, dt, dt32, st);
+        launch_convert<float>(L, vdev, f32dir, st);
+        ResArgs<float> a;
+        a.m = mvf;
+        a.F = Ff;
+        a.nv = nv;
+        a.U = f32(U32, f32dir);
+        a.W = f32(W32, W32d);
+        a.G = f32(G32, G32d);
+        a.FA = ff32(nullptr, FA32d);
+        a.T = f32(T32, T32d);
+        a.dwall = dwall32;
+        a.phi = phi32;
+        a.out = f32out;
+        a.do_limiter = 0;
+        a.diag_v = f32dir;
+        a.dt = dt32;
+        a.stream = st;
+        a.ev = take_events(4);
+        launch_jv<float>(a);
+        launches += 4 + (nv == 6 ? 5 : 4);
+        CK(cudaGetLastError());
+        return CFDG_OK;
+    }
+
     cfdg_status read_scalars(int first, int n, double* out) {
         CK(cudaMemcpyAsync(out, scal + first, sizeof(double) * n, cudaMemcpyDeviceToHost, st));
         CK(cudaStreamSynchronize(st));
@@ -926,6 +1007,8 @@ struct cfdg_solver {
         cudaFree(qbuf);
         cudaFree(oslots);
         cudaFree(obuf);
+        cudaFree(f32out);
+        cudaFree(f32dir);
         void* pt[] = {Tt, Tj, Tjd, dwall, T32, T32d, dwall32};
         for (void* p : pt) cudaFree(p);
         void* ps[] = {cf, fo, fn, ftag, perm, U, W, G, phi, FA, R, dt, D, stage, Ub, Rb, Up, Rp, vtmp, x, rhs,
@@ -1378,6 +1461,25 @@ cfdg_status cfdg_jv(cfdg_solver* s, const double* Ubase, const double* Rbase, co
     TRY(s->upload_aos(v, s->vtmp));
     TRY(s->jv64(s->Ub, s->Rb, s->vtmp, s->x, mode, false));
     return s->download_aos(s->x, Jv, s->nv, 6);
+}
+
+cfdg_status cfdg_residual32(cfdg_solver* s, const double* U, double* R) {
+    if (!s || !R) return fail(CFDG_ERR_ARG, "null solver or output");
+    double* Uin = s->U;
+    if (U) {
+        TRY(s->upload_aos(U, s->Ub));
+        Uin = s->Ub;
+    }
+    TRY(s->residual32_dev(Uin));
+    return s->download_aos32(s->f32out, R);
+}
+
+cfdg_status cfdg_jv32(cfdg_solver* s, const double* Ubase, const double* v, double* Jv) {
+    if (!s || !Ubase || !v || !Jv) return fail(CFDG_ERR_ARG, "cfdg_jv32: bad arguments");
+    TRY(s->upload_aos(Ubase, s->Ub));
+    TRY(s->upload_aos(v, s->vtmp));
+    TRY(s->jv32_dev(s->Ub, s->vtmp));
+    return s->download_aos32(s->f32out, Jv);
 }
 
 cfdg_status cfdg_gmres(cfdg_solver* s, const double* Ubase, const double* Rbase, const double* rhs, double* x,

@@ -57,9 +57,12 @@ CFD_HD SstCell<S> sst_cell(const Flow<R>& F, S r, S k, S w, S ux, S uy, S vx, S 
     S t1 = sk / (bs * wp * dd);
     S t2 = R(500) * nu / (dd * dd * wp);
     S arg1 = smin(smax(t1, t2), R(4) * r * R(C::sw2) * kp / (CDkw * dd * dd));
+    // tanh(x) is 1 to double precision for x > 20: capping the arguments there changes no
+    // value and keeps arg^4 (up to 1e45 next to a wall) inside FP32 range
+    arg1 = smin(arg1, S(R(10)));
     S a14 = arg1 * arg1 * arg1 * arg1;
     S F1 = tanh_(a14);
-    S arg2 = smax(R(2) * t1, t2);
+    S arg2 = smin(smax(R(2) * t1, t2), S(R(100)));
     S F2 = tanh_(arg2 * arg2);
     S mut = r * a1 * kp / smax(a1 * wp, Smag * F2);
     S beta = F1 * R(C::b1) + (R(1) - F1) * R(C::b2);
@@ -143,11 +146,15 @@ CFD_HD void sst_cell_b(const Flow<R>& F, R r, R k, R w, R ux, R uy, R vx, R vy, 
     R m1 = m1t2 ? t2 : t1;
     R t3 = R(4) * r * sw2 * kp / (CDkw * dd * dd);
     bool a1t3 = t3 < m1;
-    R arg1 = a1t3 ? t3 : m1;
+    R arg1u = a1t3 ? t3 : m1;
+    bool a1cap = R(10) < arg1u;
+    R arg1 = a1cap ? R(10) : arg1u;
     R a14 = arg1 * arg1 * arg1 * arg1;
     R F1 = tanh(a14);
     bool a2t2 = R(2) * t1 < t2;
-    R arg2 = a2t2 ? t2 : R(2) * t1;
+    R arg2u = a2t2 ? t2 : R(2) * t1;
+    bool a2cap = R(100) < arg2u;
+    R arg2 = a2cap ? R(100) : arg2u;
     R F2 = tanh(arg2 * arg2);
     R da = a1 * wp, ds = Smag * F2;
     bool dens = da < ds;
@@ -197,12 +204,12 @@ CFD_HD void sst_cell_b(const Flow<R>& F, R r, R k, R w, R ux, R uy, R vx, R vy, 
     } else {
         wpb += denb * a1;
     }
-    R arg2b = F2b * (R(1) - F2 * F2) * R(2) * arg2;
+    R arg2b = a2cap ? R(0) : F2b * (R(1) - F2 * F2) * R(2) * arg2;
     R t1b = 0, t2b = 0;
     if (a2t2) t2b += arg2b;
     else t1b += R(2) * arg2b;
     R a14b = F1b_ * (R(1) - F1 * F1);
-    R arg1b = a14b * R(4) * arg1 * arg1 * arg1;
+    R arg1b = a1cap ? R(0) : a14b * R(4) * arg1 * arg1 * arg1;
     R t3b = 0, m1b = 0;
     if (a1t3) t3b += arg1b;
     else m1b += arg1b;

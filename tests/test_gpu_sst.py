@@ -192,3 +192,54 @@ def test_turbulent_plate_skin_friction_adjoint_vjp(cuda_lib):
             assert abs(fd[1e-7] - fd[1e-8]) > 1e-7 * abs(a), (d, fd, a)
             bad += 1
     assert bad <= 3
+
+
+def _fp32_pair(api, spec, flow, method, sst=True, **cfg):
+    m = api.Mesh.from_spec(spec)
+    extra = dict(turbulence="sst") if sst else {}
+    s = api.Solver(m, bcset="plate", viscous=1, init="freestream", precision="mixed", jv="exact", **extra, **cfg)
+    s.setNumericalMethod(*method)
+    s.setFreestreamStatic(flow[0], 101325.0, 300.0)
+    s.setKinematicViscosity(flow[1], 1.0)
+    s.initialize()
+    return s
+
+
+@pytest.mark.parametrize("sst", [False, True])
+@pytest.mark.parametrize("spatial", ["FIRST_ORDER", "SECOND_ORDER_CENTRAL", "SECOND_ORDER_LIMITED"])
+def test_fp32_residual_and_jv_track_fp64(cuda_lib, sst, spatial):
+    s = _fp32_pair(cuda_lib, mg.laminar_plate(24, 16, ratio=1.2), (0.3, 1e4), ("ROE", spatial), sst=sst)
+    o = OracleSolver(mg.laminar_plate(24, 16, ratio=1.2), bcset="plate", viscous=True, init="freestream")
+    o.setFreestreamStatic(0.3, 101325.0, 300.0)
+    o.setKinematicViscosity(1e4, 1.0)
+    o.initialize()
+    U = _turbulent_state(o, seed=3) if sst else C.perturbed_state(o.get_state(), o.cells(), seed=3)
+    nv = 6 if sst else 4
+    R64, R32 = s.computeResiduals(U), s.residual32(U)
+    for c in range(nv):
+        scale = np.abs(R64[:, c]).max()
+        assert np.abs(R32[:, c] - R64[:, c]).max() <= 1e-4 * scale, c
+    s.set_dt(s.local_timestep(5.0))
+    v = np.random.default_rng(2).standard_normal(U.shape) * np.abs(U).mean(axis=0)
+    v[:, nv:] = 0
+    J64, J32 = s.apply_jacobian(U, None, v, mode="exact"), s.apply_jacobian32(U, v)
+    for c in range(nv):
+        scale = np.abs(J64[:, c]).max()
+        assert np.abs(J32[:, c] - J64[:, c]).max() <= 1e-3 * scale, c
+
+
+def test_fp32_sst_jv_finite_at_the_omega_floor(cuda_lib):
+    """Next to a wall with the first cell at y+ < 1 and w at its floor, arg1^4 of F1
+    reaches 1e45: FP32 must stay finite (the blending arguments are capped where tanh is
+    already 1), and the mixed-precision Newton step on the full SWBLI grid must too."""
+    spec = mg.swbli(80, 64)
+    s = _fp32_pair(cuda_lib, spec, (2.0, 1e7), ("HLLC", "FIRST_ORDER"))
+    U = s.getSolution()
+    U[:, 5] = U[:, 0] * 1.0  # w = 1, below the w_inf * 1e-6 floor of this flow
+    s.set_dt(s.local_timestep(0.1))
+    v = np.random.default_rng(4).standard_normal(U.shape) * np.abs(U).mean(axis=0)
+    J32 = s.apply_jacobian32(U, v)
+    J64 = s.apply_jacobian(U, None, v, mode="exact")
+    # finiteness is the point here: this state (free stream against a y+ < 1 wall with w
+    # at its floor) is far outside where FP32 derivatives keep their relative accuracy
+    assert np.isfinite(J32).all() and np.isfinite(J64).all()
