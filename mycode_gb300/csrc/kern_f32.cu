@@ -79,13 +79,17 @@ void launch_gmres_v0<float>(long n, float* V0, const double* rhs, const GmresDev
     k_gmres_v0<float><<<red_grid(n), RED_THREADS, 0, s>>>(n, V0, rhs, d);
 }
 template <>
-void launch_gmres_z<float>(int nv, long nc, const float* V, long L, const double* D, float* z, const GmresDev& d,
+void launch_gmres_z<float>(int nv, long nc, const float* V, long L, const float* Dinv, float* z, const GmresDev& d,
                         cudaStream_t s) {
-    NV_SWITCH(nv, (k_gmres_z<float, NVC><<<red_grid(nc), RED_THREADS, 0, s>>>(nc, V, L, D, z, d)));
+    NV_SWITCH(nv, (k_gmres_z<float, NVC><<<red_grid(nc), RED_THREADS, 0, s>>>(nc, V, L, Dinv, z, d)));
+}
+template <>
+void launch_gmres_dinv<float>(int nv, long nc, const double* D, float* Dinv, cudaStream_t s) {
+    NV_SWITCH(nv, (k_gmres_dinv<float, NVC><<<red_grid((nv == 6 ? 3 : 1) * nc), RED_THREADS, 0, s>>>(nc, D, Dinv)));
 }
 template <>
 void launch_gmres_multidot<float>(long L, const float* w, const float* V, const GmresDev& d, double* h, cudaStream_t s) {
-    k_gmres_multidot<float><<<red_grid(L), RED_THREADS, 0, s>>>(L, w, V, d, h);
+    k_gmres_multidot<float><<<kry_grid(L), RED_THREADS, 0, s>>>(L, w, V, d, h);
 }
 template <>
 void launch_gmres_update<float>(long L, float* w, const float* V, const GmresDev& d, const double* h, double* hsq,

@@ -107,13 +107,17 @@ void launch_gmres_v0<double>(long n, double* V0, const double* rhs, const GmresD
     k_gmres_v0<double><<<red_grid(n), RED_THREADS, 0, s>>>(n, V0, rhs, d);
 }
 template <>
-void launch_gmres_z<double>(int nv, long nc, const double* V, long L, const double* D, double* z, const GmresDev& d,
+void launch_gmres_z<double>(int nv, long nc, const double* V, long L, const double* Dinv, double* z, const GmresDev& d,
                         cudaStream_t s) {
-    NV_SWITCH(nv, (k_gmres_z<double, NVC><<<red_grid(nc), RED_THREADS, 0, s>>>(nc, V, L, D, z, d)));
+    NV_SWITCH(nv, (k_gmres_z<double, NVC><<<red_grid(nc), RED_THREADS, 0, s>>>(nc, V, L, Dinv, z, d)));
+}
+template <>
+void launch_gmres_dinv<double>(int nv, long nc, const double* D, double* Dinv, cudaStream_t s) {
+    NV_SWITCH(nv, (k_gmres_dinv<double, NVC><<<red_grid((nv == 6 ? 3 : 1) * nc), RED_THREADS, 0, s>>>(nc, D, Dinv)));
 }
 template <>
 void launch_gmres_multidot<double>(long L, const double* w, const double* V, const GmresDev& d, double* h, cudaStream_t s) {
-    k_gmres_multidot<double><<<red_grid(L), RED_THREADS, 0, s>>>(L, w, V, d, h);
+    k_gmres_multidot<double><<<kry_grid(L), RED_THREADS, 0, s>>>(L, w, V, d, h);
 }
 template <>
 void launch_gmres_update<double>(long L, double* w, const double* V, const GmresDev& d, const double* h, double* hsq,

@@ -53,70 +53,126 @@ static __global__ void k_gmres_init(GmresDev d, int m, double tol, cudaGraphCond
     }
 }
 
+// Arithmetic of the vector kernels.  GB300 issues FP64 at 1/64 of its FP32 rate, so with
+// an FP32 basis the per-element work (products, the update, per-thread and per-warp
+// partial sums of at most a few hundred products) is FP32 and only the block and grid
+// levels of each reduction are FP64; with an FP64 basis everything is FP64.
+template <class T> struct KryAcc { typedef double type; };
+template <> struct KryAcc<float> { typedef float type; };
+
+template <class A>
+__device__ __forceinline__ A warp_sum_t(A v) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+    return v;
+}
+
+// block reduction of K per-thread values: warp sums in A, then FP64 across the warps;
+// the FP64 block sums are valid in thread 0
+template <class A, int K>
+__device__ __forceinline__ void block_sum_mixed(const A (&v)[K], double (&out)[K]) {
+    __shared__ double sm[K][RED_THREADS / 32];
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+#pragma unroll
+    for (int k = 0; k < K; ++k) {
+        A s = warp_sum_t(v[k]);
+        if (lane == 0) sm[k][w] = (double)s;
+    }
+    __syncthreads();
+    if (w == 0) {
+#pragma unroll
+        for (int k = 0; k < K; ++k) {
+            double x = lane < (int)(blockDim.x >> 5) ? sm[k][lane] : 0.0;
+            out[k] = warp_sum(x);
+        }
+    }
+    __syncthreads();
+}
+
 // V0 = rhs * (1/beta)
 template <class T>
 __global__ void k_gmres_v0(long n, T* V0, const double* rhs, GmresDev d) {
     if (d.gi[2]) return;
-    double ib = 1.0 / d.beta[0];
+    __shared__ double ib;
+    if (threadIdx.x == 0) ib = 1.0 / d.beta[0];
+    __syncthreads();
     for (long q = (long)blockIdx.x * blockDim.x + threadIdx.x; q < n; q += (long)gridDim.x * blockDim.x)
         V0[q] = (T)(rhs[q] * ib);
 }
 
+// Dinv = 1 / D per plane (one plane, three with SST), once per solve
+template <class T, int NV>
+__global__ void k_gmres_dinv(long nc, const double* __restrict__ D, T* __restrict__ Dinv) {
+    const long n = (NV == 6 ? 3 : 1) * nc;
+    for (long q = (long)blockIdx.x * blockDim.x + threadIdx.x; q < n; q += (long)gridDim.x * blockDim.x)
+        Dinv[q] = (T)(1.0 / D[q]);
+}
+
 // z = V_j * (1/D) per cell (src/Solver.cpp:1536-1538)
 template <class T, int NV>
-__global__ void k_gmres_z(long nc, const T* V, long L, const double* D, T* z, GmresDev d) {
+__global__ void k_gmres_z(long nc, const T* V, long L, const T* __restrict__ Dinv, T* z, GmresDev d) {
     const T* Vj = V + (long)d.gi[0] * L;
     for (long i = (long)blockIdx.x * blockDim.x + threadIdx.x; i < nc; i += (long)gridDim.x * blockDim.x) {
-        double id[NV];
-        d_inv<NV>(D, nc, i, id);
+        T a = Dinv[i];
 #pragma unroll
-        for (int c = 0; c < NV; ++c) z[c * nc + i] = Vj[c * nc + i] * (T)id[c];
+        for (int c = 0; c < NV; ++c) {
+            T id = (NV == 6 && c >= 4) ? Dinv[(c - 3) * nc + i] : a;
+            z[c * nc + i] = Vj[c * nc + i] * id;
+        }
     }
 }
 
-// h[i] = <w, V_i>, i = 0..j.  Each block owns a contiguous slice of the vectors and
-// accumulates the dot products eight basis vectors at a time (one block reduction per
-// tile of eight); the last block to finish sums each h[i] over the blocks in block order,
+// h[i] = <w, V_i>, i = 0..j.  Sixteen basis vectors per pass over w (each thread keeps
+// sixteen partial products, independent loads in flight); warp sums per vector into
+// shared memory with no block barrier between passes; one barrier, then the block's
+// partials in FP64; the last block to finish sums them over the blocks in block order,
 // one warp per basis vector.
-constexpr int KRY_TILE = 8;
+constexpr int KRY_TILE = 16;
 
 template <class T>
 __global__ void __launch_bounds__(RED_THREADS) k_gmres_multidot(long L, const T* __restrict__ w,
                                                                 const T* __restrict__ V, GmresDev d, double* h) {
+    typedef typename KryAcc<T>::type A;
     const int j = d.gi[0];
-    long per = (L + gridDim.x - 1) / gridDim.x;
-    long lo = (long)blockIdx.x * per;
-    long hi = lo + per < L ? lo + per : L;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarp = blockDim.x >> 5;
+    __shared__ double wsum[KRY_MAXM + 1][RED_THREADS / 32];
     for (int i0 = 0; i0 <= j; i0 += KRY_TILE) {
-        double v[KRY_TILE];
-#pragma unroll
-        for (int t = 0; t < KRY_TILE; ++t) v[t] = 0.0;
         const int nt = (j + 1 - i0) < KRY_TILE ? (j + 1 - i0) : KRY_TILE;
-        for (long q = lo + threadIdx.x; q < hi; q += blockDim.x) {
-            double wq = (double)w[q];
+        A v[KRY_TILE];
+#pragma unroll
+        for (int t = 0; t < KRY_TILE; ++t) v[t] = A(0);
+        for (long q = (long)blockIdx.x * blockDim.x + threadIdx.x; q < L; q += (long)gridDim.x * blockDim.x) {
+            A wq = (A)w[q];
 #pragma unroll
             for (int t = 0; t < KRY_TILE; ++t)
-                if (t < nt) v[t] += wq * (double)V[(long)(i0 + t) * L + q];
+                if (t < nt) v[t] += wq * (A)V[(long)(i0 + t) * L + q];
         }
-        block_sum<KRY_TILE>(v);
-        if (threadIdx.x == 0)
-            for (int t = 0; t < nt; ++t) d.partial[(long)(i0 + t) * RED_BLOCKS + blockIdx.x] = v[t];
-        __syncthreads();
+#pragma unroll
+        for (int t = 0; t < KRY_TILE; ++t)
+            if (t < nt) {
+                A sv = warp_sum_t(v[t]);
+                if (lane == 0) wsum[i0 + t][warp] = (double)sv;
+            }
     }
+    __syncthreads();
+    for (int i = threadIdx.x; i <= j; i += blockDim.x) {
+        double sb = 0.0;
+        for (int ww = 0; ww < nwarp; ++ww) sb += wsum[i][ww];
+        d.partial[(long)i * RED_BLOCKS + blockIdx.x] = sb;
+    }
+    __threadfence();
+    __syncthreads();
     __shared__ bool last;
-    if (threadIdx.x == 0) {
-        __threadfence();
-        last = atomicAdd(d.counter, 1u) == gridDim.x - 1;
-    }
+    if (threadIdx.x == 0) last = atomicAdd(d.counter, 1u) == gridDim.x - 1;
     __syncthreads();
     if (!last) return;
     __threadfence();
-    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
-    for (int i = warp; i <= j; i += nw) {
-        double s = 0.0;
-        for (int b = lane; b < (int)gridDim.x; b += 32) s += ((volatile double*)d.partial)[(long)i * RED_BLOCKS + b];
-        s = warp_sum(s);
-        if (lane == 0) h[i] = s;
+    for (int i = warp; i <= j; i += nwarp) {
+        double sg = 0.0;
+#pragma unroll 4
+        for (int b = lane; b < (int)gridDim.x; b += 32) sg += __ldcg(d.partial + (long)i * RED_BLOCKS + b);
+        sg = warp_sum(sg);
+        if (lane == 0) h[i] = sg;
     }
     __syncthreads();
     if (threadIdx.x == 0) *d.counter = 0u;
@@ -126,31 +182,53 @@ __global__ void __launch_bounds__(RED_THREADS) k_gmres_multidot(long L, const T*
 template <class T>
 __global__ void __launch_bounds__(RED_THREADS) k_gmres_update(long L, T* __restrict__ w, const T* __restrict__ V,
                                                               GmresDev d, const double* h, double* hsq) {
+    typedef typename KryAcc<T>::type A;
     const int j = d.gi[0];
-    __shared__ double hs[KRY_MAXM + 1];
-    for (int i = threadIdx.x; i <= j; i += blockDim.x) hs[i] = h[i];
+    __shared__ A hs[KRY_MAXM + 1];
+    for (int i = threadIdx.x; i <= j; i += blockDim.x) hs[i] = (A)h[i];
     __syncthreads();
-    double v[1] = {0.0};
+    A v[1] = {A(0)};
     for (long q = (long)blockIdx.x * blockDim.x + threadIdx.x; q < L; q += (long)gridDim.x * blockDim.x) {
-        double a = (double)w[q];
-        for (int i = 0; i <= j; ++i) a -= hs[i] * (double)V[(long)i * L + q];
+        A a = (A)w[q];
+        for (int i = 0; i <= j; ++i) a -= hs[i] * (A)V[(long)i * L + q];
         T t = (T)a;
         w[q] = t;
-        v[0] += (double)t * (double)t;
+        v[0] += (A)t * (A)t;
     }
-    grid_finish<1>(v, RedScratch{d.partial, d.counter}, hsq);
+    double bs[1];
+    block_sum_mixed<A, 1>(v, bs);
+    __shared__ bool last;
+    if (threadIdx.x == 0) {
+        d.partial[blockIdx.x] = bs[0];
+        __threadfence();
+        last = atomicAdd(d.counter, 1u) == gridDim.x - 1;
+    }
+    __syncthreads();
+    if (!last) return;
+    __threadfence();
+    double s[1] = {0.0};
+    for (int b = threadIdx.x; b < (int)gridDim.x; b += blockDim.x) s[0] += __ldcg(d.partial + b);
+    block_sum_mixed<double, 1>(s, bs);
+    if (threadIdx.x == 0) {
+        *hsq = bs[0];
+        *d.counter = 0u;
+    }
 }
 
 // V_{j+1} = w / |w| when |w| > 1e-12 (the breakdown guard of src/Solver.cpp:1553-1558)
 template <class T>
 __global__ void k_gmres_store(long L, const T* w, T* V, GmresDev d) {
     const int j = d.gi[0];
-    double hv = sqrt(d.hsq[1]);
-    double inv = hv > 1e-12 ? 1.0 / hv : 1.0;
+    __shared__ T sc;
+    if (threadIdx.x == 0) {
+        double hv = sqrt(d.hsq[1]);
+        sc = (T)(hv > 1e-12 ? 1.0 / hv : 1.0);
+    }
+    __syncthreads();
     T* Vn = V + (long)(j + 1) * L;
-    T s = (T)inv;
+    const T s = sc;
     for (long q = (long)blockIdx.x * blockDim.x + threadIdx.x; q < L; q += (long)gridDim.x * blockDim.x)
-        Vn[q] = hv > 1e-12 ? w[q] * s : w[q];
+        Vn[q] = w[q] * s;
 }
 
 // Hessenberg column, Givens rotations and the convergence test (src/Solver.cpp:1550-1588);
@@ -200,7 +278,8 @@ static __global__ void k_gmres_backsub(GmresDev d) {
     }
 }
 
-// x = sum_{i<=k} V_i y_i / D (src/Solver.cpp:1610-1615); zero when the solve was empty
+// x = (sum_{i<=k} V_i y_i) / D (src/Solver.cpp:1610-1615, accumulated before the
+// scaling); zero when the solve was empty
 template <class T, int NV>
 __global__ void k_gmres_solution_dev(long nc, const T* __restrict__ V, long L, GmresDev d,
                                      const double* __restrict__ D, double* __restrict__ x) {
@@ -212,8 +291,8 @@ __global__ void k_gmres_solution_dev(long nc, const T* __restrict__ V, long L, G
         for (int c = 0; c < NV; ++c) {
             long q = c * nc + i;
             double acc = 0.0;
-            for (int j = 0; j <= k; ++j) acc = acc + (double)V[j * L + q] * d.y[j] * id[c];
-            x[q] = acc;
+            for (int j = 0; j <= k; ++j) acc += (double)V[j * L + q] * d.y[j];
+            x[q] = acc * id[c];
         }
     }
 }

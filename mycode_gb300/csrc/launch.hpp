@@ -71,6 +71,13 @@ inline unsigned red_grid(long n) {
     return (unsigned)(b < RED_BLOCKS ? (b < 1 ? 1 : b) : RED_BLOCKS);
 }
 
+// multi-dot grids: one block per SM at most (few partials for the last block to sum),
+// grid-stride beyond
+inline unsigned kry_grid(long n) {
+    long b = (n + RED_THREADS - 1) / RED_THREADS;
+    return (unsigned)(b < 152 ? (b < 1 ? 1 : b) : 152);
+}
+
 // instantiate a launch for nv = 4 or 6 (NVC is the compile-time count in __VA_ARGS__)
 #define NV_SWITCH(nv, ...)                                      \
     do {                                                        \
@@ -102,7 +109,8 @@ void launch_gmres_init(const GmresDev& d, int m, double tol, cudaGraphConditiona
 void launch_gmres_givens(const GmresDev& d, cudaGraphConditionalHandle h, cudaStream_t s);
 void launch_gmres_backsub(const GmresDev& d, cudaStream_t s);
 template <class T> void launch_gmres_v0(long n, T* V0, const double* rhs, const GmresDev& d, cudaStream_t s);
-template <class T> void launch_gmres_z(int nv, long nc, const T* V, long L, const double* D, T* z, const GmresDev& d,
+template <class T> void launch_gmres_dinv(int nv, long nc, const double* D, T* Dinv, cudaStream_t s);
+template <class T> void launch_gmres_z(int nv, long nc, const T* V, long L, const T* Dinv, T* z, const GmresDev& d,
                                        cudaStream_t s);
 template <class T> void launch_gmres_multidot(long L, const T* w, const T* V, const GmresDev& d, double* h, cudaStream_t s);
 template <class T> void launch_gmres_update(long L, T* w, const T* V, const GmresDev& d, const double* h, double* hsq,

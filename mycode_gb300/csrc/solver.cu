@@ -118,8 +118,9 @@ struct cfdg_solver {
     // FP32 (mixed precision) work
     float *U32 = nullptr, *W32 = nullptr, *W32d = nullptr, *G32 = nullptr, *G32d = nullptr, *FA32d = nullptr,
           *phi32 = nullptr, *dt32 = nullptr, *V32 = nullptr, *z32 = nullptr;
-    // Krylov basis FP64
-    double *V = nullptr, *z = nullptr;
+    // Krylov basis FP64, and 1/D of the solve in the basis precision
+    double *V = nullptr, *z = nullptr, *dinv64 = nullptr;
+    float* dinv32 = nullptr;
     int m_alloc = 0;
     // device-resident GMRES (graph with a WHILE node)
     GmresDev gd{};
@@ -447,14 +448,17 @@ struct cfdg_solver {
     cfdg_status ensure_krylov() {
         int m = cfg.gmres_m;
         if (m_alloc >= m) return CFDG_OK;
-        cudaFree(V); cudaFree(z); cudaFree(V32); cudaFree(z32);
-        V = nullptr; z = nullptr; V32 = nullptr; z32 = nullptr;
+        cudaFree(V); cudaFree(z); cudaFree(V32); cudaFree(z32); cudaFree(dinv32); cudaFree(dinv64);
+        V = nullptr; z = nullptr; V32 = nullptr; z32 = nullptr; dinv32 = nullptr; dinv64 = nullptr;
+        const size_t nd = (size_t)(nv == 6 ? 3 : 1) * nc;
         if (cfg.precision == CFDG_MIXED) {
             TRY(dalloc(&V32, (size_t)(m + 1) * L));
             TRY(dalloc(&z32, (size_t)L));
+            TRY(dalloc(&dinv32, nd));
         } else {
             TRY(dalloc(&V, (size_t)(m + 1) * L));
             TRY(dalloc(&z, (size_t)L));
+            TRY(dalloc(&dinv64, nd));
         }
         m_alloc = m;
         return CFDG_OK;
@@ -499,7 +503,9 @@ struct cfdg_solver {
         const bool mixed = cfg.precision == CFDG_MIXED;
         launch_prim64(nv, nc, F, f64(U), f64(W), st);
         launch_precond(nv, mv, F, U, W, dt, D, Tt, st);
-        launches += 2;
+        if (mixed) launch_gmres_dinv<float>(nv, nc, D, dinv32, st);
+        else launch_gmres_dinv<double>(nv, nc, D, dinv64, st);
+        launches += 3;
         if (mixed) {
             launch_convert<float>(L, Ubase, U32, st);
             launch_convert<float>(nc, phi, phi32, st);
@@ -520,7 +526,7 @@ struct cfdg_solver {
     cfdg_status enqueue_gmres_body(double* Ubase, double* Rbase, cudaGraphConditionalHandle h) {
         const bool mixed = cfg.precision == CFDG_MIXED;
         if (mixed) {
-            launch_gmres_z<float>(nv, nc, V32, L, D, z32, gd, st);
+            launch_gmres_z<float>(nv, nc, V32, L, dinv32, z32, gd, st);
             ResArgs<float> a;
             a.m = mvf;
             a.F = Ff;
@@ -546,7 +552,7 @@ struct cfdg_solver {
             launch_gmres_store<float>(L, w32, V32, gd, st);
             launches += nv == 6 ? 11 : 10;
         } else {
-            launch_gmres_z<double>(nv, nc, V, L, D, z, gd, st);
+            launch_gmres_z<double>(nv, nc, V, L, dinv64, z, gd, st);
             ++launches;
             TRY(jv64(Ubase, Rbase, z, w64, cfg.jv, true));
             launch_gmres_multidot<double>(L, w64, V, gd, gd.h1, st);
@@ -1009,6 +1015,8 @@ struct cfdg_solver {
         cudaFree(obuf);
         cudaFree(f32out);
         cudaFree(f32dir);
+        cudaFree(dinv32);
+        cudaFree(dinv64);
         void* pt[] = {Tt, Tj, Tjd, dwall, T32, T32d, dwall32};
         for (void* p : pt) cudaFree(p);
         void* ps[] = {cf, fo, fn, ftag, perm, U, W, G, phi, FA, R, dt, D, stage, Ub, Rb, Up, Rp, vtmp, x, rhs,
