@@ -90,7 +90,10 @@ typedef struct cfdg_config {
     int krylov;
 } cfdg_config;
 
-enum { CFDG_KRYLOV_AUTO = -1, CFDG_KRYLOV_HOST = 0, CFDG_KRYLOV_GRAPH = 1 };
+/* CFDG_KRYLOV_STREAM launches the graph driver's kernels one iteration at a time from a
+ * host loop (same arithmetic, one sync per iteration; with timing on every kernel is
+ * timed: stat classes 12-17) */
+enum { CFDG_KRYLOV_AUTO = -1, CFDG_KRYLOV_HOST = 0, CFDG_KRYLOV_GRAPH = 1, CFDG_KRYLOV_STREAM = 2 };
 
 /* per-step record of a Newton solve (the reference prints these, src/Solver.cpp:1725-1727, :1746) */
 typedef struct cfdg_step {
@@ -102,6 +105,7 @@ typedef struct cfdg_step {
     int limiter_updated;
     double seconds;        /* wall time of the step */
     double device_ms;      /* CUDA-event time of the step on the solver's stream (timing on) */
+    double krylov_ms;      /* CUDA-event time of the step's Krylov solve (timing on) */
 } cfdg_step;
 
 typedef struct cfdg_mesh cfdg_mesh;
@@ -235,10 +239,12 @@ cfdg_status cfdg_synchronize(cfdg_solver* s);
 cfdg_status cfdg_set_timing(cfdg_solver* s, int on);
 /* per-kernel times of the last timed residual evaluation */
 cfdg_status cfdg_kernel_times(cfdg_solver* s, double* ms_prim, double* ms_grad, double* ms_flux, double* ms_gather);
-/* accumulated per-kernel time and launch count since the last reset (12 classes): 0-3 the
+/* accumulated per-kernel time and launch count since the last reset (18 classes): 0-3 the
  * residual's prim, grad, flux, gather kernels, 4-7 the same kernels of the exact J v,
- * 8-11 the VJP's forward recomputation, face adjoint and its two cell gathers */
-cfdg_status cfdg_kernel_stats(cfdg_solver* s, double* ms12, long long* n12, int reset);
+ * 8-11 the VJP's forward recomputation, face adjoint and its two cell gathers, 12-17 the
+ * stream-driven Krylov body: z + primitives, gradients (+ SST), fluxes, gather + first
+ * CGS pass, update + second pass, final update + Givens */
+cfdg_status cfdg_kernel_stats(cfdg_solver* s, double* ms18, long long* n18, int reset);
 /* VJP at the device-resident state with the device residual as lambda (timing path) */
 cfdg_status cfdg_vjp_device(cfdg_solver* s);
 /* writes `bytes` of device memory on the solver's stream (evicts L2 between timed steps) */

@@ -53,7 +53,7 @@ class Config(C.Structure):
 class Step(C.Structure):
     _fields_ = [("res_vm", C.c_double), ("res_abs", C.c_double), ("res_rho", C.c_double),
                 ("cfl", C.c_double), ("gmres_iters", C.c_int), ("limiter_updated", C.c_int),
-                ("seconds", C.c_double), ("device_ms", C.c_double)]
+                ("seconds", C.c_double), ("device_ms", C.c_double), ("krylov_ms", C.c_double)]
 
 
 _lib = None
@@ -382,6 +382,7 @@ class Solver:
             "gmres_iters": np.array([r.gmres_iters for r in recs], dtype=np.int32),
             "seconds": np.array([r.seconds for r in recs]),
             "device_ms": np.array([r.device_ms for r in recs]),
+            "krylov_ms": np.array([r.krylov_ms for r in recs]),
             "converged": st == 0,
         }
 
@@ -392,7 +393,7 @@ class Solver:
         return s, bool(cv.value)
 
     def set_krylov(self, mode):
-        _check(lib().cfdg_set_krylov(self._h, {"host": 0, "graph": 1}.get(mode, mode)))
+        _check(lib().cfdg_set_krylov(self._h, {"host": 0, "graph": 1, "stream": 2}.get(mode, mode)))
 
     def reset_newton(self):
         _check(lib().cfdg_reset_newton(self._h))
@@ -424,11 +425,13 @@ class Solver:
 
     KERNEL_CLASSES = ["residual.prim", "residual.grad", "residual.flux", "residual.gather",
                       "jv.prim", "jv.grad", "jv.flux", "jv.gather",
-                      "vjp.forward", "vjp.flux_adj", "vjp.cell1", "vjp.cell2"]
+                      "vjp.forward", "vjp.flux_adj", "vjp.cell1", "vjp.cell2",
+                      "krylov.prim_z", "krylov.grad", "krylov.flux", "krylov.gather_dot", "krylov.update_dot",
+                      "krylov.update_final"]
 
     def kernel_stats(self, reset=False):
-        ms = np.zeros(12)
-        n = np.zeros(12, np.int64)
+        ms = np.zeros(len(self.KERNEL_CLASSES))
+        n = np.zeros(len(self.KERNEL_CLASSES), np.int64)
         _check(lib().cfdg_kernel_stats(self._h, ms, n, int(reset)))
         return {k: (float(ms[i]), int(n[i])) for i, k in enumerate(self.KERNEL_CLASSES)}
 

@@ -8,14 +8,14 @@ template <int NV>
 static void residual_nv(const ResArgs<float>& a) {
     long nc = a.m.nc, nf = a.m.nf;
     if (a.ev) cudaEventRecord(a.ev[0], a.stream);
-    k_prim<float, NV><<<grid_for(nc), 256, 0, a.stream>>>((int)nc, a.F, a.U, a.W);
+    k_prim<float, NV><<<blocks_for(nc), tpb_for(nc), 0, a.stream>>>((int)nc, a.F, a.U, a.W);
     if (a.ev) cudaEventRecord(a.ev[1], a.stream);
-    k_grad<float, NV><<<grid_for(nc), 256, 0, a.stream>>>(a.m, a.F, a.U, a.W, a.G, a.phi, a.do_limiter);
-    if (NV == 6) k_sst_cell<float, NV><<<grid_for(nc), 256, 0, a.stream>>>(a.m, a.F, a.W, a.G, a.dwall, a.T);
+    k_grad<float, NV><<<blocks_for(nc), tpb_for(nc), 0, a.stream>>>(a.m, a.F, a.U, a.W, a.G, a.phi, a.do_limiter);
+    if (NV == 6) k_sst_cell<float, NV><<<blocks_for(nc), tpb_for(nc), 0, a.stream>>>(a.m, a.F, a.W, a.G, a.dwall, a.T);
     if (a.ev) cudaEventRecord(a.ev[2], a.stream);
-    k_flux<float, NV><<<grid_for(nf), 256, 0, a.stream>>>(a.m, a.F, a.U, a.W, a.G, a.phi, a.FA, a.T);
+    k_flux<float, NV><<<blocks_for(nf), tpb_for(nf), 0, a.stream>>>(a.m, a.F, a.U, a.W, a.G, a.phi, a.FA, a.T);
     if (a.ev) cudaEventRecord(a.ev[3], a.stream);
-    k_gather<float, NV><<<grid_for(nc), 256, 0, a.stream>>>(a.m, a.FA.v, a.FA.n, a.out, nc, a.diag_v, a.dt,
+    k_gather<float, NV><<<blocks_for(nc), tpb_for(nc), 0, a.stream>>>(a.m, a.FA.v, a.FA.n, a.out, nc, a.diag_v, a.dt,
                                                            NV == 6 ? a.T.v + 2 * nc : nullptr);
     if (a.ev) cudaEventRecord(a.ev[4], a.stream);
 }
@@ -52,17 +52,17 @@ void launch_precond_apply<float>(int nv, long nc, const float* V, const double* 
 template <>
 void launch_gmres_solution<float>(int nv, long nc, const float* V, long vstride, const double* y, int k,
                                   const double* D, double* x, cudaStream_t s) {
-    NV_SWITCH(nv, (k_gmres_solution<float, NVC><<<grid_for(nc), 256, 0, s>>>(nc, V, vstride, y, k, D, x)));
+    NV_SWITCH(nv, (k_gmres_solution<float, NVC><<<blocks_for(nc), tpb_for(nc), 0, s>>>(nc, V, vstride, y, k, D, x)));
 }
 template <>
 void launch_aos_to_soa<float>(long nc, int np, int stride, const double* aos, const int* perm, float* soa,
                                  cudaStream_t s) {
-    k_aos_to_soa<float><<<grid_for(nc), 256, 0, s>>>(nc, np, stride, aos, perm, soa);
+    k_aos_to_soa<float><<<blocks_for(nc), tpb_for(nc), 0, s>>>(nc, np, stride, aos, perm, soa);
 }
 template <>
 void launch_soa_to_aos<float>(long nc, int np, int stride, const float* soa, const int* perm, double* aos,
                                  cudaStream_t s) {
-    k_soa_to_aos<float><<<grid_for(nc), 256, 0, s>>>(nc, np, stride, soa, perm, aos);
+    k_soa_to_aos<float><<<blocks_for(nc), tpb_for(nc), 0, s>>>(nc, np, stride, soa, perm, aos);
 }
 
 __global__ void k_convert_f32(long n, const double* __restrict__ in, float* __restrict__ out) {
@@ -92,18 +92,29 @@ void launch_gmres_multidot<float>(long L, const float* w, const float* V, const 
     k_gmres_multidot<float><<<kry_grid(L), RED_THREADS, 0, s>>>(L, w, V, d, h);
 }
 template <>
-void launch_gmres_update<float>(long L, float* w, const float* V, const GmresDev& d, const double* h, double* hsq,
-                             cudaStream_t s) {
-    k_gmres_update<float><<<red_grid(L), RED_THREADS, 0, s>>>(L, w, V, d, h, hsq);
+void launch_gmres_prim_z<float>(int nv, long nc, const Flow<float>& F, const float* U, const float* V, long L, const float* Dinv,
+                             float* z, Field<float> W, const GmresDev& d, cudaStream_t s) {
+    NV_SWITCH(nv, (k_gmres_prim_z<float, NVC><<<blocks_for(nc), tpb_for(nc), 0, s>>>((int)nc, F, U, V, L, Dinv, z, W, d)));
 }
 template <>
-void launch_gmres_store<float>(long L, const float* w, float* V, const GmresDev& d, cudaStream_t s) {
-    k_gmres_store<float><<<red_grid(L), RED_THREADS, 0, s>>>(L, w, V, d);
+void launch_gmres_gather_dot<float>(int nv, const MeshView<float>& m, const float* FA, float* w, const float* z, const float* dt,
+                                 const float* src, const float* V, long L, const GmresDev& d, cudaStream_t s) {
+    NV_SWITCH(nv, (k_gmres_gather_dot<float, NVC><<<dot_cells_grid(m.nc), tpb_for(m.nc), 0, s>>>(m, FA, m.nf, w, z, dt, src, V, L,
+                                                                                     d)));
+}
+template <>
+void launch_gmres_update_dot<float>(long L, float* w, const float* V, const GmresDev& d, cudaStream_t s) {
+    k_gmres_update_dot<float><<<red_grid(L), RED_THREADS, 0, s>>>(L, w, V, d);
+}
+template <>
+void launch_gmres_update_final<float>(long L, const float* w, float* V, const GmresDev& d, cudaGraphConditionalHandle h,
+                                   cudaStream_t s) {
+    k_gmres_update_final<float><<<red_grid(L), RED_THREADS, 0, s>>>(L, w, V, d, h);
 }
 template <>
 void launch_gmres_solution_dev<float>(int nv, long nc, const float* V, long L, const GmresDev& d, const double* D,
                                    double* x, cudaStream_t s) {
-    NV_SWITCH(nv, (k_gmres_solution_dev<float, NVC><<<grid_for(nc), 256, 0, s>>>(nc, V, L, d, D, x)));
+    NV_SWITCH(nv, (k_gmres_solution_dev<float, NVC><<<blocks_for(nc), tpb_for(nc), 0, s>>>(nc, V, L, d, D, x)));
 }
 
 }  // namespace cfdg

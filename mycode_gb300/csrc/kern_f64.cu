@@ -8,14 +8,14 @@ template <int NV>
 static void residual_nv(const ResArgs<double>& a) {
     long nc = a.m.nc, nf = a.m.nf;
     if (a.ev) cudaEventRecord(a.ev[0], a.stream);
-    k_prim<double, NV><<<grid_for(nc), 256, 0, a.stream>>>((int)nc, a.F, a.U, a.W);
+    k_prim<double, NV><<<blocks_for(nc), tpb_for(nc), 0, a.stream>>>((int)nc, a.F, a.U, a.W);
     if (a.ev) cudaEventRecord(a.ev[1], a.stream);
-    k_grad<double, NV><<<grid_for(nc), 256, 0, a.stream>>>(a.m, a.F, a.U, a.W, a.G, a.phi, a.do_limiter);
-    if (NV == 6) k_sst_cell<double, NV><<<grid_for(nc), 256, 0, a.stream>>>(a.m, a.F, a.W, a.G, a.dwall, a.T);
+    k_grad<double, NV><<<blocks_for(nc), tpb_for(nc), 0, a.stream>>>(a.m, a.F, a.U, a.W, a.G, a.phi, a.do_limiter);
+    if (NV == 6) k_sst_cell<double, NV><<<blocks_for(nc), tpb_for(nc), 0, a.stream>>>(a.m, a.F, a.W, a.G, a.dwall, a.T);
     if (a.ev) cudaEventRecord(a.ev[2], a.stream);
-    k_flux<double, NV><<<grid_for(nf), 256, 0, a.stream>>>(a.m, a.F, a.U, a.W, a.G, a.phi, a.FA, a.T);
+    k_flux<double, NV><<<blocks_for(nf), tpb_for(nf), 0, a.stream>>>(a.m, a.F, a.U, a.W, a.G, a.phi, a.FA, a.T);
     if (a.ev) cudaEventRecord(a.ev[3], a.stream);
-    k_gather<double, NV><<<grid_for(nc), 256, 0, a.stream>>>(a.m, a.FA.v, a.FA.n, a.out, nc, a.diag_v, a.dt,
+    k_gather<double, NV><<<blocks_for(nc), tpb_for(nc), 0, a.stream>>>(a.m, a.FA.v, a.FA.n, a.out, nc, a.diag_v, a.dt,
                                                            NV == 6 ? a.T.v + 2 * nc : nullptr);
     if (a.ev) cudaEventRecord(a.ev[4], a.stream);
 }
@@ -27,8 +27,8 @@ void launch_residual<double>(const ResArgs<double>& a) {
 }
 
 void launch_prim64(int nv, long nc, const Flow<double>& F, Field<double> U, Field<double> W, cudaStream_t s) {
-    if (nv == 6) k_prim<double, 6><<<grid_for(nc), 256, 0, s>>>((int)nc, F, U, W);
-    else k_prim<double, 4><<<grid_for(nc), 256, 0, s>>>((int)nc, F, U, W);
+    if (nv == 6) k_prim<double, 6><<<blocks_for(nc), tpb_for(nc), 0, s>>>((int)nc, F, U, W);
+    else k_prim<double, 4><<<blocks_for(nc), tpb_for(nc), 0, s>>>((int)nc, F, U, W);
 }
 
 
@@ -57,17 +57,17 @@ void launch_precond_apply<double>(int nv, long nc, const double* V, const double
 template <>
 void launch_gmres_solution<double>(int nv, long nc, const double* V, long vstride, const double* y, int k,
                                    const double* D, double* x, cudaStream_t s) {
-    NV_SWITCH(nv, (k_gmres_solution<double, NVC><<<grid_for(nc), 256, 0, s>>>(nc, V, vstride, y, k, D, x)));
+    NV_SWITCH(nv, (k_gmres_solution<double, NVC><<<blocks_for(nc), tpb_for(nc), 0, s>>>(nc, V, vstride, y, k, D, x)));
 }
 template <>
 void launch_aos_to_soa<double>(long nc, int np, int stride, const double* aos, const int* perm, double* soa,
                                  cudaStream_t s) {
-    k_aos_to_soa<double><<<grid_for(nc), 256, 0, s>>>(nc, np, stride, aos, perm, soa);
+    k_aos_to_soa<double><<<blocks_for(nc), tpb_for(nc), 0, s>>>(nc, np, stride, aos, perm, soa);
 }
 template <>
 void launch_soa_to_aos<double>(long nc, int np, int stride, const double* soa, const int* perm, double* aos,
                                  cudaStream_t s) {
-    k_soa_to_aos<double><<<grid_for(nc), 256, 0, s>>>(nc, np, stride, soa, perm, aos);
+    k_soa_to_aos<double><<<blocks_for(nc), tpb_for(nc), 0, s>>>(nc, np, stride, soa, perm, aos);
 }
 
 void launch_fd_perturb(long n, const double* U, const double* v, const double* u_sq, const double* v_sq, double* Up,
@@ -83,23 +83,20 @@ void launch_norm_vm(int nv, long nc, const double* R, const double* vol, RedScra
 }
 void launch_local_dt(int nv, const MeshView<double>& m, const Flow<double>& F, const double* U, const double* W,
                      double cfl, double* dt, cudaStream_t s) {
-    NV_SWITCH(nv, (k_local_dt<NVC><<<grid_for(m.nc), 256, 0, s>>>(m, F, U, W, cfl, dt)));
+    NV_SWITCH(nv, (k_local_dt<NVC><<<blocks_for(m.nc), tpb_for(m.nc), 0, s>>>(m, F, U, W, cfl, dt)));
 }
 void launch_precond(int nv, const MeshView<double>& m, const Flow<double>& F, const double* U, const double* W,
                     const double* dt, double* D, const double* mut, cudaStream_t s) {
-    NV_SWITCH(nv, (k_precond<NVC><<<grid_for(m.nc), 256, 0, s>>>(m, F, U, W, dt, D, mut)));
+    NV_SWITCH(nv, (k_precond<NVC><<<blocks_for(m.nc), tpb_for(m.nc), 0, s>>>(m, F, U, W, dt, D, mut)));
 }
 void launch_newton_update(int nv, long nc, double* U, const double* dU, double relax, double gam, double wmin, int* bad,
                           cudaStream_t s) {
-    NV_SWITCH(nv, (k_newton_update<NVC><<<grid_for(nc), 256, 0, s>>>(nc, U, dU, relax, gam, wmin, bad)));
+    NV_SWITCH(nv, (k_newton_update<NVC><<<blocks_for(nc), tpb_for(nc), 0, s>>>(nc, U, dU, relax, gam, wmin, bad)));
 }
 
 // ---- device-resident GMRES
 void launch_gmres_init(const GmresDev& d, int m, double tol, cudaGraphConditionalHandle h, cudaStream_t s) {
     k_gmres_init<<<1, 1, 0, s>>>(d, m, tol, h);
-}
-void launch_gmres_givens(const GmresDev& d, cudaGraphConditionalHandle h, cudaStream_t s) {
-    k_gmres_givens<<<1, 1, 0, s>>>(d, h);
 }
 void launch_gmres_backsub(const GmresDev& d, cudaStream_t s) { k_gmres_backsub<<<1, 1, 0, s>>>(d); }
 template <>
@@ -120,18 +117,29 @@ void launch_gmres_multidot<double>(long L, const double* w, const double* V, con
     k_gmres_multidot<double><<<kry_grid(L), RED_THREADS, 0, s>>>(L, w, V, d, h);
 }
 template <>
-void launch_gmres_update<double>(long L, double* w, const double* V, const GmresDev& d, const double* h, double* hsq,
-                             cudaStream_t s) {
-    k_gmres_update<double><<<red_grid(L), RED_THREADS, 0, s>>>(L, w, V, d, h, hsq);
+void launch_gmres_prim_z<double>(int nv, long nc, const Flow<double>& F, const double* U, const double* V, long L, const double* Dinv,
+                             double* z, Field<double> W, const GmresDev& d, cudaStream_t s) {
+    NV_SWITCH(nv, (k_gmres_prim_z<double, NVC><<<blocks_for(nc), tpb_for(nc), 0, s>>>((int)nc, F, U, V, L, Dinv, z, W, d)));
 }
 template <>
-void launch_gmres_store<double>(long L, const double* w, double* V, const GmresDev& d, cudaStream_t s) {
-    k_gmres_store<double><<<red_grid(L), RED_THREADS, 0, s>>>(L, w, V, d);
+void launch_gmres_gather_dot<double>(int nv, const MeshView<double>& m, const double* FA, double* w, const double* z, const double* dt,
+                                 const double* src, const double* V, long L, const GmresDev& d, cudaStream_t s) {
+    NV_SWITCH(nv, (k_gmres_gather_dot<double, NVC><<<dot_cells_grid(m.nc), tpb_for(m.nc), 0, s>>>(m, FA, m.nf, w, z, dt, src, V, L,
+                                                                                     d)));
+}
+template <>
+void launch_gmres_update_dot<double>(long L, double* w, const double* V, const GmresDev& d, cudaStream_t s) {
+    k_gmres_update_dot<double><<<red_grid(L), RED_THREADS, 0, s>>>(L, w, V, d);
+}
+template <>
+void launch_gmres_update_final<double>(long L, const double* w, double* V, const GmresDev& d, cudaGraphConditionalHandle h,
+                                   cudaStream_t s) {
+    k_gmres_update_final<double><<<red_grid(L), RED_THREADS, 0, s>>>(L, w, V, d, h);
 }
 template <>
 void launch_gmres_solution_dev<double>(int nv, long nc, const double* V, long L, const GmresDev& d, const double* D,
                                    double* x, cudaStream_t s) {
-    NV_SWITCH(nv, (k_gmres_solution_dev<double, NVC><<<grid_for(nc), 256, 0, s>>>(nc, V, L, d, D, x)));
+    NV_SWITCH(nv, (k_gmres_solution_dev<double, NVC><<<blocks_for(nc), tpb_for(nc), 0, s>>>(nc, V, L, d, D, x)));
 }
 
 }  // namespace cfdg

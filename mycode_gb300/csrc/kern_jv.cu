@@ -11,16 +11,41 @@ static void jv_nv(const ResArgs<R>& a) {
     typedef Dual<R> S;
     long nc = a.m.nc, nf = a.m.nf;
     if (a.ev) cudaEventRecord(a.ev[0], a.stream);
-    k_prim<S, NV><<<grid_for(nc), 256, 0, a.stream>>>((int)nc, a.F, a.U, a.W);
+    k_prim<S, NV><<<blocks_for(nc), tpb_for(nc), 0, a.stream>>>((int)nc, a.F, a.U, a.W);
     if (a.ev) cudaEventRecord(a.ev[1], a.stream);
-    k_grad<S, NV><<<grid_for(nc), 256, 0, a.stream>>>(a.m, a.F, a.U, a.W, a.G, a.phi, 0);
-    if (NV == 6) k_sst_cell<S, NV><<<grid_for(nc), 256, 0, a.stream>>>(a.m, a.F, a.W, a.G, a.dwall, a.T);
+    k_grad<S, NV><<<blocks_for(nc), tpb_for(nc), 0, a.stream>>>(a.m, a.F, a.U, a.W, a.G, a.phi, 0);
+    if (NV == 6) k_sst_cell<S, NV><<<blocks_for(nc), tpb_for(nc), 0, a.stream>>>(a.m, a.F, a.W, a.G, a.dwall, a.T);
     if (a.ev) cudaEventRecord(a.ev[2], a.stream);
-    k_flux<S, NV><<<grid_for(nf), 256, 0, a.stream>>>(a.m, a.F, a.U, a.W, a.G, a.phi, a.FA, a.T);
+    k_flux<S, NV><<<blocks_for(nf), tpb_for(nf), 0, a.stream>>>(a.m, a.F, a.U, a.W, a.G, a.phi, a.FA, a.T);
     if (a.ev) cudaEventRecord(a.ev[3], a.stream);
-    k_gather<R, NV><<<grid_for(nc), 256, 0, a.stream>>>(a.m, a.FA.d, a.FA.n, a.out, nc, a.diag_v, a.dt,
+    k_gather<R, NV><<<blocks_for(nc), tpb_for(nc), 0, a.stream>>>(a.m, a.FA.d, a.FA.n, a.out, nc, a.diag_v, a.dt,
                                                          NV == 6 ? a.T.d + 2 * nc : nullptr);
     if (a.ev) cudaEventRecord(a.ev[4], a.stream);
+}
+
+// a.ev (optional): 3 events around the gradient (+ SST) and flux stages
+template <class R, int NV>
+static void jv_mid_nv(const ResArgs<R>& a) {
+    typedef Dual<R> S;
+    long nc = a.m.nc, nf = a.m.nf;
+    if (a.ev) cudaEventRecord(a.ev[0], a.stream);
+    k_grad<S, NV><<<blocks_for(nc), tpb_for(nc), 0, a.stream>>>(a.m, a.F, a.U, a.W, a.G, a.phi, 0);
+    if (NV == 6) k_sst_cell<S, NV><<<blocks_for(nc), tpb_for(nc), 0, a.stream>>>(a.m, a.F, a.W, a.G, a.dwall, a.T);
+    if (a.ev) cudaEventRecord(a.ev[1], a.stream);
+    k_flux<S, NV><<<blocks_for(nf), tpb_for(nf), 0, a.stream>>>(a.m, a.F, a.U, a.W, a.G, a.phi, a.FA, a.T);
+    if (a.ev) cudaEventRecord(a.ev[2], a.stream);
+}
+
+template <>
+void launch_jv_mid<double>(const ResArgs<double>& a) {
+    if (a.nv == 6) jv_mid_nv<double, 6>(a);
+    else jv_mid_nv<double, 4>(a);
+}
+
+template <>
+void launch_jv_mid<float>(const ResArgs<float>& a) {
+    if (a.nv == 6) jv_mid_nv<float, 6>(a);
+    else jv_mid_nv<float, 4>(a);
 }
 
 template <>

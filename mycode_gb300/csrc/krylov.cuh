@@ -2,14 +2,22 @@
 // node, with the Hessenberg column, the Givens rotations and the convergence test on the
 // device, so a whole Krylov solve is one graph launch with no host round trip.
 //
-// Orthogonalisation is classical Gram-Schmidt applied twice (CGS2): two multi-dot
-// kernels and two update kernels per iteration whatever the iteration index, against
-// j+2 launches for modified Gram-Schmidt.  The Givens/least-squares arithmetic is the
-// reference's (src/Solver.cpp:1562-1599) in FP64.
+// Orthogonalisation is classical Gram-Schmidt applied twice (CGS2).  Each pass's dot
+// products are fused into the kernel that produces the vector they read:
+//   J v gather   -> w and h1 = V^T w                       (k_gmres_gather_dot)
+//   w -= V h1    -> w and h2 = V^T w                       (k_gmres_update_dot)
+//   w -= V h2    -> V_{j+1}, |w|, and the Givens step      (k_gmres_update_final)
+// Every thread reads back only the elements it wrote itself, so no grid barrier is
+// needed inside a kernel; the last block to finish each kernel sums the block partials
+// in block order (deterministic).  Basis vectors are stored unnormalised with a scale
+// factor sc[i] = 1/|V_i| (FP64) applied wherever they are read.  The Givens and
+// least-squares arithmetic is the reference's (src/Solver.cpp:1562-1599) in FP64.
 //
-// Termination: k_gmres_givens is the only kernel that advances j, it runs once per body
-// execution, and it clears the loop condition when j + 1 reaches m (or on convergence),
-// so the loop runs at most m times.
+// Termination: the last block of k_gmres_update_final is the only place that advances j;
+// it runs once per body execution and clears the loop condition when j + 1 reaches m (or
+// on convergence), so the loop runs at most m times.  The same kernels also run outside a
+// graph (in_graph = 0), launched one iteration at a time by a host loop that reads the
+// done flag: the stream driver, which times every kernel with events.
 #pragma once
 #include <cuda_runtime.h>
 #include "linalg.cuh"
@@ -28,9 +36,11 @@ struct GmresDev {
     double* y;        // [m]
     double* h1;       // [m+1] first CGS pass
     double* h2;       // [m+1] second CGS pass
-    double* hsq;      // [2] squared norms after each pass
+    double* hsq;      // [2] squared norms ([1]: after the second pass)
+    double* sc;       // [m+1] scale of each stored basis vector
     double* partial;  // [(KRY_MAXM+1) * RED_BLOCKS]
     unsigned* counter;
+    int in_graph;     // 1: the kernels run inside the WHILE graph and set its condition
 };
 
 // beta = sqrt(|rhs|^2); empty solve when beta < 1e-12 (src/Solver.cpp:1514-1516)
@@ -40,13 +50,16 @@ static __global__ void k_gmres_init(GmresDev d, int m, double tol, cudaGraphCond
     d.beta[1] = tol;
     d.gi[0] = 0;
     d.gi[3] = m;
-    for (int i = 0; i <= m; ++i) d.g[i] = 0.0;
+    for (int i = 0; i <= m; ++i) {
+        d.g[i] = 0.0;
+        d.sc[i] = 1.0;
+    }
     for (int i = 0; i < m; ++i) { d.cs[i] = 0.0; d.sn[i] = 0.0; }
     d.g[0] = b;
     if (b < 1e-12) {
         d.gi[1] = -1;
         d.gi[2] = 1;
-        cudaGraphSetConditional(h, 0);
+        if (d.in_graph) cudaGraphSetConditional(h, 0);
     } else {
         d.gi[1] = 0;
         d.gi[2] = 0;
@@ -67,26 +80,49 @@ __device__ __forceinline__ A warp_sum_t(A v) {
     return v;
 }
 
-// block reduction of K per-thread values: warp sums in A, then FP64 across the warps;
-// the FP64 block sums are valid in thread 0
-template <class A, int K>
-__device__ __forceinline__ void block_sum_mixed(const A (&v)[K], double (&out)[K]) {
-    __shared__ double sm[K][RED_THREADS / 32];
-    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+constexpr int KRY_TILE = 16;  // basis vectors per pass over a thread's elements
+constexpr int KRY_WARPS = RED_THREADS / 32;  // most warps of a block (blocks of 64-256 threads)
+
+// per-warp sums of one tile of per-thread partial dots into wsum[vector][warp]
+template <class A>
+__device__ __forceinline__ void tile_to_smem(const A (&v)[KRY_TILE], int i0, int nt, double (*wsum)[KRY_WARPS]) {
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
 #pragma unroll
-    for (int k = 0; k < K; ++k) {
-        A s = warp_sum_t(v[k]);
-        if (lane == 0) sm[k][w] = (double)s;
-    }
-    __syncthreads();
-    if (w == 0) {
-#pragma unroll
-        for (int k = 0; k < K; ++k) {
-            double x = lane < (int)(blockDim.x >> 5) ? sm[k][lane] : 0.0;
-            out[k] = warp_sum(x);
+    for (int t = 0; t < KRY_TILE; ++t)
+        if (t < nt) {
+            A s = warp_sum_t(v[t]);
+            if (lane == 0) wsum[i0 + t][warp] = (double)s;
         }
+}
+
+// Block partials of h[0..j] from wsum, then in the last block to finish the sums over the
+// blocks in block order: h[i] = sc[i] * sum.  Returns true in the last block.
+__device__ __forceinline__ bool dots_finish(const GmresDev& d, int j, double (*wsum)[KRY_WARPS], double* h) {
+    __syncthreads();
+    const int nwarp = blockDim.x >> 5;
+    for (int i = threadIdx.x; i <= j; i += blockDim.x) {
+        double sb = 0.0;
+        for (int w = 0; w < nwarp; ++w) sb += wsum[i][w];
+        d.partial[(long)i * RED_BLOCKS + blockIdx.x] = sb;
+    }
+    __threadfence();
+    __syncthreads();
+    __shared__ bool last;
+    if (threadIdx.x == 0) last = atomicAdd(d.counter, 1u) == gridDim.x - 1;
+    __syncthreads();
+    if (!last) return false;
+    __threadfence();
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    for (int i = warp; i <= j; i += nwarp) {
+        double sg = 0.0;
+#pragma unroll 4
+        for (int b = lane; b < (int)gridDim.x; b += 32) sg += __ldcg(d.partial + (long)i * RED_BLOCKS + b);
+        sg = warp_sum(sg);
+        if (lane == 0) h[i] = d.sc[i] * sg;
     }
     __syncthreads();
+    if (threadIdx.x == 0) *d.counter = 0u;
+    return true;
 }
 
 // V0 = rhs * (1/beta)
@@ -108,34 +144,53 @@ __global__ void k_gmres_dinv(long nc, const double* __restrict__ D, T* __restric
         Dinv[q] = (T)(1.0 / D[q]);
 }
 
+template <class T, int NV>
+__device__ __forceinline__ T dinv_of(const T* __restrict__ Dinv, long nc, long i, int c, T d0) {
+    return (NV == 6 && c >= 4) ? Dinv[(c - 3) * nc + i] : d0;
+}
+
 // z = V_j * (1/D) per cell (src/Solver.cpp:1536-1538)
 template <class T, int NV>
 __global__ void k_gmres_z(long nc, const T* V, long L, const T* __restrict__ Dinv, T* z, GmresDev d) {
-    const T* Vj = V + (long)d.gi[0] * L;
+    const int j = d.gi[0];
+    const T* Vj = V + (long)j * L;
+    const T sj = (T)d.sc[j];
     for (long i = (long)blockIdx.x * blockDim.x + threadIdx.x; i < nc; i += (long)gridDim.x * blockDim.x) {
         T a = Dinv[i];
 #pragma unroll
-        for (int c = 0; c < NV; ++c) {
-            T id = (NV == 6 && c >= 4) ? Dinv[(c - 3) * nc + i] : a;
-            z[c * nc + i] = Vj[c * nc + i] * id;
-        }
+        for (int c = 0; c < NV; ++c) z[c * nc + i] = Vj[c * nc + i] * sj * dinv_of<T, NV>(Dinv, nc, i, c, a);
     }
 }
 
-// h[i] = <w, V_i>, i = 0..j.  Sixteen basis vectors per pass over w (each thread keeps
-// sixteen partial products, independent loads in flight); warp sums per vector into
-// shared memory with no block barrier between passes; one barrier, then the block's
-// partials in FP64; the last block to finish sums them over the blocks in block order,
-// one warp per basis vector.
-constexpr int KRY_TILE = 16;
+// z = V_j * (1/D) fused with the primitive stage of the dual J v: W.v, W.d of (U, z)
+template <class T, int NV>
+__global__ void __launch_bounds__(256) k_gmres_prim_z(int nc, Flow<T> F, const T* __restrict__ U, const T* V, long L,
+                                                      const T* __restrict__ Dinv, T* __restrict__ z, Field<T> W,
+                                                      GmresDev d) {
+    long i = (long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= nc) return;
+    const int j = d.gi[0];
+    const T* Vj = V + (long)j * L;
+    const T sj = (T)d.sc[j];
+    const T a = Dinv[i];
+    Dual<T> u[6];
+#pragma unroll
+    for (int c = 0; c < NV; ++c) {
+        T zc = Vj[c * nc + i] * sj * dinv_of<T, NV>(Dinv, nc, i, c, a);
+        z[c * nc + i] = zc;
+        u[c] = Dual<T>(U[c * nc + i], zc);
+    }
+    if (NV == 4) u[4] = u[5] = Dual<T>(T(0), T(0));
+    prim_cell<Dual<T>, NV>(F, u[0], u[1], u[2], u[3], u[4], u[5], W, i);
+}
 
+// h[i] = sc[i] <w, V_i>, i = 0..j (the first pass of the FD J v path)
 template <class T>
 __global__ void __launch_bounds__(RED_THREADS) k_gmres_multidot(long L, const T* __restrict__ w,
                                                                 const T* __restrict__ V, GmresDev d, double* h) {
     typedef typename KryAcc<T>::type A;
     const int j = d.gi[0];
-    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarp = blockDim.x >> 5;
-    __shared__ double wsum[KRY_MAXM + 1][RED_THREADS / 32];
+    __shared__ double wsum[KRY_MAXM + 1][KRY_WARPS];
     for (int i0 = 0; i0 <= j; i0 += KRY_TILE) {
         const int nt = (j + 1 - i0) < KRY_TILE ? (j + 1 - i0) : KRY_TILE;
         A v[KRY_TILE];
@@ -147,94 +202,110 @@ __global__ void __launch_bounds__(RED_THREADS) k_gmres_multidot(long L, const T*
             for (int t = 0; t < KRY_TILE; ++t)
                 if (t < nt) v[t] += wq * (A)V[(long)(i0 + t) * L + q];
         }
-#pragma unroll
-        for (int t = 0; t < KRY_TILE; ++t)
-            if (t < nt) {
-                A sv = warp_sum_t(v[t]);
-                if (lane == 0) wsum[i0 + t][warp] = (double)sv;
-            }
+        tile_to_smem(v, i0, nt, wsum);
     }
-    __syncthreads();
-    for (int i = threadIdx.x; i <= j; i += blockDim.x) {
-        double sb = 0.0;
-        for (int ww = 0; ww < nwarp; ++ww) sb += wsum[i][ww];
-        d.partial[(long)i * RED_BLOCKS + blockIdx.x] = sb;
-    }
-    __threadfence();
-    __syncthreads();
-    __shared__ bool last;
-    if (threadIdx.x == 0) last = atomicAdd(d.counter, 1u) == gridDim.x - 1;
-    __syncthreads();
-    if (!last) return;
-    __threadfence();
-    for (int i = warp; i <= j; i += nwarp) {
-        double sg = 0.0;
-#pragma unroll 4
-        for (int b = lane; b < (int)gridDim.x; b += 32) sg += __ldcg(d.partial + (long)i * RED_BLOCKS + b);
-        sg = warp_sum(sg);
-        if (lane == 0) h[i] = sg;
-    }
-    __syncthreads();
-    if (threadIdx.x == 0) *d.counter = 0u;
+    dots_finish(d, j, wsum, h);
 }
 
-// w -= sum_{i<=j} h[i] V_i, then |w|^2 into *hsq
+// The gather of the dual J v (as k_gather: the faces' F*A derivatives in reference face
+// order, minus the SST source derivatives, plus z vol / dt) into w, fused with the first
+// CGS pass h1 = V^T w.  Grid-stride over cells (at most RED_BLOCKS blocks).
+template <class T, int NV>
+__global__ void __launch_bounds__(RED_THREADS) k_gmres_gather_dot(MeshView<T> m, const T* __restrict__ FA,
+                                                                  long fa_stride, T* __restrict__ w,
+                                                                  const T* __restrict__ z, const T* __restrict__ dt,
+                                                                  const T* __restrict__ src, const T* __restrict__ V,
+                                                                  long L, GmresDev d) {
+    typedef typename KryAcc<T>::type A;
+    const int j = d.gi[0];
+    const long nc = m.nc;
+    __shared__ double wsum[KRY_MAXM + 1][KRY_WARPS];
+    for (int i0 = 0; i0 <= j; i0 += KRY_TILE) {
+        const int nt = (j + 1 - i0) < KRY_TILE ? (j + 1 - i0) : KRY_TILE;
+        A v[KRY_TILE];
+#pragma unroll
+        for (int t = 0; t < KRY_TILE; ++t) v[t] = A(0);
+        for (long i = (long)blockIdx.x * blockDim.x + threadIdx.x; i < nc; i += (long)gridDim.x * blockDim.x) {
+            T acc[NV];
+            if (i0 == 0) {
+#pragma unroll
+                for (int c = 0; c < NV; ++c) acc[c] = T(0);
+#pragma unroll
+                for (int k = 0; k < 4; ++k) {
+                    int e = m.cf[(long)k * nc + i];
+                    if (e < 0) break;
+                    long f = e >> 1;
+                    if (e & 1) {
+#pragma unroll
+                        for (int c = 0; c < NV; ++c) acc[c] = acc[c] - FA[c * fa_stride + f];
+                    } else {
+#pragma unroll
+                        for (int c = 0; c < NV; ++c) acc[c] = acc[c] + FA[c * fa_stride + f];
+                    }
+                }
+                if constexpr (NV == 6) {
+                    acc[4] = acc[4] - src[i];
+                    acc[5] = acc[5] - src[nc + i];
+                }
+                T tc = m.vol[i] / (dt[i] + T(1e-30));
+#pragma unroll
+                for (int c = 0; c < NV; ++c) {
+                    acc[c] = acc[c] + z[c * nc + i] * tc;
+                    w[c * nc + i] = acc[c];
+                }
+            } else {
+#pragma unroll
+                for (int c = 0; c < NV; ++c) acc[c] = w[c * nc + i];
+            }
+#pragma unroll
+            for (int t = 0; t < KRY_TILE; ++t)
+                if (t < nt) {
+                    const T* Vi = V + (long)(i0 + t) * L;
+                    A s = A(0);
+#pragma unroll
+                    for (int c = 0; c < NV; ++c) s += (A)acc[c] * (A)Vi[c * nc + i];
+                    v[t] += s;
+                }
+        }
+        tile_to_smem(v, i0, nt, wsum);
+    }
+    dots_finish(d, j, wsum, d.h1);
+}
+
+// w -= sum_{i<=j} h1[i] sc[i] V_i, fused with the second CGS pass h2 = V^T w
 template <class T>
-__global__ void __launch_bounds__(RED_THREADS) k_gmres_update(long L, T* __restrict__ w, const T* __restrict__ V,
-                                                              GmresDev d, const double* h, double* hsq) {
+__global__ void __launch_bounds__(RED_THREADS) k_gmres_update_dot(long L, T* __restrict__ w, const T* __restrict__ V,
+                                                                  GmresDev d) {
     typedef typename KryAcc<T>::type A;
     const int j = d.gi[0];
     __shared__ A hs[KRY_MAXM + 1];
-    for (int i = threadIdx.x; i <= j; i += blockDim.x) hs[i] = (A)h[i];
+    __shared__ double wsum[KRY_MAXM + 1][KRY_WARPS];
+    for (int i = threadIdx.x; i <= j; i += blockDim.x) hs[i] = (A)(d.h1[i] * d.sc[i]);
     __syncthreads();
-    A v[1] = {A(0)};
     for (long q = (long)blockIdx.x * blockDim.x + threadIdx.x; q < L; q += (long)gridDim.x * blockDim.x) {
         A a = (A)w[q];
         for (int i = 0; i <= j; ++i) a -= hs[i] * (A)V[(long)i * L + q];
-        T t = (T)a;
-        w[q] = t;
-        v[0] += (A)t * (A)t;
+        w[q] = (T)a;
     }
-    double bs[1];
-    block_sum_mixed<A, 1>(v, bs);
-    __shared__ bool last;
-    if (threadIdx.x == 0) {
-        d.partial[blockIdx.x] = bs[0];
-        __threadfence();
-        last = atomicAdd(d.counter, 1u) == gridDim.x - 1;
+    for (int i0 = 0; i0 <= j; i0 += KRY_TILE) {
+        const int nt = (j + 1 - i0) < KRY_TILE ? (j + 1 - i0) : KRY_TILE;
+        A v[KRY_TILE];
+#pragma unroll
+        for (int t = 0; t < KRY_TILE; ++t) v[t] = A(0);
+        for (long q = (long)blockIdx.x * blockDim.x + threadIdx.x; q < L; q += (long)gridDim.x * blockDim.x) {
+            A wq = (A)w[q];
+#pragma unroll
+            for (int t = 0; t < KRY_TILE; ++t)
+                if (t < nt) v[t] += wq * (A)V[(long)(i0 + t) * L + q];
+        }
+        tile_to_smem(v, i0, nt, wsum);
     }
-    __syncthreads();
-    if (!last) return;
-    __threadfence();
-    double s[1] = {0.0};
-    for (int b = threadIdx.x; b < (int)gridDim.x; b += blockDim.x) s[0] += __ldcg(d.partial + b);
-    block_sum_mixed<double, 1>(s, bs);
-    if (threadIdx.x == 0) {
-        *hsq = bs[0];
-        *d.counter = 0u;
-    }
-}
-
-// V_{j+1} = w / |w| when |w| > 1e-12 (the breakdown guard of src/Solver.cpp:1553-1558)
-template <class T>
-__global__ void k_gmres_store(long L, const T* w, T* V, GmresDev d) {
-    const int j = d.gi[0];
-    __shared__ T sc;
-    if (threadIdx.x == 0) {
-        double hv = sqrt(d.hsq[1]);
-        sc = (T)(hv > 1e-12 ? 1.0 / hv : 1.0);
-    }
-    __syncthreads();
-    T* Vn = V + (long)(j + 1) * L;
-    const T s = sc;
-    for (long q = (long)blockIdx.x * blockDim.x + threadIdx.x; q < L; q += (long)gridDim.x * blockDim.x)
-        Vn[q] = w[q] * s;
+    dots_finish(d, j, wsum, d.h2);
 }
 
 // Hessenberg column, Givens rotations and the convergence test (src/Solver.cpp:1550-1588);
 // advances j or ends the loop.  One thread.
-static __global__ void k_gmres_givens(GmresDev d, cudaGraphConditionalHandle hnd) {
-    if (threadIdx.x != 0 || blockIdx.x != 0) return;
+__device__ __forceinline__ void givens_step(const GmresDev& d, cudaGraphConditionalHandle hnd) {
     const int j = d.gi[0], m = d.gi[3];
     double* col = d.H + (long)j * (m + 1);
     for (int i = 0; i <= j; ++i) col[i] = d.h1[i] + d.h2[i];
@@ -261,9 +332,61 @@ static __global__ void k_gmres_givens(GmresDev d, cudaGraphConditionalHandle hnd
     if (conv || j + 1 >= m) {
         d.gi[1] = j;
         d.gi[2] = 1;
-        cudaGraphSetConditional(hnd, 0);
+        if (d.in_graph) cudaGraphSetConditional(hnd, 0);
     } else {
         d.gi[0] = j + 1;
+    }
+}
+
+// V_{j+1} = w - sum_{i<=j} h2[i] sc[i] V_i, stored unnormalised, and |V_{j+1}|^2; the
+// last block sets sc[j+1] = 1/|V_{j+1}| (1 under the breakdown guard |.| <= 1e-12 of
+// src/Solver.cpp:1553-1558) and runs the Givens step.
+template <class T>
+__global__ void __launch_bounds__(RED_THREADS) k_gmres_update_final(long L, const T* __restrict__ w,
+                                                                    T* __restrict__ V, GmresDev d,
+                                                                    cudaGraphConditionalHandle hnd) {
+    typedef typename KryAcc<T>::type A;
+    const int j = d.gi[0];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    __shared__ A hs[KRY_MAXM + 1];
+    __shared__ double wsum[KRY_WARPS];
+    for (int i = threadIdx.x; i <= j; i += blockDim.x) hs[i] = (A)(d.h2[i] * d.sc[i]);
+    __syncthreads();
+    T* Vn = V + (long)(j + 1) * L;
+    A nrm = A(0);
+    for (long q = (long)blockIdx.x * blockDim.x + threadIdx.x; q < L; q += (long)gridDim.x * blockDim.x) {
+        A a = (A)w[q];
+        for (int i = 0; i <= j; ++i) a -= hs[i] * (A)V[(long)i * L + q];
+        T t = (T)a;
+        Vn[q] = t;
+        nrm += (A)t * (A)t;
+    }
+    nrm = warp_sum_t(nrm);
+    if (lane == 0) wsum[warp] = (double)nrm;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double sb = 0.0;
+        for (int w_ = 0; w_ < (int)(blockDim.x >> 5); ++w_) sb += wsum[w_];
+        d.partial[blockIdx.x] = sb;
+    }
+    __threadfence();
+    __syncthreads();
+    __shared__ bool last;
+    if (threadIdx.x == 0) last = atomicAdd(d.counter, 1u) == gridDim.x - 1;
+    __syncthreads();
+    if (!last) return;
+    __threadfence();
+    if (warp == 0) {
+        double sg = 0.0;
+        for (int b = lane; b < (int)gridDim.x; b += 32) sg += __ldcg(d.partial + b);
+        sg = warp_sum(sg);
+        if (lane == 0) {
+            d.hsq[1] = sg;
+            double hv = sqrt(sg);
+            d.sc[j + 1] = hv > 1e-12 ? 1.0 / hv : 1.0;
+            *d.counter = 0u;
+            givens_step(d, hnd);
+        }
     }
 }
 
@@ -278,7 +401,7 @@ static __global__ void k_gmres_backsub(GmresDev d) {
     }
 }
 
-// x = (sum_{i<=k} V_i y_i) / D (src/Solver.cpp:1610-1615, accumulated before the
+// x = (sum_{i<=k} V_i sc_i y_i) / D (src/Solver.cpp:1610-1615, accumulated before the
 // scaling); zero when the solve was empty
 template <class T, int NV>
 __global__ void k_gmres_solution_dev(long nc, const T* __restrict__ V, long L, GmresDev d,
@@ -291,7 +414,7 @@ __global__ void k_gmres_solution_dev(long nc, const T* __restrict__ V, long L, G
         for (int c = 0; c < NV; ++c) {
             long q = c * nc + i;
             double acc = 0.0;
-            for (int j = 0; j <= k; ++j) acc += (double)V[j * L + q] * d.y[j];
+            for (int j = 0; j <= k; ++j) acc += (double)V[j * L + q] * (d.y[j] * d.sc[j]);
             x[q] = acc * id[c];
         }
     }

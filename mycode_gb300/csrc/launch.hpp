@@ -31,6 +31,8 @@ struct ResArgs {
 template <class R> void launch_residual(const ResArgs<R>& a);
 // J v by forward linearisation with the limiter frozen (kern_jv.cu)
 template <class R> void launch_jv(const ResArgs<R>& a);
+// the middle of it (gradients, SST terms, face fluxes) for the fused Arnoldi body
+template <class R> void launch_jv_mid(const ResArgs<R>& a);
 
 // ---- vectors (T = double in kern_f64.cu, T = float in kern_f32.cu)
 template <class T> void launch_dot(int nv, long nc, const T* a, const T* b, RedScratch rs, double* out, cudaStream_t s);
@@ -71,6 +73,17 @@ inline unsigned red_grid(long n) {
     return (unsigned)(b < RED_BLOCKS ? (b < 1 ? 1 : b) : RED_BLOCKS);
 }
 
+// Per-cell and per-face kernels: blocks of 64-256 threads so that even small meshes
+// spread over every SM (two blocks per SM at least where the mesh allows)
+inline unsigned tpb_for(long n) { return n >= 2L * 152 * 256 ? 256u : (n >= 2L * 152 * 128 ? 128u : 64u); }
+inline unsigned blocks_for(long n) { return grid_for(n, (int)tpb_for(n)); }
+
+// the fused gather + dot kernel: per-cell blocks, at most RED_BLOCKS of them
+inline unsigned dot_cells_grid(long nc) {
+    unsigned b = blocks_for(nc);
+    return b < (unsigned)RED_BLOCKS ? b : (unsigned)RED_BLOCKS;
+}
+
 // multi-dot grids: one block per SM at most (few partials for the last block to sum),
 // grid-stride beyond
 inline unsigned kry_grid(long n) {
@@ -106,16 +119,22 @@ void launch_objective(int nv, int kind, int n, const int* slots, const double* w
 #include "krylov.cuh"
 namespace cfdg {
 void launch_gmres_init(const GmresDev& d, int m, double tol, cudaGraphConditionalHandle h, cudaStream_t s);
-void launch_gmres_givens(const GmresDev& d, cudaGraphConditionalHandle h, cudaStream_t s);
 void launch_gmres_backsub(const GmresDev& d, cudaStream_t s);
 template <class T> void launch_gmres_v0(long n, T* V0, const double* rhs, const GmresDev& d, cudaStream_t s);
 template <class T> void launch_gmres_dinv(int nv, long nc, const double* D, T* Dinv, cudaStream_t s);
 template <class T> void launch_gmres_z(int nv, long nc, const T* V, long L, const T* Dinv, T* z, const GmresDev& d,
                                        cudaStream_t s);
 template <class T> void launch_gmres_multidot(long L, const T* w, const T* V, const GmresDev& d, double* h, cudaStream_t s);
-template <class T> void launch_gmres_update(long L, T* w, const T* V, const GmresDev& d, const double* h, double* hsq,
-                                            cudaStream_t s);
-template <class T> void launch_gmres_store(long L, const T* w, T* V, const GmresDev& d, cudaStream_t s);
+// the fused Arnoldi stages (krylov.cuh): z + dual primitives, gather + first CGS pass,
+// update + second pass, final update + norm + Givens
+template <class T> void launch_gmres_prim_z(int nv, long nc, const Flow<T>& F, const T* U, const T* V, long L,
+                                            const T* Dinv, T* z, Field<T> W, const GmresDev& d, cudaStream_t s);
+template <class T> void launch_gmres_gather_dot(int nv, const MeshView<T>& m, const T* FA, T* w, const T* z,
+                                                const T* dt, const T* src, const T* V, long L, const GmresDev& d,
+                                                cudaStream_t s);
+template <class T> void launch_gmres_update_dot(long L, T* w, const T* V, const GmresDev& d, cudaStream_t s);
+template <class T> void launch_gmres_update_final(long L, const T* w, T* V, const GmresDev& d,
+                                                  cudaGraphConditionalHandle h, cudaStream_t s);
 template <class T> void launch_gmres_solution_dev(int nv, long nc, const T* V, long L, const GmresDev& d,
                                                   const double* D, double* x, cudaStream_t s);
 }  // namespace cfdg

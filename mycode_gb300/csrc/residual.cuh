@@ -100,10 +100,7 @@ __device__ __forceinline__ CS<S> load_cs(const Field<R>& U, const Field<R>& W, l
 // ---------------------------------------------------------------- k_prim
 // u, v, p, T as the reference computes them per face (src/Solver.cpp:93-102).
 template <class S, int NV, class R>
-__global__ void __launch_bounds__(256) k_prim(int nc, Flow<R> F, Field<R> U, Field<R> W) {
-    long i = (long)blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= nc) return;
-    S r = Acc<S>::ld(U, 0, i), ru = Acc<S>::ld(U, 1, i), rv = Acc<S>::ld(U, 2, i), rE = Acc<S>::ld(U, 3, i);
+__device__ __forceinline__ void prim_cell(const Flow<R>& F, S r, S ru, S rv, S rE, S rk, S rw, Field<R> W, long i) {
     S u = ru / r, v = rv / r;
     S p = pressure(F, r, ru, rv, rE);
     S T = p / (r * F.Rgas);
@@ -113,9 +110,22 @@ __global__ void __launch_bounds__(256) k_prim(int nc, Flow<R> F, Field<R> U, Fie
     Acc<S>::st(W, W_P, i, p);
     Acc<S>::st(W, W_T, i, T);
     if (NV == 6) {
-        Acc<S>::st(W, W_K, i, Acc<S>::ld(U, 4, i) / r);
-        Acc<S>::st(W, W_W, i, Acc<S>::ld(U, 5, i) / r);
+        Acc<S>::st(W, W_K, i, rk / r);
+        Acc<S>::st(W, W_W, i, rw / r);
     }
+}
+
+template <class S, int NV, class R>
+__global__ void __launch_bounds__(256) k_prim(int nc, Flow<R> F, Field<R> U, Field<R> W) {
+    long i = (long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= nc) return;
+    S r = Acc<S>::ld(U, 0, i), ru = Acc<S>::ld(U, 1, i), rv = Acc<S>::ld(U, 2, i), rE = Acc<S>::ld(U, 3, i);
+    S rk = S(R(0)), rw = S(R(0));
+    if (NV == 6) {
+        rk = Acc<S>::ld(U, 4, i);
+        rw = Acc<S>::ld(U, 5, i);
+    }
+    prim_cell<S, NV>(F, r, ru, rv, rE, rk, rw, W, i);
 }
 
 // ---------------------------------------------------------------- k_grad
@@ -135,10 +145,15 @@ __global__ void __launch_bounds__(256) k_grad(MeshView<R> m, Flow<R> F, Field<R>
 #pragma unroll
     for (int q = 0; q < 2 * NQ; ++q) acc[q] = S(R(0));
     R pmax = val(wi[W_P]), pmin = val(wi[W_P]);
-#pragma unroll 1
+    // face entries first, so the four faces' loads can be in flight together; the -1 pads
+    // are trailing, so skipping them is stopping at them
+    int ek[4];
+#pragma unroll
+    for (int k = 0; k < 4; ++k) ek[k] = m.cf[(long)k * m.nc + i];
+#pragma unroll
     for (int k = 0; k < 4; ++k) {
-        int e = m.cf[(long)k * m.nc + i];
-        if (e < 0) break;
+        int e = ek[k];
+        if (e < 0) continue;
         int f = e >> 1, side = e & 1;
         R nx = m.nx[f], ny = m.ny[f], A = m.area[f];
         S wj[NQ];
@@ -190,10 +205,10 @@ __global__ void __launch_bounds__(256) k_grad(MeshView<R> m, Flow<R> F, Field<R>
     R Tc = val(wi[W_T]);
     R gTx = val(acc[G_T]), gTy = val(acc[G_T + 1]);
     R lim = R(1.0);
-#pragma unroll 1
+#pragma unroll
     for (int k = 0; k < 4; ++k) {
-        int e = m.cf[(long)k * m.nc + i];
-        if (e < 0) break;
+        int e = ek[k];
+        if (e < 0) continue;
         int f = e >> 1, side = e & 1;
         R dx = side ? m.dxn[f] : m.dxo[f];
         R dy = side ? m.dyn[f] : m.dyo[f];
@@ -320,10 +335,13 @@ __global__ void __launch_bounds__(256) k_gather(MeshView<R> m, const R* __restri
     R acc[NV];
 #pragma unroll
     for (int c = 0; c < NV; ++c) acc[c] = R(0);
+    int ek[4];
+#pragma unroll
+    for (int k = 0; k < 4; ++k) ek[k] = m.cf[(long)k * m.nc + i];
 #pragma unroll
     for (int k = 0; k < 4; ++k) {
-        int e = m.cf[(long)k * m.nc + i];
-        if (e < 0) break;
+        int e = ek[k];
+        if (e < 0) continue;
         long f = e >> 1;
         if (e & 1) {
 #pragma unroll

@@ -146,46 +146,51 @@ struct cfdg_solver {
     int timing = 0;
     std::vector<cudaEvent_t> pool;
     size_t pool_used = 0;
-    std::vector<std::pair<int, size_t>> pending;
+    std::vector<std::pair<int, std::pair<size_t, int>>> pending;
     // classes 8-11: the VJP's forward recomputation, face adjoint, cell gathers 1 and 2
-    double kstat_ms[12] = {0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0};
-    long long kstat_n[12] = {0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0};
+    // classes 12-17: the fused Krylov body (stream driver): z + primitives, gradients
+    // (+ SST terms), face fluxes, gather + first CGS pass, update + second pass, final update
+    static constexpr int NSTAT = 18;
+    double kstat_ms[NSTAT] = {};
+    long long kstat_n[NSTAT] = {};
     // adjoint work buffers (allocated on the first VJP)
     AdjBufs ab{};
     double* adj_mem = nullptr;
     int* adj_imem = nullptr;
     double* phi_adj = nullptr;
     float kms[4] = {0, 0, 0, 0};
-    cudaEvent_t step_ev[2] = {nullptr, nullptr};
+    cudaEvent_t step_ev[4] = {nullptr, nullptr, nullptr, nullptr};  // step start/end, Krylov start/end
     long long launches = 0;
     unsigned char* l2buf = nullptr;
     size_t l2bytes = 0;
     int l2fill = 0;
 
-    cudaEvent_t* take_events(int base) {
+    // nint + 1 events bracketing nint consecutive kernels of stat classes base..base+nint-1
+    cudaEvent_t* take_events(int base, int nint = 4) {
         if (!timing || capturing) return nullptr;  // event nodes are not allowed in graph bodies
-        while (pool_used + 5 > pool.size()) {
+        while (pool_used + nint + 1 > pool.size()) {
             cudaEvent_t e;
             if (cudaEventCreate(&e) != cudaSuccess) return nullptr;
             pool.push_back(e);
         }
-        pending.push_back({base, pool_used});
+        pending.push_back({base, {pool_used, nint}});
         cudaEvent_t* e = &pool[pool_used];
-        pool_used += 5;
+        pool_used += nint + 1;
         return e;
     }
 
     // call only after the stream has been synchronised
     void collect() {
         for (auto& p : pending) {
-            float ms[4];
-            for (int k = 0; k < 4; ++k) {
-                cudaEventElapsedTime(&ms[k], pool[p.second + k], pool[p.second + k + 1]);
-                kstat_ms[p.first + k] += ms[k];
+            const size_t i0 = p.second.first;
+            const int nint = p.second.second;
+            for (int k = 0; k < nint; ++k) {
+                float ms = 0;
+                cudaEventElapsedTime(&ms, pool[i0 + k], pool[i0 + k + 1]);
+                kstat_ms[p.first + k] += ms;
                 ++kstat_n[p.first + k];
+                if (p.first == 0 && k < 4) kms[k] = ms;
             }
-            if (p.first == 0)
-                for (int k = 0; k < 4; ++k) kms[k] = ms[k];
         }
         pending.clear();
         pool_used = 0;
@@ -525,8 +530,13 @@ struct cfdg_solver {
     // one Arnoldi iteration (graph WHILE body)
     cfdg_status enqueue_gmres_body(double* Ubase, double* Rbase, cudaGraphConditionalHandle h) {
         const bool mixed = cfg.precision == CFDG_MIXED;
+        // the exact (dual-number) J v runs fused with the Arnoldi kernels: z with the
+        // primitives, the gather with the first CGS pass; the FD J v keeps its own kernels.
+        // ev (stream driver with timing): 7 events around the 6 stages, stat classes 12-17
+        cudaEvent_t* ev = (mixed || cfg.jv == CFDG_JV_EXACT) ? take_events(12, 6) : nullptr;
+        if (ev) CK(cudaEventRecord(ev[0], st));
         if (mixed) {
-            launch_gmres_z<float>(nv, nc, V32, L, dinv32, z32, gd, st);
+            launch_gmres_prim_z<float>(nv, nc, Ff, U32, V32, L, dinv32, z32, f32(W32, W32d), gd, st);
             ResArgs<float> a;
             a.m = mvf;
             a.F = Ff;
@@ -538,32 +548,49 @@ struct cfdg_solver {
             a.T = f32(T32, T32d);
             a.dwall = dwall32;
             a.phi = phi32;
-            a.out = w32;
-            a.do_limiter = 0;
-            a.diag_v = z32;
-            a.dt = dt32;
             a.stream = st;
-            a.ev = nullptr;
-            launch_jv<float>(a);
-            launch_gmres_multidot<float>(L, w32, V32, gd, gd.h1, st);
-            launch_gmres_update<float>(L, w32, V32, gd, gd.h1, gd.hsq, st);
-            launch_gmres_multidot<float>(L, w32, V32, gd, gd.h2, st);
-            launch_gmres_update<float>(L, w32, V32, gd, gd.h2, gd.hsq + 1, st);
-            launch_gmres_store<float>(L, w32, V32, gd, st);
-            launches += nv == 6 ? 11 : 10;
+            a.ev = ev ? ev + 1 : nullptr;
+            launch_jv_mid<float>(a);
+            launch_gmres_gather_dot<float>(nv, mvf, FA32d, w32, z32, dt32, nv == 6 ? T32d + 2 * nc : nullptr, V32, L, gd,
+                                           st);
+            if (ev) CK(cudaEventRecord(ev[4], st));
+            launch_gmres_update_dot<float>(L, w32, V32, gd, st);
+            if (ev) CK(cudaEventRecord(ev[5], st));
+            launch_gmres_update_final<float>(L, w32, V32, gd, h, st);
+            if (ev) CK(cudaEventRecord(ev[6], st));
+            launches += nv == 6 ? 7 : 6;
+        } else if (cfg.jv == CFDG_JV_EXACT) {
+            launch_gmres_prim_z<double>(nv, nc, F, Ubase, V, L, dinv64, z, f64(Wj, Wjd), gd, st);
+            ResArgs<double> a;
+            a.m = mv;
+            a.F = F;
+            a.nv = nv;
+            a.U = f64(Ubase, z);
+            a.W = f64(Wj, Wjd);
+            a.G = f64(Gj, Gjd);
+            a.FA = ff64(nullptr, FAjd);
+            a.T = f64(Tj, Tjd);
+            a.dwall = dwall;
+            a.phi = phi;
+            a.stream = st;
+            a.ev = ev ? ev + 1 : nullptr;
+            launch_jv_mid<double>(a);
+            launch_gmres_gather_dot<double>(nv, mv, FAjd, w64, z, dt, nv == 6 ? Tjd + 2 * nc : nullptr, V, L, gd, st);
+            if (ev) CK(cudaEventRecord(ev[4], st));
+            launch_gmres_update_dot<double>(L, w64, V, gd, st);
+            if (ev) CK(cudaEventRecord(ev[5], st));
+            launch_gmres_update_final<double>(L, w64, V, gd, h, st);
+            if (ev) CK(cudaEventRecord(ev[6], st));
+            launches += nv == 6 ? 7 : 6;
         } else {
             launch_gmres_z<double>(nv, nc, V, L, dinv64, z, gd, st);
             ++launches;
             TRY(jv64(Ubase, Rbase, z, w64, cfg.jv, true));
             launch_gmres_multidot<double>(L, w64, V, gd, gd.h1, st);
-            launch_gmres_update<double>(L, w64, V, gd, gd.h1, gd.hsq, st);
-            launch_gmres_multidot<double>(L, w64, V, gd, gd.h2, st);
-            launch_gmres_update<double>(L, w64, V, gd, gd.h2, gd.hsq + 1, st);
-            launch_gmres_store<double>(L, w64, V, gd, st);
-            launches += 5;
+            launch_gmres_update_dot<double>(L, w64, V, gd, st);
+            launch_gmres_update_final<double>(L, w64, V, gd, h, st);
+            launches += 3;
         }
-        launch_gmres_givens(gd, h, st);
-        ++launches;
         CK(cudaGetLastError());
         return CFDG_OK;
     }
@@ -576,6 +603,9 @@ struct cfdg_solver {
     }
 
     cfdg_status build_gmres_graph(double* Ubase, double* Rbase, double* rhsd, double* xout) {
+        // the captured kernels take GmresDev by value: they must be the graph's variant,
+        // whose Givens step ends the WHILE loop
+        gd.in_graph = 1;
         if (gexec) {
             cudaGraphExecDestroy(gexec);
             gexec = nullptr;
@@ -653,6 +683,36 @@ struct cfdg_solver {
         return fail(CFDG_ERR_CUDA, std::string("building the GMRES graph: ") + cudaGetErrorString(e));
     }
 
+    // the graph's kernels launched one iteration at a time (no graph; the kernels see
+    // in_graph = 0 and only raise the done flag), one host read of the flag per iteration
+    cfdg_status gmres_stream(double* Ubase, double* Rbase, double* rhsd, double* xout, int* iters) {
+        TRY(ensure_krylov());
+        gd.in_graph = 0;
+        cudaGraphConditionalHandle none = 0;
+        enqueue_gmres_pre(Ubase, rhsd, none);
+        int done = 0;
+        CK(cudaMemcpyAsync(&done, gd.gi + 2, sizeof(int), cudaMemcpyDeviceToHost, st));
+        CK(cudaStreamSynchronize(st));
+        for (int it = 0; !done && it < cfg.gmres_m; ++it) {
+            cfdg_status e = enqueue_gmres_body(Ubase, Rbase, none);
+            if (e != CFDG_OK) {
+                gd.in_graph = 1;
+                return e;
+            }
+            CK(cudaMemcpyAsync(&done, gd.gi + 2, sizeof(int), cudaMemcpyDeviceToHost, st));
+            CK(cudaStreamSynchronize(st));
+        }
+        enqueue_gmres_post(xout);
+        int k = -1;
+        CK(cudaMemcpyAsync(&k, gd.gi + 1, sizeof(int), cudaMemcpyDeviceToHost, st));
+        CK(cudaStreamSynchronize(st));
+        collect();
+        gd.in_graph = 1;
+        *iters = k + 1;
+        CK(cudaGetLastError());
+        return CFDG_OK;
+    }
+
     cfdg_status gmres_graph(double* Ubase, double* Rbase, double* rhsd, double* xout, int* iters) {
         TRY(ensure_krylov());
         if (!gexec || graph_version != flow_version || gkey[0] != Ubase || gkey[1] != Rbase || gkey[2] != rhsd ||
@@ -672,6 +732,7 @@ struct cfdg_solver {
     // current state; rhs and xout are FP64 device vectors.
     cfdg_status gmres(double* Ubase, double* Rbase, double* rhsd, double* xout, int* iters) {
         if (cfg.krylov == CFDG_KRYLOV_GRAPH) return gmres_graph(Ubase, Rbase, rhsd, xout, iters);
+        if (cfg.krylov == CFDG_KRYLOV_STREAM) return gmres_stream(Ubase, Rbase, rhsd, xout, iters);
         const int m = cfg.gmres_m;
         const bool mixed = cfg.precision == CFDG_MIXED;
         const int mode = mixed ? CFDG_JV_EXACT : cfg.jv;
@@ -811,6 +872,10 @@ struct cfdg_solver {
             float ms = 0;
             CK(cudaEventElapsedTime(&ms, step_ev[0], step_ev[1]));
             rec.device_ms = ms;
+            if (rec.gmres_iters > 0) {
+                CK(cudaEventElapsedTime(&ms, step_ev[2], step_ev[3]));
+                rec.krylov_ms = ms;
+            }
         }
         return CFDG_OK;
     }
@@ -842,6 +907,7 @@ struct cfdg_solver {
         rec.limiter_updated = upd ? 1 : 0;
         rec.seconds = 0;
         rec.device_ms = 0;
+        rec.krylov_ms = 0;
         if (!std::isfinite(resVM)) {
             if (info) *info = rec;
             return fail(CFDG_ERR_NAN, "non-finite residual at Newton step " + std::to_string(step));
@@ -858,7 +924,9 @@ struct cfdg_solver {
         launch_scale_from<double>(L, rhs, R, scal + 6, 0, st);
         ++launches;
         int it = 0;
+        if (timing) CK(cudaEventRecord(step_ev[2], st));
         TRY(gmres(U, R, rhs, x, &it));
+        if (timing) CK(cudaEventRecord(step_ev[3], st));
         rec.gmres_iters = it;
         if (it >= 29) {
             cfl *= 0.5;
@@ -1157,7 +1225,7 @@ cfdg_status cfdg_solver_create(const cfdg_mesh* m, const cfdg_config* cfg, cfdg_
     if (cfg) c = *cfg;
     else cfdg_config_default(&c);
     if (c.gmres_m < 1 || c.gmres_m > 400) return fail(CFDG_ERR_ARG, "gmres_m must be in [1, 400]");
-    if (c.krylov < CFDG_KRYLOV_AUTO || c.krylov > CFDG_KRYLOV_GRAPH) return fail(CFDG_ERR_ARG, "unknown krylov driver");
+    if (c.krylov < CFDG_KRYLOV_AUTO || c.krylov > CFDG_KRYLOV_STREAM) return fail(CFDG_ERR_ARG, "unknown krylov driver");
     if (c.krylov != CFDG_KRYLOV_HOST && c.gmres_m > KRY_MAXM)
         return fail(CFDG_ERR_ARG, "the graph Krylov driver supports gmres_m <= 128");
     if (c.flux < 0 || c.flux > 3 || c.spatial < 0 || c.spatial > 2 || c.bcset < 0 || c.bcset > 2)
@@ -1246,7 +1314,7 @@ cfdg_status cfdg_solver_create(const cfdg_mesh* m, const cfdg_config* cfg, cfdg_
         int m = c.gmres_m;
         TRYS(dalloc(&s->gdi, 4));
         size_t nd = 3 + (size_t)(m + 1) + 2 * (size_t)m + (size_t)(m + 1) * m + m + 2 * (size_t)(m + 1) + 2 +
-                    (size_t)(KRY_MAXM + 1) * RED_BLOCKS + 4;
+                    (size_t)(m + 1) + (size_t)(KRY_MAXM + 1) * RED_BLOCKS + 4;
         TRYS(dalloc(&s->gdd, nd));
         double* q = s->gdd;
         GmresDev& d = s->gd;
@@ -1260,8 +1328,10 @@ cfdg_status cfdg_solver_create(const cfdg_mesh* m, const cfdg_config* cfg, cfdg_
         d.h1 = q; q += m + 1;
         d.h2 = q; q += m + 1;
         d.hsq = q; q += 2;
+        d.sc = q; q += m + 1;
         d.partial = q; q += (size_t)(KRY_MAXM + 1) * RED_BLOCKS;
         d.counter = reinterpret_cast<unsigned*>(q);
+        d.in_graph = 1;
         if (c.precision == CFDG_MIXED) TRYS(dalloc(&s->w32, (size_t)L));
         else TRYS(dalloc(&s->w64, (size_t)L));
     }
@@ -1522,8 +1592,9 @@ cfdg_status cfdg_norm_vm(cfdg_solver* s, const double* R, double* out) {
 }
 
 cfdg_status cfdg_set_krylov(cfdg_solver* s, int mode) {
-    if (!s || (mode != CFDG_KRYLOV_HOST && mode != CFDG_KRYLOV_GRAPH)) return fail(CFDG_ERR_ARG, "bad krylov mode");
-    if (mode == CFDG_KRYLOV_GRAPH && !s->gdi) return fail(CFDG_ERR_ARG, "the graph driver needs gmres_m <= 128");
+    if (!s || (mode != CFDG_KRYLOV_HOST && mode != CFDG_KRYLOV_GRAPH && mode != CFDG_KRYLOV_STREAM))
+        return fail(CFDG_ERR_ARG, "bad krylov mode");
+    if (mode != CFDG_KRYLOV_HOST && !s->gdi) return fail(CFDG_ERR_ARG, "the device drivers need gmres_m <= 128");
     s->cfg.krylov = mode;
     return CFDG_OK;
 }
@@ -1671,7 +1742,7 @@ cfdg_status cfdg_kernel_times(cfdg_solver* s, double* a, double* b, double* c, d
 
 cfdg_status cfdg_kernel_stats(cfdg_solver* s, double* ms8, long long* n8, int reset) {
     if (!s) return fail(CFDG_ERR_ARG, "null solver");
-    for (int k = 0; k < 12; ++k) {
+    for (int k = 0; k < cfdg_solver::NSTAT; ++k) {
         if (ms8) ms8[k] = s->kstat_ms[k];
         if (n8) n8[k] = s->kstat_n[k];
         if (reset) {

@@ -80,3 +80,30 @@ def test_graph_newton_solve_matches_host_driver(cuda_lib):
         out[kry] = tr
     a, b = out[0]["res_vm"], out[1]["res_vm"]
     np.testing.assert_allclose(b, a, rtol=1e-3)
+
+
+@pytest.mark.parametrize("name", ["supersonic", "plate_visc"])
+@pytest.mark.parametrize("precision,jv", [("mixed", "exact"), ("fp64", "exact"), ("fp64", "fd")])
+def test_stream_driver_is_the_graph_bit_for_bit(cuda_lib, name, precision, jv):
+    """The stream driver launches the graph's kernels one iteration at a time: the same
+    arithmetic in the same order, so the same solution bit for bit, and with timing on
+    every stage of the fused body is timed."""
+    out = {}
+    for kry in (1, 2):
+        s, spec, case = _solver(cuda_lib, name, precision=precision, jv=jv, krylov=kry, gmres_m=12)
+        o = OracleSolver(spec, bcset=case["bcset"], viscous=case["viscous"], init=case["init"])
+        C.setup(o, case)
+        U = C.perturbed_state(o.get_state(), o.cells(), seed=14)
+        s.setNumericalMethod("ROE", "SECOND_ORDER_CENTRAL")
+        R = s.computeResiduals(U)
+        s.set_state(U)
+        s.local_timestep(20.0)
+        s.set_timing(True)
+        s.kernel_stats(reset=True)
+        out[kry] = s.gmres(U, R, -R)
+        st = s.kernel_stats(reset=True)
+        if kry == 2 and (precision == "mixed" or jv == "exact"):
+            n = [st[k][1] for k in s.KERNEL_CLASSES if k.startswith("krylov.")]
+            assert min(n) == max(n) == out[kry][0]
+    assert out[1][0] == out[2][0]
+    np.testing.assert_array_equal(out[1][1], out[2][1])
