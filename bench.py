@@ -407,6 +407,10 @@ def ours(args):
     adjoint = {"ratio": t_vjp / t_res, "residual_ms": t_res, "vjp_ms": t_vjp,
                "note": "FP64 VJP of the full residual (forward recomputation included) / FP64 residual"}
 
+    # ---- time to a density residual of 1e-10: mixed vs the FP64 paths on the supersonic
+    # wedge (the reference's own CPU case, which converges under the reference's CFL control)
+    t2c = time_to_converge(api) if (rank == 0 and not args.no_t2c) else None
+
     # ---- CPU baseline: the oracle port on this host, bounded sample
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
@@ -428,10 +432,51 @@ def ours(args):
             "e2e": e2e,
             "fp64": fp64,
             "adjoint_over_primal": adjoint,
+            "time_to_1e-10": t2c,
             "clocks": clocks,
             "cpu_baseline": cpu,
         }
         print(json.dumps(line))
+
+
+def time_to_converge(api, max_steps=1500):
+    """Wall time of full solves from the free stream to a volume-weighted density residual
+    of 1e-10: the wedge 120 x 80 x 2 triangles (19,200 cells, 10 % jitter), M 2.5, HLLC with
+    the Barth-Jespersen limiter, GMRES(30), CFL from 10, for the mixed path (FP32 Krylov and
+    exact J v, FP64 residual and update), the FP64 path with exact J v and the FP64 path
+    with the reference's FD J v.  Also the relative L2 difference of the converged states."""
+    from mycode_gb300 import meshgen
+    import numpy as np
+    mesh = api.Mesh.from_spec(meshgen.wedge(120, 80, jitter=0.10, seed=0))
+    out, states = {}, {}
+    for name, prec, jv in (("mixed", "mixed", "exact"), ("fp64_exact", "fp64", "exact"), ("fp64_fd", "fp64", "fd")):
+        s = api.Solver(mesh, bcset="supersonic", init="freestream", viscous=0, precision=prec, jv=jv, gmres_m=30,
+                       cfl0=10.0, flux="HLLC", spatial="SECOND_ORDER_LIMITED")
+        s.setFlowConditions(2.5, 101325.0, 300.0)
+        s.initialize()
+        s.synchronize()
+        t0 = time.perf_counter()
+        n, reached, its = 0, False, 0
+        while n < max_steps:
+            rec, _ = s.newton_step(0.0)
+            n += 1
+            its += rec.gmres_iters
+            if rec.res_rho <= 1e-10 and n > 5:
+                reached = True
+                break
+        s.synchronize()
+        t = time.perf_counter() - t0
+        out[name] = {"seconds": round(t, 4), "newton_steps": n, "gmres_iters": its, "reached": reached,
+                     "final_res_rho": rec.res_rho}
+        states[name] = s.getSolution()
+        s.close()
+    ref = states["fp64_fd"]
+    for name in ("mixed", "fp64_exact"):
+        out[name]["state_rel_l2_vs_fp64_fd"] = float(np.linalg.norm(states[name] - ref) / np.linalg.norm(ref))
+    out["speedup_mixed_vs_fp64_fd"] = out["fp64_fd"]["seconds"] / out["mixed"]["seconds"]
+    out["speedup_mixed_vs_fp64_exact"] = out["fp64_exact"]["seconds"] / out["mixed"]["seconds"]
+    out["workload"] = "supersonic wedge 120x80x2 (19,200 cells), M 2.5, HLLC + BJ limiter, GMRES(30), CFL0 10"
+    return out
 
 
 # ---------------------------------------------------------------- CPU side
@@ -630,6 +675,7 @@ def main():
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--cpu-seconds", type=float, default=15.0)
+    ap.add_argument("--no-t2c", action="store_true", help="skip the time-to-1e-10 solves")
     ap.add_argument("--sweep", action="store_true", help="bandwidth sweep on the bump channel instead")
     ap.add_argument("--sweep-sizes", default="", help="comma-separated target cell counts")
     ap.add_argument("--sweep-reps", type=int, default=10)

@@ -25,36 +25,39 @@ CFD_HD CSb<R> csb_zero() {
 }
 
 // getPressure (include/Flux.hpp:12-15)
+// (The reverse code multiplies by reciprocals instead of dividing where a value is
+// divided more than once: GB300's FP64 divide costs about ten FP64 operations, and the
+// adjoint, unlike the residual, has no bit-for-bit reference to follow.)
+//
+// p = (g-1)(rE - (ru^2 + rv^2) / (2 r)): dp/drE = g-1, dp/dru = -(g-1) u, dp/drv = -(g-1) v,
+// dp/dr = (g-1)(u^2 + v^2)/2 with u = ru/r, v = rv/r
+template <class R>
+CFD_HD void pressure_b_uv(const Flow<R>& F, R u, R v, R pb, R& rb, R& rub, R& rvb, R& rEb) {
+    R t = (F.gam - R(1.0)) * pb;
+    rEb += t;
+    rub -= t * u;
+    rvb -= t * v;
+    rb += R(0.5) * t * (u * u + v * v);
+}
+
 template <class R>
 CFD_HD void pressure_b(const Flow<R>& F, R r, R ru, R rv, R rE, R pb, R& rb, R& rub, R& rvb, R& rEb) {
-    R gm = F.gam - R(1.0);
-    R num = ru * ru + rv * rv, den = r * r;
-    R V2 = num / den;
-    R t = gm * pb;
-    rEb += t;
-    rb += -R(0.5) * V2 * t;
-    R V2b = -R(0.5) * r * t;
-    R numb = V2b / den;
-    R denb = -V2b * V2 / den;
-    rub += R(2) * ru * numb;
-    rvb += R(2) * rv * numb;
-    rb += R(2) * r * denb;
+    R ir = R(1) / r;
+    pressure_b_uv(F, ru * ir, rv * ir, pb, rb, rub, rvb, rEb);
 }
 
 // make_cs: conservative adjoints of a state from the adjoints of all its fields
 template <class R>
 CFD_HD void cs_back(const Flow<R>& F, const CS<R>& c, const CSb<R>& b, R* ub) {
-    ub[0] += b.r;
-    ub[1] += b.ru;
-    ub[2] += b.rv;
+    R ir = R(1) / c.r;
+    R bu = b.u * ir, bv = b.v * ir;
+    ub[0] += b.r - bu * c.u - bv * c.v;
+    ub[1] += b.ru + bu;
+    ub[2] += b.rv + bv;
     ub[3] += b.rE;
     ub[4] += b.rk;
     ub[5] += b.rw;
-    ub[1] += b.u / c.r;
-    ub[0] -= b.u * c.u / c.r;
-    ub[2] += b.v / c.r;
-    ub[0] -= b.v * c.v / c.r;
-    pressure_b(F, c.r, c.ru, c.rv, c.rE, b.p, ub[0], ub[1], ub[2], ub[3]);
+    pressure_b_uv(F, c.u, c.v, b.p, ub[0], ub[1], ub[2], ub[3]);
 }
 
 // Same folding into a CSb (conservative entries only) of the state c itself
@@ -70,7 +73,10 @@ CFD_HD void cs_fold(const Flow<R>& F, const CS<R>& c, CSb<R>& b) {
 // (r, u, v, p) from the adjoint of the resulting state (k = w = 0 inputs)
 template <class R>
 CFD_HD void p2c_b(const Flow<R>& F, R r, R u, R v, R p, const CSb<R>& ob, R& rb, R& ub, R& vb, R& pb) {
-    CS<R> o = p2c(F, r, u, v, p, R(0), R(0));
+    CS<R> o;  // the fields cs_back reads of p2c(r, u, v, p)
+    o.r = r;
+    o.u = u;
+    o.v = v;
     R cb[6] = {R(0), R(0), R(0), R(0), R(0), R(0)};
     cs_back(F, o, ob, cb);
     // rE = p/(g-1) + 0.5 r (u^2 + v^2); ru = r u; rv = r v
@@ -99,11 +105,12 @@ template <class R>
 CFD_HD R sgn(R x) { return x < R(0) ? R(-1) : R(1); }
 
 // c = sqrt(g p / r)
+// (dc/dp = g / (2 c r), dc/dr = -c / (2 r) since c^2 = g p / r)
 template <class R>
 CFD_HD void sound_b(const Flow<R>& F, const CS<R>& U, R c, R cb, CSb<R>& Ub) {
-    R qb = cb / (c + c);
-    Ub.p += qb * F.gam / U.r;
-    Ub.r -= qb * F.gam * U.p / (U.r * U.r);
+    R t = cb / ((c + c) * U.r);
+    Ub.p += t * F.gam;
+    Ub.r -= t * c * c;
 }
 
 // computeFluxLLF (include/Flux.hpp:81-108)
@@ -145,7 +152,8 @@ CFD_HD void flux_roe_b(const Flow<R>& F, const CS<R>& L, const CS<R>& Rt, R nx, 
                        CSb<R>& Rb) {
     const R gm = F.gam - R(1.0);
     // forward
-    R hL = (L.rE + L.p) / L.r, hR = (Rt.rE + Rt.p) / Rt.r;
+    const R irL = R(1) / L.r, irR = R(1) / Rt.r;
+    R hL = (L.rE + L.p) * irL, hR = (Rt.rE + Rt.p) * irR;
     R sL = sqrt(L.r), sR = sqrt(Rt.r);
     R S = sL + sR;
     R inv = R(1.0) / S;
@@ -159,24 +167,26 @@ CFD_HD void flux_roe_b(const Flow<R>& F, const CS<R>& L, const CS<R>& Rt, R nx, 
     R utt = -ut * ny + vt * nx;
     R raw[4] = {unt - ct, unt, unt, unt + ct};
     R eps = R(0.1) * ct;
+    const R ieps = R(1) / eps;
     R fix[4], lam[4];
     bool fixed[4];
     for (int i = 0; i < 4; ++i) {
         fixed[i] = fabs(raw[i]) < eps;
-        fix[i] = fixed[i] ? R(0.5) * (raw[i] * raw[i] / eps + eps) : raw[i];
+        fix[i] = fixed[i] ? R(0.5) * (raw[i] * raw[i] * ieps + eps) : raw[i];
         lam[i] = fabs(fix[i]);
     }
     R dr = Rt.r - L.r, du = Rt.u - L.u, dv = Rt.v - L.v, dp = Rt.p - L.p;
     R dun = du * nx + dv * ny;
     R dut = -du * ny + dv * nx;
     R rt = sL * sR;
-    R k0 = R(0.5) / c2;
+    const R ic2 = R(1) / c2;
+    R k0 = R(0.5) * ic2;
     R in0 = dp - rt * ct * dun, in3 = dp + rt * ct * dun;
-    R al0 = k0 * in0, al1 = dr - dp / c2, al2 = rt * dut, al3 = k0 * in3;
+    R al0 = k0 * in0, al1 = dr - dp * ic2, al2 = rt * dut, al3 = k0 * in3;
     R w1 = lam[0] * al0, w2 = lam[1] * al1, w3 = lam[2] * al2, w4 = lam[3] * al3;
     R aunt = fabs(unt);
-    R kd = Rt.rk / Rt.r - L.rk / L.r;
-    R wd = Rt.rw / Rt.r - L.rw / L.r;
+    R kd = Rt.rk * irR - L.rk * irL;
+    R wd = Rt.rw * irR - L.rw * irL;
     // reverse: F = 0.5 (FL + FR) - 0.5 D
     R FLb[6], Db[6];
     for (int c = 0; c < 6; ++c) {
@@ -191,14 +201,12 @@ CFD_HD void flux_roe_b(const Flow<R>& F, const CS<R>& L, const CS<R>& Rt, R nx, 
     auntb += Db[4] * kd * rt + Db[5] * wd * rt;
     R kdb = Db[4] * aunt * rt, wdb = Db[5] * aunt * rt;
     rtb += Db[4] * aunt * kd + Db[5] * aunt * wd;
-    Rb.rk += kdb / Rt.r;
-    Rb.r -= kdb * Rt.rk / (Rt.r * Rt.r);
-    Lb.rk -= kdb / L.r;
-    Lb.r += kdb * L.rk / (L.r * L.r);
-    Rb.rw += wdb / Rt.r;
-    Rb.r -= wdb * Rt.rw / (Rt.r * Rt.r);
-    Lb.rw -= wdb / L.r;
-    Lb.r += wdb * L.rw / (L.r * L.r);
+    Rb.rk += kdb * irR;
+    Rb.r -= (kdb * Rt.rk + wdb * Rt.rw) * irR * irR;
+    Lb.rk -= kdb * irL;
+    Lb.r += (kdb * L.rk + wdb * L.rw) * irL * irL;
+    Rb.rw += wdb * irR;
+    Lb.rw -= wdb * irL;
     untb += auntb * sgn(unt);
     // D3 = w1 (ht - unt ct) + w2 (0.5 V2) + w3 utt + w4 (ht + unt ct)
     w1b += Db[3] * (ht - unt * ct);
@@ -247,11 +255,11 @@ CFD_HD void flux_roe_b(const Flow<R>& F, const CS<R>& L, const CS<R>& Rt, R nx, 
     rtb += (-in0b + in3b) * ct * dun;
     ctb += (-in0b + in3b) * rt * dun;
     R dunb = (-in0b + in3b) * rt * ct;
-    R c2b = -k0b * R(0.5) / (c2 * c2);
+    R c2b = -k0b * R(0.5) * ic2 * ic2;
     // al1 = dr - dp / c2
     R drb = al1b;
-    dpb -= al1b / c2;
-    c2b += al1b * dp / (c2 * c2);
+    dpb -= al1b * ic2;
+    c2b += al1b * dp * ic2 * ic2;
     // al2 = rt dut
     rtb += al2b * dut;
     R dutb = al2b * rt;
@@ -268,8 +276,8 @@ CFD_HD void flux_roe_b(const Flow<R>& F, const CS<R>& L, const CS<R>& Rt, R nx, 
         R fixb = lamb[i] * sgn(fix[i]);
         R rawb;
         if (fixed[i]) {
-            rawb = fixb * raw[i] / eps;
-            epsb += fixb * R(0.5) * (R(1) - raw[i] * raw[i] / (eps * eps));
+            rawb = fixb * raw[i] * ieps;
+            epsb += fixb * R(0.5) * (R(1) - raw[i] * raw[i] * ieps * ieps);
         } else {
             rawb = fixb;
         }
@@ -303,8 +311,9 @@ CFD_HD void flux_roe_b(const Flow<R>& F, const CS<R>& L, const CS<R>& Rt, R nx, 
     Lb.r += sLb / (sL + sL);
     Rb.r += sRb / (sR + sR);
     // h = (rE + p) / r
-    Lb.rE += hLb / L.r; Lb.p += hLb / L.r; Lb.r -= hLb * hL / L.r;
-    Rb.rE += hRb / Rt.r; Rb.p += hRb / Rt.r; Rb.r -= hRb * hR / Rt.r;
+    R hLr = hLb * irL, hRr = hRb * irR;
+    Lb.rE += hLr; Lb.p += hLr; Lb.r -= hLr * hL;
+    Rb.rE += hRr; Rb.p += hRr; Rb.r -= hRr * hR;
 }
 
 // computeFluxHLLC (include/Flux.hpp:36-76)
@@ -623,14 +632,15 @@ CFD_HD void face_flux_b(const Flow<R>& F, const CS<R>& L, const CS<R>& Rn, bool 
         R a0, b0, c0, e0, dTdx, dTdy;
         R d2 = g.dxlr * g.dxlr + g.dylr * g.dylr;
         bool corr = !wall && d2 > R(1e-14);
+        const R id2w = wall ? R(1) / d2w : R(0), id2 = corr ? R(1) / d2 : R(0);
         R du = Rt.u - L.u, dv = Rt.v - L.v;
         R dudx, dudy, dvdx, dvdy;
         if (wall) {
             a0 = b0 = c0 = e0 = R(0);
-            dudx = -L.u * dx / d2w;
-            dudy = -L.u * dy / d2w;
-            dvdx = -L.v * dx / d2w;
-            dvdy = -L.v * dy / d2w;
+            dudx = -L.u * dx * id2w;
+            dudy = -L.u * dy * id2w;
+            dvdx = -L.v * dx * id2w;
+            dvdy = -L.v * dy * id2w;
             dTdx = dTdy = R(0);
         } else {
             a0 = R(0.5) * (gL[FG_U] + gRv[FG_U]);
@@ -641,10 +651,11 @@ CFD_HD void face_flux_b(const Flow<R>& F, const CS<R>& L, const CS<R>& Rn, bool 
             dTdy = R(0.5) * (gL[FG_T + 1] + gRv[FG_T + 1]);
             dudx = a0; dudy = b0; dvdx = c0; dvdy = e0;
             if (corr) {
-                dudx = a0 - (a0 * g.dxlr + b0 * g.dylr - du) * g.dxlr / d2;
-                dudy = b0 - (a0 * g.dxlr + b0 * g.dylr - du) * g.dylr / d2;
-                dvdx = c0 - (c0 * g.dxlr + e0 * g.dylr - dv) * g.dxlr / d2;
-                dvdy = e0 - (c0 * g.dxlr + e0 * g.dylr - dv) * g.dylr / d2;
+                R cu = (a0 * g.dxlr + b0 * g.dylr - du) * id2, cv = (c0 * g.dxlr + e0 * g.dylr - dv) * id2;
+                dudx = a0 - cu * g.dxlr;
+                dudy = b0 - cu * g.dylr;
+                dvdx = c0 - cv * g.dxlr;
+                dvdy = e0 - cv * g.dylr;
             }
         }
         R Cp = F.gam * F.Rgas / (F.gam - R(1.0));
@@ -686,14 +697,14 @@ CFD_HD void face_flux_b(const Flow<R>& F, const CS<R>& L, const CS<R>& Rn, bool 
         Lb.v += R(0.5) * vfb;
         Rtb.v += R(0.5) * vfb;
         if (wall) {
-            Lb.u -= (dudxb * dx + dudyb * dy) / d2w;
-            Lb.v -= (dvdxb * dx + dvdyb * dy) / d2w;
+            Lb.u -= (dudxb * dx + dudyb * dy) * id2w;
+            Lb.v -= (dvdxb * dx + dvdyb * dy) * id2w;
         } else {
             R a0b = dudxb, b0b = dudyb, c0b = dvdxb, e0b = dvdyb;
             if (corr) {
                 // dudx = a0 - cu dxlr, dudy = b0 - cu dylr with cu = (a0 dxlr + b0 dylr - du) / d2
-                R cub = -(dudxb * g.dxlr + dudyb * g.dylr) / d2;
-                R cvb = -(dvdxb * g.dxlr + dvdyb * g.dylr) / d2;
+                R cub = -(dudxb * g.dxlr + dudyb * g.dylr) * id2;
+                R cvb = -(dvdxb * g.dxlr + dvdyb * g.dylr) * id2;
                 a0b += cub * g.dxlr;
                 b0b += cub * g.dylr;
                 R dub_ = -cub;

@@ -120,15 +120,16 @@ __global__ void __launch_bounds__(128) k_flux_adj(MeshView<double> m, Flow<doubl
 template <int NQ>
 __device__ __forceinline__ void w_to_csb(const Flow<double>& F, double r, double p, double rk, double rw,
                                          const double* wb, CSb<double>& cb) {
-    double T = p / (r * F.Rgas);
-    cb.r += wb[W_R] - wb[W_T] * T / r;
+    const double ir = 1.0 / r, irR = ir / F.Rgas;
+    double T = p * irR;
+    cb.r += wb[W_R] - wb[W_T] * T * ir;
     cb.u += wb[W_U];
     cb.v += wb[W_V];
-    cb.p += wb[W_P] + wb[W_T] / (r * F.Rgas);
+    cb.p += wb[W_P] + wb[W_T] * irR;
     if constexpr (NQ == 7) {
-        cb.rk += wb[W_K] / r;
-        cb.rw += wb[W_W] / r;
-        cb.r -= (wb[W_K] * (rk / r) + wb[W_W] * (rw / r)) / r;
+        cb.rk += wb[W_K] * ir;
+        cb.rw += wb[W_W] * ir;
+        cb.r -= (wb[W_K] * rk + wb[W_W] * rw) * ir * ir;
     }
 }
 
@@ -260,10 +261,10 @@ __global__ void __launch_bounds__(128) k_adj_cell1(MeshView<double> m, Flow<doub
         }
     }
     // Green-Gauss reverse, own half of every face (G = acc / vol)
-    double vol = m.vol[i];
+    const double ivol = 1.0 / m.vol[i];
     double accb[NG];
     for (int q = 0; q < NG; ++q) {
-        accb[q] = gb[q] / vol;
+        accb[q] = gb[q] * ivol;
         b.accb[q * nc + i] = accb[q];
     }
     for (int k = 0; k < 4; ++k) {

@@ -33,9 +33,12 @@ template <class R> CFD_HD Dual<R> operator+(Dual<R> a, Dual<R> b) { return Dual<
 template <class R> CFD_HD Dual<R> operator-(Dual<R> a, Dual<R> b) { return Dual<R>(a.v - b.v, a.d - b.d); }
 template <class R> CFD_HD Dual<R> operator-(Dual<R> a) { return Dual<R>(-a.v, -a.d); }
 template <class R> CFD_HD Dual<R> operator*(Dual<R> a, Dual<R> b) { return Dual<R>(a.v * b.v, a.d * b.v + a.v * b.d); }
+// Quotients go through one reciprocal (a divide costs about ten FP64 operations on
+// GB300); the value may then differ from a plain divide in the last bit.
 template <class R> CFD_HD Dual<R> operator/(Dual<R> a, Dual<R> b) {
-    R q = a.v / b.v;
-    return Dual<R>(q, (a.d - q * b.d) / b.v);
+    R ib = R(1) / b.v;
+    R q = a.v * ib;
+    return Dual<R>(q, (a.d - q * b.d) * ib);
 }
 // mixed scalar forms (the scalar is a constant: zero derivative)
 template <class R> CFD_HD Dual<R> operator+(Dual<R> a, R b) { return Dual<R>(a.v + b, a.d); }
@@ -44,10 +47,14 @@ template <class R> CFD_HD Dual<R> operator-(Dual<R> a, R b) { return Dual<R>(a.v
 template <class R> CFD_HD Dual<R> operator-(R a, Dual<R> b) { return Dual<R>(a - b.v, -b.d); }
 template <class R> CFD_HD Dual<R> operator*(Dual<R> a, R b) { return Dual<R>(a.v * b, a.d * b); }
 template <class R> CFD_HD Dual<R> operator*(R a, Dual<R> b) { return Dual<R>(a * b.v, a * b.d); }
-template <class R> CFD_HD Dual<R> operator/(Dual<R> a, R b) { return Dual<R>(a.v / b, a.d / b); }
+template <class R> CFD_HD Dual<R> operator/(Dual<R> a, R b) {
+    R ib = R(1) / b;
+    return Dual<R>(a.v * ib, a.d * ib);
+}
 template <class R> CFD_HD Dual<R> operator/(R a, Dual<R> b) {
-    R q = a / b.v;
-    return Dual<R>(q, -q * b.d / b.v);
+    R ib = R(1) / b.v;
+    R q = a * ib;
+    return Dual<R>(q, -q * b.d * ib);
 }
 template <class R> CFD_HD Dual<R>& operator+=(Dual<R>& a, Dual<R> b) { a = a + b; return a; }
 template <class R> CFD_HD Dual<R>& operator-=(Dual<R>& a, Dual<R> b) { a = a - b; return a; }

@@ -99,17 +99,17 @@ void launch_gmres_prim_z<float>(int nv, long nc, const Flow<float>& F, const flo
 template <>
 void launch_gmres_gather_dot<float>(int nv, const MeshView<float>& m, const float* FA, float* w, const float* z, const float* dt,
                                  const float* src, const float* V, long L, const GmresDev& d, cudaStream_t s) {
-    NV_SWITCH(nv, (k_gmres_gather_dot<float, NVC><<<dot_cells_grid(m.nc), tpb_for(m.nc), 0, s>>>(m, FA, m.nf, w, z, dt, src, V, L,
+    NV_SWITCH(nv, (k_gmres_gather_dot<float, NVC><<<kry_grid(m.nc), RED_THREADS, 0, s>>>(m, FA, m.nf, w, z, dt, src, V, L,
                                                                                      d)));
 }
 template <>
 void launch_gmres_update_dot<float>(long L, float* w, const float* V, const GmresDev& d, cudaStream_t s) {
-    k_gmres_update_dot<float><<<red_grid(L), RED_THREADS, 0, s>>>(L, w, V, d);
+    k_gmres_update_dot<float><<<kry_grid(L), RED_THREADS, 0, s>>>(L, w, V, d);
 }
 template <>
 void launch_gmres_update_final<float>(long L, const float* w, float* V, const GmresDev& d, cudaGraphConditionalHandle h,
                                    cudaStream_t s) {
-    k_gmres_update_final<float><<<red_grid(L), RED_THREADS, 0, s>>>(L, w, V, d, h);
+    k_gmres_update_final<float><<<kry_grid(L), RED_THREADS, 0, s>>>(L, w, V, d, h);
 }
 template <>
 void launch_gmres_solution_dev<float>(int nv, long nc, const float* V, long L, const GmresDev& d, const double* D,

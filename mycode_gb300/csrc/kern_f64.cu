@@ -124,17 +124,17 @@ void launch_gmres_prim_z<double>(int nv, long nc, const Flow<double>& F, const d
 template <>
 void launch_gmres_gather_dot<double>(int nv, const MeshView<double>& m, const double* FA, double* w, const double* z, const double* dt,
                                  const double* src, const double* V, long L, const GmresDev& d, cudaStream_t s) {
-    NV_SWITCH(nv, (k_gmres_gather_dot<double, NVC><<<dot_cells_grid(m.nc), tpb_for(m.nc), 0, s>>>(m, FA, m.nf, w, z, dt, src, V, L,
+    NV_SWITCH(nv, (k_gmres_gather_dot<double, NVC><<<kry_grid(m.nc), RED_THREADS, 0, s>>>(m, FA, m.nf, w, z, dt, src, V, L,
                                                                                      d)));
 }
 template <>
 void launch_gmres_update_dot<double>(long L, double* w, const double* V, const GmresDev& d, cudaStream_t s) {
-    k_gmres_update_dot<double><<<red_grid(L), RED_THREADS, 0, s>>>(L, w, V, d);
+    k_gmres_update_dot<double><<<kry_grid(L), RED_THREADS, 0, s>>>(L, w, V, d);
 }
 template <>
 void launch_gmres_update_final<double>(long L, const double* w, double* V, const GmresDev& d, cudaGraphConditionalHandle h,
                                    cudaStream_t s) {
-    k_gmres_update_final<double><<<red_grid(L), RED_THREADS, 0, s>>>(L, w, V, d, h);
+    k_gmres_update_final<double><<<kry_grid(L), RED_THREADS, 0, s>>>(L, w, V, d, h);
 }
 template <>
 void launch_gmres_solution_dev<double>(int nv, long nc, const double* V, long L, const GmresDev& d, const double* D,

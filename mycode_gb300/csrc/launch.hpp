@@ -78,14 +78,8 @@ inline unsigned red_grid(long n) {
 inline unsigned tpb_for(long n) { return n >= 2L * 152 * 256 ? 256u : (n >= 2L * 152 * 128 ? 128u : 64u); }
 inline unsigned blocks_for(long n) { return grid_for(n, (int)tpb_for(n)); }
 
-// the fused gather + dot kernel: per-cell blocks, at most RED_BLOCKS of them
-inline unsigned dot_cells_grid(long nc) {
-    unsigned b = blocks_for(nc);
-    return b < (unsigned)RED_BLOCKS ? b : (unsigned)RED_BLOCKS;
-}
-
-// multi-dot grids: one block per SM at most (few partials for the last block to sum),
-// grid-stride beyond
+// Kernels that end in multi-dot reductions: blocks of RED_THREADS, one per SM at most, so
+// the last block sums few partials with all its warps; grid-stride beyond
 inline unsigned kry_grid(long n) {
     long b = (n + RED_THREADS - 1) / RED_THREADS;
     return (unsigned)(b < 152 ? (b < 1 ? 1 : b) : 152);
