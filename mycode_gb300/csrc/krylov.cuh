@@ -304,38 +304,56 @@ __global__ void __launch_bounds__(RED_THREADS) k_gmres_update_dot(long L, T* __r
 }
 
 // Hessenberg column, Givens rotations and the convergence test (src/Solver.cpp:1550-1588);
-// advances j or ends the loop.  One thread.
-__device__ __forceinline__ void givens_step(const GmresDev& d, cudaGraphConditionalHandle hnd) {
+// advances j or ends the loop.  Called by one full warp: the lanes stage the column and
+// the previous rotations in shared memory, lane 0 runs the rotation chain there (the
+// chain is serial; shared memory keeps its loads short), the lanes write back.
+__device__ __forceinline__ void givens_step(const GmresDev& d, cudaGraphConditionalHandle hnd, double hsq) {
+    __shared__ double col_s[KRY_MAXM + 2], cs_s[KRY_MAXM], sn_s[KRY_MAXM];
+    const int lane = threadIdx.x & 31;
     const int j = d.gi[0], m = d.gi[3];
     double* col = d.H + (long)j * (m + 1);
-    for (int i = 0; i <= j; ++i) col[i] = d.h1[i] + d.h2[i];
-    col[j + 1] = sqrt(d.hsq[1]);
-    for (int i = 0; i < j; ++i) {
-        double t = d.cs[i] * col[i] + d.sn[i] * col[i + 1];
-        col[i + 1] = -d.sn[i] * col[i] + d.cs[i] * col[i + 1];
-        col[i] = t;
+    for (int i = lane; i <= j; i += 32) {
+        col_s[i] = d.h1[i] + d.h2[i];
+        if (i < j) {
+            cs_s[i] = d.cs[i];
+            sn_s[i] = d.sn[i];
+        }
     }
-    double a = col[j], b = col[j + 1];
-    if (fabs(b) < 1e-14) {
-        d.cs[j] = 1.0;
-        d.sn[j] = 0.0;
-    } else {
-        double t = sqrt(a * a + b * b);
-        d.cs[j] = a / t;
-        d.sn[j] = b / t;
+    __syncwarp();
+    if (lane == 0) {
+        col_s[j + 1] = sqrt(hsq);
+        for (int i = 0; i < j; ++i) {
+            double t = cs_s[i] * col_s[i] + sn_s[i] * col_s[i + 1];
+            col_s[i + 1] = -sn_s[i] * col_s[i] + cs_s[i] * col_s[i + 1];
+            col_s[i] = t;
+        }
+        double a = col_s[j], b = col_s[j + 1], c, sn;
+        if (fabs(b) < 1e-14) {
+            c = 1.0;
+            sn = 0.0;
+        } else {
+            double t = sqrt(a * a + b * b);
+            c = a / t;
+            sn = b / t;
+        }
+        d.cs[j] = c;
+        d.sn[j] = sn;
+        col_s[j] = c * a + sn * b;
+        col_s[j + 1] = 0.0;
+        double gj = d.g[j];
+        d.g[j + 1] = -sn * gj;
+        d.g[j] = c * gj;
+        bool conv = fabs(-sn * gj) < d.beta[1] * d.beta[0];
+        if (conv || j + 1 >= m) {
+            d.gi[1] = j;
+            d.gi[2] = 1;
+            if (d.in_graph) cudaGraphSetConditional(hnd, 0);
+        } else {
+            d.gi[0] = j + 1;
+        }
     }
-    col[j] = d.cs[j] * a + d.sn[j] * b;
-    col[j + 1] = 0.0;
-    d.g[j + 1] = -d.sn[j] * d.g[j];
-    d.g[j] = d.cs[j] * d.g[j];
-    bool conv = fabs(d.g[j + 1]) < d.beta[1] * d.beta[0];
-    if (conv || j + 1 >= m) {
-        d.gi[1] = j;
-        d.gi[2] = 1;
-        if (d.in_graph) cudaGraphSetConditional(hnd, 0);
-    } else {
-        d.gi[0] = j + 1;
-    }
+    __syncwarp();
+    for (int i = lane; i <= j + 1; i += 32) col[i] = col_s[i];
 }
 
 // V_{j+1} = w - sum_{i<=j} h2[i] sc[i] V_i, stored unnormalised, and |V_{j+1}|^2; the
@@ -378,15 +396,16 @@ __global__ void __launch_bounds__(RED_THREADS) k_gmres_update_final(long L, cons
     __threadfence();
     if (warp == 0) {
         double sg = 0.0;
+#pragma unroll 4
         for (int b = lane; b < (int)gridDim.x; b += 32) sg += __ldcg(d.partial + b);
-        sg = warp_sum(sg);
+        sg = __shfl_sync(0xffffffffu, warp_sum(sg), 0);
         if (lane == 0) {
             d.hsq[1] = sg;
             double hv = sqrt(sg);
             d.sc[j + 1] = hv > 1e-12 ? 1.0 / hv : 1.0;
             *d.counter = 0u;
-            givens_step(d, hnd);
         }
+        givens_step(d, hnd, sg);
     }
 }
 
