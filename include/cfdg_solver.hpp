@@ -13,11 +13,16 @@
 //   solver.computeResiduals(U, R, upd);        (same; any 6-double State type)
 //   solver.solveImplicit(tol, maxSteps);       (same; returns the per-step record)
 //   solver.getSolution();                      (same; vector<StateT>)
+//   solver.calculateDrag(), calculateEntropyError(), extractSkinFriction(file)   (same)
 //
 // Failures throw cfdg::Error (the reference has no error reporting).  Header-only; link
 // with libcfdgpu.so.
 #pragma once
 
+#include <algorithm>
+#include <cmath>
+#include <fstream>
+#include <iostream>
 #include <stdexcept>
 #include <string>
 #include <vector>
@@ -78,7 +83,7 @@ private:
 class GpuSolver {
 public:
     explicit GpuSolver(const GpuMesh& mesh) : GpuSolver(mesh, defaults()) {}
-    GpuSolver(const GpuMesh& mesh, const cfdg_config& cfg) : n_(mesh.getNumCells()) {
+    GpuSolver(const GpuMesh& mesh, const cfdg_config& cfg) : n_(mesh.getNumCells()), gamma_(cfg.gamma) {
         check(cfdg_solver_create(mesh.handle(), &cfg, &s_));
     }
     GpuSolver(const GpuSolver&) = delete;
@@ -125,10 +130,70 @@ public:
         return U;
     }
 
+    // Solver::calculateDrag (src/Solver.cpp:1307-1325): prints " Drag :<value>" like the
+    // reference and returns the value
+    double calculateDrag() {
+        double d = 0;
+        check(cfdg_drag(s_, &d));
+        std::cout << " Drag :" << d << std::endl;
+        return d;
+    }
+
+    // Solver::calculateEntropyError (src/Solver.cpp:1620-1646): prints as the reference
+    double calculateEntropyError() {
+        double e = 0;
+        check(cfdg_entropy_error(s_, &e));
+        std::cout << " GRS " << std::endl;
+        std::cout << " Cells: " << n_ << std::endl;
+        std::cout << " L2 Entropy Error: " << e << std::endl;
+        return e;
+    }
+
+    // Solver::extractSkinFriction (src/Solver.cpp:1899-1979): x, Cf and the Blasius Cf of
+    // the no-slip (tag 4) faces, sorted by x, into a CSV with the reference's columns
+    void extractSkinFriction(const std::string& filename) {
+        int n = 0;
+        check(cfdg_wall_coefficients(s_, 4, nullptr, nullptr, nullptr, &n));
+        std::vector<double> x((size_t)n), cp((size_t)n), cf((size_t)n);
+        if (n) check(cfdg_wall_coefficients(s_, 4, x.data(), cp.data(), cf.data(), &n));
+        double p[6];
+        check(cfdg_get_params(s_, p));  // M_inf, P0, T0, Pexit, nu, R_gas
+        const double g = gamma_;
+        double Ts = p[2] / (1.0 + 0.5 * (g - 1.0) * p[0] * p[0]);
+        double u_inf = p[0] * std::sqrt(g * p[5] * Ts);
+        std::vector<size_t> order((size_t)n);
+        for (size_t k = 0; k < order.size(); ++k) order[k] = k;
+        std::stable_sort(order.begin(), order.end(), [&](size_t a, size_t b) { return x[a] < x[b]; });
+        std::ofstream out(filename);
+        out << "x,Cf,Cf_theory\n";
+        for (size_t k : order) {
+            double re_x = u_inf * x[k] / p[4];
+            out << x[k] << "," << cf[k] << "," << (re_x > 0 ? 0.664 / std::sqrt(re_x) : 0.0) << "\n";
+        }
+        std::cout << "Skin friction coefficient distribution exported to " << filename << std::endl;
+    }
+
+    // computeWallDistances (src/Solver.cpp:1981-2015), per cell in the caller's numbering
+    std::vector<double> wallDistances() {
+        std::vector<double> d((size_t)n_);
+        check(cfdg_wall_distance(s_, d.data()));
+        return d;
+    }
+
+    // the adjoint: (dR/dU)^T lambda at the current state (no reference counterpart)
+    template <class StateT>
+    std::vector<StateT> vjp(const std::vector<StateT>& lambda) {
+        static_assert(sizeof(StateT) == 6 * sizeof(double), "State must be 6 doubles");
+        std::vector<StateT> g(lambda.size());
+        check(cfdg_vjp(s_, nullptr, reinterpret_cast<const double*>(lambda.data()), reinterpret_cast<double*>(g.data())));
+        return g;
+    }
+
     cfdg_solver* handle() { return s_; }
 
 private:
     int n_ = 0;
+    double gamma_ = 1.4;
     cfdg_solver* s_ = nullptr;
 };
 

@@ -1,7 +1,8 @@
 // The reference's default case (AmberMond/mycode src/main.cpp:53-100: bump channel,
 // M = 0.5, P = 101325 Pa, T = 300 K, LLF, first order, JFNK to 1e-5) written against
 // cfdg::GpuMesh / cfdg::GpuSolver instead of Mesh / Solver.  Prints the residual
-// history in the reference's results/residual_history.csv format.
+// history in the reference's results/residual_history.csv format, then the entropy
+// error and the drag as the reference prints them.
 //
 //   g++ -O2 -std=c++17 -I include bump_main.cpp -L mycode_gb300/_lib -lcfdgpu -o bump_main
 //   ./bump_main mesh_file [max_steps]
@@ -35,6 +36,12 @@ int main(int argc, char** argv) {
         solver.computeResiduals(U, R, false);
         std::fprintf(stderr, "cells %d steps %zu final %g\n", mesh.getNumCells(), trace.size(),
                      trace.empty() ? 0.0 : trace.back().res_vm);
+        std::fflush(stdout);
+        // the reference's post-processing (src/main.cpp:91-95)
+        std::cout << " Grs " << std::endl;
+        solver.calculateEntropyError();
+        std::cout << " Drag " << std::endl;
+        solver.calculateDrag();
     } catch (const cfdg::Error& e) {
         std::fprintf(stderr, "cfdg error %d: %s\n", (int)e.status, e.what());
         return 1;
