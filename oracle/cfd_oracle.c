@@ -341,6 +341,7 @@ typedef struct {
     double* pmin;
     int gmres_m;
     double gmres_tol;
+    double cfl0;
 } om_solver;
 
 enum { GR_RHO = 0, GR_U = 2, GR_V = 4, GR_P = 6, GR_T = 8 };
@@ -358,6 +359,7 @@ om_solver* om_solver_create(const om_mesh* m) {
     s->nu = 0.01;             /* include/Solver.hpp:42 */
     s->gmres_m = 40;          /* src/Solver.cpp:1479 */
     s->gmres_tol = 1e-2;      /* src/Solver.cpp:1587 */
+    s->cfl0 = 0.1;            /* src/Solver.cpp:1700 */
     int n = m->n_cells;
     s->grad = (double*)calloc((size_t)10 * n, sizeof(double));
     s->phi = (double*)malloc(sizeof(double) * n);
@@ -382,6 +384,8 @@ void om_set_case(om_solver* s, int bcset, int viscous, int init_mode) {
 }
 void om_set_gmres(om_solver* s, int m, double tol) { s->gmres_m = m; s->gmres_tol = tol; }
 void om_set_nu(om_solver* s, double nu) { s->nu = nu; }
+/* the first pseudo-time CFL of solveImplicit (the reference hard-codes 0.1) */
+void om_set_cfl0(om_solver* s, double cfl0) { s->cfl0 = cfl0; }
 
 /* setFlowConditions (src/Solver.cpp:12-32) */
 void om_set_flow_conditions(om_solver* s, double M, double P, double T) {
@@ -909,7 +913,7 @@ int om_solve_implicit(om_solver* s, double tol, int max_steps, double* res_vm, d
     int n = s->m->n_cells;
     size_t len = (size_t)NV * n;
     double g = s->gamma;
-    double CFL = 0.1;
+    double CFL = s->cfl0;
     double* R = (double*)malloc(sizeof(double) * len);
     double* rhs = (double*)malloc(sizeof(double) * len);
     double* dU = (double*)malloc(sizeof(double) * len);

@@ -67,6 +67,7 @@ def _oracle_lib():
             "om_set_case": (None, [vp, C.c_int, C.c_int, C.c_int]),
             "om_set_gmres": (None, [vp, C.c_int, C.c_double]),
             "om_set_nu": (None, [vp, C.c_double]),
+            "om_set_cfl0": (None, [vp, C.c_double]),
             "om_set_flow_conditions": (None, [vp, C.c_double, C.c_double, C.c_double]),
             "om_set_freestream_static": (None, [vp, C.c_double, C.c_double, C.c_double]),
             "om_set_kinematic_viscosity": (None, [vp, C.c_double, C.c_double]),
@@ -169,6 +170,9 @@ class OracleSolver(_Base):
 
     def setNu(self, nu):
         self._L.om_set_nu(self._s, float(nu))
+
+    def setCFL0(self, cfl0):
+        self._L.om_set_cfl0(self._s, float(cfl0))
 
     def setFlowConditions(self, M, P, T):
         self._L.om_set_flow_conditions(self._s, M, P, T)

@@ -243,3 +243,44 @@ def test_fp32_sst_jv_finite_at_the_omega_floor(cuda_lib):
     # finiteness is the point here: this state (free stream against a y+ < 1 wall with w
     # at its floor) is far outside where FP32 derivatives keep their relative accuracy
     assert np.isfinite(J32).all() and np.isfinite(J64).all()
+
+
+def test_swbli_submesh_wall_pressure_adjoint_gradcheck(cuda_lib):
+    """The SWBLI recipe on a 1,920-cell sub-mesh (40 x 32, outer half in triangles): M 2,
+    Re 1e7, SST, HLLC with the Barth-Jespersen limiter, 8-degree shock inflow.  The wall-
+    pressure integral over the interaction region drives the VJP (lambda = dJ/dU), which is
+    checked against central differences of lambda^T R along 16 seeded directions (limiter
+    switches detected by a second step size), and dJ/dU against differences of J."""
+    spec = mg.swbli(40, 32)
+    m = cuda_lib.Mesh.from_spec(spec)
+    assert m.n_cells == 1920
+    s = cuda_lib.Solver(m, bcset="plate", viscous=1, init="freestream", turbulence="sst", shock_deflection_deg=8.0)
+    s.setNumericalMethod("HLLC", "SECOND_ORDER_LIMITED")
+    s.setFreestreamStatic(2.0, 101325.0, 300.0)
+    s.setKinematicViscosity(1e7, 1.0)
+    s.initialize()
+    s.solveImplicit(tol=1e-30, max_steps=30)
+    U = s.getSolution()
+    assert np.isfinite(U).all()
+    J, lam = s.objective("wall_pressure", 0.3, 0.7)
+    assert J > 0 and np.abs(lam).max() > 0
+    gU = s.vjp(lam, U)
+    rng = np.random.default_rng(31)
+    scale = np.abs(U).mean(axis=0)
+    bad = 0
+    for d in range(16):
+        v = rng.standard_normal(U.shape) * scale
+        s.set_state(U + 1e-6 * v)
+        jp = s.objective("wall_pressure", 0.3, 0.7, gradient=False)
+        s.set_state(U - 1e-6 * v)
+        jm = s.objective("wall_pressure", 0.3, 0.7, gradient=False)
+        assert (jp - jm) / 2e-6 == pytest.approx(float(np.sum(lam * v)), rel=1e-6)
+        # limiter and model kinks are everywhere on this grid: steps of 1e-7 of the state
+        # cross some of them, 1e-9 rarely does
+        fd = {h: float(np.sum(lam * (s.computeResiduals(U + h * v) - s.computeResiduals(U - h * v)))) / (2 * h)
+              for h in (1e-8, 1e-9)}
+        a = float(np.sum(gU * v))
+        if abs(fd[1e-9] - a) > 1e-6 * abs(a):
+            assert abs(fd[1e-8] - fd[1e-9]) > 1e-7 * abs(a), (d, fd, a)
+            bad += 1
+    assert bad <= 3
