@@ -156,6 +156,16 @@ cfdg_status cfdg_get_params(const cfdg_solver* s, double* out6);
 cfdg_status cfdg_set_state(cfdg_solver* s, const double* U);
 cfdg_status cfdg_get_state(cfdg_solver* s, double* U);
 
+/* Solver::timeStepExplicit (src/Solver.cpp:1219-1243): one forward-Euler step of dt with
+ * the reference's positivity clamps; res_l2 (may be NULL) gets norm_L2 of the residual
+ * the step used (the reference prints it every 100 steps). */
+cfdg_status cfdg_time_step_explicit(cfdg_solver* s, double dt, double* res_l2);
+/* Solver::solveUnsteady (src/Solver.cpp:1801-1864): n_steps physical steps of dt_phy by
+ * dual time stepping (BDF1; per step at most 15 Newton steps to a volume-weighted residual
+ * of 1e-6, GMRES with the time term vol / dt_phy, updates relaxed by 0.7).  Per step
+ * (arrays may be NULL): the Newton steps taken and the last residual. */
+cfdg_status cfdg_solve_unsteady(cfdg_solver* s, double dt_phy, int n_steps, int* newton_steps, double* res_vm);
+
 /* The mixed-precision kernels on their own (solvers created with precision = mixed):
  * the FP32 residual of U (AoS, NULL = current state; the limiter recomputed in FP32 for
  * the limited scheme) and the FP32 exact J v (dual numbers; limiter frozen at the current

@@ -130,6 +130,21 @@ public:
         return U;
     }
 
+    // Solver::timeStepExplicit (src/Solver.cpp:1219-1243); returns norm_L2 of the residual
+    double timeStepExplicit(double dt) {
+        double r = 0;
+        check(cfdg_time_step_explicit(s_, dt, &r));
+        return r;
+    }
+
+    // Solver::solveUnsteady (src/Solver.cpp:1801-1864); per physical step the Newton steps
+    std::vector<int> solveUnsteady(double dt_phy, int maxTimeSteps) {
+        std::vector<int> it((size_t)(maxTimeSteps > 0 ? maxTimeSteps : 1));
+        check(cfdg_solve_unsteady(s_, dt_phy, maxTimeSteps, it.data(), nullptr));
+        it.resize((size_t)(maxTimeSteps > 0 ? maxTimeSteps : 0));
+        return it;
+    }
+
     // Solver::calculateDrag (src/Solver.cpp:1307-1325): prints " Drag :<value>" like the
     // reference and returns the value
     double calculateDrag() {

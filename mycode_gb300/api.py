@@ -107,6 +107,8 @@ SIGNATURES = {
     "cfdg_wall_coefficients": (C.c_int, [_vp, C.c_int, C.c_void_p, C.c_void_p, C.c_void_p, C.POINTER(C.c_int)]),
     "cfdg_wall_distance": (C.c_int, [_vp, C.c_void_p]),
     "cfdg_residual32": (C.c_int, [_vp, C.c_void_p, _dp]),
+    "cfdg_time_step_explicit": (C.c_int, [_vp, C.c_double, C.POINTER(C.c_double)]),
+    "cfdg_solve_unsteady": (C.c_int, [_vp, C.c_double, C.c_int, C.c_void_p, C.c_void_p]),
     "cfdg_jv32": (C.c_int, [_vp, _dp, _dp, _dp]),
     "cfdg_objective": (C.c_int, [_vp, C.c_int, C.c_double, C.c_double, C.POINTER(C.c_double), C.c_void_p]),
     "cfdg_drag": (C.c_int, [_vp, C.POINTER(C.c_double)]),
@@ -385,6 +387,21 @@ class Solver:
             "krylov_ms": np.array([r.krylov_ms for r in recs]),
             "converged": st == 0,
         }
+
+    def timeStepExplicit(self, dt):
+        """Solver::timeStepExplicit: returns norm_L2 of the residual the step used."""
+        r = C.c_double()
+        _check(lib().cfdg_time_step_explicit(self._h, float(dt), C.byref(r)))
+        return r.value
+
+    def solveUnsteady(self, dt_phy, max_time_steps):
+        """Solver::solveUnsteady: per physical step the Newton steps taken and the last
+        residual."""
+        n = int(max_time_steps)
+        it = np.zeros(max(n, 1), np.int32)
+        res = np.zeros(max(n, 1))
+        _check(lib().cfdg_solve_unsteady(self._h, float(dt_phy), n, it.ctypes.data_as(_vp), res.ctypes.data_as(_vp)))
+        return {"newton_steps": it[:n], "res_vm": res[:n]}
 
     def newton_step(self, tol=0.0):
         s = Step()

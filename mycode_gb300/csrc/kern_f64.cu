@@ -89,6 +89,18 @@ void launch_precond(int nv, const MeshView<double>& m, const Flow<double>& F, co
                     const double* dt, double* D, const double* mut, cudaStream_t s) {
     NV_SWITCH(nv, (k_precond<NVC><<<blocks_for(m.nc), tpb_for(m.nc), 0, s>>>(m, F, U, W, dt, D, mut)));
 }
+void launch_explicit_update(int nv, long nc, double* U, const double* R, const double* vol, double dt, int* bad,
+                            cudaStream_t s) {
+    NV_SWITCH(nv, (k_explicit_update<NVC><<<blocks_for(nc), tpb_for(nc), 0, s>>>(nc, U, R, vol, dt, bad)));
+}
+void launch_unsteady_rhs(int nv, long nc, const double* U, const double* Uold, const double* R, const double* vol,
+                         double dt, double* rhs, RedScratch rs, double* out2, cudaStream_t s) {
+    NV_SWITCH(nv, (k_unsteady_rhs<NVC><<<red_grid(nc), RED_THREADS, 0, s>>>(nc, U, Uold, R, vol, dt, rhs, rs, out2)));
+}
+void launch_relaxed_add(int nv, long nc, double* U, const double* dU, double relax, int* bad, cudaStream_t s) {
+    NV_SWITCH(nv, (k_relaxed_add<NVC><<<blocks_for(nc), tpb_for(nc), 0, s>>>(nc, U, dU, relax, bad)));
+}
+void launch_fill(long n, double* x, double v, cudaStream_t s) { k_fill<<<red_grid(n), RED_THREADS, 0, s>>>(n, x, v); }
 void launch_newton_update(int nv, long nc, double* U, const double* dU, double relax, double gam, double wmin, int* bad,
                           cudaStream_t s) {
     NV_SWITCH(nv, (k_newton_update<NVC><<<blocks_for(nc), tpb_for(nc), 0, s>>>(nc, U, dU, relax, gam, wmin, bad)));

@@ -64,6 +64,13 @@ void launch_precond(int nv, const MeshView<double>& m, const Flow<double>& F, co
                     const double* dt, double* D, const double* mut, cudaStream_t s);
 void launch_newton_update(int nv, long nc, double* U, const double* dU, double relax, double gam, double wmin, int* bad,
                           cudaStream_t s);
+// time stepping: timeStepExplicit's update, solveUnsteady's right-hand side and update
+void launch_explicit_update(int nv, long nc, double* U, const double* R, const double* vol, double dt, int* bad,
+                            cudaStream_t s);
+void launch_unsteady_rhs(int nv, long nc, const double* U, const double* Uold, const double* R, const double* vol,
+                         double dt, double* rhs, RedScratch rs, double* out2, cudaStream_t s);
+void launch_relaxed_add(int nv, long nc, double* U, const double* dU, double relax, int* bad, cudaStream_t s);
+void launch_fill(long n, double* x, double v, cudaStream_t s);
 
 inline unsigned grid_for(long n, int threads = 256) { return (unsigned)((n + threads - 1) / threads); }
 // reduction / streaming grids: one entry per thread up to RED_BLOCKS blocks (enough warps

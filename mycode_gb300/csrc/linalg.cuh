@@ -334,6 +334,77 @@ __global__ void k_newton_update(long nc, double* __restrict__ U, const double* _
     if (!ok) atomicOr(bad, 1);
 }
 
+// timeStepExplicit (src/Solver.cpp:1219-1243): U -= R (dt / vol), then rho >= 1e-3 and
+// rhoE - kinetic energy >= 1e-3, in the reference's operation order; flags non-finite
+template <int NV>
+__global__ void k_explicit_update(long nc, double* __restrict__ U, const double* __restrict__ R,
+                                  const double* __restrict__ vol, double dt, int* bad) {
+    long i = (long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= nc) return;
+    const double s = dt / vol[i];
+    double u[NV];
+#pragma unroll
+    for (int c = 0; c < NV; ++c) u[c] = U[c * nc + i] - R[c * nc + i] * s;
+    if (u[0] < 1e-3) u[0] = 1e-3;
+    double ke = 0.5 * (u[1] * u[1] + u[2] * u[2]) / u[0];
+    double ie = u[3] - ke;
+    if (ie < 1e-3) u[3] = ke + 1e-3;
+    bool ok = true;
+#pragma unroll
+    for (int c = 0; c < NV; ++c) {
+        ok = ok && isfinite(u[c]);
+        U[c * nc + i] = u[c];
+    }
+    if (!ok) atomicOr(bad, 1);
+}
+
+// solveUnsteady's Newton right-hand side (src/Solver.cpp:1822-1838):
+// F = (U - U_old) vol / dt + R, rhs = -F, with the pieces of the volume-weighted norm of
+// F / vol over rho, rhou, rhov, rhoE: out2 = (sum of |F/vol|^2 vol, sum of vol)
+template <int NV>
+__global__ void __launch_bounds__(RED_THREADS) k_unsteady_rhs(long nc, const double* __restrict__ U,
+                                                              const double* __restrict__ Uold,
+                                                              const double* __restrict__ R,
+                                                              const double* __restrict__ vol, double dt,
+                                                              double* __restrict__ rhs, RedScratch rs, double* out2) {
+    double v[2] = {0.0, 0.0};
+    for (long i = (long)blockIdx.x * blockDim.x + threadIdx.x; i < nc; i += (long)gridDim.x * blockDim.x) {
+        const double vl = vol[i];
+        const double s = vl / dt;
+        double f[NV];
+#pragma unroll
+        for (int c = 0; c < NV; ++c) {
+            long q = c * nc + i;
+            f[c] = (U[q] - Uold[q]) * s + R[q];
+            rhs[q] = f[c] * (-1.0);
+        }
+        double a = f[0] / vl, b = f[1] / vl, c2 = f[2] / vl, e = f[3] / vl;
+        v[0] += (a * a + b * b + c2 * c2 + e * e) * vl;
+        v[1] += vl;
+    }
+    grid_finish<2>(v, rs, out2);
+}
+
+// U += relax * dU (the dual-time Newton update of src/Solver.cpp:1853-1856, no clamps)
+template <int NV>
+__global__ void k_relaxed_add(long nc, double* __restrict__ U, const double* __restrict__ dU, double relax, int* bad) {
+    long i = (long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= nc) return;
+    bool ok = true;
+#pragma unroll
+    for (int c = 0; c < NV; ++c) {
+        long q = c * nc + i;
+        double u = U[q] + dU[q] * relax;
+        ok = ok && isfinite(u);
+        U[q] = u;
+    }
+    if (!ok) atomicOr(bad, 1);
+}
+
+static __global__ void k_fill(long n, double* __restrict__ x, double v) {
+    for (long q = (long)blockIdx.x * blockDim.x + threadIdx.x; q < n; q += (long)gridDim.x * blockDim.x) x[q] = v;
+}
+
 // AoS (stride doubles per cell, reference numbering) <-> SoA (np planes, internal
 // numbering); AoS slots np..stride-1 are written as zero
 template <class T>

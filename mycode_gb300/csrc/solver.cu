@@ -880,6 +880,78 @@ struct cfdg_solver {
         return CFDG_OK;
     }
 
+    // ---- time stepping (src/Solver.cpp:1219-1243, :1801-1864)
+    double* Uold = nullptr;  // solveUnsteady's U at the start of the physical step
+    double physical_time = 0.0;
+    long long exp_steps = 0;
+
+    // timeStepExplicit: residual (limiter updated), U -= R dt / vol, positivity clamps;
+    // res_l2 (optional) = norm_L2 of that residual
+    cfdg_status time_step_explicit(double dtp, double* res_l2) {
+        TRY(residual_dev(U, R, 1));
+        if (res_l2) {
+            launch_dot<double>(nv, nc, R, R, rs, scal + 11, st);
+            ++launches;
+        }
+        CK(cudaMemsetAsync(bad, 0, sizeof(int), st));
+        launch_explicit_update(nv, nc, U, R, g64.vol, dtp, bad, st);
+        ++launches;
+        ++exp_steps;
+        int hbad = 0;
+        CK(cudaMemcpyAsync(&hbad, bad, sizeof(int), cudaMemcpyDeviceToHost, st));
+        if (res_l2) {
+            double sq;
+            TRY(read_scalars(11, 1, &sq));
+            *res_l2 = std::sqrt(sq);
+        } else {
+            CK(cudaStreamSynchronize(st));
+            collect();
+        }
+        if (hbad) return fail(CFDG_ERR_NAN, "non-finite state after explicit step " + std::to_string(exp_steps));
+        return CFDG_OK;
+    }
+
+    // solveUnsteady: dual time stepping with BDF1, at most 15 Newton steps per physical
+    // step to a residual of 1e-6 (after the first), GMRES with dt = dt_phy in the time
+    // term and the preconditioner, update relaxed by 0.7.  Per physical step: Newton steps
+    // taken and the last residual.
+    cfdg_status solve_unsteady(double dt_phy, int n_steps, int* newton, double* res) {
+        if (!Uold) TRY(dalloc(&Uold, (size_t)L));
+        launch_fill(nc, dt, dt_phy, st);
+        ++launches;
+        for (int t = 1; t <= n_steps; ++t) {
+            CK(cudaMemcpyAsync(Uold, U, sizeof(double) * L, cudaMemcpyDeviceToDevice, st));
+            physical_time += dt_phy;
+            int taken = 0;
+            double resVM = 0.0;
+            for (int step = 0; step < 15; ++step) {
+                TRY(residual_dev(U, R, 1));
+                launch_unsteady_rhs(nv, nc, U, Uold, R, g64.vol, dt_phy, rhs, rs, scal + 8, st);
+                ++launches;
+                double s2[2];
+                TRY(read_scalars(8, 2, s2));
+                resVM = std::sqrt(s2[0] / s2[1]);
+                taken = step;
+                if (!std::isfinite(resVM))
+                    return fail(CFDG_ERR_NAN, "non-finite unsteady residual at time step " + std::to_string(t));
+                if (resVM < 1e-6 && step > 0) break;
+                int it = 0;
+                TRY(gmres(U, R, rhs, x, &it));
+                CK(cudaMemsetAsync(bad, 0, sizeof(int), st));
+                launch_relaxed_add(nv, nc, U, x, 0.7, bad, st);
+                ++launches;
+                taken = step + 1;
+            }
+            if (newton) newton[t - 1] = taken;
+            if (res) res[t - 1] = resVM;
+        }
+        int hbad = 0;
+        CK(cudaMemcpyAsync(&hbad, bad, sizeof(int), cudaMemcpyDeviceToHost, st));
+        CK(cudaStreamSynchronize(st));
+        if (hbad) return fail(CFDG_ERR_NAN, "non-finite state in the unsteady solve");
+        return CFDG_OK;
+    }
+
     // one step of solveImplicit (src/Solver.cpp:1705-1797)
     cfdg_status newton_step(double tol, cfdg_step* info, int* converged) {
         double t0 = now_s();
@@ -1083,6 +1155,7 @@ struct cfdg_solver {
         cudaFree(obuf);
         cudaFree(f32out);
         cudaFree(f32dir);
+        cudaFree(Uold);
         cudaFree(dinv32);
         cudaFree(dinv64);
         void* pt[] = {Tt, Tj, Tjd, dwall, T32, T32d, dwall32};
@@ -1539,6 +1612,16 @@ cfdg_status cfdg_jv(cfdg_solver* s, const double* Ubase, const double* Rbase, co
     TRY(s->upload_aos(v, s->vtmp));
     TRY(s->jv64(s->Ub, s->Rb, s->vtmp, s->x, mode, false));
     return s->download_aos(s->x, Jv, s->nv, 6);
+}
+
+cfdg_status cfdg_time_step_explicit(cfdg_solver* s, double dt, double* res_l2) {
+    if (!s || !(dt > 0)) return fail(CFDG_ERR_ARG, "null solver or non-positive dt");
+    return s->time_step_explicit(dt, res_l2);
+}
+
+cfdg_status cfdg_solve_unsteady(cfdg_solver* s, double dt_phy, int n_steps, int* newton_steps, double* res_vm) {
+    if (!s || !(dt_phy > 0) || n_steps < 0) return fail(CFDG_ERR_ARG, "bad arguments");
+    return s->solve_unsteady(dt_phy, n_steps, newton_steps, res_vm);
 }
 
 cfdg_status cfdg_residual32(cfdg_solver* s, const double* U, double* R) {

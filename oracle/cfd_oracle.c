@@ -904,6 +904,69 @@ done:
     return k + 1;
 }
 
+/* timeStepExplicit (src/Solver.cpp:1219-1243): residual with the limiter updated,
+ * U -= R (dt / vol), rho >= 1e-3, rhoE - kinetic energy >= 1e-3.  Returns norm_L2 of the
+ * residual used. */
+double om_time_step_explicit(om_solver* s, double dt) {
+    int n = s->m->n_cells;
+    double* R = (double*)malloc(sizeof(double) * NV * (size_t)n);
+    om_residual(s, s->U, R, 1);
+    double rn = om_norm(n, R);
+    for (int i = 0; i < n; ++i) {
+        double vol = s->m->vol[i];
+        st_t u = st_sub(st_load(s->U + NV * i), st_mul(st_load(R + NV * i), dt / vol));
+        if (u.r < 1e-3) u.r = 1e-3;
+        double ke = 0.5 * (u.ru * u.ru + u.rv * u.rv) / u.r;
+        double ie = u.rE - ke;
+        if (ie < 1e-3) u.rE = ke + 1e-3;
+        st_store(s->U + NV * i, u);
+    }
+    free(R);
+    return rn;
+}
+
+/* solveUnsteady (src/Solver.cpp:1801-1864): dual time stepping, BDF1, at most 15 Newton
+ * steps per physical step to 1e-6 (after the first), GMRES with dt_local = dt_phy,
+ * updates relaxed by 0.7.  Writes per physical step the Newton steps taken and the last
+ * residual. */
+void om_solve_unsteady(om_solver* s, double dt_phy, int n_steps, int* newton, double* res_out) {
+    int n = s->m->n_cells;
+    size_t len = (size_t)NV * n;
+    double* Uold = (double*)malloc(sizeof(double) * len);
+    double* R = (double*)malloc(sizeof(double) * len);
+    double* rhs = (double*)malloc(sizeof(double) * len);
+    double* dU = (double*)malloc(sizeof(double) * len);
+    for (int i = 0; i < n; ++i) s->dt[i] = dt_phy;
+    for (int t = 1; t <= n_steps; ++t) {
+        memcpy(Uold, s->U, sizeof(double) * len);
+        int taken = 0;
+        double resVM = 0.0;
+        for (int step = 0; step < 15; ++step) {
+            om_residual(s, s->U, R, 1);
+            double norm_sq = 0.0, total_vol = 0.0;
+            for (int i = 0; i < n; ++i) {
+                double vol = s->m->vol[i];
+                st_t dUdt = st_mul(st_sub(st_load(s->U + NV * i), st_load(Uold + NV * i)), vol / dt_phy);
+                st_t F = st_add(dUdt, st_load(R + NV * i));
+                st_store(rhs + NV * i, st_mul(F, -1.0));
+                double a = F.r / vol, b = F.ru / vol, c = F.rv / vol, e = F.rE / vol;
+                norm_sq += (a * a + b * b + c * c + e * e) * vol;
+                total_vol += vol;
+            }
+            resVM = sqrt(norm_sq / total_vol);
+            taken = step;
+            if (resVM < 1e-6 && step > 0) break;
+            om_gmres(s, s->U, R, rhs, dU);
+            for (int i = 0; i < n; ++i)
+                st_store(s->U + NV * i, st_add(st_load(s->U + NV * i), st_mul(st_load(dU + NV * i), 0.7)));
+            taken = step + 1;
+        }
+        if (newton) newton[t - 1] = taken;
+        if (res_out) res_out[t - 1] = resVM;
+    }
+    free(Uold); free(R); free(rhs); free(dU);
+}
+
 /* solveImplicit: pseudo-transient Newton with the reference CFL schedule, limiter
  * freeze, relaxation and positivity clamps (src/Solver.cpp:1696-1799).  Writes, per
  * step, the volume-weighted and plain residual norms, the CFL and the GMRES count;

@@ -68,6 +68,8 @@ def _oracle_lib():
             "om_set_gmres": (None, [vp, C.c_int, C.c_double]),
             "om_set_nu": (None, [vp, C.c_double]),
             "om_set_cfl0": (None, [vp, C.c_double]),
+            "om_time_step_explicit": (C.c_double, [vp, C.c_double]),
+            "om_solve_unsteady": (None, [vp, C.c_double, C.c_int, _ip, _dp]),
             "om_set_flow_conditions": (None, [vp, C.c_double, C.c_double, C.c_double]),
             "om_set_freestream_static": (None, [vp, C.c_double, C.c_double, C.c_double]),
             "om_set_kinematic_viscosity": (None, [vp, C.c_double, C.c_double]),
@@ -173,6 +175,15 @@ class OracleSolver(_Base):
 
     def setCFL0(self, cfl0):
         self._L.om_set_cfl0(self._s, float(cfl0))
+
+    def timeStepExplicit(self, dt):
+        return self._L.om_time_step_explicit(self._s, float(dt))
+
+    def solveUnsteady(self, dt_phy, max_time_steps):
+        n = int(max_time_steps)
+        it, res = np.zeros(max(n, 1), np.int32), np.zeros(max(n, 1))
+        self._L.om_solve_unsteady(self._s, float(dt_phy), n, it, res)
+        return {"newton_steps": it[:n], "res_vm": res[:n]}
 
     def setFlowConditions(self, M, P, T):
         self._L.om_set_flow_conditions(self._s, M, P, T)
@@ -350,6 +361,8 @@ class RefSolver(_Base):
                 "ref_drag": (C.c_double, [vp]),
                 "ref_entropy_error": (C.c_double, [vp]),
                 "ref_skin_friction": (C.c_int, [vp, C.c_char_p, _dp, _dp, C.c_int]),
+                "ref_time_step_explicit": (None, [vp, C.c_double]),
+                "ref_solve_unsteady": (None, [vp, C.c_double, C.c_int]),
             }
             for name, (res, args) in sig.items():
                 fn = getattr(lib, name)
@@ -481,3 +494,9 @@ class RefSolver(_Base):
         x, cf = np.zeros(cap), np.zeros(cap)
         n = self._L.ref_skin_friction(self._h, str(path).encode(), x, cf, cap)
         return x[:n], cf[:n]
+
+    def timeStepExplicit(self, dt):
+        self._L.ref_time_step_explicit(self._h, float(dt))
+
+    def solveUnsteady(self, dt_phy, max_time_steps):
+        self._L.ref_solve_unsteady(self._h, float(dt_phy), int(max_time_steps))

@@ -279,6 +279,18 @@ std::string captured(Fn f) {
 
 extern "C" {
 
+// timeStepExplicit (src/Solver.cpp:1219-1243) on the current state (its output captured)
+void ref_time_step_explicit(void* p, double dt) {
+    Solver* s = ((Handle*)p)->solver;
+    captured([&] { s->timeStepExplicit(dt); });
+}
+
+// solveUnsteady (src/Solver.cpp:1801-1864) from the current state (its output captured)
+void ref_solve_unsteady(void* p, double dt_phy, int n_steps) {
+    Solver* s = ((Handle*)p)->solver;
+    captured([&] { s->solveUnsteady(dt_phy, n_steps); });
+}
+
 // computeWallDistances (src/Solver.cpp:1981-2015)
 void ref_wall_distance(void* p, double* d) {
     Solver* s = ((Handle*)p)->solver;
