@@ -89,6 +89,11 @@ void launch_precond(int nv, const MeshView<double>& m, const Flow<double>& F, co
                     const double* dt, double* D, const double* mut, cudaStream_t s) {
     NV_SWITCH(nv, (k_precond<NVC><<<blocks_for(m.nc), tpb_for(m.nc), 0, s>>>(m, F, U, W, dt, D, mut)));
 }
+void launch_newton_update_dev(int nv, long nc, double* U, const double* dU, const double* norms, double tol, double gam,
+                              double wmin, int* bad, cudaStream_t s) {
+    NV_SWITCH(nv, (k_newton_update_dev<NVC><<<blocks_for(nc), tpb_for(nc), 0, s>>>(nc, U, dU, norms, tol, gam, wmin,
+                                                                                   bad)));
+}
 void launch_explicit_update(int nv, long nc, double* U, const double* R, const double* vol, double dt, int* bad,
                             cudaStream_t s) {
     NV_SWITCH(nv, (k_explicit_update<NVC><<<blocks_for(nc), tpb_for(nc), 0, s>>>(nc, U, R, vol, dt, bad)));

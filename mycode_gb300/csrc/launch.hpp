@@ -64,6 +64,9 @@ void launch_precond(int nv, const MeshView<double>& m, const Flow<double>& F, co
                     const double* dt, double* D, const double* mut, cudaStream_t s);
 void launch_newton_update(int nv, long nc, double* U, const double* dU, double relax, double gam, double wmin, int* bad,
                           cudaStream_t s);
+// the Newton update with its decisions (converged / non-finite / relaxation) on the device
+void launch_newton_update_dev(int nv, long nc, double* U, const double* dU, const double* norms, double tol, double gam,
+                              double wmin, int* bad, cudaStream_t s);
 // time stepping: timeStepExplicit's update, solveUnsteady's right-hand side and update
 void launch_explicit_update(int nv, long nc, double* U, const double* R, const double* vol, double dt, int* bad,
                             cudaStream_t s);

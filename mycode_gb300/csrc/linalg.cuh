@@ -334,6 +334,45 @@ __global__ void k_newton_update(long nc, double* __restrict__ U, const double* _
     if (!ok) atomicOr(bad, 1);
 }
 
+// The same update with the step's decisions taken on the device from the residual norm
+// pieces norms[0..1] (sum of R^2 vol, sum of vol): no update when the volume-weighted
+// norm is below tol (converged) or not finite, relaxation 0.5 above 1e6 (as the host
+// driver, src/Solver.cpp:1753-1758).  Lets the whole Newton step run without a host
+// round trip before the update.
+template <int NV>
+__global__ void k_newton_update_dev(long nc, double* __restrict__ U, const double* __restrict__ dU,
+                                    const double* __restrict__ norms, double tol, double gam, double wmin, int* bad) {
+    long i = (long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= nc) return;
+    const double s0 = norms[0], s1 = norms[1];
+    const double resVM = s1 == 0 ? 0.0 : sqrt(s0 / s1);
+    if (!(resVM >= tol) || !isfinite(resVM)) return;
+    double relax = 1.0;
+    if (resVM > 1e6) relax = 0.5;
+    else if (resVM > 2e3 && resVM < 1e2) relax = 0.9;
+    double u[NV];
+#pragma unroll
+    for (int c = 0; c < NV; ++c) u[c] = U[c * nc + i] + dU[c * nc + i] * relax;
+    double ke = 0.5 * (u[1] * u[1] + u[2] * u[2]) / (u[0] + 1e-12);
+    double pn = (gam - 1.0) * (u[3] - ke);
+    if (u[0] < 1e-5) u[0] = 1e-5;
+    if (pn < 1e-5) {
+        pn = 1e-5;
+        u[3] = pn / (gam - 1.0) + ke;
+    }
+    if constexpr (NV == 6) {
+        if (u[4] < 0.0) u[4] = 0.0;
+        if (u[5] < u[0] * wmin) u[5] = u[0] * wmin;
+    }
+    bool ok = true;
+#pragma unroll
+    for (int c = 0; c < NV; ++c) {
+        ok = ok && isfinite(u[c]);
+        U[c * nc + i] = u[c];
+    }
+    if (!ok) atomicOr(bad, 1);
+}
+
 // timeStepExplicit (src/Solver.cpp:1219-1243): U -= R (dt / vol), then rho >= 1e-3 and
 // rhoE - kinetic energy >= 1e-3, in the reference's operation order; flags non-finite
 template <int NV>

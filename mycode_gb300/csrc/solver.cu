@@ -952,8 +952,91 @@ struct cfdg_solver {
         return CFDG_OK;
     }
 
+    // pinned host words the single-sync Newton step reads back: [0..3] the norm pieces,
+    // [4] the GMRES k, [5] the non-finite flag
+    double* hpin = nullptr;
+
+    // One step of solveImplicit with the graph driver and a single host round trip: the
+    // residual, its norms, the GMRES graph and the update (its decisions taken on the
+    // device) are enqueued together, the CFL control runs on the host afterwards.  Same
+    // arithmetic and the same decisions as newton_step's host-driven sequence.
+    cfdg_status newton_step_graph(double tol, cfdg_step* info, int* converged) {
+        double t0 = now_s();
+        *converged = 0;
+        TRY(ensure_krylov());
+        if (!gexec || graph_version != flow_version || gkey[0] != U || gkey[1] != R || gkey[2] != rhs || gkey[3] != x) {
+            CK(cudaStreamSynchronize(st));
+            TRY(build_gmres_graph(U, R, rhs, x));
+        }
+        if (timing) CK(cudaEventRecord(step_ev[0], st));
+        launch_prim64(nv, nc, F, f64(U), f64(W), st);
+        launch_local_dt(nv, mv, F, U, W, cfl, dt, st);
+        launches += 2;
+        bool upd = !(step > cfg.limiter_freeze_step || cfl > cfg.limiter_freeze_cfl);
+        TRY(residual_dev(U, R, upd ? 1 : 0));
+        launch_norm_vm(nv, nc, R, g64.vol, rs, scal + 8, st);
+        launch_dot<double>(nv, nc, R, R, rs, scal + 11, st);
+        launch_scale_from<double>(L, rhs, R, scal + 6, 0, st);  // rhs = -R (scal[6] holds -1)
+        launches += 3;
+        if (timing) CK(cudaEventRecord(step_ev[2], st));
+        CK(cudaGraphLaunch(gexec, st));
+        if (timing) CK(cudaEventRecord(step_ev[3], st));
+        CK(cudaMemsetAsync(bad, 0, sizeof(int), st));
+        launch_newton_update_dev(nv, nc, U, x, scal + 8, tol, cfg.gamma, F.w_inf * SstConst::w_min_frac, bad, st);
+        ++launches;
+        CK(cudaMemcpyAsync(hpin, scal + 8, 4 * sizeof(double), cudaMemcpyDeviceToHost, st));
+        int* hi = reinterpret_cast<int*>(hpin + 4);
+        CK(cudaMemcpyAsync(hi, gd.gi + 1, sizeof(int), cudaMemcpyDeviceToHost, st));
+        CK(cudaMemcpyAsync(hi + 1, bad, sizeof(int), cudaMemcpyDeviceToHost, st));
+        cfdg_step rec;
+        rec.gmres_iters = 0;
+        rec.krylov_ms = 0;
+        TRY(step_time(rec, t0));
+        const double* s = hpin;
+        double resVM = s[1] == 0 ? 0.0 : std::sqrt(s[0] / s[1]);
+        rec.res_vm = resVM;
+        rec.res_abs = std::sqrt(s[3]);
+        rec.res_rho = s[1] == 0 ? 0.0 : std::sqrt(s[2] / s[1]);
+        rec.cfl = cfl;
+        rec.limiter_updated = upd ? 1 : 0;
+        if (!std::isfinite(resVM)) {
+            if (info) *info = rec;
+            return fail(CFDG_ERR_NAN, "non-finite residual at Newton step " + std::to_string(step));
+        }
+        if (resVM < tol) {  // the update was skipped on the device
+            rec.krylov_ms = 0;
+            *converged = 1;
+            if (info) *info = rec;
+            return CFDG_OK;
+        }
+        const int it = hi[0] + 1;
+        launches += graph_pre + (long long)it * graph_body + graph_post;
+        rec.gmres_iters = it;
+        if (timing) {
+            float ms = 0;
+            CK(cudaEventElapsedTime(&ms, step_ev[2], step_ev[3]));
+            rec.krylov_ms = ms;
+        }
+        if (it >= 29) {
+            cfl *= 0.5;
+            if (cfl < 0.05) cfl = 0.05;
+        }
+        if (step > 5) {
+            if (resVM > 1e6) cfl *= 1.2;
+            else cfl *= 1.5;
+            if (it >= 25) cfl *= 0.5;
+            if (cfl > cfg.cfl_max) cfl = cfg.cfl_max;
+            if (cfl < 0.1) cfl = 0.1;
+        }
+        ++step;
+        if (info) *info = rec;
+        if (hi[1]) return fail(CFDG_ERR_NAN, "non-finite state after the Newton update at step " + std::to_string(step - 1));
+        return CFDG_OK;
+    }
+
     // one step of solveImplicit (src/Solver.cpp:1705-1797)
     cfdg_status newton_step(double tol, cfdg_step* info, int* converged) {
+        if (cfg.krylov == CFDG_KRYLOV_GRAPH) return newton_step_graph(tol, info, converged);
         double t0 = now_s();
         *converged = 0;
         if (timing) CK(cudaEventRecord(step_ev[0], st));
@@ -1156,6 +1239,7 @@ struct cfdg_solver {
         cudaFree(f32out);
         cudaFree(f32dir);
         cudaFree(Uold);
+        if (hpin) cudaFreeHost(hpin);
         cudaFree(dinv32);
         cudaFree(dinv64);
         void* pt[] = {Tt, Tj, Tjd, dwall, T32, T32d, dwall32};
@@ -1383,6 +1467,13 @@ cfdg_status cfdg_solver_create(const cfdg_mesh* m, const cfdg_config* cfg, cfdg_
     TRYS(dalloc(&s->rs.counter, 1));
     TRYS(dalloc(&s->scal, 16 + (size_t)(c.gmres_m + 2) * (c.gmres_m + 2) + 8));
     TRYS(dalloc(&s->bad, 1));
+    {
+        // scal[6] = -1, the constant of rhs = -R; pinned words for the single-sync step
+        const double m1 = -1.0;
+        if (cudaMemcpy(s->scal + 6, &m1, sizeof(double), cudaMemcpyHostToDevice) != cudaSuccess ||
+            cudaMallocHost((void**)&s->hpin, 8 * sizeof(double)) != cudaSuccess)
+            return bail(fail(CFDG_ERR_CUDA, "scalar scratch"));
+    }
     if (c.gmres_m <= KRY_MAXM) {  // device-GMRES state, so the driver can be switched at run time
         int m = c.gmres_m;
         TRYS(dalloc(&s->gdi, 4));
