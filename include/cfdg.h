@@ -88,6 +88,11 @@ typedef struct cfdg_config {
      * solve as one CUDA graph (WHILE node, device Givens, CGS2 orthogonalisation);
      * CFDG_KRYLOV_AUTO picks GRAPH for mixed precision or exact J v, else HOST. */
     int krylov;
+    /* graph driver with exact J v: 1 runs each Arnoldi iteration as one persistent kernel
+     * with grid barriers between its phases, 0 (default) as six kernels; measured on the
+     * 28,800-cell plate: FP32 basis 63-72 us per iteration persistent vs 54-64 us six
+     * kernels, FP64 exact 186-200 vs 186-211 us */
+    int persistent;
 } cfdg_config;
 
 /* CFDG_KRYLOV_STREAM launches the graph driver's kernels one iteration at a time from a

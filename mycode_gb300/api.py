@@ -46,7 +46,7 @@ class Config(C.Structure):
         ("Pr", C.c_double), ("nu", C.c_double), ("cfl0", C.c_double), ("cfl_max", C.c_double),
         ("limiter_freeze_step", C.c_int), ("limiter_freeze_cfl", C.c_double),
         ("turb_intensity", C.c_double), ("mut_ratio", C.c_double), ("shock_deflection_deg", C.c_double),
-        ("renumber", C.c_int), ("device", C.c_int), ("krylov", C.c_int),
+        ("renumber", C.c_int), ("device", C.c_int), ("krylov", C.c_int), ("persistent", C.c_int),
     ]
 
 

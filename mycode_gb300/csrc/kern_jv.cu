@@ -3,6 +3,7 @@
 // limiter is frozen (phi read, zero derivative), as in the reference's applyJacobian
 // (src/Solver.cpp:1366).  The gather adds the time term v * vol/(dt + 1e-30).
 #include "launch.hpp"
+#include "arnoldi.cuh"
 
 namespace cfdg {
 
@@ -59,5 +60,40 @@ void launch_jv<float>(const ResArgs<float>& a) {
     if (a.nv == 6) jv_nv<float, 6>(a);
     else jv_nv<float, 4>(a);
 }
+
+template <class T>
+int arnoldi_blocks(int nv) {
+    int dev = 0, sms = 0, per = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    if (nv == 6) cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_arnoldi<T, 6>, RED_THREADS, 0);
+    else cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_arnoldi<T, 4>, RED_THREADS, 0);
+    long b = (long)sms * per;
+    return (int)(b < RED_BLOCKS ? b : RED_BLOCKS);
+}
+
+template <class T>
+cudaError_t launch_arnoldi(int nv, const ArnoldiArgs<T>& a, cudaGraphConditionalHandle h, int blocks, bool coop,
+                           cudaStream_t s) {
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3((unsigned)blocks);
+    cfg.blockDim = dim3(RED_THREADS);
+    cfg.dynamicSmemBytes = 0;
+    cfg.stream = s;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeCooperative;
+    attr[0].val.cooperative = 1;
+    cfg.attrs = coop ? attr : nullptr;
+    cfg.numAttrs = coop ? 1 : 0;
+    if (nv == 6) return cudaLaunchKernelEx(&cfg, k_arnoldi<T, 6>, a, h);
+    return cudaLaunchKernelEx(&cfg, k_arnoldi<T, 4>, a, h);
+}
+
+template int arnoldi_blocks<float>(int);
+template int arnoldi_blocks<double>(int);
+template cudaError_t launch_arnoldi<float>(int, const ArnoldiArgs<float>&, cudaGraphConditionalHandle, int, bool,
+                                           cudaStream_t);
+template cudaError_t launch_arnoldi<double>(int, const ArnoldiArgs<double>&, cudaGraphConditionalHandle, int, bool,
+                                            cudaStream_t);
 
 }  // namespace cfdg

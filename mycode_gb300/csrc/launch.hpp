@@ -143,6 +143,16 @@ template <class T> void launch_gmres_solution_dev(int nv, long nc, const T* V, l
                                                   const double* D, double* x, cudaStream_t s);
 }  // namespace cfdg
 
+// ---- one Arnoldi iteration as one persistent kernel (arnoldi.cuh, kern_jv.cu)
+namespace cfdg {
+template <class T> struct ArnoldiArgs;
+// blocks that can be resident at once (at most RED_BLOCKS)
+template <class T> int arnoldi_blocks(int nv);
+// launch (cooperative when coop); returns the launch's error
+template <class T> cudaError_t launch_arnoldi(int nv, const ArnoldiArgs<T>& a, cudaGraphConditionalHandle h,
+                                              int blocks, bool coop, cudaStream_t s);
+}  // namespace cfdg
+
 // ---- adjoint of the FP64 residual (kern_adj.cu); a.phi receives the recomputed limiter
 namespace cfdg {
 struct AdjBufs;

@@ -133,11 +133,9 @@ __global__ void __launch_bounds__(256) k_prim(int nc, Flow<R> F, Field<R> U, Fie
 // in reference face order, then (limited scheme, limiter not frozen) computeLimiters
 // (src/Solver.cpp:152-253) for the same cell from its own fresh gradient.
 template <class S, int NV, class R>
-__global__ void __launch_bounds__(256) k_grad(MeshView<R> m, Flow<R> F, Field<R> U, Field<R> W, Field<R> G,
-                                              R* phi, int do_limiter) {
+__device__ __forceinline__ void grad_item(const MeshView<R>& m, const Flow<R>& F, const Field<R>& U,
+                                          const Field<R>& W, const Field<R>& G, R* phi, int do_limiter, long i) {
     constexpr int NQ = NV == 6 ? 7 : 5;
-    long i = (long)blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= m.nc) return;
     S wi[NQ];
 #pragma unroll
     for (int q = 0; q < NQ; ++q) wi[q] = Acc<S>::ld(W, q, i);
@@ -228,6 +226,14 @@ __global__ void __launch_bounds__(256) k_grad(MeshView<R> m, Flow<R> F, Field<R>
     phi[i] = lim;
 }
 
+template <class S, int NV, class R>
+__global__ void __launch_bounds__(256) k_grad(MeshView<R> m, Flow<R> F, Field<R> U, Field<R> W, Field<R> G,
+                                              R* phi, int do_limiter) {
+    long i = (long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= m.nc) return;
+    grad_item<S, NV>(m, F, U, W, G, phi, do_limiter, i);
+}
+
 // ---------------------------------------------------------------- k_flux
 // The face loop of computeResiduals (src/Solver.cpp:543-800) through face_flux:
 // reconstruction, the wall pressure flux or the Riemann flux, and (viscous) the
@@ -255,10 +261,8 @@ __device__ __forceinline__ FaceGeo<R> load_geo(const MeshView<R>& m, long f) {
 
 // SST cell terms (sst.cuh): T planes 0 mu_t, 1 F1, 2 S_k vol, 3 S_w vol
 template <class S, int NV, class R>
-__global__ void __launch_bounds__(256) k_sst_cell(MeshView<R> m, Flow<R> F, Field<R> W, Field<R> G,
-                                                  const R* __restrict__ dwall, Field<R> T) {
-    long i = (long)blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= m.nc) return;
+__device__ __forceinline__ void sst_item(const MeshView<R>& m, const Flow<R>& F, const Field<R>& W,
+                                         const Field<R>& G, const R* __restrict__ dwall, const Field<R>& T, long i) {
     SstCell<S> c = sst_cell(F, Acc<S>::ld(W, W_R, i), Acc<S>::ld(W, W_K, i), Acc<S>::ld(W, W_W, i),
                             Acc<S>::ld(G, G_U, i), Acc<S>::ld(G, G_U + 1, i), Acc<S>::ld(G, G_V, i),
                             Acc<S>::ld(G, G_V + 1, i), Acc<S>::ld(G, G_K, i), Acc<S>::ld(G, G_K + 1, i),
@@ -271,10 +275,17 @@ __global__ void __launch_bounds__(256) k_sst_cell(MeshView<R> m, Flow<R> F, Fiel
 }
 
 template <class S, int NV, class R>
-__global__ void __launch_bounds__(256) k_flux(MeshView<R> m, Flow<R> F, Field<R> U, Field<R> W, Field<R> G,
-                                              const R* __restrict__ phi, Field<R> FA, Field<R> T) {
-    long f = (long)blockIdx.x * blockDim.x + threadIdx.x;
-    if (f >= m.nf) return;
+__global__ void __launch_bounds__(256) k_sst_cell(MeshView<R> m, Flow<R> F, Field<R> W, Field<R> G,
+                                                  const R* __restrict__ dwall, Field<R> T) {
+    long i = (long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= m.nc) return;
+    sst_item<S, NV>(m, F, W, G, dwall, T, i);
+}
+
+template <class S, int NV, class R>
+__device__ __forceinline__ void flux_item(const MeshView<R>& m, const Flow<R>& F, const Field<R>& U,
+                                          const Field<R>& W, const Field<R>& G, const R* __restrict__ phi,
+                                          const Field<R>& FA, const Field<R>& T, long f) {
     int o = m.fo[f], n = m.fn[f];
     bool interior = n >= 0;
     int tag = interior ? 0 : m.ftag[f];
@@ -319,6 +330,14 @@ __global__ void __launch_bounds__(256) k_flux(MeshView<R> m, Flow<R> F, Field<R>
     Flux6<S> out = face_flux(F, L, Rn, interior, tag, g, gL, gR, phL, phR);
 #pragma unroll
     for (int c = 0; c < NV; ++c) Acc<S>::st(FA, c, f, out.f[c]);
+}
+
+template <class S, int NV, class R>
+__global__ void __launch_bounds__(256) k_flux(MeshView<R> m, Flow<R> F, Field<R> U, Field<R> W, Field<R> G,
+                                              const R* __restrict__ phi, Field<R> FA, Field<R> T) {
+    long f = (long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (f >= m.nf) return;
+    flux_item<S, NV>(m, F, U, W, G, phi, FA, T, f);
 }
 
 // ---------------------------------------------------------------- k_gather

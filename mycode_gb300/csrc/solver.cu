@@ -17,6 +17,7 @@
 
 #include "../../include/cfdg.h"
 #include "adjoint_kernels.cuh"
+#include "arnoldi.cuh"
 #include "launch.hpp"
 #include "mesh.hpp"
 
@@ -465,8 +466,56 @@ struct cfdg_solver {
             TRY(dalloc(&z, (size_t)L));
             TRY(dalloc(&dinv64, nd));
         }
+        if (!bar) {
+            // persistent Arnoldi kernel: barrier words and three sets of block partials
+            TRY(dalloc(&bar, 4));
+            TRY(dalloc(&apart, (2 * (size_t)(KRY_MAXM + 1) + 1) * RED_BLOCKS));
+        }
         m_alloc = m;
         return CFDG_OK;
+    }
+
+    // a grid barrier of the persistent kernel gave up: reset its words, report
+    cfdg_status barrier_timeout() {
+        CK(cudaMemsetAsync(bar, 0, 4 * sizeof(unsigned), st));
+        CK(cudaStreamSynchronize(st));
+        return fail(CFDG_ERR_TIMEOUT, "a grid barrier of the persistent Arnoldi kernel timed out "
+                                      "(its blocks were not all resident); set persistent = 0");
+    }
+
+    // the persistent Arnoldi kernel (arnoldi.cuh) replaces the fused six-kernel body in
+    // the graph driver for the exact J v; grid = the blocks that fit at once
+    unsigned* bar = nullptr;
+    double* apart = nullptr;
+    int ablocks = 0;
+    bool use_persistent() const {
+        return cfg.persistent && cfg.krylov == CFDG_KRYLOV_GRAPH &&
+               (cfg.precision == CFDG_MIXED || cfg.jv == CFDG_JV_EXACT);
+    }
+    template <class T>
+    ArnoldiArgs<T> arnoldi_args(const MeshView<T>& m, const Flow<T>& Fx, const T* Ub, T* zz, Field<T> Wf, Field<T> Gf,
+                                Field<T> FAf, Field<T> Tf, const T* dw, const T* ph, const T* dtx, const T* di, T* ww,
+                                T* VV) {
+        ArnoldiArgs<T> a;
+        a.m = m;
+        a.F = Fx;
+        a.U = Ub;
+        a.z = zz;
+        a.W = Wf;
+        a.G = Gf;
+        a.FA = FAf;
+        a.Tsst = Tf;
+        a.dwall = dw;
+        a.phi = ph;
+        a.dt = dtx;
+        a.Dinv = di;
+        a.w = ww;
+        a.V = VV;
+        a.L = L;
+        a.d = gd;
+        a.part = apart;
+        a.bar = GridBar{bar, bar + 1, reinterpret_cast<int*>(bar + 2)};
+        return a;
     }
 
     // ---- adjoint: gU = (dR/dU)^T lam at Uin, limiter recomputed into a scratch buffer
@@ -533,6 +582,23 @@ struct cfdg_solver {
         // the exact (dual-number) J v runs fused with the Arnoldi kernels: z with the
         // primitives, the gather with the first CGS pass; the FD J v keeps its own kernels.
         // ev (stream driver with timing): 7 events around the 6 stages, stat classes 12-17
+        if (use_persistent() && capturing) {
+            if (!ablocks) ablocks = mixed ? arnoldi_blocks<float>(nv) : arnoldi_blocks<double>(nv);
+            cudaError_t e;
+            if (mixed)
+                e = launch_arnoldi<float>(nv, arnoldi_args<float>(mvf, Ff, U32, z32, f32(W32, W32d), f32(G32, G32d),
+                                                                   ff32(nullptr, FA32d), f32(T32, T32d), dwall32, phi32,
+                                                                   dt32, dinv32, w32, V32),
+                                          h, ablocks, false, st);
+            else
+                e = launch_arnoldi<double>(nv, arnoldi_args<double>(mv, F, Ubase, z, f64(Wj, Wjd), f64(Gj, Gjd),
+                                                                     ff64(nullptr, FAjd), f64(Tj, Tjd), dwall, phi, dt,
+                                                                     dinv64, w64, V),
+                                           h, ablocks, false, st);
+            if (e != cudaSuccess) return fail(CFDG_ERR_CUDA, std::string("Arnoldi kernel: ") + cudaGetErrorString(e));
+            ++launches;
+            return CFDG_OK;
+        }
         cudaEvent_t* ev = (mixed || cfg.jv == CFDG_JV_EXACT) ? take_events(12, 6) : nullptr;
         if (ev) CK(cudaEventRecord(ev[0], st));
         if (mixed) {
@@ -719,10 +785,14 @@ struct cfdg_solver {
             gkey[3] != xout)
             TRY(build_gmres_graph(Ubase, Rbase, rhsd, xout));
         CK(cudaGraphLaunch(gexec, st));
-        int k = -1;
-        CK(cudaMemcpyAsync(&k, gd.gi + 1, sizeof(int), cudaMemcpyDeviceToHost, st));
+        int* hi = reinterpret_cast<int*>(hpin + 4);
+        hi[2] = 0;
+        CK(cudaMemcpyAsync(hi, gd.gi + 1, sizeof(int), cudaMemcpyDeviceToHost, st));
+        if (bar) CK(cudaMemcpyAsync(hi + 2, bar + 2, sizeof(int), cudaMemcpyDeviceToHost, st));
         CK(cudaStreamSynchronize(st));
         collect();
+        if (hi[2]) return barrier_timeout();
+        int k = hi[0];
         *iters = k + 1;
         launches += graph_pre + (long long)(k + 1) * graph_body + graph_post;
         return CFDG_OK;
@@ -988,10 +1058,13 @@ struct cfdg_solver {
         int* hi = reinterpret_cast<int*>(hpin + 4);
         CK(cudaMemcpyAsync(hi, gd.gi + 1, sizeof(int), cudaMemcpyDeviceToHost, st));
         CK(cudaMemcpyAsync(hi + 1, bad, sizeof(int), cudaMemcpyDeviceToHost, st));
+        hi[2] = 0;
+        if (bar) CK(cudaMemcpyAsync(hi + 2, bar + 2, sizeof(int), cudaMemcpyDeviceToHost, st));
         cfdg_step rec;
         rec.gmres_iters = 0;
         rec.krylov_ms = 0;
         TRY(step_time(rec, t0));
+        if (hi[2]) return barrier_timeout();
         const double* s = hpin;
         double resVM = s[1] == 0 ? 0.0 : std::sqrt(s[0] / s[1]);
         rec.res_vm = resVM;
@@ -1239,6 +1312,8 @@ struct cfdg_solver {
         cudaFree(f32out);
         cudaFree(f32dir);
         cudaFree(Uold);
+        cudaFree(bar);
+        cudaFree(apart);
         if (hpin) cudaFreeHost(hpin);
         cudaFree(dinv32);
         cudaFree(dinv64);
@@ -1312,6 +1387,7 @@ void cfdg_config_default(cfdg_config* c) {
     c->renumber = CFDG_RENUMBER_HILBERT;
     c->device = 0;
     c->krylov = CFDG_KRYLOV_AUTO;
+    c->persistent = 0;
 }
 
 cfdg_status cfdg_mesh_create(int n_nodes, const double* xy, int n_cells, const int* cells, int n_bedges,

@@ -90,7 +90,7 @@ def test_stream_driver_is_the_graph_bit_for_bit(cuda_lib, name, precision, jv):
     every stage of the fused body is timed."""
     out = {}
     for kry in (1, 2):
-        s, spec, case = _solver(cuda_lib, name, precision=precision, jv=jv, krylov=kry, gmres_m=12)
+        s, spec, case = _solver(cuda_lib, name, precision=precision, jv=jv, krylov=kry, gmres_m=12, persistent=0)
         o = OracleSolver(spec, bcset=case["bcset"], viscous=case["viscous"], init=case["init"])
         C.setup(o, case)
         U = C.perturbed_state(o.get_state(), o.cells(), seed=14)
@@ -107,3 +107,38 @@ def test_stream_driver_is_the_graph_bit_for_bit(cuda_lib, name, precision, jv):
             assert min(n) == max(n) == out[kry][0]
     assert out[1][0] == out[2][0]
     np.testing.assert_array_equal(out[1][1], out[2][1])
+
+
+@pytest.mark.parametrize("name", ["supersonic", "plate_visc", "bump_visc"])
+@pytest.mark.parametrize("precision", ["mixed", "fp64"])
+def test_persistent_arnoldi_kernel_matches_the_six_kernel_body(cuda_lib, name, precision):
+    """One persistent kernel per Arnoldi iteration (grid barriers between the phases)
+    against the six-kernel body: the same arithmetic per element, reductions partitioned
+    over a different number of blocks, so the same iterations and the same solution to
+    the basis precision."""
+    out = {}
+    for pers in (0, 1):
+        s, spec, case = _solver(cuda_lib, name, precision=precision, jv="exact", krylov=1, gmres_m=20, persistent=pers)
+        o = OracleSolver(spec, bcset=case["bcset"], viscous=case["viscous"], init=case["init"])
+        C.setup(o, case)
+        U = C.perturbed_state(o.get_state(), o.cells(), seed=15)
+        s.setNumericalMethod("ROE", "SECOND_ORDER_CENTRAL")
+        R = s.computeResiduals(U)
+        s.set_state(U)
+        s.local_timestep(20.0)
+        out[pers] = s.gmres(U, R, -R)
+    assert abs(out[0][0] - out[1][0]) <= 1
+    x0, x1 = out[0][1], out[1][1]
+    tol = 1e-4 if precision == "mixed" else 1e-10
+    if out[0][0] == out[1][0]:
+        assert np.linalg.norm(x1 - x0) <= tol * np.linalg.norm(x0)
+
+
+def test_persistent_arnoldi_newton_solve(cuda_lib):
+    """Newton steps with the persistent kernel follow the six-kernel driver."""
+    tr = {}
+    for pers in (0, 1):
+        s, _, _ = _solver(cuda_lib, "supersonic", precision="mixed", krylov=1, persistent=pers)
+        s.setNumericalMethod("HLLC", "FIRST_ORDER")
+        tr[pers] = s.solveImplicit(0.0, 15)
+    np.testing.assert_allclose(tr[1]["res_vm"], tr[0]["res_vm"], rtol=1e-4)
