@@ -110,14 +110,16 @@ def krylov_bytes(stage: str, nc: int, nf: int, nv: int, s: int, jbar: float) -> 
     L = nv * nc
     nb = jbar + 1.0
     if stage == "prim_z":
-        return nc * (nv * s + s + nv * s + nv * s + 2 * (7 if nv == 6 else 5) * s)
+        # deferred V_j = w - V h2 (w and j basis vectors in, V_j out; none at j = 0), then
+        # z = V_j / D and the dual primitives
+        return nc * (nv * s + s + nv * s + nv * s + 2 * (7 if nv == 6 else 5) * s) + L * s * (jbar + 2)
     if stage in ("grad", "flux"):
         return algorithmic_bytes(stage, nc, nf, nv, s, "SECOND_ORDER_CENTRAL", True, True)
     if stage == "gather_dot":
         return nc * 16 + nf * nv * s + nc * (nv * s + 2 * s + nv * s) + nb * L * s
     if stage == "update_dot":
         return L * s * (2 + nb)
-    if stage == "update_final":
+    if stage == "update_final":  # FD J v body only
         return L * s * (2 + nb)
     raise ValueError(stage)
 
@@ -414,7 +416,7 @@ def ours(args):
     # ---- CPU baseline: the oracle port on this host, bounded sample
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
-        cpu = cpu_baseline_sample(args.cpu_seconds)
+        cpu = cpu_baseline_sample(args.cpu_steps)
 
     if rank == 0:
         line = {
@@ -507,12 +509,13 @@ def cpu_kind():
     return "reference" if ref_available("plate_visc") else "port"
 
 
-def cpu_baseline_sample(seconds: float):
+def cpu_baseline_sample(steps: int):
+    """The first `steps` Newton steps of the workload on one host core (the GMRES
+    iterations per step grow along the solve: 150 steps are about 2,400 evaluations,
+    15-35 s of FP64 FD work on one core)."""
     from oracle.oracle import build_oracle
     build_oracle()
     kind = cpu_kind()
-    e1, t1, _ = _cpu_worker((0, 2, kind))
-    steps = max(2, int(seconds / max(t1 / 2, 1e-3)))
     evals, t, n = _cpu_worker((0, steps, kind))
     nc = WORKLOAD["n_cells"]
     return {"value": evals * nc / t, "unit": UNIT, "cores": 1, "kind": kind,
@@ -674,7 +677,7 @@ def main():
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--no-cpu-baseline", action="store_true")
-    ap.add_argument("--cpu-seconds", type=float, default=15.0)
+    ap.add_argument("--cpu-steps", type=int, default=150)
     ap.add_argument("--no-t2c", action="store_true", help="skip the time-to-1e-10 solves")
     ap.add_argument("--sweep", action="store_true", help="bandwidth sweep on the bump channel instead")
     ap.add_argument("--sweep-sizes", default="", help="comma-separated target cell counts")

@@ -96,8 +96,8 @@ typedef struct cfdg_config {
 } cfdg_config;
 
 /* CFDG_KRYLOV_STREAM launches the graph driver's kernels one iteration at a time from a
- * host loop (same arithmetic, one sync per iteration; with timing on every kernel is
- * timed: stat classes 12-17) */
+ * host loop (same arithmetic, one sync per iteration; with timing on every kernel of the
+ * exact J v body is timed: stat classes 12-16) */
 enum { CFDG_KRYLOV_AUTO = -1, CFDG_KRYLOV_HOST = 0, CFDG_KRYLOV_GRAPH = 1, CFDG_KRYLOV_STREAM = 2 };
 
 /* per-step record of a Newton solve (the reference prints these, src/Solver.cpp:1725-1727, :1746) */
@@ -256,9 +256,10 @@ cfdg_status cfdg_set_timing(cfdg_solver* s, int on);
 cfdg_status cfdg_kernel_times(cfdg_solver* s, double* ms_prim, double* ms_grad, double* ms_flux, double* ms_gather);
 /* accumulated per-kernel time and launch count since the last reset (18 classes): 0-3 the
  * residual's prim, grad, flux, gather kernels, 4-7 the same kernels of the exact J v,
- * 8-11 the VJP's forward recomputation, face adjoint and its two cell gathers, 12-17 the
- * stream-driven Krylov body: z + primitives, gradients (+ SST), fluxes, gather + first
- * CGS pass, update + second pass, final update + Givens */
+ * 8-11 the VJP's forward recomputation, face adjoint and its two cell gathers, 12-16 the
+ * stream-driven exact J v Krylov body: deferred basis update + z + primitives, gradients
+ * (+ SST), fluxes, gather + first CGS pass, update + second pass + norm + Givens; 17 is
+ * reserved (the FD body's final update, not timed) */
 cfdg_status cfdg_kernel_stats(cfdg_solver* s, double* ms18, long long* n18, int reset);
 /* VJP at the device-resident state with the device residual as lambda (timing path) */
 cfdg_status cfdg_vjp_device(cfdg_solver* s);

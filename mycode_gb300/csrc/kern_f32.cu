@@ -92,9 +92,9 @@ void launch_gmres_multidot<float>(long L, const float* w, const float* V, const 
     k_gmres_multidot<float><<<kry_grid(L), RED_THREADS, 0, s>>>(L, w, V, d, h);
 }
 template <>
-void launch_gmres_prim_z<float>(int nv, long nc, const Flow<float>& F, const float* U, const float* V, long L, const float* Dinv,
-                             float* z, Field<float> W, const GmresDev& d, cudaStream_t s) {
-    NV_SWITCH(nv, (k_gmres_prim_z<float, NVC><<<blocks_for(nc), tpb_for(nc), 0, s>>>((int)nc, F, U, V, L, Dinv, z, W, d)));
+void launch_gmres_prim_z<float>(int nv, long nc, const Flow<float>& F, const float* U, float* V, long L, const float* Dinv,
+                             float* z, Field<float> W, const float* w, const GmresDev& d, cudaStream_t s) {
+    NV_SWITCH(nv, (k_gmres_prim_z<float, NVC><<<blocks_for(nc), tpb_for(nc), 0, s>>>((int)nc, F, U, V, L, Dinv, z, W, w, d)));
 }
 template <>
 void launch_gmres_gather_dot<float>(int nv, const MeshView<float>& m, const float* FA, float* w, const float* z, const float* dt,
@@ -104,7 +104,12 @@ void launch_gmres_gather_dot<float>(int nv, const MeshView<float>& m, const floa
 }
 template <>
 void launch_gmres_update_dot<float>(long L, float* w, const float* V, const GmresDev& d, cudaStream_t s) {
-    k_gmres_update_dot<float><<<kry_grid(L), RED_THREADS, 0, s>>>(L, w, V, d);
+    k_gmres_update_dot<float, false><<<kry_grid(L), RED_THREADS, 0, s>>>(L, w, V, d, 0);
+}
+template <>
+void launch_gmres_update_dot_last<float>(long L, float* w, const float* V, const GmresDev& d, cudaGraphConditionalHandle h,
+                                   cudaStream_t s) {
+    k_gmres_update_dot<float, true><<<kry_grid(L), RED_THREADS, 0, s>>>(L, w, V, d, h);
 }
 template <>
 void launch_gmres_update_final<float>(long L, const float* w, float* V, const GmresDev& d, cudaGraphConditionalHandle h,

@@ -134,9 +134,9 @@ void launch_gmres_multidot<double>(long L, const double* w, const double* V, con
     k_gmres_multidot<double><<<kry_grid(L), RED_THREADS, 0, s>>>(L, w, V, d, h);
 }
 template <>
-void launch_gmres_prim_z<double>(int nv, long nc, const Flow<double>& F, const double* U, const double* V, long L, const double* Dinv,
-                             double* z, Field<double> W, const GmresDev& d, cudaStream_t s) {
-    NV_SWITCH(nv, (k_gmres_prim_z<double, NVC><<<blocks_for(nc), tpb_for(nc), 0, s>>>((int)nc, F, U, V, L, Dinv, z, W, d)));
+void launch_gmres_prim_z<double>(int nv, long nc, const Flow<double>& F, const double* U, double* V, long L, const double* Dinv,
+                             double* z, Field<double> W, const double* w, const GmresDev& d, cudaStream_t s) {
+    NV_SWITCH(nv, (k_gmres_prim_z<double, NVC><<<blocks_for(nc), tpb_for(nc), 0, s>>>((int)nc, F, U, V, L, Dinv, z, W, w, d)));
 }
 template <>
 void launch_gmres_gather_dot<double>(int nv, const MeshView<double>& m, const double* FA, double* w, const double* z, const double* dt,
@@ -146,7 +146,12 @@ void launch_gmres_gather_dot<double>(int nv, const MeshView<double>& m, const do
 }
 template <>
 void launch_gmres_update_dot<double>(long L, double* w, const double* V, const GmresDev& d, cudaStream_t s) {
-    k_gmres_update_dot<double><<<kry_grid(L), RED_THREADS, 0, s>>>(L, w, V, d);
+    k_gmres_update_dot<double, false><<<kry_grid(L), RED_THREADS, 0, s>>>(L, w, V, d, 0);
+}
+template <>
+void launch_gmres_update_dot_last<double>(long L, double* w, const double* V, const GmresDev& d, cudaGraphConditionalHandle h,
+                                   cudaStream_t s) {
+    k_gmres_update_dot<double, true><<<kry_grid(L), RED_THREADS, 0, s>>>(L, w, V, d, h);
 }
 template <>
 void launch_gmres_update_final<double>(long L, const double* w, double* V, const GmresDev& d, cudaGraphConditionalHandle h,

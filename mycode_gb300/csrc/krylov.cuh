@@ -3,10 +3,19 @@
 // device, so a whole Krylov solve is one graph launch with no host round trip.
 //
 // Orthogonalisation is classical Gram-Schmidt applied twice (CGS2).  Each pass's dot
-// products are fused into the kernel that produces the vector they read:
-//   J v gather   -> w and h1 = V^T w                       (k_gmres_gather_dot)
-//   w -= V h1    -> w and h2 = V^T w                       (k_gmres_update_dot)
-//   w -= V h2    -> V_{j+1}, |w|, and the Givens step      (k_gmres_update_final)
+// products are fused into the kernel that produces the vector they read.  With the exact
+// (dual-number) J v an iteration is five kernels and two grid reductions:
+//   V_j = w - V h2 (deferred), z = V_j / D, dual primitives    (k_gmres_prim_z)
+//   dual gradients, dual face fluxes                           (k_grad, k_flux)
+//   J v gather   -> w and h1 = V^T w                           (k_gmres_gather_dot)
+//   w -= V h1    -> w, h2 = V^T w and |w|^2; Givens step        (k_gmres_update_dot<T, true>)
+// The norm of V_{j+1} = w - V h2 is taken as |w|^2 - |h2|^2 (Pythagoras over the
+// orthonormal basis, as in the one-reduction CGS2 variants of Swirydowicz, Langou,
+// Ananthan, Yang and Thomas, "Low synchronization Gram-Schmidt and GMRES algorithms",
+// Numer. Linear Algebra Appl. 2021), so V_{j+1} itself is formed by the next iteration's
+// first kernel and never needs a reduction of its own.  The FD J v path keeps the
+// explicit final pass:
+//   w -= V h2    -> V_{j+1}, |V_{j+1}|, and the Givens step  (k_gmres_update_final)
 // Every thread reads back only the elements it wrote itself, so no grid barrier is
 // needed inside a kernel; the last block to finish each kernel sums the block partials
 // in block order (deterministic).  Basis vectors are stored unnormalised with a scale
@@ -96,8 +105,10 @@ __device__ __forceinline__ void tile_to_smem(const A (&v)[KRY_TILE], int i0, int
 }
 
 // Block partials of h[0..j] from wsum, then in the last block to finish the sums over the
-// blocks in block order: h[i] = sc[i] * sum.  Returns true in the last block.
-__device__ __forceinline__ bool dots_finish(const GmresDev& d, int j, double (*wsum)[KRY_WARPS], double* h) {
+// blocks in block order: h[i] = sc[i] * sum (h[jraw] = sum, unscaled).  Returns true in
+// the last block.
+__device__ __forceinline__ bool dots_finish(const GmresDev& d, int j, double (*wsum)[KRY_WARPS], double* h,
+                                            int jraw = -1) {
     __syncthreads();
     const int nwarp = blockDim.x >> 5;
     for (int i = threadIdx.x; i <= j; i += blockDim.x) {
@@ -118,7 +129,7 @@ __device__ __forceinline__ bool dots_finish(const GmresDev& d, int j, double (*w
 #pragma unroll 4
         for (int b = lane; b < (int)gridDim.x; b += 32) sg += __ldcg(d.partial + (long)i * RED_BLOCKS + b);
         sg = warp_sum(sg);
-        if (lane == 0) h[i] = d.sc[i] * sg;
+        if (lane == 0) h[i] = (i == jraw ? 1.0 : d.sc[i]) * sg;
     }
     __syncthreads();
     if (threadIdx.x == 0) *d.counter = 0u;
@@ -162,21 +173,50 @@ __global__ void k_gmres_z(long nc, const T* V, long L, const T* __restrict__ Din
     }
 }
 
+// For j > 0 first the deferred end of the previous iteration's orthogonalisation,
+// V_j = w - sum_{i<j} h2[i] sc[i] V_i (stored unnormalised; sc[j] is already set), then
 // z = V_j * (1/D) fused with the primitive stage of the dual J v: W.v, W.d of (U, z)
 template <class T, int NV>
-__global__ void __launch_bounds__(256) k_gmres_prim_z(int nc, Flow<T> F, const T* __restrict__ U, const T* V, long L,
+__global__ void __launch_bounds__(256) k_gmres_prim_z(int nc, Flow<T> F, const T* __restrict__ U, T* V, long L,
                                                       const T* __restrict__ Dinv, T* __restrict__ z, Field<T> W,
-                                                      GmresDev d) {
+                                                      const T* __restrict__ w, GmresDev d) {
+    typedef typename KryAcc<T>::type A;
+    const int j = d.gi[0];
+    __shared__ A hs[KRY_MAXM];
+    if (j > 0) {
+        for (int k = threadIdx.x; k < j; k += blockDim.x) hs[k] = (A)(d.h2[k] * d.sc[k]);
+        __syncthreads();
+    }
     long i = (long)blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= nc) return;
-    const int j = d.gi[0];
-    const T* Vj = V + (long)j * L;
+    T* Vj = V + (long)j * L;
     const T sj = (T)d.sc[j];
     const T a = Dinv[i];
+    T vj[NV];
+    if (j > 0) {
+        A acc[NV];
+#pragma unroll
+        for (int c = 0; c < NV; ++c) acc[c] = (A)w[c * nc + i];
+#pragma unroll 2
+        for (int k = 0; k < j; ++k) {
+            const T* Vk = V + (long)k * L;
+            const A hk = hs[k];
+#pragma unroll
+            for (int c = 0; c < NV; ++c) acc[c] -= hk * (A)Vk[c * nc + i];
+        }
+#pragma unroll
+        for (int c = 0; c < NV; ++c) {
+            vj[c] = (T)acc[c];
+            Vj[c * nc + i] = vj[c];
+        }
+    } else {
+#pragma unroll
+        for (int c = 0; c < NV; ++c) vj[c] = Vj[c * nc + i];
+    }
     Dual<T> u[6];
 #pragma unroll
     for (int c = 0; c < NV; ++c) {
-        T zc = Vj[c * nc + i] * sj * dinv_of<T, NV>(Dinv, nc, i, c, a);
+        T zc = vj[c] * sj * dinv_of<T, NV>(Dinv, nc, i, c, a);
         z[c * nc + i] = zc;
         u[c] = Dual<T>(U[c * nc + i], zc);
     }
@@ -272,20 +312,33 @@ __global__ void __launch_bounds__(RED_THREADS) k_gmres_gather_dot(MeshView<T> m,
     dots_finish(d, j, wsum, d.h1);
 }
 
-// w -= sum_{i<=j} h1[i] sc[i] V_i, fused with the second CGS pass h2 = V^T w
-template <class T>
+__device__ __forceinline__ void givens_step(const GmresDev& d, cudaGraphConditionalHandle hnd, double hsq);
+
+// w -= sum_{i<=j} h1[i] sc[i] V_i, fused with the second CGS pass h2 = V^T w.  With LAST
+// (the exact J v body) also |w|^2, and the last block takes |V_{j+1}|^2 = |w|^2 - |h2|^2
+// (clamped at 0), sets sc[j+1] = 1/|V_{j+1}| (1 under the breakdown guard |.| <= 1e-12 of
+// src/Solver.cpp:1553-1558) and runs the Givens step; V_{j+1} = w - V h2 is formed by the
+// next iteration's k_gmres_prim_z.
+template <class T, bool LAST>
 __global__ void __launch_bounds__(RED_THREADS) k_gmres_update_dot(long L, T* __restrict__ w, const T* __restrict__ V,
-                                                                  GmresDev d) {
+                                                                  GmresDev d, cudaGraphConditionalHandle hnd) {
     typedef typename KryAcc<T>::type A;
     const int j = d.gi[0];
     __shared__ A hs[KRY_MAXM + 1];
     __shared__ double wsum[KRY_MAXM + 1][KRY_WARPS];
     for (int i = threadIdx.x; i <= j; i += blockDim.x) hs[i] = (A)(d.h1[i] * d.sc[i]);
     __syncthreads();
+    A nw = A(0);
     for (long q = (long)blockIdx.x * blockDim.x + threadIdx.x; q < L; q += (long)gridDim.x * blockDim.x) {
         A a = (A)w[q];
         for (int i = 0; i <= j; ++i) a -= hs[i] * (A)V[(long)i * L + q];
-        w[q] = (T)a;
+        T t = (T)a;
+        w[q] = t;
+        if (LAST) nw += (A)t * (A)t;
+    }
+    if (LAST) {
+        nw = warp_sum_t(nw);
+        if ((threadIdx.x & 31) == 0) wsum[j + 1][threadIdx.x >> 5] = (double)nw;
     }
     for (int i0 = 0; i0 <= j; i0 += KRY_TILE) {
         const int nt = (j + 1 - i0) < KRY_TILE ? (j + 1 - i0) : KRY_TILE;
@@ -300,7 +353,26 @@ __global__ void __launch_bounds__(RED_THREADS) k_gmres_update_dot(long L, T* __r
         }
         tile_to_smem(v, i0, nt, wsum);
     }
-    dots_finish(d, j, wsum, d.h2);
+    if (!LAST) {
+        dots_finish(d, j, wsum, d.h2);
+        return;
+    }
+    if (!dots_finish(d, j + 1, wsum, d.h2, j + 1)) return;
+    if (threadIdx.x >= 32) return;
+    const int lane = threadIdx.x;
+    double s2 = 0.0;
+    for (int i = lane; i <= j; i += 32) {
+        double h = d.h2[i];
+        s2 += h * h;
+    }
+    s2 = __shfl_sync(0xffffffffu, warp_sum(s2), 0);
+    const double hsq = fmax(d.h2[j + 1] - s2, 0.0);
+    if (lane == 0) {
+        d.hsq[1] = hsq;
+        double hv = sqrt(hsq);
+        d.sc[j + 1] = hv > 1e-12 ? 1.0 / hv : 1.0;
+    }
+    givens_step(d, hnd, hsq);
 }
 
 // Hessenberg column, Givens rotations and the convergence test (src/Solver.cpp:1550-1588);

@@ -581,7 +581,6 @@ struct cfdg_solver {
         const bool mixed = cfg.precision == CFDG_MIXED;
         // the exact (dual-number) J v runs fused with the Arnoldi kernels: z with the
         // primitives, the gather with the first CGS pass; the FD J v keeps its own kernels.
-        // ev (stream driver with timing): 7 events around the 6 stages, stat classes 12-17
         if (use_persistent() && capturing) {
             if (!ablocks) ablocks = mixed ? arnoldi_blocks<float>(nv) : arnoldi_blocks<double>(nv);
             cudaError_t e;
@@ -599,10 +598,11 @@ struct cfdg_solver {
             ++launches;
             return CFDG_OK;
         }
-        cudaEvent_t* ev = (mixed || cfg.jv == CFDG_JV_EXACT) ? take_events(12, 6) : nullptr;
+        // ev (stream driver with timing): 6 events around the 5 stages, stat classes 12-16
+        cudaEvent_t* ev = (mixed || cfg.jv == CFDG_JV_EXACT) ? take_events(12, 5) : nullptr;
         if (ev) CK(cudaEventRecord(ev[0], st));
         if (mixed) {
-            launch_gmres_prim_z<float>(nv, nc, Ff, U32, V32, L, dinv32, z32, f32(W32, W32d), gd, st);
+            launch_gmres_prim_z<float>(nv, nc, Ff, U32, V32, L, dinv32, z32, f32(W32, W32d), w32, gd, st);
             ResArgs<float> a;
             a.m = mvf;
             a.F = Ff;
@@ -620,13 +620,11 @@ struct cfdg_solver {
             launch_gmres_gather_dot<float>(nv, mvf, FA32d, w32, z32, dt32, nv == 6 ? T32d + 2 * nc : nullptr, V32, L, gd,
                                            st);
             if (ev) CK(cudaEventRecord(ev[4], st));
-            launch_gmres_update_dot<float>(L, w32, V32, gd, st);
+            launch_gmres_update_dot_last<float>(L, w32, V32, gd, h, st);
             if (ev) CK(cudaEventRecord(ev[5], st));
-            launch_gmres_update_final<float>(L, w32, V32, gd, h, st);
-            if (ev) CK(cudaEventRecord(ev[6], st));
-            launches += nv == 6 ? 7 : 6;
+            launches += nv == 6 ? 6 : 5;
         } else if (cfg.jv == CFDG_JV_EXACT) {
-            launch_gmres_prim_z<double>(nv, nc, F, Ubase, V, L, dinv64, z, f64(Wj, Wjd), gd, st);
+            launch_gmres_prim_z<double>(nv, nc, F, Ubase, V, L, dinv64, z, f64(Wj, Wjd), w64, gd, st);
             ResArgs<double> a;
             a.m = mv;
             a.F = F;
@@ -643,11 +641,9 @@ struct cfdg_solver {
             launch_jv_mid<double>(a);
             launch_gmres_gather_dot<double>(nv, mv, FAjd, w64, z, dt, nv == 6 ? Tjd + 2 * nc : nullptr, V, L, gd, st);
             if (ev) CK(cudaEventRecord(ev[4], st));
-            launch_gmres_update_dot<double>(L, w64, V, gd, st);
+            launch_gmres_update_dot_last<double>(L, w64, V, gd, h, st);
             if (ev) CK(cudaEventRecord(ev[5], st));
-            launch_gmres_update_final<double>(L, w64, V, gd, h, st);
-            if (ev) CK(cudaEventRecord(ev[6], st));
-            launches += nv == 6 ? 7 : 6;
+            launches += nv == 6 ? 6 : 5;
         } else {
             launch_gmres_z<double>(nv, nc, V, L, dinv64, z, gd, st);
             ++launches;
