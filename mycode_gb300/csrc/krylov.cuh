@@ -92,44 +92,91 @@ __device__ __forceinline__ A warp_sum_t(A v) {
 constexpr int KRY_TILE = 16;  // basis vectors per pass over a thread's elements
 constexpr int KRY_WARPS = RED_THREADS / 32;  // most warps of a block (blocks of 64-256 threads)
 
-// per-warp sums of one tile of per-thread partial dots into wsum[vector][warp]
+// per-warp sums of one tile of per-thread partial dots into wsum[vector][warp]: a
+// butterfly reduce-scatter (each exchange step halves the values a lane holds: 8, 4, 2
+// and 1 shuffles, then one more), 16 shuffles for the 16 dots instead of 5 per dot; lane
+// l ends with dot 8 b4 + 4 b3 + 2 b2 + b1 (bk: bit k of l), summed over the warp
 template <class A>
 __device__ __forceinline__ void tile_to_smem(const A (&v)[KRY_TILE], int i0, int nt, double (*wsum)[KRY_WARPS]) {
+    static_assert(KRY_TILE == 16, "the butterfly is written for 16 values per lane");
+    const unsigned full = 0xffffffffu;
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    A x[8], y[4], z[2];
+    bool hi = lane & 16;
 #pragma unroll
-    for (int t = 0; t < KRY_TILE; ++t)
-        if (t < nt) {
-            A s = warp_sum_t(v[t]);
-            if (lane == 0) wsum[i0 + t][warp] = (double)s;
-        }
+    for (int k = 0; k < 8; ++k) x[k] = (hi ? v[k + 8] : v[k]) + __shfl_xor_sync(full, hi ? v[k] : v[k + 8], 16);
+    hi = lane & 8;
+#pragma unroll
+    for (int k = 0; k < 4; ++k) y[k] = (hi ? x[k + 4] : x[k]) + __shfl_xor_sync(full, hi ? x[k] : x[k + 4], 8);
+    hi = lane & 4;
+#pragma unroll
+    for (int k = 0; k < 2; ++k) z[k] = (hi ? y[k + 2] : y[k]) + __shfl_xor_sync(full, hi ? y[k] : y[k + 2], 4);
+    hi = lane & 2;
+    A u = (hi ? z[1] : z[0]) + __shfl_xor_sync(full, hi ? z[0] : z[1], 2);
+    u += __shfl_xor_sync(full, u, 1);
+    const int d = ((lane >> 4) & 1) * 8 + ((lane >> 3) & 1) * 4 + ((lane >> 2) & 1) * 2 + ((lane >> 1) & 1);
+    if ((lane & 1) == 0 && d < nt) wsum[i0 + d][warp] = (double)u;
+}
+
+constexpr int KRY_RC = 2 * KRY_TILE;  // basis vectors held in registers by the one-pass kernels
+
+// Sum of n <= 8 doubles as a balanced tree: GB300 runs a dependent FP64 add in about 40
+// cycles, so the depth of the tree, not the count, sets the latency.
+__device__ __forceinline__ double tree8(const double (&x)[8]) {
+    return ((x[0] + x[1]) + (x[2] + x[3])) + ((x[4] + x[5]) + (x[6] + x[7]));
 }
 
 // Block partials of h[0..j] from wsum, then in the last block to finish the sums over the
-// blocks in block order: h[i] = sc[i] * sum (h[jraw] = sum, unscaled).  Returns true in
-// the last block.
+// blocks: h[i] = sc[i] * sum (h[jraw] = sum, unscaled), also into hsm when given.  The
+// last block gives each dot an aligned group of G lanes (G the largest power of two up
+// to 32 with G (j+1) <= blockDim.x): each lane loads its strided share of the blocks
+// eight at a time and sums them as trees, the group then reduces by shuffles, so every
+// dot's loads are in flight at once and the order is fixed (deterministic).  One thread
+// per block fences and takes the ticket after the block barrier (the fence is
+// cumulative over the writes the barrier ordered before it).  scs: sc staged in shared
+// memory (or null: read d.sc).  Returns true in the last block.  Needs j + 1 <=
+// blockDim.x, a multiple of 32, and blockDim.x <= RED_THREADS.
 __device__ __forceinline__ bool dots_finish(const GmresDev& d, int j, double (*wsum)[KRY_WARPS], double* h,
-                                            int jraw = -1) {
+                                            int jraw = -1, const double* scs = nullptr, double* hsm = nullptr) {
     __syncthreads();
     const int nwarp = blockDim.x >> 5;
     for (int i = threadIdx.x; i <= j; i += blockDim.x) {
-        double sb = 0.0;
-        for (int w = 0; w < nwarp; ++w) sb += wsum[i][w];
-        d.partial[(long)i * RED_BLOCKS + blockIdx.x] = sb;
+        double x[8];
+#pragma unroll
+        for (int w = 0; w < 8; ++w) x[w] = w < nwarp ? wsum[i][w] : 0.0;
+        d.partial[(long)i * RED_BLOCKS + blockIdx.x] = tree8(x);
     }
-    __threadfence();
     __syncthreads();
     __shared__ bool last;
-    if (threadIdx.x == 0) last = atomicAdd(d.counter, 1u) == gridDim.x - 1;
+    if (threadIdx.x == 0) {
+        __threadfence();
+        last = atomicAdd(d.counter, 1u) == gridDim.x - 1;
+        if (last) __threadfence();
+    }
     __syncthreads();
     if (!last) return false;
-    __threadfence();
-    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    for (int i = warp; i <= j; i += nwarp) {
-        double sg = 0.0;
-#pragma unroll 4
-        for (int b = lane; b < (int)gridDim.x; b += 32) sg += __ldcg(d.partial + (long)i * RED_BLOCKS + b);
-        sg = warp_sum(sg);
-        if (lane == 0) h[i] = (i == jraw ? 1.0 : d.sc[i]) * sg;
+    const int nd = j + 1, nb = (int)gridDim.x;
+    int G = 32;  // lanes per dot: aligned groups within a warp
+    while (G > 1 && G * nd > (int)blockDim.x) G >>= 1;
+    const int i = threadIdx.x / G, g = threadIdx.x % G;
+    double sg = 0.0;
+    if (i < nd) {
+        const double* p = d.partial + (long)i * RED_BLOCKS;
+        for (int b0 = g; b0 < nb; b0 += 8 * G) {
+            double x[8];
+#pragma unroll
+            for (int k = 0; k < 8; ++k) {
+                const int b = b0 + k * G;
+                x[k] = b < nb ? __ldcg(p + b) : 0.0;
+            }
+            sg += tree8(x);
+        }
+    }
+    for (int o = G >> 1; o > 0; o >>= 1) sg += __shfl_xor_sync(0xffffffffu, sg, o);
+    if (i < nd && g == 0) {
+        const double hv = (i == jraw ? 1.0 : (scs ? scs[i] : d.sc[i])) * sg;
+        h[i] = hv;
+        if (hsm) hsm[i] = hv;
     }
     __syncthreads();
     if (threadIdx.x == 0) *d.counter = 0u;
@@ -260,65 +307,96 @@ __global__ void __launch_bounds__(RED_THREADS) k_gmres_gather_dot(MeshView<T> m,
     const int j = d.gi[0];
     const long nc = m.nc;
     __shared__ double wsum[KRY_MAXM + 1][KRY_WARPS];
-    for (int i0 = 0; i0 <= j; i0 += KRY_TILE) {
-        const int nt = (j + 1 - i0) < KRY_TILE ? (j + 1 - i0) : KRY_TILE;
-        A v[KRY_TILE];
+    __shared__ double scs[KRY_MAXM + 1];
+    for (int i = threadIdx.x; i <= j; i += blockDim.x) scs[i] = d.sc[i];
+    // w = the gathered J v of cell i (reference face order)
+    auto gather = [&](long i, T (&acc)[NV]) {
 #pragma unroll
-        for (int t = 0; t < KRY_TILE; ++t) v[t] = A(0);
-        for (long i = (long)blockIdx.x * blockDim.x + threadIdx.x; i < nc; i += (long)gridDim.x * blockDim.x) {
-            T acc[NV];
-            if (i0 == 0) {
+        for (int c = 0; c < NV; ++c) acc[c] = T(0);
+        int ek[4];
 #pragma unroll
-                for (int c = 0; c < NV; ++c) acc[c] = T(0);
+        for (int k = 0; k < 4; ++k) ek[k] = m.cf[(long)k * nc + i];
 #pragma unroll
-                for (int k = 0; k < 4; ++k) {
-                    int e = m.cf[(long)k * nc + i];
-                    if (e < 0) break;
-                    long f = e >> 1;
-                    if (e & 1) {
+        for (int k = 0; k < 4; ++k) {
+            const int e = ek[k];
+            if (e < 0) continue;  // pads only at the end of a cell's list
+            long f = e >> 1;
+            if (e & 1) {
 #pragma unroll
-                        for (int c = 0; c < NV; ++c) acc[c] = acc[c] - FA[c * fa_stride + f];
-                    } else {
-#pragma unroll
-                        for (int c = 0; c < NV; ++c) acc[c] = acc[c] + FA[c * fa_stride + f];
-                    }
-                }
-                if constexpr (NV == 6) {
-                    acc[4] = acc[4] - src[i];
-                    acc[5] = acc[5] - src[nc + i];
-                }
-                T tc = m.vol[i] / (dt[i] + T(1e-30));
-#pragma unroll
-                for (int c = 0; c < NV; ++c) {
-                    acc[c] = acc[c] + z[c * nc + i] * tc;
-                    w[c * nc + i] = acc[c];
-                }
+                for (int c = 0; c < NV; ++c) acc[c] = acc[c] - FA[c * fa_stride + f];
             } else {
 #pragma unroll
-                for (int c = 0; c < NV; ++c) acc[c] = w[c * nc + i];
+                for (int c = 0; c < NV; ++c) acc[c] = acc[c] + FA[c * fa_stride + f];
             }
+        }
+        if constexpr (NV == 6) {
+            acc[4] = acc[4] - src[i];
+            acc[5] = acc[5] - src[nc + i];
+        }
+        T tc = m.vol[i] / (dt[i] + T(1e-30));
 #pragma unroll
-            for (int t = 0; t < KRY_TILE; ++t)
-                if (t < nt) {
-                    const T* Vi = V + (long)(i0 + t) * L;
+        for (int c = 0; c < NV; ++c) {
+            acc[c] = acc[c] + z[c * nc + i] * tc;
+            w[c * nc + i] = acc[c];
+        }
+    };
+    if (j < KRY_RC) {
+        // one pass over the cells: up to 32 dots accumulated in two register tiles
+        A v0[KRY_TILE], v1[KRY_TILE];
+#pragma unroll
+        for (int t = 0; t < KRY_TILE; ++t) v0[t] = v1[t] = A(0);
+        for (long i = (long)blockIdx.x * blockDim.x + threadIdx.x; i < nc; i += (long)gridDim.x * blockDim.x) {
+            T acc[NV];
+            gather(i, acc);
+#pragma unroll
+            for (int t = 0; t < KRY_RC; ++t)
+                if (t <= j) {
+                    const T* Vi = V + (long)t * L;
                     A s = A(0);
 #pragma unroll
                     for (int c = 0; c < NV; ++c) s += (A)acc[c] * (A)Vi[c * nc + i];
-                    v[t] += s;
+                    if (t < KRY_TILE) v0[t] += s;
+                    else v1[t - KRY_TILE] += s;
                 }
         }
-        tile_to_smem(v, i0, nt, wsum);
+        tile_to_smem(v0, 0, j + 1 < KRY_TILE ? j + 1 : KRY_TILE, wsum);
+        if (j >= KRY_TILE) tile_to_smem(v1, KRY_TILE, j + 1 - KRY_TILE, wsum);
+    } else {
+        for (int i0 = 0; i0 <= j; i0 += KRY_TILE) {
+            const int nt = (j + 1 - i0) < KRY_TILE ? (j + 1 - i0) : KRY_TILE;
+            A v[KRY_TILE];
+#pragma unroll
+            for (int t = 0; t < KRY_TILE; ++t) v[t] = A(0);
+            for (long i = (long)blockIdx.x * blockDim.x + threadIdx.x; i < nc; i += (long)gridDim.x * blockDim.x) {
+                T acc[NV];
+                if (i0 == 0) {
+                    gather(i, acc);
+                } else {
+#pragma unroll
+                    for (int c = 0; c < NV; ++c) acc[c] = w[c * nc + i];
+                }
+#pragma unroll
+                for (int t = 0; t < KRY_TILE; ++t)
+                    if (t < nt) {
+                        const T* Vi = V + (long)(i0 + t) * L;
+                        A s = A(0);
+#pragma unroll
+                        for (int c = 0; c < NV; ++c) s += (A)acc[c] * (A)Vi[c * nc + i];
+                        v[t] += s;
+                    }
+            }
+            tile_to_smem(v, i0, nt, wsum);
+        }
     }
-    dots_finish(d, j, wsum, d.h1);
+    dots_finish(d, j, wsum, d.h1, -1, scs);
 }
-
-__device__ __forceinline__ void givens_step(const GmresDev& d, cudaGraphConditionalHandle hnd, double hsq);
 
 // w -= sum_{i<=j} h1[i] sc[i] V_i, fused with the second CGS pass h2 = V^T w.  With LAST
 // (the exact J v body) also |w|^2, and the last block takes |V_{j+1}|^2 = |w|^2 - |h2|^2
 // (clamped at 0), sets sc[j+1] = 1/|V_{j+1}| (1 under the breakdown guard |.| <= 1e-12 of
 // src/Solver.cpp:1553-1558) and runs the Givens step; V_{j+1} = w - V h2 is formed by the
-// next iteration's k_gmres_prim_z.
+// next iteration's k_gmres_prim_z.  Every block stages h1, sc and the previous rotations
+// in shared memory up front, so the last block's serial tail reads no global memory.
 template <class T, bool LAST>
 __global__ void __launch_bounds__(RED_THREADS) k_gmres_update_dot(long L, T* __restrict__ w, const T* __restrict__ V,
                                                                   GmresDev d, cudaGraphConditionalHandle hnd) {
@@ -326,53 +404,138 @@ __global__ void __launch_bounds__(RED_THREADS) k_gmres_update_dot(long L, T* __r
     const int j = d.gi[0];
     __shared__ A hs[KRY_MAXM + 1];
     __shared__ double wsum[KRY_MAXM + 1][KRY_WARPS];
-    for (int i = threadIdx.x; i <= j; i += blockDim.x) hs[i] = (A)(d.h1[i] * d.sc[i]);
+    __shared__ double scs[KRY_MAXM + 1], col[KRY_MAXM + 2], h2s[KRY_MAXM + 2], css[KRY_MAXM], sns[KRY_MAXM];
+    __shared__ double hout[KRY_MAXM + 2];
+    __shared__ double gj, tolb;
+    __shared__ int mm;
+    for (int i = threadIdx.x; i <= j; i += blockDim.x) {
+        const double h1 = d.h1[i], sc = d.sc[i];
+        hs[i] = (A)(h1 * sc);
+        scs[i] = sc;
+        if (LAST) {
+            col[i] = h1;
+            if (i < j) {
+                css[i] = d.cs[i];
+                sns[i] = d.sn[i];
+            }
+        }
+    }
+    if (LAST && threadIdx.x == 0) {
+        gj = d.g[j];
+        tolb = d.beta[1] * d.beta[0];
+        mm = d.gi[3];
+    }
     __syncthreads();
     A nw = A(0);
-    for (long q = (long)blockIdx.x * blockDim.x + threadIdx.x; q < L; q += (long)gridDim.x * blockDim.x) {
-        A a = (A)w[q];
-        for (int i = 0; i <= j; ++i) a -= hs[i] * (A)V[(long)i * L + q];
-        T t = (T)a;
-        w[q] = t;
-        if (LAST) nw += (A)t * (A)t;
+    if (j < KRY_RC) {
+        // one pass: each element's basis values stay in registers between the update
+        // and the dots
+        A v0[KRY_TILE], v1[KRY_TILE];
+#pragma unroll
+        for (int t = 0; t < KRY_TILE; ++t) v0[t] = v1[t] = A(0);
+        for (long q = (long)blockIdx.x * blockDim.x + threadIdx.x; q < L; q += (long)gridDim.x * blockDim.x) {
+            T vv[KRY_RC];
+#pragma unroll
+            for (int t = 0; t < KRY_RC; ++t) vv[t] = t <= j ? V[(long)t * L + q] : T(0);
+            A a = (A)w[q];
+#pragma unroll
+            for (int t = 0; t < KRY_RC; ++t)
+                if (t <= j) a -= hs[t] * (A)vv[t];
+            const T tq = (T)a;
+            w[q] = tq;
+            if (LAST) nw += (A)tq * (A)tq;
+#pragma unroll
+            for (int t = 0; t < KRY_TILE; ++t) {
+                v0[t] += (A)tq * (A)vv[t];
+                v1[t] += (A)tq * (A)vv[KRY_TILE + t];
+            }
+        }
+        tile_to_smem(v0, 0, j + 1 < KRY_TILE ? j + 1 : KRY_TILE, wsum);
+        if (j >= KRY_TILE) tile_to_smem(v1, KRY_TILE, j + 1 - KRY_TILE, wsum);
+    } else {
+        for (long q = (long)blockIdx.x * blockDim.x + threadIdx.x; q < L; q += (long)gridDim.x * blockDim.x) {
+            A a = (A)w[q];
+            for (int i = 0; i <= j; ++i) a -= hs[i] * (A)V[(long)i * L + q];
+            T t = (T)a;
+            w[q] = t;
+            if (LAST) nw += (A)t * (A)t;
+        }
+        for (int i0 = 0; i0 <= j; i0 += KRY_TILE) {
+            const int nt = (j + 1 - i0) < KRY_TILE ? (j + 1 - i0) : KRY_TILE;
+            A v[KRY_TILE];
+#pragma unroll
+            for (int t = 0; t < KRY_TILE; ++t) v[t] = A(0);
+            for (long q = (long)blockIdx.x * blockDim.x + threadIdx.x; q < L; q += (long)gridDim.x * blockDim.x) {
+                A wq = (A)w[q];
+#pragma unroll
+                for (int t = 0; t < KRY_TILE; ++t)
+                    if (t < nt) v[t] += wq * (A)V[(long)(i0 + t) * L + q];
+            }
+            tile_to_smem(v, i0, nt, wsum);
+        }
     }
     if (LAST) {
         nw = warp_sum_t(nw);
         if ((threadIdx.x & 31) == 0) wsum[j + 1][threadIdx.x >> 5] = (double)nw;
     }
-    for (int i0 = 0; i0 <= j; i0 += KRY_TILE) {
-        const int nt = (j + 1 - i0) < KRY_TILE ? (j + 1 - i0) : KRY_TILE;
-        A v[KRY_TILE];
-#pragma unroll
-        for (int t = 0; t < KRY_TILE; ++t) v[t] = A(0);
-        for (long q = (long)blockIdx.x * blockDim.x + threadIdx.x; q < L; q += (long)gridDim.x * blockDim.x) {
-            A wq = (A)w[q];
-#pragma unroll
-            for (int t = 0; t < KRY_TILE; ++t)
-                if (t < nt) v[t] += wq * (A)V[(long)(i0 + t) * L + q];
-        }
-        tile_to_smem(v, i0, nt, wsum);
-    }
     if (!LAST) {
-        dots_finish(d, j, wsum, d.h2);
+        dots_finish(d, j, wsum, d.h2, -1, scs);
         return;
     }
-    if (!dots_finish(d, j + 1, wsum, d.h2, j + 1)) return;
+    if (!dots_finish(d, j + 1, wsum, d.h2, j + 1, scs, h2s)) return;
     if (threadIdx.x >= 32) return;
+    // The Givens step (src/Solver.cpp:1550-1588) on lane 0 from shared memory, written for
+    // GB300's FP64 latencies (dependent FMA ~40 cycles, divide ~440, square root ~680):
+    // the rotation chain keeps its running entry in a register (one FMA deep per
+    // rotation) and runs interleaved with the sum of squares of h2, and the two
+    // normalisations take one reciprocal square root each instead of a square root and a
+    // divide (c = a / sqrt(a^2 + b^2) as a * rsqrt(a^2 + b^2)).
     const int lane = threadIdx.x;
-    double s2 = 0.0;
-    for (int i = lane; i <= j; i += 32) {
-        double h = d.h2[i];
-        s2 += h * h;
-    }
-    s2 = __shfl_sync(0xffffffffu, warp_sum(s2), 0);
-    const double hsq = fmax(d.h2[j + 1] - s2, 0.0);
+    for (int i = lane; i <= j; i += 32) col[i] += h2s[i];
+    __syncwarp();
     if (lane == 0) {
+        double carry = col[0], s2 = 0.0;
+        for (int i = 0; i < j; ++i) {
+            const double ci = css[i], si = sns[i], nx = col[i + 1], hi = h2s[i];
+            hout[i] = fma(ci, carry, si * nx);
+            carry = fma(-si, carry, ci * nx);
+            s2 = fma(hi, hi, s2);
+        }
+        s2 = fma(h2s[j], h2s[j], s2);
+        const double hsq = fmax(h2s[j + 1] - s2, 0.0);
+        const double r = hsq > 0.0 ? rsqrt(hsq) : 0.0;
+        const double hv = hsq * r;
         d.hsq[1] = hsq;
-        double hv = sqrt(hsq);
-        d.sc[j + 1] = hv > 1e-12 ? 1.0 / hv : 1.0;
+        d.sc[j + 1] = hv > 1e-12 ? r : 1.0;
+        const double a = carry, b = hv;
+        double c, sn;
+        if (fabs(b) < 1e-14) {
+            c = 1.0;
+            sn = 0.0;
+            hout[j] = a;
+        } else {
+            const double q = fma(a, a, b * b), rq = rsqrt(q);
+            c = a * rq;
+            sn = b * rq;
+            hout[j] = q * rq;
+        }
+        hout[j + 1] = 0.0;
+        d.cs[j] = c;
+        d.sn[j] = sn;
+        d.g[j + 1] = -sn * gj;
+        d.g[j] = c * gj;
+        const bool conv = fabs(-sn * gj) < tolb;
+        if (conv || j + 1 >= mm) {
+            d.gi[1] = j;
+            d.gi[2] = 1;
+            if (d.in_graph) cudaGraphSetConditional(hnd, 0);
+        } else {
+            d.gi[0] = j + 1;
+        }
     }
-    givens_step(d, hnd, hsq);
+    __syncwarp();
+    double* Hc = d.H + (long)j * (mm + 1);
+    for (int i = lane; i <= j + 1; i += 32) Hc[i] = hout[i];
 }
 
 // Hessenberg column, Givens rotations and the convergence test (src/Solver.cpp:1550-1588);
