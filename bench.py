@@ -314,6 +314,7 @@ def ours(args):
     clocks = clk.stop()
     launches = s.launch_count() - l0
     stats = s.kernel_stats(reset=True)
+    kinfo = s.krylov_info()
     # Event nodes are not allowed inside the graph's WHILE body, so the Krylov kernels of
     # the timed steps carry no per-kernel events: replay a few steps with the stream driver
     # (the graph's kernels, launched one iteration at a time between events) to time them.
@@ -429,6 +430,7 @@ def ours(args):
             "gmres_iters": [r[1] for r in recs],
             "res_vm": [r[0] for r in recs],
             "gpu_launches": launches,
+            "krylov_driver": kinfo,
             "roofline": roofline,
             "kernels": kern,
             "e2e": e2e,

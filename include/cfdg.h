@@ -89,10 +89,14 @@ typedef struct cfdg_config {
      * CFDG_KRYLOV_AUTO picks GRAPH for mixed precision or exact J v, else HOST. */
     int krylov;
     /* graph driver with exact J v: 1 runs each Arnoldi iteration as one persistent kernel
-     * with grid barriers between its phases, 0 (default) as six kernels; measured on the
-     * 28,800-cell plate: FP32 basis 63-72 us per iteration persistent vs 54-64 us six
-     * kernels, FP64 exact 186-200 vs 186-211 us */
+     * with grid barriers between its phases, 0 (default) as five kernels; measured on the
+     * 28,800-cell plate: FP32 basis 63-72 us per iteration persistent vs 54-64 us with the
+     * six-kernel body of the time, FP64 exact 186-200 vs 186-211 us */
     int persistent;
+    /* graph driver with exact J v: 1 (default) launches the Arnoldi body's kernels after
+     * the first with programmatic dependent launch, so each starts while its predecessor's
+     * tail (grid reduction, Givens step) runs; 0 launches them plainly */
+    int pdl;
 } cfdg_config;
 
 /* CFDG_KRYLOV_STREAM launches the graph driver's kernels one iteration at a time from a
@@ -281,6 +285,10 @@ cfdg_status cfdg_norm_vm_noalloc(const double* R, const double* vol, long n_cell
                                  void* stream);
 /* kernel launches issued by this solver since creation (all of them are this library's) */
 cfdg_status cfdg_launch_count(cfdg_solver* s, long long* n);
+/* the Krylov driver in effect: [0] CFDG_KRYLOV_* mode, [1] kernels per Arnoldi iteration
+ * of the last built graph body (0 before the first), [2] 1 when the body's kernels use
+ * programmatic dependent launch, [3] 1 for the persistent Arnoldi kernel */
+cfdg_status cfdg_krylov_info(cfdg_solver* s, int* out4);
 
 #ifdef __cplusplus
 }

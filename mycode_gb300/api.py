@@ -46,7 +46,7 @@ class Config(C.Structure):
         ("Pr", C.c_double), ("nu", C.c_double), ("cfl0", C.c_double), ("cfl_max", C.c_double),
         ("limiter_freeze_step", C.c_int), ("limiter_freeze_cfl", C.c_double),
         ("turb_intensity", C.c_double), ("mut_ratio", C.c_double), ("shock_deflection_deg", C.c_double),
-        ("renumber", C.c_int), ("device", C.c_int), ("krylov", C.c_int), ("persistent", C.c_int),
+        ("renumber", C.c_int), ("device", C.c_int), ("krylov", C.c_int), ("persistent", C.c_int), ("pdl", C.c_int),
     ]
 
 
@@ -121,6 +121,7 @@ SIGNATURES = {
     "cfdg_kernel_stats": (C.c_int, [_vp, _dp, np.ctypeslib.ndpointer(dtype=np.int64, flags="C_CONTIGUOUS"), C.c_int]),
     "cfdg_flush_l2": (C.c_int, [_vp, C.c_size_t]),
     "cfdg_launch_count": (C.c_int, [_vp, C.POINTER(C.c_longlong)]),
+    "cfdg_krylov_info": (C.c_int, [_vp, np.ctypeslib.ndpointer(dtype=np.int32, flags="C_CONTIGUOUS")]),
     "cfdg_norm_vm_noalloc": (C.c_int, [C.c_void_p, C.c_void_p, C.c_long, C.c_int, C.c_void_p, C.c_void_p]),
 }
 
@@ -497,3 +498,10 @@ class Solver:
         n = C.c_longlong()
         _check(lib().cfdg_launch_count(self._h, C.byref(n)))
         return n.value
+
+    def krylov_info(self):
+        """The Krylov driver in effect: mode, kernels per Arnoldi iteration of the last
+        built graph body, programmatic dependent launch in the body, persistent kernel."""
+        v = np.zeros(4, np.int32)
+        _check(lib().cfdg_krylov_info(self._h, v))
+        return {"mode": int(v[0]), "body_kernels": int(v[1]), "pdl": bool(v[2]), "persistent": bool(v[3])}

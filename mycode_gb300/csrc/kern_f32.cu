@@ -98,9 +98,9 @@ void launch_gmres_prim_z<float>(int nv, long nc, const Flow<float>& F, const flo
 }
 template <>
 void launch_gmres_gather_dot<float>(int nv, const MeshView<float>& m, const float* FA, float* w, const float* z, const float* dt,
-                                 const float* src, const float* V, long L, const GmresDev& d, cudaStream_t s) {
-    NV_SWITCH(nv, (k_gmres_gather_dot<float, NVC><<<kry_grid(m.nc), RED_THREADS, 0, s>>>(m, FA, m.nf, w, z, dt, src, V, L,
-                                                                                     d)));
+                                 const float* src, const float* V, long L, const GmresDev& d, cudaStream_t s, bool pdl) {
+    NV_SWITCH(nv, launch_k(pdl, k_gmres_gather_dot<float, NVC>, dim3(kry_grid(m.nc)), dim3(RED_THREADS), s, m, FA, (long)m.nf,
+                           w, z, dt, src, V, L, d));
 }
 template <>
 void launch_gmres_update_dot<float>(long L, float* w, const float* V, const GmresDev& d, cudaStream_t s) {
@@ -108,8 +108,8 @@ void launch_gmres_update_dot<float>(long L, float* w, const float* V, const Gmre
 }
 template <>
 void launch_gmres_update_dot_last<float>(long L, float* w, const float* V, const GmresDev& d, cudaGraphConditionalHandle h,
-                                   cudaStream_t s) {
-    k_gmres_update_dot<float, true><<<kry_grid(L), RED_THREADS, 0, s>>>(L, w, V, d, h);
+                                   cudaStream_t s, bool pdl) {
+    launch_k(pdl, k_gmres_update_dot<float, true>, dim3(kry_grid(L)), dim3(RED_THREADS), s, L, w, V, d, h);
 }
 template <>
 void launch_gmres_update_final<float>(long L, const float* w, float* V, const GmresDev& d, cudaGraphConditionalHandle h,

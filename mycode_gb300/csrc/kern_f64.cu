@@ -140,9 +140,9 @@ void launch_gmres_prim_z<double>(int nv, long nc, const Flow<double>& F, const d
 }
 template <>
 void launch_gmres_gather_dot<double>(int nv, const MeshView<double>& m, const double* FA, double* w, const double* z, const double* dt,
-                                 const double* src, const double* V, long L, const GmresDev& d, cudaStream_t s) {
-    NV_SWITCH(nv, (k_gmres_gather_dot<double, NVC><<<kry_grid(m.nc), RED_THREADS, 0, s>>>(m, FA, m.nf, w, z, dt, src, V, L,
-                                                                                     d)));
+                                 const double* src, const double* V, long L, const GmresDev& d, cudaStream_t s, bool pdl) {
+    NV_SWITCH(nv, launch_k(pdl, k_gmres_gather_dot<double, NVC>, dim3(kry_grid(m.nc)), dim3(RED_THREADS), s, m, FA, (long)m.nf,
+                           w, z, dt, src, V, L, d));
 }
 template <>
 void launch_gmres_update_dot<double>(long L, double* w, const double* V, const GmresDev& d, cudaStream_t s) {
@@ -150,8 +150,8 @@ void launch_gmres_update_dot<double>(long L, double* w, const double* V, const G
 }
 template <>
 void launch_gmres_update_dot_last<double>(long L, double* w, const double* V, const GmresDev& d, cudaGraphConditionalHandle h,
-                                   cudaStream_t s) {
-    k_gmres_update_dot<double, true><<<kry_grid(L), RED_THREADS, 0, s>>>(L, w, V, d, h);
+                                   cudaStream_t s, bool pdl) {
+    launch_k(pdl, k_gmres_update_dot<double, true>, dim3(kry_grid(L)), dim3(RED_THREADS), s, L, w, V, d, h);
 }
 template <>
 void launch_gmres_update_final<double>(long L, const double* w, double* V, const GmresDev& d, cudaGraphConditionalHandle h,

@@ -7,8 +7,9 @@
 // (dual-number) J v an iteration is five kernels and two grid reductions:
 //   V_j = w - V h2 (deferred), z = V_j / D, dual primitives    (k_gmres_prim_z)
 //   dual gradients, dual face fluxes                           (k_grad, k_flux)
-//   J v gather   -> w and h1 = V^T w                           (k_gmres_gather_dot)
-//   w -= V h1    -> w, h2 = V^T w and |w|^2; Givens step        (k_gmres_update_dot<T, true>)
+//   J v gather   -> w and block partials of h1 = V^T w         (k_gmres_gather_dot)
+//   h1 from the partials (every block), w -= V h1 -> w, h2 = V^T w and |w|^2; the last
+//   block: the Givens step                                     (k_gmres_update_dot<T, true>)
 // The norm of V_{j+1} = w - V h2 is taken as |w|^2 - |h2|^2 (Pythagoras over the
 // orthonormal basis, as in the one-reduction CGS2 variants of Swirydowicz, Langou,
 // Ananthan, Yang and Thomas, "Low synchronization Gram-Schmidt and GMRES algorithms",
@@ -17,19 +18,23 @@
 // explicit final pass:
 //   w -= V h2    -> V_{j+1}, |V_{j+1}|, and the Givens step  (k_gmres_update_final)
 // Every thread reads back only the elements it wrote itself, so no grid barrier is
-// needed inside a kernel; the last block to finish each kernel sums the block partials
-// in block order (deterministic).  Basis vectors are stored unnormalised with a scale
-// factor sc[i] = 1/|V_i| (FP64) applied wherever they are read.  The Givens and
-// least-squares arithmetic is the reference's (src/Solver.cpp:1562-1599) in FP64.
+// needed inside a kernel.  A grid reduction is either finished by the last block to
+// finish (a ticket counter) or, for h1, by every block of the next kernel from the block
+// partials; both sum in a fixed order (deterministic).  Basis vectors are stored
+// unnormalised with a scale factor sc[i] = 1/|V_i| (FP64) applied wherever they are
+// read.  The Givens and least-squares arithmetic is the reference's
+// (src/Solver.cpp:1562-1599) in FP64.
 //
-// Termination: the last block of k_gmres_update_final is the only place that advances j;
-// it runs once per body execution and clears the loop condition when j + 1 reaches m (or
-// on convergence), so the loop runs at most m times.  The same kernels also run outside a
+// Termination: the last block of the body's last kernel (k_gmres_update_dot<T, true>, or
+// k_gmres_update_final on the FD path) is the only place that advances j; it runs once
+// per body execution and clears the loop condition when j + 1 reaches m (or on
+// convergence), so the loop runs at most m times.  The same kernels also run outside a
 // graph (in_graph = 0), launched one iteration at a time by a host loop that reads the
 // done flag: the stream driver, which times every kernel with events.
 #pragma once
 #include <cuda_runtime.h>
 #include "linalg.cuh"
+#include "pdl.cuh"
 
 namespace cfdg {
 
@@ -48,6 +53,8 @@ struct GmresDev {
     double* hsq;      // [2] squared norms ([1]: after the second pass)
     double* sc;       // [m+1] scale of each stored basis vector
     double* partial;  // [(KRY_MAXM+1) * RED_BLOCKS]
+    double* partial1; // [(KRY_MAXM+1) * RED_BLOCKS] block partials of h1 (exact J v body)
+    int nb1;          // blocks of the gather kernel that writes partial1
     unsigned* counter;
     int in_graph;     // 1: the kernels run inside the WHILE graph and set its condition
 };
@@ -136,32 +143,32 @@ __device__ __forceinline__ double tree8(const double (&x)[8]) {
 // cumulative over the writes the barrier ordered before it).  scs: sc staged in shared
 // memory (or null: read d.sc).  Returns true in the last block.  Needs j + 1 <=
 // blockDim.x, a multiple of 32, and blockDim.x <= RED_THREADS.
-__device__ __forceinline__ bool dots_finish(const GmresDev& d, int j, double (*wsum)[KRY_WARPS], double* h,
-                                            int jraw = -1, const double* scs = nullptr, double* hsm = nullptr) {
+// This block's partials of the dots 0..j (sums of the per-warp sums in wsum) into
+// partial[i * RED_BLOCKS + blockIdx.x]
+__device__ __forceinline__ void block_partials(double* partial, int j, double (*wsum)[KRY_WARPS]) {
     __syncthreads();
     const int nwarp = blockDim.x >> 5;
     for (int i = threadIdx.x; i <= j; i += blockDim.x) {
         double x[8];
 #pragma unroll
         for (int w = 0; w < 8; ++w) x[w] = w < nwarp ? wsum[i][w] : 0.0;
-        d.partial[(long)i * RED_BLOCKS + blockIdx.x] = tree8(x);
+        partial[(long)i * RED_BLOCKS + blockIdx.x] = tree8(x);
     }
-    __syncthreads();
-    __shared__ bool last;
-    if (threadIdx.x == 0) {
-        __threadfence();
-        last = atomicAdd(d.counter, 1u) == gridDim.x - 1;
-        if (last) __threadfence();
-    }
-    __syncthreads();
-    if (!last) return false;
-    const int nd = j + 1, nb = (int)gridDim.x;
-    int G = 32;  // lanes per dot: aligned groups within a warp
+}
+
+// The sums over blocks b < nb of partial[i * RED_BLOCKS + b], i < nd, by the whole block:
+// dot i = threadIdx.x / G gets an aligned group of G lanes (G the largest power of two up
+// to 32 with G nd <= blockDim.x); each lane loads its strided share eight at a time and
+// sums them as trees, the group reduces by shuffles.  Every lane of group i returns the
+// sum (0 for i >= nd); the order is fixed, so every block that calls this gets the same
+// bits.  *gsz returns G.  Needs nd <= blockDim.x, a multiple of 32.
+__device__ __forceinline__ double partials_sum(const double* partial, int nd, int nb, int* gsz) {
+    int G = 32;
     while (G > 1 && G * nd > (int)blockDim.x) G >>= 1;
     const int i = threadIdx.x / G, g = threadIdx.x % G;
     double sg = 0.0;
     if (i < nd) {
-        const double* p = d.partial + (long)i * RED_BLOCKS;
+        const double* p = partial + (long)i * RED_BLOCKS;
         for (int b0 = g; b0 < nb; b0 += 8 * G) {
             double x[8];
 #pragma unroll
@@ -173,7 +180,32 @@ __device__ __forceinline__ bool dots_finish(const GmresDev& d, int j, double (*w
         }
     }
     for (int o = G >> 1; o > 0; o >>= 1) sg += __shfl_xor_sync(0xffffffffu, sg, o);
-    if (i < nd && g == 0) {
+    *gsz = G;
+    return sg;
+}
+
+// Block partials of h[0..j] from wsum, then in the last block to finish the sums over the
+// blocks (partials_sum): h[i] = sc[i] * sum (h[jraw] = sum, unscaled), also into hsm when
+// given.  One thread per block fences and takes the ticket after the block barrier (the
+// fence is cumulative over the writes the barrier ordered before it).  scs: sc staged in
+// shared memory (or null: read d.sc).  Returns true in the last block.  Needs j + 1 <=
+// blockDim.x, a multiple of 32, and blockDim.x <= RED_THREADS.
+__device__ __forceinline__ bool dots_finish(const GmresDev& d, int j, double (*wsum)[KRY_WARPS], double* h,
+                                            int jraw = -1, const double* scs = nullptr, double* hsm = nullptr) {
+    block_partials(d.partial, j, wsum);
+    __syncthreads();
+    __shared__ bool last;
+    if (threadIdx.x == 0) {
+        __threadfence();
+        last = atomicAdd(d.counter, 1u) == gridDim.x - 1;
+        if (last) __threadfence();
+    }
+    __syncthreads();
+    if (!last) return false;
+    int G;
+    const double sg = partials_sum(d.partial, j + 1, (int)gridDim.x, &G);
+    const int i = threadIdx.x / G;
+    if (i <= j && threadIdx.x % G == 0) {
         const double hv = (i == jraw ? 1.0 : (scs ? scs[i] : d.sc[i])) * sg;
         h[i] = hv;
         if (hsm) hsm[i] = hv;
@@ -228,6 +260,7 @@ __global__ void __launch_bounds__(256) k_gmres_prim_z(int nc, Flow<T> F, const T
                                                       const T* __restrict__ Dinv, T* __restrict__ z, Field<T> W,
                                                       const T* __restrict__ w, GmresDev d) {
     typedef typename KryAcc<T>::type A;
+    pdl_trigger();  // first kernel of the body: the gradient kernel may launch now
     const int j = d.gi[0];
     __shared__ A hs[KRY_MAXM];
     if (j > 0) {
@@ -309,6 +342,8 @@ __global__ void __launch_bounds__(RED_THREADS) k_gmres_gather_dot(MeshView<T> m,
     __shared__ double wsum[KRY_MAXM + 1][KRY_WARPS];
     __shared__ double scs[KRY_MAXM + 1];
     for (int i = threadIdx.x; i <= j; i += blockDim.x) scs[i] = d.sc[i];
+    pdl_wait();  // the face fluxes are the predecessor's (pdl.cuh)
+    pdl_trigger();
     // w = the gathered J v of cell i (reference face order)
     auto gather = [&](long i, T (&acc)[NV]) {
 #pragma unroll
@@ -388,7 +423,9 @@ __global__ void __launch_bounds__(RED_THREADS) k_gmres_gather_dot(MeshView<T> m,
             tile_to_smem(v, i0, nt, wsum);
         }
     }
-    dots_finish(d, j, wsum, d.h1, -1, scs);
+    // block partials only: every block of the next kernel sums them itself (partials_sum),
+    // which costs less than a last-block reduction here and its fence and ticket
+    block_partials(d.partial1, j, wsum);
 }
 
 // w -= sum_{i<=j} h1[i] sc[i] V_i, fused with the second CGS pass h2 = V^T w.  With LAST
@@ -408,22 +445,35 @@ __global__ void __launch_bounds__(RED_THREADS) k_gmres_update_dot(long L, T* __r
     __shared__ double hout[KRY_MAXM + 2];
     __shared__ double gj, tolb;
     __shared__ int mm;
+    // the previous iterations' state first, then (after the wait) h1 and w, which are
+    // the predecessor's (pdl.cuh)
     for (int i = threadIdx.x; i <= j; i += blockDim.x) {
-        const double h1 = d.h1[i], sc = d.sc[i];
-        hs[i] = (A)(h1 * sc);
-        scs[i] = sc;
-        if (LAST) {
-            col[i] = h1;
-            if (i < j) {
-                css[i] = d.cs[i];
-                sns[i] = d.sn[i];
-            }
+        scs[i] = d.sc[i];
+        if (LAST && i < j) {
+            css[i] = d.cs[i];
+            sns[i] = d.sn[i];
         }
     }
     if (LAST && threadIdx.x == 0) {
         gj = d.g[j];
         tolb = d.beta[1] * d.beta[0];
         mm = d.gi[3];
+    }
+    pdl_wait();
+    pdl_trigger();
+    if (LAST) {
+        // h1 = sc * (the gather kernel's block partials), summed by every block
+        int G;
+        const double sg = partials_sum(d.partial1, j + 1, d.nb1, &G);
+        const int i = threadIdx.x / G;
+        if (i <= j && threadIdx.x % G == 0) {
+            const double h1 = scs[i] * sg;
+            hs[i] = (A)(h1 * scs[i]);
+            col[i] = h1;
+            if (blockIdx.x == 0) d.h1[i] = h1;
+        }
+    } else {
+        for (int i = threadIdx.x; i <= j; i += blockDim.x) hs[i] = (A)(d.h1[i] * scs[i]);
     }
     __syncthreads();
     A nw = A(0);

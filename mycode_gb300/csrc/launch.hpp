@@ -25,7 +25,30 @@ struct ResArgs {
     cudaEvent_t* ev;        // optional 5 events around the four kernels
     Field<R> T{nullptr, nullptr, 0};  // SST cell terms (mu_t, F1, S_k vol, S_w vol); nv = 6 only
     const R* dwall = nullptr;         // wall distance per cell; nv = 6 only
+    bool pdl = false;                 // launch_jv_mid: programmatic dependent launch (pdl.cuh)
 };
+
+// A kernel launch, with the programmatic stream-serialisation attribute when pdl: the
+// kernel may then start before its predecessor in the stream (or graph) completes and
+// must keep the rules of pdl.cuh.
+template <typename... KArgs, typename... Args>
+inline void launch_k(bool pdl, void (*kern)(KArgs...), dim3 grid, dim3 block, cudaStream_t s, Args... args) {
+    if (!pdl) {
+        kern<<<grid, block, 0, s>>>(args...);
+        return;
+    }
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = grid;
+    cfg.blockDim = block;
+    cfg.dynamicSmemBytes = 0;
+    cfg.stream = s;
+    cudaLaunchAttribute at[1];
+    at[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    at[0].val.programmaticStreamSerializationAllowed = 1;
+    cfg.attrs = at;
+    cfg.numAttrs = 1;
+    cudaLaunchKernelEx(&cfg, kern, args...);
+}
 
 // R(U) (kern_f64.cu for double, kern_f32.cu for float)
 template <class R> void launch_residual(const ResArgs<R>& a);
@@ -137,10 +160,10 @@ template <class T> void launch_gmres_prim_z(int nv, long nc, const Flow<T>& F, c
                                             cudaStream_t s);
 template <class T> void launch_gmres_gather_dot(int nv, const MeshView<T>& m, const T* FA, T* w, const T* z,
                                                 const T* dt, const T* src, const T* V, long L, const GmresDev& d,
-                                                cudaStream_t s);
+                                                cudaStream_t s, bool pdl = false);
 template <class T> void launch_gmres_update_dot(long L, T* w, const T* V, const GmresDev& d, cudaStream_t s);
 template <class T> void launch_gmres_update_dot_last(long L, T* w, const T* V, const GmresDev& d,
-                                                     cudaGraphConditionalHandle h, cudaStream_t s);
+                                                     cudaGraphConditionalHandle h, cudaStream_t s, bool pdl = false);
 template <class T> void launch_gmres_update_final(long L, const T* w, T* V, const GmresDev& d,
                                                   cudaGraphConditionalHandle h, cudaStream_t s);
 template <class T> void launch_gmres_solution_dev(int nv, long nc, const T* V, long L, const GmresDev& d,

@@ -15,6 +15,7 @@
 #pragma once
 #include <cuda_runtime.h>
 #include "face.cuh"
+#include "pdl.cuh"
 #include "sst.cuh"
 
 namespace cfdg {
@@ -231,6 +232,8 @@ __global__ void __launch_bounds__(256) k_grad(MeshView<R> m, Flow<R> F, Field<R>
                                               R* phi, int do_limiter) {
     long i = (long)blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= m.nc) return;
+    pdl_wait();
+    pdl_trigger();
     grad_item<S, NV>(m, F, U, W, G, phi, do_limiter, i);
 }
 
@@ -279,6 +282,8 @@ __global__ void __launch_bounds__(256) k_sst_cell(MeshView<R> m, Flow<R> F, Fiel
                                                   const R* __restrict__ dwall, Field<R> T) {
     long i = (long)blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= m.nc) return;
+    pdl_wait();
+    pdl_trigger();
     sst_item<S, NV>(m, F, W, G, dwall, T, i);
 }
 
@@ -292,6 +297,10 @@ __device__ __forceinline__ void flux_item(const MeshView<R>& m, const Flow<R>& F
     FaceGeo<R> g = load_geo(m, f);
     CS<S> L = load_cs<S, NV>(U, W, o);
     CS<S> Rn = interior ? load_cs<S, NV>(U, W, n) : L;
+    // the state and primitives come from two or more kernels back in the Arnoldi body,
+    // the gradients, limiter and SST terms from the predecessor (pdl.cuh)
+    pdl_wait();
+    pdl_trigger();
     S gL[10], gR[10];
 #pragma unroll
     for (int q = 0; q < 10; ++q) { gL[q] = S(R(0)); gR[q] = S(R(0)); }

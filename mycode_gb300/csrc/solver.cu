@@ -133,6 +133,7 @@ struct cfdg_solver {
     const void* gkey[4] = {nullptr, nullptr, nullptr, nullptr};
     int flow_version = 0, graph_version = -1;
     bool capturing = false;
+    bool pdl_failed = false;  // the body would not build with programmatic dependent launch
     long long graph_pre = 0, graph_body = 0, graph_post = 0;
     // reductions
     RedScratch rs{nullptr, nullptr};
@@ -600,6 +601,9 @@ struct cfdg_solver {
         }
         // ev (stream driver with timing): 6 events around the 5 stages, stat classes 12-16
         cudaEvent_t* ev = (mixed || cfg.jv == CFDG_JV_EXACT) ? take_events(12, 5) : nullptr;
+        // programmatic dependent launch for the kernels after the first (pdl.cuh); not
+        // with per-kernel events, which time each kernel alone
+        const bool pdl = cfg.pdl && !ev && !pdl_failed;
         if (ev) CK(cudaEventRecord(ev[0], st));
         if (mixed) {
             launch_gmres_prim_z<float>(nv, nc, Ff, U32, V32, L, dinv32, z32, f32(W32, W32d), w32, gd, st);
@@ -616,11 +620,12 @@ struct cfdg_solver {
             a.phi = phi32;
             a.stream = st;
             a.ev = ev ? ev + 1 : nullptr;
+            a.pdl = pdl;
             launch_jv_mid<float>(a);
             launch_gmres_gather_dot<float>(nv, mvf, FA32d, w32, z32, dt32, nv == 6 ? T32d + 2 * nc : nullptr, V32, L, gd,
-                                           st);
+                                           st, pdl);
             if (ev) CK(cudaEventRecord(ev[4], st));
-            launch_gmres_update_dot_last<float>(L, w32, V32, gd, h, st);
+            launch_gmres_update_dot_last<float>(L, w32, V32, gd, h, st, pdl);
             if (ev) CK(cudaEventRecord(ev[5], st));
             launches += nv == 6 ? 6 : 5;
         } else if (cfg.jv == CFDG_JV_EXACT) {
@@ -638,10 +643,12 @@ struct cfdg_solver {
             a.phi = phi;
             a.stream = st;
             a.ev = ev ? ev + 1 : nullptr;
+            a.pdl = pdl;
             launch_jv_mid<double>(a);
-            launch_gmres_gather_dot<double>(nv, mv, FAjd, w64, z, dt, nv == 6 ? Tjd + 2 * nc : nullptr, V, L, gd, st);
+            launch_gmres_gather_dot<double>(nv, mv, FAjd, w64, z, dt, nv == 6 ? Tjd + 2 * nc : nullptr, V, L, gd, st,
+                                            pdl);
             if (ev) CK(cudaEventRecord(ev[4], st));
-            launch_gmres_update_dot_last<double>(L, w64, V, gd, h, st);
+            launch_gmres_update_dot_last<double>(L, w64, V, gd, h, st, pdl);
             if (ev) CK(cudaEventRecord(ev[5], st));
             launches += nv == 6 ? 6 : 5;
         } else {
@@ -665,6 +672,18 @@ struct cfdg_solver {
     }
 
     cfdg_status build_gmres_graph(double* Ubase, double* Rbase, double* rhsd, double* xout) {
+        cfdg_status e = build_gmres_graph_once(Ubase, Rbase, rhsd, xout);
+        if (e != CFDG_OK && cfg.pdl && !pdl_failed) {
+            // no programmatic dependent launch inside a conditional body on this driver:
+            // build the body with plain launches
+            pdl_failed = true;
+            cudaGetLastError();
+            e = build_gmres_graph_once(Ubase, Rbase, rhsd, xout);
+        }
+        return e;
+    }
+
+    cfdg_status build_gmres_graph_once(double* Ubase, double* Rbase, double* rhsd, double* xout) {
         // the captured kernels take GmresDev by value: they must be the graph's variant,
         // whose Givens step ends the WHILE loop
         gd.in_graph = 1;
@@ -1384,6 +1403,7 @@ void cfdg_config_default(cfdg_config* c) {
     c->device = 0;
     c->krylov = CFDG_KRYLOV_AUTO;
     c->persistent = 0;
+    c->pdl = 1;
 }
 
 cfdg_status cfdg_mesh_create(int n_nodes, const double* xy, int n_cells, const int* cells, int n_bedges,
@@ -1550,7 +1570,7 @@ cfdg_status cfdg_solver_create(const cfdg_mesh* m, const cfdg_config* cfg, cfdg_
         int m = c.gmres_m;
         TRYS(dalloc(&s->gdi, 4));
         size_t nd = 3 + (size_t)(m + 1) + 2 * (size_t)m + (size_t)(m + 1) * m + m + 2 * (size_t)(m + 1) + 2 +
-                    (size_t)(m + 1) + (size_t)(KRY_MAXM + 1) * RED_BLOCKS + 4;
+                    (size_t)(m + 1) + 2 * (size_t)(KRY_MAXM + 1) * RED_BLOCKS + 4;
         TRYS(dalloc(&s->gdd, nd));
         double* q = s->gdd;
         GmresDev& d = s->gd;
@@ -1566,6 +1586,8 @@ cfdg_status cfdg_solver_create(const cfdg_mesh* m, const cfdg_config* cfg, cfdg_
         d.hsq = q; q += 2;
         d.sc = q; q += m + 1;
         d.partial = q; q += (size_t)(KRY_MAXM + 1) * RED_BLOCKS;
+        d.partial1 = q; q += (size_t)(KRY_MAXM + 1) * RED_BLOCKS;
+        d.nb1 = (int)kry_grid(nc);
         d.counter = reinterpret_cast<unsigned*>(q);
         d.in_graph = 1;
         if (c.precision == CFDG_MIXED) TRYS(dalloc(&s->w32, (size_t)L));
@@ -2015,6 +2037,15 @@ cfdg_status cfdg_flush_l2(cfdg_solver* s, size_t bytes) {
 cfdg_status cfdg_launch_count(cfdg_solver* s, long long* n) {
     if (!s || !n) return fail(CFDG_ERR_ARG, "null argument");
     *n = s->launches;
+    return CFDG_OK;
+}
+
+cfdg_status cfdg_krylov_info(cfdg_solver* s, int* out4) {
+    if (!s || !out4) return fail(CFDG_ERR_ARG, "null argument");
+    out4[0] = s->cfg.krylov;
+    out4[1] = (int)s->graph_body;
+    out4[2] = s->cfg.pdl && !s->pdl_failed && !s->use_persistent() ? 1 : 0;
+    out4[3] = s->use_persistent() ? 1 : 0;
     return CFDG_OK;
 }
 
