@@ -82,10 +82,14 @@ static __global__ void k_gmres_init(GmresDev d, int m, double tol, cudaGraphCond
     }
 }
 
-// Arithmetic of the vector kernels.  GB300 issues FP64 at 1/64 of its FP32 rate, so with
-// an FP32 basis the per-element work (products, the update, per-thread and per-warp
-// partial sums of at most a few hundred products) is FP32 and only the block and grid
-// levels of each reduction are FP64; with an FP64 basis everything is FP64.
+// Arithmetic of the vector kernels.  On GB300 every FP64 warp instruction occupies its
+// SM sub-partition for about 64 cycles (measured: a dependent FMA chain runs at 61
+// cycles per FMA, a divide at 437, a square root at 684, whatever the number of active
+// lanes), 64 times the cost of its FP32 counterpart.  With an FP32 basis all the vector
+// arithmetic and the block and grid levels of the dot products are FP32 (the products
+// are FP32 already; FP64 sums of them would halve a reduction error of ~1e-6 relative at
+// 64 times the cost in the serial tails); the Hessenberg column, the rotations and the
+// least squares stay FP64.  With an FP64 basis everything is FP64.
 template <class T> struct KryAcc { typedef double type; };
 template <> struct KryAcc<float> { typedef float type; };
 
@@ -103,8 +107,8 @@ constexpr int KRY_WARPS = RED_THREADS / 32;  // most warps of a block (blocks of
 // butterfly reduce-scatter (each exchange step halves the values a lane holds: 8, 4, 2
 // and 1 shuffles, then one more), 16 shuffles for the 16 dots instead of 5 per dot; lane
 // l ends with dot 8 b4 + 4 b3 + 2 b2 + b1 (bk: bit k of l), summed over the warp
-template <class A>
-__device__ __forceinline__ void tile_to_smem(const A (&v)[KRY_TILE], int i0, int nt, double (*wsum)[KRY_WARPS]) {
+template <class A, class W>
+__device__ __forceinline__ void tile_to_smem(const A (&v)[KRY_TILE], int i0, int nt, W (*wsum)[KRY_WARPS]) {
     static_assert(KRY_TILE == 16, "the butterfly is written for 16 values per lane");
     const unsigned full = 0xffffffffu;
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
@@ -122,36 +126,27 @@ __device__ __forceinline__ void tile_to_smem(const A (&v)[KRY_TILE], int i0, int
     A u = (hi ? z[1] : z[0]) + __shfl_xor_sync(full, hi ? z[0] : z[1], 2);
     u += __shfl_xor_sync(full, u, 1);
     const int d = ((lane >> 4) & 1) * 8 + ((lane >> 3) & 1) * 4 + ((lane >> 2) & 1) * 2 + ((lane >> 1) & 1);
-    if ((lane & 1) == 0 && d < nt) wsum[i0 + d][warp] = (double)u;
+    if ((lane & 1) == 0 && d < nt) wsum[i0 + d][warp] = (W)u;
 }
 
 constexpr int KRY_RC = 2 * KRY_TILE;  // basis vectors held in registers by the one-pass kernels
 
-// Sum of n <= 8 doubles as a balanced tree: GB300 runs a dependent FP64 add in about 40
-// cycles, so the depth of the tree, not the count, sets the latency.
-__device__ __forceinline__ double tree8(const double (&x)[8]) {
+// Sum of 8 values as a balanced tree (depth 3).
+template <class A>
+__device__ __forceinline__ A tree8(const A (&x)[8]) {
     return ((x[0] + x[1]) + (x[2] + x[3])) + ((x[4] + x[5]) + (x[6] + x[7]));
 }
 
-// Block partials of h[0..j] from wsum, then in the last block to finish the sums over the
-// blocks: h[i] = sc[i] * sum (h[jraw] = sum, unscaled), also into hsm when given.  The
-// last block gives each dot an aligned group of G lanes (G the largest power of two up
-// to 32 with G (j+1) <= blockDim.x): each lane loads its strided share of the blocks
-// eight at a time and sums them as trees, the group then reduces by shuffles, so every
-// dot's loads are in flight at once and the order is fixed (deterministic).  One thread
-// per block fences and takes the ticket after the block barrier (the fence is
-// cumulative over the writes the barrier ordered before it).  scs: sc staged in shared
-// memory (or null: read d.sc).  Returns true in the last block.  Needs j + 1 <=
-// blockDim.x, a multiple of 32, and blockDim.x <= RED_THREADS.
 // This block's partials of the dots 0..j (sums of the per-warp sums in wsum) into
 // partial[i * RED_BLOCKS + blockIdx.x]
-__device__ __forceinline__ void block_partials(double* partial, int j, double (*wsum)[KRY_WARPS]) {
+template <class A>
+__device__ __forceinline__ void block_partials(A* partial, int j, A (*wsum)[KRY_WARPS]) {
     __syncthreads();
     const int nwarp = blockDim.x >> 5;
     for (int i = threadIdx.x; i <= j; i += blockDim.x) {
-        double x[8];
+        A x[8];
 #pragma unroll
-        for (int w = 0; w < 8; ++w) x[w] = w < nwarp ? wsum[i][w] : 0.0;
+        for (int w = 0; w < 8; ++w) x[w] = w < nwarp ? wsum[i][w] : A(0);
         partial[(long)i * RED_BLOCKS + blockIdx.x] = tree8(x);
     }
 }
@@ -162,19 +157,20 @@ __device__ __forceinline__ void block_partials(double* partial, int j, double (*
 // sums them as trees, the group reduces by shuffles.  Every lane of group i returns the
 // sum (0 for i >= nd); the order is fixed, so every block that calls this gets the same
 // bits.  *gsz returns G.  Needs nd <= blockDim.x, a multiple of 32.
-__device__ __forceinline__ double partials_sum(const double* partial, int nd, int nb, int* gsz) {
+template <class A>
+__device__ __forceinline__ A partials_sum(const A* partial, int nd, int nb, int* gsz) {
     int G = 32;
     while (G > 1 && G * nd > (int)blockDim.x) G >>= 1;
     const int i = threadIdx.x / G, g = threadIdx.x % G;
-    double sg = 0.0;
+    A sg = A(0);
     if (i < nd) {
-        const double* p = partial + (long)i * RED_BLOCKS;
+        const A* p = partial + (long)i * RED_BLOCKS;
         for (int b0 = g; b0 < nb; b0 += 8 * G) {
-            double x[8];
+            A x[8];
 #pragma unroll
             for (int k = 0; k < 8; ++k) {
                 const int b = b0 + k * G;
-                x[k] = b < nb ? __ldcg(p + b) : 0.0;
+                x[k] = b < nb ? __ldcg(p + b) : A(0);
             }
             sg += tree8(x);
         }
@@ -190,9 +186,11 @@ __device__ __forceinline__ double partials_sum(const double* partial, int nd, in
 // fence is cumulative over the writes the barrier ordered before it).  scs: sc staged in
 // shared memory (or null: read d.sc).  Returns true in the last block.  Needs j + 1 <=
 // blockDim.x, a multiple of 32, and blockDim.x <= RED_THREADS.
-__device__ __forceinline__ bool dots_finish(const GmresDev& d, int j, double (*wsum)[KRY_WARPS], double* h,
+template <class A>
+__device__ __forceinline__ bool dots_finish(const GmresDev& d, int j, A (*wsum)[KRY_WARPS], double* h,
                                             int jraw = -1, const double* scs = nullptr, double* hsm = nullptr) {
-    block_partials(d.partial, j, wsum);
+    A* partial = reinterpret_cast<A*>(d.partial);
+    block_partials(partial, j, wsum);
     __syncthreads();
     __shared__ bool last;
     if (threadIdx.x == 0) {
@@ -203,10 +201,10 @@ __device__ __forceinline__ bool dots_finish(const GmresDev& d, int j, double (*w
     __syncthreads();
     if (!last) return false;
     int G;
-    const double sg = partials_sum(d.partial, j + 1, (int)gridDim.x, &G);
+    const A sg = partials_sum(partial, j + 1, (int)gridDim.x, &G);
     const int i = threadIdx.x / G;
     if (i <= j && threadIdx.x % G == 0) {
-        const double hv = (i == jraw ? 1.0 : (scs ? scs[i] : d.sc[i])) * sg;
+        const double hv = (i == jraw ? 1.0 : (scs ? scs[i] : d.sc[i])) * (double)sg;
         h[i] = hv;
         if (hsm) hsm[i] = hv;
     }
@@ -310,7 +308,7 @@ __global__ void __launch_bounds__(RED_THREADS) k_gmres_multidot(long L, const T*
                                                                 const T* __restrict__ V, GmresDev d, double* h) {
     typedef typename KryAcc<T>::type A;
     const int j = d.gi[0];
-    __shared__ double wsum[KRY_MAXM + 1][KRY_WARPS];
+    __shared__ A wsum[KRY_MAXM + 1][KRY_WARPS];
     for (int i0 = 0; i0 <= j; i0 += KRY_TILE) {
         const int nt = (j + 1 - i0) < KRY_TILE ? (j + 1 - i0) : KRY_TILE;
         A v[KRY_TILE];
@@ -339,7 +337,7 @@ __global__ void __launch_bounds__(RED_THREADS) k_gmres_gather_dot(MeshView<T> m,
     typedef typename KryAcc<T>::type A;
     const int j = d.gi[0];
     const long nc = m.nc;
-    __shared__ double wsum[KRY_MAXM + 1][KRY_WARPS];
+    __shared__ A wsum[KRY_MAXM + 1][KRY_WARPS];
     __shared__ double scs[KRY_MAXM + 1];
     for (int i = threadIdx.x; i <= j; i += blockDim.x) scs[i] = d.sc[i];
     pdl_wait();  // the face fluxes are the predecessor's (pdl.cuh)
@@ -425,7 +423,7 @@ __global__ void __launch_bounds__(RED_THREADS) k_gmres_gather_dot(MeshView<T> m,
     }
     // block partials only: every block of the next kernel sums them itself (partials_sum),
     // which costs less than a last-block reduction here and its fence and ticket
-    block_partials(d.partial1, j, wsum);
+    block_partials(reinterpret_cast<A*>(d.partial1), j, wsum);
 }
 
 // w -= sum_{i<=j} h1[i] sc[i] V_i, fused with the second CGS pass h2 = V^T w.  With LAST
@@ -440,7 +438,7 @@ __global__ void __launch_bounds__(RED_THREADS) k_gmres_update_dot(long L, T* __r
     typedef typename KryAcc<T>::type A;
     const int j = d.gi[0];
     __shared__ A hs[KRY_MAXM + 1];
-    __shared__ double wsum[KRY_MAXM + 1][KRY_WARPS];
+    __shared__ A wsum[KRY_MAXM + 1][KRY_WARPS];
     __shared__ double scs[KRY_MAXM + 1], col[KRY_MAXM + 2], h2s[KRY_MAXM + 2], css[KRY_MAXM], sns[KRY_MAXM];
     __shared__ double hout[KRY_MAXM + 2];
     __shared__ double gj, tolb;
@@ -464,10 +462,10 @@ __global__ void __launch_bounds__(RED_THREADS) k_gmres_update_dot(long L, T* __r
     if (LAST) {
         // h1 = sc * (the gather kernel's block partials), summed by every block
         int G;
-        const double sg = partials_sum(d.partial1, j + 1, d.nb1, &G);
+        const A sg = partials_sum(reinterpret_cast<const A*>(d.partial1), j + 1, d.nb1, &G);
         const int i = threadIdx.x / G;
         if (i <= j && threadIdx.x % G == 0) {
-            const double h1 = scs[i] * sg;
+            const double h1 = scs[i] * (double)sg;
             hs[i] = (A)(h1 * scs[i]);
             col[i] = h1;
             if (blockIdx.x == 0) d.h1[i] = h1;
@@ -526,7 +524,7 @@ __global__ void __launch_bounds__(RED_THREADS) k_gmres_update_dot(long L, T* __r
     }
     if (LAST) {
         nw = warp_sum_t(nw);
-        if ((threadIdx.x & 31) == 0) wsum[j + 1][threadIdx.x >> 5] = (double)nw;
+        if ((threadIdx.x & 31) == 0) wsum[j + 1][threadIdx.x >> 5] = nw;
     }
     if (!LAST) {
         dots_finish(d, j, wsum, d.h2, -1, scs);
@@ -534,25 +532,48 @@ __global__ void __launch_bounds__(RED_THREADS) k_gmres_update_dot(long L, T* __r
     }
     if (!dots_finish(d, j + 1, wsum, d.h2, j + 1, scs, h2s)) return;
     if (threadIdx.x >= 32) return;
-    // The Givens step (src/Solver.cpp:1550-1588) on lane 0 from shared memory, written for
-    // GB300's FP64 latencies (dependent FMA ~40 cycles, divide ~440, square root ~680):
-    // the rotation chain keeps its running entry in a register (one FMA deep per
-    // rotation) and runs interleaved with the sum of squares of h2, and the two
-    // normalisations take one reciprocal square root each instead of a square root and a
-    // divide (c = a / sqrt(a^2 + b^2) as a * rsqrt(a^2 + b^2)).
+    // The Givens step (src/Solver.cpp:1550-1588) by warp 0 of the last block.  Each FP64
+    // warp instruction costs ~64 cycles on GB300 whatever the active lanes, so the work is
+    // spread over the lanes: the previous rotations applied to the new column are the
+    // affine recurrence carry_{i+1} = -s_i carry_i + c_i col[i+1] (carry_0 = col[0]),
+    // evaluated as a parallel prefix over 32 rotations at a time (compositions of affine
+    // maps, Kogge-Stone), and out[i] = c_i carry_i + s_i col[i+1] by every lane at once.
+    // |h2|^2 is summed in the basis precision (it is ~1e-14 of |w|^2).  The new rotation
+    // takes c = a / sqrt(a^2 + b^2) as a * rsqrt(a^2 + b^2), and sc[j+1] = rsqrt(hsq).
+    const unsigned full = 0xffffffffu;
     const int lane = threadIdx.x;
-    for (int i = lane; i <= j; i += 32) col[i] += h2s[i];
+    A s2p = A(0);
+    for (int i = lane; i <= j; i += 32) {
+        const A h = (A)h2s[i];
+        s2p += h * h;
+        col[i] += h2s[i];
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) s2p += __shfl_xor_sync(full, s2p, o);
     __syncwarp();
-    if (lane == 0) {
-        double carry = col[0], s2 = 0.0;
-        for (int i = 0; i < j; ++i) {
-            const double ci = css[i], si = sns[i], nx = col[i + 1], hi = h2s[i];
-            hout[i] = fma(ci, carry, si * nx);
-            carry = fma(-si, carry, ci * nx);
-            s2 = fma(hi, hi, s2);
+    double carry = col[0];
+    for (int base = 0; base < j; base += 32) {
+        const int i = base + lane;
+        const bool act = i < j;
+        const double ci = act ? css[i] : 1.0, si = act ? sns[i] : 0.0, nx = act ? col[i + 1] : 0.0;
+        const double snx = si * nx;
+        double fa = act ? -si : 1.0, fb = act ? ci * nx : 0.0;  // f_i(x) = fa x + fb
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const double ap = __shfl_up_sync(full, fa, o), bp = __shfl_up_sync(full, fb, o);
+            if (lane >= o) {
+                fb = fma(fa, bp, fb);
+                fa = fa * ap;
+            }
         }
-        s2 = fma(h2s[j], h2s[j], s2);
-        const double hsq = fmax(h2s[j + 1] - s2, 0.0);
+        const double cnext = fma(fa, carry, fb);        // carry after rotation i
+        double cprev = __shfl_up_sync(full, cnext, 1);  // carry before rotation i
+        if (lane == 0) cprev = carry;
+        if (act) hout[i] = fma(ci, cprev, snx);
+        carry = __shfl_sync(full, cnext, 31);
+    }
+    if (lane == 0) {
+        const double hsq = fmax(h2s[j + 1] - (double)s2p, 0.0);
         const double r = hsq > 0.0 ? rsqrt(hsq) : 0.0;
         const double hv = hsq * r;
         d.hsq[1] = hsq;
@@ -564,7 +585,7 @@ __global__ void __launch_bounds__(RED_THREADS) k_gmres_update_dot(long L, T* __r
             sn = 0.0;
             hout[j] = a;
         } else {
-            const double q = fma(a, a, b * b), rq = rsqrt(q);
+            const double q = fma(a, a, hsq), rq = rsqrt(q);
             c = a * rq;
             sn = b * rq;
             hout[j] = q * rq;
