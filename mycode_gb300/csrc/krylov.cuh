@@ -477,25 +477,40 @@ __global__ void __launch_bounds__(RED_THREADS) k_gmres_update_dot(long L, T* __r
     A nw = A(0);
     if (j < KRY_RC) {
         // one pass: each element's basis values stay in registers between the update
-        // and the dots
+        // and the dots, and (FP32) a thread's three grid-stride elements are loaded
+        // together, so their loads are in flight at once
+        constexpr int EPT = sizeof(T) == 4 ? 3 : 1;
         A v0[KRY_TILE], v1[KRY_TILE];
 #pragma unroll
         for (int t = 0; t < KRY_TILE; ++t) v0[t] = v1[t] = A(0);
-        for (long q = (long)blockIdx.x * blockDim.x + threadIdx.x; q < L; q += (long)gridDim.x * blockDim.x) {
-            T vv[KRY_RC];
+        const long stride = (long)gridDim.x * blockDim.x;
+        for (long q0 = (long)blockIdx.x * blockDim.x + threadIdx.x; q0 < L; q0 += EPT * stride) {
+            T vv[EPT][KRY_RC];
+            A a[EPT];
 #pragma unroll
-            for (int t = 0; t < KRY_RC; ++t) vv[t] = t <= j ? V[(long)t * L + q] : T(0);
-            A a = (A)w[q];
+            for (int e = 0; e < EPT; ++e) {
+                const long q = q0 + e * stride;
+                const bool ok = q < L;
+                a[e] = ok ? (A)w[q] : A(0);
 #pragma unroll
-            for (int t = 0; t < KRY_RC; ++t)
-                if (t <= j) a -= hs[t] * (A)vv[t];
-            const T tq = (T)a;
-            w[q] = tq;
-            if (LAST) nw += (A)tq * (A)tq;
+                for (int t = 0; t < KRY_RC; ++t) vv[e][t] = ok && t <= j ? V[(long)t * L + q] : T(0);
+            }
 #pragma unroll
-            for (int t = 0; t < KRY_TILE; ++t) {
-                v0[t] += (A)tq * (A)vv[t];
-                v1[t] += (A)tq * (A)vv[KRY_TILE + t];
+            for (int e = 0; e < EPT; ++e) {
+                const long q = q0 + e * stride;
+                if (q >= L) continue;
+                A ae = a[e];
+#pragma unroll
+                for (int t = 0; t < KRY_RC; ++t)
+                    if (t <= j) ae -= hs[t] * (A)vv[e][t];
+                const T tq = (T)ae;
+                w[q] = tq;
+                if (LAST) nw += (A)tq * (A)tq;
+#pragma unroll
+                for (int t = 0; t < KRY_TILE; ++t) {
+                    v0[t] += (A)tq * (A)vv[e][t];
+                    v1[t] += (A)tq * (A)vv[e][KRY_TILE + t];
+                }
             }
         }
         tile_to_smem(v0, 0, j + 1 < KRY_TILE ? j + 1 : KRY_TILE, wsum);
