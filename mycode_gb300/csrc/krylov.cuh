@@ -459,6 +459,27 @@ __global__ void __launch_bounds__(RED_THREADS) k_gmres_update_dot(long L, T* __r
     }
     pdl_wait();
     pdl_trigger();
+    // one pass (j < KRY_RC): each element's basis values stay in registers between the
+    // update and the dots, and (FP32) a thread's three grid-stride elements are loaded
+    // together, so their loads are in flight at once; with FP32 the first such group is
+    // loaded before the h1 reduction below, so its loads overlap it
+    constexpr int EPT = sizeof(T) == 4 ? 3 : 1;
+    const long stride = (long)gridDim.x * blockDim.x;
+    const long qfirst = (long)blockIdx.x * blockDim.x + threadIdx.x;
+    T vv[EPT][KRY_RC];
+    A a[EPT];
+    auto load_group = [&](long q0) {
+#pragma unroll
+        for (int e = 0; e < EPT; ++e) {
+            const long q = q0 + e * stride;
+            const bool ok = q < L;
+            a[e] = ok ? (A)w[q] : A(0);
+#pragma unroll
+            for (int t = 0; t < KRY_RC; ++t) vv[e][t] = ok && t <= j ? V[(long)t * L + q] : T(0);
+        }
+    };
+    constexpr bool early = sizeof(T) == 4;  // (FP64: the registers are not there)
+    if (early && j < KRY_RC) load_group(qfirst);
     if (LAST) {
         // h1 = sc * (the gather kernel's block partials), summed by every block
         int G;
@@ -476,25 +497,11 @@ __global__ void __launch_bounds__(RED_THREADS) k_gmres_update_dot(long L, T* __r
     __syncthreads();
     A nw = A(0);
     if (j < KRY_RC) {
-        // one pass: each element's basis values stay in registers between the update
-        // and the dots, and (FP32) a thread's three grid-stride elements are loaded
-        // together, so their loads are in flight at once
-        constexpr int EPT = sizeof(T) == 4 ? 3 : 1;
         A v0[KRY_TILE], v1[KRY_TILE];
 #pragma unroll
         for (int t = 0; t < KRY_TILE; ++t) v0[t] = v1[t] = A(0);
-        const long stride = (long)gridDim.x * blockDim.x;
-        for (long q0 = (long)blockIdx.x * blockDim.x + threadIdx.x; q0 < L; q0 += EPT * stride) {
-            T vv[EPT][KRY_RC];
-            A a[EPT];
-#pragma unroll
-            for (int e = 0; e < EPT; ++e) {
-                const long q = q0 + e * stride;
-                const bool ok = q < L;
-                a[e] = ok ? (A)w[q] : A(0);
-#pragma unroll
-                for (int t = 0; t < KRY_RC; ++t) vv[e][t] = ok && t <= j ? V[(long)t * L + q] : T(0);
-            }
+        for (long q0 = qfirst; q0 < L; q0 += EPT * stride) {
+            if (!early || q0 != qfirst) load_group(q0);
 #pragma unroll
             for (int e = 0; e < EPT; ++e) {
                 const long q = q0 + e * stride;

@@ -137,6 +137,33 @@ template <class S, int NV, class R>
 __device__ __forceinline__ void grad_item(const MeshView<R>& m, const Flow<R>& F, const Field<R>& U,
                                           const Field<R>& W, const Field<R>& G, R* phi, int do_limiter, long i) {
     constexpr int NQ = NV == 6 ? 7 : 5;
+    // Mesh data first (face entries, then each face's normal, area and neighbour, and for
+    // a boundary face its distance and tag): no kernel writes it, so it is loaded before
+    // the wait for the predecessor's primitives (pdl.cuh) and only the primitive loads
+    // follow the wait.  The -1 pads are trailing, so skipping them is stopping at them.
+    int ek[4], nbr[4], ftg[4];
+    R fnx[4], fny[4], fA[4], fdn[4];
+#pragma unroll
+    for (int k = 0; k < 4; ++k) ek[k] = m.cf[(long)k * m.nc + i];
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+        const int e = ek[k];
+        nbr[k] = -1;
+        ftg[k] = 0;
+        fnx[k] = fny[k] = fA[k] = fdn[k] = R(0);
+        if (e < 0) continue;
+        const int f = e >> 1;
+        fnx[k] = m.nx[f];
+        fny[k] = m.ny[f];
+        fA[k] = m.area[f];
+        nbr[k] = (e & 1) ? m.fo[f] : m.fn[f];
+        if (nbr[k] < 0) {
+            fdn[k] = m.dxo[f] * fnx[k] + m.dyo[f] * fny[k];
+            ftg[k] = m.ftag[f];
+        }
+    }
+    pdl_wait();
+    pdl_trigger();
     S wi[NQ];
 #pragma unroll
     for (int q = 0; q < NQ; ++q) wi[q] = Acc<S>::ld(W, q, i);
@@ -144,26 +171,21 @@ __device__ __forceinline__ void grad_item(const MeshView<R>& m, const Flow<R>& F
 #pragma unroll
     for (int q = 0; q < 2 * NQ; ++q) acc[q] = S(R(0));
     R pmax = val(wi[W_P]), pmin = val(wi[W_P]);
-    // face entries first, so the four faces' loads can be in flight together; the -1 pads
-    // are trailing, so skipping them is stopping at them
-    int ek[4];
-#pragma unroll
-    for (int k = 0; k < 4; ++k) ek[k] = m.cf[(long)k * m.nc + i];
 #pragma unroll
     for (int k = 0; k < 4; ++k) {
         int e = ek[k];
         if (e < 0) continue;
-        int f = e >> 1, side = e & 1;
-        R nx = m.nx[f], ny = m.ny[f], A = m.area[f];
+        int side = e & 1;
+        R nx = fnx[k], ny = fny[k], A = fA[k];
         S wj[NQ];
-        int j = side ? m.fo[f] : m.fn[f];
+        int j = nbr[k];
         if (j >= 0) {
 #pragma unroll
             for (int q = 0; q < NQ; ++q) wj[q] = Acc<S>::ld(W, q, j);
         } else {
             CS<S> Ui = load_cs<S, NV>(U, W, i);
-            R dn = m.dxo[f] * nx + m.dyo[f] * ny;
-            CS<S> g = ghost_state(F, Ui, m.ftag[f], nx, ny, dn < R(0) ? -dn : dn);
+            R dn = fdn[k];
+            CS<S> g = ghost_state(F, Ui, ftg[k], nx, ny, dn < R(0) ? -dn : dn);
             wj[W_R] = g.r;
             wj[W_U] = g.u;
             wj[W_V] = g.v;
@@ -232,9 +254,7 @@ __global__ void __launch_bounds__(256) k_grad(MeshView<R> m, Flow<R> F, Field<R>
                                               R* phi, int do_limiter) {
     long i = (long)blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= m.nc) return;
-    pdl_wait();
-    pdl_trigger();
-    grad_item<S, NV>(m, F, U, W, G, phi, do_limiter, i);
+    grad_item<S, NV>(m, F, U, W, G, phi, do_limiter, i);  // waits for its predecessor (pdl.cuh)
 }
 
 // ---------------------------------------------------------------- k_flux
