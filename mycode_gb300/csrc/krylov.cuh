@@ -340,18 +340,30 @@ __global__ void __launch_bounds__(RED_THREADS) k_gmres_gather_dot(MeshView<T> m,
     __shared__ A wsum[KRY_MAXM + 1][KRY_WARPS];
     __shared__ double scs[KRY_MAXM + 1];
     for (int i = threadIdx.x; i <= j; i += blockDim.x) scs[i] = d.sc[i];
-    pdl_wait();  // the face fluxes are the predecessor's (pdl.cuh)
-    pdl_trigger();
-    // w = the gathered J v of cell i (reference face order)
-    auto gather = [&](long i, T (&acc)[NV]) {
+    // w = the gathered J v of cell i (reference face order).  Everything but the face
+    // fluxes comes from two or more kernels back (pdl.cuh), so a thread loads it for its
+    // first cell before the wait for the fluxes.
+    struct Pre {
+        int ek[4];
+        T tc, zc[NV], s4, s5;
+    };
+    auto pre = [&](long i, Pre& p) {
+#pragma unroll
+        for (int k = 0; k < 4; ++k) p.ek[k] = m.cf[(long)k * nc + i];
+        p.tc = m.vol[i] / (dt[i] + T(1e-30));
+#pragma unroll
+        for (int c = 0; c < NV; ++c) p.zc[c] = z[c * nc + i];
+        if constexpr (NV == 6) {
+            p.s4 = src[i];
+            p.s5 = src[nc + i];
+        }
+    };
+    auto gather = [&](long i, const Pre& p, T (&acc)[NV]) {
 #pragma unroll
         for (int c = 0; c < NV; ++c) acc[c] = T(0);
-        int ek[4];
-#pragma unroll
-        for (int k = 0; k < 4; ++k) ek[k] = m.cf[(long)k * nc + i];
 #pragma unroll
         for (int k = 0; k < 4; ++k) {
-            const int e = ek[k];
+            const int e = p.ek[k];
             if (e < 0) continue;  // pads only at the end of a cell's list
             long f = e >> 1;
             if (e & 1) {
@@ -363,24 +375,34 @@ __global__ void __launch_bounds__(RED_THREADS) k_gmres_gather_dot(MeshView<T> m,
             }
         }
         if constexpr (NV == 6) {
-            acc[4] = acc[4] - src[i];
-            acc[5] = acc[5] - src[nc + i];
+            acc[4] = acc[4] - p.s4;
+            acc[5] = acc[5] - p.s5;
         }
-        T tc = m.vol[i] / (dt[i] + T(1e-30));
 #pragma unroll
         for (int c = 0; c < NV; ++c) {
-            acc[c] = acc[c] + z[c * nc + i] * tc;
+            acc[c] = acc[c] + p.zc[c] * p.tc;
             w[c * nc + i] = acc[c];
         }
     };
+    const long ifirst = (long)blockIdx.x * blockDim.x + threadIdx.x;
+    Pre p0;
+    if (ifirst < nc) pre(ifirst, p0);
+    pdl_wait();  // the face fluxes are the predecessor's
+    pdl_trigger();
     if (j < KRY_RC) {
         // one pass over the cells: up to 32 dots accumulated in two register tiles
         A v0[KRY_TILE], v1[KRY_TILE];
 #pragma unroll
         for (int t = 0; t < KRY_TILE; ++t) v0[t] = v1[t] = A(0);
-        for (long i = (long)blockIdx.x * blockDim.x + threadIdx.x; i < nc; i += (long)gridDim.x * blockDim.x) {
+        for (long i = ifirst; i < nc; i += (long)gridDim.x * blockDim.x) {
             T acc[NV];
-            gather(i, acc);
+            if (i == ifirst) {
+                gather(i, p0, acc);
+            } else {
+                Pre p;
+                pre(i, p);
+                gather(i, p, acc);
+            }
 #pragma unroll
             for (int t = 0; t < KRY_RC; ++t)
                 if (t <= j) {
@@ -403,7 +425,9 @@ __global__ void __launch_bounds__(RED_THREADS) k_gmres_gather_dot(MeshView<T> m,
             for (long i = (long)blockIdx.x * blockDim.x + threadIdx.x; i < nc; i += (long)gridDim.x * blockDim.x) {
                 T acc[NV];
                 if (i0 == 0) {
-                    gather(i, acc);
+                    Pre p;
+                    pre(i, p);
+                    gather(i, p, acc);
                 } else {
 #pragma unroll
                     for (int c = 0; c < NV; ++c) acc[c] = w[c * nc + i];
