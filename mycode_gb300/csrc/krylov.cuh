@@ -25,10 +25,13 @@
 // read.  The Givens and least-squares arithmetic is the reference's
 // (src/Solver.cpp:1562-1599) in FP64.
 //
-// Termination: the last block of the body's last kernel (k_gmres_update_dot<T, true>, or
-// k_gmres_update_final on the FD path) is the only place that advances j; it runs once
-// per body execution and clears the loop condition when j + 1 reaches m (or on
-// convergence), so the loop runs at most m times.  The same kernels also run outside a
+// Termination: the last block of an iteration's last kernel (k_gmres_update_dot<T, true>,
+// or k_gmres_update_final on the FD path) is the only place that advances j; it runs
+// once per iteration and clears the loop condition and raises the done flag when j + 1
+// reaches m (or on convergence), so at most m iterations run.  The exact J v graph body
+// holds several iterations (a WHILE iteration costs ~3 us of its own on GB300); the
+// kernels of the iterations after the finishing one see the done flag and return at
+// once.  The same kernels also run outside a
 // graph (in_graph = 0), launched one iteration at a time by a host loop that reads the
 // done flag: the stream driver, which times every kernel with events.
 #pragma once
@@ -39,9 +42,12 @@
 namespace cfdg {
 
 constexpr int KRY_MAXM = 128;  // largest Krylov dimension of the device solver
+// Arnoldi iterations per WHILE-body execution with the exact J v; measured on the
+// 28,800-cell plate: 1, 2, 4 give 574, 583, 584 M cell-residuals/s
+constexpr int KRY_BODY_ITERS = 4;
 
 struct GmresDev {
-    int* gi;          // [0] j, [1] k (last iteration), [2] done, [3] m
+    int* gi;          // [0] j, [1] k (last iteration), [2] done, [3] m (16-byte aligned)
     double* beta;     // [0] beta, [1] tol, [2] beta^2
     double* g;        // [m+1]
     double* cs;       // [m]
@@ -258,8 +264,10 @@ __global__ void __launch_bounds__(256) k_gmres_prim_z(int nc, Flow<T> F, const T
                                                       const T* __restrict__ Dinv, T* __restrict__ z, Field<T> W,
                                                       const T* __restrict__ w, GmresDev d) {
     typedef typename KryAcc<T>::type A;
-    pdl_trigger();  // first kernel of the body: the gradient kernel may launch now
-    const int j = d.gi[0];
+    const int4 gi4 = *reinterpret_cast<const int4*>(d.gi);  // j and the done flag in one load
+    if (gi4.z) return;  // the solve finished in an earlier iteration of an unrolled body
+    pdl_trigger();      // first kernel of the body: the gradient kernel may launch now
+    const int j = gi4.x;
     __shared__ A hs[KRY_MAXM];
     if (j > 0) {
         for (int k = threadIdx.x; k < j; k += blockDim.x) hs[k] = (A)(d.h2[k] * d.sc[k]);
@@ -335,7 +343,9 @@ __global__ void __launch_bounds__(RED_THREADS) k_gmres_gather_dot(MeshView<T> m,
                                                                   const T* __restrict__ src, const T* __restrict__ V,
                                                                   long L, GmresDev d) {
     typedef typename KryAcc<T>::type A;
-    const int j = d.gi[0];
+    const int4 gi4 = *reinterpret_cast<const int4*>(d.gi);  // j and the done flag in one load
+    if (gi4.z) return;  // the solve finished in an earlier iteration of an unrolled body
+    const int j = gi4.x;
     const long nc = m.nc;
     __shared__ A wsum[KRY_MAXM + 1][KRY_WARPS];
     __shared__ double scs[KRY_MAXM + 1];
@@ -460,7 +470,9 @@ template <class T, bool LAST>
 __global__ void __launch_bounds__(RED_THREADS) k_gmres_update_dot(long L, T* __restrict__ w, const T* __restrict__ V,
                                                                   GmresDev d, cudaGraphConditionalHandle hnd) {
     typedef typename KryAcc<T>::type A;
-    const int j = d.gi[0];
+    const int4 gi4 = *reinterpret_cast<const int4*>(d.gi);  // j and the done flag in one load
+    if (LAST && gi4.z) return;  // the solve finished in an earlier iteration of an unrolled body
+    const int j = gi4.x;
     __shared__ A hs[KRY_MAXM + 1];
     __shared__ A wsum[KRY_MAXM + 1][KRY_WARPS];
     __shared__ double scs[KRY_MAXM + 1], col[KRY_MAXM + 2], h2s[KRY_MAXM + 2], css[KRY_MAXM], sns[KRY_MAXM];

@@ -26,6 +26,7 @@ struct ResArgs {
     Field<R> T{nullptr, nullptr, 0};  // SST cell terms (mu_t, F1, S_k vol, S_w vol); nv = 6 only
     const R* dwall = nullptr;         // wall distance per cell; nv = 6 only
     bool pdl = false;                 // launch_jv_mid: programmatic dependent launch (pdl.cuh)
+    const int* done = nullptr;        // launch_jv_mid: skip when *done (a finished Krylov solve)
 };
 
 // A kernel launch, with the programmatic stream-serialisation attribute when pdl: the

@@ -135,7 +135,10 @@ __global__ void __launch_bounds__(256) k_prim(int nc, Flow<R> F, Field<R> U, Fie
 // (src/Solver.cpp:152-253) for the same cell from its own fresh gradient.
 template <class S, int NV, class R>
 __device__ __forceinline__ void grad_item(const MeshView<R>& m, const Flow<R>& F, const Field<R>& U,
-                                          const Field<R>& W, const Field<R>& G, R* phi, int do_limiter, long i) {
+                                          const Field<R>& W, const Field<R>& G, R* phi, int do_limiter, long i,
+                                          const int* done = nullptr) {
+    // done: a finished Krylov solve (krylov.cuh); read with the mesh loads, tested after
+    const int skip = done ? *done : 0;
     constexpr int NQ = NV == 6 ? 7 : 5;
     // Mesh data first (face entries, then each face's normal, area and neighbour, and for
     // a boundary face its distance and tag): no kernel writes it, so it is loaded before
@@ -162,6 +165,7 @@ __device__ __forceinline__ void grad_item(const MeshView<R>& m, const Flow<R>& F
             ftg[k] = m.ftag[f];
         }
     }
+    if (skip) return;
     pdl_wait();
     pdl_trigger();
     S wi[NQ];
@@ -251,10 +255,10 @@ __device__ __forceinline__ void grad_item(const MeshView<R>& m, const Flow<R>& F
 
 template <class S, int NV, class R>
 __global__ void __launch_bounds__(256) k_grad(MeshView<R> m, Flow<R> F, Field<R> U, Field<R> W, Field<R> G,
-                                              R* phi, int do_limiter) {
+                                              R* phi, int do_limiter, const int* done) {
     long i = (long)blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= m.nc) return;
-    grad_item<S, NV>(m, F, U, W, G, phi, do_limiter, i);  // waits for its predecessor (pdl.cuh)
+    grad_item<S, NV>(m, F, U, W, G, phi, do_limiter, i, done);  // waits for its predecessor (pdl.cuh)
 }
 
 // ---------------------------------------------------------------- k_flux
@@ -299,9 +303,9 @@ __device__ __forceinline__ void sst_item(const MeshView<R>& m, const Flow<R>& F,
 
 template <class S, int NV, class R>
 __global__ void __launch_bounds__(256) k_sst_cell(MeshView<R> m, Flow<R> F, Field<R> W, Field<R> G,
-                                                  const R* __restrict__ dwall, Field<R> T) {
+                                                  const R* __restrict__ dwall, Field<R> T, const int* done) {
     long i = (long)blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= m.nc) return;
+    if (i >= m.nc || (done && *done)) return;
     pdl_wait();
     pdl_trigger();
     sst_item<S, NV>(m, F, W, G, dwall, T, i);
@@ -310,7 +314,8 @@ __global__ void __launch_bounds__(256) k_sst_cell(MeshView<R> m, Flow<R> F, Fiel
 template <class S, int NV, class R>
 __device__ __forceinline__ void flux_item(const MeshView<R>& m, const Flow<R>& F, const Field<R>& U,
                                           const Field<R>& W, const Field<R>& G, const R* __restrict__ phi,
-                                          const Field<R>& FA, const Field<R>& T, long f) {
+                                          const Field<R>& FA, const Field<R>& T, long f, const int* done = nullptr) {
+    const int skip = done ? *done : 0;  // a finished Krylov solve: tested after the first loads
     int o = m.fo[f], n = m.fn[f];
     bool interior = n >= 0;
     int tag = interior ? 0 : m.ftag[f];
@@ -319,6 +324,7 @@ __device__ __forceinline__ void flux_item(const MeshView<R>& m, const Flow<R>& F
     CS<S> Rn = interior ? load_cs<S, NV>(U, W, n) : L;
     // the state and primitives come from two or more kernels back in the Arnoldi body,
     // the gradients, limiter and SST terms from the predecessor (pdl.cuh)
+    if (skip) return;
     pdl_wait();
     pdl_trigger();
     S gL[10], gR[10];
@@ -363,10 +369,10 @@ __device__ __forceinline__ void flux_item(const MeshView<R>& m, const Flow<R>& F
 
 template <class S, int NV, class R>
 __global__ void __launch_bounds__(256) k_flux(MeshView<R> m, Flow<R> F, Field<R> U, Field<R> W, Field<R> G,
-                                              const R* __restrict__ phi, Field<R> FA, Field<R> T) {
+                                              const R* __restrict__ phi, Field<R> FA, Field<R> T, const int* done) {
     long f = (long)blockIdx.x * blockDim.x + threadIdx.x;
     if (f >= m.nf) return;
-    flux_item<S, NV>(m, F, U, W, G, phi, FA, T, f);
+    flux_item<S, NV>(m, F, U, W, G, phi, FA, T, f, done);
 }
 
 // ---------------------------------------------------------------- k_gather

@@ -604,6 +604,24 @@ struct cfdg_solver {
         // programmatic dependent launch for the kernels after the first (pdl.cuh); not
         // with per-kernel events, which time each kernel alone
         const bool pdl = cfg.pdl && !ev && !pdl_failed;
+        // a graph body holds body_unroll() iterations (the kernels of the iterations after
+        // the finishing one return at once)
+        const int reps = capturing && (mixed || cfg.jv == CFDG_JV_EXACT) ? body_unroll() : 1;
+        for (int rep = 0; rep < reps; ++rep) TRY(enqueue_arnoldi_iteration(Ubase, Rbase, h, ev, pdl));
+        CK(cudaGetLastError());
+        return CFDG_OK;
+    }
+
+    int body_unroll() const { return KRY_BODY_ITERS; }
+    // WHILE-body executions of a graph solve of `iters` iterations
+    long long body_runs(int iters) const {
+        const int u = use_persistent() || !(cfg.precision == CFDG_MIXED || cfg.jv == CFDG_JV_EXACT) ? 1 : body_unroll();
+        return (iters + u - 1) / u;
+    }
+
+    cfdg_status enqueue_arnoldi_iteration(double* Ubase, double* Rbase, cudaGraphConditionalHandle h,
+                                          cudaEvent_t* ev, bool pdl) {
+        const bool mixed = cfg.precision == CFDG_MIXED;
         if (ev) CK(cudaEventRecord(ev[0], st));
         if (mixed) {
             launch_gmres_prim_z<float>(nv, nc, Ff, U32, V32, L, dinv32, z32, f32(W32, W32d), w32, gd, st);
@@ -621,6 +639,7 @@ struct cfdg_solver {
             a.stream = st;
             a.ev = ev ? ev + 1 : nullptr;
             a.pdl = pdl;
+            a.done = gd.gi + 2;
             launch_jv_mid<float>(a);
             launch_gmres_gather_dot<float>(nv, mvf, FA32d, w32, z32, dt32, nv == 6 ? T32d + 2 * nc : nullptr, V32, L, gd,
                                            st, pdl);
@@ -644,6 +663,7 @@ struct cfdg_solver {
             a.stream = st;
             a.ev = ev ? ev + 1 : nullptr;
             a.pdl = pdl;
+            a.done = gd.gi + 2;
             launch_jv_mid<double>(a);
             launch_gmres_gather_dot<double>(nv, mv, FAjd, w64, z, dt, nv == 6 ? Tjd + 2 * nc : nullptr, V, L, gd, st,
                                             pdl);
@@ -809,7 +829,7 @@ struct cfdg_solver {
         if (hi[2]) return barrier_timeout();
         int k = hi[0];
         *iters = k + 1;
-        launches += graph_pre + (long long)(k + 1) * graph_body + graph_post;
+        launches += graph_pre + (long long)body_runs(k + 1) * graph_body + graph_post;
         return CFDG_OK;
     }
 
@@ -1098,7 +1118,7 @@ struct cfdg_solver {
             return CFDG_OK;
         }
         const int it = hi[0] + 1;
-        launches += graph_pre + (long long)it * graph_body + graph_post;
+        launches += graph_pre + (long long)body_runs(it) * graph_body + graph_post;
         rec.gmres_iters = it;
         if (timing) {
             float ms = 0;
