@@ -271,7 +271,7 @@ def run_steps(s, steps, flush=True):
         rec, _ = s.newton_step(0.0)
         tot_ms += rec.device_ms
         evals += 1 + rec.gmres_iters
-        recs.append((rec.res_vm, rec.gmres_iters, rec.device_ms, rec.cfl))
+        recs.append((rec.res_vm, rec.gmres_iters, rec.device_ms, rec.cfl, rec.krylov_ms))
     return tot_ms / 1e3, evals, recs
 
 
@@ -336,6 +336,14 @@ def ours(args):
     value = units / t_max
 
     # ---- roofline of the dominant kernel class
+    # The timed steps' GMRES graphs are timed whole (CUDA events around each graph launch:
+    # krylov_ms).  The replay times every Arnoldi kernel alone (its events add ~2-3 us per
+    # launch and it runs without programmatic dependent launch), so the graph time is
+    # attributed to the kernel classes in proportion to their replay averages.
+    iters = evals - args.steps
+    t_kry_ms = sum(r[4] for r in recs)
+    replay_sum = sum(ms / n for k, (ms, n) in stats.items() if k.startswith("krylov.") and n)
+    attr = t_kry_ms / (replay_sum * iters) if replay_sum > 0 and iters > 0 else 1.0
     peak, peak_kind = measured_peak()
     kern = {}
     for k, (ms, n) in stats.items():
@@ -349,12 +357,18 @@ def ours(args):
             b = algorithmic_bytes(name, nc, nf, 4, 4 if dual else 8, "SECOND_ORDER_CENTRAL", True, dual)
         avg = ms / n
         kern[k] = {"launches": n, "total_ms": round(ms, 4), "avg_us": round(avg * 1e3, 3),
-                   "algorithmic_bytes": int(b), "achieved_gbs": round(b / (avg * 1e-3) / 1e9, 1)}
+                   "algorithmic_bytes": int(b)}
         if grp == "krylov":
-            # replayed launches: scale their average to the Arnoldi iterations of the timed steps
-            kern[k]["timed_launches"] = evals - args.steps
-            kern[k]["est_total_ms"] = round(avg * (evals - args.steps), 4)
-            kern[k]["source"] = "stream-driver replay of the graph's kernels"
+            # replayed launches: their averages scaled to the graph's measured time, times
+            # the Arnoldi iterations of the timed steps
+            kern[k]["replay_avg_us"] = kern[k].pop("avg_us")
+            avg = avg * attr
+            kern[k]["avg_us"] = round(avg * 1e3, 3)
+            kern[k]["timed_launches"] = iters
+            kern[k]["est_total_ms"] = round(avg * iters, 4)
+            kern[k]["source"] = ("stream-driver replay of the graph's kernels, scaled by the graph time "
+                                 f"(factor {attr:.3f})")
+        kern[k]["achieved_gbs"] = round(b / (avg * 1e-3) / 1e9, 1)
         kern[k]["share_of_step"] = round(kern[k].get("est_total_ms", ms) / (t_dev * 1e3), 4)
     dom = max(kern, key=lambda k: kern[k].get("est_total_ms", kern[k]["total_ms"]))
     d = kern[dom]

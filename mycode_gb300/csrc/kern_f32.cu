@@ -75,8 +75,16 @@ void launch_convert<float>(long n, const double* in, float* out, cudaStream_t s)
 
 // ---- device-resident GMRES
 template <>
-void launch_gmres_v0<float>(long n, float* V0, const double* rhs, const GmresDev& d, cudaStream_t s) {
-    k_gmres_v0<float><<<red_grid(n), RED_THREADS, 0, s>>>(n, V0, rhs, d);
+void launch_gmres_start<float>(long n, float* V0, const double* rhs, const GmresDev& d, int m, double tol,
+                               cudaGraphConditionalHandle h, const double* bsq, cudaStream_t s) {
+    k_gmres_start<float><<<red_grid(n), RED_THREADS, 0, s>>>(n, V0, rhs, d, m, tol, h, bsq);
+}
+void launch_mixed_pre(int nv, const MeshView<float>& m, const Flow<float>& F, const double* U, const double* Ub,
+                      const double* W,
+                      const double* phi, const double* mut, const double* cfl, const double* dt_in, float* U32,
+                      float* phi32, float* dt32, double* D, float* Dinv32, cudaStream_t s) {
+    NV_SWITCH(nv, (k_mixed_pre<NVC><<<blocks_for(m.nc), tpb_for(m.nc), 0, s>>>(m, F, U, Ub, W, phi, mut, cfl, dt_in, U32,
+                                                                             phi32, dt32, D, Dinv32)));
 }
 template <>
 void launch_gmres_z<float>(int nv, long nc, const float* V, long L, const float* Dinv, float* z, const GmresDev& d,

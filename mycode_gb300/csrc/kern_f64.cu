@@ -81,6 +81,10 @@ void launch_fd_combine(int nv, long nc, const double* Rp, const double* Rb, cons
 void launch_norm_vm(int nv, long nc, const double* R, const double* vol, RedScratch rs, double* out3, cudaStream_t s) {
     NV_SWITCH(nv, (k_norm_vm<NVC><<<red_grid(nc), RED_THREADS, 0, s>>>(nc, R, vol, rs, out3)));
 }
+void launch_step_norms(int nv, long nc, const double* R, const double* vol, double* rhs, RedScratch rs, double* out4,
+                       int* flag, cudaStream_t s) {
+    NV_SWITCH(nv, (k_step_norms<NVC><<<red_grid(nc), RED_THREADS, 0, s>>>(nc, R, vol, rhs, rs, out4, flag)));
+}
 void launch_local_dt(int nv, const MeshView<double>& m, const Flow<double>& F, const double* U, const double* W,
                      double cfl, double* dt, cudaStream_t s) {
     NV_SWITCH(nv, (k_local_dt<NVC><<<blocks_for(m.nc), tpb_for(m.nc), 0, s>>>(m, F, U, W, cfl, dt)));
@@ -112,13 +116,11 @@ void launch_newton_update(int nv, long nc, double* U, const double* dU, double r
 }
 
 // ---- device-resident GMRES
-void launch_gmres_init(const GmresDev& d, int m, double tol, cudaGraphConditionalHandle h, cudaStream_t s) {
-    k_gmres_init<<<1, 1, 0, s>>>(d, m, tol, h);
-}
 void launch_gmres_backsub(const GmresDev& d, cudaStream_t s) { k_gmres_backsub<<<1, 1, 0, s>>>(d); }
 template <>
-void launch_gmres_v0<double>(long n, double* V0, const double* rhs, const GmresDev& d, cudaStream_t s) {
-    k_gmres_v0<double><<<red_grid(n), RED_THREADS, 0, s>>>(n, V0, rhs, d);
+void launch_gmres_start<double>(long n, double* V0, const double* rhs, const GmresDev& d, int m, double tol,
+                                cudaGraphConditionalHandle h, const double* bsq, cudaStream_t s) {
+    k_gmres_start<double><<<red_grid(n), RED_THREADS, 0, s>>>(n, V0, rhs, d, m, tol, h, bsq);
 }
 template <>
 void launch_gmres_z<double>(int nv, long nc, const double* V, long L, const double* Dinv, double* z, const GmresDev& d,

@@ -65,29 +65,6 @@ struct GmresDev {
     int in_graph;     // 1: the kernels run inside the WHILE graph and set its condition
 };
 
-// beta = sqrt(|rhs|^2); empty solve when beta < 1e-12 (src/Solver.cpp:1514-1516)
-static __global__ void k_gmres_init(GmresDev d, int m, double tol, cudaGraphConditionalHandle h) {
-    double b = sqrt(d.beta[2]);
-    d.beta[0] = b;
-    d.beta[1] = tol;
-    d.gi[0] = 0;
-    d.gi[3] = m;
-    for (int i = 0; i <= m; ++i) {
-        d.g[i] = 0.0;
-        d.sc[i] = 1.0;
-    }
-    for (int i = 0; i < m; ++i) { d.cs[i] = 0.0; d.sn[i] = 0.0; }
-    d.g[0] = b;
-    if (b < 1e-12) {
-        d.gi[1] = -1;
-        d.gi[2] = 1;
-        if (d.in_graph) cudaGraphSetConditional(h, 0);
-    } else {
-        d.gi[1] = 0;
-        d.gi[2] = 0;
-    }
-}
-
 // Arithmetic of the vector kernels.  On GB300 every FP64 warp instruction occupies its
 // SM sub-partition for about 64 cycles (measured: a dependent FMA chain runs at 61
 // cycles per FMA, a divide at 437, a square root at 684, whatever the number of active
@@ -219,12 +196,42 @@ __device__ __forceinline__ bool dots_finish(const GmresDev& d, int j, A (*wsum)[
     return true;
 }
 
-// V0 = rhs * (1/beta)
+// Start of a solve: every block takes beta = sqrt(beta^2) (from
+// *bsq when given, else d.beta[2]), block 0 initialises the solve state, and unless the
+// solve is empty (beta < 1e-12, src/Solver.cpp:1514-1516) V0 = rhs * (1/beta).
 template <class T>
-__global__ void k_gmres_v0(long n, T* V0, const double* rhs, GmresDev d) {
-    if (d.gi[2]) return;
+__global__ void k_gmres_start(long n, T* V0, const double* rhs, GmresDev d, int m, double tol,
+                              cudaGraphConditionalHandle h, const double* bsq) {
     __shared__ double ib;
-    if (threadIdx.x == 0) ib = 1.0 / d.beta[0];
+    const double b2 = bsq ? *bsq : d.beta[2];
+    const double b = sqrt(b2);
+    if (blockIdx.x == 0) {
+        for (int i = threadIdx.x; i <= m; i += blockDim.x) {
+            d.g[i] = i == 0 ? b : 0.0;
+            d.sc[i] = 1.0;
+            if (i < m) {
+                d.cs[i] = 0.0;
+                d.sn[i] = 0.0;
+            }
+        }
+        if (threadIdx.x == 0) {
+            d.beta[0] = b;
+            d.beta[1] = tol;
+            d.beta[2] = b2;
+            d.gi[0] = 0;
+            d.gi[3] = m;
+            if (b < 1e-12) {
+                d.gi[1] = -1;
+                d.gi[2] = 1;
+                if (d.in_graph) cudaGraphSetConditional(h, 0);
+            } else {
+                d.gi[1] = 0;
+                d.gi[2] = 0;
+            }
+        }
+    }
+    if (b < 1e-12) return;
+    if (threadIdx.x == 0) ib = 1.0 / b;
     __syncthreads();
     for (long q = (long)blockIdx.x * blockDim.x + threadIdx.x; q < n; q += (long)gridDim.x * blockDim.x)
         V0[q] = (T)(rhs[q] * ib);

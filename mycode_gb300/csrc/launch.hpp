@@ -81,6 +81,14 @@ void launch_fd_perturb(long n, const double* U, const double* v, const double* u
 void launch_fd_combine(int nv, long nc, const double* Rp, const double* Rb, const double* v, const double* eps,
                        const double* vol, const double* dt, double* Jv, cudaStream_t s);
 void launch_norm_vm(int nv, long nc, const double* R, const double* vol, RedScratch rs, double* out3, cudaStream_t s);
+// norm_vm pieces, sum R^2 (out4[3]) and rhs = -R in one pass; clears *flag
+void launch_step_norms(int nv, long nc, const double* R, const double* vol, double* rhs, RedScratch rs, double* out4,
+                       int* flag, cudaStream_t s);
+// the mixed-precision prologue of a Krylov solve (linalg.cuh k_mixed_pre; kern_f32.cu)
+void launch_mixed_pre(int nv, const MeshView<float>& m, const Flow<float>& F, const double* U, const double* Ub,
+                      const double* W,
+                      const double* phi, const double* mut, const double* cfl, const double* dt_in, float* U32,
+                      float* phi32, float* dt32, double* D, float* Dinv32, cudaStream_t s);
 void launch_local_dt(int nv, const MeshView<double>& m, const Flow<double>& F, const double* U, const double* W,
                      double cfl, double* dt, cudaStream_t s);
 // D: one plane per cell, three with SST (mean flow, k, w); mut: SST eddy viscosity or null
@@ -146,9 +154,10 @@ void launch_objective(int nv, int kind, int n, const int* slots, const double* w
 // ---- device-resident GMRES (krylov.cuh); T = float in kern_f32.cu, double in kern_f64.cu
 #include "krylov.cuh"
 namespace cfdg {
-void launch_gmres_init(const GmresDev& d, int m, double tol, cudaGraphConditionalHandle h, cudaStream_t s);
 void launch_gmres_backsub(const GmresDev& d, cudaStream_t s);
-template <class T> void launch_gmres_v0(long n, T* V0, const double* rhs, const GmresDev& d, cudaStream_t s);
+// solve state and V0 = rhs / |rhs| (|rhs|^2 from *bsq, or d.beta[2] when bsq is null)
+template <class T> void launch_gmres_start(long n, T* V0, const double* rhs, const GmresDev& d, int m, double tol,
+                                           cudaGraphConditionalHandle h, const double* bsq, cudaStream_t s);
 template <class T> void launch_gmres_dinv(int nv, long nc, const double* D, T* Dinv, cudaStream_t s);
 template <class T> void launch_gmres_z(int nv, long nc, const T* V, long L, const T* Dinv, T* z, const GmresDev& d,
                                        cudaStream_t s);

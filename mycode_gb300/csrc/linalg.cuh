@@ -234,6 +234,126 @@ __global__ void __launch_bounds__(RED_THREADS) k_norm_vm(long nc, const double* 
     grid_finish<3>(v, rs, out3);
 }
 
+// The residual reductions of a Newton step in one pass over R: the volume-weighted norm
+// pieces of k_norm_vm (same arithmetic), sum R^2 (as k_dot, summed in this kernel's own
+// order) into out4[0..3], and rhs = -R.  Clears *flag (the update's non-finite flag).
+template <int NV>
+__global__ void __launch_bounds__(RED_THREADS) k_step_norms(long nc, const double* __restrict__ R,
+                                                            const double* __restrict__ vol, double* __restrict__ rhs,
+                                                            RedScratch rs, double* out4, int* flag) {
+    if (blockIdx.x == 0 && threadIdx.x == 0) *flag = 0;
+    double v[4] = {0.0, 0.0, 0.0, 0.0};
+    for (long i = (long)blockIdx.x * blockDim.x + threadIdx.x; i < nc; i += (long)gridDim.x * blockDim.x) {
+        double vv = vol[i];
+        double s = 0.0, q = 0.0;
+#pragma unroll
+        for (int c = 0; c < NV; ++c) {
+            const double Rc = R[c * nc + i];
+            rhs[c * nc + i] = -Rc;
+            double r = Rc / vv;
+            s = (c == 0) ? r * r : s + r * r;
+            q += Rc * Rc;
+        }
+        double r0 = R[i] / vv;
+        v[0] += s * vv;
+        v[1] += vv;
+        v[2] += r0 * r0 * vv;
+        v[3] += q;
+    }
+    grid_finish<4>(v, rs, out4);
+}
+
+// The mixed-precision prologue of a Krylov solve in one pass per cell, FP32 arithmetic on
+// the FP64 state: U32 = Ub (the linearisation state), phi32 = phi; at the current state
+// U, W the local time step (k_local_dt's expression; from *cfl, or the given dt when
+// cfl is null) into dt32 and the diagonal preconditioner (k_precond's expression) into D
+// (FP64 storage) and its reciprocals into Dinv32.  The preconditioner and the
+// pseudo-time term only shape the FP32 linear system, whose J v is FP32 already.
+template <int NV>
+__global__ void __launch_bounds__(256) k_mixed_pre(MeshView<float> m, Flow<float> F, const double* __restrict__ U,
+                                                   const double* __restrict__ Ub,
+                                                   const double* __restrict__ W, const double* __restrict__ phi,
+                                                   const double* __restrict__ mut, const double* cfl,
+                                                   const double* __restrict__ dt_in, float* __restrict__ U32,
+                                                   float* __restrict__ phi32, float* __restrict__ dt32,
+                                                   double* __restrict__ D, float* __restrict__ Dinv32) {
+    long i = (long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= m.nc) return;
+    const long nc = m.nc;
+#pragma unroll
+    for (int c = 0; c < NV; ++c) U32[c * nc + i] = (float)Ub[c * nc + i];
+    phi32[i] = (float)phi[i];
+    int ek[4];
+#pragma unroll
+    for (int k = 0; k < 4; ++k) ek[k] = m.cf[(long)k * nc + i];
+    const float vol = m.vol[i];
+    float dt;
+    if (cfl) {
+        const float r = (float)U[i], ru = (float)U[nc + i], rv = (float)U[2 * nc + i];
+        const float c = sqrtf(F.gam * (float)W[3 * nc + i] / r);
+        float lam = 1e-12f;
+#pragma unroll
+        for (int k = 0; k < 4; ++k) {
+            const int e = ek[k];
+            if (e < 0) continue;
+            const int f = e >> 1;
+            const float un = (e & 1) ? (ru * (-m.nx[f]) + rv * (-m.ny[f])) / r : (ru * m.nx[f] + rv * m.ny[f]) / r;
+            lam += (fabsf(un) + c) * m.area[f];
+        }
+        dt = (float)*cfl * vol / lam;
+    } else {
+        dt = (float)dt_in[i];
+    }
+    dt32[i] = dt;
+    auto state = [&](long j) {
+        CS<float> q;
+        q.r = (float)U[j];
+        q.ru = (float)U[nc + j];
+        q.rv = (float)U[2 * nc + j];
+        q.rE = (float)U[3 * nc + j];
+        q.rk = NV == 6 ? (float)U[4 * nc + j] : 0.f;
+        q.rw = NV == 6 ? (float)U[5 * nc + j] : 0.f;
+        q.u = (float)W[W_U * nc + j];
+        q.v = (float)W[W_V * nc + j];
+        q.p = (float)W[W_P * nc + j];
+        return q;
+    };
+    float acc = 0.f;
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+        const int e = ek[k];
+        if (e < 0) continue;
+        const int f = e >> 1;
+        const int o = m.fo[f], n = m.fn[f];
+        const float nx = m.nx[f], ny = m.ny[f];
+        const CS<float> L = state(o);
+        const CS<float> Rr = n >= 0 ? state(n) : ghost_state(F, L, m.ftag[f], nx, ny);
+        const float g = F.gam;
+        const float cL = sqrtf(g * L.p / L.r);
+        const float cR = sqrtf(g * (Rr.p > 0 ? Rr.p : 1e-3f) / (Rr.r > 0 ? Rr.r : 1e-3f));
+        const float cf = 0.5f * (cL + cR);
+        const float vn = fabsf(0.5f * (L.u + Rr.u) * nx + 0.5f * (L.v + Rr.v) * ny);
+        const float li = vn + cf;
+        const float dx = sqrtf(m.vol[o]);
+        float mu = 0.5f * (L.r + Rr.r) * F.nu;
+        if (NV == 6 && mut) mu = mu + 0.5f * ((float)mut[o] + (float)mut[n >= 0 ? n : o]);
+        const float lv = 2.f * mu / (0.5f * (L.r + Rr.r) * dx + 1e-12f);
+        acc += (li + lv) * m.area[f] * 0.5f;
+    }
+    float d = vol / (dt + 1e-30f) + acc;
+    if (d < 1e-12f) d = 1e-12f;
+    D[i] = d;
+    Dinv32[i] = 1.f / d;
+    if (NV == 6) {
+        const float w = (float)W[W_W * nc + i];
+        const float dk = d + (float)SstConst::beta_s * w * vol, dw = d + 2.f * (float)SstConst::b1 * w * vol;
+        D[nc + i] = dk;
+        D[2 * nc + i] = dw;
+        Dinv32[nc + i] = 1.f / dk;
+        Dinv32[2 * nc + i] = 1.f / dw;
+    }
+}
+
 // computeLocalTimeStep (src/Solver.cpp:1388-1422) as a per-cell gather: each face
 // adds (|u_n| + c) A from the cell's own state, owner and neighbour with their own
 // expressions, summed in reference face order from 1e-12.

@@ -131,6 +131,7 @@ struct cfdg_solver {
     double* w64 = nullptr;
     cudaGraphExec_t gexec = nullptr;
     const void* gkey[4] = {nullptr, nullptr, nullptr, nullptr};
+    bool gnewton = false;  // the graph was built for newton_step_graph (enqueue_gmres_pre)
     int flow_version = 0, graph_version = -1;
     bool capturing = false;
     bool pdl_failed = false;  // the body would not build with programmatic dependent launch
@@ -553,28 +554,36 @@ struct cfdg_solver {
 
     // ---- device-resident GMRES: one graph per (Ubase, Rbase, rhs, x, flow parameters)
 
-    // preconditioner, FP32 copies, beta and V0 (graph prologue)
-    void enqueue_gmres_pre(double* Ubase, double* rhsd, cudaGraphConditionalHandle h) {
+    // preconditioner, FP32 copies, beta and V0 (graph prologue).  In a Newton step's graph
+    // (newton) the primitives W of U are current (the step's residual computed them), the
+    // step's reduction kernel has put |rhs|^2 in scal[11], and the mixed path takes its
+    // local time step from the CFL number in scal[12]; otherwise dt is the caller's.
+    void enqueue_gmres_pre(double* Ubase, double* rhsd, cudaGraphConditionalHandle h, bool newton) {
         const bool mixed = cfg.precision == CFDG_MIXED;
-        launch_prim64(nv, nc, F, f64(U), f64(W), st);
-        launch_precond(nv, mv, F, U, W, dt, D, Tt, st);
-        if (mixed) launch_gmres_dinv<float>(nv, nc, D, dinv32, st);
-        else launch_gmres_dinv<double>(nv, nc, D, dinv64, st);
-        launches += 3;
-        if (mixed) {
-            launch_convert<float>(L, Ubase, U32, st);
-            launch_convert<float>(nc, phi, phi32, st);
-            launch_convert<float>(nc, dt, dt32, st);
-            launches += 3;
-        } else if (cfg.jv == CFDG_JV_FD) {
-            launch_dot<double>(nv, nc, Ubase, Ubase, rs, scal + 0, st);
+        if (!newton) {
+            launch_prim64(nv, nc, F, f64(U), f64(W), st);
             ++launches;
         }
-        launch_dot<double>(nv, nc, rhsd, rhsd, rs, gd.beta + 2, st);
-        launch_gmres_init(gd, cfg.gmres_m, cfg.gmres_tol, h, st);
-        if (mixed) launch_gmres_v0<float>(L, V32, rhsd, gd, st);
-        else launch_gmres_v0<double>(L, V, rhsd, gd, st);
-        launches += 3;
+        if (mixed) {
+            launch_mixed_pre(nv, mvf, Ff, U, Ubase, W, phi, nv == 6 ? Tt : nullptr, newton ? scal + 12 : nullptr, dt,
+                             U32, phi32, dt32, D, dinv32, st);
+            ++launches;
+        } else {
+            launch_precond(nv, mv, F, U, W, dt, D, Tt, st);
+            launch_gmres_dinv<double>(nv, nc, D, dinv64, st);
+            launches += 2;
+            if (cfg.jv == CFDG_JV_FD) {
+                launch_dot<double>(nv, nc, Ubase, Ubase, rs, scal + 0, st);
+                ++launches;
+            }
+        }
+        if (!newton) {
+            launch_dot<double>(nv, nc, rhsd, rhsd, rs, gd.beta + 2, st);
+            ++launches;
+        }
+        if (mixed) launch_gmres_start<float>(L, V32, rhsd, gd, cfg.gmres_m, cfg.gmres_tol, h, newton ? scal + 11 : nullptr, st);
+        else launch_gmres_start<double>(L, V, rhsd, gd, cfg.gmres_m, cfg.gmres_tol, h, newton ? scal + 11 : nullptr, st);
+        ++launches;
     }
 
     // one Arnoldi iteration (graph WHILE body)
@@ -691,19 +700,19 @@ struct cfdg_solver {
         launches += 2;
     }
 
-    cfdg_status build_gmres_graph(double* Ubase, double* Rbase, double* rhsd, double* xout) {
-        cfdg_status e = build_gmres_graph_once(Ubase, Rbase, rhsd, xout);
+    cfdg_status build_gmres_graph(double* Ubase, double* Rbase, double* rhsd, double* xout, bool newton) {
+        cfdg_status e = build_gmres_graph_once(Ubase, Rbase, rhsd, xout, newton);
         if (e != CFDG_OK && cfg.pdl && !pdl_failed) {
             // no programmatic dependent launch inside a conditional body on this driver:
             // build the body with plain launches
             pdl_failed = true;
             cudaGetLastError();
-            e = build_gmres_graph_once(Ubase, Rbase, rhsd, xout);
+            e = build_gmres_graph_once(Ubase, Rbase, rhsd, xout, newton);
         }
         return e;
     }
 
-    cfdg_status build_gmres_graph_once(double* Ubase, double* Rbase, double* rhsd, double* xout) {
+    cfdg_status build_gmres_graph_once(double* Ubase, double* Rbase, double* rhsd, double* xout, bool newton) {
         // the captured kernels take GmresDev by value: they must be the graph's variant,
         // whose Givens step ends the WHILE loop
         gd.in_graph = 1;
@@ -728,7 +737,7 @@ struct cfdg_solver {
         capturing = true;
         e = cudaStreamBeginCaptureToGraph(st, G, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal);
         if (e != cudaSuccess) goto cuda_fail;
-        enqueue_gmres_pre(Ubase, rhsd, h);
+        enqueue_gmres_pre(Ubase, rhsd, h, newton);
         e = cudaStreamGetCaptureInfo(st, &cs, nullptr, nullptr, &deps, nullptr, &nd);
         if (e == cudaSuccess) leaf.assign(deps, deps + nd);
         {
@@ -775,6 +784,7 @@ struct cfdg_solver {
             return fail(CFDG_ERR_CUDA, std::string("GMRES graph instantiation: ") + cudaGetErrorString(e));
         }
         gkey[0] = Ubase; gkey[1] = Rbase; gkey[2] = rhsd; gkey[3] = xout;
+        gnewton = newton;
         graph_version = flow_version;
         return CFDG_OK;
     cuda_fail:
@@ -790,7 +800,7 @@ struct cfdg_solver {
         TRY(ensure_krylov());
         gd.in_graph = 0;
         cudaGraphConditionalHandle none = 0;
-        enqueue_gmres_pre(Ubase, rhsd, none);
+        enqueue_gmres_pre(Ubase, rhsd, none, false);
         int done = 0;
         CK(cudaMemcpyAsync(&done, gd.gi + 2, sizeof(int), cudaMemcpyDeviceToHost, st));
         CK(cudaStreamSynchronize(st));
@@ -817,8 +827,8 @@ struct cfdg_solver {
     cfdg_status gmres_graph(double* Ubase, double* Rbase, double* rhsd, double* xout, int* iters) {
         TRY(ensure_krylov());
         if (!gexec || graph_version != flow_version || gkey[0] != Ubase || gkey[1] != Rbase || gkey[2] != rhsd ||
-            gkey[3] != xout)
-            TRY(build_gmres_graph(Ubase, Rbase, rhsd, xout));
+            gkey[3] != xout || gnewton)
+            TRY(build_gmres_graph(Ubase, Rbase, rhsd, xout, false));
         CK(cudaGraphLaunch(gexec, st));
         int* hi = reinterpret_cast<int*>(hpin + 4);
         hi[2] = 0;
@@ -1069,24 +1079,29 @@ struct cfdg_solver {
         double t0 = now_s();
         *converged = 0;
         TRY(ensure_krylov());
-        if (!gexec || graph_version != flow_version || gkey[0] != U || gkey[1] != R || gkey[2] != rhs || gkey[3] != x) {
+        if (!gexec || graph_version != flow_version || gkey[0] != U || gkey[1] != R || gkey[2] != rhs || gkey[3] != x ||
+            !gnewton) {
             CK(cudaStreamSynchronize(st));
-            TRY(build_gmres_graph(U, R, rhs, x));
+            TRY(build_gmres_graph(U, R, rhs, x, true));
         }
+        const bool mixed = cfg.precision == CFDG_MIXED;
         if (timing) CK(cudaEventRecord(step_ev[0], st));
-        launch_prim64(nv, nc, F, f64(U), f64(W), st);
-        launch_local_dt(nv, mv, F, U, W, cfl, dt, st);
-        launches += 2;
+        if (mixed) {  // the graph's mixed prologue takes the local time step from scal[12]
+            hpin[6] = cfl;
+            CK(cudaMemcpyAsync(scal + 12, hpin + 6, sizeof(double), cudaMemcpyHostToDevice, st));
+        }
         bool upd = !(step > cfg.limiter_freeze_step || cfl > cfg.limiter_freeze_cfl);
-        TRY(residual_dev(U, R, upd ? 1 : 0));
-        launch_norm_vm(nv, nc, R, g64.vol, rs, scal + 8, st);
-        launch_dot<double>(nv, nc, R, R, rs, scal + 11, st);
-        launch_scale_from<double>(L, rhs, R, scal + 6, 0, st);  // rhs = -R (scal[6] holds -1)
-        launches += 3;
+        TRY(residual_dev(U, R, upd ? 1 : 0));  // also the primitives W of U
+        if (!mixed) {
+            launch_local_dt(nv, mv, F, U, W, cfl, dt, st);
+            ++launches;
+        }
+        // norms, |R|^2 and rhs = -R in one pass; also clears the update's non-finite flag
+        launch_step_norms(nv, nc, R, g64.vol, rhs, rs, scal + 8, bad, st);
+        ++launches;
         if (timing) CK(cudaEventRecord(step_ev[2], st));
         CK(cudaGraphLaunch(gexec, st));
         if (timing) CK(cudaEventRecord(step_ev[3], st));
-        CK(cudaMemsetAsync(bad, 0, sizeof(int), st));
         launch_newton_update_dev(nv, nc, U, x, scal + 8, tol, cfg.gamma, F.w_inf * SstConst::w_min_frac, bad, st);
         ++launches;
         CK(cudaMemcpyAsync(hpin, scal + 8, 4 * sizeof(double), cudaMemcpyDeviceToHost, st));
@@ -1575,7 +1590,7 @@ cfdg_status cfdg_solver_create(const cfdg_mesh* m, const cfdg_config* cfg, cfdg_
         TRYS(dalloc(&s->G32, (size_t)NG * nc)); TRYS(dalloc(&s->G32d, (size_t)NG * nc));
         TRYS(dalloc(&s->FA32d, (size_t)nv * nf)); TRYS(dalloc(&s->phi32, nc)); TRYS(dalloc(&s->dt32, nc));
     }
-    TRYS(dalloc(&s->rs.partial, 3 * (size_t)RED_BLOCKS));
+    TRYS(dalloc(&s->rs.partial, 4 * (size_t)RED_BLOCKS));
     TRYS(dalloc(&s->rs.counter, 1));
     TRYS(dalloc(&s->scal, 16 + (size_t)(c.gmres_m + 2) * (c.gmres_m + 2) + 8));
     TRYS(dalloc(&s->bad, 1));
