@@ -148,19 +148,23 @@ def measured_peak():
         return 6800.0, "fallback"
 
 
-def profile_traffic(kernel_class: str):
-    """DRAM bytes per launch of a kernel class from the committed ncu summary, if any."""
+def profile_traffic(kernel_class: str, jbar: float = 0.0):
+    """DRAM bytes per launch of a kernel class from the committed ncu summary
+    (profiles/traffic.txt: bytes at Arnoldi iteration 0 and per further basis vector),
+    evaluated at the mean iteration jbar; None when the class is not listed."""
     path = os.path.join(ROOT, "profiles", "traffic.txt")
     if not os.path.exists(path):
         return None
     with open(path) as fh:
         for line in fh:
             parts = line.split()
-            if len(parts) >= 2 and parts[0] == kernel_class:
+            if len(parts) >= 2 and not parts[0].startswith("#") and parts[0] == kernel_class:
                 try:
-                    return float(parts[1])
+                    base = float(parts[1])
+                    per = float(parts[2]) if len(parts) > 2 else 0.0
                 except ValueError:
                     return None
+                return round(base + per * jbar)
     return None
 
 
@@ -372,7 +376,7 @@ def ours(args):
         kern[k]["share_of_step"] = round(kern[k].get("est_total_ms", ms) / (t_dev * 1e3), 4)
     dom = max(kern, key=lambda k: kern[k].get("est_total_ms", kern[k]["total_ms"]))
     d = kern[dom]
-    traffic = profile_traffic(dom)
+    traffic = profile_traffic(dom, jbar)
     roofline = {"bound": "hbm", "kernel": dom, "achieved": d["achieved_gbs"], "peak": peak, "unit": "GB/s",
                 "frac": round(d["achieved_gbs"] / peak, 4), "peak_source": f"{peak_kind} (MEASURED_PEAKS.json hbm_gbs)"
                 if peak_kind == "measured" else "fallback 6.8 TB/s",

@@ -82,6 +82,29 @@ def test_graph_newton_solve_matches_host_driver(cuda_lib):
     np.testing.assert_allclose(b, a, rtol=1e-3)
 
 
+@pytest.mark.parametrize("precision", ["mixed", "fp64"])
+def test_graph_newton_step_norm_and_update(cuda_lib, precision):
+    """One graph Newton step: the norm that its fused reduction kernel takes of R (with
+    |R|^2 and rhs = -R in the same pass) is the volume-weighted norm of R bit for bit, and
+    its update (the mixed path's time step and preconditioner computed in FP32 inside the
+    graph) follows the host-driven step to the GMRES tolerance."""
+    out = {}
+    for kry in (0, 1):
+        s, spec, case = _solver(cuda_lib, "supersonic", precision=precision, jv="exact", krylov=kry)
+        o = OracleSolver(spec, bcset=case["bcset"], viscous=case["viscous"], init=case["init"])
+        C.setup(o, case)
+        U = C.perturbed_state(o.get_state(), o.cells(), seed=16)
+        s.setNumericalMethod("ROE", "SECOND_ORDER_LIMITED")
+        s.set_state(U)
+        ref = s.norm_vm(s.computeResiduals(U))
+        s.set_state(U)
+        rec, _ = s.newton_step(0.0)
+        assert rec.res_vm == ref
+        out[kry] = s.getSolution() - U
+    d0, d1 = out[0], out[1]
+    assert np.linalg.norm(d1 - d0) <= 5e-2 * np.linalg.norm(d0)
+
+
 @pytest.mark.parametrize("name", ["supersonic", "plate_visc"])
 @pytest.mark.parametrize("precision,jv", [("mixed", "exact"), ("fp64", "exact"), ("fp64", "fd")])
 def test_stream_driver_is_the_graph_bit_for_bit(cuda_lib, name, precision, jv):
