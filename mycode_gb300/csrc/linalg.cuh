@@ -219,14 +219,14 @@ __global__ void __launch_bounds__(RED_THREADS) k_norm_vm(long nc, const double* 
                                                          const double* __restrict__ vol, RedScratch rs, double* out3) {
     double v[3] = {0.0, 0.0, 0.0};
     for (long i = (long)blockIdx.x * blockDim.x + threadIdx.x; i < nc; i += (long)gridDim.x * blockDim.x) {
-        double vv = vol[i];
+        double vv = vol[i], iv = 1.0 / vv;  // the quotients by one reciprocal (quot_by_recip)
         double s = 0.0;
 #pragma unroll
         for (int c = 0; c < NV; ++c) {
-            double r = R[c * nc + i] / vv;
+            double r = quot_by_recip(R[c * nc + i], vv, iv);
             s = (c == 0) ? r * r : s + r * r;
         }
-        double r0 = R[i] / vv;
+        double r0 = quot_by_recip(R[i], vv, iv);
         v[0] += s * vv;
         v[1] += vv;
         v[2] += r0 * r0 * vv;
@@ -244,17 +244,17 @@ __global__ void __launch_bounds__(RED_THREADS) k_step_norms(long nc, const doubl
     if (blockIdx.x == 0 && threadIdx.x == 0) *flag = 0;
     double v[4] = {0.0, 0.0, 0.0, 0.0};
     for (long i = (long)blockIdx.x * blockDim.x + threadIdx.x; i < nc; i += (long)gridDim.x * blockDim.x) {
-        double vv = vol[i];
+        double vv = vol[i], iv = 1.0 / vv;  // the quotients by one reciprocal (quot_by_recip)
         double s = 0.0, q = 0.0;
 #pragma unroll
         for (int c = 0; c < NV; ++c) {
             const double Rc = R[c * nc + i];
             rhs[c * nc + i] = -Rc;
-            double r = Rc / vv;
+            double r = quot_by_recip(Rc, vv, iv);
             s = (c == 0) ? r * r : s + r * r;
             q += Rc * Rc;
         }
-        double r0 = R[i] / vv;
+        double r0 = quot_by_recip(R[i], vv, iv);
         v[0] += s * vv;
         v[1] += vv;
         v[2] += r0 * r0 * vv;

@@ -19,6 +19,21 @@ enum FluxScheme { FLUX_LLF = 0, FLUX_ROE = 1, FLUX_HLLC = 2, FLUX_AUSM = 3 };
 enum SpatialScheme { SP_FIRST = 0, SP_CENTRAL = 1, SP_LIMITED = 2 };
 enum BcSet { BC_BUMP = 0, BC_SUPERSONIC = 1, BC_PLATE = 2 };
 
+// a / b correctly rounded, from y = RN(1/b): q = RN(a y) is within an ulp of a / b, the
+// remainder a - b q is exact under an FMA, and RN(q + (a - b q) y) = RN(a / b) (Markstein's
+// theorem: P. Markstein, IBM J. Res. Dev. 34(1), 1990).  Finite operands without
+// underflow; a = -0 would give +0 (sums that start from +0 never are -0).  Several
+// quotients by one b then cost one divide and three FP64 operations each, where a GB300
+// FP64 divide costs about seven.
+CFD_HD double quot_by_recip(double a, double b, double y) {
+    const double q = a * y;
+    return fma(fma(-q, b, a), y, q);
+}
+// a / b by the reciprocal y = 1 / b for FP64 (the same bits as the division), plain
+// division for the other scalar types
+template <class S, class R> CFD_HD S div_shared(S a, R b, R) { return a / b; }
+CFD_HD double div_shared(double a, double b, double y) { return quot_by_recip(a, b, y); }
+
 // libstdc++'s std::max / std::min selection rule (NaN behaviour included)
 template <class S> CFD_HD S smax(S a, S b) { return (val(a) < val(b)) ? b : a; }
 template <class S> CFD_HD S smin(S a, S b) { return (val(b) < val(a)) ? b : a; }

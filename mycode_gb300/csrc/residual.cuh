@@ -216,10 +216,11 @@ __device__ __forceinline__ void grad_item(const MeshView<R>& m, const Flow<R>& F
         }
     }
     R vol = m.vol[i];
+    const R ivol = R(1.0) / vol;  // FP64: the ten quotients by one reciprocal (div_shared)
     // gradient planes are in CellGradient order rho, u, v, p, T (= primitive order)
 #pragma unroll
     for (int q = 0; q < 2 * NQ; ++q) {
-        acc[q] = acc[q] / vol;
+        acc[q] = div_shared(acc[q], vol, ivol);
         Acc<S>::st(G, q, i, acc[q]);
     }
     if (!do_limiter) return;
