@@ -81,11 +81,12 @@ CFD_HD Flux6<S> face_flux(const Flow<R>& F, const CS<S>& L, const CS<S>& Rn, boo
         if (!interior && tag == 4) {
             R dx = g.dxL, dy = g.dyL;
             R d2 = dx * dx + dy * dy;
+            const R id2 = R(1.0) / d2;  // FP64: four quotients by one reciprocal (div_shared)
             S uc = L.u, vc = L.v;
-            dudx = -uc * dx / d2;
-            dudy = -uc * dy / d2;
-            dvdx = -vc * dx / d2;
-            dvdy = -vc * dy / d2;
+            dudx = div_shared(-uc * dx, d2, id2);
+            dudy = div_shared(-uc * dy, d2, id2);
+            dvdx = div_shared(-vc * dx, d2, id2);
+            dvdy = div_shared(-vc * dy, d2, id2);
             dTdx = S(R(0.0));
             dTdy = S(R(0.0));
         } else {
@@ -97,13 +98,14 @@ CFD_HD Flux6<S> face_flux(const Flow<R>& F, const CS<S>& L, const CS<S>& Rn, boo
             dTdy = R(0.5) * (gL[FG_T + 1] + gRv[FG_T + 1]);
             R d2 = g.dxlr * g.dxlr + g.dylr * g.dylr;
             if (d2 > R(1e-14)) {
+                const R id2 = R(1.0) / d2;  // FP64: four quotients by one reciprocal (div_shared)
                 S du = Rt.u - L.u;
                 S dv = Rt.v - L.v;
                 S a0 = dudx, b0 = dudy, c0 = dvdx, e0 = dvdy;
-                dudx = a0 - (a0 * g.dxlr + b0 * g.dylr - du) * g.dxlr / d2;
-                dudy = b0 - (a0 * g.dxlr + b0 * g.dylr - du) * g.dylr / d2;
-                dvdx = c0 - (c0 * g.dxlr + e0 * g.dylr - dv) * g.dxlr / d2;
-                dvdy = e0 - (c0 * g.dxlr + e0 * g.dylr - dv) * g.dylr / d2;
+                dudx = a0 - div_shared((a0 * g.dxlr + b0 * g.dylr - du) * g.dxlr, d2, id2);
+                dudy = b0 - div_shared((a0 * g.dxlr + b0 * g.dylr - du) * g.dylr, d2, id2);
+                dvdx = c0 - div_shared((c0 * g.dxlr + e0 * g.dylr - dv) * g.dxlr, d2, id2);
+                dvdy = e0 - div_shared((c0 * g.dxlr + e0 * g.dylr - dv) * g.dylr, d2, id2);
             }
         }
         R Cp = F.gam * F.Rgas / (F.gam - R(1.0));
