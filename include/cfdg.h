@@ -253,8 +253,9 @@ cfdg_status cfdg_entropy_error(cfdg_solver* s, double* err);
 /* R(U_current) into the solver's device residual */
 cfdg_status cfdg_residual_device(cfdg_solver* s, int update_limiters);
 cfdg_status cfdg_synchronize(cfdg_solver* s);
-/* timing on: CUDA events around every kernel of every residual and exact-J v
- * evaluation and around each Newton step (cfdg_step.device_ms) */
+/* timing: 0 off; 1 CUDA events around every kernel of every residual and exact-J v
+ * evaluation and around each Newton step (cfdg_step.device_ms, krylov_ms); 2 around each
+ * Newton step only (no events between its kernels) */
 cfdg_status cfdg_set_timing(cfdg_solver* s, int on);
 /* per-kernel times of the last timed residual evaluation */
 cfdg_status cfdg_kernel_times(cfdg_solver* s, double* ms_prim, double* ms_grad, double* ms_flux, double* ms_gather);

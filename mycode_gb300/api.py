@@ -285,10 +285,17 @@ class Solver:
     def set_state(self, U):
         _check(lib().cfdg_set_state(self._h, np.ascontiguousarray(U, np.float64).ravel()))
 
-    def getSolution(self):
-        U = np.zeros(6 * self.n_cells)
-        _check(lib().cfdg_get_state(self._h, U))
-        return U.reshape(-1, 6)
+    def getSolution(self, out=None):
+        """The state in the reference's AoS layout (n_cells x 6); into ``out`` (a C-contiguous
+        float64 array of that size, e.g. pinned host memory) when given."""
+        if out is None:
+            U = np.zeros(6 * self.n_cells)
+            _check(lib().cfdg_get_state(self._h, U))
+            return U.reshape(-1, 6)
+        if out.dtype != np.float64 or not out.flags["C_CONTIGUOUS"] or out.size != 6 * self.n_cells:
+            raise ValueError("getSolution: out must be a C-contiguous float64 array of n_cells x 6")
+        _check(lib().cfdg_get_state(self._h, out.reshape(-1)))
+        return out
 
     get_state = getSolution
 
@@ -434,7 +441,9 @@ class Solver:
         _check(lib().cfdg_synchronize(self._h))
 
     def set_timing(self, on=True):
-        _check(lib().cfdg_set_timing(self._h, int(on)))
+        """True: events around every kernel and every Newton step; "steps": around each
+        Newton step only; False: off."""
+        _check(lib().cfdg_set_timing(self._h, 2 if on == "steps" else int(bool(on))))
 
     def kernel_times(self):
         v = [C.c_double() for _ in range(4)]

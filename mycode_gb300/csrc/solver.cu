@@ -170,7 +170,8 @@ struct cfdg_solver {
 
     // nint + 1 events bracketing nint consecutive kernels of stat classes base..base+nint-1
     cudaEvent_t* take_events(int base, int nint = 4) {
-        if (!timing || capturing) return nullptr;  // event nodes are not allowed in graph bodies
+        // per-kernel events at timing level 1 only; event nodes are not allowed in graph bodies
+        if (timing != 1 || capturing) return nullptr;
         while (pool_used + nint + 1 > pool.size()) {
             cudaEvent_t e;
             if (cudaEventCreate(&e) != cudaSuccess) return nullptr;
