@@ -47,7 +47,8 @@ constexpr int KRY_MAXM = 128;  // largest Krylov dimension of the device solver
 constexpr int KRY_BODY_ITERS = 4;
 
 struct GmresDev {
-    int* gi;          // [0] j, [1] k (last iteration), [2] done, [3] m (16-byte aligned)
+    int* gi;          // [0] j (FD body), [1] k (last iteration), [2] done, [3] m, [4] this iteration
+                      // (exact J v body), [5] updates completed (exact J v body); 16-byte aligned
     double* beta;     // [0] beta, [1] tol, [2] beta^2
     double* g;        // [m+1]
     double* cs;       // [m]
@@ -61,6 +62,7 @@ struct GmresDev {
     double* partial;  // [(KRY_MAXM+1) * RED_BLOCKS]
     double* partial1; // [(KRY_MAXM+1) * RED_BLOCKS] block partials of h1 (exact J v body)
     int nb1;          // blocks of the gather kernel that writes partial1
+    int nb2;          // blocks of the update kernel that writes partial (exact J v body)
     unsigned* counter;
     int in_graph;     // 1: the kernels run inside the WHILE graph and set its condition
 };
@@ -220,6 +222,8 @@ __global__ void k_gmres_start(long n, T* V0, const double* rhs, GmresDev d, int 
             d.beta[2] = b2;
             d.gi[0] = 0;
             d.gi[3] = m;
+            d.gi[4] = 0;
+            d.gi[5] = 0;
             if (b < 1e-12) {
                 d.gi[1] = -1;
                 d.gi[2] = 1;
@@ -263,35 +267,156 @@ __global__ void k_gmres_z(long nc, const T* V, long L, const T* __restrict__ Din
     }
 }
 
-// For j > 0 first the deferred end of the previous iteration's orthogonalisation,
-// V_j = w - sum_{i<j} h2[i] sc[i] V_i (stored unnormalised; sc[j] is already set), then
-// z = V_j * (1/D) fused with the primitive stage of the dual J v: W.v, W.d of (U, z)
+// The Givens step for Hessenberg column j (src/Solver.cpp:1550-1588), run by one full
+// warp.  Each FP64 warp instruction costs ~64 cycles on GB300 whatever the active lanes,
+// so the work is spread over the lanes: the previous rotations applied to the new column
+// are the affine recurrence carry_{i+1} = -s_i carry_i + c_i col[i+1] (carry_0 = col[0]),
+// evaluated as a parallel prefix over 32 rotations at a time (compositions of affine
+// maps, Kogge-Stone), and out[i] = c_i carry_i + s_i col[i+1] by every lane at once.  The
+// new rotation takes c = a / sqrt(a^2 + b^2) as a * rsqrt(a^2 + b^2).  col[0..j] holds
+// h1 + h2, hv = |V_{j+1}|, hsq = hv^2.  Ends the solve (done flag, loop condition) on
+// convergence or when j + 1 reaches m.
+__device__ __forceinline__ void givens_column(const GmresDev& d, int j, int m, double* col, double hv, double hsq,
+                                              cudaGraphConditionalHandle hnd) {
+    __shared__ double hout[KRY_MAXM + 2];
+    const unsigned full = 0xffffffffu;
+    const int lane = threadIdx.x & 31;
+    double carry = col[0];
+    for (int base = 0; base < j; base += 32) {
+        const int i = base + lane;
+        const bool act = i < j;
+        const double ci = act ? d.cs[i] : 1.0, si = act ? d.sn[i] : 0.0, nx = act ? col[i + 1] : 0.0;
+        const double snx = si * nx;
+        double fa = act ? -si : 1.0, fb = act ? ci * nx : 0.0;  // f_i(x) = fa x + fb
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const double ap = __shfl_up_sync(full, fa, o), bp = __shfl_up_sync(full, fb, o);
+            if (lane >= o) {
+                fb = fma(fa, bp, fb);
+                fa = fa * ap;
+            }
+        }
+        const double cnext = fma(fa, carry, fb);        // carry after rotation i
+        double cprev = __shfl_up_sync(full, cnext, 1);  // carry before rotation i
+        if (lane == 0) cprev = carry;
+        if (act) hout[i] = fma(ci, cprev, snx);
+        carry = __shfl_sync(full, cnext, 31);
+    }
+    if (lane == 0) {
+        const double a = carry, b = hv;
+        double c, sn;
+        if (fabs(b) < 1e-14) {
+            c = 1.0;
+            sn = 0.0;
+            hout[j] = a;
+        } else {
+            const double q = fma(a, a, hsq), rq = rsqrt(q);
+            c = a * rq;
+            sn = b * rq;
+            hout[j] = q * rq;
+        }
+        hout[j + 1] = 0.0;
+        d.cs[j] = c;
+        d.sn[j] = sn;
+        const double gj = d.g[j];
+        d.g[j + 1] = -sn * gj;
+        d.g[j] = c * gj;
+        const bool conv = fabs(-sn * gj) < d.beta[1] * d.beta[0];
+        if (conv || j + 1 >= m) {
+            d.gi[1] = j;
+            d.gi[2] = 1;
+            if (d.in_graph) cudaGraphSetConditional(hnd, 0);
+        }
+    }
+    __syncwarp();
+    double* Hc = d.H + (long)j * (m + 1);
+    for (int i = lane; i <= j + 1; i += 32) Hc[i] = hout[i];
+}
+
+// First kernel of an Arnoldi iteration (exact J v body).  At iteration jn > 0 it first
+// finishes iteration jn - 1: every block sums the update kernel's block partials of h2 and
+// |w|^2, takes |V_jn|^2 = |w|^2 - |h2|^2 (clamped at 0; sc[jn] = 1/|V_jn|, or 1 under the
+// breakdown guard |.| <= 1e-12 of src/Solver.cpp:1553-1558) and forms V_jn = w - sum_{k<jn}
+// h2[k] sc[k] V_k (stored unnormalised) for its cells; one extra block runs the Givens
+// step of column jn - 1 meanwhile and records sc[jn] and this iteration's index for the
+// gather and update kernels.  Then z = V_jn * (1/D) and the primitive stage of the dual
+// J v: W.v, W.d of (U, z).  The iteration after the last one runs only this finishing
+// part (the Givens step raises the done flag; the other kernels then return at once).
 template <class T, int NV>
 __global__ void __launch_bounds__(256) k_gmres_prim_z(int nc, Flow<T> F, const T* __restrict__ U, T* V, long L,
                                                       const T* __restrict__ Dinv, T* __restrict__ z, Field<T> W,
-                                                      const T* __restrict__ w, GmresDev d) {
+                                                      const T* __restrict__ w, GmresDev d,
+                                                      cudaGraphConditionalHandle hnd) {
     typedef typename KryAcc<T>::type A;
-    const int4 gi4 = *reinterpret_cast<const int4*>(d.gi);  // j and the done flag in one load
-    if (gi4.z) return;  // the solve finished in an earlier iteration of an unrolled body
-    pdl_trigger();      // first kernel of the body: the gradient kernel may launch now
-    const int j = gi4.x;
+    const int4 ga = *reinterpret_cast<const int4*>(d.gi);
+    const int4 gb = *reinterpret_cast<const int4*>(d.gi + 4);
+    if (ga.z) return;  // the solve has ended
+    pdl_trigger();     // the gradient kernel may launch now
+    const int jn = gb.y, m = ga.w;
     __shared__ A hs[KRY_MAXM];
-    if (j > 0) {
-        for (int k = threadIdx.x; k < j; k += blockDim.x) hs[k] = (A)(d.h2[k] * d.sc[k]);
+    __shared__ double h2s[KRY_MAXM + 1], col[KRY_MAXM + 2];
+    __shared__ double scn, hv_s, hsq_s;
+    const bool givens_block = blockIdx.x == gridDim.x - 1;
+    if (jn > 0) {
+        // dots 0..jn in windows of at most blockDim.x (partials_sum's limit)
+        for (int base = 0; base <= jn; base += blockDim.x) {
+            const int nd = jn + 1 - base < (int)blockDim.x ? jn + 1 - base : (int)blockDim.x;
+            int G;
+            const A sg = partials_sum(reinterpret_cast<const A*>(d.partial) + (long)base * RED_BLOCKS, nd, d.nb2, &G);
+            const int i = base + (int)threadIdx.x / G;
+            if ((int)threadIdx.x / G < nd && threadIdx.x % G == 0)
+                h2s[i] = (i == jn ? 1.0 : d.sc[i]) * (double)sg;  // h2s[jn]: |w|^2
+        }
+        __syncthreads();
+        if (threadIdx.x < 32) {
+            A s2p = A(0);
+            for (int k = threadIdx.x; k < jn; k += 32) {
+                const A h = (A)h2s[k];
+                s2p += h * h;  // |h2|^2 in the basis precision (it is ~1e-14 of |w|^2)
+            }
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1) s2p += __shfl_xor_sync(0xffffffffu, s2p, o);
+            if (threadIdx.x == 0) {
+                const double hsq = fmax(h2s[jn] - (double)s2p, 0.0);
+                const double r = hsq > 0.0 ? rsqrt(hsq) : 0.0;
+                const double hv = hsq * r;
+                hsq_s = hsq;
+                hv_s = hv;
+                scn = hv > 1e-12 ? r : 1.0;
+            }
+        }
+        for (int k = threadIdx.x; k < jn; k += blockDim.x) hs[k] = (A)(h2s[k] * d.sc[k]);
         __syncthreads();
     }
-    long i = (long)blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= nc) return;
-    T* Vj = V + (long)j * L;
-    const T sj = (T)d.sc[j];
+    if (givens_block) {
+        if (jn > 0 && threadIdx.x < 32) {
+            const int j = jn - 1;
+            for (int i = threadIdx.x; i <= j; i += 32) {
+                col[i] = d.h1[i] + h2s[i];
+                d.h2[i] = h2s[i];
+            }
+            __syncwarp();
+            if (threadIdx.x == 0) {
+                d.sc[jn] = scn;
+                d.hsq[1] = hsq_s;
+            }
+            givens_column(d, j, m, col, hv_s, hsq_s, hnd);
+        }
+        if (threadIdx.x == 0) d.gi[4] = jn;
+        return;
+    }
+    T* Vj = V + (long)jn * L;
+    const T sj = jn > 0 ? (T)scn : (T)d.sc[0];
+    const long cstride = (long)(gridDim.x - 1) * blockDim.x;  // the cell blocks, grid-stride
+    for (long i = (long)blockIdx.x * blockDim.x + threadIdx.x; i < nc; i += cstride) {
     const T a = Dinv[i];
     T vj[NV];
-    if (j > 0) {
+    if (jn > 0) {
         A acc[NV];
 #pragma unroll
         for (int c = 0; c < NV; ++c) acc[c] = (A)w[c * nc + i];
 #pragma unroll 2
-        for (int k = 0; k < j; ++k) {
+        for (int k = 0; k < jn; ++k) {
             const T* Vk = V + (long)k * L;
             const A hk = hs[k];
 #pragma unroll
@@ -315,6 +440,7 @@ __global__ void __launch_bounds__(256) k_gmres_prim_z(int nc, Flow<T> F, const T
     }
     if (NV == 4) u[4] = u[5] = Dual<T>(T(0), T(0));
     prim_cell<Dual<T>, NV>(F, u[0], u[1], u[2], u[3], u[4], u[5], W, i);
+    }
 }
 
 // h[i] = sc[i] <w, V_i>, i = 0..j (the first pass of the FD J v path)
@@ -350,9 +476,9 @@ __global__ void __launch_bounds__(RED_THREADS) k_gmres_gather_dot(MeshView<T> m,
                                                                   const T* __restrict__ src, const T* __restrict__ V,
                                                                   long L, GmresDev d) {
     typedef typename KryAcc<T>::type A;
-    const int4 gi4 = *reinterpret_cast<const int4*>(d.gi);  // j and the done flag in one load
-    if (gi4.z) return;  // the solve finished in an earlier iteration of an unrolled body
-    const int j = gi4.x;
+    const int done = d.gi[2];
+    const int j = d.gi[4];  // this iteration (set by k_gmres_prim_z)
+    if (done) return;       // the solve has ended
     const long nc = m.nc;
     __shared__ A wsum[KRY_MAXM + 1][KRY_WARPS];
     __shared__ double scs[KRY_MAXM + 1];
@@ -467,39 +593,24 @@ __global__ void __launch_bounds__(RED_THREADS) k_gmres_gather_dot(MeshView<T> m,
     block_partials(reinterpret_cast<A*>(d.partial1), j, wsum);
 }
 
-// w -= sum_{i<=j} h1[i] sc[i] V_i, fused with the second CGS pass h2 = V^T w.  With LAST
-// (the exact J v body) also |w|^2, and the last block takes |V_{j+1}|^2 = |w|^2 - |h2|^2
-// (clamped at 0), sets sc[j+1] = 1/|V_{j+1}| (1 under the breakdown guard |.| <= 1e-12 of
-// src/Solver.cpp:1553-1558) and runs the Givens step; V_{j+1} = w - V h2 is formed by the
-// next iteration's k_gmres_prim_z.  Every block stages h1, sc and the previous rotations
-// in shared memory up front, so the last block's serial tail reads no global memory.
+// w -= sum_{i<=j} h1[i] sc[i] V_i, fused with the second CGS pass h2 = V^T w.  Without
+// LAST (the FD J v body) the last block to finish sums the h2 partials.  With LAST (the
+// exact J v body) h1 comes from the gather kernel's block partials (summed by every
+// block), the kernel also takes |w|^2, and it only writes its block partials of h2 and
+// |w|^2: the next iteration's k_gmres_prim_z sums them, forms V_{j+1} = w - V h2 and runs
+// the Givens step.
 template <class T, bool LAST>
 __global__ void __launch_bounds__(RED_THREADS) k_gmres_update_dot(long L, T* __restrict__ w, const T* __restrict__ V,
                                                                   GmresDev d, cudaGraphConditionalHandle hnd) {
     typedef typename KryAcc<T>::type A;
-    const int4 gi4 = *reinterpret_cast<const int4*>(d.gi);  // j and the done flag in one load
-    if (LAST && gi4.z) return;  // the solve finished in an earlier iteration of an unrolled body
-    const int j = gi4.x;
+    const int4 gi4 = *reinterpret_cast<const int4*>(d.gi);
+    if (LAST && gi4.z) return;  // the solve has ended
+    const int j = LAST ? d.gi[4] : gi4.x;  // this iteration
     __shared__ A hs[KRY_MAXM + 1];
     __shared__ A wsum[KRY_MAXM + 1][KRY_WARPS];
-    __shared__ double scs[KRY_MAXM + 1], col[KRY_MAXM + 2], h2s[KRY_MAXM + 2], css[KRY_MAXM], sns[KRY_MAXM];
-    __shared__ double hout[KRY_MAXM + 2];
-    __shared__ double gj, tolb;
-    __shared__ int mm;
-    // the previous iterations' state first, then (after the wait) h1 and w, which are
-    // the predecessor's (pdl.cuh)
-    for (int i = threadIdx.x; i <= j; i += blockDim.x) {
-        scs[i] = d.sc[i];
-        if (LAST && i < j) {
-            css[i] = d.cs[i];
-            sns[i] = d.sn[i];
-        }
-    }
-    if (LAST && threadIdx.x == 0) {
-        gj = d.g[j];
-        tolb = d.beta[1] * d.beta[0];
-        mm = d.gi[3];
-    }
+    __shared__ double scs[KRY_MAXM + 1];
+    // sc first, then (after the wait) h1 and w, which are the predecessor's (pdl.cuh)
+    for (int i = threadIdx.x; i <= j; i += blockDim.x) scs[i] = d.sc[i];
     pdl_wait();
     pdl_trigger();
     // one pass (j < KRY_RC): each element's basis values stay in registers between the
@@ -531,8 +642,7 @@ __global__ void __launch_bounds__(RED_THREADS) k_gmres_update_dot(long L, T* __r
         if (i <= j && threadIdx.x % G == 0) {
             const double h1 = scs[i] * (double)sg;
             hs[i] = (A)(h1 * scs[i]);
-            col[i] = h1;
-            if (blockIdx.x == 0) d.h1[i] = h1;
+            if (blockIdx.x == 0) d.h1[i] = h1;  // for the Givens step
         }
     } else {
         for (int i = threadIdx.x; i <= j; i += blockDim.x) hs[i] = (A)(d.h1[i] * scs[i]);
@@ -595,83 +705,8 @@ __global__ void __launch_bounds__(RED_THREADS) k_gmres_update_dot(long L, T* __r
         dots_finish(d, j, wsum, d.h2, -1, scs);
         return;
     }
-    if (!dots_finish(d, j + 1, wsum, d.h2, j + 1, scs, h2s)) return;
-    if (threadIdx.x >= 32) return;
-    // The Givens step (src/Solver.cpp:1550-1588) by warp 0 of the last block.  Each FP64
-    // warp instruction costs ~64 cycles on GB300 whatever the active lanes, so the work is
-    // spread over the lanes: the previous rotations applied to the new column are the
-    // affine recurrence carry_{i+1} = -s_i carry_i + c_i col[i+1] (carry_0 = col[0]),
-    // evaluated as a parallel prefix over 32 rotations at a time (compositions of affine
-    // maps, Kogge-Stone), and out[i] = c_i carry_i + s_i col[i+1] by every lane at once.
-    // |h2|^2 is summed in the basis precision (it is ~1e-14 of |w|^2).  The new rotation
-    // takes c = a / sqrt(a^2 + b^2) as a * rsqrt(a^2 + b^2), and sc[j+1] = rsqrt(hsq).
-    const unsigned full = 0xffffffffu;
-    const int lane = threadIdx.x;
-    A s2p = A(0);
-    for (int i = lane; i <= j; i += 32) {
-        const A h = (A)h2s[i];
-        s2p += h * h;
-        col[i] += h2s[i];
-    }
-#pragma unroll
-    for (int o = 16; o > 0; o >>= 1) s2p += __shfl_xor_sync(full, s2p, o);
-    __syncwarp();
-    double carry = col[0];
-    for (int base = 0; base < j; base += 32) {
-        const int i = base + lane;
-        const bool act = i < j;
-        const double ci = act ? css[i] : 1.0, si = act ? sns[i] : 0.0, nx = act ? col[i + 1] : 0.0;
-        const double snx = si * nx;
-        double fa = act ? -si : 1.0, fb = act ? ci * nx : 0.0;  // f_i(x) = fa x + fb
-#pragma unroll
-        for (int o = 1; o < 32; o <<= 1) {
-            const double ap = __shfl_up_sync(full, fa, o), bp = __shfl_up_sync(full, fb, o);
-            if (lane >= o) {
-                fb = fma(fa, bp, fb);
-                fa = fa * ap;
-            }
-        }
-        const double cnext = fma(fa, carry, fb);        // carry after rotation i
-        double cprev = __shfl_up_sync(full, cnext, 1);  // carry before rotation i
-        if (lane == 0) cprev = carry;
-        if (act) hout[i] = fma(ci, cprev, snx);
-        carry = __shfl_sync(full, cnext, 31);
-    }
-    if (lane == 0) {
-        const double hsq = fmax(h2s[j + 1] - (double)s2p, 0.0);
-        const double r = hsq > 0.0 ? rsqrt(hsq) : 0.0;
-        const double hv = hsq * r;
-        d.hsq[1] = hsq;
-        d.sc[j + 1] = hv > 1e-12 ? r : 1.0;
-        const double a = carry, b = hv;
-        double c, sn;
-        if (fabs(b) < 1e-14) {
-            c = 1.0;
-            sn = 0.0;
-            hout[j] = a;
-        } else {
-            const double q = fma(a, a, hsq), rq = rsqrt(q);
-            c = a * rq;
-            sn = b * rq;
-            hout[j] = q * rq;
-        }
-        hout[j + 1] = 0.0;
-        d.cs[j] = c;
-        d.sn[j] = sn;
-        d.g[j + 1] = -sn * gj;
-        d.g[j] = c * gj;
-        const bool conv = fabs(-sn * gj) < tolb;
-        if (conv || j + 1 >= mm) {
-            d.gi[1] = j;
-            d.gi[2] = 1;
-            if (d.in_graph) cudaGraphSetConditional(hnd, 0);
-        } else {
-            d.gi[0] = j + 1;
-        }
-    }
-    __syncwarp();
-    double* Hc = d.H + (long)j * (mm + 1);
-    for (int i = lane; i <= j + 1; i += 32) Hc[i] = hout[i];
+    block_partials(reinterpret_cast<A*>(d.partial), j + 1, wsum);  // rows 0..j: h2, j + 1: |w|^2
+    if (blockIdx.x == 0 && threadIdx.x == 0) d.gi[5] = j + 1;      // updates completed
 }
 
 // Hessenberg column, Givens rotations and the convergence test (src/Solver.cpp:1550-1588);

@@ -167,7 +167,7 @@ template <class T> void launch_gmres_multidot(long L, const T* w, const T* V, co
 // J v body's final update + norm + Givens
 template <class T> void launch_gmres_prim_z(int nv, long nc, const Flow<T>& F, const T* U, T* V, long L,
                                             const T* Dinv, T* z, Field<T> W, const T* w, const GmresDev& d,
-                                            cudaStream_t s);
+                                            cudaGraphConditionalHandle h, cudaStream_t s);
 template <class T> void launch_gmres_gather_dot(int nv, const MeshView<T>& m, const T* FA, T* w, const T* z,
                                                 const T* dt, const T* src, const T* V, long L, const GmresDev& d,
                                                 cudaStream_t s, bool pdl = false);

@@ -625,8 +625,10 @@ struct cfdg_solver {
     int body_unroll() const { return KRY_BODY_ITERS; }
     // WHILE-body executions of a graph solve of `iters` iterations
     long long body_runs(int iters) const {
-        const int u = use_persistent() || !(cfg.precision == CFDG_MIXED || cfg.jv == CFDG_JV_EXACT) ? 1 : body_unroll();
-        return (iters + u - 1) / u;
+        if (use_persistent() || !(cfg.precision == CFDG_MIXED || cfg.jv == CFDG_JV_EXACT)) return iters;
+        // the exact J v body runs once more than the iterations (the last run ends the solve)
+        const int u = body_unroll();
+        return (iters + 1 + u - 1) / u;
     }
 
     cfdg_status enqueue_arnoldi_iteration(double* Ubase, double* Rbase, cudaGraphConditionalHandle h,
@@ -634,7 +636,7 @@ struct cfdg_solver {
         const bool mixed = cfg.precision == CFDG_MIXED;
         if (ev) CK(cudaEventRecord(ev[0], st));
         if (mixed) {
-            launch_gmres_prim_z<float>(nv, nc, Ff, U32, V32, L, dinv32, z32, f32(W32, W32d), w32, gd, st);
+            launch_gmres_prim_z<float>(nv, nc, Ff, U32, V32, L, dinv32, z32, f32(W32, W32d), w32, gd, h, st);
             ResArgs<float> a;
             a.m = mvf;
             a.F = Ff;
@@ -658,7 +660,7 @@ struct cfdg_solver {
             if (ev) CK(cudaEventRecord(ev[5], st));
             launches += nv == 6 ? 6 : 5;
         } else if (cfg.jv == CFDG_JV_EXACT) {
-            launch_gmres_prim_z<double>(nv, nc, F, Ubase, V, L, dinv64, z, f64(Wj, Wjd), w64, gd, st);
+            launch_gmres_prim_z<double>(nv, nc, F, Ubase, V, L, dinv64, z, f64(Wj, Wjd), w64, gd, h, st);
             ResArgs<double> a;
             a.m = mv;
             a.F = F;
@@ -805,7 +807,10 @@ struct cfdg_solver {
         int done = 0;
         CK(cudaMemcpyAsync(&done, gd.gi + 2, sizeof(int), cudaMemcpyDeviceToHost, st));
         CK(cudaStreamSynchronize(st));
-        for (int it = 0; !done && it < cfg.gmres_m; ++it) {
+        // the exact J v body finishes iteration j in the first kernel of iteration j + 1, so
+        // it runs once more than the iterations (that last run only ends the solve)
+        const bool exact_body = cfg.precision == CFDG_MIXED || cfg.jv == CFDG_JV_EXACT;
+        for (int it = 0; !done && it < cfg.gmres_m + (exact_body ? 1 : 0); ++it) {
             cfdg_status e = enqueue_gmres_body(Ubase, Rbase, none);
             if (e != CFDG_OK) {
                 gd.in_graph = 1;
@@ -1604,7 +1609,7 @@ cfdg_status cfdg_solver_create(const cfdg_mesh* m, const cfdg_config* cfg, cfdg_
     }
     if (c.gmres_m <= KRY_MAXM) {  // device-GMRES state, so the driver can be switched at run time
         int m = c.gmres_m;
-        TRYS(dalloc(&s->gdi, 4));
+        TRYS(dalloc(&s->gdi, 8));
         size_t nd = 3 + (size_t)(m + 1) + 2 * (size_t)m + (size_t)(m + 1) * m + m + 2 * (size_t)(m + 1) + 2 +
                     (size_t)(m + 1) + 2 * (size_t)(KRY_MAXM + 1) * RED_BLOCKS + 4;
         TRYS(dalloc(&s->gdd, nd));
@@ -1624,6 +1629,7 @@ cfdg_status cfdg_solver_create(const cfdg_mesh* m, const cfdg_config* cfg, cfdg_
         d.partial = q; q += (size_t)(KRY_MAXM + 1) * RED_BLOCKS;
         d.partial1 = q; q += (size_t)(KRY_MAXM + 1) * RED_BLOCKS;
         d.nb1 = (int)kry_grid(nc);
+        d.nb2 = (int)kry_grid(L);
         d.counter = reinterpret_cast<unsigned*>(q);
         d.in_graph = 1;
         if (c.precision == CFDG_MIXED) TRYS(dalloc(&s->w32, (size_t)L));

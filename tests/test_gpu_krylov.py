@@ -126,8 +126,10 @@ def test_stream_driver_is_the_graph_bit_for_bit(cuda_lib, name, precision, jv):
         out[kry] = s.gmres(U, R, -R)
         st = s.kernel_stats(reset=True)
         if kry == 2 and (precision == "mixed" or jv == "exact"):
+            # the exact J v body runs once more than the iterations: that last run's first
+            # kernel ends the solve (the Givens step of the last column), the others return
             n = [st[k][1] for k in s.KERNEL_CLASSES if k.startswith("krylov.") and k != "krylov.update_final"]
-            assert min(n) == max(n) == out[kry][0]
+            assert min(n) == max(n) == out[kry][0] + 1
             assert st["krylov.update_final"][1] == 0
     assert out[1][0] == out[2][0]
     np.testing.assert_array_equal(out[1][1], out[2][1])
