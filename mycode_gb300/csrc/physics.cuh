@@ -33,6 +33,12 @@ CFD_HD double quot_by_recip(double a, double b, double y) {
 // division for the other scalar types
 template <class S, class R> CFD_HD S div_shared(S a, R b, R) { return a / b; }
 CFD_HD double div_shared(double a, double b, double y) { return quot_by_recip(a, b, y); }
+// the same with a divisor of the scalar type: recip_for(b) is 1 / b for FP64 (unused
+// otherwise), quot_shared(a, b, y) the quotient
+template <class S> CFD_HD S recip_for(S) { return S(1.0f); }
+CFD_HD double recip_for(double b) { return 1.0 / b; }
+template <class S> CFD_HD S quot_shared(S a, S b, S) { return a / b; }
+CFD_HD double quot_shared(double a, double b, double y) { return quot_by_recip(a, b, y); }
 
 // libstdc++'s std::max / std::min selection rule (NaN behaviour included)
 template <class S> CFD_HD S smax(S a, S b) { return (val(a) < val(b)) ? b : a; }
@@ -72,8 +78,9 @@ template <class S, class R>
 CFD_HD CS<S> make_cs(const Flow<R>& F, S r, S ru, S rv, S rE, S rk, S rw) {
     CS<S> c;
     c.r = r; c.ru = ru; c.rv = rv; c.rE = rE; c.rk = rk; c.rw = rw;
-    c.u = ru / r;
-    c.v = rv / r;
+    const S ir = recip_for(r);  // FP64: u and v by one reciprocal (quot_shared)
+    c.u = quot_shared(ru, r, ir);
+    c.v = quot_shared(rv, r, ir);
     c.p = pressure(F, r, ru, rv, rE);
     return c;
 }

@@ -102,7 +102,8 @@ __device__ __forceinline__ CS<S> load_cs(const Field<R>& U, const Field<R>& W, l
 // u, v, p, T as the reference computes them per face (src/Solver.cpp:93-102).
 template <class S, int NV, class R>
 __device__ __forceinline__ void prim_cell(const Flow<R>& F, S r, S ru, S rv, S rE, S rk, S rw, Field<R> W, long i) {
-    S u = ru / r, v = rv / r;
+    const S ir = recip_for(r);  // FP64: u and v by one reciprocal (quot_shared)
+    S u = quot_shared(ru, r, ir), v = quot_shared(rv, r, ir);
     S p = pressure(F, r, ru, rv, rE);
     S T = p / (r * F.Rgas);
     Acc<S>::st(W, W_R, i, r);
