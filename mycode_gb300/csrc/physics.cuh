@@ -34,7 +34,9 @@ CFD_HD double quot_by_recip(double a, double b, double y) {
 template <class S, class R> CFD_HD S div_shared(S a, R b, R) { return a / b; }
 CFD_HD double div_shared(double a, double b, double y) { return quot_by_recip(a, b, y); }
 // the same with a divisor of the scalar type: recip_for(b) is 1 / b for FP64 (unused
-// otherwise), quot_shared(a, b, y) the quotient
+// otherwise), quot_shared(a, b, y) the quotient.  The flux functions take every quotient
+// by a state's density this way, so after inlining all of them share the one reciprocal
+// that make_cs takes for u and v.
 template <class S> CFD_HD S recip_for(S) { return S(1.0f); }
 CFD_HD double recip_for(double b) { return 1.0 / b; }
 template <class S> CFD_HD S quot_shared(S a, S b, S) { return a / b; }
@@ -114,9 +116,9 @@ template <class S, class R>
 CFD_HD Flux6<S> flux_llf(const Flow<R>& F, const CS<S>& L, const CS<S>& Rt, R nx, R ny) {
     Flux6<S> FL = normal_flux(L, nx, ny), FR = normal_flux(Rt, nx, ny);
     S unL = L.u * nx + L.v * ny;
-    S cL = sqrt(F.gam * L.p / L.r);
+    S cL = sqrt(quot_shared(F.gam * L.p, L.r, recip_for(L.r)));
     S unR = Rt.u * nx + Rt.v * ny;
-    S cR = sqrt(F.gam * Rt.p / Rt.r);
+    S cR = sqrt(quot_shared(F.gam * Rt.p, Rt.r, recip_for(Rt.r)));
     S a = smax(fabs(unL) + cL, fabs(unR) + cR);
     S ha = R(0.5) * a;
     S UL[6] = {L.r, L.ru, L.rv, L.rE, L.rk, L.rw};
@@ -130,8 +132,8 @@ CFD_HD Flux6<S> flux_llf(const Flow<R>& F, const CS<S>& L, const CS<S>& Rt, R nx
 // computeFluxROE with Harten's entropy fix (include/Flux.hpp:112-213)
 template <class S, class R>
 CFD_HD Flux6<S> flux_roe(const Flow<R>& F, const CS<S>& L, const CS<S>& Rt, R nx, R ny) {
-    S hL = (L.rE + L.p) / L.r;
-    S hR = (Rt.rE + Rt.p) / Rt.r;
+    S hL = quot_shared(L.rE + L.p, L.r, recip_for(L.r));
+    S hR = quot_shared(Rt.rE + Rt.p, Rt.r, recip_for(Rt.r));
     S sL = sqrt(L.r), sR = sqrt(Rt.r);
     S inv = R(1.0) / (sL + sR);
     S ut = (sL * L.u + sR * Rt.u) * inv;
@@ -163,8 +165,8 @@ CFD_HD Flux6<S> flux_roe(const Flow<R>& F, const CS<S>& L, const CS<S>& Rt, R nx
     D[1] = w1 * (ut - ct * nx) + w2 * ut + w3 * (-ny) + w4 * (ut + ct * nx);
     D[2] = w1 * (vt - ct * ny) + w2 * vt + w3 * nx + w4 * (vt + ct * ny);
     D[3] = w1 * (ht - unt * ct) + w2 * (R(0.5) * V2) + w3 * utt + w4 * (ht + unt * ct);
-    D[4] = fabs(unt) * (Rt.rk / Rt.r - L.rk / L.r) * rt;
-    D[5] = fabs(unt) * (Rt.rw / Rt.r - L.rw / L.r) * rt;
+    D[4] = fabs(unt) * (quot_shared(Rt.rk, Rt.r, recip_for(Rt.r)) - quot_shared(L.rk, L.r, recip_for(L.r))) * rt;
+    D[5] = fabs(unt) * (quot_shared(Rt.rw, Rt.r, recip_for(Rt.r)) - quot_shared(L.rw, L.r, recip_for(L.r))) * rt;
     Flux6<S> FL = normal_flux(L, nx, ny), FR = normal_flux(Rt, nx, ny);
     Flux6<S> o;
 #pragma unroll
@@ -177,8 +179,8 @@ CFD_HD Flux6<S> flux_roe(const Flow<R>& F, const CS<S>& L, const CS<S>& Rt, R nx
 template <class S, class R>
 CFD_HD Flux6<S> flux_hllc(const Flow<R>& F, const CS<S>& L, const CS<S>& Rt, R nx, R ny) {
     S unL = L.u * nx + L.v * ny, unR = Rt.u * nx + Rt.v * ny;
-    S cL = sqrt(F.gam * L.p / L.r), cR = sqrt(F.gam * Rt.p / Rt.r);
-    S hL = (L.rE + L.p) / L.r, hR = (Rt.rE + Rt.p) / Rt.r;
+    S cL = sqrt(quot_shared(F.gam * L.p, L.r, recip_for(L.r))), cR = sqrt(quot_shared(F.gam * Rt.p, Rt.r, recip_for(Rt.r)));
+    S hL = quot_shared(L.rE + L.p, L.r, recip_for(L.r)), hR = quot_shared(Rt.rE + Rt.p, Rt.r, recip_for(Rt.r));
     S sL = sqrt(L.r), sR = sqrt(Rt.r);
     S ut = (sL * L.u + sR * Rt.u) / (sL + sR);
     S vt = (sL * L.v + sR * Rt.v) / (sL + sR);
