@@ -1,6 +1,8 @@
 // Test-only host build of the residual's face function (face.cuh) and its hand-written
 // adjoint (adjoint.cuh), so the adjoint can be checked against finite differences of the
 // same operation sequence on the CPU.  Not part of the library.
+#include <cstring>
+
 #include "../../mycode_gb300/csrc/adjoint.cuh"
 
 using namespace cfdg;
@@ -24,6 +26,18 @@ CS<double> cs(const Flow<double>& F, const double* U) { return make_cs(F, U[0], 
 }  // namespace
 
 extern "C" {
+
+// quot_by_recip (physics.cuh) against IEEE division on n pairs: a = m_a 2^ea, b = m_b 2^eb
+// from the given significand and exponent arrays; returns the number of pairs whose bits
+// differ
+long quot_mismatches(long n, const double* a, const double* b) {
+    long bad = 0;
+    for (long i = 0; i < n; ++i) {
+        const double q = quot_by_recip(a[i], b[i], 1.0 / b[i]), ref = a[i] / b[i];
+        if (std::memcmp(&q, &ref, sizeof(double)) != 0) ++bad;
+    }
+    return bad;
+}
 
 // fl: bcset, flux, spatial, viscous, interior, tag
 void face_eval(const double* p, const int* fl, const double* g, const double* UL, const double* UR, const double* gL,

@@ -257,3 +257,26 @@ def test_sst_boundary_face_adjoint(harness, bcset, tags, flux):
     for tag in tags:
         for seed in (7, 8):
             check_sst_face(harness, [bcset, flux, 2, 1, 0, tag], seed)
+
+
+def test_shared_reciprocal_quotient_is_the_division(harness):
+    """quot_by_recip (Markstein's correction of a * (1/b)), which the FP64 residual uses
+    for quotients that share a divisor, gives the bits of a / b: random operands over a wide
+    exponent range, divisors with all-ones and near-power-of-two significands, and the
+    magnitudes the residual divides (volumes, densities, squared distances)."""
+    rng = np.random.default_rng(7)
+    n = 400_000
+    a = rng.uniform(1.0, 2.0, n) * np.exp2(rng.integers(-300, 300, n)) * rng.choice([-1.0, 1.0], n)
+    b = rng.uniform(1.0, 2.0, n) * np.exp2(rng.integers(-60, 60, n))
+    b[: n // 8] = np.exp2(rng.integers(-40, 40, n // 8)) * (2.0 - 2.0 ** -52)      # all-ones significands
+    b[n // 8: n // 4] = np.exp2(rng.integers(-40, 40, n // 8)) * (1.0 + rng.integers(0, 16, n // 8) * 2.0 ** -52)
+    vol = rng.uniform(1e-9, 1e-2, n)
+    a2 = rng.standard_normal(n) * 10.0 ** rng.integers(-8, 6, n)
+    f = harness.quot_mismatches
+    f.restype = C.c_long
+    f.argtypes = [C.c_long, C.c_void_p, C.c_void_p]
+    for x, y in ((a, b), (a2, vol)):
+        x = np.ascontiguousarray(x)
+        y = np.ascontiguousarray(y)
+        assert f(n, x.ctypes.data, y.ctypes.data) == 0
+
