@@ -131,8 +131,8 @@ void launch_gmres_update_final<float>(long L, const float* w, float* V, const Gm
 }
 template <>
 void launch_gmres_solution_dev<float>(int nv, long nc, const float* V, long L, const GmresDev& d, const double* D,
-                                   double* x, cudaStream_t s) {
-    NV_SWITCH(nv, (k_gmres_solution_dev<float, NVC><<<blocks_for(nc), tpb_for(nc), 0, s>>>(nc, V, L, d, D, x)));
+                                   const float* Dinv32, double* x, cudaStream_t s) {
+    NV_SWITCH(nv, (k_gmres_solution_dev<float, NVC><<<blocks_for(nc), tpb_for(nc), 0, s>>>(nc, V, L, d, D, Dinv32, x)));
 }
 
 }  // namespace cfdg

@@ -116,7 +116,7 @@ void launch_newton_update(int nv, long nc, double* U, const double* dU, double r
 }
 
 // ---- device-resident GMRES
-void launch_gmres_backsub(const GmresDev& d, cudaStream_t s) { k_gmres_backsub<<<1, 1, 0, s>>>(d); }
+void launch_gmres_backsub(const GmresDev& d, cudaStream_t s) { k_gmres_backsub<<<1, 32, 0, s>>>(d); }
 template <>
 void launch_gmres_start<double>(long n, double* V0, const double* rhs, const GmresDev& d, int m, double tol,
                                 cudaGraphConditionalHandle h, const double* bsq, cudaStream_t s) {
@@ -167,8 +167,8 @@ void launch_gmres_update_final<double>(long L, const double* w, double* V, const
 }
 template <>
 void launch_gmres_solution_dev<double>(int nv, long nc, const double* V, long L, const GmresDev& d, const double* D,
-                                   double* x, cudaStream_t s) {
-    NV_SWITCH(nv, (k_gmres_solution_dev<double, NVC><<<blocks_for(nc), tpb_for(nc), 0, s>>>(nc, V, L, d, D, x)));
+                                   const double* Dinv32, double* x, cudaStream_t s) {
+    NV_SWITCH(nv, (k_gmres_solution_dev<double, NVC><<<blocks_for(nc), tpb_for(nc), 0, s>>>(nc, V, L, d, D, Dinv32, x)));
 }
 
 }  // namespace cfdg

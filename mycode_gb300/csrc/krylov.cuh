@@ -815,32 +815,64 @@ __global__ void __launch_bounds__(RED_THREADS) k_gmres_update_final(long L, cons
     }
 }
 
-// back substitution H y = g over the k+1 leading columns (src/Solver.cpp:1592-1599)
+// back substitution H y = g over the k+1 leading columns (src/Solver.cpp:1592-1599), by
+// one warp: the triangle is staged in shared memory, the reciprocals of the diagonal are
+// taken by all lanes at once, then column by column (l = k .. 0) y_l = g_l / H_ll and every
+// lane i < l takes g_i -= H_il y_l, so the serial chain is one multiply and one FMA per
+// column (an FP64 warp instruction costs ~64 cycles on GB300, a divide about seven of them).
+constexpr int KRY_BS = 64;  // columns of the triangle staged in shared memory (33 KB)
+
 static __global__ void k_gmres_backsub(GmresDev d) {
-    if (threadIdx.x != 0 || blockIdx.x != 0) return;
-    const int k = d.gi[1], m = d.gi[3];
-    for (int i = k; i >= 0; --i) {
-        double yi = d.g[i];
-        for (int l = i + 1; l <= k; ++l) yi -= d.H[(long)l * (m + 1) + i] * d.y[l];
-        d.y[i] = yi / d.H[(long)i * (m + 1) + i];
+    __shared__ double R[KRY_BS][KRY_BS + 1], gs[KRY_MAXM + 1], rd[KRY_MAXM + 1], ys[KRY_MAXM + 1];
+    if (blockIdx.x != 0 || threadIdx.x >= 32) return;
+    const int k = d.gi[1], m = d.gi[3], lane = threadIdx.x;
+    if (k < 0) return;
+    const bool staged = k < KRY_BS;
+    // H_il = column l, row i (i <= l)
+    auto Hil = [&](int i, int l) { return staged ? R[l][i] : d.H[(long)l * (m + 1) + i]; };
+    if (staged)
+        for (int l = 0; l <= k; ++l)
+            for (int i = lane; i <= l; i += 32) R[l][i] = d.H[(long)l * (m + 1) + i];
+    for (int i = lane; i <= k; i += 32) gs[i] = d.g[i];
+    __syncwarp();
+    for (int i = lane; i <= k; i += 32) rd[i] = 1.0 / Hil(i, i);
+    __syncwarp();
+    for (int l = k; l >= 0; --l) {
+        const double yl = gs[l] * rd[l];
+        if (lane == 0) ys[l] = yl;
+        for (int i = lane; i < l; i += 32) gs[i] = fma(-Hil(i, l), yl, gs[i]);
+        __syncwarp();
     }
+    for (int i = lane; i <= k; i += 32) d.y[i] = ys[i];
 }
 
 // x = (sum_{i<=k} V_i sc_i y_i) / D (src/Solver.cpp:1610-1615, accumulated before the
 // scaling); zero when the solve was empty
+// With an FP32 basis the sum is FP32 (the update only has to solve the Newton system to
+// the GMRES tolerance) and 1/D the FP32 reciprocal the solve used (Dinv32).
 template <class T, int NV>
 __global__ void k_gmres_solution_dev(long nc, const T* __restrict__ V, long L, GmresDev d,
-                                     const double* __restrict__ D, double* __restrict__ x) {
+                                     const double* __restrict__ D, const T* __restrict__ Dinv32,
+                                     double* __restrict__ x) {
+    typedef typename KryAcc<T>::type A;
+    __shared__ A ys[KRY_MAXM];
     const int k = d.gi[1];
+    for (int j = threadIdx.x; j <= k; j += blockDim.x) ys[j] = (A)(d.y[j] * d.sc[j]);
+    __syncthreads();
     for (long i = (long)blockIdx.x * blockDim.x + threadIdx.x; i < nc; i += (long)gridDim.x * blockDim.x) {
         double id[NV];
-        d_inv<NV>(D, nc, i, id);
+        if (sizeof(T) == 4) {
+#pragma unroll
+            for (int c = 0; c < NV; ++c) id[c] = (double)dinv_of<T, NV>(Dinv32, nc, i, c, Dinv32[i]);
+        } else {
+            d_inv<NV>(D, nc, i, id);
+        }
 #pragma unroll
         for (int c = 0; c < NV; ++c) {
             long q = c * nc + i;
-            double acc = 0.0;
-            for (int j = 0; j <= k; ++j) acc += (double)V[j * L + q] * (d.y[j] * d.sc[j]);
-            x[q] = acc * id[c];
+            A acc = A(0);
+            for (int j = 0; j <= k; ++j) acc += (A)V[j * L + q] * ys[j];
+            x[q] = (double)acc * id[c];
         }
     }
 }

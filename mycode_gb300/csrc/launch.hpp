@@ -177,7 +177,7 @@ template <class T> void launch_gmres_update_dot_last(long L, T* w, const T* V, c
 template <class T> void launch_gmres_update_final(long L, const T* w, T* V, const GmresDev& d,
                                                   cudaGraphConditionalHandle h, cudaStream_t s);
 template <class T> void launch_gmres_solution_dev(int nv, long nc, const T* V, long L, const GmresDev& d,
-                                                  const double* D, double* x, cudaStream_t s);
+                                                  const double* D, const T* Dinv32, double* x, cudaStream_t s);
 }  // namespace cfdg
 
 // ---- one Arnoldi iteration as one persistent kernel (arnoldi.cuh, kern_jv.cu)

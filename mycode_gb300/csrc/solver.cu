@@ -698,8 +698,8 @@ struct cfdg_solver {
 
     void enqueue_gmres_post(double* xout) {
         launch_gmres_backsub(gd, st);
-        if (cfg.precision == CFDG_MIXED) launch_gmres_solution_dev<float>(nv, nc, V32, L, gd, D, xout, st);
-        else launch_gmres_solution_dev<double>(nv, nc, V, L, gd, D, xout, st);
+        if (cfg.precision == CFDG_MIXED) launch_gmres_solution_dev<float>(nv, nc, V32, L, gd, D, dinv32, xout, st);
+        else launch_gmres_solution_dev<double>(nv, nc, V, L, gd, D, nullptr, xout, st);
         launches += 2;
     }
 
