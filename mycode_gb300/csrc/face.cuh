@@ -108,7 +108,8 @@ CFD_HD Flux6<S> face_flux(const Flow<R>& F, const CS<S>& L, const CS<S>& Rn, boo
                 dvdy = e0 - div_shared((c0 * g.dxlr + e0 * g.dylr - dv) * g.dylr, d2, id2);
             }
         }
-        R Cp = F.gam * F.Rgas / (F.gam - R(1.0));
+        const R gm1 = F.gam - R(1.0);
+        R Cp = div_shared(F.gam * F.Rgas, gm1, recip_for(gm1));  // 1/(gamma-1) shared with the reconstruction
         S mu = rf * F.nu;
         S kc = mu * Cp / F.Pr;
         if (F.sst) {

@@ -90,7 +90,8 @@ CFD_HD CS<S> make_cs(const Flow<R>& F, S r, S ru, S rv, S rE, S rk, S rw) {
 // primitiveToConservative (src/Solver.cpp:498-501)
 template <class S, class R>
 CFD_HD CS<S> p2c(const Flow<R>& F, S r, S u, S v, S p, S k, S w) {
-    S rE = p / (F.gam - R(1.0)) + R(0.5) * r * (u * u + v * v);
+    const R gm1 = F.gam - R(1.0);
+    S rE = div_shared(p, gm1, recip_for(gm1)) + R(0.5) * r * (u * u + v * v);  // 1/(gamma-1) shared
     return make_cs(F, r, r * u, r * v, rE, r * k, r * w);
 }
 
