@@ -148,6 +148,24 @@ def measured_peak():
         return 6800.0, "fallback"
 
 
+def profile_fp64_pipe():
+    """FP64 pipe fraction and FP64 flops per unit of the FP64 residual's kernels from the
+    committed ncu summary (profiles/fp64_pipe.txt)."""
+    path = os.path.join(ROOT, "profiles", "fp64_pipe.txt")
+    out = {}
+    if os.path.exists(path):
+        with open(path) as fh:
+            for line in fh:
+                parts = line.split()
+                if len(parts) == 4 and not parts[0].startswith("#"):
+                    try:
+                        out[parts[0]] = {"fp64_pipe_frac": float(parts[1]), "fp64_flops_per_unit": float(parts[2]),
+                                         "unit": parts[3]}
+                    except ValueError:
+                        pass
+    return out
+
+
 def profile_traffic(kernel_class: str, jbar: float = 0.0):
     """DRAM bytes per launch of a kernel class from the committed ncu summary
     (profiles/traffic.txt: bytes at Arnoldi iteration 0 and per further basis vector),
@@ -389,6 +407,16 @@ def ours(args):
                 if peak_kind == "measured" else "fallback 6.8 TB/s",
                 "traffic": traffic}
 
+    # ---- the FP64 residual: HBM fraction (live) beside the FP64-pipe fraction (ncu)
+    pipe = profile_fp64_pipe()
+    fp64_residual = {}
+    for k in ("residual.prim", "residual.grad", "residual.flux", "residual.gather"):
+        if k in kern:
+            e = {"avg_us": kern[k]["avg_us"], "hbm_frac": round(kern[k]["achieved_gbs"] / peak, 4)}
+            e.update(pipe.get(k, {}))
+            fp64_residual[k.split(".")[1]] = e
+    fp64_residual["source"] = "hbm_frac: this run; fp64_pipe_frac, flops: profiles/fp64_pipe.txt (ncu)"
+
     # ---- e2e through the C ABI with pinned host buffers (per-kernel timing off: the
     # production call)
     import torch
@@ -460,6 +488,7 @@ def ours(args):
             "krylov_driver": kinfo,
             "roofline": roofline,
             "kernels": kern,
+            "fp64_residual": fp64_residual,
             "e2e": e2e,
             "fp64": fp64,
             "adjoint_over_primal": adjoint,
@@ -475,14 +504,18 @@ def time_to_converge(api, max_steps=1500):
     of 1e-10: the wedge 120 x 80 x 2 triangles (19,200 cells, 10 % jitter), M 2.5, HLLC with
     the Barth-Jespersen limiter, GMRES(30), CFL from 10, for the mixed path (FP32 Krylov and
     exact J v, FP64 residual and update), the FP64 path with exact J v and the FP64 path
-    with the reference's FD J v.  Also the relative L2 difference of the converged states."""
+    with the reference's FD J v.  Also the relative L2 difference of the converged states and
+    of their wall pressure coefficients (the slip wall, tag 3).  The limited scheme freezes
+    its limiter early (src/Solver.cpp:1714), at slightly different values in each run, so
+    its converged states solve slightly different discrete problems; the first-order pair
+    (same wedge, no limiter) shows the mixed path converging to the FP64 solution itself."""
     from mycode_gb300 import meshgen
     import numpy as np
     mesh = api.Mesh.from_spec(meshgen.wedge(120, 80, jitter=0.10, seed=0))
-    out, states = {}, {}
-    for name, prec, jv in (("mixed", "mixed", "exact"), ("fp64_exact", "fp64", "exact"), ("fp64_fd", "fp64", "fd")):
+
+    def solve(prec, jv, spatial):
         s = api.Solver(mesh, bcset="supersonic", init="freestream", viscous=0, precision=prec, jv=jv, gmres_m=30,
-                       cfl0=10.0, flux="HLLC", spatial="SECOND_ORDER_LIMITED")
+                       cfl0=10.0, flux="HLLC", spatial=spatial)
         s.setFlowConditions(2.5, 101325.0, 300.0)
         s.initialize()
         s.synchronize()
@@ -497,16 +530,30 @@ def time_to_converge(api, max_steps=1500):
                 break
         s.synchronize()
         t = time.perf_counter() - t0
-        out[name] = {"seconds": round(t, 4), "newton_steps": n, "gmres_iters": its, "reached": reached,
-                     "final_res_rho": rec.res_rho}
-        states[name] = s.getSolution()
+        res = {"seconds": round(t, 4), "newton_steps": n, "gmres_iters": its, "reached": reached,
+               "final_res_rho": rec.res_rho}
+        U, cp = s.getSolution(), s.wall_coefficients(3)[1]
         s.close()
+        return res, U, cp
+
+    out, states, cps = {}, {}, {}
+    for name, prec, jv in (("mixed", "mixed", "exact"), ("fp64_exact", "fp64", "exact"), ("fp64_fd", "fp64", "fd")):
+        out[name], states[name], cps[name] = solve(prec, jv, "SECOND_ORDER_LIMITED")
     ref = states["fp64_fd"]
     for name in ("mixed", "fp64_exact"):
         out[name]["state_rel_l2_vs_fp64_fd"] = float(np.linalg.norm(states[name] - ref) / np.linalg.norm(ref))
+        out[name]["wall_cp_max_abs_diff_vs_fp64_fd"] = float(np.abs(cps[name] - cps["fp64_fd"]).max())
     out["speedup_mixed_vs_fp64_fd"] = out["fp64_fd"]["seconds"] / out["mixed"]["seconds"]
     out["speedup_mixed_vs_fp64_exact"] = out["fp64_exact"]["seconds"] / out["mixed"]["seconds"]
     out["workload"] = "supersonic wedge 120x80x2 (19,200 cells), M 2.5, HLLC + BJ limiter, GMRES(30), CFL0 10"
+    m1, Um, cpm = solve("mixed", "exact", "FIRST_ORDER")
+    f1, Uf, cpf = solve("fp64", "exact", "FIRST_ORDER")
+    out["first_order"] = {
+        "mixed": m1, "fp64_exact": f1, "speedup_mixed_vs_fp64_exact": f1["seconds"] / m1["seconds"],
+        "state_rel_l2_mixed_vs_fp64": float(np.linalg.norm(Um - Uf) / np.linalg.norm(Uf)),
+        "wall_cp_max_abs_diff_mixed_vs_fp64": float(np.abs(cpm - cpf).max()),
+        "wall_cp_range": [float(cpf.min()), float(cpf.max())],
+        "workload": "the same wedge, HLLC first order (no limiter), to a density residual of 1e-10"}
     return out
 
 
