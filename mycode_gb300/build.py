@@ -2,8 +2,9 @@
 
 Translation units and their floating-point contracts:
   kern_f64.cu  nvcc --fmad=false  (FP64 residual/Krylov kernels match the CPU reference)
-  kern_f32.cu  nvcc               (FP32 residual and mixed-precision vectors)
-  kern_jv.cu   nvcc               (dual-number exact J v)
+  kern_f32.cu  nvcc --prec-div=false --prec-sqrt=false  (FP32 residual and mixed-precision
+               vectors: FP32 divides and square roots to ~2 ulp; FP64 untouched)
+  kern_jv.cu   nvcc --prec-div=false --prec-sqrt=false  (dual-number exact J v, same)
   solver.cu    nvcc               (host driver and C ABI; host code without contraction)
   noalloc.cu   nvcc --fmad=false  (residual norm with static scratch, no allocation)
   kern_adj.cu  nvcc               (adjoint / VJP of the FP64 residual)
@@ -26,8 +27,8 @@ ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 CU = {
     "kern_f64.cu": ["--fmad=false"],
-    "kern_f32.cu": [],
-    "kern_jv.cu": [],
+    "kern_f32.cu": ["--prec-div=false", "--prec-sqrt=false"],
+    "kern_jv.cu": ["--prec-div=false", "--prec-sqrt=false"],
     "solver.cu": [],
     "noalloc.cu": ["--fmad=false"],
     "kern_adj.cu": [],
