@@ -150,14 +150,15 @@ __device__ __forceinline__ A partials_sum(const A* partial, int nd, int nb, int*
     A sg = A(0);
     if (i < nd) {
         const A* p = partial + (long)i * RED_BLOCKS;
-        for (int b0 = g; b0 < nb; b0 += 8 * G) {
-            A x[8];
+        for (int b0 = g; b0 < nb; b0 += 16 * G) {  // sixteen loads in flight per lane
+            A x[8], y[8];
 #pragma unroll
             for (int k = 0; k < 8; ++k) {
-                const int b = b0 + k * G;
+                const int b = b0 + k * G, c = b0 + (k + 8) * G;
                 x[k] = b < nb ? __ldcg(p + b) : A(0);
+                y[k] = c < nb ? __ldcg(p + c) : A(0);
             }
-            sg += tree8(x);
+            sg += tree8(x) + tree8(y);
         }
     }
     for (int o = G >> 1; o > 0; o >>= 1) sg += __shfl_xor_sync(0xffffffffu, sg, o);
