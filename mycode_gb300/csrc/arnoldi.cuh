@@ -16,9 +16,10 @@
 // with wrong numbers but finishes; the host reports the flag as an error.  The kernel is
 // launched with at most the blocks that fit on the GPU at once (occupancy query).
 //
-// Measured on the 28,800-cell laminar plate it does not beat the six-kernel body for the
-// FP32 basis (63-72 vs 54-64 us per iteration) and matches it in FP64 (186-200 vs
-// 186-211 us), so the six kernels stay the default; the switch is cfdg_config.persistent.
+// Measured on the 28,800-cell laminar plate it did not beat the multi-kernel body of the
+// time for the FP32 basis (63-72 vs 54-64 us per iteration; the five-kernel body since
+// runs an iteration in about 35 us) and matched it in FP64 (186-200 vs 186-211 us), so the
+// multi-kernel body is the default; the switch is cfdg_config.persistent.
 #pragma once
 #include "krylov.cuh"
 

@@ -486,7 +486,7 @@ struct cfdg_solver {
                                       "(its blocks were not all resident); set persistent = 0");
     }
 
-    // the persistent Arnoldi kernel (arnoldi.cuh) replaces the fused six-kernel body in
+    // the persistent Arnoldi kernel (arnoldi.cuh) replaces the fused five-kernel body in
     // the graph driver for the exact J v; grid = the blocks that fit at once
     unsigned* bar = nullptr;
     double* apart = nullptr;
