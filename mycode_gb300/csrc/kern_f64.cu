@@ -15,8 +15,13 @@ static void residual_nv(const ResArgs<double>& a) {
     if (a.ev) cudaEventRecord(a.ev[2], a.stream);
     k_flux<double, NV><<<blocks_for(nf), tpb_for(nf), 0, a.stream>>>(a.m, a.F, a.U, a.W, a.G, a.phi, a.FA, a.T, nullptr);
     if (a.ev) cudaEventRecord(a.ev[3], a.stream);
-    k_gather<double, NV><<<blocks_for(nc), tpb_for(nc), 0, a.stream>>>(a.m, a.FA.v, a.FA.n, a.out, nc, a.diag_v, a.dt,
-                                                           NV == 6 ? a.T.v + 2 * nc : nullptr);
+    if (a.norms_out)
+        k_gather_norms<NV><<<red_grid(nc), RED_THREADS, 0, a.stream>>>(a.m, a.FA.v, a.FA.n, a.out,
+                                                                        NV == 6 ? a.T.v + 2 * nc : nullptr, a.rhs_out,
+                                                                        a.rs, a.norms_out, a.flag);
+    else
+        k_gather<double, NV><<<blocks_for(nc), tpb_for(nc), 0, a.stream>>>(a.m, a.FA.v, a.FA.n, a.out, nc, a.diag_v,
+                                                                           a.dt, NV == 6 ? a.T.v + 2 * nc : nullptr);
     if (a.ev) cudaEventRecord(a.ev[4], a.stream);
 }
 

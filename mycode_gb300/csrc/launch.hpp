@@ -27,6 +27,12 @@ struct ResArgs {
     const R* dwall = nullptr;         // wall distance per cell; nv = 6 only
     bool pdl = false;                 // launch_jv_mid: programmatic dependent launch (pdl.cuh)
     const int* done = nullptr;        // launch_jv_mid: skip when *done (a finished Krylov solve)
+    // launch_residual<double> of a Newton step: the gather fused with the step's reductions
+    // (k_gather_norms) when norms_out is set
+    double* rhs_out = nullptr;
+    double* norms_out = nullptr;
+    int* flag = nullptr;
+    RedScratch rs{nullptr, nullptr};
 };
 
 // A kernel launch, with the programmatic stream-serialisation attribute when pdl: the

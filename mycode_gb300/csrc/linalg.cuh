@@ -263,6 +263,40 @@ __global__ void __launch_bounds__(RED_THREADS) k_step_norms(long nc, const doubl
     grid_finish<4>(v, rs, out4);
 }
 
+// k_gather (FP64) of a Newton step fused with k_step_norms: R (the same bits), rhs = -R,
+// the norm pieces and sum R^2 into out4, *flag cleared.  Grid-stride over the cells with
+// at most RED_BLOCKS blocks (the partials of grid_finish).
+template <int NV>
+__global__ void __launch_bounds__(RED_THREADS) k_gather_norms(MeshView<double> m, const double* __restrict__ FA,
+                                                              long fa_stride, double* __restrict__ Rout,
+                                                              const double* __restrict__ src,
+                                                              double* __restrict__ rhs, RedScratch rs, double* out4,
+                                                              int* flag) {
+    if (blockIdx.x == 0 && threadIdx.x == 0) *flag = 0;
+    const long nc = m.nc;
+    double v[4] = {0.0, 0.0, 0.0, 0.0};
+    for (long i = (long)blockIdx.x * blockDim.x + threadIdx.x; i < nc; i += (long)gridDim.x * blockDim.x) {
+        double acc[NV];
+        gather_cell<double, NV>(m, FA, fa_stride, src, nc, i, acc);
+        const double vv = m.vol[i], iv = 1.0 / vv;  // the quotients by one reciprocal (quot_by_recip)
+        double s = 0.0, q = 0.0;
+#pragma unroll
+        for (int c = 0; c < NV; ++c) {
+            Rout[c * nc + i] = acc[c];
+            rhs[c * nc + i] = -acc[c];
+            double r = quot_by_recip(acc[c], vv, iv);
+            s = (c == 0) ? r * r : s + r * r;
+            q += acc[c] * acc[c];
+        }
+        double r0 = quot_by_recip(acc[0], vv, iv);
+        v[0] += s * vv;
+        v[1] += vv;
+        v[2] += r0 * r0 * vv;
+        v[3] += q;
+    }
+    grid_finish<4>(v, rs, out4);
+}
+
 // The mixed-precision prologue of a Krylov solve in one pass per cell, FP32 arithmetic on
 // the FP64 state: U32 = Ub (the linearisation state), phi32 = phi; at the current state
 // U, W the local time step (k_local_dt's expression; from *cfl, or the given dt when

@@ -381,14 +381,11 @@ __global__ void __launch_bounds__(256) k_flux(MeshView<R> m, Flow<R> F, Field<R>
 // R_i = sum over the cell's faces, in reference face order, of +F*A (owner) or -F*A
 // (neighbour) (src/Solver.cpp:795-799).  Optionally adds diag_v * vol/(dt + 1e-30)
 // (the time term of applyJacobian, src/Solver.cpp:1381-1384).
+// The faces' F*A of cell i in reference face order (+ owner, - neighbour), minus the SST
+// sources (times the cell volume) when given
 template <class R, int NV>
-__global__ void __launch_bounds__(256) k_gather(MeshView<R> m, const R* __restrict__ FA, long fa_stride,
-                                                R* __restrict__ Rout, long r_stride,
-                                                const R* __restrict__ diag_v, const R* __restrict__ dt,
-                                                const R* __restrict__ src) {
-    long i = (long)blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= m.nc) return;
-    R acc[NV];
+__device__ __forceinline__ void gather_cell(const MeshView<R>& m, const R* __restrict__ FA, long fa_stride,
+                                            const R* __restrict__ src, long r_stride, long i, R (&acc)[NV]) {
 #pragma unroll
     for (int c = 0; c < NV; ++c) acc[c] = R(0);
     int ek[4];
@@ -414,6 +411,17 @@ __global__ void __launch_bounds__(256) k_gather(MeshView<R> m, const R* __restri
             acc[5] = acc[5] - src[r_stride + i];
         }
     }
+}
+
+template <class R, int NV>
+__global__ void __launch_bounds__(256) k_gather(MeshView<R> m, const R* __restrict__ FA, long fa_stride,
+                                                R* __restrict__ Rout, long r_stride,
+                                                const R* __restrict__ diag_v, const R* __restrict__ dt,
+                                                const R* __restrict__ src) {
+    long i = (long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= m.nc) return;
+    R acc[NV];
+    gather_cell<R, NV>(m, FA, fa_stride, src, r_stride, i, acc);
     if (diag_v) {
         R tc = m.vol[i] / (dt[i] + R(1e-30));
 #pragma unroll

@@ -301,9 +301,17 @@ struct cfdg_solver {
         return a;
     }
 
-    cfdg_status residual_dev(double* Uin, double* out, int update_limiters) {
+    // norms (a Newton step): the gather also writes rhs = -R, the norm pieces and |R|^2 into
+    // scal[8..11] and clears the update's non-finite flag (k_gather_norms)
+    cfdg_status residual_dev(double* Uin, double* out, int update_limiters, bool norms = false) {
         int do_lim = (cfg.spatial == CFDG_SECOND_ORDER_LIMITED && update_limiters) ? 1 : 0;
         ResArgs<double> a = res64(Uin, out, do_lim);
+        if (norms) {
+            a.rhs_out = rhs;
+            a.norms_out = scal + 8;
+            a.flag = bad;
+            a.rs = rs;
+        }
         a.ev = take_events(0);
         launch_residual<double>(a);
         launches += nv == 6 ? 5 : 4;
@@ -1097,14 +1105,13 @@ struct cfdg_solver {
             CK(cudaMemcpyAsync(scal + 12, hpin + 6, sizeof(double), cudaMemcpyHostToDevice, st));
         }
         bool upd = !(step > cfg.limiter_freeze_step || cfl > cfg.limiter_freeze_cfl);
-        TRY(residual_dev(U, R, upd ? 1 : 0));  // also the primitives W of U
+        // also the primitives W of U, and (fused into the gather) the norms, |R|^2 and
+        // rhs = -R; clears the update's non-finite flag
+        TRY(residual_dev(U, R, upd ? 1 : 0, true));
         if (!mixed) {
             launch_local_dt(nv, mv, F, U, W, cfl, dt, st);
             ++launches;
         }
-        // norms, |R|^2 and rhs = -R in one pass; also clears the update's non-finite flag
-        launch_step_norms(nv, nc, R, g64.vol, rhs, rs, scal + 8, bad, st);
-        ++launches;
         if (timing) CK(cudaEventRecord(step_ev[2], st));
         CK(cudaGraphLaunch(gexec, st));
         if (timing) CK(cudaEventRecord(step_ev[3], st));
