@@ -61,6 +61,27 @@ def test_graph_gmres_runs_exactly_m_iterations_at_zero_tolerance(cuda_lib):
         assert np.isfinite(x).all()
 
 
+@pytest.mark.parametrize("precision", ["mixed", "fp64"])
+def test_graph_gmres_long_basis(cuda_lib, precision):
+    """m = 80 at tolerance 0: 80 iterations (the back substitution's triangle then exceeds
+    its shared-memory stage and is read from global memory); the solution still solves
+    the system better than the 40-iteration one."""
+    s, spec, case = _solver(cuda_lib, "supersonic", precision=precision, jv="exact", gmres_m=80, gmres_tol=0.0)
+    s_ref, _, _ = _solver(cuda_lib, "supersonic", jv="exact", krylov=0)
+    o = OracleSolver(spec, bcset=case["bcset"], viscous=case["viscous"], init=case["init"])
+    C.setup(o, case)
+    U = C.perturbed_state(o.get_state(), o.cells(), seed=17)
+    for t in (s, s_ref):
+        t.setNumericalMethod("ROE", "SECOND_ORDER_LIMITED")
+        R = t.computeResiduals(U)
+        t.set_state(U)
+        t.local_timestep(50.0)
+    it, x = s.gmres(U, R, -R)
+    assert it == 80
+    assert np.isfinite(x).all()
+    assert _linear_residual(s_ref, U, R, x) <= (1e-3 if precision == "fp64" else 1e-2)
+
+
 def test_graph_gmres_empty_solve(cuda_lib):
     s, spec, case = _solver(cuda_lib, "bump", precision="mixed")
     U = s.getSolution()
