@@ -149,6 +149,7 @@ __device__ __forceinline__ void grad_item(const MeshView<R>& m, const Flow<R>& F
     R fnx[4], fny[4], fA[4], fdn[4];
 #pragma unroll
     for (int k = 0; k < 4; ++k) ek[k] = m.cf[(long)k * m.nc + i];
+    if (skip) return;  // tested with the first loads in flight, before the dependent ones
 #pragma unroll
     for (int k = 0; k < 4; ++k) {
         const int e = ek[k];
@@ -166,7 +167,6 @@ __device__ __forceinline__ void grad_item(const MeshView<R>& m, const Flow<R>& F
             ftg[k] = m.ftag[f];
         }
     }
-    if (skip) return;
     pdl_wait();
     pdl_trigger();
     S wi[NQ];
@@ -322,11 +322,11 @@ __device__ __forceinline__ void flux_item(const MeshView<R>& m, const Flow<R>& F
     bool interior = n >= 0;
     int tag = interior ? 0 : m.ftag[f];
     FaceGeo<R> g = load_geo(m, f);
+    if (skip) return;
     CS<S> L = load_cs<S, NV>(U, W, o);
     CS<S> Rn = interior ? load_cs<S, NV>(U, W, n) : L;
     // the state and primitives come from two or more kernels back in the Arnoldi body,
     // the gradients, limiter and SST terms from the predecessor (pdl.cuh)
-    if (skip) return;
     pdl_wait();
     pdl_trigger();
     S gL[10], gR[10];
