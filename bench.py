@@ -468,6 +468,7 @@ def ours(args):
     # ---- time to a density residual of 1e-10: mixed vs the FP64 paths on the supersonic
     # wedge (the reference's own CPU case, which converges under the reference's CFL control)
     t2c = time_to_converge(api) if (rank == 0 and not args.no_t2c) else None
+    others = other_configs(api) if (rank == 0 and not args.no_t2c) else None
 
     # ---- CPU baseline: the oracle port on this host, bounded sample
     cpu = None
@@ -493,10 +494,43 @@ def ours(args):
             "fp64": fp64,
             "adjoint_over_primal": adjoint,
             "time_to_1e-10": t2c,
+            "other_configs": others,
             "clocks": clocks,
             "cpu_baseline": cpu,
         }
         print(json.dumps(line))
+
+
+def other_configs(api, steps=20, warmup=3):
+    """The mixed-precision Newton step on the SST configurations at full size, from the
+    free stream, CUDA events around each step (secondary measurements, not the headline):
+    the turbulent flat plate 480 x 240 (115,200 cells, Roe, central) and the shock/boundary-
+    layer interaction box 800 x 640 with its outer half split (768,000 cells, HLLC + BJ
+    limiter, 8-degree shock inflow)."""
+    from mycode_gb300 import meshgen
+    out = {}
+    cases = (
+        ("turbulent_plate_sst", meshgen.turb_plate(), dict(flux="ROE", spatial="SECOND_ORDER_CENTRAL"),
+         (0.2, 5e6), {}),
+        ("swbli_sst", meshgen.swbli(), dict(flux="HLLC", spatial="SECOND_ORDER_LIMITED"), (2.0, 1e7),
+         dict(shock_deflection_deg=8.0)),
+    )
+    for name, spec, method, (mach, re), extra in cases:
+        mesh = api.Mesh.from_spec(spec)
+        s = api.Solver(mesh, bcset="plate", viscous=1, init="freestream", turbulence="sst", precision="mixed",
+                       jv="exact", **method, **extra)
+        s.setFreestreamStatic(mach, 101325.0, 300.0)
+        s.setKinematicViscosity(re, 1.0)
+        s.initialize()
+        s.set_timing("steps")
+        for _ in range(warmup):
+            s.newton_step(0.0)
+        t, evals, recs = run_steps(s, steps)
+        out[name] = {"n_cells": mesh.n_cells, "n_faces": mesh.n_faces, "value": evals * mesh.n_cells / t,
+                     "unit": UNIT, "ms_per_step": 1e3 * t / steps, "steps": steps, "warmup": warmup,
+                     "gmres_iters": [r[1] for r in recs], "res_vm_first_last": [recs[0][0], recs[-1][0]]}
+        s.close()
+    return out
 
 
 def time_to_converge(api, max_steps=1500):
