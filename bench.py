@@ -110,16 +110,15 @@ def krylov_bytes(stage: str, nc: int, nf: int, nv: int, s: int, jbar: float) -> 
     L = nv * nc
     nb = jbar + 1.0
     if stage == "prim_z":
-        # deferred V_j = w - V h2 (w and j basis vectors in, V_j out; none at j = 0), then
-        # z = V_j / D and the dual primitives
-        return nc * (nv * s + s + nv * s + nv * s + 2 * (7 if nv == 6 else 5) * s) + L * s * (jbar + 2)
+        # second pass of the pending vector and first pass of the last product (the pending
+        # vector, the product and j basis vectors in; the finished basis vector and the new
+        # pending vector out), then U and 1/D in, z and the dual primitives out
+        return nc * (nv * s + s + nv * s + 2 * (7 if nv == 6 else 5) * s) + L * s * (jbar + 4)
     if stage in ("grad", "flux"):
         return algorithmic_bytes(stage, nc, nf, nv, s, "SECOND_ORDER_CENTRAL", True, True)
     if stage == "gather_dot":
         return nc * 16 + nf * nv * s + nc * (nv * s + 2 * s + nv * s) + nb * L * s
-    if stage == "update_dot":
-        return L * s * (2 + nb)
-    if stage == "update_final":  # FD J v body only
+    if stage in ("update_dot", "update_final"):  # FD J v body only
         return L * s * (2 + nb)
     raise ValueError(stage)
 

@@ -85,14 +85,15 @@ typedef struct cfdg_config {
     int device;            /* CUDA device ordinal */
     /* Krylov driver: CFDG_KRYLOV_HOST runs the reference's modified Gram-Schmidt loop with
      * the Hessenberg on the host (one sync per iteration); CFDG_KRYLOV_GRAPH runs the whole
-     * solve as one CUDA graph (WHILE node, device Givens, CGS2 orthogonalisation);
+     * solve as one CUDA graph (WHILE node, device Givens, CGS2 orthogonalisation, in its
+     * delayed one-reduction form with the exact J v);
      * CFDG_KRYLOV_AUTO picks GRAPH for mixed precision or exact J v, else HOST. */
     int krylov;
     /* graph driver with exact J v: 1 runs each Arnoldi iteration as one persistent kernel
-     * with grid barriers between its phases, 0 (default) as five kernels; measured on the
-     * 28,800-cell plate: FP32 basis 63-72 us per iteration persistent vs 54-64 us with the
-     * six-kernel body of the time (the five-kernel body since: about 35 us), FP64 exact
-     * 186-200 vs 186-211 us */
+     * with grid barriers between its phases (two-reduction CGS2), 0 (default) as four
+     * kernels; measured on the 28,800-cell plate: FP32 basis 63-72 us per iteration
+     * persistent vs 54-64 us with the six-kernel body of the time (a five-kernel body
+     * since: about 35 us), FP64 exact 186-200 vs 186-211 us */
     int persistent;
     /* graph driver with exact J v: 1 (default) launches the Arnoldi body's kernels after
      * the first with programmatic dependent launch, so each starts while its predecessor's
@@ -102,7 +103,7 @@ typedef struct cfdg_config {
 
 /* CFDG_KRYLOV_STREAM launches the graph driver's kernels one iteration at a time from a
  * host loop (same arithmetic, one sync per iteration; with timing on every kernel of the
- * exact J v body is timed: stat classes 12-16) */
+ * exact J v body is timed: stat classes 12-15) */
 enum { CFDG_KRYLOV_AUTO = -1, CFDG_KRYLOV_HOST = 0, CFDG_KRYLOV_GRAPH = 1, CFDG_KRYLOV_STREAM = 2 };
 
 /* per-step record of a Newton solve (the reference prints these, src/Solver.cpp:1725-1727, :1746) */
@@ -262,10 +263,11 @@ cfdg_status cfdg_set_timing(cfdg_solver* s, int on);
 cfdg_status cfdg_kernel_times(cfdg_solver* s, double* ms_prim, double* ms_grad, double* ms_flux, double* ms_gather);
 /* accumulated per-kernel time and launch count since the last reset (18 classes): 0-3 the
  * residual's prim, grad, flux, gather kernels, 4-7 the same kernels of the exact J v,
- * 8-11 the VJP's forward recomputation, face adjoint and its two cell gathers, 12-16 the
- * stream-driven exact J v Krylov body: deferred basis update + z + primitives, gradients
- * (+ SST), fluxes, gather + first CGS pass, update + second pass + norm + Givens; 17 is
- * reserved (the FD body's final update, not timed) */
+ * 8-11 the VJP's forward recomputation, face adjoint and its two cell gathers, 12-15 the
+ * stream-driven exact J v Krylov body: second pass of the pending vector + first pass of
+ * the last product + z + primitives (+ Givens), gradients (+ SST), fluxes, gather + the
+ * iteration's dots; 16-17 are reserved (the FD body's update and final update, not
+ * timed) */
 cfdg_status cfdg_kernel_stats(cfdg_solver* s, double* ms18, long long* n18, int reset);
 /* VJP at the device-resident state with the device residual as lambda (timing path) */
 cfdg_status cfdg_vjp_device(cfdg_solver* s);

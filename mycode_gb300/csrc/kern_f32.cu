@@ -117,12 +117,7 @@ void launch_gmres_gather_dot<float>(int nv, const MeshView<float>& m, const floa
 }
 template <>
 void launch_gmres_update_dot<float>(long L, float* w, const float* V, const GmresDev& d, cudaStream_t s) {
-    k_gmres_update_dot<float, false><<<kry_grid(L), RED_THREADS, 0, s>>>(L, w, V, d, 0);
-}
-template <>
-void launch_gmres_update_dot_last<float>(long L, float* w, const float* V, const GmresDev& d, cudaGraphConditionalHandle h,
-                                   cudaStream_t s, bool pdl) {
-    launch_k(pdl, k_gmres_update_dot<float, true>, dim3(kry_grid(L)), dim3(RED_THREADS), s, L, w, V, d, h);
+    k_gmres_update_dot<float><<<kry_grid(L), RED_THREADS, 0, s>>>(L, w, V, d);
 }
 template <>
 void launch_gmres_update_final<float>(long L, const float* w, float* V, const GmresDev& d, cudaGraphConditionalHandle h,

@@ -158,12 +158,7 @@ void launch_gmres_gather_dot<double>(int nv, const MeshView<double>& m, const do
 }
 template <>
 void launch_gmres_update_dot<double>(long L, double* w, const double* V, const GmresDev& d, cudaStream_t s) {
-    k_gmres_update_dot<double, false><<<kry_grid(L), RED_THREADS, 0, s>>>(L, w, V, d, 0);
-}
-template <>
-void launch_gmres_update_dot_last<double>(long L, double* w, const double* V, const GmresDev& d, cudaGraphConditionalHandle h,
-                                   cudaStream_t s, bool pdl) {
-    launch_k(pdl, k_gmres_update_dot<double, true>, dim3(kry_grid(L)), dim3(RED_THREADS), s, L, w, V, d, h);
+    k_gmres_update_dot<double><<<kry_grid(L), RED_THREADS, 0, s>>>(L, w, V, d);
 }
 template <>
 void launch_gmres_update_final<double>(long L, const double* w, double* V, const GmresDev& d, cudaGraphConditionalHandle h,

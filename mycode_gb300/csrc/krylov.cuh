@@ -2,37 +2,39 @@
 // node, with the Hessenberg column, the Givens rotations and the convergence test on the
 // device, so a whole Krylov solve is one graph launch with no host round trip.
 //
-// Orthogonalisation is classical Gram-Schmidt applied twice (CGS2).  Each pass's dot
-// products are fused into the kernel that produces the vector they read.  With the exact
-// (dual-number) J v an iteration is five kernels and two grid reductions:
-//   V_j = w - V h2 (deferred), z = V_j / D, dual primitives    (k_gmres_prim_z)
-//   dual gradients, dual face fluxes                           (k_grad, k_flux)
-//   J v gather   -> w and block partials of h1 = V^T w         (k_gmres_gather_dot)
-//   h1 from the partials (every block), w -= V h1 -> w, h2 = V^T w and |w|^2; the last
-//   block: the Givens step                                     (k_gmres_update_dot<T, true>)
-// The norm of V_{j+1} = w - V h2 is taken as |w|^2 - |h2|^2 (Pythagoras over the
-// orthonormal basis, as in the one-reduction CGS2 variants of Swirydowicz, Langou,
+// Orthogonalisation is classical Gram-Schmidt applied twice (CGS2).  With the exact
+// (dual-number) J v it runs in its delayed one-reduction form (DCGS2: Swirydowicz, Langou,
 // Ananthan, Yang and Thomas, "Low synchronization Gram-Schmidt and GMRES algorithms",
-// Numer. Linear Algebra Appl. 2021), so V_{j+1} itself is formed by the next iteration's
-// first kernel and never needs a reduction of its own.  The FD J v path keeps the
-// explicit final pass:
+// Numer. Linear Algebra Appl. 2021): J is applied to the pending vector P_j, the product
+// of the first pass only, and the second pass of P_j happens one iteration later, from
+// dots taken in the same reduction as the next first pass.  An iteration is four kernels
+// and one grid reduction:
+//   finish P_{j-1} (second pass, norm by Pythagoras) into V_{j-1}, first pass of the
+//   last product into P_j, z = P_j / D, dual primitives   (k_gmres_prim_z; one extra
+//   block: the Givens step of column j - 2, first-pass entries of column j - 1)
+//   dual gradients, dual face fluxes                       (k_grad, k_flux)
+//   J v gather -> w, block partials of the dots of
+//   V_0..V_{j-1}, P_j with P_j and with w                  (k_gmres_gather_dot)
+// The first-pass entries of the new Hessenberg column come from the Arnoldi relation
+// J V s = V H s over the finished columns, so no reduction reads the corrected product.
+// The FD J v path keeps the explicit three-kernel CGS2:
+//   h1 = V^T w                                              (k_gmres_multidot)
+//   w -= V h1, h2 = V^T w                                   (k_gmres_update_dot)
 //   w -= V h2    -> V_{j+1}, |V_{j+1}|, and the Givens step  (k_gmres_update_final)
 // Every thread reads back only the elements it wrote itself, so no grid barrier is
 // needed inside a kernel.  A grid reduction is either finished by the last block to
-// finish (a ticket counter) or, for h1, by every block of the next kernel from the block
-// partials; both sum in a fixed order (deterministic).  Basis vectors are stored
-// unnormalised with a scale factor sc[i] = 1/|V_i| (FP64) applied wherever they are
-// read.  The Givens and least-squares arithmetic is the reference's
+// finish (a ticket counter, FD path) or, in the exact body, by every block of the next
+// kernel from the block partials; both sum in a fixed order (deterministic).  Basis
+// vectors are stored unnormalised with a scale factor sc[i] = 1/|V_i| (FP64) applied
+// wherever they are read.  The Givens and least-squares arithmetic is the reference's
 // (src/Solver.cpp:1562-1599) in FP64.
 //
-// Termination: the last block of an iteration's last kernel (k_gmres_update_dot<T, true>,
-// or k_gmres_update_final on the FD path) is the only place that advances j; it runs
-// once per iteration and clears the loop condition and raises the done flag when j + 1
-// reaches m (or on convergence), so at most m iterations run.  The exact J v graph body
-// holds several iterations (a WHILE iteration costs ~3 us of its own on GB300); the
-// kernels of the iterations after the finishing one see the done flag and return at
-// once.  The same kernels also run outside a
-// graph (in_graph = 0), launched one iteration at a time by a host loop that reads the
+// Termination: the Givens step is the only place that ends the loop: it clears the loop
+// condition and raises the done flag when j + 1 reaches m (or on convergence), so at most
+// m columns are formed.  The exact J v graph body holds several iterations (a WHILE
+// iteration costs ~3 us of its own on GB300); the kernels of the iterations after the
+// finishing one see the done flag and return at once.  The same kernels also run outside
+// a graph (in_graph = 0), launched one iteration at a time by a host loop that reads the
 // done flag: the stream driver, which times every kernel with events.
 #pragma once
 #include <cuda_runtime.h>
@@ -48,21 +50,21 @@ constexpr int KRY_BODY_ITERS = 4;
 
 struct GmresDev {
     int* gi;          // [0] j (FD body), [1] k (last iteration), [2] done, [3] m, [4] this iteration
-                      // (exact J v body), [5] updates completed (exact J v body); 16-byte aligned
+                      // (exact J v body), [5] products reduced (exact J v body); 16-byte aligned
     double* beta;     // [0] beta, [1] tol, [2] beta^2
     double* g;        // [m+1]
     double* cs;       // [m]
     double* sn;       // [m]
-    double* H;        // [(m+1) * m], column j at H + j*(m+1)
+    double* H;        // [(m+1) * m], column j at H + j*(m+1) (rotated)
+    double* Hu;       // [(m+1) * m], the same columns before the rotations (exact J v body)
+    double* sig;      // [m+2] scale of each iteration's pending vector (exact J v body)
     double* y;        // [m]
-    double* h1;       // [m+1] first CGS pass
+    double* h1;       // [m+1] first CGS pass (of the newest column)
     double* h2;       // [m+1] second CGS pass
     double* hsq;      // [2] squared norms ([1]: after the second pass)
     double* sc;       // [m+1] scale of each stored basis vector
-    double* partial;  // [(KRY_MAXM+1) * RED_BLOCKS]
-    double* partial1; // [(KRY_MAXM+1) * RED_BLOCKS] block partials of h1 (exact J v body)
-    int nb1;          // blocks of the gather kernel that writes partial1
-    int nb2;          // blocks of the update kernel that writes partial (exact J v body)
+    double* partial;  // [2 (KRY_MAXM+1) * RED_BLOCKS] block partials (rows of RED_BLOCKS)
+    int nb1;          // blocks of the gather kernel that writes them (exact J v body)
     unsigned* counter;
     int in_graph;     // 1: the kernels run inside the WHILE graph and set its condition
 };
@@ -225,6 +227,7 @@ __global__ void k_gmres_start(long n, T* V0, const double* rhs, GmresDev d, int 
             d.gi[3] = m;
             d.gi[4] = 0;
             d.gi[5] = 0;
+            d.sig[0] = 1.0;
             if (b < 1e-12) {
                 d.gi[1] = -1;
                 d.gi[2] = 1;
@@ -334,15 +337,22 @@ __device__ __forceinline__ void givens_column(const GmresDev& d, int j, int m, d
     for (int i = lane; i <= j + 1; i += 32) Hc[i] = hout[i];
 }
 
-// First kernel of an Arnoldi iteration (exact J v body).  At iteration jn > 0 it first
-// finishes iteration jn - 1: every block sums the update kernel's block partials of h2 and
-// |w|^2, takes |V_jn|^2 = |w|^2 - |h2|^2 (clamped at 0; sc[jn] = 1/|V_jn|, or 1 under the
-// breakdown guard |.| <= 1e-12 of src/Solver.cpp:1553-1558) and forms V_jn = w - sum_{k<jn}
-// h2[k] sc[k] V_k (stored unnormalised) for its cells; one extra block runs the Givens
-// step of column jn - 1 meanwhile and records sc[jn] and this iteration's index for the
-// gather and update kernels.  Then z = V_jn * (1/D) and the primitive stage of the dual
-// J v: W.v, W.d of (U, z).  The iteration after the last one runs only this finishing
-// part (the Givens step raises the done flag; the other kernels then return at once).
+// First kernel of iteration jn of the exact J v body (DCGS2).  Iteration j applied J to
+// the pending vector P_j (slot j of V, scale sig[j]): w = J sig_j P_j.  With jn > 0 every
+// block sums the gather kernel's block partials of <V_k, P_j> and <V_k, w> (k < j, V_k the
+// stored basis vectors) and of |P_j|^2 and <P_j, w>, then, with v_k = sc_k V_k:
+//   s_k = sig_j <v_k, P_j>,  beta^2 = sig_j^2 |P_j|^2 - |s|^2         (Pythagoras)
+//   V_j = P_j - sum_k sc_k^2 <V_k, P_j> V_k   (slot j; sc_j = sig_j / beta)
+//   g_k = <v_k, w> (k < j),  g_j = (sig_j <P_j, w> - s.g) / beta = <v_j, w>
+//   P_jn = w - sum_{k<=j} g_k v_k             (slot jn; sig_jn = 1 / beta)
+// so P_jn = beta (J v_j - V h_j), the first pass of J v_j, since J v_j = (w - J V s) / beta
+// and J V s = V H s over the finished columns: h_j = (g - H s) / beta.  Column j - 1 is
+// (h_{j-1} + s, beta); one extra block runs its Givens step (which can end the solve),
+// then forms h_j and records sc_j, sig_jn and this iteration's index for the gather
+// kernel.  Then z = sig_jn P_jn / D and the primitive stage of the dual J v: W.v, W.d of
+// (U, z).  j = 0 keeps P_0 = V_0 = rhs / |rhs| as it is (beta = 1).  The breakdown guard
+// beta <= 1e-12 (src/Solver.cpp:1553-1558) keeps the scales finite; the Givens step then
+// ends the solve.  Iteration m + 1 runs only the Givens step of column m - 1.
 template <class T, int NV>
 __global__ void __launch_bounds__(256) k_gmres_prim_z(int nc, Flow<T> F, const T* __restrict__ U, T* V, long L,
                                                       const T* __restrict__ Dinv, T* __restrict__ z, Field<T> W,
@@ -353,89 +363,148 @@ __global__ void __launch_bounds__(256) k_gmres_prim_z(int nc, Flow<T> F, const T
     const int4 gb = *reinterpret_cast<const int4*>(d.gi + 4);
     if (ga.z) return;  // the solve has ended
     pdl_trigger();     // the gradient kernel may launch now
-    const int jn = gb.y, m = ga.w;
-    __shared__ A hs[KRY_MAXM];
-    __shared__ double h2s[KRY_MAXM + 1], col[KRY_MAXM + 2];
-    __shared__ double scn, hv_s, hsq_s;
+    const int jn = gb.y, m = ga.w, j = jn - 1;
+    __shared__ A cu[KRY_MAXM + 1], cp[KRY_MAXM + 1];  // coefficients of V_k in V_j and in P_jn
+    __shared__ double dp[KRY_MAXM + 2], dw[KRY_MAXM + 2], sv[KRY_MAXM + 1];
+    __shared__ double r_s, hv_s, hsq_s, scj_s;
     const bool givens_block = blockIdx.x == gridDim.x - 1;
     if (jn > 0) {
-        // dots 0..jn in windows of at most blockDim.x (partials_sum's limit)
-        for (int base = 0; base <= jn; base += blockDim.x) {
-            const int nd = jn + 1 - base < (int)blockDim.x ? jn + 1 - base : (int)blockDim.x;
+        // dots of slots 0..j with P_j (partial rows 0..j) and with w (rows j+1..2j+1), in
+        // windows of at most blockDim.x rows (partials_sum's limit)
+        const int nrow = 2 * (j + 1);
+        for (int base = 0; base < nrow; base += blockDim.x) {
+            const int nd = nrow - base < (int)blockDim.x ? nrow - base : (int)blockDim.x;
             int G;
-            const A sg = partials_sum(reinterpret_cast<const A*>(d.partial) + (long)base * RED_BLOCKS, nd, d.nb2, &G);
-            const int i = base + (int)threadIdx.x / G;
-            if ((int)threadIdx.x / G < nd && threadIdx.x % G == 0)
-                h2s[i] = (i == jn ? 1.0 : d.sc[i]) * (double)sg;  // h2s[jn]: |w|^2
+            const A sg = partials_sum(reinterpret_cast<const A*>(d.partial) + (long)base * RED_BLOCKS, nd, d.nb1, &G);
+            const int r = base + (int)threadIdx.x / G;
+            if ((int)threadIdx.x / G < nd && threadIdx.x % G == 0) {
+                if (r <= j) dp[r] = (double)sg;
+                else dw[r - j - 1] = (double)sg;
+            }
+        }
+        __syncthreads();
+        const double sigj = d.sig[j];
+        for (int k = threadIdx.x; k < j; k += blockDim.x) {
+            const double sck = d.sc[k];
+            sv[k] = sck * sigj * dp[k];
+            dw[k] = sck * dw[k];  // g_k
+            cu[k] = (A)(sck * sck * dp[k]);
         }
         __syncthreads();
         if (threadIdx.x < 32) {
-            A s2p = A(0);
-            for (int k = threadIdx.x; k < jn; k += 32) {
-                const A h = (A)h2s[k];
-                s2p += h * h;  // |h2|^2 in the basis precision (it is ~1e-14 of |w|^2)
+            // |s|^2 and s.g in the basis precision (corrections of ~1e-7 relative with FP32)
+            A ss = A(0), sg = A(0);
+            for (int k = threadIdx.x; k < j; k += 32) {
+                const A sk = (A)sv[k];
+                ss += sk * sk;
+                sg += sk * (A)dw[k];
             }
 #pragma unroll
-            for (int o = 16; o > 0; o >>= 1) s2p += __shfl_xor_sync(0xffffffffu, s2p, o);
+            for (int o = 16; o > 0; o >>= 1) {
+                ss += __shfl_xor_sync(0xffffffffu, ss, o);
+                sg += __shfl_xor_sync(0xffffffffu, sg, o);
+            }
             if (threadIdx.x == 0) {
-                const double hsq = fmax(h2s[jn] - (double)s2p, 0.0);
-                const double r = hsq > 0.0 ? rsqrt(hsq) : 0.0;
-                const double hv = hsq * r;
+                double hsq = 1.0, hv = 1.0, r = 1.0;
+                if (j > 0) {
+                    hsq = fmax(sigj * sigj * dp[j] - (double)ss, 0.0);
+                    const double rq = hsq > 0.0 ? rsqrt(hsq) : 0.0;
+                    hv = hsq * rq;
+                    r = hv > 1e-12 ? rq : 1.0;
+                }
                 hsq_s = hsq;
                 hv_s = hv;
-                scn = hv > 1e-12 ? r : 1.0;
+                r_s = r;
+                scj_s = sigj * r;
+                dw[j] = (sigj * dw[j] - (double)sg) * r;  // g_j
             }
         }
-        for (int k = threadIdx.x; k < jn; k += blockDim.x) hs[k] = (A)(h2s[k] * d.sc[k]);
+        __syncthreads();
+        for (int k = threadIdx.x; k <= j; k += blockDim.x) cp[k] = (A)(dw[k] * (k == j ? scj_s : d.sc[k]));
         __syncthreads();
     }
     if (givens_block) {
-        if (jn > 0 && threadIdx.x < 32) {
-            const int j = jn - 1;
-            for (int i = threadIdx.x; i <= j; i += 32) {
-                col[i] = d.h1[i] + h2s[i];
-                d.h2[i] = h2s[i];
+        if (jn > 0) {
+            __shared__ double col[KRY_MAXM + 2];
+            const int c = j - 1;
+            if (j > 0 && threadIdx.x < 32) {
+                // column j - 1 is final: its first-pass entries plus s, subdiagonal beta
+                double* Hc = d.Hu + (long)c * (m + 1);
+                for (int i = threadIdx.x; i <= c; i += 32) {
+                    col[i] = d.h1[i] + sv[i];
+                    Hc[i] = col[i];
+                }
+                if (threadIdx.x == 0) {
+                    col[c + 1] = hv_s;
+                    Hc[c + 1] = hv_s;
+                }
             }
-            __syncwarp();
-            if (threadIdx.x == 0) {
-                d.sc[jn] = scn;
-                d.hsq[1] = hsq_s;
+            __syncthreads();
+            if (threadIdx.x < 32) {
+                if (j > 0) givens_column(d, c, m, col, hv_s, hsq_s, hnd);
+                if (threadIdx.x == 0) {
+                    d.sc[j] = scj_s;
+                    d.sig[jn] = r_s;
+                    d.hsq[1] = hsq_s;
+                }
+            } else if (j < m) {
+                // meanwhile warps 1.. form column j's first-pass entries h_j = (g - H s) / beta,
+                // one row per thread; H s is a correction of the size of s, so it is summed in
+                // the basis precision (columns before c from memory, column c from col)
+                for (int i = (int)threadIdx.x - 32; i <= j; i += (int)blockDim.x - 32) {
+                    A hs = A(0);
+#pragma unroll 8
+                    for (int k = i > 0 ? i - 1 : 0; k < c; ++k) hs += (A)d.Hu[(long)k * (m + 1) + i] * (A)sv[k];
+                    if (j > 0 && i <= j) hs += (A)col[i] * (A)sv[c];
+                    d.h1[i] = (dw[i] - (double)hs) * r_s;
+                }
             }
-            givens_column(d, j, m, col, hv_s, hsq_s, hnd);
         }
         if (threadIdx.x == 0) d.gi[4] = jn;
         return;
     }
-    T* Vj = V + (long)jn * L;
-    const T sj = jn > 0 ? (T)scn : (T)d.sc[0];
+    if (jn > m) return;  // the last column's Givens step only
+    T* Vj = V + (long)(jn > 0 ? j : 0) * L;
+    T* Vn = V + (long)jn * L;
+    const T sn = jn > 0 ? (T)r_s : T(1);
+    const A cpj = jn > 0 ? cp[j] : A(0);
     const long cstride = (long)(gridDim.x - 1) * blockDim.x;  // the cell blocks, grid-stride
     for (long i = (long)blockIdx.x * blockDim.x + threadIdx.x; i < nc; i += cstride) {
     const T a = Dinv[i];
-    T vj[NV];
+    T pn[NV];
     if (jn > 0) {
-        A acc[NV];
+        A au[NV], ap[NV];
 #pragma unroll
-        for (int c = 0; c < NV; ++c) acc[c] = (A)w[c * nc + i];
+        for (int c = 0; c < NV; ++c) {
+            au[c] = (A)Vj[c * nc + i];
+            ap[c] = (A)w[c * nc + i];
+        }
 #pragma unroll 2
-        for (int k = 0; k < jn; ++k) {
+        for (int k = 0; k < j; ++k) {
             const T* Vk = V + (long)k * L;
-            const A hk = hs[k];
+            const A uk = cu[k], pk = cp[k];
 #pragma unroll
-            for (int c = 0; c < NV; ++c) acc[c] -= hk * (A)Vk[c * nc + i];
+            for (int c = 0; c < NV; ++c) {
+                const A vk = (A)Vk[c * nc + i];
+                au[c] -= uk * vk;
+                ap[c] -= pk * vk;
+            }
         }
 #pragma unroll
         for (int c = 0; c < NV; ++c) {
-            vj[c] = (T)acc[c];
-            Vj[c * nc + i] = vj[c];
+            const T uj = (T)au[c];
+            if (j > 0) Vj[c * nc + i] = uj;
+            pn[c] = (T)(ap[c] - cpj * (A)uj);
+            Vn[c * nc + i] = pn[c];
         }
     } else {
 #pragma unroll
-        for (int c = 0; c < NV; ++c) vj[c] = Vj[c * nc + i];
+        for (int c = 0; c < NV; ++c) pn[c] = Vn[c * nc + i];
     }
     Dual<T> u[6];
 #pragma unroll
     for (int c = 0; c < NV; ++c) {
-        T zc = vj[c] * sj * dinv_of<T, NV>(Dinv, nc, i, c, a);
+        T zc = pn[c] * sn * dinv_of<T, NV>(Dinv, nc, i, c, a);
         z[c * nc + i] = zc;
         u[c] = Dual<T>(U[c * nc + i], zc);
     }
@@ -468,8 +537,11 @@ __global__ void __launch_bounds__(RED_THREADS) k_gmres_multidot(long L, const T*
 }
 
 // The gather of the dual J v (as k_gather: the faces' F*A derivatives in reference face
-// order, minus the SST source derivatives, plus z vol / dt) into w, fused with the first
-// CGS pass h1 = V^T w.  Grid-stride over cells (at most RED_BLOCKS blocks).
+// order, minus the SST source derivatives, plus z vol / dt) into w, fused with the one
+// reduction of the iteration: the dots of slots 0..j of V (the basis vectors V_0..V_{j-1}
+// and the pending vector P_j) with P_j and with w, as block partials (rows 0..j and
+// j+1..2j+1 of partial) that every block of the next k_gmres_prim_z sums.  Grid-stride over cells (at
+// most RED_BLOCKS blocks).
 template <class T, int NV>
 __global__ void __launch_bounds__(RED_THREADS) k_gmres_gather_dot(MeshView<T> m, const T* __restrict__ FA,
                                                                   long fa_stride, T* __restrict__ w,
@@ -481,22 +553,24 @@ __global__ void __launch_bounds__(RED_THREADS) k_gmres_gather_dot(MeshView<T> m,
     const int j = d.gi[4];  // this iteration (set by k_gmres_prim_z)
     if (done) return;       // the solve has ended
     const long nc = m.nc;
-    __shared__ A wsum[KRY_MAXM + 1][KRY_WARPS];
-    __shared__ double scs[KRY_MAXM + 1];
-    for (int i = threadIdx.x; i <= j; i += blockDim.x) scs[i] = d.sc[i];
+    __shared__ A wsw[KRY_MAXM + 1][KRY_WARPS], wsp[KRY_MAXM + 1][KRY_WARPS];
+    const T* Pj = V + (long)j * L;
     // w = the gathered J v of cell i (reference face order).  Everything but the face
     // fluxes comes from two or more kernels back (pdl.cuh), so a thread loads it for its
     // first cell before the wait for the fluxes.
     struct Pre {
         int ek[4];
-        T tc, zc[NV], s4, s5;
+        T tc, zc[NV], pj[NV], s4, s5;
     };
     auto pre = [&](long i, Pre& p) {
 #pragma unroll
         for (int k = 0; k < 4; ++k) p.ek[k] = m.cf[(long)k * nc + i];
         p.tc = m.vol[i] / (dt[i] + T(1e-30));
 #pragma unroll
-        for (int c = 0; c < NV; ++c) p.zc[c] = z[c * nc + i];
+        for (int c = 0; c < NV; ++c) {
+            p.zc[c] = z[c * nc + i];
+            p.pj[c] = Pj[c * nc + i];
+        }
         if constexpr (NV == 6) {
             p.s4 = src[i];
             p.s5 = src[nc + i];
@@ -533,129 +607,136 @@ __global__ void __launch_bounds__(RED_THREADS) k_gmres_gather_dot(MeshView<T> m,
     if (ifirst < nc) pre(ifirst, p0);
     pdl_wait();  // the face fluxes are the predecessor's
     pdl_trigger();
-    if (j < KRY_RC) {
-        // one pass over the cells: up to 32 dots accumulated in two register tiles
-        A v0[KRY_TILE], v1[KRY_TILE];
+    // one pass over the cells when the dots fit the register tiles (two tiles per product
+    // with an FP32 basis, one with FP64)
+    constexpr int RC = sizeof(T) == 4 ? KRY_RC : KRY_TILE;
+    if (j < RC) {
+        A vw0[KRY_TILE], vw1[KRY_TILE], vp0[KRY_TILE], vp1[KRY_TILE];
 #pragma unroll
-        for (int t = 0; t < KRY_TILE; ++t) v0[t] = v1[t] = A(0);
+        for (int t = 0; t < KRY_TILE; ++t) vw0[t] = vw1[t] = vp0[t] = vp1[t] = A(0);
         for (long i = ifirst; i < nc; i += (long)gridDim.x * blockDim.x) {
             T acc[NV];
+            Pre p;
             if (i == ifirst) {
-                gather(i, p0, acc);
+                p = p0;
             } else {
-                Pre p;
                 pre(i, p);
-                gather(i, p, acc);
             }
+            gather(i, p, acc);
 #pragma unroll
-            for (int t = 0; t < KRY_RC; ++t)
+            for (int t = 0; t < RC; ++t)
                 if (t <= j) {
                     const T* Vi = V + (long)t * L;
-                    A s = A(0);
+                    A sw = A(0), sp = A(0);
 #pragma unroll
-                    for (int c = 0; c < NV; ++c) s += (A)acc[c] * (A)Vi[c * nc + i];
-                    if (t < KRY_TILE) v0[t] += s;
-                    else v1[t - KRY_TILE] += s;
+                    for (int c = 0; c < NV; ++c) {
+                        const A vt = (A)Vi[c * nc + i];
+                        sw += (A)acc[c] * vt;
+                        sp += (A)p.pj[c] * vt;
+                    }
+                    if (t < KRY_TILE) {
+                        vw0[t] += sw;
+                        vp0[t] += sp;
+                    } else {
+                        vw1[t - KRY_TILE] += sw;
+                        vp1[t - KRY_TILE] += sp;
+                    }
                 }
         }
-        tile_to_smem(v0, 0, j + 1 < KRY_TILE ? j + 1 : KRY_TILE, wsum);
-        if (j >= KRY_TILE) tile_to_smem(v1, KRY_TILE, j + 1 - KRY_TILE, wsum);
+        const int n0 = j + 1 < KRY_TILE ? j + 1 : KRY_TILE;
+        tile_to_smem(vw0, 0, n0, wsw);
+        tile_to_smem(vp0, 0, n0, wsp);
+        if (RC > KRY_TILE && j >= KRY_TILE) {
+            tile_to_smem(vw1, KRY_TILE, j + 1 - KRY_TILE, wsw);
+            tile_to_smem(vp1, KRY_TILE, j + 1 - KRY_TILE, wsp);
+        }
     } else {
         for (int i0 = 0; i0 <= j; i0 += KRY_TILE) {
             const int nt = (j + 1 - i0) < KRY_TILE ? (j + 1 - i0) : KRY_TILE;
-            A v[KRY_TILE];
+            A vw[KRY_TILE], vp[KRY_TILE];
 #pragma unroll
-            for (int t = 0; t < KRY_TILE; ++t) v[t] = A(0);
-            for (long i = (long)blockIdx.x * blockDim.x + threadIdx.x; i < nc; i += (long)gridDim.x * blockDim.x) {
-                T acc[NV];
+            for (int t = 0; t < KRY_TILE; ++t) vw[t] = vp[t] = A(0);
+            for (long i = ifirst; i < nc; i += (long)gridDim.x * blockDim.x) {
+                T acc[NV], pj[NV];
                 if (i0 == 0) {
                     Pre p;
-                    pre(i, p);
+                    if (i == ifirst) {
+                        p = p0;
+                    } else {
+                        pre(i, p);
+                    }
                     gather(i, p, acc);
+#pragma unroll
+                    for (int c = 0; c < NV; ++c) pj[c] = p.pj[c];
                 } else {
 #pragma unroll
-                    for (int c = 0; c < NV; ++c) acc[c] = w[c * nc + i];
+                    for (int c = 0; c < NV; ++c) {
+                        acc[c] = w[c * nc + i];
+                        pj[c] = Pj[c * nc + i];
+                    }
                 }
 #pragma unroll
                 for (int t = 0; t < KRY_TILE; ++t)
                     if (t < nt) {
                         const T* Vi = V + (long)(i0 + t) * L;
-                        A s = A(0);
+                        A sw = A(0), sp = A(0);
 #pragma unroll
-                        for (int c = 0; c < NV; ++c) s += (A)acc[c] * (A)Vi[c * nc + i];
-                        v[t] += s;
+                        for (int c = 0; c < NV; ++c) {
+                            const A vt = (A)Vi[c * nc + i];
+                            sw += (A)acc[c] * vt;
+                            sp += (A)pj[c] * vt;
+                        }
+                        vw[t] += sw;
+                        vp[t] += sp;
                     }
             }
-            tile_to_smem(v, i0, nt, wsum);
+            tile_to_smem(vw, i0, nt, wsw);
+            tile_to_smem(vp, i0, nt, wsp);
         }
     }
     // block partials only: every block of the next kernel sums them itself (partials_sum),
     // which costs less than a last-block reduction here and its fence and ticket
-    block_partials(reinterpret_cast<A*>(d.partial1), j, wsum);
+    block_partials(reinterpret_cast<A*>(d.partial), j, wsp);
+    block_partials(reinterpret_cast<A*>(d.partial) + (long)(j + 1) * RED_BLOCKS, j, wsw);
+    if (blockIdx.x == 0 && threadIdx.x == 0) d.gi[5] = j + 1;  // products reduced
 }
 
-// w -= sum_{i<=j} h1[i] sc[i] V_i, fused with the second CGS pass h2 = V^T w.  Without
-// LAST (the FD J v body) the last block to finish sums the h2 partials.  With LAST (the
-// exact J v body) h1 comes from the gather kernel's block partials (summed by every
-// block), the kernel also takes |w|^2, and it only writes its block partials of h2 and
-// |w|^2: the next iteration's k_gmres_prim_z sums them, forms V_{j+1} = w - V h2 and runs
-// the Givens step.
-template <class T, bool LAST>
+// w -= sum_{i<=j} h1[i] sc[i] V_i, fused with the second CGS pass h2 = V^T w (FD J v
+// body); the last block to finish sums the h2 partials.
+template <class T>
 __global__ void __launch_bounds__(RED_THREADS) k_gmres_update_dot(long L, T* __restrict__ w, const T* __restrict__ V,
-                                                                  GmresDev d, cudaGraphConditionalHandle hnd) {
+                                                                  GmresDev d) {
     typedef typename KryAcc<T>::type A;
-    const int4 gi4 = *reinterpret_cast<const int4*>(d.gi);
-    if (LAST && gi4.z) return;  // the solve has ended
-    const int j = LAST ? d.gi[4] : gi4.x;  // this iteration
+    const int j = d.gi[0];
     __shared__ A hs[KRY_MAXM + 1];
     __shared__ A wsum[KRY_MAXM + 1][KRY_WARPS];
     __shared__ double scs[KRY_MAXM + 1];
-    // sc first, then (after the wait) h1 and w, which are the predecessor's (pdl.cuh)
-    for (int i = threadIdx.x; i <= j; i += blockDim.x) scs[i] = d.sc[i];
-    pdl_wait();
-    pdl_trigger();
+    for (int i = threadIdx.x; i <= j; i += blockDim.x) {
+        scs[i] = d.sc[i];
+        hs[i] = (A)(d.h1[i] * scs[i]);
+    }
+    __syncthreads();
     // one pass (j < KRY_RC): each element's basis values stay in registers between the
     // update and the dots, and (FP32) a thread's three grid-stride elements are loaded
-    // together, so their loads are in flight at once; with FP32 the first such group is
-    // loaded before the h1 reduction below, so its loads overlap it
+    // together, so their loads are in flight at once
     constexpr int EPT = sizeof(T) == 4 ? 3 : 1;
     const long stride = (long)gridDim.x * blockDim.x;
     const long qfirst = (long)blockIdx.x * blockDim.x + threadIdx.x;
-    T vv[EPT][KRY_RC];
-    A a[EPT];
-    auto load_group = [&](long q0) {
-#pragma unroll
-        for (int e = 0; e < EPT; ++e) {
-            const long q = q0 + e * stride;
-            const bool ok = q < L;
-            a[e] = ok ? (A)w[q] : A(0);
-#pragma unroll
-            for (int t = 0; t < KRY_RC; ++t) vv[e][t] = ok && t <= j ? V[(long)t * L + q] : T(0);
-        }
-    };
-    constexpr bool early = sizeof(T) == 4;  // (FP64: the registers are not there)
-    if (early && j < KRY_RC) load_group(qfirst);
-    if (LAST) {
-        // h1 = sc * (the gather kernel's block partials), summed by every block
-        int G;
-        const A sg = partials_sum(reinterpret_cast<const A*>(d.partial1), j + 1, d.nb1, &G);
-        const int i = threadIdx.x / G;
-        if (i <= j && threadIdx.x % G == 0) {
-            const double h1 = scs[i] * (double)sg;
-            hs[i] = (A)(h1 * scs[i]);
-            if (blockIdx.x == 0) d.h1[i] = h1;  // for the Givens step
-        }
-    } else {
-        for (int i = threadIdx.x; i <= j; i += blockDim.x) hs[i] = (A)(d.h1[i] * scs[i]);
-    }
-    __syncthreads();
-    A nw = A(0);
     if (j < KRY_RC) {
+        T vv[EPT][KRY_RC];
+        A a[EPT];
         A v0[KRY_TILE], v1[KRY_TILE];
 #pragma unroll
         for (int t = 0; t < KRY_TILE; ++t) v0[t] = v1[t] = A(0);
         for (long q0 = qfirst; q0 < L; q0 += EPT * stride) {
-            if (!early || q0 != qfirst) load_group(q0);
+#pragma unroll
+            for (int e = 0; e < EPT; ++e) {
+                const long q = q0 + e * stride;
+                const bool ok = q < L;
+                a[e] = ok ? (A)w[q] : A(0);
+#pragma unroll
+                for (int t = 0; t < KRY_RC; ++t) vv[e][t] = ok && t <= j ? V[(long)t * L + q] : T(0);
+            }
 #pragma unroll
             for (int e = 0; e < EPT; ++e) {
                 const long q = q0 + e * stride;
@@ -666,7 +747,6 @@ __global__ void __launch_bounds__(RED_THREADS) k_gmres_update_dot(long L, T* __r
                     if (t <= j) ae -= hs[t] * (A)vv[e][t];
                 const T tq = (T)ae;
                 w[q] = tq;
-                if (LAST) nw += (A)tq * (A)tq;
 #pragma unroll
                 for (int t = 0; t < KRY_TILE; ++t) {
                     v0[t] += (A)tq * (A)vv[e][t];
@@ -677,19 +757,17 @@ __global__ void __launch_bounds__(RED_THREADS) k_gmres_update_dot(long L, T* __r
         tile_to_smem(v0, 0, j + 1 < KRY_TILE ? j + 1 : KRY_TILE, wsum);
         if (j >= KRY_TILE) tile_to_smem(v1, KRY_TILE, j + 1 - KRY_TILE, wsum);
     } else {
-        for (long q = (long)blockIdx.x * blockDim.x + threadIdx.x; q < L; q += (long)gridDim.x * blockDim.x) {
+        for (long q = qfirst; q < L; q += stride) {
             A a = (A)w[q];
             for (int i = 0; i <= j; ++i) a -= hs[i] * (A)V[(long)i * L + q];
-            T t = (T)a;
-            w[q] = t;
-            if (LAST) nw += (A)t * (A)t;
+            w[q] = (T)a;
         }
         for (int i0 = 0; i0 <= j; i0 += KRY_TILE) {
             const int nt = (j + 1 - i0) < KRY_TILE ? (j + 1 - i0) : KRY_TILE;
             A v[KRY_TILE];
 #pragma unroll
             for (int t = 0; t < KRY_TILE; ++t) v[t] = A(0);
-            for (long q = (long)blockIdx.x * blockDim.x + threadIdx.x; q < L; q += (long)gridDim.x * blockDim.x) {
+            for (long q = qfirst; q < L; q += stride) {
                 A wq = (A)w[q];
 #pragma unroll
                 for (int t = 0; t < KRY_TILE; ++t)
@@ -698,16 +776,7 @@ __global__ void __launch_bounds__(RED_THREADS) k_gmres_update_dot(long L, T* __r
             tile_to_smem(v, i0, nt, wsum);
         }
     }
-    if (LAST) {
-        nw = warp_sum_t(nw);
-        if ((threadIdx.x & 31) == 0) wsum[j + 1][threadIdx.x >> 5] = nw;
-    }
-    if (!LAST) {
-        dots_finish(d, j, wsum, d.h2, -1, scs);
-        return;
-    }
-    block_partials(reinterpret_cast<A*>(d.partial), j + 1, wsum);  // rows 0..j: h2, j + 1: |w|^2
-    if (blockIdx.x == 0 && threadIdx.x == 0) d.gi[5] = j + 1;      // updates completed
+    dots_finish(d, j, wsum, d.h2, -1, scs);
 }
 
 // Hessenberg column, Givens rotations and the convergence test (src/Solver.cpp:1550-1588);

@@ -168,9 +168,10 @@ template <class T> void launch_gmres_dinv(int nv, long nc, const double* D, T* D
 template <class T> void launch_gmres_z(int nv, long nc, const T* V, long L, const T* Dinv, T* z, const GmresDev& d,
                                        cudaStream_t s);
 template <class T> void launch_gmres_multidot(long L, const T* w, const T* V, const GmresDev& d, double* h, cudaStream_t s);
-// the fused Arnoldi stages (krylov.cuh): deferred V_j + z + dual primitives, gather +
-// first CGS pass, update + second pass (+ norm + Givens in the exact J v body); the FD
-// J v body's final update + norm + Givens
+// the fused Arnoldi stages (krylov.cuh): the exact J v body's second pass of the pending
+// vector + first pass of the last product + z + dual primitives (+ Givens), and its
+// gather + the iteration's dots; the FD J v body's update + second pass and final
+// update + norm + Givens
 template <class T> void launch_gmres_prim_z(int nv, long nc, const Flow<T>& F, const T* U, T* V, long L,
                                             const T* Dinv, T* z, Field<T> W, const T* w, const GmresDev& d,
                                             cudaGraphConditionalHandle h, cudaStream_t s);
@@ -178,8 +179,6 @@ template <class T> void launch_gmres_gather_dot(int nv, const MeshView<T>& m, co
                                                 const T* dt, const T* src, const T* V, long L, const GmresDev& d,
                                                 cudaStream_t s, bool pdl = false);
 template <class T> void launch_gmres_update_dot(long L, T* w, const T* V, const GmresDev& d, cudaStream_t s);
-template <class T> void launch_gmres_update_dot_last(long L, T* w, const T* V, const GmresDev& d,
-                                                     cudaGraphConditionalHandle h, cudaStream_t s, bool pdl = false);
 template <class T> void launch_gmres_update_final(long L, const T* w, T* V, const GmresDev& d,
                                                   cudaGraphConditionalHandle h, cudaStream_t s);
 template <class T> void launch_gmres_solution_dev(int nv, long nc, const T* V, long L, const GmresDev& d,

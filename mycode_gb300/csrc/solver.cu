@@ -151,8 +151,9 @@ struct cfdg_solver {
     size_t pool_used = 0;
     std::vector<std::pair<int, std::pair<size_t, int>>> pending;
     // classes 8-11: the VJP's forward recomputation, face adjoint, cell gathers 1 and 2
-    // classes 12-17: the fused Krylov body (stream driver): z + primitives, gradients
-    // (+ SST terms), face fluxes, gather + first CGS pass, update + second pass, final update
+    // classes 12-17: the fused Krylov body (stream driver): second and first passes + z +
+    // primitives, gradients (+ SST terms), face fluxes, gather + dots; 16-17 the FD body's
+    // update + second pass and final update (not timed)
     static constexpr int NSTAT = 18;
     double kstat_ms[NSTAT] = {};
     long long kstat_n[NSTAT] = {};
@@ -494,7 +495,7 @@ struct cfdg_solver {
                                       "(its blocks were not all resident); set persistent = 0");
     }
 
-    // the persistent Arnoldi kernel (arnoldi.cuh) replaces the fused five-kernel body in
+    // the persistent Arnoldi kernel (arnoldi.cuh) replaces the fused four-kernel body in
     // the graph driver for the exact J v; grid = the blocks that fit at once
     unsigned* bar = nullptr;
     double* apart = nullptr;
@@ -617,8 +618,8 @@ struct cfdg_solver {
             ++launches;
             return CFDG_OK;
         }
-        // ev (stream driver with timing): 6 events around the 5 stages, stat classes 12-16
-        cudaEvent_t* ev = (mixed || cfg.jv == CFDG_JV_EXACT) ? take_events(12, 5) : nullptr;
+        // ev (stream driver with timing): 5 events around the 4 stages, stat classes 12-15
+        cudaEvent_t* ev = (mixed || cfg.jv == CFDG_JV_EXACT) ? take_events(12, 4) : nullptr;
         // programmatic dependent launch for the kernels after the first (pdl.cuh); not
         // with per-kernel events, which time each kernel alone
         const bool pdl = cfg.pdl && !ev && !pdl_failed;
@@ -634,9 +635,11 @@ struct cfdg_solver {
     // WHILE-body executions of a graph solve of `iters` iterations
     long long body_runs(int iters) const {
         if (use_persistent() || !(cfg.precision == CFDG_MIXED || cfg.jv == CFDG_JV_EXACT)) return iters;
-        // the exact J v body runs once more than the iterations (the last run ends the solve)
+        // the exact J v body runs twice more than the iterations: the column of iteration
+        // j is final after the product of iteration j + 1, and its Givens step runs in the
+        // first kernel of iteration j + 2
         const int u = body_unroll();
-        return (iters + 1 + u - 1) / u;
+        return (iters + 2 + u - 1) / u;
     }
 
     cfdg_status enqueue_arnoldi_iteration(double* Ubase, double* Rbase, cudaGraphConditionalHandle h,
@@ -664,9 +667,7 @@ struct cfdg_solver {
             launch_gmres_gather_dot<float>(nv, mvf, FA32d, w32, z32, dt32, nv == 6 ? T32d + 2 * nc : nullptr, V32, L, gd,
                                            st, pdl);
             if (ev) CK(cudaEventRecord(ev[4], st));
-            launch_gmres_update_dot_last<float>(L, w32, V32, gd, h, st, pdl);
-            if (ev) CK(cudaEventRecord(ev[5], st));
-            launches += nv == 6 ? 6 : 5;
+            launches += nv == 6 ? 5 : 4;
         } else if (cfg.jv == CFDG_JV_EXACT) {
             launch_gmres_prim_z<double>(nv, nc, F, Ubase, V, L, dinv64, z, f64(Wj, Wjd), w64, gd, h, st);
             ResArgs<double> a;
@@ -688,9 +689,7 @@ struct cfdg_solver {
             launch_gmres_gather_dot<double>(nv, mv, FAjd, w64, z, dt, nv == 6 ? Tjd + 2 * nc : nullptr, V, L, gd, st,
                                             pdl);
             if (ev) CK(cudaEventRecord(ev[4], st));
-            launch_gmres_update_dot_last<double>(L, w64, V, gd, h, st, pdl);
-            if (ev) CK(cudaEventRecord(ev[5], st));
-            launches += nv == 6 ? 6 : 5;
+            launches += nv == 6 ? 5 : 4;
         } else {
             launch_gmres_z<double>(nv, nc, V, L, dinv64, z, gd, st);
             ++launches;
@@ -815,10 +814,10 @@ struct cfdg_solver {
         int done = 0;
         CK(cudaMemcpyAsync(&done, gd.gi + 2, sizeof(int), cudaMemcpyDeviceToHost, st));
         CK(cudaStreamSynchronize(st));
-        // the exact J v body finishes iteration j in the first kernel of iteration j + 1, so
-        // it runs once more than the iterations (that last run only ends the solve)
+        // the exact J v body finishes column j in the first kernel of iteration j + 2, so it
+        // runs twice more than the iterations (the last run only ends the solve)
         const bool exact_body = cfg.precision == CFDG_MIXED || cfg.jv == CFDG_JV_EXACT;
-        for (int it = 0; !done && it < cfg.gmres_m + (exact_body ? 1 : 0); ++it) {
+        for (int it = 0; !done && it < cfg.gmres_m + (exact_body ? 2 : 0); ++it) {
             cfdg_status e = enqueue_gmres_body(Ubase, Rbase, none);
             if (e != CFDG_OK) {
                 gd.in_graph = 1;
@@ -1617,8 +1616,8 @@ cfdg_status cfdg_solver_create(const cfdg_mesh* m, const cfdg_config* cfg, cfdg_
     if (c.gmres_m <= KRY_MAXM) {  // device-GMRES state, so the driver can be switched at run time
         int m = c.gmres_m;
         TRYS(dalloc(&s->gdi, 8));
-        size_t nd = 3 + (size_t)(m + 1) + 2 * (size_t)m + (size_t)(m + 1) * m + m + 2 * (size_t)(m + 1) + 2 +
-                    (size_t)(m + 1) + 2 * (size_t)(KRY_MAXM + 1) * RED_BLOCKS + 4;
+        size_t nd = 3 + (size_t)(m + 1) + 2 * (size_t)m + 2 * (size_t)(m + 1) * m + (size_t)(m + 2) + m +
+                    2 * (size_t)(m + 1) + 2 + (size_t)(m + 1) + 2 * (size_t)(KRY_MAXM + 1) * RED_BLOCKS + 4;
         TRYS(dalloc(&s->gdd, nd));
         double* q = s->gdd;
         GmresDev& d = s->gd;
@@ -1628,15 +1627,15 @@ cfdg_status cfdg_solver_create(const cfdg_mesh* m, const cfdg_config* cfg, cfdg_
         d.cs = q; q += m;
         d.sn = q; q += m;
         d.H = q; q += (size_t)(m + 1) * m;
+        d.Hu = q; q += (size_t)(m + 1) * m;
+        d.sig = q; q += m + 2;
         d.y = q; q += m;
         d.h1 = q; q += m + 1;
         d.h2 = q; q += m + 1;
         d.hsq = q; q += 2;
         d.sc = q; q += m + 1;
-        d.partial = q; q += (size_t)(KRY_MAXM + 1) * RED_BLOCKS;
-        d.partial1 = q; q += (size_t)(KRY_MAXM + 1) * RED_BLOCKS;
+        d.partial = q; q += 2 * (size_t)(KRY_MAXM + 1) * RED_BLOCKS;
         d.nb1 = (int)kry_grid(nc);
-        d.nb2 = (int)kry_grid(L);
         d.counter = reinterpret_cast<unsigned*>(q);
         d.in_graph = 1;
         if (c.precision == CFDG_MIXED) TRYS(dalloc(&s->w32, (size_t)L));
