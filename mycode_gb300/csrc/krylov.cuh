@@ -369,6 +369,9 @@ __global__ void __launch_bounds__(256) k_gmres_prim_z(int nc, Flow<T> F, const T
     __shared__ double r_s, hv_s, hsq_s, scj_s;
     const bool givens_block = blockIdx.x == gridDim.x - 1;
     if (jn > 0) {
+        // the scales (lane k of warp 0: sc_k) and sig_j load with the partials
+        const double sigj = d.sig[j];
+        const double sclane = (int)threadIdx.x < j && threadIdx.x < 32 ? d.sc[threadIdx.x] : 0.0;
         // dots of slots 0..j with P_j (partial rows 0..j) and with w (rows j+1..2j+1), in
         // windows of at most blockDim.x rows (partials_sum's limit)
         const int nrow = 2 * (j + 1);
@@ -383,21 +386,19 @@ __global__ void __launch_bounds__(256) k_gmres_prim_z(int nc, Flow<T> F, const T
             }
         }
         __syncthreads();
-        const double sigj = d.sig[j];
-        for (int k = threadIdx.x; k < j; k += blockDim.x) {
-            const double sck = d.sc[k];
-            sv[k] = sck * sigj * dp[k];
-            dw[k] = sck * dw[k];  // g_k
-            cu[k] = (A)(sck * sck * dp[k]);
-        }
-        __syncthreads();
         if (threadIdx.x < 32) {
-            // |s|^2 and s.g in the basis precision (corrections of ~1e-7 relative with FP32)
+            // warp 0: s_k, g_k and the coefficients, lane k; |s|^2 and s.g in the basis
+            // precision (corrections of ~1e-7 relative with FP32)
             A ss = A(0), sg = A(0);
             for (int k = threadIdx.x; k < j; k += 32) {
-                const A sk = (A)sv[k];
-                ss += sk * sk;
-                sg += sk * (A)dw[k];
+                const double sck = k < 32 ? sclane : d.sc[k];
+                const double sk = sck * sigj * dp[k], gk = sck * dw[k];
+                sv[k] = sk;
+                dw[k] = gk;
+                cu[k] = (A)(sck * sck * dp[k]);
+                cp[k] = (A)(gk * sck);
+                ss += (A)sk * (A)sk;
+                sg += (A)sk * (A)gk;
             }
 #pragma unroll
             for (int o = 16; o > 0; o >>= 1) {
@@ -416,11 +417,11 @@ __global__ void __launch_bounds__(256) k_gmres_prim_z(int nc, Flow<T> F, const T
                 hv_s = hv;
                 r_s = r;
                 scj_s = sigj * r;
-                dw[j] = (sigj * dw[j] - (double)sg) * r;  // g_j
+                const double gj = (sigj * dw[j] - (double)sg) * r;
+                dw[j] = gj;
+                cp[j] = (A)(gj * (sigj * r));
             }
         }
-        __syncthreads();
-        for (int k = threadIdx.x; k <= j; k += blockDim.x) cp[k] = (A)(dw[k] * (k == j ? scj_s : d.sc[k]));
         __syncthreads();
     }
     if (givens_block) {
