@@ -45,7 +45,8 @@ namespace cfdg {
 
 constexpr int KRY_MAXM = 128;  // largest Krylov dimension of the device solver
 // Arnoldi iterations per WHILE-body execution with the exact J v; measured on the
-// 28,800-cell plate: 1, 2, 4 give 574, 583, 584 M cell-residuals/s
+// 28,800-cell plate with the four-kernel body: 3, 4, 5, 6 give 783.5, 783, 780, 780 M
+// cell-residuals/s (the same GB300)
 constexpr int KRY_BODY_ITERS = 4;
 
 struct GmresDev {
