@@ -59,12 +59,13 @@ struct GmresDev {
     double* H;        // [(m+1) * m], column j at H + j*(m+1) (rotated)
     double* Hu;       // [(m+1) * m], the same columns before the rotations (exact J v body)
     double* sig;      // [m+2] scale of each iteration's pending vector (exact J v body)
+    double* ilam;     // [m+2] its first-pass vector over that vector (exact J v body)
     double* y;        // [m]
     double* h1;       // [m+1] first CGS pass (of the newest column)
     double* h2;       // [m+1] second CGS pass
     double* hsq;      // [2] squared norms ([1]: after the second pass)
     double* sc;       // [m+1] scale of each stored basis vector
-    double* partial;  // [2 (KRY_MAXM+1) * RED_BLOCKS] block partials (rows of RED_BLOCKS)
+    double* partial;  // [(2 KRY_MAXM + 3) * RED_BLOCKS] block partials (rows of RED_BLOCKS)
     int nb1;          // blocks of the gather kernel that writes them (exact J v body)
     unsigned* counter;
     int in_graph;     // 1: the kernels run inside the WHILE graph and set its condition
@@ -229,6 +230,7 @@ __global__ void k_gmres_start(long n, T* V0, const double* rhs, GmresDev d, int 
             d.gi[4] = 0;
             d.gi[5] = 0;
             d.sig[0] = 1.0;
+            d.ilam[0] = 1.0;
             if (b < 1e-12) {
                 d.gi[1] = -1;
                 d.gi[2] = 1;
@@ -341,19 +343,22 @@ __device__ __forceinline__ void givens_column(const GmresDev& d, int j, int m, d
 // First kernel of iteration jn of the exact J v body (DCGS2).  Iteration j applied J to
 // the pending vector P_j (slot j of V, scale sig[j]): w = J sig_j P_j.  With jn > 0 every
 // block sums the gather kernel's block partials of <V_k, P_j> and <V_k, w> (k < j, V_k the
-// stored basis vectors) and of |P_j|^2 and <P_j, w>, then, with v_k = sc_k V_k:
+// stored basis vectors), |P_j|^2, <P_j, w> and |w|^2, then, with v_k = sc_k V_k:
 //   s_k = sig_j <v_k, P_j>,  beta^2 = sig_j^2 |P_j|^2 - |s|^2         (Pythagoras)
 //   V_j = P_j - sum_k sc_k^2 <V_k, P_j> V_k   (slot j; sc_j = sig_j / beta)
 //   g_k = <v_k, w> (k < j),  g_j = (sig_j <P_j, w> - s.g) / beta = <v_j, w>
-//   P_jn = w - sum_{k<=j} g_k v_k             (slot jn; sig_jn = 1 / beta)
-// so P_jn = beta (J v_j - V h_j), the first pass of J v_j, since J v_j = (w - J V s) / beta
-// and J V s = V H s over the finished columns: h_j = (g - H s) / beta.  Column j - 1 is
-// (h_{j-1} + s, beta); one extra block runs its Givens step (which can end the solve),
-// then forms h_j and records sc_j, sig_jn and this iteration's index for the gather
-// kernel.  Then z = sig_jn P_jn / D and the primitive stage of the dual J v: W.v, W.d of
-// (U, z).  j = 0 keeps P_0 = V_0 = rhs / |rhs| as it is (beta = 1).  The breakdown guard
-// beta <= 1e-12 (src/Solver.cpp:1553-1558) keeps the scales finite; the Givens step then
-// ends the solve.  Iteration m + 1 runs only the Givens step of column m - 1.
+//   P_jn = w - sum_{k<=j} g_k v_k             (slot jn; sig_jn = 1 / |w|)
+// J v_j = (w - J V s) / beta and J V s = V H s over the finished columns (the Arnoldi
+// relation), so P_jn = beta (J v_j - V h_j) with the first-pass entries h_j = (g - H s) /
+// beta: the pending vector sig_jn P_jn is lam_jn = sig_jn beta times the first-pass vector
+// of J v_j.  Scaling by 1/|w| keeps every product's input at norm <= 1 (their dots stay
+// in range in FP32 for stiff systems).  Column j - 1 is (h_{j-1} + s / lam_j, beta /
+// lam_j); one extra block runs its Givens step (which can end the solve), then forms h_j
+// and records sc_j, sig_jn, 1/lam_jn and this iteration's index for the gather kernel.
+// Then z = sig_jn P_jn / D and the primitive stage of the dual J v: W.v, W.d of (U, z).
+// j = 0 keeps P_0 = V_0 = rhs / |rhs| as it is (beta = 1).  The breakdown guard beta <=
+// 1e-12 (src/Solver.cpp:1553-1558) keeps the scales finite; the Givens step then ends the
+// solve.  Iteration m + 1 runs only the Givens step of column m - 1.
 template <class T, int NV>
 __global__ void __launch_bounds__(256) k_gmres_prim_z(int nc, Flow<T> F, const T* __restrict__ U, T* V, long L,
                                                       const T* __restrict__ Dinv, T* __restrict__ z, Field<T> W,
@@ -367,15 +372,15 @@ __global__ void __launch_bounds__(256) k_gmres_prim_z(int nc, Flow<T> F, const T
     const int jn = gb.y, m = ga.w, j = jn - 1;
     __shared__ A cu[KRY_MAXM + 1], cp[KRY_MAXM + 1];  // coefficients of V_k in V_j and in P_jn
     __shared__ double dp[KRY_MAXM + 2], dw[KRY_MAXM + 2], sv[KRY_MAXM + 1];
-    __shared__ double r_s, hv_s, hsq_s, scj_s;
+    __shared__ double r_s, hv_s, hsq_s, scj_s, sgn_s, ilmn_s, ilam_s;
     const bool givens_block = blockIdx.x == gridDim.x - 1;
     if (jn > 0) {
-        // the scales (lane k of warp 0: sc_k) and sig_j load with the partials
-        const double sigj = d.sig[j];
+        // the scales (lane k of warp 0: sc_k), sig_j and 1/lam_j load with the partials
+        const double sigj = d.sig[j], ilamj = d.ilam[j];
         const double sclane = (int)threadIdx.x < j && threadIdx.x < 32 ? d.sc[threadIdx.x] : 0.0;
-        // dots of slots 0..j with P_j (partial rows 0..j) and with w (rows j+1..2j+1), in
-        // windows of at most blockDim.x rows (partials_sum's limit)
-        const int nrow = 2 * (j + 1);
+        // dots of slots 0..j with P_j (partial rows 0..j) and with w (rows j+1..2j+1), |w|^2
+        // (row 2j+2), in windows of at most blockDim.x rows (partials_sum's limit)
+        const int nrow = 2 * (j + 1) + 1;
         for (int base = 0; base < nrow; base += blockDim.x) {
             const int nd = nrow - base < (int)blockDim.x ? nrow - base : (int)blockDim.x;
             int G;
@@ -412,7 +417,7 @@ __global__ void __launch_bounds__(256) k_gmres_prim_z(int nc, Flow<T> F, const T
                     hsq = fmax(sigj * sigj * dp[j] - (double)ss, 0.0);
                     const double rq = hsq > 0.0 ? rsqrt(hsq) : 0.0;
                     hv = hsq * rq;
-                    r = hv > 1e-12 ? rq : 1.0;
+                    r = hv * ilamj > 1e-12 ? rq : 1.0;  // the guard on the column's entry hv / lam_j
                 }
                 hsq_s = hsq;
                 hv_s = hv;
@@ -421,6 +426,13 @@ __global__ void __launch_bounds__(256) k_gmres_prim_z(int nc, Flow<T> F, const T
                 const double gj = (sigj * dw[j] - (double)sg) * r;
                 dw[j] = gj;
                 cp[j] = (A)(gj * (sigj * r));
+                // sig_jn = 1/|w|, 1/lam_jn = r/sig_jn = r |w| (multiplies: an FP64 divide costs
+                // about seven dependent FMAs)
+                const double wsq = dw[j + 1];
+                const double sgn = wsq > 0.0 ? rsqrt(wsq) : 1.0;
+                sgn_s = sgn;
+                ilmn_s = r * (wsq > 0.0 ? wsq * sgn : 1.0);
+                ilam_s = ilamj;
             }
         }
         __syncthreads();
@@ -431,22 +443,28 @@ __global__ void __launch_bounds__(256) k_gmres_prim_z(int nc, Flow<T> F, const T
             const int c = j - 1;
             if (j > 0 && threadIdx.x < 32) {
                 // column j - 1 is final: its first-pass entries plus s, subdiagonal beta
+                // (P_j is lam_j times the first-pass vector of column j - 1)
                 double* Hc = d.Hu + (long)c * (m + 1);
+                const double il = ilam_s;
                 for (int i = threadIdx.x; i <= c; i += 32) {
-                    col[i] = d.h1[i] + sv[i];
+                    col[i] = d.h1[i] + sv[i] * il;
                     Hc[i] = col[i];
                 }
                 if (threadIdx.x == 0) {
-                    col[c + 1] = hv_s;
-                    Hc[c + 1] = hv_s;
+                    col[c + 1] = hv_s * il;
+                    Hc[c + 1] = col[c + 1];
                 }
             }
             __syncthreads();
             if (threadIdx.x < 32) {
-                if (j > 0) givens_column(d, c, m, col, hv_s, hsq_s, hnd);
+                if (j > 0) {
+                    const double hvc = col[c + 1];
+                    givens_column(d, c, m, col, hvc, hvc * hvc, hnd);
+                }
                 if (threadIdx.x == 0) {
                     d.sc[j] = scj_s;
-                    d.sig[jn] = r_s;
+                    d.sig[jn] = sgn_s;
+                    d.ilam[jn] = ilmn_s;
                     d.hsq[1] = hsq_s;
                 }
             } else if (j < m) {
@@ -468,7 +486,7 @@ __global__ void __launch_bounds__(256) k_gmres_prim_z(int nc, Flow<T> F, const T
     if (jn > m) return;  // the last column's Givens step only
     T* Vj = V + (long)(jn > 0 ? j : 0) * L;
     T* Vn = V + (long)jn * L;
-    const T sn = jn > 0 ? (T)r_s : T(1);
+    const T sn = jn > 0 ? (T)sgn_s : T(1);
     const A cpj = jn > 0 ? cp[j] : A(0);
     const long cstride = (long)(gridDim.x - 1) * blockDim.x;  // the cell blocks, grid-stride
     for (long i = (long)blockIdx.x * blockDim.x + threadIdx.x; i < nc; i += cstride) {
@@ -541,8 +559,8 @@ __global__ void __launch_bounds__(RED_THREADS) k_gmres_multidot(long L, const T*
 // The gather of the dual J v (as k_gather: the faces' F*A derivatives in reference face
 // order, minus the SST source derivatives, plus z vol / dt) into w, fused with the one
 // reduction of the iteration: the dots of slots 0..j of V (the basis vectors V_0..V_{j-1}
-// and the pending vector P_j) with P_j and with w, as block partials (rows 0..j and
-// j+1..2j+1 of partial) that every block of the next k_gmres_prim_z sums.  Grid-stride over cells (at
+// and the pending vector P_j) with P_j and with w, and |w|^2, as block partials (rows
+// 0..j, j+1..2j+1 and 2j+2 of partial) that every block of the next k_gmres_prim_z sums.  Grid-stride over cells (at
 // most RED_BLOCKS blocks).
 template <class T, int NV>
 __global__ void __launch_bounds__(RED_THREADS) k_gmres_gather_dot(MeshView<T> m, const T* __restrict__ FA,
@@ -555,7 +573,7 @@ __global__ void __launch_bounds__(RED_THREADS) k_gmres_gather_dot(MeshView<T> m,
     const int j = d.gi[4];  // this iteration (set by k_gmres_prim_z)
     if (done) return;       // the solve has ended
     const long nc = m.nc;
-    __shared__ A wsw[KRY_MAXM + 1][KRY_WARPS], wsp[KRY_MAXM + 1][KRY_WARPS];
+    __shared__ A wsw[KRY_MAXM + 2][KRY_WARPS], wsp[KRY_MAXM + 1][KRY_WARPS];
     const T* Pj = V + (long)j * L;
     // w = the gathered J v of cell i (reference face order).  Everything but the face
     // fluxes comes from two or more kernels back (pdl.cuh), so a thread loads it for its
@@ -578,6 +596,7 @@ __global__ void __launch_bounds__(RED_THREADS) k_gmres_gather_dot(MeshView<T> m,
             p.s5 = src[nc + i];
         }
     };
+    A nw = A(0);  // |w|^2
     auto gather = [&](long i, const Pre& p, T (&acc)[NV]) {
 #pragma unroll
         for (int c = 0; c < NV; ++c) acc[c] = T(0);
@@ -602,6 +621,7 @@ __global__ void __launch_bounds__(RED_THREADS) k_gmres_gather_dot(MeshView<T> m,
         for (int c = 0; c < NV; ++c) {
             acc[c] = acc[c] + p.zc[c] * p.tc;
             w[c * nc + i] = acc[c];
+            nw += (A)acc[c] * (A)acc[c];
         }
     };
     const long ifirst = (long)blockIdx.x * blockDim.x + threadIdx.x;
@@ -698,8 +718,10 @@ __global__ void __launch_bounds__(RED_THREADS) k_gmres_gather_dot(MeshView<T> m,
     }
     // block partials only: every block of the next kernel sums them itself (partials_sum),
     // which costs less than a last-block reduction here and its fence and ticket
+    nw = warp_sum_t(nw);
+    if ((threadIdx.x & 31) == 0) wsw[j + 1][threadIdx.x >> 5] = nw;
     block_partials(reinterpret_cast<A*>(d.partial), j, wsp);
-    block_partials(reinterpret_cast<A*>(d.partial) + (long)(j + 1) * RED_BLOCKS, j, wsw);
+    block_partials(reinterpret_cast<A*>(d.partial) + (long)(j + 1) * RED_BLOCKS, j + 1, wsw);
     if (blockIdx.x == 0 && threadIdx.x == 0) d.gi[5] = j + 1;  // products reduced
 }
 

@@ -1616,8 +1616,8 @@ cfdg_status cfdg_solver_create(const cfdg_mesh* m, const cfdg_config* cfg, cfdg_
     if (c.gmres_m <= KRY_MAXM) {  // device-GMRES state, so the driver can be switched at run time
         int m = c.gmres_m;
         TRYS(dalloc(&s->gdi, 8));
-        size_t nd = 3 + (size_t)(m + 1) + 2 * (size_t)m + 2 * (size_t)(m + 1) * m + (size_t)(m + 2) + m +
-                    2 * (size_t)(m + 1) + 2 + (size_t)(m + 1) + 2 * (size_t)(KRY_MAXM + 1) * RED_BLOCKS + 4;
+        size_t nd = 3 + (size_t)(m + 1) + 2 * (size_t)m + 2 * (size_t)(m + 1) * m + 2 * (size_t)(m + 2) + m +
+                    2 * (size_t)(m + 1) + 2 + (size_t)(m + 1) + (2 * (size_t)KRY_MAXM + 3) * RED_BLOCKS + 4;
         TRYS(dalloc(&s->gdd, nd));
         double* q = s->gdd;
         GmresDev& d = s->gd;
@@ -1629,12 +1629,13 @@ cfdg_status cfdg_solver_create(const cfdg_mesh* m, const cfdg_config* cfg, cfdg_
         d.H = q; q += (size_t)(m + 1) * m;
         d.Hu = q; q += (size_t)(m + 1) * m;
         d.sig = q; q += m + 2;
+        d.ilam = q; q += m + 2;
         d.y = q; q += m;
         d.h1 = q; q += m + 1;
         d.h2 = q; q += m + 1;
         d.hsq = q; q += 2;
         d.sc = q; q += m + 1;
-        d.partial = q; q += 2 * (size_t)(KRY_MAXM + 1) * RED_BLOCKS;
+        d.partial = q; q += (2 * (size_t)KRY_MAXM + 3) * RED_BLOCKS;
         d.nb1 = (int)kry_grid(nc);
         d.counter = reinterpret_cast<unsigned*>(q);
         d.in_graph = 1;
