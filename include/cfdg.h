@@ -92,8 +92,8 @@ typedef struct cfdg_config {
     /* graph driver with exact J v: 1 runs each Arnoldi iteration as one persistent kernel
      * with grid barriers between its phases (two-reduction CGS2), 0 (default) as four
      * kernels; measured on the 28,800-cell plate: FP32 basis 63-72 us per iteration
-     * persistent vs 54-64 us with the six-kernel body of the time (a five-kernel body
-     * since: about 35 us), FP64 exact 186-200 vs 186-211 us */
+     * persistent vs 54-64 us with the six-kernel body of the time (the four-kernel body
+     * since: about 30 us), FP64 exact 186-200 vs 186-211 us */
     int persistent;
     /* graph driver with exact J v: 1 (default) launches the Arnoldi body's kernels after
      * the first with programmatic dependent launch, so each starts while its predecessor's

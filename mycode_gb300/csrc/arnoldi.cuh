@@ -17,9 +17,10 @@
 // launched with at most the blocks that fit on the GPU at once (occupancy query).
 //
 // Measured on the 28,800-cell laminar plate it did not beat the multi-kernel body of the
-// time for the FP32 basis (63-72 vs 54-64 us per iteration; the five-kernel body since
-// runs an iteration in about 35 us) and matched it in FP64 (186-200 vs 186-211 us), so the
-// multi-kernel body is the default; the switch is cfdg_config.persistent.
+// time for the FP32 basis (63-72 vs 54-64 us per iteration; the four-kernel delayed-CGS2
+// body since runs an iteration in about 30 us) and matched it in FP64 (186-200 vs 186-211
+// us), so the multi-kernel body is the default; the switch is cfdg_config.persistent.
+// This kernel keeps the two-reduction CGS2 (its own phases; the same GMRES state).
 #pragma once
 #include "krylov.cuh"
 
