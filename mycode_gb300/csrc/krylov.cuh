@@ -281,10 +281,13 @@ __global__ void k_gmres_z(long nc, const T* V, long L, const T* __restrict__ Din
 // evaluated as a parallel prefix over 32 rotations at a time (compositions of affine
 // maps, Kogge-Stone), and out[i] = c_i carry_i + s_i col[i+1] by every lane at once.  The
 // new rotation takes c = a / sqrt(a^2 + b^2) as a * rsqrt(a^2 + b^2).  col[0..j] holds
-// h1 + h2, hv = |V_{j+1}|, hsq = hv^2.  Ends the solve (done flag, loop condition) on
+// the column's entries above the subdiagonal hv, hsq = hv^2.  Ends the solve (done flag, loop condition) on
 // convergence or when j + 1 reaches m.
+// c0, s0: this lane's rotation of the first 32 (cs[lane], sn[lane]; 1, 0 past j), gj = g[j]
+// and tolb = tol * beta, loaded by the caller ahead of time.
 __device__ __forceinline__ void givens_column(const GmresDev& d, int j, int m, double* col, double hv, double hsq,
-                                              cudaGraphConditionalHandle hnd) {
+                                              cudaGraphConditionalHandle hnd, double c0, double s0, double gj,
+                                              double tolb) {
     __shared__ double hout[KRY_MAXM + 2];
     const unsigned full = 0xffffffffu;
     const int lane = threadIdx.x & 31;
@@ -292,7 +295,8 @@ __device__ __forceinline__ void givens_column(const GmresDev& d, int j, int m, d
     for (int base = 0; base < j; base += 32) {
         const int i = base + lane;
         const bool act = i < j;
-        const double ci = act ? d.cs[i] : 1.0, si = act ? d.sn[i] : 0.0, nx = act ? col[i + 1] : 0.0;
+        const double ci = base == 0 ? c0 : (act ? d.cs[i] : 1.0), si = base == 0 ? s0 : (act ? d.sn[i] : 0.0);
+        const double nx = act ? col[i + 1] : 0.0;
         const double snx = si * nx;
         double fa = act ? -si : 1.0, fb = act ? ci * nx : 0.0;  // f_i(x) = fa x + fb
 #pragma unroll
@@ -325,10 +329,9 @@ __device__ __forceinline__ void givens_column(const GmresDev& d, int j, int m, d
         hout[j + 1] = 0.0;
         d.cs[j] = c;
         d.sn[j] = sn;
-        const double gj = d.g[j];
         d.g[j + 1] = -sn * gj;
         d.g[j] = c * gj;
-        const bool conv = fabs(-sn * gj) < d.beta[1] * d.beta[0];
+        const bool conv = fabs(-sn * gj) < tolb;
         if (conv || j + 1 >= m) {
             d.gi[1] = j;
             d.gi[2] = 1;
@@ -370,10 +373,23 @@ __global__ void __launch_bounds__(256) k_gmres_prim_z(int nc, Flow<T> F, const T
     if (ga.z) return;  // the solve has ended
     pdl_trigger();     // the gradient kernel may launch now
     const int jn = gb.y, m = ga.w, j = jn - 1;
+    const bool givens_block = blockIdx.x == gridDim.x - 1;
+    // the Givens warp's inputs from earlier kernels (column j - 2's first-pass entries, the
+    // rotations, g and tol beta) load with the partials below, not after them
+    double pre_h1 = 0.0, pre_c = 1.0, pre_s = 0.0, pre_g = 0.0, pre_tolb = 0.0;
+    if (givens_block && threadIdx.x < 32 && jn >= 2) {
+        const int c = jn - 2, lane = threadIdx.x;
+        if (lane <= c) pre_h1 = d.h1[lane];
+        if (lane < c) {
+            pre_c = d.cs[lane];
+            pre_s = d.sn[lane];
+        }
+        pre_g = d.g[c];
+        pre_tolb = d.beta[1] * d.beta[0];
+    }
     __shared__ A cu[KRY_MAXM + 1], cp[KRY_MAXM + 1];  // coefficients of V_k in V_j and in P_jn
     __shared__ double dp[KRY_MAXM + 2], dw[KRY_MAXM + 2], sv[KRY_MAXM + 1];
     __shared__ double r_s, hv_s, hsq_s, scj_s, sgn_s, ilmn_s, ilam_s;
-    const bool givens_block = blockIdx.x == gridDim.x - 1;
     if (jn > 0) {
         // the scales (lane k of warp 0: sc_k), sig_j and 1/lam_j load with the partials
         const double sigj = d.sig[j], ilamj = d.ilam[j];
@@ -392,7 +408,42 @@ __global__ void __launch_bounds__(256) k_gmres_prim_z(int nc, Flow<T> F, const T
             }
         }
         __syncthreads();
-        if (threadIdx.x < 32) {
+        constexpr bool f32 = sizeof(A) == 4;
+        if (threadIdx.x < 32 && f32 && !givens_block) {
+            // cell blocks with an FP32 basis: the coefficients only feed FP32 arithmetic, so
+            // warp 0 forms them in FP32 (a dependent FP64 operation costs as much as ~16 FP32
+            // ones here); the Givens block forms the FP64 values of the Hessenberg column
+            if constexpr (f32) {
+                const float sigf = (float)sigj;
+                float ss = 0.f, sg = 0.f;
+                for (int k = threadIdx.x; k < j; k += 32) {
+                    const float sck = (float)(k < 32 ? sclane : d.sc[k]);
+                    const float pk = (float)dp[k], wk = (float)dw[k];
+                    const float sk = sck * sigf * pk, gk = sck * wk;
+                    cu[k] = sck * sck * pk;
+                    cp[k] = gk * sck;
+                    ss += sk * sk;
+                    sg += sk * gk;
+                }
+#pragma unroll
+                for (int o = 16; o > 0; o >>= 1) {
+                    ss += __shfl_xor_sync(0xffffffffu, ss, o);
+                    sg += __shfl_xor_sync(0xffffffffu, sg, o);
+                }
+                if (threadIdx.x == 0) {
+                    float r = 1.f;
+                    if (j > 0) {
+                        const float hsq = fmaxf(sigf * sigf * (float)dp[j] - ss, 0.f);
+                        const float rq = hsq > 0.f ? rsqrtf(hsq) : 0.f;
+                        r = hsq * rq * (float)ilamj > 1e-12f ? rq : 1.f;
+                    }
+                    const float gj = (sigf * (float)dw[j] - sg) * r;
+                    cp[j] = gj * (sigf * r);
+                    const float wsq = (float)dw[j + 1];
+                    sgn_s = wsq > 0.f ? (double)rsqrtf(wsq) : 1.0;
+                }
+            }
+        } else if (threadIdx.x < 32) {
             // warp 0: s_k, g_k and the coefficients, lane k; |s|^2 and s.g in the basis
             // precision (corrections of ~1e-7 relative with FP32)
             A ss = A(0), sg = A(0);
@@ -429,7 +480,8 @@ __global__ void __launch_bounds__(256) k_gmres_prim_z(int nc, Flow<T> F, const T
                 // sig_jn = 1/|w|, 1/lam_jn = r/sig_jn = r |w| (multiplies: an FP64 divide costs
                 // about seven dependent FMAs)
                 const double wsq = dw[j + 1];
-                const double sgn = wsq > 0.0 ? rsqrt(wsq) : 1.0;
+                // (with an FP32 basis the cell blocks' FP32 value, so both use the same scale)
+                const double sgn = wsq > 0.0 ? (f32 ? (double)rsqrtf((float)wsq) : rsqrt(wsq)) : 1.0;
                 sgn_s = sgn;
                 ilmn_s = r * (wsq > 0.0 ? wsq * sgn : 1.0);
                 ilam_s = ilamj;
@@ -447,7 +499,7 @@ __global__ void __launch_bounds__(256) k_gmres_prim_z(int nc, Flow<T> F, const T
                 double* Hc = d.Hu + (long)c * (m + 1);
                 const double il = ilam_s;
                 for (int i = threadIdx.x; i <= c; i += 32) {
-                    col[i] = d.h1[i] + sv[i] * il;
+                    col[i] = (i < 32 ? pre_h1 : d.h1[i]) + sv[i] * il;
                     Hc[i] = col[i];
                 }
                 if (threadIdx.x == 0) {
@@ -459,7 +511,7 @@ __global__ void __launch_bounds__(256) k_gmres_prim_z(int nc, Flow<T> F, const T
             if (threadIdx.x < 32) {
                 if (j > 0) {
                     const double hvc = col[c + 1];
-                    givens_column(d, c, m, col, hvc, hvc * hvc, hnd);
+                    givens_column(d, c, m, col, hvc, hvc * hvc, hnd, pre_c, pre_s, pre_g, pre_tolb);
                 }
                 if (threadIdx.x == 0) {
                     d.sc[j] = scj_s;
