@@ -103,7 +103,7 @@ template <>
 void launch_gmres_prim_z<float>(int nv, long nc, const Flow<float>& F, const float* U, float* V, long L, const float* Dinv,
                              float* z, Field<float> W, const float* w, const GmresDev& d, cudaGraphConditionalHandle h,
                              cudaStream_t s) {
-    // blocks of RED_THREADS (every block sums the update kernel's partials: wide blocks keep
+    // blocks of RED_THREADS (every block sums the gather kernel's partials: wide blocks keep
     // that short, and at most RED_BLOCKS of them, grid-stride over the cells) and one block
     // more for the Givens step
     NV_SWITCH(nv, (k_gmres_prim_z<float, NVC><<<red_grid(nc) + 1, RED_THREADS, 0, s>>>((int)nc, F, U, V, L, Dinv, z, W, w, d,

@@ -144,7 +144,7 @@ template <>
 void launch_gmres_prim_z<double>(int nv, long nc, const Flow<double>& F, const double* U, double* V, long L, const double* Dinv,
                              double* z, Field<double> W, const double* w, const GmresDev& d, cudaGraphConditionalHandle h,
                              cudaStream_t s) {
-    // blocks of RED_THREADS (every block sums the update kernel's partials: wide blocks keep
+    // blocks of RED_THREADS (every block sums the gather kernel's partials: wide blocks keep
     // that short, and at most RED_BLOCKS of them, grid-stride over the cells) and one block
     // more for the Givens step
     NV_SWITCH(nv, (k_gmres_prim_z<double, NVC><<<red_grid(nc) + 1, RED_THREADS, 0, s>>>((int)nc, F, U, V, L, Dinv, z, W, w, d,
