@@ -146,14 +146,18 @@ void launch_gmres_prim_z<double>(int nv, long nc, const Flow<double>& F, const d
                              cudaStream_t s) {
     // blocks of RED_THREADS (every block sums the gather kernel's partials: wide blocks keep
     // that short, and at most RED_BLOCKS of them, grid-stride over the cells) and one block
-    // more for the Givens step
-    NV_SWITCH(nv, (k_gmres_prim_z<double, NVC><<<red_grid(nc) + 1, RED_THREADS, 0, s>>>((int)nc, F, U, V, L, Dinv, z, W, w, d,
+    // more for the Givens step; the partials it sums are the gather kernel's (gather_grid
+    // blocks with this basis precision)
+    GmresDev dd = d;
+    dd.nb1 = (int)gather_grid(nc, 8);
+    NV_SWITCH(nv, (k_gmres_prim_z<double, NVC><<<red_grid(nc) + 1, RED_THREADS, 0, s>>>((int)nc, F, U, V, L, Dinv, z, W, w, dd,
                                                                                   h)));
 }
 template <>
 void launch_gmres_gather_dot<double>(int nv, const MeshView<double>& m, const double* FA, double* w, const double* z, const double* dt,
                                  const double* src, const double* V, long L, const GmresDev& d, cudaStream_t s, bool pdl) {
-    NV_SWITCH(nv, launch_k(pdl, k_gmres_gather_dot<double, NVC>, dim3(kry_grid(m.nc)), dim3(RED_THREADS), s, m, FA, (long)m.nf,
+    NV_SWITCH(nv, launch_k(pdl, k_gmres_gather_dot<double, NVC>, dim3(gather_grid(m.nc, 8)), dim3(RED_THREADS), s, m, FA,
+                           (long)m.nf,
                            w, z, dt, src, V, L, d));
 }
 template <>

@@ -66,7 +66,7 @@ struct GmresDev {
     double* hsq;      // [2] squared norms ([1]: after the second pass)
     double* sc;       // [m+1] scale of each stored basis vector
     double* partial;  // [(2 KRY_MAXM + 3) * RED_BLOCKS] block partials (rows of RED_BLOCKS)
-    int nb1;          // blocks of the gather kernel that writes them (exact J v body)
+    int nb1;          // blocks of the gather kernel that writes them (exact J v body; set at launch)
     unsigned* counter;
     int in_graph;     // 1: the kernels run inside the WHILE graph and set its condition
 };
@@ -612,10 +612,13 @@ __global__ void __launch_bounds__(RED_THREADS) k_gmres_multidot(long L, const T*
 // order, minus the SST source derivatives, plus z vol / dt) into w, fused with the one
 // reduction of the iteration: the dots of slots 0..j of V (the basis vectors V_0..V_{j-1}
 // and the pending vector P_j) with P_j and with w, and |w|^2, as block partials (rows
-// 0..j, j+1..2j+1 and 2j+2 of partial) that every block of the next k_gmres_prim_z sums.  Grid-stride over cells (at
-// most RED_BLOCKS blocks).
+// 0..j, j+1..2j+1 and 2j+2 of partial) that every block of the next k_gmres_prim_z sums.
+// Grid-stride over cells (gather_grid blocks).  With an FP32 basis the kernel fits 128
+// registers without spills, so two blocks share an SM (a streaming pass over a
+// million-cell basis needs the loads of more than one block in flight per SM).
 template <class T, int NV>
-__global__ void __launch_bounds__(RED_THREADS) k_gmres_gather_dot(MeshView<T> m, const T* __restrict__ FA,
+__global__ void __launch_bounds__(RED_THREADS, sizeof(T) == 4 ? 2 : 1)
+    k_gmres_gather_dot(MeshView<T> m, const T* __restrict__ FA,
                                                                   long fa_stride, T* __restrict__ w,
                                                                   const T* __restrict__ z, const T* __restrict__ dt,
                                                                   const T* __restrict__ src, const T* __restrict__ V,

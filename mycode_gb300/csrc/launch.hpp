@@ -132,6 +132,13 @@ inline unsigned kry_grid(long n) {
     long b = (n + RED_THREADS - 1) / RED_THREADS;
     return (unsigned)(b < 152 ? (b < 1 ? 1 : b) : 152);
 }
+// blocks of the exact J v gather kernel (k_gmres_gather_dot): two per SM with an FP32
+// basis (elem 4), one with FP64; its block partials are rows of RED_BLOCKS
+inline unsigned gather_grid(long nc, int elem) {
+    const long cap = elem == 4 ? 2 * 152 : 152;
+    long b = (nc + RED_THREADS - 1) / RED_THREADS;
+    return (unsigned)(b < cap ? (b < 1 ? 1 : b) : cap);
+}
 
 // instantiate a launch for nv = 4 or 6 (NVC is the compile-time count in __VA_ARGS__)
 #define NV_SWITCH(nv, ...)                                      \

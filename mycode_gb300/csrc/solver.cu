@@ -1636,7 +1636,7 @@ cfdg_status cfdg_solver_create(const cfdg_mesh* m, const cfdg_config* cfg, cfdg_
         d.hsq = q; q += 2;
         d.sc = q; q += m + 1;
         d.partial = q; q += (2 * (size_t)KRY_MAXM + 3) * RED_BLOCKS;
-        d.nb1 = (int)kry_grid(nc);
+        d.nb1 = 0;  // set by the first kernel's launcher for its basis precision
         d.counter = reinterpret_cast<unsigned*>(q);
         d.in_graph = 1;
         if (c.precision == CFDG_MIXED) TRYS(dalloc(&s->w32, (size_t)L));

@@ -2,6 +2,7 @@
 
     python -m mycode_gb300.profile_case --path residual64 --cells 1000000 --reps 3
     python -m mycode_gb300.profile_case --path krylov_stream --workload laminar_plate --reps 8
+    python -m mycode_gb300.profile_case --path krylov_stream --cells 4000000 --gmres-m 20 --gmres-tol 0
 
 Workloads: the bump channel (3 x 1, Gaussian bump) triangulated at ``--cells`` with
 HLLC, second-order limited reconstruction and the viscous flux, from a perturbed
@@ -52,12 +53,19 @@ def main(argv=None):
     ap.add_argument("--flux", default="HLLC")
     ap.add_argument("--spatial", default="SECOND_ORDER_LIMITED")
     ap.add_argument("--inviscid", action="store_true")
+    ap.add_argument("--gmres-m", type=int, default=None, help="Krylov dimension (krylov_stream)")
+    ap.add_argument("--gmres-tol", type=float, default=None, help="GMRES tolerance; 0 runs m iterations")
     a = ap.parse_args(argv)
+    gm = {}
+    if a.gmres_m is not None:
+        gm["gmres_m"] = a.gmres_m
+    if a.gmres_tol is not None:
+        gm["gmres_tol"] = a.gmres_tol
     from mycode_gb300 import api, meshgen
     if a.workload == "laminar_plate":
         m = api.Mesh.from_spec(meshgen.laminar_plate(240, 120, ratio=1.08))
         s = api.Solver(m, bcset="plate", init="freestream", viscous=1, flux="ROE", spatial="SECOND_ORDER_CENTRAL",
-                       precision="mixed", jv="exact", krylov=2)
+                       precision="mixed", jv="exact", krylov=2, **gm)
         s.setFreestreamStatic(0.2, 101325.0, 300.0)
         s.setKinematicViscosity(1e5, 1.0)
         s.initialize()
@@ -65,7 +73,7 @@ def main(argv=None):
     else:
         api, spec, m = build(a.cells)
         cfg = dict(bcset="bump", init="bump", viscous=0 if a.inviscid else 1, flux=a.flux, spatial=a.spatial,
-                   precision="mixed", jv="exact", krylov=2)
+                   precision="mixed", jv="exact", krylov=2, **gm)
         s = api.Solver(m, **cfg)
         s.setFlowConditions(0.5, 101325.0, 300.0)
         s.setKinematicViscosity(3e6, 1.0)
@@ -88,13 +96,23 @@ def main(argv=None):
     s.synchronize()
     s.kernel_stats(reset=True)
     t0 = time.perf_counter()
+    iters = []
     for _ in range(a.reps):
-        run[0]()
+        r = run[0]()
+        if a.path == "krylov_stream":
+            iters.append(r[0].gmres_iters)
     s.synchronize()
     st = s.kernel_stats(reset=True)
     out = {k: round(v[0] / max(v[1], 1), 5) for k, v in st.items() if k.startswith(run[1]) and v[1]}
-    print(json.dumps({"path": a.path, "workload": a.workload, "cells": m.n_cells, "faces": m.n_faces,
-                      "ms_per_launch": out, "wall_s": time.perf_counter() - t0}))
+    line = {"path": a.path, "workload": a.workload, "cells": m.n_cells, "faces": m.n_faces,
+            "ms_per_launch": out, "wall_s": time.perf_counter() - t0}
+    if iters:
+        # Arnoldi iterations per solve and the mean basis index j over them (iteration j
+        # reads j + 1 stored vectors)
+        line["gmres_iters"] = iters
+        line["mean_j"] = sum(i * (i - 1) / 2 for i in iters) / max(1, sum(iters))
+        line["launches"] = {k: v[1] for k, v in st.items() if k.startswith(run[1]) and v[1]}
+    print(json.dumps(line))
 
 
 if __name__ == "__main__":
