@@ -1,27 +1,34 @@
 #!/usr/bin/env python3
 """Benchmark of the residual-and-Newton path: cell-residuals per second.
 
-Workload (one GPU): the laminar flat plate — Navier-Stokes, M = 0.2, Re_L = 1e5,
-Pr = 0.72, adiabatic no-slip plate from x = 0 behind a 0.2 symmetry lead-in, 240 x 120
-quads (28,800 cells, 57,960 faces) with wall-normal stretching 1.08; Roe flux plus the
-viscous flux, second-order central reconstruction; pseudo-transient JFNK.  Synthetic
-mesh and state (seeded recipe, no dataset).
+Workload (one GPU): the Gaussian-bump channel at its largest size — a 3 x 1 channel with a
+bump of height 0.05 and width 0.2, 2448 x 816 quads split into 3,995,136 triangles
+(5,995,968 faces) with 10 % seeded jitter; M = 0.5, Re = 3e6, the SST k-omega model (six
+conserved variables), HLLC, second-order reconstruction with the Barth-Jespersen limiter,
+the viscous flux; the initial state with a seeded smooth perturbation.  Synthetic mesh and
+state (seeded recipe, no dataset).
 
-A step is one pseudo-transient Newton step of the solve: local time step, residual,
-one right-preconditioned GMRES solve (each Krylov iteration one J v product) and the
-clamped update.  The unit of work is one cell-residual: one cell of one residual or
-J v evaluation, so a step processes n_cells * (1 + GMRES iterations) cell-residuals.
+A step is one evaluation of the FP64 residual R(U) (computeResiduals with the limiter
+recomputed) over the whole mesh, in the reference's floating-point operation order.  The
+unit of work is one cell-residual, so a step is n_cells cell-residuals.
 
-  value  mixed precision (FP32 Krylov basis, FP32 exact J v and preconditioner; FP64
-         residual, update, Hessenberg/Givens and norms), state resident in HBM; device
-         time from CUDA events on the solver's stream; L2 flushed between steps
-  e2e    the same step through the C ABI with the state uploaded from pinned host
-         memory before and read back after every step (wall clock)
-  fp64   the plain FP64 path (FD J v as the reference) on the same workload
+  value  state resident in HBM; device time from CUDA events on the solver's stream;
+         inputs larger than L2 (U alone is 192 MB) and L2 flushed between steps
+  e2e    the same evaluations through the C ABI (cfdg_residual) with the state in pinned
+         host memory, in the reference's AoS layout and numbering: the host-to-device
+         copy, the renumbering, the residual, the renumbering back and the device-to-host
+         copy of R inside the timed region (wall clock)
 
-``--impl reference`` times the reference's algorithm on the host cores instead: the
-reference built from its sources (oracle/_ref) when present, else the plain-C
-restatement (oracle/), one independent copy per host core.
+Beside it, at the same size: the FP32 residual, the exact J v in FP32 and FP64 and the
+FP64 adjoint (VJP); the mixed-precision Newton step on the laminar flat plate; the time
+to a density residual of 1e-10 (mixed vs FP64) with its wall-Cp error against the FP64
+CPU oracle; the other full-size configurations.
+
+``--impl reference`` times the CPU path instead: the plain-C restatement of the
+reference's residual with the SST terms (oracle/; the reference itself has no SST), one
+independent copy per host core on the same mesh, state and scheme.
+``--sweep`` runs the bandwidth sweep over 64k-4M cells; ``--profile-case`` one kernel
+path on a chosen case for ncu captures.
 """
 from __future__ import annotations
 
@@ -42,27 +49,49 @@ sys.path.insert(0, ROOT)
 METRIC = "cell-residuals/s; JFNK time-to-1e-10 mixed vs FP64 GPU; adjoint/primal cost"
 UNIT = "cell-residuals/s"
 L2_FLUSH_BYTES = 256 << 20
+HEADLINE_CELLS = 4_000_000
 
 
-def workload_spec():
+def headline_spec(target: int = HEADLINE_CELLS):
     from mycode_gb300 import meshgen
-    return meshgen.laminar_plate(240, 120, ratio=1.08)
+    return meshgen.bump(target, jitter=0.10, seed=0)
 
 
-WORKLOAD = {
-    "workload": "laminar flat plate 240x120 quads (28,800 cells, 57,960 faces), stretching 1.08, "
-                "Navier-Stokes M=0.2 Re_L=1e5 Pr=0.72, Roe + viscous flux, 2nd-order central, "
-                "pseudo-transient JFNK-GMRES(40), one Newton step per step",
-    "n_cells": 28800,
-    "n_faces": 57960,
-}
+def headline_workload(spec) -> dict:
+    return {
+        "workload": f"Gaussian-bump channel 3x1 (bump height 0.05, width 0.2), {spec.n_cells:,} triangles "
+                    f"({spec.expected_faces():,} faces), 10% seeded jitter; M=0.5 Re=3e6, SST k-omega (6 conserved "
+                    "variables), HLLC, 2nd-order Barth-Jespersen-limited reconstruction, viscous flux; one FP64 "
+                    "residual evaluation R(U) per step (limiter recomputed), seeded smooth perturbation of the "
+                    "initial state",
+        "n_cells": spec.n_cells,
+        "n_faces": spec.expected_faces(),
+        "precision": "fp64, the reference's operation order (bit-exact residual path)",
+        "l2": f"inputs larger than L2 (U alone {spec.n_cells * 48 / 1e6:.0f} MB) and L2 flushed (256 MiB write) "
+              "between steps",
+    }
 
 
-def setup_flow(s):
-    s.setFreestreamStatic(0.2, 101325.0, 300.0)
-    s.setKinematicViscosity(1e5, 1.0)
+def perturb_state(U0, xyc):
+    """The benchmark state: the initial state times a seeded smooth perturbation (5 %) of
+    rho, rho u, rho v, rho E and (half as strong) of rho k, rho w."""
+    from mycode_gb300 import meshgen
+    pert = meshgen.smooth_perturbation(xyc, 7, 0.05)
+    U = U0.copy()
+    for c in range(4):
+        U[:, c] *= 1.0 + pert[:, c]
+    U[:, 4] *= 1.0 + 0.5 * pert[:, 0]
+    U[:, 5] *= 1.0 + 0.5 * pert[:, 1]
+    return U
+
+
+def bump_solver(api, mesh, device=0, precision="mixed", sst=True):
+    s = api.Solver(mesh, bcset="bump", init="bump", viscous=1, turbulence="sst" if sst else "none",
+                   precision=precision, jv="exact", flux="HLLC", spatial="SECOND_ORDER_LIMITED", device=device)
+    s.setFlowConditions(0.5, 101325.0, 300.0)
+    s.setKinematicViscosity(3e6, 1.0)
     s.initialize()
-    s.setNumericalMethod("ROE", "SECOND_ORDER_CENTRAL")
+    return s
 
 
 # ---------------------------------------------------------------- roofline helpers
@@ -148,42 +177,42 @@ def measured_peak():
         return 6800.0, "fallback"
 
 
-def profile_fp64_pipe():
-    """FP64 pipe fraction and FP64 flops per unit of the FP64 residual's kernels from the
-    committed ncu summary (profiles/fp64_pipe.txt)."""
-    path = os.path.join(ROOT, "profiles", "fp64_pipe.txt")
+def _profile_table(name: str) -> dict:
+    """Rows of a committed ncu summary under profiles/: `class value...` per line, `#`
+    comments; the values as floats."""
+    path = os.path.join(ROOT, "profiles", name)
     out = {}
     if os.path.exists(path):
         with open(path) as fh:
             for line in fh:
                 parts = line.split()
-                if len(parts) == 4 and not parts[0].startswith("#"):
+                if len(parts) >= 2 and not parts[0].startswith("#"):
                     try:
-                        out[parts[0]] = {"fp64_pipe_frac": float(parts[1]), "fp64_flops_per_unit": float(parts[2]),
-                                         "unit": parts[3]}
+                        out[parts[0]] = [float(x) for x in parts[1:]]
                     except ValueError:
                         pass
     return out
 
 
+def profile_fp64_pipe() -> dict:
+    """FP64 pipe of the FP64 residual's kernels on the headline workload, from ncu
+    (profiles/fp64_pipe.txt): per class the pipe's busy fraction, its warp instructions
+    and DRAM bytes per unit (per face for the flux, per cell otherwise)."""
+    out = {}
+    for k, v in _profile_table("fp64_pipe.txt").items():
+        if len(v) >= 3:
+            out[k] = {"pipe_frac_ncu": v[0], "fp64_warp_inst_per_unit": v[1], "dram_bytes_per_unit": v[2]}
+    return out
+
+
 def profile_traffic(kernel_class: str, jbar: float = 0.0):
-    """DRAM bytes per launch of a kernel class from the committed ncu summary
-    (profiles/traffic.txt: bytes at Arnoldi iteration 0 and per further basis vector),
-    evaluated at the mean iteration jbar; None when the class is not listed."""
-    path = os.path.join(ROOT, "profiles", "traffic.txt")
-    if not os.path.exists(path):
+    """DRAM bytes per launch of a kernel class from ncu (profiles/traffic.txt: bytes at
+    Arnoldi iteration 0 and per further basis vector), evaluated at the mean iteration
+    jbar; None when the class is not listed."""
+    v = _profile_table("traffic.txt").get(kernel_class)
+    if not v:
         return None
-    with open(path) as fh:
-        for line in fh:
-            parts = line.split()
-            if len(parts) >= 2 and not parts[0].startswith("#") and parts[0] == kernel_class:
-                try:
-                    base = float(parts[1])
-                    per = float(parts[2]) if len(parts) > 2 else 0.0
-                except ValueError:
-                    return None
-                return round(base + per * jbar)
-    return None
+    return round(v[0] + (v[1] if len(v) > 1 else 0.0) * jbar)
 
 
 # ---------------------------------------------------------------- clocks
@@ -295,7 +324,209 @@ def all_sum(world, x: float) -> float:
 
 # ---------------------------------------------------------------- our arm
 
-def run_steps(s, steps, flush=True):
+def timed_kernels(s, fn, prefix, reps, warm=1):
+    """Per-class CUDA-event kernel times of `reps` calls of fn (L2 flushed before each):
+    {class: (total ms, launches)} for the classes starting with prefix."""
+    for _ in range(warm):
+        fn()
+    s.synchronize()
+    s.kernel_stats(reset=True)
+    for _ in range(reps):
+        s.flush_l2(L2_FLUSH_BYTES)
+        fn()
+    s.synchronize()
+    st = s.kernel_stats(reset=True)
+    return {k: v for k, v in st.items() if k.startswith(prefix) and v[1]}
+
+
+def fp64_roofline_row(cls, avg_ms, nc, nf, peak_gbs, pipe_peak_warp, pipe_prof):
+    """One FP64 residual kernel class: its time, HBM fraction of algorithmic bytes and FP64
+    pipe fraction (the pipe's warp instructions per unit from ncu over the live time,
+    against the live FP64 pipe rate).  Bound: the FP64 pipe."""
+    kind = cls.split(".")[1]
+    b = algorithmic_bytes(kind, nc, nf, 6, 8, "SECOND_ORDER_LIMITED", True, False)
+    units = nf if kind == "flux" else nc
+    row = {"avg_us": round(avg_ms * 1e3, 2), "algorithmic_bytes": int(b),
+           "hbm_gbs": round(b / (avg_ms * 1e-3) / 1e9, 1), "hbm_frac": round(b / (avg_ms * 1e-3) / 1e9 / peak_gbs, 4),
+           # the gather only adds face fluxes: memory-bound, the other classes FP64-pipe-bound
+           "bound": "hbm" if kind == "gather" else "fp64_pipe"}
+    p = pipe_prof.get(cls)
+    if p:
+        inst = p["fp64_warp_inst_per_unit"] * units
+        ach = inst / (avg_ms * 1e-3)
+        row.update(fp64_warp_inst_per_launch=int(inst), fp64_pipe_ginst_s=round(ach / 1e9, 3),
+                   fp64_pipe_frac=round(ach / pipe_peak_warp, 4), fp64_pipe_frac_ncu=p["pipe_frac_ncu"],
+                   traffic=int(p["dram_bytes_per_unit"] * units))
+    return row
+
+
+def kernel_paths(s, U, nc, nf, peak_gbs, reps, pipe_peak_warp=None, pipe_prof=None):
+    """The residual, exact J v and VJP kernel paths on one state: per path its time per
+    evaluation, cell-residuals/s and per-kernel fractions (FP32 and dual kernels against
+    HBM, FP64 kernels against the FP64 pipe where ncu counts exist)."""
+    import numpy as np
+    s.set_timing(True)
+    s.residual_device(True)          # the limiter the J v products freeze
+    s.set_dt(s.local_timestep(10.0))  # the time term of J v
+    v = np.random.default_rng(1).standard_normal(U.shape) * np.abs(U).mean(axis=0)
+    lam = np.random.default_rng(2).standard_normal(U.shape)
+    ops = {
+        "residual_fp64": (lambda: s.residual_device(True), "residual.", 8, False),
+        "residual_fp32": (lambda: s.residual32(), "residual.", 4, False),
+        "jv_fp64": (lambda: s.apply_jacobian(U, None, v, mode="exact"), "jv.", 8, True),
+        "jv_fp32": (lambda: s.apply_jacobian32(U, v), "jv.", 4, True),
+        "vjp_fp64": (lambda: s.vjp(lam, U), "vjp.", 8, None),
+    }
+    out = {}
+    for name, (fn, prefix, sz, dual) in ops.items():
+        st = timed_kernels(s, fn, prefix, reps)
+        kern, tot = {}, 0.0
+        for k, (ms, n) in st.items():
+            avg = ms / n
+            tot += avg
+            if dual is None:
+                kern[k.split(".")[1]] = {"avg_us": round(avg * 1e3, 2)}
+            elif sz == 8 and not dual and pipe_prof is not None:
+                kern[k.split(".")[1]] = fp64_roofline_row(k, avg, nc, nf, peak_gbs, pipe_peak_warp, pipe_prof)
+            else:
+                b = algorithmic_bytes(k.split(".")[1], nc, nf, 6, sz, "SECOND_ORDER_LIMITED", True, dual)
+                kern[k.split(".")[1]] = {"avg_us": round(avg * 1e3, 2), "algorithmic_bytes": int(b),
+                                         "hbm_gbs": round(b / (avg * 1e-3) / 1e9, 1),
+                                         "hbm_frac": round(b / (avg * 1e-3) / 1e9 / peak_gbs, 4),
+                                         "bound": "fp64_pipe" if sz == 8 else "hbm"}
+        r = {"ms": round(tot, 4), "cell_residuals_per_s": nc / (tot * 1e-3), "kernels": kern}
+        if dual is None:
+            b = vjp_algorithmic_bytes(nc, nf, 6, "SECOND_ORDER_LIMITED")
+            r.update(algorithmic_bytes=int(b), hbm_gbs=round(b / (tot * 1e-3) / 1e9, 1),
+                     hbm_frac=round(b / (tot * 1e-3) / 1e9 / peak_gbs, 4), bound="fp64_pipe")
+        out[name] = r
+    out["vjp_over_residual_fp64"] = out["vjp_fp64"]["ms"] / out["residual_fp64"]["ms"]
+    return out
+
+
+def ours(args):
+    world, rank, local = dist_setup(args.gpus)
+    from mycode_gb300 import api
+    import numpy as np
+    import torch
+    spec = headline_spec(args.cells)
+    t_mesh = time.perf_counter()
+    mesh = api.Mesh.from_spec(spec)
+    t_mesh = time.perf_counter() - t_mesh
+    nc, nf = mesh.n_cells, mesh.n_faces
+    s = bump_solver(api, mesh, local)
+    U = perturb_state(s.getSolution(), mesh.cells()[:, 1:])
+    s.set_state(U)
+    peak, peak_kind = measured_peak()
+    pipe_fma = api.fp64_pipe_rate(local)  # thread FMAs per second, measured now
+    pipe_peak_warp = pipe_fma / 32.0
+    pipe_prof = profile_fp64_pipe()
+
+    # the clock sampler (50 ms period) is live before the warm-up and runs through the
+    # timed steps and the e2e steps
+    clk = ClockSampler(local)
+    clk.start()
+    clk.wait_first()
+
+    # ---- value: FP64 residual, state resident in HBM, CUDA events around every kernel
+    s.set_timing(True)
+    for _ in range(args.warmup):
+        s.flush_l2(L2_FLUSH_BYTES)
+        s.residual_device(True)
+    s.synchronize()
+    s.kernel_stats(reset=True)
+    l0 = s.launch_count()
+    barrier(world)
+    for _ in range(args.steps):
+        s.flush_l2(L2_FLUSH_BYTES)
+        s.residual_device(True)
+    s.synchronize()
+    barrier(world)
+    launches = s.launch_count() - l0
+    st = {k: v for k, v in s.kernel_stats(reset=True).items() if k.startswith("residual.") and v[1]}
+    t_dev = sum(v[0] for v in st.values()) / 1e3
+    t_max = all_max(world, t_dev)
+    value = all_sum(world, float(args.steps * nc)) / t_max
+
+    # ---- e2e: the same evaluations through cfdg_residual with pinned host buffers
+    Uh = torch.empty((nc, 6), dtype=torch.float64, pin_memory=True).numpy()
+    Rh = torch.empty((nc, 6), dtype=torch.float64, pin_memory=True).numpy()
+    Uh[:] = U
+    s.set_timing(False)
+    for _ in range(args.warmup):
+        s.computeResiduals(Uh, True, out=Rh)
+    s.synchronize()
+    barrier(world)
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        s.computeResiduals(Uh, True, out=Rh)
+    t_e2e = all_max(world, time.perf_counter() - t0)
+    clocks = clk.stop()
+    clocks["window"] = "warm-up, timed steps and e2e steps"
+    e2e = {"value": all_sum(world, float(args.steps * nc)) / t_e2e, "unit": UNIT,
+           "h2d_bytes_per_step": int(Uh.nbytes), "d2h_bytes_per_step": int(Rh.nbytes),
+           "api": "cfdg_residual (host AoS state in pinned memory -> host AoS residual)", "ms_per_step":
+           1e3 * t_e2e / args.steps}
+
+    # ---- per-kernel roofline: every class of the FP64 residual is bound by the FP64 pipe
+    kern = {}
+    for k, (ms, n) in st.items():
+        kern[k] = fp64_roofline_row(k, ms / n, nc, nf, peak, pipe_peak_warp, pipe_prof)
+        kern[k].update(launches=n, share_of_step=round(ms / (t_dev * 1e3), 4))
+    dom = max(kern, key=lambda k: kern[k]["share_of_step"])
+    d = kern[dom]
+    roofline = {"bound": "fp64_pipe", "kernel": dom, "unit": "G FP64-pipe warp instructions/s",
+                "achieved": d.get("fp64_pipe_ginst_s"), "peak": round(pipe_peak_warp / 1e9, 3),
+                "frac": d.get("fp64_pipe_frac"),
+                "peak_source": "measured live in this run (cfdg_fp64_pipe_rate: an FP64 FMA stream over all SMs); "
+                               "instructions per launch from ncu (profiles/fp64_pipe.txt) scaled to this mesh",
+                "traffic": d.get("traffic"), "algorithmic_bytes": d["algorithmic_bytes"],
+                "hbm": {"achieved": d["hbm_gbs"], "peak": peak, "unit": "GB/s", "frac": d["hbm_frac"],
+                        "peak_source": f"{peak_kind} (MEASURED_PEAKS.json hbm_gbs)" if peak_kind == "measured"
+                        else "fallback 6.8 TB/s"},
+                "fp64_pipe_frac_ncu": d.get("fp64_pipe_frac_ncu")}
+
+    # ---- the other kernel paths at the same size (FP32 residual, exact J v, VJP)
+    paths = kernel_paths(s, U, nc, nf, peak, min(args.steps, 5), pipe_peak_warp, pipe_prof) \
+        if not args.quick else None
+    s.close()
+    del mesh
+
+    extra = {}
+    if rank == 0 and not args.quick:
+        extra["newton_laminar_plate"] = newton_plate(api, args, local)
+        extra["time_to_1e-10"] = time_to_converge(api)
+        extra["other_configs"] = other_configs(api)
+    cpu = None
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        cpu = cpu_baseline_sample(args.cells, args.cpu_seconds)
+
+    if rank == 0:
+        line = {
+            "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": 1e3 * t_max / args.steps, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+            "data": "synthetic (seeded mesh recipe and seeded smooth perturbation of the initial state)",
+            "config": dict(headline_workload(spec), parallelism="replicas" if world > 1 else "1 GPU"),
+            "gpu_launches": launches,
+            "roofline": roofline,
+            "kernels": kern,
+            "e2e": e2e,
+            "mesh_upload_s": round(t_mesh, 3),
+            "fp64_pipe_fma_per_s": pipe_fma,
+            "kernel_paths": paths,
+            "adjoint_over_primal": None if paths is None else {
+                "ratio": paths["vjp_over_residual_fp64"], "residual_ms": paths["residual_fp64"]["ms"],
+                "vjp_ms": paths["vjp_fp64"]["ms"],
+                "note": "FP64 VJP of the full residual (forward recomputation included) / FP64 residual, same mesh"},
+            **extra,
+            "clocks": clocks,
+            "cpu_baseline": cpu,
+        }
+        print(json.dumps(line))
+
+
+def run_newton_steps(s, steps, flush=True):
     """Timed Newton steps; returns (device seconds, cell-residual evaluations, per-step records)."""
     tot_ms, evals, recs = 0.0, 0, []
     for _ in range(steps):
@@ -308,211 +539,75 @@ def run_steps(s, steps, flush=True):
     return tot_ms / 1e3, evals, recs
 
 
-def make_solver(api, mesh, device, precision):
-    cfg = dict(bcset="plate", init="freestream", viscous=1, flux="ROE", spatial="SECOND_ORDER_CENTRAL",
-               device=device)
+PLATE = ("laminar flat plate 240x120 quads (28,800 cells, 57,960 faces), stretching 1.08, Navier-Stokes M=0.2 "
+         "Re_L=1e5 Pr=0.72, Roe + viscous flux, 2nd-order central, pseudo-transient JFNK-GMRES(40) from the free "
+         "stream; one Newton step per step")
+
+
+def plate_solver(api, mesh, device, precision):
+    cfg = dict(bcset="plate", init="freestream", viscous=1, flux="ROE", spatial="SECOND_ORDER_CENTRAL", device=device)
     if precision == "mixed":
         cfg.update(precision="mixed", jv="exact")
     else:
         cfg.update(precision="fp64", jv="fd")
     s = api.Solver(mesh, **cfg)
-    setup_flow(s)
+    s.setFreestreamStatic(0.2, 101325.0, 300.0)
+    s.setKinematicViscosity(1e5, 1.0)
+    s.initialize()
+    s.setNumericalMethod("ROE", "SECOND_ORDER_CENTRAL")
     return s
 
 
-def ours(args):
-    world, rank, local = dist_setup(args.gpus)
-    from mycode_gb300 import api
-    import numpy as np
-    spec = workload_spec()
-    mesh = api.Mesh.from_spec(spec)
-    nc, nf = mesh.n_cells, mesh.n_faces
-
-    # ---- primary: mixed precision, state resident in HBM
-    s = make_solver(api, mesh, local, "mixed")
-    # the timed steps carry CUDA events around each step and its GMRES graph only; the
-    # per-kernel times come from the replay below
-    s.set_timing("steps")
-    # the clock sampler (50 ms period) is live before the warm-up and runs through the
-    # timed steps, the kernel replay and the e2e steps, so that it has samples under load
-    # although the timed region itself lasts only ~30 ms
-    clk = ClockSampler(local)
-    clk.start()
-    clk.wait_first()
-    for _ in range(args.warmup):
-        s.newton_step(0.0)
-    s.kernel_stats(reset=True)
-    l0 = s.launch_count()
-    s.synchronize()
-    barrier(world)
-    t_dev, evals, recs = run_steps(s, args.steps)
-    s.synchronize()
-    barrier(world)
-    launches = s.launch_count() - l0
-    kinfo = s.krylov_info()
-    # Per-kernel times: event nodes are not allowed inside the graph's WHILE body, and
-    # events between the timed steps' kernels would add to their time, so a few steps are
-    # replayed with the stream driver (the graph's kernels launched one iteration at a
-    # time) and every kernel timed with events there.
-    Usnap = s.getSolution()
-    s.set_timing(True)
-    s.set_krylov("stream")
-    run_steps(s, 1)  # one untimed stream-driven step first
-    s.kernel_stats(reset=True)
-    _, _, rrecs = run_steps(s, min(args.steps, 10))
-    s.synchronize()
-    stats = s.kernel_stats(reset=True)
-    s.set_krylov("graph")
-    s.set_state(Usnap)
-    # mean number of basis vectors read per iteration in the replay (j + 1 at iteration j)
-    jits = [r[1] for r in rrecs]
-    jbar = (sum(i * (i + 1) / 2 for i in jits) / max(1, sum(jits))) - 1.0
-    t_max = all_max(world, t_dev)
-    units = all_sum(world, float(evals * nc))
-    value = units / t_max
-
-    # ---- roofline of the dominant kernel class
-    # The timed steps' GMRES graphs are timed whole (CUDA events around each graph launch:
-    # krylov_ms).  The replay times every Arnoldi kernel alone (its events add ~2-3 us per
-    # launch and it runs without programmatic dependent launch), so the graph time is
-    # attributed to the kernel classes in proportion to their replay averages.
-    iters = evals - args.steps
-    t_kry_ms = sum(r[4] for r in recs)
-    replay_sum = sum(ms / n for k, (ms, n) in stats.items() if k.startswith("krylov.") and n)
-    attr = t_kry_ms / (replay_sum * iters) if replay_sum > 0 and iters > 0 else 1.0
-    peak, peak_kind = measured_peak()
-    kern = {}
-    for k, (ms, n) in stats.items():
-        if n == 0:
-            continue
-        grp, name = k.split(".")
-        if grp == "krylov":
-            b = krylov_bytes(name, nc, nf, 4, 4, jbar)
-        else:
-            dual = grp == "jv"
-            b = algorithmic_bytes(name, nc, nf, 4, 4 if dual else 8, "SECOND_ORDER_CENTRAL", True, dual)
-        avg = ms / n
-        kern[k] = {"replay_launches": n, "avg_us": round(avg * 1e3, 3), "algorithmic_bytes": int(b)}
-        if grp == "residual":
-            kern[k]["timed_launches"] = args.steps
-            kern[k]["est_total_ms"] = round(avg * args.steps, 4)
-            kern[k]["source"] = "stream-driver replay (CUDA events around the kernel)"
-        elif grp != "krylov":
-            kern[k]["est_total_ms"] = round(ms, 4)
-        if grp == "krylov":
-            # replayed launches: their averages scaled to the graph's measured time, times
-            # the Arnoldi iterations of the timed steps
-            kern[k]["replay_avg_us"] = kern[k].pop("avg_us")
-            avg = avg * attr
-            kern[k]["avg_us"] = round(avg * 1e3, 3)
-            kern[k]["timed_launches"] = iters
-            kern[k]["est_total_ms"] = round(avg * iters, 4)
-            kern[k]["source"] = ("stream-driver replay of the graph's kernels, scaled by the graph time "
-                                 f"(factor {attr:.3f})")
-        kern[k]["achieved_gbs"] = round(b / (avg * 1e-3) / 1e9, 1)
-        kern[k]["share_of_step"] = round(kern[k]["est_total_ms"] / (t_dev * 1e3), 4)
-    dom = max(kern, key=lambda k: kern[k]["est_total_ms"])
-    d = kern[dom]
-    traffic = profile_traffic(dom, jbar)
-    roofline = {"bound": "hbm", "kernel": dom, "achieved": d["achieved_gbs"], "peak": peak, "unit": "GB/s",
-                "frac": round(d["achieved_gbs"] / peak, 4), "peak_source": f"{peak_kind} (MEASURED_PEAKS.json hbm_gbs)"
-                if peak_kind == "measured" else "fallback 6.8 TB/s",
-                "traffic": traffic}
-
-    # ---- the FP64 residual: HBM fraction (live) beside the FP64-pipe fraction (ncu)
-    pipe = profile_fp64_pipe()
-    fp64_residual = {}
-    for k in ("residual.prim", "residual.grad", "residual.flux", "residual.gather"):
-        if k in kern:
-            e = {"avg_us": kern[k]["avg_us"], "hbm_frac": round(kern[k]["achieved_gbs"] / peak, 4)}
-            e.update(pipe.get(k, {}))
-            fp64_residual[k.split(".")[1]] = e
-    fp64_residual["source"] = "hbm_frac: this run; fp64_pipe_frac, flops: profiles/fp64_pipe.txt (ncu)"
-
-    # ---- e2e through the C ABI with pinned host buffers (per-kernel timing off: the
-    # production call)
+def newton_plate(api, args, device, steps=20, warmup=5):
+    """The mixed-precision Newton step (FP32 Krylov basis and exact J v, FP64 residual and
+    update) on the laminar flat plate: device time of `steps` steps after `warmup`, the same
+    steps end to end through the C ABI (state restored with its CFL and step counter, then
+    uploaded from and read back to pinned host memory every step), and the plain FP64
+    path with the reference's FD J v on the same steps."""
+    from mycode_gb300 import meshgen
     import torch
+    mesh = api.Mesh.from_spec(meshgen.laminar_plate(240, 120, ratio=1.08))
+    nc = mesh.n_cells
+    s = plate_solver(api, mesh, device, "mixed")
+    s.set_timing("steps")
+    for _ in range(warmup):
+        s.newton_step(0.0)
+    Usnap = s.getSolution()
+    cfl, step = s.newton_state()
+    s.synchronize()
+    t_dev, evals, recs = run_newton_steps(s, steps)
+    # e2e: the same steps again (same state, CFL and step counter)
     Uh = torch.empty((nc, 6), dtype=torch.float64, pin_memory=True).numpy()
-    s.getSolution(out=Uh)
+    Uh[:] = Usnap
+    s.set_newton_state(cfl, step)
     s.set_timing(False)
     s.synchronize()
-    barrier(world)
     t0 = time.perf_counter()
-    e_evals = 0
-    for _ in range(args.steps):
+    e_evals, e_iters = 0, []
+    for _ in range(steps):
         s.set_state(Uh)
         rec, _ = s.newton_step(0.0)
         s.getSolution(out=Uh)
         e_evals += 1 + rec.gmres_iters
+        e_iters.append(rec.gmres_iters)
     s.synchronize()
-    barrier(world)
-    t_e2e = all_max(world, time.perf_counter() - t0)
-    clocks = clk.stop()
-    clocks["window"] = "warm-up, timed steps, kernel replay and e2e steps"
-    e_units = all_sum(world, float(e_evals * nc))
-    e2e = {"value": e_units / t_e2e, "unit": UNIT, "h2d_bytes_per_step": nc * 6 * 8, "d2h_bytes_per_step": nc * 6 * 8,
-           "api": "cfdg_set_state + cfdg_newton_step + cfdg_get_state"}
-
-    # ---- the plain FP64 path (FD J v), same protocol
-    s64 = make_solver(api, mesh, local, "fp64")
-    s64.set_timing(True)
-    for _ in range(args.warmup):
+    t_e2e = time.perf_counter() - t0
+    s.close()
+    s64 = plate_solver(api, mesh, device, "fp64")
+    s64.set_timing("steps")
+    for _ in range(warmup):
         s64.newton_step(0.0)
     s64.synchronize()
-    t64, ev64, recs64 = run_steps(s64, args.steps)
-    fp64 = {"value": ev64 * nc / t64, "unit": UNIT, "ms_per_step": 1e3 * t64 / args.steps,
-            "gmres_iters": [r[1] for r in recs64], "jv": "one-sided FD (reference)"}
-
-    # ---- adjoint / primal cost: FP64 VJP (gradients and limiter recomputed) over one FP64
-    # residual, CUDA-event kernel time on the same state, L2 flushed before each
-    s64.set_timing(True)
-    s64.kernel_stats(reset=True)
-    reps = 20
-    for _ in range(reps):
-        s64.flush_l2(L2_FLUSH_BYTES)
-        s64.residual_device(True)
-        s64.flush_l2(L2_FLUSH_BYTES)
-        s64.vjp_device()
-    st64 = s64.kernel_stats(reset=True)
-    t_res = sum(st64[k][0] for k in st64 if k.startswith("residual.")) / reps
-    t_vjp = sum(st64[k][0] for k in st64 if k.startswith("vjp.")) / reps
-    adjoint = {"ratio": t_vjp / t_res, "residual_ms": t_res, "vjp_ms": t_vjp,
-               "note": "FP64 VJP of the full residual (forward recomputation included) / FP64 residual"}
-
-    # ---- time to a density residual of 1e-10: mixed vs the FP64 paths on the supersonic
-    # wedge (the reference's own CPU case, which converges under the reference's CFL control)
-    t2c = time_to_converge(api) if (rank == 0 and not args.no_t2c) else None
-    others = other_configs(api) if (rank == 0 and not args.no_t2c) else None
-
-    # ---- CPU baseline: the oracle port on this host, bounded sample
-    cpu = None
-    if rank == 0 and world == 1 and not args.no_cpu_baseline:
-        cpu = cpu_baseline_sample(args.cpu_steps)
-
-    if rank == 0:
-        line = {
-            "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
-            "warmup": args.warmup, "ms_per_step": 1e3 * t_max / args.steps, "higher_is_better": True,
-            "scaling": "weak", "vs_baseline": None, "dtype": "f32 Krylov/J v + f64 residual/update",
-            "data": "synthetic (seeded mesh recipe, free-stream start)",
-            "config": dict(WORKLOAD, precision="mixed", jv="exact (dual numbers, FP32)",
-                           l2="flushed between timed steps (256 MiB write)", parallelism="replicas" if world > 1 else "1 GPU"),
-            "gmres_iters": [r[1] for r in recs],
-            "res_vm": [r[0] for r in recs],
-            "gpu_launches": launches,
-            "krylov_driver": kinfo,
-            "roofline": roofline,
-            "kernels": kern,
-            "fp64_residual": fp64_residual,
-            "e2e": e2e,
-            "fp64": fp64,
-            "adjoint_over_primal": adjoint,
-            "time_to_1e-10": t2c,
-            "other_configs": others,
-            "clocks": clocks,
-            "cpu_baseline": cpu,
-        }
-        print(json.dumps(line))
+    t64, ev64, recs64 = run_newton_steps(s64, steps)
+    s64.close()
+    return {"workload": PLATE, "steps": steps, "warmup": warmup, "value": evals * nc / t_dev, "unit": UNIT,
+            "ms_per_step": 1e3 * t_dev / steps, "gmres_iters": [r[1] for r in recs],
+            "precision": "mixed (FP32 Krylov basis and exact J v; FP64 residual, update, Hessenberg, norms)",
+            "e2e": {"value": e_evals * nc / t_e2e, "unit": UNIT, "gmres_iters": e_iters,
+                    "h2d_bytes_per_step": nc * 6 * 8, "d2h_bytes_per_step": nc * 6 * 8,
+                    "api": "cfdg_set_state + cfdg_newton_step + cfdg_get_state"},
+            "fp64": {"value": ev64 * nc / t64, "unit": UNIT, "ms_per_step": 1e3 * t64 / steps,
+                     "gmres_iters": [r[1] for r in recs64], "jv": "one-sided FD (reference)"}}
 
 
 def other_configs(api, steps=20, warmup=3):
@@ -540,7 +635,7 @@ def other_configs(api, steps=20, warmup=3):
         try:
             for _ in range(warmup):
                 s.newton_step(0.0)
-            t, evals, recs = run_steps(s, steps)
+            t, evals, recs = run_newton_steps(s, steps)
             out[name] = {"n_cells": mesh.n_cells, "n_faces": mesh.n_faces, "value": evals * mesh.n_cells / t,
                          "unit": UNIT, "ms_per_step": 1e3 * t / steps, "steps": steps, "warmup": warmup,
                          "gmres_iters": [r[1] for r in recs], "res_vm_first_last": [recs[0][0], recs[-1][0]]}
@@ -611,44 +706,59 @@ def time_to_converge(api, max_steps=1500):
 
 # ---------------------------------------------------------------- CPU side
 
+def _oracle_headline(target: int):
+    """The CPU restatement (oracle/) on the headline mesh, scheme and state."""
+    from oracle.oracle import OracleSolver
+    spec = headline_spec(target)
+    o = OracleSolver(spec, bcset="bump", viscous=True, init="bump")
+    o.setNumericalMethod("HLLC", "SECOND_ORDER_LIMITED")
+    o.setFlowConditions(0.5, 101325.0, 300.0)
+    o.setKinematicViscosity(3e6, 1.0)
+    o.initialize()
+    U = o.get_state()
+    k, w = o.sst_freestream()
+    U[:, 4] = U[:, 0] * k
+    U[:, 5] = U[:, 0] * w
+    return spec, o, perturb_state(U, o.cells()[:, 1:])
+
+
 def _cpu_worker(args):
-    """One independent copy of the CPU path: untimed warm-up Newton steps, then a timed
-    solveImplicit of `steps` steps continuing from that state."""
-    warm, steps, kind = args
+    """One independent copy of the CPU path: `warm` untimed FP64 SST residual evaluations of
+    the headline case, then `steps` timed ones (or as many as fit in `seconds` when steps is
+    0)."""
+    target, warm, steps, seconds = args
     sys.path.insert(0, ROOT)
-    from oracle.oracle import OracleSolver, RefSolver
-    spec = workload_spec()
-    if kind == "reference":
-        s = RefSolver(spec, "plate_visc")
-    else:
-        s = OracleSolver(spec, bcset="plate", viscous=True, init="freestream")
-    setup_flow(s)
-    if warm:
-        s.solveImplicit(0.0, warm)
-    t0 = time.perf_counter()
-    tr = s.solveImplicit(0.0, steps)
-    t = time.perf_counter() - t0
-    evals = int(len(tr["res_vm"]) + tr["gmres_iters"].sum())
-    return evals, t, len(tr["res_vm"])
+    spec, o, U = _oracle_headline(target)
+    for _ in range(warm):
+        o.residual_sst(U)
+    n, t0 = 0, time.perf_counter()
+    while (steps and n < steps) or (not steps and time.perf_counter() - t0 < seconds):
+        o.residual_sst(U)
+        n += 1
+    return n, time.perf_counter() - t0, o.n_cells
 
 
-def cpu_kind():
-    from oracle.oracle import ref_available
-    return "reference" if ref_available("plate_visc") else "port"
-
-
-def cpu_baseline_sample(steps: int):
-    """The first `steps` Newton steps of the workload on one host core (the GMRES
-    iterations per step grow along the solve: 150 steps are about 2,400 evaluations,
-    15-35 s of FP64 FD work on one core)."""
+def cpu_baseline_sample(target: int, seconds: float):
+    """The CPU path on one host core: FP64 SST residual evaluations of the headline case for
+    about `seconds` after one untimed evaluation."""
     from oracle.oracle import build_oracle
     build_oracle()
-    kind = cpu_kind()
-    evals, t, n = _cpu_worker((0, steps, kind))
-    nc = WORKLOAD["n_cells"]
-    return {"value": evals * nc / t, "unit": UNIT, "cores": 1, "kind": kind,
-            "sample": f"{n} Newton steps ({evals} residual/J v evaluations, FD J v, FP64) of the same workload "
-                      f"from the free-stream start on 1 host core, {t:.1f} s"}
+    n, t, nc = _cpu_worker((target, 1, 0, seconds))
+    return {"value": n * nc / t, "unit": UNIT, "cores": 1, "kind": "port",
+            "sample": f"{n} FP64 residual evaluations (SST, HLLC, BJ limiter, viscous) of the same {nc:,}-cell "
+                      f"mesh and state on 1 host core after one untimed evaluation, {t:.1f} s (oracle/ restatement; "
+                      "the reference has no SST)"}
+
+
+def reference_copies(per_copy_bytes: float = 3.2e9) -> int:
+    """One copy per host core, capped by the memory available (a copy of the 4M-cell case
+    holds about 2.5 GB)."""
+    cores = os.cpu_count() or 1
+    try:
+        avail = os.sysconf("SC_AVPHYS_PAGES") * os.sysconf("SC_PAGE_SIZE")
+        return max(1, min(cores, int(avail // per_copy_bytes)))
+    except (ValueError, OSError, AttributeError):
+        return cores
 
 
 def reference_arm(args):
@@ -658,24 +768,28 @@ def reference_arm(args):
         return
     from oracle.oracle import build_oracle
     build_oracle()
-    kind = cpu_kind()
-    cores = os.cpu_count() or 1
+    copies = reference_copies()
     import multiprocessing as mp
     ctx = mp.get_context("spawn")
-    with ctx.Pool(cores) as pool:
-        res = pool.map(_cpu_worker, [(args.warmup, args.steps, kind)] * cores)
-    nc = WORKLOAD["n_cells"]
+    with ctx.Pool(copies) as pool:
+        res = pool.map(_cpu_worker, [(args.cells, args.warmup, args.steps, 0.0)] * copies)
+    nc = res[0][2]
     evals = sum(r[0] for r in res)
     t = max(r[1] for r in res)
     value = evals * nc / t
+    spec = headline_spec(args.cells)
     line = {
         "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": 1e3 * t / args.steps, "higher_is_better": True, "scaling": "weak",
-        "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded mesh recipe, free-stream start)",
-        "config": dict(WORKLOAD, precision="fp64", jv="one-sided FD (reference)"),
-        "cpu_baseline": {"value": value, "unit": UNIT, "cores": cores, "kind": kind,
-                         "sample": f"{cores} independent copies x {args.steps} Newton steps after {args.warmup} "
-                                   f"warm-up steps ({evals} evaluations in {t:.1f} s)"},
+        "vs_baseline": None, "dtype": "f64",
+        "data": "synthetic (seeded mesh recipe and seeded smooth perturbation of the initial state)",
+        "config": dict(headline_workload(spec), parallelism="1 GPU"),
+        "cpu_baseline": {"value": value, "unit": UNIT, "cores": copies, "kind": "port",
+                         "sample": f"{copies} independent copies (one per host core{' the memory allows' if copies < (os.cpu_count() or 1) else ''}) "
+                                   f"x {args.steps} FP64 residual evaluations of the same {nc:,}-cell mesh and state "
+                                   f"after {args.warmup} untimed ones ({evals} evaluations in {t:.1f} s); the plain-C "
+                                   "restatement of the reference's residual with the SST terms (oracle/; the "
+                                   "reference has no SST)"},
         "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line))
@@ -687,133 +801,136 @@ SWEEP_SIZES = (64_000, 256_000, 1_000_000, 4_000_000)
 
 
 def sweep(args):
-    """Per-kernel throughput of the residual, the exact J v and the VJP in FP64 and FP32
-    on the Gaussian-bump channel (3 x 1, height 0.05, width 0.2, triangles, 10 % seeded
-    jitter) at M = 0.5, Re = 3e6 with SST, HLLC, second-order limited; one JSON line."""
-    from mycode_gb300 import api, meshgen
-    import numpy as np
+    """Per-kernel throughput of the residual, the exact J v and the VJP in FP64 and FP32 on
+    the headline's Gaussian-bump channel at 64k-4M cells; one JSON line."""
+    from mycode_gb300 import api
     peak, peak_kind = measured_peak()
     sizes = [int(x) for x in args.sweep_sizes.split(",")] if args.sweep_sizes else SWEEP_SIZES
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    pipe_peak_warp = api.fp64_pipe_rate(local) / 32.0
+    pipe_prof = profile_fp64_pipe()
     out = []
-    clk = ClockSampler(int(os.environ.get("LOCAL_RANK", "0")))
+    clk = ClockSampler(local)
     clk.start()
     for target in sizes:
-        spec = meshgen.bump(target, jitter=0.10, seed=0)
+        spec = headline_spec(target)
         mesh = api.Mesh.from_spec(spec)
-        nc, nf = mesh.n_cells, mesh.n_faces
-        s = api.Solver(mesh, bcset="bump", init="bump", viscous=1, turbulence="sst", precision="mixed", jv="exact",
-                       flux="HLLC", spatial="SECOND_ORDER_LIMITED")
-        s.setFlowConditions(0.5, 101325.0, 300.0)
-        s.setKinematicViscosity(3e6, 1.0)
-        s.initialize()
-        U0 = s.getSolution()
-        cells = mesh.cells()
-        pert = meshgen.smooth_perturbation(cells[:, 1:], 7, 0.05)
-        U = U0.copy()
-        for c in range(4):
-            U[:, c] *= 1.0 + pert[:, c]
-        U[:, 4] *= 1.0 + 0.5 * pert[:, 0]
-        U[:, 5] *= 1.0 + 0.5 * pert[:, 1]
+        s = bump_solver(api, mesh, local)
+        U = perturb_state(s.getSolution(), mesh.cells()[:, 1:])
         s.set_state(U)
-        s.residual_device(True)
-        s.set_dt(s.local_timestep(10.0))
-        v = np.random.default_rng(1).standard_normal(U.shape) * np.abs(U).mean(axis=0)
-        lam = np.random.default_rng(2).standard_normal(U.shape)
-        s.set_timing(True)
-        ops = {
-            "residual_fp64": (lambda: s.residual_device(True), "residual.", 8, False),
-            "residual_fp32": (lambda: s.residual32(), "residual.", 4, False),
-            "jv_fp64": (lambda: s.apply_jacobian(U, None, v, mode="exact"), "jv.", 8, True),
-            "jv_fp32": (lambda: s.apply_jacobian32(U, v), "jv.", 4, True),
-            "vjp_fp64": (lambda: s.vjp(lam, U), "vjp.", 8, None),
-        }
-        res = {"n_cells": nc, "n_faces": nf}
-        for name, (fn, cls, sz, dual) in ops.items():
-            for _ in range(2):
-                fn()
-            s.synchronize()
-            s.kernel_stats(reset=True)
-            for _ in range(args.sweep_reps):
-                s.flush_l2(L2_FLUSH_BYTES)
-                fn()
-            s.synchronize()
-            st = s.kernel_stats(reset=True)
-            kern, tot = {}, 0.0
-            for k, (ms, n) in st.items():
-                if not k.startswith(cls) or n == 0:
-                    continue
-                avg = ms / n
-                tot += avg
-                entry = {"avg_us": round(avg * 1e3, 2)}
-                if dual is not None:
-                    b = algorithmic_bytes(k.split(".")[1], nc, nf, 6, sz, "SECOND_ORDER_LIMITED", True, dual)
-                    entry.update(algorithmic_bytes=int(b), gbs=round(b / (avg * 1e-3) / 1e9, 1),
-                                 hbm_frac=round(b / (avg * 1e-3) / 1e9 / peak, 4))
-                kern[k.split(".")[1]] = entry
-            r = {"ms": round(tot, 4), "cell_residuals_per_s": nc / (tot * 1e-3), "kernels": kern}
-            if dual is None:
-                b = vjp_algorithmic_bytes(nc, nf, 6, "SECOND_ORDER_LIMITED")
-                r.update(algorithmic_bytes=int(b), gbs=round(b / (tot * 1e-3) / 1e9, 1),
-                         hbm_frac=round(b / (tot * 1e-3) / 1e9 / peak, 4))
-            res[name] = r
+        res = {"n_cells": mesh.n_cells, "n_faces": mesh.n_faces}
+        res.update(kernel_paths(s, U, mesh.n_cells, mesh.n_faces, peak, args.sweep_reps, pipe_peak_warp, pipe_prof))
         res["vjp_fp32"] = None  # the adjoint runs in FP64 only
-        res["vjp_over_residual_fp64"] = res["vjp_fp64"]["ms"] / res["residual_fp64"]["ms"]
         out.append(res)
         s.close()
         del mesh
     clocks = clk.stop()
-    cpu = None
-    if not args.no_cpu_baseline:
-        cpu = sweep_cpu_sample(SWEEP_SIZES[0])
+    cpu = None if args.no_cpu_baseline else cpu_baseline_sample(sizes[0], 5.0)
     line = {"metric": "bandwidth sweep: cell-residuals/s per kernel", "unit": UNIT,
             "config": {"workload": "Gaussian bump channel 3x1 (height 0.05, width 0.2), triangles, 10% seeded jitter, "
                                    "M=0.5 Re=3e6, SST, HLLC, 2nd-order limited; seeded smooth perturbation of the "
                                    "initial state", "l2": "flushed before every evaluation"},
-            "peak_gbs": peak, "peak_source": peak_kind, "sizes": out, "clocks": clocks, "cpu_baseline": cpu}
+            "peak_gbs": peak, "peak_source": peak_kind, "fp64_pipe_warp_inst_per_s": pipe_peak_warp, "sizes": out,
+            "clocks": clocks, "cpu_baseline": cpu}
     print(json.dumps(line))
 
 
-def sweep_cpu_sample(target: int):
-    """The oracle's FP64 SST residual on one host core at the smallest sweep size."""
-    from oracle.oracle import build_oracle, OracleSolver
-    from mycode_gb300 import meshgen
-    build_oracle()
-    spec = meshgen.bump(target, jitter=0.10, seed=0)
-    o = OracleSolver(spec, bcset="bump", viscous=True, init="bump")
-    o.setNumericalMethod("HLLC", "SECOND_ORDER_LIMITED")
-    o.setFlowConditions(0.5, 101325.0, 300.0)
-    o.setKinematicViscosity(3e6, 1.0)
-    o.initialize()
-    U = o.get_state()
-    k, w = o.sst_freestream()
-    U[:, 4] = U[:, 0] * k
-    U[:, 5] = U[:, 0] * w
-    o.residual_sst(U)
-    n, t0 = 0, time.perf_counter()
-    while time.perf_counter() - t0 < 5.0:
-        o.residual_sst(U)
-        n += 1
-    t = time.perf_counter() - t0
-    return {"value": n * o.n_cells / t, "unit": UNIT, "cores": 1, "kind": "port",
-            "sample": f"{n} FP64 SST residual evaluations of the {o.n_cells}-cell bump on 1 host core, {t:.1f} s"}
+# ---------------------------------------------------------------- profiling cases
+
+def profile_case(args):
+    """One kernel path, `--reps` times, on a chosen case, printing per-kernel CUDA-event
+    times: the workload for ncu captures (profiles/ gives the exact commands).
+    Paths: residual64 / residual32 (the FP64 / FP32 residual), jv64 / jv32 (exact J v),
+    vjp64 (the adjoint), krylov_stream (mixed Newton steps whose GMRES runs the graph
+    driver's kernels from the stream driver, outside a graph, so ncu sees them).
+    Workloads: the headline's bump channel at --cells (SST unless --no-sst) or the laminar
+    plate of the Newton-step measurement."""
+    import numpy as np
+    from mycode_gb300 import api, meshgen
+    gm = {}
+    if args.gmres_m is not None:
+        gm["gmres_m"] = args.gmres_m
+    if args.gmres_tol is not None:
+        gm["gmres_tol"] = args.gmres_tol
+    if args.profile_workload == "laminar_plate":
+        m = api.Mesh.from_spec(meshgen.laminar_plate(240, 120, ratio=1.08))
+        s = api.Solver(m, bcset="plate", init="freestream", viscous=1, flux="ROE", spatial="SECOND_ORDER_CENTRAL",
+                       precision="mixed", jv="exact", krylov=2, **gm)
+        s.setFreestreamStatic(0.2, 101325.0, 300.0)
+        s.setKinematicViscosity(1e5, 1.0)
+        s.initialize()
+        U = s.getSolution()
+    else:
+        m = api.Mesh.from_spec(headline_spec(args.cells))
+        s = api.Solver(m, bcset="bump", init="bump", viscous=1, turbulence="none" if args.no_sst else "sst",
+                       flux="HLLC", spatial="SECOND_ORDER_LIMITED", precision="mixed", jv="exact", krylov=2, **gm)
+        s.setFlowConditions(0.5, 101325.0, 300.0)
+        s.setKinematicViscosity(3e6, 1.0)
+        s.initialize()
+        U = perturb_state(s.getSolution(), m.cells()[:, 1:])
+        s.set_state(U)
+    s.set_timing(True)
+    s.residual_device(True)
+    s.set_dt(s.local_timestep(100.0))
+    v = np.random.default_rng(3).standard_normal(U.shape) * np.abs(U).mean(axis=0)
+    lam = np.random.default_rng(4).standard_normal(U.shape)
+    run, prefix = {
+        "residual64": (lambda: s.residual_device(True), "residual."),
+        "residual32": (lambda: s.residual32(), "residual."),
+        "jv64": (lambda: s.apply_jacobian(U, None, v, mode="exact"), "jv."),
+        "jv32": (lambda: s.apply_jacobian32(U, v), "jv."),
+        "vjp64": (lambda: s.vjp(lam, U), "vjp."),
+        "krylov_stream": (lambda: s.newton_step(0.0), "krylov."),
+    }[args.profile_case]
+    s.synchronize()
+    s.kernel_stats(reset=True)
+    t0 = time.perf_counter()
+    iters = []
+    for _ in range(args.reps):
+        r = run()
+        if args.profile_case == "krylov_stream":
+            iters.append(r[0].gmres_iters)
+    s.synchronize()
+    st = s.kernel_stats(reset=True)
+    line = {"path": args.profile_case, "workload": args.profile_workload, "cells": m.n_cells, "faces": m.n_faces,
+            "ms_per_launch": {k: round(v[0] / v[1], 5) for k, v in st.items() if k.startswith(prefix) and v[1]},
+            "wall_s": time.perf_counter() - t0}
+    if iters:
+        # Arnoldi iterations per solve and the mean basis index j over them (iteration j
+        # reads j + 1 stored vectors)
+        line["gmres_iters"] = iters
+        line["mean_j"] = sum(i * (i - 1) / 2 for i in iters) / max(1, sum(iters))
+        line["launches"] = {k: v[1] for k, v in st.items() if k.startswith(prefix) and v[1]}
+    print(json.dumps(line))
 
 
 def main():
     ap = argparse.ArgumentParser(description=__doc__.split("\n")[0])
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=60)
+    ap.add_argument("--steps", type=int, default=20)
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    ap.add_argument("--cells", type=int, default=HEADLINE_CELLS, help="target cells of the bump channel")
     ap.add_argument("--no-cpu-baseline", action="store_true")
-    ap.add_argument("--cpu-steps", type=int, default=150)
-    ap.add_argument("--no-t2c", action="store_true", help="skip the time-to-1e-10 solves")
+    ap.add_argument("--cpu-seconds", type=float, default=15.0)
+    ap.add_argument("--quick", action="store_true", help="the headline only (no secondary measurements)")
     ap.add_argument("--sweep", action="store_true", help="bandwidth sweep on the bump channel instead")
     ap.add_argument("--sweep-sizes", default="", help="comma-separated target cell counts")
     ap.add_argument("--sweep-reps", type=int, default=10)
+    ap.add_argument("--profile-case", default=None,
+                    choices=["residual64", "residual32", "jv64", "jv32", "vjp64", "krylov_stream"],
+                    help="run one kernel path --reps times (ncu workload) instead")
+    ap.add_argument("--profile-workload", default="bump", choices=["bump", "laminar_plate"])
+    ap.add_argument("--no-sst", action="store_true", help="profile case: the bump without SST")
+    ap.add_argument("--reps", type=int, default=3)
+    ap.add_argument("--gmres-m", type=int, default=None, help="profile case: Krylov dimension")
+    ap.add_argument("--gmres-tol", type=float, default=None, help="profile case: GMRES tolerance (0: m iterations)")
     args = ap.parse_args()
-    if args.warmup < 3:
+    if args.warmup < 3 and not args.profile_case:
         ap.error("--warmup must be at least 3")
-    if args.sweep:
+    if args.profile_case:
+        profile_case(args)
+    elif args.sweep:
         sweep(args)
     elif args.impl == "reference":
         reference_arm(args)

@@ -37,8 +37,10 @@ typedef enum cfdg_status {
     CFDG_ERR_NOT_CONVERGED = 4, /* solve stopped at max_steps above tolerance */
     CFDG_ERR_TIMEOUT = 5,       /* a bounded device-side wait gave up */
     CFDG_ERR_MESH = 6,          /* mesh file or connectivity error */
-    CFDG_ERR_UNSUPPORTED = 7,   /* option combination not available */
-    CFDG_ERR_BREAKDOWN = 8      /* GMRES breakdown (zero Krylov direction) */
+    CFDG_ERR_UNSUPPORTED = 7    /* option combination not available */
+    /* A GMRES breakdown (h_{j+1,j} <= 1e-12, src/Solver.cpp:1553) is not an error: as in the
+     * reference the basis vector is left unscaled and the solve goes on; a non-finite
+     * solution then surfaces as CFDG_ERR_NAN at the Newton update. */
 } cfdg_status;
 
 /* FluxScheme (include/Types.hpp:38-43); AUSM evaluates LLF as in include/Flux.hpp:225 */
@@ -99,6 +101,9 @@ typedef struct cfdg_config {
      * the first with programmatic dependent launch, so each starts while its predecessor's
      * tail (grid reduction, Givens step) runs; 0 launches them plainly */
     int pdl;
+    /* persistent Arnoldi kernel: polls of a grid barrier before the wait gives up and the
+     * solve reports CFDG_ERR_TIMEOUT (0 = the default, 2^24 polls, seconds in all) */
+    int barrier_poll_limit;
 } cfdg_config;
 
 /* CFDG_KRYLOV_STREAM launches the graph driver's kernels one iteration at a time from a
@@ -222,6 +227,11 @@ cfdg_status cfdg_newton_step(cfdg_solver* s, double tol, cfdg_step* info, int* c
 cfdg_status cfdg_set_krylov(cfdg_solver* s, int mode);
 /* Newton driver state (CFL, step counter) */
 cfdg_status cfdg_reset_newton(cfdg_solver* s);
+/* The pseudo-transient driver's two loop variables, the CFL number and the step counter
+ * of solveImplicit (src/Solver.cpp:1701, :1705), read and restored: a caller that saves
+ * the state (cfdg_get_state) and these two can replay the same Newton steps later. */
+cfdg_status cfdg_get_newton_state(cfdg_solver* s, double* cfl, int* step);
+cfdg_status cfdg_set_newton_state(cfdg_solver* s, double cfl, int step);
 
 /* Adjoint: gU = (dR/dU)^T lambda for the full residual at U, gradients and limiter
  * recomputed and differentiated along the branches the forward pass took (no
@@ -281,12 +291,19 @@ cfdg_status cfdg_flush_l2(cfdg_solver* s, size_t bytes);
  * out: one device double, receives sqrt(sum_i (sum_c (R_c,i/vol_i)^2) vol_i / sum_i vol_i).
  * stream: a cudaStream_t (NULL = default stream); the call only enqueues work.
  * Allocates nothing: its reduction scratch is a static device array sized for at most
- * 8,388,608 cells (larger n_cells is rejected with CFDG_ERR_ARG).  The first call on a
- * device looks that array's address up (cudaGetSymbolAddress) with the device current;
- * make that first call before any stream capture.  All calls share the array: calls
- * that overlap on the GPU race and must be serialised by the caller. */
+ * 8,388,608 cells (larger n_cells is rejected with CFDG_ERR_ARG).  Every call made outside
+ * a stream capture looks that array's address up (cudaGetSymbolAddress) with the device
+ * current; a call inside a capture uses the address of the device's last uncaptured call,
+ * so make one call before any stream capture (and again after a cudaDeviceReset).  All
+ * calls share the array: calls that overlap on the GPU race and must be serialised by
+ * the caller. */
 cfdg_status cfdg_norm_vm_noalloc(const double* R, const double* vol, long n_cells, int nv, double* out,
                                  void* stream);
+/* Throughput of the FP64 pipe of `device`: a stream of independent FP64 fused
+ * multiply-adds over every SM, timed with CUDA events (no reference counterpart; the
+ * denominator of the FP64 residual's roofline).  *fma_per_s gets thread-level FMAs per
+ * second (one FP64 pipe instruction each). */
+cfdg_status cfdg_fp64_pipe_rate(int device, double* fma_per_s);
 /* kernel launches issued by this solver since creation (all of them are this library's) */
 cfdg_status cfdg_launch_count(cfdg_solver* s, long long* n);
 /* the Krylov driver in effect: [0] CFDG_KRYLOV_* mode, [1] kernels per Arnoldi iteration

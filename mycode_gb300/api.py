@@ -29,7 +29,7 @@ PRECISION = {"fp64": 0, "mixed": 1}
 JV = {"fd": 0, "exact": 1}
 RENUMBER = {"none": 0, "hilbert": 1, "rcm": 2}
 STATUS = {0: "OK", 1: "ERR_ARG", 2: "ERR_CUDA", 3: "ERR_NAN", 4: "ERR_NOT_CONVERGED", 5: "ERR_TIMEOUT",
-          6: "ERR_MESH", 7: "ERR_UNSUPPORTED", 8: "ERR_BREAKDOWN"}
+          6: "ERR_MESH", 7: "ERR_UNSUPPORTED"}
 
 
 class CfdgError(RuntimeError):
@@ -47,6 +47,7 @@ class Config(C.Structure):
         ("limiter_freeze_step", C.c_int), ("limiter_freeze_cfl", C.c_double),
         ("turb_intensity", C.c_double), ("mut_ratio", C.c_double), ("shock_deflection_deg", C.c_double),
         ("renumber", C.c_int), ("device", C.c_int), ("krylov", C.c_int), ("persistent", C.c_int), ("pdl", C.c_int),
+        ("barrier_poll_limit", C.c_int),
     ]
 
 
@@ -102,6 +103,9 @@ SIGNATURES = {
     "cfdg_solve_implicit": (C.c_int, [_vp, C.c_double, C.c_int, C.POINTER(Step), C.POINTER(C.c_int)]),
     "cfdg_newton_step": (C.c_int, [_vp, C.c_double, C.POINTER(Step), C.POINTER(C.c_int)]),
     "cfdg_reset_newton": (C.c_int, [_vp]),
+    "cfdg_get_newton_state": (C.c_int, [_vp, C.POINTER(C.c_double), C.POINTER(C.c_int)]),
+    "cfdg_set_newton_state": (C.c_int, [_vp, C.c_double, C.c_int]),
+    "cfdg_fp64_pipe_rate": (C.c_int, [C.c_int, C.POINTER(C.c_double)]),
     "cfdg_set_krylov": (C.c_int, [_vp, C.c_int]),
     "cfdg_vjp": (C.c_int, [_vp, C.c_void_p, _dp, _dp]),
     "cfdg_wall_coefficients": (C.c_int, [_vp, C.c_int, C.c_void_p, C.c_void_p, C.c_void_p, C.POINTER(C.c_int)]),
@@ -151,6 +155,13 @@ def device_count() -> int:
     n = C.c_int(0)
     _check(lib().cfdg_device_count(C.byref(n)))
     return n.value
+
+
+def fp64_pipe_rate(device: int = 0) -> float:
+    """Thread-level FP64 FMAs per second of the device's FP64 pipe (a live measurement)."""
+    r = C.c_double(0.0)
+    _check(lib().cfdg_fp64_pipe_rate(int(device), C.byref(r)))
+    return r.value
 
 
 def default_config(**overrides) -> Config:
@@ -300,8 +311,15 @@ class Solver:
     get_state = getSolution
 
     # ---- residual path
-    def computeResiduals(self, U=None, update_limiters=True):
-        R = np.zeros(6 * self.n_cells)
+    def computeResiduals(self, U=None, update_limiters=True, out=None):
+        """R(U) in the reference's AoS layout; into ``out`` (a C-contiguous float64 array of
+        n_cells x 6, e.g. pinned host memory) when given."""
+        if out is None:
+            R = np.zeros(6 * self.n_cells)
+        else:
+            if out.dtype != np.float64 or not out.flags["C_CONTIGUOUS"] or out.size != 6 * self.n_cells:
+                raise ValueError("computeResiduals: out must be a C-contiguous float64 array of n_cells x 6")
+            R = out.reshape(-1)
         u = None if U is None else np.ascontiguousarray(U, np.float64).ravel()
         _check(lib().cfdg_residual(self._h, None if u is None else u.ctypes.data_as(_vp), R, int(update_limiters)))
         return R.reshape(-1, 6)
@@ -422,6 +440,15 @@ class Solver:
 
     def reset_newton(self):
         _check(lib().cfdg_reset_newton(self._h))
+
+    def newton_state(self):
+        """(CFL, step) of the pseudo-transient driver."""
+        c, n = C.c_double(), C.c_int()
+        _check(lib().cfdg_get_newton_state(self._h, C.byref(c), C.byref(n)))
+        return c.value, n.value
+
+    def set_newton_state(self, cfl, step):
+        _check(lib().cfdg_set_newton_state(self._h, float(cfl), int(step)))
 
     def vjp(self, lam, U=None):
         g = np.zeros(6 * self.n_cells)

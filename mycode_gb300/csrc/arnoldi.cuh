@@ -30,9 +30,10 @@ struct GridBar {
     unsigned* count;  // arrivals of the current barrier
     unsigned* gen;    // barrier generation
     int* err;         // set when a wait ran out
+    unsigned limit;   // polls before a wait gives up (2^24 by default)
 };
 
-// all blocks of the grid wait here; bounded wait (at most 2^24 polls)
+// all blocks of the grid wait here; bounded wait (at most b.limit polls)
 __device__ __forceinline__ void grid_barrier(const GridBar& b) {
     __syncthreads();
     if (threadIdx.x == 0) {
@@ -47,7 +48,7 @@ __device__ __forceinline__ void grid_barrier(const GridBar& b) {
         } else {
             unsigned polls = 0;
             while (*vgen == g) {
-                if (++polls > (1u << 24)) {  // each poll is an L2 round trip: seconds in all
+                if (++polls > b.limit) {  // each poll is an L2 round trip: 2^24 are seconds
                     atomicExch(b.err, 1);
                     break;
                 }

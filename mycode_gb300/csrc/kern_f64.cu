@@ -115,6 +115,27 @@ void launch_relaxed_add(int nv, long nc, double* U, const double* dU, double rel
     NV_SWITCH(nv, (k_relaxed_add<NVC><<<blocks_for(nc), tpb_for(nc), 0, s>>>(nc, U, dU, relax, bad)));
 }
 void launch_fill(long n, double* x, double v, cudaStream_t s) { k_fill<<<red_grid(n), RED_THREADS, 0, s>>>(n, x, v); }
+
+// FP64 pipe probe: FP64_STREAM_CHAINS independent chains x <- fma(x, a, b) per thread, so
+// every FP64 pipe issue slot can be filled; the result is stored only under a condition
+// no chain meets (x stays finite and positive), which keeps the chains live.
+__global__ void __launch_bounds__(256) k_fp64_fma_stream(double* sink, int iters, double a, double b) {
+    double x[FP64_STREAM_CHAINS];
+#pragma unroll
+    for (int k = 0; k < FP64_STREAM_CHAINS; ++k) x[k] = 1.0 + 1e-3 * (threadIdx.x + k);
+    for (int i = 0; i < iters; ++i) {
+#pragma unroll
+        for (int k = 0; k < FP64_STREAM_CHAINS; ++k) x[k] = fma(x[k], a, b);
+    }
+    double acc = 0.0;
+#pragma unroll
+    for (int k = 0; k < FP64_STREAM_CHAINS; ++k) acc += x[k];
+    if (acc < 0.0) sink[0] = acc;
+}
+
+void launch_fp64_fma_stream(int blocks, int threads, double* sink, int iters, cudaStream_t s) {
+    k_fp64_fma_stream<<<blocks, threads, 0, s>>>(sink, iters, 0.999999, 1e-6);
+}
 void launch_newton_update(int nv, long nc, double* U, const double* dU, double relax, double gam, double wmin, int* bad,
                           cudaStream_t s) {
     NV_SWITCH(nv, (k_newton_update<NVC><<<blocks_for(nc), tpb_for(nc), 0, s>>>(nc, U, dU, relax, gam, wmin, bad)));

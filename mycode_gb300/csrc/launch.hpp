@@ -112,6 +112,10 @@ void launch_unsteady_rhs(int nv, long nc, const double* U, const double* Uold, c
                          double dt, double* rhs, RedScratch rs, double* out2, cudaStream_t s);
 void launch_relaxed_add(int nv, long nc, double* U, const double* dU, double relax, int* bad, cudaStream_t s);
 void launch_fill(long n, double* x, double v, cudaStream_t s);
+// FP64 pipe probe: each thread runs FP64_STREAM_CHAINS independent FMA chains of `iters`
+// steps (kern_f64.cu)
+constexpr int FP64_STREAM_CHAINS = 8;
+void launch_fp64_fma_stream(int blocks, int threads, double* sink, int iters, cudaStream_t s);
 
 inline unsigned grid_for(long n, int threads = 256) { return (unsigned)((n + threads - 1) / threads); }
 // reduction / streaming grids: one entry per thread up to RED_BLOCKS blocks (enough warps

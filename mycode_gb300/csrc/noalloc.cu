@@ -41,9 +41,13 @@ constexpr int NA_COUNTER_SLOT = 2 * NA_MAX_BLOCKS;                            //
 // then the ticket counter in the first 4 bytes of slot NA_COUNTER_SLOT
 static __device__ __align__(256) double g_norm_scratch[2 * NA_MAX_BLOCKS + 32];
 
-// Same per-cell sum as norm_L2_VolumeWeighted (src/Solver.cpp:1280-1303) and k_norm_vm;
-// each block owns a fixed range of cells, the last block to finish combines the partials
-// in index order and writes sqrt(sum_sq / total_vol).
+// The per-cell sum of norm_L2_VolumeWeighted (src/Solver.cpp:1280-1303) with the
+// reference's own division R / vol per component; k_norm_vm takes the same quotients
+// through a shared reciprocal with a correction step, which rounds to the same bits, so
+// the per-cell terms agree exactly.  The sums over cells run in another order than
+// k_norm_vm's (each block owns a fixed range of cells, the last block to finish combines
+// the partials in index order and writes sqrt(sum_sq / total_vol)), so the two norms
+// agree to rounding, not bit for bit.
 __global__ void __launch_bounds__(NA_THREADS) k_norm_vm_static(long nc, int nv, const double* __restrict__ R,
                                                               const double* __restrict__ vol, double* scratch,
                                                               double* out) {
@@ -88,9 +92,13 @@ __global__ void __launch_bounds__(NA_THREADS) k_norm_vm_static(long nc, int nv, 
 std::mutex g_setup_mutex;
 double* g_scratch_ptr[128] = {};
 
-// Device address of the static scratch on the current device, looked up once per device
-// (the host-side name g_norm_scratch is only a stand-in, not a device address).
-cfdg_status scratch_address(double** out) {
+// Device address of the static scratch on the current device (the host-side name
+// g_norm_scratch is only a stand-in, not a device address).  Looked up again on every
+// call outside a stream capture, so a context torn down and made again (cudaDeviceReset)
+// gets the address in its new module; inside a capture the address from the device's
+// last uncaptured call is used, so a capture needs one uncaptured call on the device
+// first (and a fresh one after a device reset).
+cfdg_status scratch_address(cudaStream_t stream, double** out) {
     int dev = 0;
     cudaError_t e = cudaGetDevice(&dev);
     if (e != cudaSuccess) {
@@ -101,8 +109,19 @@ cfdg_status scratch_address(double** out) {
         cfdg::set_error_message("cfdg_norm_vm_noalloc: device ordinal above 127");
         return CFDG_ERR_ARG;
     }
+    cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;
+    e = cudaStreamIsCapturing(stream, &cap);
+    if (e != cudaSuccess) {
+        cfdg::set_error_message(std::string("cfdg_norm_vm_noalloc: cudaStreamIsCapturing: ") + cudaGetErrorString(e));
+        return CFDG_ERR_CUDA;
+    }
     std::lock_guard<std::mutex> lock(g_setup_mutex);
-    if (!g_scratch_ptr[dev]) {
+    if (cap != cudaStreamCaptureStatusNone) {
+        if (!g_scratch_ptr[dev]) {
+            cfdg::set_error_message("cfdg_norm_vm_noalloc: the first call on a device must come before any stream capture");
+            return CFDG_ERR_ARG;
+        }
+    } else {
         void* p = nullptr;
         e = cudaGetSymbolAddress(&p, g_norm_scratch);
         if (e != cudaSuccess || !p) {
@@ -137,9 +156,9 @@ extern "C" cfdg_status cfdg_norm_vm_noalloc(const double* R, const double* vol, 
         return CFDG_ERR_ARG;
     }
     double* scratch = nullptr;
-    cfdg_status st = scratch_address(&scratch);
-    if (st != CFDG_OK) return st;
     cudaStream_t s = static_cast<cudaStream_t>(stream);
+    cfdg_status st = scratch_address(s, &scratch);
+    if (st != CFDG_OK) return st;
     cudaError_t e = cudaMemsetAsync(scratch + NA_COUNTER_SLOT, 0, sizeof(unsigned), s);
     if (e != cudaSuccess) {
         cfdg::set_error_message(std::string("cfdg_norm_vm_noalloc: clearing the counter: ") + cudaGetErrorString(e));

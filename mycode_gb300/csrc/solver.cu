@@ -526,7 +526,8 @@ struct cfdg_solver {
         a.L = L;
         a.d = gd;
         a.part = apart;
-        a.bar = GridBar{bar, bar + 1, reinterpret_cast<int*>(bar + 2)};
+        a.bar = GridBar{bar, bar + 1, reinterpret_cast<int*>(bar + 2),
+                        cfg.barrier_poll_limit > 0 ? (unsigned)cfg.barrier_poll_limit : (1u << 24)};
         return a;
     }
 
@@ -1451,6 +1452,7 @@ void cfdg_config_default(cfdg_config* c) {
     c->krylov = CFDG_KRYLOV_AUTO;
     c->persistent = 0;
     c->pdl = 1;
+    c->barrier_poll_limit = 0;
 }
 
 cfdg_status cfdg_mesh_create(int n_nodes, const double* xy, int n_cells, const int* cells, int n_bedges,
@@ -1923,6 +1925,20 @@ cfdg_status cfdg_reset_newton(cfdg_solver* s) {
     return CFDG_OK;
 }
 
+cfdg_status cfdg_get_newton_state(cfdg_solver* s, double* cfl, int* step) {
+    if (!s || !cfl || !step) return fail(CFDG_ERR_ARG, "null argument");
+    *cfl = s->cfl;
+    *step = s->step;
+    return CFDG_OK;
+}
+
+cfdg_status cfdg_set_newton_state(cfdg_solver* s, double cfl, int step) {
+    if (!s || !(cfl > 0.0) || step < 0) return fail(CFDG_ERR_ARG, "bad Newton state");
+    s->cfl = cfl;
+    s->step = step;
+    return CFDG_OK;
+}
+
 cfdg_status cfdg_newton_step(cfdg_solver* s, double tol, cfdg_step* info, int* converged) {
     if (!s) return fail(CFDG_ERR_ARG, "null solver");
     int cv = 0;
@@ -2081,6 +2097,40 @@ cfdg_status cfdg_flush_l2(cfdg_solver* s, size_t bytes) {
     }
     CK(cudaMemsetAsync(s->l2buf, ++s->l2fill & 0xff, bytes, s->st));
     return CFDG_OK;
+}
+
+cfdg_status cfdg_fp64_pipe_rate(int device, double* fma_per_s) {
+    if (!fma_per_s) return fail(CFDG_ERR_ARG, "null argument");
+    int ndev = 0;
+    if (cudaGetDeviceCount(&ndev) != cudaSuccess || device < 0 || device >= ndev)
+        return fail(CFDG_ERR_CUDA, "no such CUDA device");
+    CK(cudaSetDevice(device));
+    int nsm = 0;
+    CK(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, device));
+    const int blocks = 4 * nsm, threads = 256, iters = 16384;
+    cudaStream_t st = nullptr;
+    cudaEvent_t e0 = nullptr, e1 = nullptr;
+    double* sink = nullptr;
+    cfdg_status rc = CFDG_OK;
+    float ms = 0;
+    if (cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking) != cudaSuccess || cudaEventCreate(&e0) != cudaSuccess ||
+        cudaEventCreate(&e1) != cudaSuccess || cudaMalloc((void**)&sink, sizeof(double)) != cudaSuccess) {
+        rc = fail(CFDG_ERR_CUDA, "cfdg_fp64_pipe_rate: set-up failed");
+    } else {
+        launch_fp64_fma_stream(blocks, threads, sink, iters / 8, st);  // warm-up
+        cudaEventRecord(e0, st);
+        launch_fp64_fma_stream(blocks, threads, sink, iters, st);
+        cudaEventRecord(e1, st);
+        cudaError_t e = cudaStreamSynchronize(st);
+        if (e == cudaSuccess) e = cudaEventElapsedTime(&ms, e0, e1);
+        if (e != cudaSuccess || ms <= 0) rc = fail(CFDG_ERR_CUDA, std::string("cfdg_fp64_pipe_rate: ") + cudaGetErrorString(e));
+    }
+    if (rc == CFDG_OK) *fma_per_s = (double)blocks * threads * iters * FP64_STREAM_CHAINS / (ms * 1e-3);
+    if (sink) cudaFree(sink);
+    if (e0) cudaEventDestroy(e0);
+    if (e1) cudaEventDestroy(e1);
+    if (st) cudaStreamDestroy(st);
+    return rc;
 }
 
 cfdg_status cfdg_launch_count(cfdg_solver* s, long long* n) {

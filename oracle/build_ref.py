@@ -16,7 +16,13 @@ term replace that index by the owner, which makes the non-orthogonal correction
 vanish (dist2 = 0) on those faces; the CPU restatement and the CUDA kernels define
 the same behaviour.
 
-Usage: python oracle/build_ref.py [--src /root/reference]
+Where the reference checkout is: ``--src``, else the CFD_REFERENCE environment variable,
+else the read-only checkout this recipe was written against (REFERENCE_CHECKOUT); this
+file is the only one that names that location.  Where none exists (e.g. on a machine
+that has only this repository) nothing is built and the tests that need these objects
+skip; the committed fixtures under tests/golden/ still pin the restatement.
+
+Usage: python oracle/build_ref.py [--src PATH]
 """
 from __future__ import annotations
 
@@ -29,6 +35,15 @@ import tempfile
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 OUT = os.path.join(HERE, "_ref")
+REFERENCE_CHECKOUT = "/root/reference"
+
+
+def reference_source():
+    """The reference checkout to build from, or None when there is none here."""
+    for cand in (os.environ.get("CFD_REFERENCE"), REFERENCE_CHECKOUT):
+        if cand and os.path.isdir(os.path.join(cand, "src")):
+            return cand
+    return None
 
 # (first line, last line) ranges of src/Solver.cpp, 1-based inclusive
 ACTIVE_INIT = (46, 65)
@@ -137,9 +152,12 @@ def _wait(item):
 
 def main(argv=None):
     ap = argparse.ArgumentParser()
-    ap.add_argument("--src", default="/root/reference")
+    ap.add_argument("--src", default=None)
     a = ap.parse_args(argv)
-    for so in build(a.src):
+    src = a.src or reference_source()
+    if src is None:
+        raise SystemExit("no reference checkout: pass --src or set CFD_REFERENCE")
+    for so in build(src):
         print(so)
 
 

@@ -342,6 +342,9 @@ typedef struct {
     int gmres_m;
     double gmres_tol;
     double cfl0;
+    int freeze_step;    /* the limiter freezes when step > freeze_step or CFL > freeze_cfl */
+    double freeze_cfl;
+    double stop_rho;    /* solveImplicit also stops when the density residual is below this */
 } om_solver;
 
 enum { GR_RHO = 0, GR_U = 2, GR_V = 4, GR_P = 6, GR_T = 8 };
@@ -360,6 +363,9 @@ om_solver* om_solver_create(const om_mesh* m) {
     s->gmres_m = 40;          /* src/Solver.cpp:1479 */
     s->gmres_tol = 1e-2;      /* src/Solver.cpp:1587 */
     s->cfl0 = 0.1;            /* src/Solver.cpp:1700 */
+    s->freeze_step = 150;     /* src/Solver.cpp:1714 */
+    s->freeze_cfl = 10.0;
+    s->stop_rho = 0.0;
     int n = m->n_cells;
     s->grad = (double*)calloc((size_t)10 * n, sizeof(double));
     s->phi = (double*)malloc(sizeof(double) * n);
@@ -386,6 +392,15 @@ void om_set_gmres(om_solver* s, int m, double tol) { s->gmres_m = m; s->gmres_to
 void om_set_nu(om_solver* s, double nu) { s->nu = nu; }
 /* the first pseudo-time CFL of solveImplicit (the reference hard-codes 0.1) */
 void om_set_cfl0(om_solver* s, double cfl0) { s->cfl0 = cfl0; }
+/* the limiter-freeze rule of solveImplicit (the reference hard-codes step > 150 ||
+ * CFL > 10, src/Solver.cpp:1714); freeze_step = -1 keeps the current limiter throughout */
+void om_set_freeze(om_solver* s, int freeze_step, double freeze_cfl) {
+    s->freeze_step = freeze_step;
+    s->freeze_cfl = freeze_cfl;
+}
+/* an extra stop of solveImplicit: the volume-weighted density residual below stop_rho
+ * (0 = off; the reference stops on the all-component norm only) */
+void om_set_stop_rho(om_solver* s, double stop_rho) { s->stop_rho = stop_rho; }
 
 /* setFlowConditions (src/Solver.cpp:12-32) */
 void om_set_flow_conditions(om_solver* s, double M, double P, double T) {
@@ -732,6 +747,19 @@ double om_dot(int n, const double* a, const double* b) {
     }
     return sum;
 }
+/* the density component of norm_L2_VolumeWeighted: sqrt(sum (R_rho / V)^2 V / sum V) */
+double om_norm_vm_rho(const om_solver* s, const double* R) {
+    double sq = 0.0, tv = 0.0;
+    for (int i = 0; i < s->m->n_cells; ++i) {
+        double v = s->m->vol[i];
+        double a = R[NV * i] / v;
+        sq += a * a * v;
+        tv += v;
+    }
+    if (tv == 0) return 0.0;
+    return sqrt(sq / tv);
+}
+
 double om_norm_vm(const om_solver* s, const double* R) {
     double sq = 0.0, tv = 0.0;
     for (int i = 0; i < s->m->n_cells; ++i) {
@@ -972,7 +1000,7 @@ void om_solve_unsteady(om_solver* s, double dt_phy, int n_steps, int* newton, do
  * step, the volume-weighted and plain residual norms, the CFL and the GMRES count;
  * returns the number of steps logged. */
 int om_solve_implicit(om_solver* s, double tol, int max_steps, double* res_vm, double* res_abs,
-                      double* cfl_out, int* iters_out) {
+                      double* cfl_out, int* iters_out, double* res_rho) {
     int n = s->m->n_cells;
     size_t len = (size_t)NV * n;
     double g = s->gamma;
@@ -984,13 +1012,16 @@ int om_solve_implicit(om_solver* s, double tol, int max_steps, double* res_vm, d
     for (int step = 0; step < max_steps; ++step) {
         om_local_timestep(s, CFL);
         int upd = 1;
-        if (step > 150 || CFL > 10.0) upd = 0;
+        if (step > s->freeze_step || CFL > s->freeze_cfl) upd = 0;
         om_residual(s, s->U, R, upd);
         double rvm = om_norm_vm(s, R);
         double rn = om_norm(n, R);
+        double rrho = om_norm_vm_rho(s, R);
         res_vm[step] = rvm; res_abs[step] = rn; cfl_out[step] = CFL; iters_out[step] = 0;
+        if (res_rho) res_rho[step] = rrho;
         logged = step + 1;
         if (rvm < tol) break;
+        if (s->stop_rho > 0.0 && rrho <= s->stop_rho && step > 5) break;
         for (int i = 0; i < n; ++i) st_store(rhs + NV * i, st_mul(st_load(R + NV * i), -1.0));
         int it = om_gmres(s, s->U, R, rhs, dU);
         iters_out[step] = it;

@@ -92,7 +92,10 @@ def _oracle_lib():
             "om_preconditioner": (None, [vp, _dp]),
             "om_apply_jacobian": (None, [vp, _dp, _dp, _dp, _dp]),
             "om_gmres": (C.c_int, [vp, _dp, _dp, _dp, _dp]),
-            "om_solve_implicit": (C.c_int, [vp, C.c_double, C.c_int, _dp, _dp, _dp, _ip]),
+            "om_solve_implicit": (C.c_int, [vp, C.c_double, C.c_int, _dp, _dp, _dp, _ip, _dp]),
+            "om_set_freeze": (None, [vp, C.c_int, C.c_double]),
+            "om_set_stop_rho": (None, [vp, C.c_double]),
+            "om_norm_vm_rho": (C.c_double, [vp, _dp]),
             "om_drag": (C.c_double, [vp]),
             "om_entropy_error": (C.c_double, [vp]),
             "om_residual_sst": (None, [vp, _dp, _dp, C.c_double, C.c_double]),
@@ -265,10 +268,22 @@ class OracleSolver(_Base):
         return self._L.om_norm_vm(self._s, np.ascontiguousarray(R, np.float64).ravel())
 
     def solveImplicit(self, tol, max_steps):
-        a, b, c = np.zeros(max_steps), np.zeros(max_steps), np.zeros(max_steps)
+        a, b, c, d = np.zeros(max_steps), np.zeros(max_steps), np.zeros(max_steps), np.zeros(max_steps)
         it = np.zeros(max_steps, np.int32)
-        n = self._L.om_solve_implicit(self._s, float(tol), int(max_steps), a, b, c, it)
-        return {"res_vm": a[:n], "res_abs": b[:n], "cfl": c[:n], "gmres_iters": it[:n]}
+        n = self._L.om_solve_implicit(self._s, float(tol), int(max_steps), a, b, c, it, d)
+        return {"res_vm": a[:n], "res_abs": b[:n], "cfl": c[:n], "gmres_iters": it[:n], "res_rho": d[:n]}
+
+    def setLimiterFreeze(self, step, cfl=10.0):
+        """The limiter-freeze rule (reference: step > 150 or CFL > 10); step = -1 keeps the
+        current limiter for the whole solve."""
+        self._L.om_set_freeze(self._s, int(step), float(cfl))
+
+    def setStopRho(self, tol):
+        """Also stop solveImplicit once the density residual is at or below tol (0 = off)."""
+        self._L.om_set_stop_rho(self._s, float(tol))
+
+    def norm_vm_rho(self, R):
+        return self._L.om_norm_vm_rho(self._s, np.ascontiguousarray(R, np.float64).ravel())
 
     def drag(self):
         return self._L.om_drag(self._s)

@@ -34,7 +34,9 @@ from mycode_gb300 import meshgen as mg  # noqa: E402
 from oracle.oracle import RefSolver, ref_variant  # noqa: E402
 import cases as C  # noqa: E402
 
-REF_SRC = os.environ.get("CFD_REFERENCE", "/root/reference")
+from oracle.build_ref import reference_source  # noqa: E402
+
+REF_SRC = reference_source()
 
 
 def gen_cases():
@@ -133,6 +135,8 @@ def parse_vtk_cell_scalars(path):
 
 
 if __name__ == "__main__":
+    if REF_SRC is None:
+        raise SystemExit("no reference checkout: set CFD_REFERENCE (see oracle/build_ref.py)")
     gen_cases()
     gen_bump()
     for f in sorted(os.listdir(HERE)):
