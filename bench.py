@@ -646,60 +646,102 @@ def other_configs(api, steps=20, warmup=3):
     return out
 
 
+def _golden(name):
+    """A converged FP64 CPU-oracle solution (tests/golden/make_converged.py) and its mesh."""
+    import numpy as np
+    from mycode_gb300 import meshgen
+    d = np.load(os.path.join(ROOT, "tests", "golden", name))
+    return d, meshgen.MeshSpec(str(d["name"]), d["nodes"], d["cells"], d["bedges"])
+
+
+def _solve_to(s, max_steps, tol_rho=1e-10):
+    """Newton steps from the current state until the density residual is at or below
+    tol_rho (after step 5): wall time, steps, GMRES iterations."""
+    s.synchronize()
+    t0 = time.perf_counter()
+    n, reached, its, rec = 0, False, 0, None
+    while n < max_steps:
+        rec, _ = s.newton_step(0.0)
+        n += 1
+        its += rec.gmres_iters
+        if rec.res_rho <= tol_rho and n > 5:
+            reached = True
+            break
+    s.synchronize()
+    return {"seconds": round(time.perf_counter() - t0, 4), "newton_steps": n, "gmres_iters": its,
+            "reached": reached, "final_res_rho": rec.res_rho}
+
+
 def time_to_converge(api, max_steps=1500):
     """Wall time of full solves from the free stream to a volume-weighted density residual
-    of 1e-10: the wedge 120 x 80 x 2 triangles (19,200 cells, 10 % jitter), M 2.5, HLLC with
-    the Barth-Jespersen limiter, GMRES(30), CFL from 10, for the mixed path (FP32 Krylov and
-    exact J v, FP64 residual and update), the FP64 path with exact J v and the FP64 path
-    with the reference's FD J v.  Also the relative L2 difference of the converged states and
-    of their wall pressure coefficients (the slip wall, tag 3).  The limited scheme freezes
-    its limiter early (src/Solver.cpp:1714), at slightly different values in each run, so
-    its converged states solve slightly different discrete problems; the first-order pair
-    (same wedge, no limiter) shows the mixed path converging to the FP64 solution itself."""
-    from mycode_gb300 import meshgen
+    of 1e-10, mixed precision (FP32 Krylov basis and exact J v, FP64 residual and update)
+    against the FP64 paths, with the errors of the converged solutions against the FP64
+    CPU oracle's converged solution (tests/golden/, made by tests/golden/make_converged.py
+    and checked bit for bit against the compiled reference):
+      wedge   120 x 80 x 2 (19,200 cells, 10 % jitter), M 2.5, HLLC + BJ limiter, GMRES(30),
+              first CFL 10.  The reference freezes its limiter at the state step 7 reached
+              (src/Solver.cpp:1714); every run here keeps the oracle's frozen limiter from the
+              start, so all of them solve the oracle's discrete problem.  Error: the wall Cp
+              (slip wall, tag 3) and the state.
+      plate   the laminar flat plate 60 x 30 (Roe + viscous, central, the reference's
+              GMRES(40) and first CFL 0.1).  Error: wall Cf and Cp (tag 4) and the state.
+    Also the first-order wedge pair (no limiter) against each other."""
     import numpy as np
-    mesh = api.Mesh.from_spec(meshgen.wedge(120, 80, jitter=0.10, seed=0))
+    dw, spec_w = _golden("wedge_converged.npz")
+    mesh_w = api.Mesh.from_spec(spec_w)
 
-    def solve(prec, jv, spatial):
-        s = api.Solver(mesh, bcset="supersonic", init="freestream", viscous=0, precision=prec, jv=jv, gmres_m=30,
-                       cfl0=10.0, flux="HLLC", spatial=spatial)
+    def wedge(prec, jv, spatial="SECOND_ORDER_LIMITED"):
+        limited = spatial == "SECOND_ORDER_LIMITED"
+        s = api.Solver(mesh_w, bcset="supersonic", init="freestream", viscous=0, precision=prec, jv=jv, gmres_m=30,
+                       cfl0=10.0, flux="HLLC", spatial=spatial, limiter_freeze_step=-1 if limited else 150)
         s.setFlowConditions(2.5, 101325.0, 300.0)
         s.initialize()
-        s.synchronize()
-        t0 = time.perf_counter()
-        n, reached, its = 0, False, 0
-        while n < max_steps:
-            rec, _ = s.newton_step(0.0)
-            n += 1
-            its += rec.gmres_iters
-            if rec.res_rho <= 1e-10 and n > 5:
-                reached = True
-                break
-        s.synchronize()
-        t = time.perf_counter() - t0
-        res = {"seconds": round(t, 4), "newton_steps": n, "gmres_iters": its, "reached": reached,
-               "final_res_rho": rec.res_rho}
-        U, cp = s.getSolution(), s.wall_coefficients(3)[1]
+        if limited:
+            s.set_limiters(dw["phi"])
+        res = _solve_to(s, max_steps)
+        U, cp = s.getSolution()[:, :4], s.wall_coefficients(3)[1]
         s.close()
         return res, U, cp
 
-    out, states, cps = {}, {}, {}
+    out = {"workload": "supersonic wedge 120x80x2 (19,200 cells), M 2.5, HLLC + BJ limiter (the FP64 oracle's frozen "
+                       "limiter in every run), GMRES(30), first CFL 10"}
     for name, prec, jv in (("mixed", "mixed", "exact"), ("fp64_exact", "fp64", "exact"), ("fp64_fd", "fp64", "fd")):
-        out[name], states[name], cps[name] = solve(prec, jv, "SECOND_ORDER_LIMITED")
-    ref = states["fp64_fd"]
-    for name in ("mixed", "fp64_exact"):
-        out[name]["state_rel_l2_vs_fp64_fd"] = float(np.linalg.norm(states[name] - ref) / np.linalg.norm(ref))
-        out[name]["wall_cp_max_abs_diff_vs_fp64_fd"] = float(np.abs(cps[name] - cps["fp64_fd"]).max())
+        r, U, cp = wedge(prec, jv)
+        r["state_rel_l2_vs_fp64_oracle"] = float(np.linalg.norm(U - dw["U"]) / np.linalg.norm(dw["U"]))
+        r["wall_cp_max_abs_diff_vs_fp64_oracle"] = float(np.abs(cp - dw["cp_wall"]).max())
+        out[name] = r
+    out["oracle_steps_to_1e-10"] = int(dw["n_reach"])
     out["speedup_mixed_vs_fp64_fd"] = out["fp64_fd"]["seconds"] / out["mixed"]["seconds"]
     out["speedup_mixed_vs_fp64_exact"] = out["fp64_exact"]["seconds"] / out["mixed"]["seconds"]
-    out["workload"] = "supersonic wedge 120x80x2 (19,200 cells), M 2.5, HLLC + BJ limiter, GMRES(30), CFL0 10"
-    m1, Um, cpm = solve("mixed", "exact", "FIRST_ORDER")
-    f1, Uf, cpf = solve("fp64", "exact", "FIRST_ORDER")
+
+    dp, spec_p = _golden("plate_converged.npz")
+    mesh_p = api.Mesh.from_spec(spec_p)
+    plate = {"workload": "laminar flat plate 60x30 quads (1,800 cells), stretching 1.08, M 0.2, Re_L 1e5, Roe + "
+                         "viscous, 2nd-order central, GMRES(40), first CFL 0.1",
+             "oracle_steps_to_1e-10": int(dp["n_reach"])}
+    for name, prec, jv in (("mixed", "mixed", "exact"), ("fp64_fd", "fp64", "fd")):
+        s = api.Solver(mesh_p, bcset="plate", init="freestream", viscous=1, precision=prec, jv=jv, flux="ROE",
+                       spatial="SECOND_ORDER_CENTRAL")
+        s.setFreestreamStatic(0.2, 101325.0, 300.0)
+        s.setKinematicViscosity(1e5, 1.0)
+        s.initialize()
+        r = _solve_to(s, 4 * max_steps)
+        _, cp, cf = s.wall_coefficients(4)
+        U = s.getSolution()[:, :4]
+        s.close()
+        r["state_rel_l2_vs_fp64_oracle"] = float(np.linalg.norm(U - dp["U"]) / np.linalg.norm(dp["U"]))
+        r["wall_cf_max_abs_diff_vs_fp64_oracle"] = float(np.abs(cf - dp["cf_wall"]).max())
+        r["wall_cp_max_abs_diff_vs_fp64_oracle"] = float(np.abs(cp - dp["cp_wall"]).max())
+        plate[name] = r
+    plate["speedup_mixed_vs_fp64_fd"] = plate["fp64_fd"]["seconds"] / plate["mixed"]["seconds"]
+    out["laminar_plate"] = plate
+
+    m1, Um, cpm = wedge("mixed", "exact", "FIRST_ORDER")
+    f1, Uf, cpf = wedge("fp64", "exact", "FIRST_ORDER")
     out["first_order"] = {
         "mixed": m1, "fp64_exact": f1, "speedup_mixed_vs_fp64_exact": f1["seconds"] / m1["seconds"],
         "state_rel_l2_mixed_vs_fp64": float(np.linalg.norm(Um - Uf) / np.linalg.norm(Uf)),
         "wall_cp_max_abs_diff_mixed_vs_fp64": float(np.abs(cpm - cpf).max()),
-        "wall_cp_range": [float(cpf.min()), float(cpf.max())],
         "workload": "the same wedge, HLLC first order (no limiter), to a density residual of 1e-10"}
     return out
 

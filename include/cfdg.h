@@ -104,6 +104,10 @@ typedef struct cfdg_config {
     /* persistent Arnoldi kernel: polls of a grid barrier before the wait gives up and the
      * solve reports CFDG_ERR_TIMEOUT (0 = the default, 2^24 polls, seconds in all) */
     int barrier_poll_limit;
+    /* graph driver: cfdg_solve_implicit runs its Newton steps in chains of this many, one
+     * host synchronisation per chain (the CFL control on the device between the steps;
+     * the same trace for any value); 1 = one synchronisation per step.  Default 8. */
+    int newton_chain;
 } cfdg_config;
 
 /* CFDG_KRYLOV_STREAM launches the graph driver's kernels one iteration at a time from a
@@ -223,6 +227,14 @@ cfdg_status cfdg_solve_implicit(cfdg_solver* s, double tol, int max_steps, cfdg_
 /* one pseudo-transient Newton step of solveImplicit; *converged set when the
  * step's residual was already below tol (no update made) */
 cfdg_status cfdg_newton_step(cfdg_solver* s, double tol, cfdg_step* info, int* converged);
+/* k steps of solveImplicit from the driver's current CFL and step counter.  With the graph
+ * driver they are enqueued back to back with one host synchronisation per 64 steps: the
+ * reference's CFL control (src/Solver.cpp:1747-1750, :1780-1796) and limiter-freeze
+ * decision (:1714) run on the device between the steps, with the same arithmetic and the
+ * same trace as k single steps.  Stops at convergence (*converged set: that step's
+ * residual was below tol and no update was made) or an error.  trace (may be NULL) gets
+ * the records of the steps taken, *n_done their count. */
+cfdg_status cfdg_newton_steps(cfdg_solver* s, double tol, int k, cfdg_step* trace, int* n_done, int* converged);
 /* switch the Krylov driver (CFDG_KRYLOV_HOST or CFDG_KRYLOV_GRAPH) between solves */
 cfdg_status cfdg_set_krylov(cfdg_solver* s, int mode);
 /* Newton driver state (CFL, step counter) */

@@ -47,7 +47,7 @@ class Config(C.Structure):
         ("limiter_freeze_step", C.c_int), ("limiter_freeze_cfl", C.c_double),
         ("turb_intensity", C.c_double), ("mut_ratio", C.c_double), ("shock_deflection_deg", C.c_double),
         ("renumber", C.c_int), ("device", C.c_int), ("krylov", C.c_int), ("persistent", C.c_int), ("pdl", C.c_int),
-        ("barrier_poll_limit", C.c_int),
+        ("barrier_poll_limit", C.c_int), ("newton_chain", C.c_int),
     ]
 
 
@@ -102,6 +102,7 @@ SIGNATURES = {
     "cfdg_norm_vm": (C.c_int, [_vp, _dp, C.POINTER(C.c_double)]),
     "cfdg_solve_implicit": (C.c_int, [_vp, C.c_double, C.c_int, C.POINTER(Step), C.POINTER(C.c_int)]),
     "cfdg_newton_step": (C.c_int, [_vp, C.c_double, C.POINTER(Step), C.POINTER(C.c_int)]),
+    "cfdg_newton_steps": (C.c_int, [_vp, C.c_double, C.c_int, C.c_void_p, C.POINTER(C.c_int), C.POINTER(C.c_int)]),
     "cfdg_reset_newton": (C.c_int, [_vp]),
     "cfdg_get_newton_state": (C.c_int, [_vp, C.POINTER(C.c_double), C.POINTER(C.c_int)]),
     "cfdg_set_newton_state": (C.c_int, [_vp, C.c_double, C.c_int]),
@@ -434,6 +435,14 @@ class Solver:
         cv = C.c_int(0)
         _check(lib().cfdg_newton_step(self._h, float(tol), C.byref(s), C.byref(cv)))
         return s, bool(cv.value)
+
+    def newton_steps(self, k, tol=0.0):
+        """k Newton steps enqueued back to back (graph driver: one host synchronisation);
+        returns (records of the steps taken, converged)."""
+        tr = (Step * max(int(k), 1))()
+        n, cv = C.c_int(0), C.c_int(0)
+        _check(lib().cfdg_newton_steps(self._h, float(tol), int(k), C.cast(tr, C.c_void_p), C.byref(n), C.byref(cv)))
+        return list(tr[: n.value]), bool(cv.value)
 
     def set_krylov(self, mode):
         _check(lib().cfdg_set_krylov(self._h, {"host": 0, "graph": 1, "stream": 2}.get(mode, mode)))

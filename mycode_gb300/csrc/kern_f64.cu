@@ -10,7 +10,8 @@ static void residual_nv(const ResArgs<double>& a) {
     if (a.ev) cudaEventRecord(a.ev[0], a.stream);
     k_prim<double, NV><<<blocks_for(nc), tpb_for(nc), 0, a.stream>>>((int)nc, a.F, a.U, a.W);
     if (a.ev) cudaEventRecord(a.ev[1], a.stream);
-    k_grad<double, NV><<<blocks_for(nc), tpb_for(nc), 0, a.stream>>>(a.m, a.F, a.U, a.W, a.G, a.phi, a.do_limiter, nullptr);
+    k_grad<double, NV><<<blocks_for(nc), tpb_for(nc), 0, a.stream>>>(a.m, a.F, a.U, a.W, a.G, a.phi, a.do_limiter, nullptr,
+                                                                    a.lim_dev);
     if (NV == 6) k_sst_cell<double, NV><<<blocks_for(nc), tpb_for(nc), 0, a.stream>>>(a.m, a.F, a.W, a.G, a.dwall, a.T, nullptr);
     if (a.ev) cudaEventRecord(a.ev[2], a.stream);
     k_flux<double, NV><<<blocks_for(nf), tpb_for(nf), 0, a.stream>>>(a.m, a.F, a.U, a.W, a.G, a.phi, a.FA, a.T, nullptr);
@@ -91,8 +92,13 @@ void launch_step_norms(int nv, long nc, const double* R, const double* vol, doub
     NV_SWITCH(nv, (k_step_norms<NVC><<<red_grid(nc), RED_THREADS, 0, s>>>(nc, R, vol, rhs, rs, out4, flag)));
 }
 void launch_local_dt(int nv, const MeshView<double>& m, const Flow<double>& F, const double* U, const double* W,
-                     double cfl, double* dt, cudaStream_t s) {
-    NV_SWITCH(nv, (k_local_dt<NVC><<<blocks_for(m.nc), tpb_for(m.nc), 0, s>>>(m, F, U, W, cfl, dt)));
+                     double cfl, double* dt, cudaStream_t s, const double* cfl_dev) {
+    NV_SWITCH(nv, (k_local_dt<NVC><<<blocks_for(m.nc), tpb_for(m.nc), 0, s>>>(m, F, U, W, cfl, dt, cfl_dev)));
+}
+void launch_newton_update_chain(int nv, long nc, double* U, const double* dU, const double* norms, double tol,
+                                double gam, double wmin, int* bad, const NewtonCtl& c, int k, cudaStream_t s) {
+    NV_SWITCH(nv, (k_newton_update_chain<NVC><<<blocks_for(nc), tpb_for(nc), 0, s>>>(nc, U, dU, norms, tol, gam, wmin,
+                                                                                     bad, c, k)));
 }
 void launch_precond(int nv, const MeshView<double>& m, const Flow<double>& F, const double* U, const double* W,
                     const double* dt, double* D, const double* mut, cudaStream_t s) {

@@ -69,6 +69,8 @@ struct GmresDev {
     int nb1;          // blocks of the gather kernel that writes them (exact J v body; set at launch)
     unsigned* counter;
     int in_graph;     // 1: the kernels run inside the WHILE graph and set its condition
+    const int* skip;  // optional: when *skip is set the solve is empty (x = 0, no iteration):
+                      // a chained Newton step after the chain stopped
 };
 
 // Arithmetic of the vector kernels.  On GB300 every FP64 warp instruction occupies its
@@ -212,6 +214,7 @@ __global__ void k_gmres_start(long n, T* V0, const double* rhs, GmresDev d, int 
     __shared__ double ib;
     const double b2 = bsq ? *bsq : d.beta[2];
     const double b = sqrt(b2);
+    const bool empty = b < 1e-12 || (d.skip && *d.skip);
     if (blockIdx.x == 0) {
         for (int i = threadIdx.x; i <= m; i += blockDim.x) {
             d.g[i] = i == 0 ? b : 0.0;
@@ -231,7 +234,7 @@ __global__ void k_gmres_start(long n, T* V0, const double* rhs, GmresDev d, int 
             d.gi[5] = 0;
             d.sig[0] = 1.0;
             d.ilam[0] = 1.0;
-            if (b < 1e-12) {
+            if (empty) {
                 d.gi[1] = -1;
                 d.gi[2] = 1;
                 if (d.in_graph) cudaGraphSetConditional(h, 0);
@@ -241,7 +244,7 @@ __global__ void k_gmres_start(long n, T* V0, const double* rhs, GmresDev d, int 
             }
         }
     }
-    if (b < 1e-12) return;
+    if (empty) return;
     if (threadIdx.x == 0) ib = 1.0 / b;
     __syncthreads();
     for (long q = (long)blockIdx.x * blockDim.x + threadIdx.x; q < n; q += (long)gridDim.x * blockDim.x)

@@ -27,6 +27,7 @@ struct ResArgs {
     const R* dwall = nullptr;         // wall distance per cell; nv = 6 only
     bool pdl = false;                 // launch_jv_mid: programmatic dependent launch (pdl.cuh)
     const int* done = nullptr;        // launch_jv_mid: skip when *done (a finished Krylov solve)
+    const int* lim_dev = nullptr;     // launch_residual<double>: the limiter also needs *lim_dev
     // launch_residual<double> of a Newton step: the gather fused with the step's reductions
     // (k_gather_norms) when norms_out is set
     double* rhs_out = nullptr;
@@ -95,8 +96,9 @@ void launch_mixed_pre(int nv, const MeshView<float>& m, const Flow<float>& F, co
                       const double* W,
                       const double* phi, const double* mut, const double* cfl, const double* dt_in, float* U32,
                       float* phi32, float* dt32, double* D, float* Dinv32, cudaStream_t s);
+// cfl_dev (optional): the CFL number from device memory instead of cfl
 void launch_local_dt(int nv, const MeshView<double>& m, const Flow<double>& F, const double* U, const double* W,
-                     double cfl, double* dt, cudaStream_t s);
+                     double cfl, double* dt, cudaStream_t s, const double* cfl_dev = nullptr);
 // D: one plane per cell, three with SST (mean flow, k, w); mut: SST eddy viscosity or null
 void launch_precond(int nv, const MeshView<double>& m, const Flow<double>& F, const double* U, const double* W,
                     const double* dt, double* D, const double* mut, cudaStream_t s);
@@ -105,6 +107,9 @@ void launch_newton_update(int nv, long nc, double* U, const double* dU, double r
 // the Newton update with its decisions (converged / non-finite / relaxation) on the device
 void launch_newton_update_dev(int nv, long nc, double* U, const double* dU, const double* norms, double tol, double gam,
                               double wmin, int* bad, cudaStream_t s);
+// the same update plus the step's scalar control on the device (step k of a chain)
+void launch_newton_update_chain(int nv, long nc, double* U, const double* dU, const double* norms, double tol,
+                                double gam, double wmin, int* bad, const NewtonCtl& c, int k, cudaStream_t s);
 // time stepping: timeStepExplicit's update, solveUnsteady's right-hand side and update
 void launch_explicit_update(int nv, long nc, double* U, const double* R, const double* vol, double dt, int* bad,
                             cudaStream_t s);

@@ -390,12 +390,15 @@ __global__ void __launch_bounds__(256) k_mixed_pre(MeshView<float> m, Flow<float
 
 // computeLocalTimeStep (src/Solver.cpp:1388-1422) as a per-cell gather: each face
 // adds (|u_n| + c) A from the cell's own state, owner and neighbour with their own
-// expressions, summed in reference face order from 1e-12.
+// expressions, summed in reference face order from 1e-12.  cfl_dev (optional): the CFL
+// number from device memory (a Newton step whose CFL control ran on the device).
 template <int NV>
 __global__ void k_local_dt(MeshView<double> m, Flow<double> F, const double* __restrict__ U,
-                           const double* __restrict__ W, double cfl, double* __restrict__ dt) {
+                           const double* __restrict__ W, double cfl, double* __restrict__ dt,
+                           const double* __restrict__ cfl_dev) {
     long i = (long)blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= m.nc) return;
+    if (cfl_dev) cfl = *cfl_dev;
     long nc = m.nc;
     double r = U[i], ru = U[nc + i], rv = U[2 * nc + i];
     double p = W[3 * nc + i];
@@ -523,6 +526,111 @@ __global__ void k_newton_update_dev(long nc, double* __restrict__ U, const doubl
     for (int c = 0; c < NV; ++c) {
         ok = ok && isfinite(u[c]);
         U[c * nc + i] = u[c];
+    }
+    if (!ok) atomicOr(bad, 1);
+}
+
+// The scalar control of a Newton step on the device, so that steps can follow one
+// another without the host: the step's record, then (not converged, residual finite) the
+// reference's CFL control (src/Solver.cpp:1747-1750, :1780-1796), the step counter and the
+// next step's limiter-freeze decision (src/Solver.cpp:1714).  The same expressions in the
+// same order as the host driver, so the trace is the same bit for bit.
+struct NewtonCtl {
+    int* ctl;        // [0] step, [1] stop (0 running, 1 converged, 2 non-finite residual),
+                     // [2] the current step recomputes the limiter
+    double* cfl;     // the CFL number (the next step's local time step reads it)
+    double* rec;     // NEWTON_REC doubles per step of the chain
+    const int* gi;   // the GMRES solve's ints: gi[1] = its last iteration
+    int freeze_step;
+    double freeze_cfl, cfl_max;
+    int limited;     // second-order limited scheme
+};
+// record: res_vm, res_abs, res_rho, CFL used, GMRES iterations of the step's solve,
+// limiter recomputed, outcome (0 updated, 1 converged, 2 non-finite residual, 3 not taken:
+// an earlier step of the chain stopped), step index
+constexpr int NEWTON_REC = 8;
+
+__device__ __forceinline__ void newton_control(const NewtonCtl& c, const double* norms, double tol, int k) {
+    const double s0 = norms[0], s1 = norms[1];
+    const double resVM = s1 == 0 ? 0.0 : sqrt(s0 / s1);
+    double* r = c.rec + (long)NEWTON_REC * k;
+    const double cfl = *c.cfl;
+    const int step = c.ctl[0];
+    const int it = c.gi[1] + 1;
+    r[0] = resVM;
+    r[1] = sqrt(norms[3]);
+    r[2] = s1 == 0 ? 0.0 : sqrt(norms[2] / s1);
+    r[3] = cfl;
+    r[4] = it;
+    r[5] = c.ctl[2];
+    r[7] = step;
+    if (c.ctl[1]) {
+        r[6] = 3.0;
+        return;
+    }
+    if (!isfinite(resVM)) {
+        c.ctl[1] = 2;
+        r[6] = 2.0;
+        return;
+    }
+    if (resVM < tol) {
+        c.ctl[1] = 1;
+        r[6] = 1.0;
+        return;
+    }
+    r[6] = 0.0;
+    double cf = cfl;
+    if (it >= 29) {
+        cf *= 0.5;
+        if (cf < 0.05) cf = 0.05;
+    }
+    if (step > 5) {
+        if (resVM > 1e6) cf *= 1.2;
+        else cf *= 1.5;
+        if (it >= 25) cf *= 0.5;
+        if (cf > c.cfl_max) cf = c.cfl_max;
+        if (cf < 0.1) cf = 0.1;
+    }
+    *c.cfl = cf;
+    c.ctl[0] = step + 1;
+    c.ctl[2] = (c.limited && !((step + 1) > c.freeze_step || cf > c.freeze_cfl)) ? 1 : 0;
+}
+
+// k_newton_update_dev's update plus the scalar control in thread 0 of block 0 (chain
+// step k).  The other threads take their converged / non-finite / relaxation decisions
+// from the same norms, so a step after a stop changes nothing.
+template <int NV>
+__global__ void k_newton_update_chain(long nc, double* __restrict__ U, const double* __restrict__ dU,
+                                      const double* __restrict__ norms, double tol, double gam, double wmin, int* bad,
+                                      NewtonCtl c, int k) {
+    long i = (long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i == 0) newton_control(c, norms, tol, k);
+    if (i >= nc) return;
+    const double s0 = norms[0], s1 = norms[1];
+    const double resVM = s1 == 0 ? 0.0 : sqrt(s0 / s1);
+    if (!(resVM >= tol) || !isfinite(resVM)) return;
+    double relax = 1.0;
+    if (resVM > 1e6) relax = 0.5;
+    else if (resVM > 2e3 && resVM < 1e2) relax = 0.9;
+    double u[NV];
+#pragma unroll
+    for (int cc = 0; cc < NV; ++cc) u[cc] = U[cc * nc + i] + dU[cc * nc + i] * relax;
+    double ke = 0.5 * (u[1] * u[1] + u[2] * u[2]) / (u[0] + 1e-12);
+    double pn = (gam - 1.0) * (u[3] - ke);
+    if (u[0] < 1e-5) u[0] = 1e-5;
+    if (pn < 1e-5) {
+        pn = 1e-5;
+        u[3] = pn / (gam - 1.0) + ke;
+    }
+    if constexpr (NV == 6) {
+        if (u[4] < 0.0) u[4] = 0.0;
+        if (u[5] < u[0] * wmin) u[5] = u[0] * wmin;
+    }
+    bool ok = true;
+#pragma unroll
+    for (int cc = 0; cc < NV; ++cc) {
+        ok = ok && isfinite(u[cc]);
+        U[cc * nc + i] = u[cc];
     }
     if (!ok) atomicOr(bad, 1);
 }

@@ -255,11 +255,14 @@ __device__ __forceinline__ void grad_item(const MeshView<R>& m, const Flow<R>& F
     phi[i] = lim;
 }
 
+// lim_dev (optional): the limiter is recomputed only when *lim_dev is also set (a Newton
+// step whose limiter-freeze decision was taken on the device)
 template <class S, int NV, class R>
 __global__ void __launch_bounds__(256) k_grad(MeshView<R> m, Flow<R> F, Field<R> U, Field<R> W, Field<R> G,
-                                              R* phi, int do_limiter, const int* done) {
+                                              R* phi, int do_limiter, const int* done, const int* lim_dev) {
     long i = (long)blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= m.nc) return;
+    if (lim_dev && !*lim_dev) do_limiter = 0;
     grad_item<S, NV>(m, F, U, W, G, phi, do_limiter, i, done);  // waits for its predecessor (pdl.cuh)
 }
 

@@ -8,6 +8,7 @@
 // expressions so the Newton trace follows the reference.
 #include <cuda_runtime.h>
 
+#include <algorithm>
 #include <chrono>
 #include <cmath>
 #include <cstdio>
@@ -131,7 +132,7 @@ struct cfdg_solver {
     double* w64 = nullptr;
     cudaGraphExec_t gexec = nullptr;
     const void* gkey[4] = {nullptr, nullptr, nullptr, nullptr};
-    bool gnewton = false;  // the graph was built for newton_step_graph (enqueue_gmres_pre)
+    bool gnewton = false;  // the graph was built for a Newton step (newton_chain; enqueue_gmres_pre)
     int flow_version = 0, graph_version = -1;
     bool capturing = false;
     bool pdl_failed = false;  // the body would not build with programmatic dependent launch
@@ -303,16 +304,20 @@ struct cfdg_solver {
     }
 
     // norms (a Newton step): the gather also writes rhs = -R, the norm pieces and |R|^2 into
-    // scal[8..11] and clears the update's non-finite flag (k_gather_norms)
-    cfdg_status residual_dev(double* Uin, double* out, int update_limiters, bool norms = false) {
+    // scal[8..11] and clears the update's non-finite flag (k_gather_norms; `flag`, default
+    // bad).  lim_dev: the limiter is recomputed only where *lim_dev is also set (a chained
+    // Newton step, whose limiter-freeze decision is taken on the device).
+    cfdg_status residual_dev(double* Uin, double* out, int update_limiters, bool norms = false, int* flag = nullptr,
+                             const int* lim_dev = nullptr) {
         int do_lim = (cfg.spatial == CFDG_SECOND_ORDER_LIMITED && update_limiters) ? 1 : 0;
         ResArgs<double> a = res64(Uin, out, do_lim);
         if (norms) {
             a.rhs_out = rhs;
             a.norms_out = scal + 8;
-            a.flag = bad;
+            a.flag = flag ? flag : bad;
             a.rs = rs;
         }
+        a.lim_dev = lim_dev;
         a.ev = take_events(0);
         launch_residual<double>(a);
         launches += nv == 6 ? 5 : 4;
@@ -482,6 +487,11 @@ struct cfdg_solver {
             // persistent Arnoldi kernel: barrier words and three sets of block partials
             TRY(dalloc(&bar, 4));
             TRY(dalloc(&apart, (2 * (size_t)(KRY_MAXM + 1) + 1) * RED_BLOCKS));
+        }
+        if (!chain_ctl) {
+            TRY(dalloc(&chain_ctl, 4 + (size_t)CHAIN_MAX));
+            TRY(dalloc(&chain_rec, (size_t)NEWTON_REC * CHAIN_MAX));
+            CK(cudaMallocHost((void**)&chain_h, sizeof(double) * CHAIN_HOST_DOUBLES));
         }
         m_alloc = m;
         return CFDG_OK;
@@ -725,8 +735,10 @@ struct cfdg_solver {
 
     cfdg_status build_gmres_graph_once(double* Ubase, double* Rbase, double* rhsd, double* xout, bool newton) {
         // the captured kernels take GmresDev by value: they must be the graph's variant,
-        // whose Givens step ends the WHILE loop
+        // whose Givens step ends the WHILE loop; a Newton step's graph skips its solve once
+        // a chain of steps has stopped (converged or non-finite)
         gd.in_graph = 1;
+        gd.skip = newton ? chain_ctl + 1 : nullptr;
         if (gexec) {
             cudaGraphExecDestroy(gexec);
             gexec = nullptr;
@@ -810,6 +822,7 @@ struct cfdg_solver {
     cfdg_status gmres_stream(double* Ubase, double* Rbase, double* rhsd, double* xout, int* iters) {
         TRY(ensure_krylov());
         gd.in_graph = 0;
+        gd.skip = nullptr;
         cudaGraphConditionalHandle none = 0;
         enqueue_gmres_pre(Ubase, rhsd, none, false);
         int done = 0;
@@ -1081,17 +1094,34 @@ struct cfdg_solver {
         return CFDG_OK;
     }
 
-    // pinned host words the single-sync Newton step reads back: [0..3] the norm pieces,
-    // [4] the GMRES k, [5] the non-finite flag
+    // pinned host words of the graph GMRES solve: [4] its last iteration, [6] the barrier flag
     double* hpin = nullptr;
 
-    // One step of solveImplicit with the graph driver and a single host round trip: the
-    // residual, its norms, the GMRES graph and the update (its decisions taken on the
-    // device) are enqueued together, the CFL control runs on the host afterwards.  Same
-    // arithmetic and the same decisions as newton_step's host-driven sequence.
-    cfdg_status newton_step_graph(double tol, cfdg_step* info, int* converged) {
-        double t0 = now_s();
+    // ---- chained Newton steps (graph driver): the steps' scalar control on the device
+    static constexpr int CHAIN_MAX = 64;
+    // pinned host words: the records, the CFL, then the ints (ctl[0..3], per-step
+    // non-finite flags, the persistent kernel's barrier flag)
+    static constexpr int CHAIN_HOST_DOUBLES = NEWTON_REC * CHAIN_MAX + 1 + (4 + CHAIN_MAX + 2) / 2 + 1;
+    int* chain_ctl = nullptr;     // device: NewtonCtl's ctl[0..3], then one non-finite flag per step
+    double* chain_rec = nullptr;  // device: NEWTON_REC doubles per step
+    double* chain_h = nullptr;
+    std::vector<cudaEvent_t> chain_ev;
+
+    // Up to k steps of solveImplicit (src/Solver.cpp:1705-1797) enqueued back to back with
+    // one host synchronisation: per step the residual with its norms, |R|^2 and rhs = -R
+    // (FP64: the local time step from the device CFL number), the GMRES graph and the
+    // update, whose first thread records the step and runs the reference's CFL control,
+    // step counter and limiter-freeze decision on the device (k_newton_update_chain).
+    // Same arithmetic and decisions as one step at a time, so the trace is the same for
+    // any k.  A step after convergence or a non-finite residual changes nothing (its solve
+    // is empty, its update skipped) and is not reported.  recs gets the steps taken
+    // (*n_done); *converged when the last of them found the residual below tol.
+    cfdg_status newton_chain(double tol, int k, cfdg_step* recs, int* n_done, int* converged) {
         *converged = 0;
+        *n_done = 0;
+        if (k < 1) return CFDG_OK;
+        if (k > CHAIN_MAX) k = CHAIN_MAX;
+        double t0 = now_s();
         TRY(ensure_krylov());
         if (!gexec || graph_version != flow_version || gkey[0] != U || gkey[1] != R || gkey[2] != rhs || gkey[3] != x ||
             !gnewton) {
@@ -1099,80 +1129,112 @@ struct cfdg_solver {
             TRY(build_gmres_graph(U, R, rhs, x, true));
         }
         const bool mixed = cfg.precision == CFDG_MIXED;
-        if (timing) CK(cudaEventRecord(step_ev[0], st));
-        if (mixed) {  // the graph's mixed prologue takes the local time step from scal[12]
-            hpin[6] = cfl;
-            CK(cudaMemcpyAsync(scal + 12, hpin + 6, sizeof(double), cudaMemcpyHostToDevice, st));
-        }
-        bool upd = !(step > cfg.limiter_freeze_step || cfl > cfg.limiter_freeze_cfl);
-        // also the primitives W of U, and (fused into the gather) the norms, |R|^2 and
-        // rhs = -R; clears the update's non-finite flag
-        TRY(residual_dev(U, R, upd ? 1 : 0, true));
-        if (!mixed) {
-            launch_local_dt(nv, mv, F, U, W, cfl, dt, st);
+        const bool limited = cfg.spatial == CFDG_SECOND_ORDER_LIMITED;
+        double* hcfl = chain_h + NEWTON_REC * CHAIN_MAX;
+        int* hc = reinterpret_cast<int*>(hcfl + 1);
+        hc[0] = step;
+        hc[1] = 0;
+        hc[2] = !(step > cfg.limiter_freeze_step || cfl > cfg.limiter_freeze_cfl) ? 1 : 0;
+        hc[3] = 0;
+        *hcfl = cfl;
+        CK(cudaMemcpyAsync(chain_ctl, hc, 4 * sizeof(int), cudaMemcpyHostToDevice, st));
+        CK(cudaMemcpyAsync(scal + 12, hcfl, sizeof(double), cudaMemcpyHostToDevice, st));
+        if (timing)
+            while (chain_ev.size() < 4 * (size_t)k) {
+                cudaEvent_t e;
+                CK(cudaEventCreate(&e));
+                chain_ev.push_back(e);
+            }
+        NewtonCtl c{chain_ctl, scal + 12, chain_rec, gd.gi, cfg.limiter_freeze_step, cfg.limiter_freeze_cfl,
+                    cfg.cfl_max, limited ? 1 : 0};
+        const double wmin = F.w_inf * SstConst::w_min_frac;
+        for (int j = 0; j < k; ++j) {
+            if (timing) CK(cudaEventRecord(chain_ev[4 * j], st));
+            TRY(residual_dev(U, R, limited ? 1 : 0, true, chain_ctl + 4 + j, chain_ctl + 2));
+            if (!mixed) {  // the mixed graph's prologue takes the local time step from scal[12]
+                launch_local_dt(nv, mv, F, U, W, 0.0, dt, st, scal + 12);
+                ++launches;
+            }
+            if (timing) CK(cudaEventRecord(chain_ev[4 * j + 1], st));
+            CK(cudaGraphLaunch(gexec, st));
+            if (timing) CK(cudaEventRecord(chain_ev[4 * j + 2], st));
+            launch_newton_update_chain(nv, nc, U, x, scal + 8, tol, cfg.gamma, wmin, chain_ctl + 4 + j, c, j, st);
             ++launches;
+            if (timing) CK(cudaEventRecord(chain_ev[4 * j + 3], st));
         }
-        if (timing) CK(cudaEventRecord(step_ev[2], st));
-        CK(cudaGraphLaunch(gexec, st));
-        if (timing) CK(cudaEventRecord(step_ev[3], st));
-        launch_newton_update_dev(nv, nc, U, x, scal + 8, tol, cfg.gamma, F.w_inf * SstConst::w_min_frac, bad, st);
-        ++launches;
-        CK(cudaMemcpyAsync(hpin, scal + 8, 4 * sizeof(double), cudaMemcpyDeviceToHost, st));
-        int* hi = reinterpret_cast<int*>(hpin + 4);
-        CK(cudaMemcpyAsync(hi, gd.gi + 1, sizeof(int), cudaMemcpyDeviceToHost, st));
-        CK(cudaMemcpyAsync(hi + 1, bad, sizeof(int), cudaMemcpyDeviceToHost, st));
-        hi[2] = 0;
-        if (bar) CK(cudaMemcpyAsync(hi + 2, bar + 2, sizeof(int), cudaMemcpyDeviceToHost, st));
-        cfdg_step rec;
-        rec.gmres_iters = 0;
-        rec.krylov_ms = 0;
-        TRY(step_time(rec, t0));
-        if (hi[2]) return barrier_timeout();
-        const double* s = hpin;
-        double resVM = s[1] == 0 ? 0.0 : std::sqrt(s[0] / s[1]);
-        rec.res_vm = resVM;
-        rec.res_abs = std::sqrt(s[3]);
-        rec.res_rho = s[1] == 0 ? 0.0 : std::sqrt(s[2] / s[1]);
-        rec.cfl = cfl;
-        rec.limiter_updated = upd ? 1 : 0;
-        if (!std::isfinite(resVM)) {
-            if (info) *info = rec;
-            return fail(CFDG_ERR_NAN, "non-finite residual at Newton step " + std::to_string(step));
+        CK(cudaGetLastError());
+        CK(cudaMemcpyAsync(chain_h, chain_rec, sizeof(double) * NEWTON_REC * k, cudaMemcpyDeviceToHost, st));
+        CK(cudaMemcpyAsync(hc, chain_ctl, sizeof(int) * (4 + k), cudaMemcpyDeviceToHost, st));
+        CK(cudaMemcpyAsync(hcfl, scal + 12, sizeof(double), cudaMemcpyDeviceToHost, st));
+        int* hbar = hc + 4 + CHAIN_MAX;
+        *hbar = 0;
+        if (bar) CK(cudaMemcpyAsync(hbar, bar + 2, sizeof(int), cudaMemcpyDeviceToHost, st));
+        CK(cudaStreamSynchronize(st));
+        collect();
+        const double wall = now_s() - t0;
+        if (limited) limiter_valid = true;
+        // every enqueued step ran its kernels; the WHILE body only in the steps that solved
+        for (int j = 0; j < k; ++j) {
+            const int its = (int)chain_h[NEWTON_REC * j + 4];
+            launches += graph_pre + graph_post + (its > 0 ? body_runs(its) * graph_body : 0);
         }
-        if (resVM < tol) {  // the update was skipped on the device
+        step = hc[0];
+        cfl = *hcfl;
+        if (*hbar) return barrier_timeout();
+        cfdg_status result = CFDG_OK;
+        int taken = 0;
+        for (int j = 0; j < k; ++j) {
+            const double* r = chain_h + NEWTON_REC * j;
+            const int outcome = (int)r[6];
+            if (outcome == 3) break;
+            cfdg_step rec;
+            rec.res_vm = r[0];
+            rec.res_abs = r[1];
+            rec.res_rho = r[2];
+            rec.cfl = r[3];
+            rec.gmres_iters = outcome == 0 ? (int)r[4] : 0;
+            rec.limiter_updated = (int)r[5];
+            rec.seconds = wall / k;
+            rec.device_ms = 0;
             rec.krylov_ms = 0;
-            *converged = 1;
-            if (info) *info = rec;
-            return CFDG_OK;
+            if (timing) {
+                float ms = 0;
+                CK(cudaEventElapsedTime(&ms, chain_ev[4 * j], chain_ev[4 * j + 3]));
+                rec.device_ms = ms;
+                if (outcome == 0) {
+                    CK(cudaEventElapsedTime(&ms, chain_ev[4 * j + 1], chain_ev[4 * j + 2]));
+                    rec.krylov_ms = ms;
+                }
+            }
+            if (recs) recs[taken] = rec;
+            ++taken;
+            const int stepno = (int)r[7];
+            if (outcome == 2) {
+                result = fail(CFDG_ERR_NAN, "non-finite residual at Newton step " + std::to_string(stepno));
+                break;
+            }
+            if (outcome == 1) {
+                *converged = 1;
+                break;
+            }
+            if (hc[4 + j]) {
+                result = fail(CFDG_ERR_NAN, "non-finite state after the Newton update at step " + std::to_string(stepno));
+                break;
+            }
         }
-        const int it = hi[0] + 1;
-        launches += graph_pre + (long long)body_runs(it) * graph_body + graph_post;
-        rec.gmres_iters = it;
-        if (timing) {
-            float ms = 0;
-            CK(cudaEventElapsedTime(&ms, step_ev[2], step_ev[3]));
-            rec.krylov_ms = ms;
-        }
-        if (it >= 29) {
-            cfl *= 0.5;
-            if (cfl < 0.05) cfl = 0.05;
-        }
-        if (step > 5) {
-            if (resVM > 1e6) cfl *= 1.2;
-            else cfl *= 1.5;
-            if (it >= 25) cfl *= 0.5;
-            if (cfl > cfg.cfl_max) cfl = cfg.cfl_max;
-            if (cfl < 0.1) cfl = 0.1;
-        }
-        ++step;
-        if (info) *info = rec;
-        if (hi[1]) return fail(CFDG_ERR_NAN, "non-finite state after the Newton update at step " + std::to_string(step - 1));
-        return CFDG_OK;
+        *n_done = taken;
+        return result;
     }
 
     // one step of solveImplicit (src/Solver.cpp:1705-1797)
     cfdg_status newton_step(double tol, cfdg_step* info, int* converged) {
-        if (cfg.krylov == CFDG_KRYLOV_GRAPH) return newton_step_graph(tol, info, converged);
+        if (cfg.krylov == CFDG_KRYLOV_GRAPH) {
+            int n = 0;
+            cfdg_step rec{};
+            cfdg_status e = newton_chain(tol, 1, &rec, &n, converged);
+            if (info && n) *info = rec;
+            return e;
+        }
         double t0 = now_s();
         *converged = 0;
         if (timing) CK(cudaEventRecord(step_ev[0], st));
@@ -1378,6 +1440,10 @@ struct cfdg_solver {
         cudaFree(bar);
         cudaFree(apart);
         if (hpin) cudaFreeHost(hpin);
+        cudaFree(chain_ctl);
+        cudaFree(chain_rec);
+        if (chain_h) cudaFreeHost(chain_h);
+        for (cudaEvent_t e : chain_ev) cudaEventDestroy(e);
         cudaFree(dinv32);
         cudaFree(dinv64);
         void* pt[] = {Tt, Tj, Tjd, dwall, T32, T32d, dwall32};
@@ -1453,6 +1519,7 @@ void cfdg_config_default(cfdg_config* c) {
     c->persistent = 0;
     c->pdl = 1;
     c->barrier_poll_limit = 0;
+    c->newton_chain = 8;
 }
 
 cfdg_status cfdg_mesh_create(int n_nodes, const double* xy, int n_cells, const int* cells, int n_bedges,
@@ -1947,9 +2014,50 @@ cfdg_status cfdg_newton_step(cfdg_solver* s, double tol, cfdg_step* info, int* c
     return st;
 }
 
+cfdg_status cfdg_newton_steps(cfdg_solver* s, double tol, int k, cfdg_step* trace, int* n_done, int* converged) {
+    if (!s || k < 0) return fail(CFDG_ERR_ARG, "bad arguments");
+    int n = 0, cv = 0;
+    if (n_done) *n_done = 0;
+    if (converged) *converged = 0;
+    while (n < k && !cv) {
+        int done = 0;
+        cfdg_status st;
+        if (s->cfg.krylov == CFDG_KRYLOV_GRAPH) {
+            st = s->newton_chain(tol, std::min(k - n, (int)cfdg_solver::CHAIN_MAX), trace ? trace + n : nullptr, &done, &cv);
+        } else {
+            cfdg_step rec;
+            st = s->newton_step(tol, &rec, &cv);
+            if (trace) trace[n] = rec;
+            done = 1;
+        }
+        n += done;
+        if (n_done) *n_done = n;
+        if (converged) *converged = cv;
+        if (st != CFDG_OK) return st;
+        if (done == 0) break;
+    }
+    return CFDG_OK;
+}
+
 cfdg_status cfdg_solve_implicit(cfdg_solver* s, double tol, int max_steps, cfdg_step* trace, int* n_steps) {
     if (!s || max_steps < 0) return fail(CFDG_ERR_ARG, "bad arguments");
     TRY(cfdg_reset_newton(s));
+    if (s->cfg.krylov == CFDG_KRYLOV_GRAPH && s->cfg.newton_chain > 1) {
+        // steps in chains of newton_chain, one host synchronisation per chain
+        int n = 0, cv = 0;
+        if (n_steps) *n_steps = 0;
+        while (n < max_steps) {
+            int done = 0;
+            const int kk = std::min(max_steps - n, std::min(s->cfg.newton_chain, (int)cfdg_solver::CHAIN_MAX));
+            cfdg_status st = s->newton_chain(tol, kk, trace ? trace + n : nullptr, &done, &cv);
+            n += done;
+            if (n_steps) *n_steps = n;
+            if (st != CFDG_OK) return st;
+            if (cv) return CFDG_OK;
+            if (done == 0) break;
+        }
+        return fail(CFDG_ERR_NOT_CONVERGED, "solveImplicit reached max_steps above the tolerance");
+    }
     int n = 0;
     for (int k = 0; k < max_steps; ++k) {
         cfdg_step rec;

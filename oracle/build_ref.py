@@ -53,13 +53,28 @@ BC_PLATE = (1088, 1139)
 INIT_FREESTREAM = (905, 920)
 
 VARIANTS = {
-    # name: (bc range to enable or None, init range to enable or None, viscous)
+    # name: (bc range to enable or None, init range to enable or None, viscous[, knobs])
     "bump": (None, None, False),
     "bump_visc": (None, None, True),
     "supersonic": (BC_SUPERSONIC, INIT_FREESTREAM, False),
     "plate": (BC_PLATE, INIT_FREESTREAM, False),
     "plate_visc": (BC_PLATE, INIT_FREESTREAM, True),
+    # the supersonic wedge of the converged-solution fixtures: GMRES(30) and a first CFL of
+    # 10, with the reference's limiter freeze and with the limiter frozen from the start
+    "supersonic_m30_cfl10": (BC_SUPERSONIC, INIT_FREESTREAM, False, dict(REF_GMRES_M=30, REF_CFL0=10.0)),
+    "supersonic_m30_cfl10_frozen": (BC_SUPERSONIC, INIT_FREESTREAM, False,
+                                    dict(REF_GMRES_M=30, REF_CFL0=10.0, REF_FREEZE_STEP=-1)),
 }
+
+# Hard-coded constants of solveGMRES / solveImplicit made compile-time knobs; their
+# defaults are the reference's own values, so a variant without knobs compiles to the
+# reference's code.  (line, original text, replacement)
+KNOBS = (
+    (1479, "int m = 40;", "int m = REF_GMRES_M;"),
+    (1701, "double CFL = 0.1;", "double CFL = REF_CFL0;"),
+    (1714, "if (step > 150 || CFL > 10.0)", "if (step > REF_FREEZE_STEP || CFL > REF_FREEZE_CFL)"),
+)
+KNOB_DEFAULTS = dict(REF_GMRES_M=40, REF_CFL0=0.1, REF_FREEZE_STEP=150, REF_FREEZE_CFL=10.0)
 
 
 def _expect(lines, no, needle):
@@ -88,6 +103,9 @@ def _uncomment(lines, rng):
 
 def make_variant(src_lines, bc, init, viscous):
     lines = list(src_lines)
+    for no, old, new in KNOBS:
+        _expect(lines, no, old)
+        lines[no - 1] = lines[no - 1].replace(old, new)
     _expect(lines, 46, "void Solver::initialize()")
     _expect(lines, 806, "State Solver::getBoundaryGhostState")
     _expect(lines, 863, "}")
@@ -109,7 +127,9 @@ def make_variant(src_lines, bc, init, viscous):
         nb = "mesh.cells[f.neighbor >= 0 ? f.neighbor : f.owner]"
         lines[728] = lines[728].replace("mesh.cells[f.neighbor]", nb)
         lines[729] = lines[729].replace("mesh.cells[f.neighbor]", nb)
-    return lines
+    # the knobs' defaults, prepended last so the line numbers above are the reference's
+    defaults = "".join(f"#ifndef {k}\n#define {k} {v}\n#endif\n" for k, v in KNOB_DEFAULTS.items())
+    return [defaults + lines[0]] + lines[1:]
 
 
 def build(src_root: str, jobs: int = 4) -> list[str]:
@@ -124,13 +144,16 @@ def build(src_root: str, jobs: int = 4) -> list[str]:
     tmp = tempfile.mkdtemp(prefix="cfd_ref_")
     procs, outs = [], []
     try:
-        for name, (bc, init, visc) in VARIANTS.items():
+        for name, spec in VARIANTS.items():
+            bc, init, visc = spec[:3]
+            knobs = spec[3] if len(spec) > 3 else {}
             gen = os.path.join(tmp, f"Solver_{name}.cpp")
             with open(gen, "w", newline="") as fh:
                 fh.write("\n".join(make_variant(src_lines, bc, init, visc)))
             so = os.path.join(OUT, f"libref_{name}.so")
             cmd = ["g++", "-O2", "-std=c++17", "-fPIC", "-shared", "-ffp-contract=off",
                    f"-I{inc}", f'-DREF_SOLVER_CPP="{gen}"', f'-DREF_MESH_CPP="{mesh}"',
+                   *[f"-D{k}={v}" for k, v in knobs.items()],
                    os.path.join(HERE, "ref_harness.cpp"), "-o", so]
             procs.append((name, subprocess.Popen(cmd, stderr=subprocess.PIPE, text=True)))
             outs.append(so)
