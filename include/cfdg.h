@@ -232,9 +232,11 @@ cfdg_status cfdg_newton_step(cfdg_solver* s, double tol, cfdg_step* info, int* c
  * reference's CFL control (src/Solver.cpp:1747-1750, :1780-1796) and limiter-freeze
  * decision (:1714) run on the device between the steps, with the same arithmetic and the
  * same trace as k single steps.  Stops at convergence (*converged set: that step's
- * residual was below tol and no update was made) or an error.  trace (may be NULL) gets
- * the records of the steps taken, *n_done their count. */
-cfdg_status cfdg_newton_steps(cfdg_solver* s, double tol, int k, cfdg_step* trace, int* n_done, int* converged);
+ * residual was below tol, or with tol_rho > 0 its volume-weighted density residual at or
+ * below tol_rho after step 5; with the graph driver that step made no update) or an
+ * error.  trace (may be NULL) gets the records of the steps taken, *n_done their count. */
+cfdg_status cfdg_newton_steps(cfdg_solver* s, double tol, double tol_rho, int k, cfdg_step* trace, int* n_done,
+                              int* converged);
 /* switch the Krylov driver (CFDG_KRYLOV_HOST or CFDG_KRYLOV_GRAPH) between solves */
 cfdg_status cfdg_set_krylov(cfdg_solver* s, int mode);
 /* Newton driver state (CFL, step counter) */

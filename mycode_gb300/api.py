@@ -102,7 +102,8 @@ SIGNATURES = {
     "cfdg_norm_vm": (C.c_int, [_vp, _dp, C.POINTER(C.c_double)]),
     "cfdg_solve_implicit": (C.c_int, [_vp, C.c_double, C.c_int, C.POINTER(Step), C.POINTER(C.c_int)]),
     "cfdg_newton_step": (C.c_int, [_vp, C.c_double, C.POINTER(Step), C.POINTER(C.c_int)]),
-    "cfdg_newton_steps": (C.c_int, [_vp, C.c_double, C.c_int, C.c_void_p, C.POINTER(C.c_int), C.POINTER(C.c_int)]),
+    "cfdg_newton_steps": (C.c_int, [_vp, C.c_double, C.c_double, C.c_int, C.c_void_p, C.POINTER(C.c_int),
+                                    C.POINTER(C.c_int)]),
     "cfdg_reset_newton": (C.c_int, [_vp]),
     "cfdg_get_newton_state": (C.c_int, [_vp, C.POINTER(C.c_double), C.POINTER(C.c_int)]),
     "cfdg_set_newton_state": (C.c_int, [_vp, C.c_double, C.c_int]),
@@ -436,12 +437,14 @@ class Solver:
         _check(lib().cfdg_newton_step(self._h, float(tol), C.byref(s), C.byref(cv)))
         return s, bool(cv.value)
 
-    def newton_steps(self, k, tol=0.0):
-        """k Newton steps enqueued back to back (graph driver: one host synchronisation);
+    def newton_steps(self, k, tol=0.0, tol_rho=0.0):
+        """k Newton steps enqueued back to back (graph driver: one host synchronisation),
+        stopping at res_vm < tol or (tol_rho > 0) a density residual <= tol_rho after step 5;
         returns (records of the steps taken, converged)."""
         tr = (Step * max(int(k), 1))()
         n, cv = C.c_int(0), C.c_int(0)
-        _check(lib().cfdg_newton_steps(self._h, float(tol), int(k), C.cast(tr, C.c_void_p), C.byref(n), C.byref(cv)))
+        _check(lib().cfdg_newton_steps(self._h, float(tol), float(tol_rho), int(k), C.cast(tr, C.c_void_p), C.byref(n),
+                                       C.byref(cv)))
         return list(tr[: n.value]), bool(cv.value)
 
     def set_krylov(self, mode):

@@ -111,9 +111,9 @@ CFD_HD Flux6<S> face_flux(const Flow<R>& F, const CS<S>& L, const CS<S>& Rn, boo
         const R gm1 = F.gam - R(1.0);
         R Cp = div_shared(F.gam * F.Rgas, gm1, recip_for(gm1));  // 1/(gamma-1) shared with the reconstruction
         S mu = rf * F.nu;
-        S kc = mu * Cp / F.Pr;
+        S kc = div_shared(mu * Cp, F.Pr, F.inv_Pr);  // FP64: by the reciprocal of Pr, the same bits
         if (F.sst) {
-            kc = kc + mutf * Cp / F.Pr_t;
+            kc = kc + div_shared(mutf * Cp, F.Pr_t, F.inv_Prt);
             mu = mu + mutf;
         }
         S div = dudx + dvdy;
@@ -138,10 +138,13 @@ CFD_HD Flux6<S> face_flux(const Flow<R>& F, const CS<S>& L, const CS<S>& Rn, boo
 // mu_t,f = (mu_t,L + mu_t,R) / 2 (zero at a no-slip wall), then the k and w rows
 // (sst_face_flux) from the mean flow's mass flux.  gkL/gkR: k_x, k_y, w_x, w_y of each
 // side.  On the boundary the right-hand mu_t, F1 and k, w gradients are the owner's.
+// kwL/kwR: the specific k, w (rho k / rho, rho w / rho) of the owner and the neighbour, the
+// primitives the cells already hold (the same quotients); on the boundary the ghost's are
+// formed here.
 template <class S, class R>
 CFD_HD Flux6<S> face_flux_sst(const Flow<R>& F, const CS<S>& L, const CS<S>& Rn, bool interior, int tag,
                               const FaceGeo<R>& g, const S* gL, const S* gR, const S* gkL, const S* gkR, S phL,
-                              S phR, S mutL, S mutR, S F1L, S F1R) {
+                              S phR, S mutL, S mutR, S F1L, S F1R, const S* kwL, const S* kwR) {
     bool wall = !interior && tag == 4;
     if (!interior) {
         mutR = mutL;
@@ -153,8 +156,17 @@ CFD_HD Flux6<S> face_flux_sst(const Flow<R>& F, const CS<S>& L, const CS<S>& Rn,
     CS<S> Rt = face_right(F, L, Rn, interior, tag, g.nx, g.ny, wall_normal_distance(g));
     const S* gkRv = interior ? gkR : gkL;
     S Fk, Fw;
-    sst_face_flux(F, out.f[0], L.rk / L.r, L.rw / L.r, Rt.rk / Rt.r, Rt.rw / Rt.r, R(0.5) * (L.r + Rt.r), mutf, F1f,
-                  gkL, gkRv, wall, g.nx, g.ny, g.A, g.dxL, g.dyL, g.dxlr, g.dylr, Fk, Fw);
+    S kR, wR;
+    if (interior) {
+        kR = kwR[0];
+        wR = kwR[1];
+    } else {
+        const S ig = recip_for(Rt.r);
+        kR = quot_shared(Rt.rk, Rt.r, ig);
+        wR = quot_shared(Rt.rw, Rt.r, ig);
+    }
+    sst_face_flux(F, out.f[0], kwL[0], kwL[1], kR, wR, R(0.5) * (L.r + Rt.r), mutf, F1f, gkL, gkRv, wall, g.nx, g.ny,
+                  g.A, g.dxL, g.dyL, g.dxlr, g.dylr, Fk, Fw);
     out.f[4] = Fk;
     out.f[5] = Fw;
     return out;

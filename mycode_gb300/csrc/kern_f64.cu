@@ -96,9 +96,9 @@ void launch_local_dt(int nv, const MeshView<double>& m, const Flow<double>& F, c
     NV_SWITCH(nv, (k_local_dt<NVC><<<blocks_for(m.nc), tpb_for(m.nc), 0, s>>>(m, F, U, W, cfl, dt, cfl_dev)));
 }
 void launch_newton_update_chain(int nv, long nc, double* U, const double* dU, const double* norms, double tol,
-                                double gam, double wmin, int* bad, const NewtonCtl& c, int k, cudaStream_t s) {
+                                double gam, double wmin, int* bad, const NewtonCtl& c, int k, int step, cudaStream_t s) {
     NV_SWITCH(nv, (k_newton_update_chain<NVC><<<blocks_for(nc), tpb_for(nc), 0, s>>>(nc, U, dU, norms, tol, gam, wmin,
-                                                                                     bad, c, k)));
+                                                                                     bad, c, k, step)));
 }
 void launch_precond(int nv, const MeshView<double>& m, const Flow<double>& F, const double* U, const double* W,
                     const double* dt, double* D, const double* mut, cudaStream_t s) {

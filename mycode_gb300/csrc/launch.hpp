@@ -109,7 +109,8 @@ void launch_newton_update_dev(int nv, long nc, double* U, const double* dU, cons
                               double wmin, int* bad, cudaStream_t s);
 // the same update plus the step's scalar control on the device (step k of a chain)
 void launch_newton_update_chain(int nv, long nc, double* U, const double* dU, const double* norms, double tol,
-                                double gam, double wmin, int* bad, const NewtonCtl& c, int k, cudaStream_t s);
+                                double gam, double wmin, int* bad, const NewtonCtl& c, int k, int step,
+                                cudaStream_t s);
 // time stepping: timeStepExplicit's update, solveUnsteady's right-hand side and update
 void launch_explicit_update(int nv, long nc, double* U, const double* R, const double* vol, double dt, int* bad,
                             cudaStream_t s);

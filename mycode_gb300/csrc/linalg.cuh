@@ -544,11 +544,25 @@ struct NewtonCtl {
     int freeze_step;
     double freeze_cfl, cfl_max;
     int limited;     // second-order limited scheme
+    double tol_rho;  // also stop at a density residual at or below this after step 5 (0 = off)
 };
 // record: res_vm, res_abs, res_rho, CFL used, GMRES iterations of the step's solve,
 // limiter recomputed, outcome (0 updated, 1 converged, 2 non-finite residual, 3 not taken:
 // an earlier step of the chain stopped), step index
 constexpr int NEWTON_REC = 8;
+
+// the step is converged: the reference's test on the all-component norm, or the optional
+// density test (step is the step's index; every thread evaluates this from the same norms)
+__device__ __forceinline__ bool newton_converged(const NewtonCtl& c, const double* norms, double resVM, double tol,
+                                                 int step) {
+    if (resVM < tol) return true;
+    if (c.tol_rho > 0.0 && step > 5) {
+        const double s1 = norms[1];
+        const double rho = s1 == 0 ? 0.0 : sqrt(norms[2] / s1);
+        return rho <= c.tol_rho;
+    }
+    return false;
+}
 
 __device__ __forceinline__ void newton_control(const NewtonCtl& c, const double* norms, double tol, int k) {
     const double s0 = norms[0], s1 = norms[1];
@@ -573,7 +587,7 @@ __device__ __forceinline__ void newton_control(const NewtonCtl& c, const double*
         r[6] = 2.0;
         return;
     }
-    if (resVM < tol) {
+    if (newton_converged(c, norms, resVM, tol, step)) {
         c.ctl[1] = 1;
         r[6] = 1.0;
         return;
@@ -597,18 +611,19 @@ __device__ __forceinline__ void newton_control(const NewtonCtl& c, const double*
 }
 
 // k_newton_update_dev's update plus the scalar control in thread 0 of block 0 (chain
-// step k).  The other threads take their converged / non-finite / relaxation decisions
-// from the same norms, so a step after a stop changes nothing.
+// step k, the solve's step `step` when no earlier step of the chain stopped).  The other
+// threads take their converged / non-finite / relaxation decisions from the same norms,
+// so a step after a stop changes nothing.
 template <int NV>
 __global__ void k_newton_update_chain(long nc, double* __restrict__ U, const double* __restrict__ dU,
                                       const double* __restrict__ norms, double tol, double gam, double wmin, int* bad,
-                                      NewtonCtl c, int k) {
+                                      NewtonCtl c, int k, int step) {
     long i = (long)blockIdx.x * blockDim.x + threadIdx.x;
     if (i == 0) newton_control(c, norms, tol, k);
     if (i >= nc) return;
     const double s0 = norms[0], s1 = norms[1];
     const double resVM = s1 == 0 ? 0.0 : sqrt(s0 / s1);
-    if (!(resVM >= tol) || !isfinite(resVM)) return;
+    if (!isfinite(resVM) || newton_converged(c, norms, resVM, tol, step)) return;
     double relax = 1.0;
     if (resVM > 1e6) relax = 0.5;
     else if (resVM > 2e3 && resVM < 1e2) relax = 0.9;

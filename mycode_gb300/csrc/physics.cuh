@@ -58,6 +58,7 @@ struct Flow {
     R shock[4]; // post-shock inflow state for tag 6 (no reference counterpart)
     // SST (no reference counterpart; parity unpinned)
     R k_inf, w_inf, Pr_t;
+    R inv_Pr, inv_Prt;  // RN(1 / Pr), RN(1 / Pr_t): quotients by them through quot_by_recip
     int bcset, flux, spatial, viscous;
     int sst;    // 1: the state carries rhok, rhow (SST)
 };
@@ -183,9 +184,10 @@ CFD_HD Flux6<S> flux_hllc(const Flow<R>& F, const CS<S>& L, const CS<S>& Rt, R n
     S cL = sqrt(quot_shared(F.gam * L.p, L.r, recip_for(L.r))), cR = sqrt(quot_shared(F.gam * Rt.p, Rt.r, recip_for(Rt.r)));
     S hL = quot_shared(L.rE + L.p, L.r, recip_for(L.r)), hR = quot_shared(Rt.rE + Rt.p, Rt.r, recip_for(Rt.r));
     S sL = sqrt(L.r), sR = sqrt(Rt.r);
-    S ut = (sL * L.u + sR * Rt.u) / (sL + sR);
-    S vt = (sL * L.v + sR * Rt.v) / (sL + sR);
-    S ht = (sL * hL + sR * hR) / (sL + sR);
+    const S iLR = recip_for(sL + sR);  // FP64: the three quotients by sL + sR through one reciprocal
+    S ut = quot_shared(sL * L.u + sR * Rt.u, sL + sR, iLR);
+    S vt = quot_shared(sL * L.v + sR * Rt.v, sL + sR, iLR);
+    S ht = quot_shared(sL * hL + sR * hR, sL + sR, iLR);
     S unt = ut * nx + vt * ny;
     S ct = sqrt((F.gam - R(1.0)) * (ht - R(0.5) * (ut * ut + vt * vt)));
     S SL = smin(unL - cL, unt - ct);
@@ -197,12 +199,13 @@ CFD_HD Flux6<S> flux_hllc(const Flow<R>& F, const CS<S>& L, const CS<S>& Rt, R n
     const CS<S>& K = (val(Ss) >= R(0.0)) ? L : Rt;
     S SK = (val(Ss) >= R(0.0)) ? SL : SR;
     S unK = (val(Ss) >= R(0.0)) ? unL : unR;
+    const S iK = (val(Ss) >= R(0.0)) ? recip_for(L.r) : recip_for(Rt.r);  // the sound speeds' reciprocals
     S coef = K.r * (SK - unK) / (SK - Ss);
     S Us[6];
     Us[0] = coef;
     Us[1] = coef * (K.u + (Ss - unK) * nx);
     Us[2] = coef * (K.v + (Ss - unK) * ny);
-    Us[3] = coef * (K.rE / K.r + (Ss - unK) * (Ss + K.p / (K.r * (SK - unK))));
+    Us[3] = coef * (quot_shared(K.rE, K.r, iK) + (Ss - unK) * (Ss + K.p / (K.r * (SK - unK))));
     Us[4] = S(R(0));
     Us[5] = S(R(0));
     S UK[6] = {K.r, K.ru, K.rv, K.rE, K.rk, K.rw};

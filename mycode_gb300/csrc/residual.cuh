@@ -353,6 +353,8 @@ __device__ __forceinline__ void flux_item(const MeshView<R>& m, const Flow<R>& F
         gk[3] = Acc<S>::ld(G, G_W + 1, o);
         gk[4] = gk[0], gk[5] = gk[1], gk[6] = gk[2], gk[7] = gk[3];
         S mutR = S(R(0)), F1R = S(R(0));
+        // specific k, w of the two cells: the primitives k_prim formed (rho k / rho, rho w / rho)
+        S kw[4] = {Acc<S>::ld(W, W_K, o), Acc<S>::ld(W, W_W, o), S(R(0)), S(R(0))};
         if (interior) {
             gk[4] = Acc<S>::ld(G, G_K, n);
             gk[5] = Acc<S>::ld(G, G_K + 1, n);
@@ -360,9 +362,11 @@ __device__ __forceinline__ void flux_item(const MeshView<R>& m, const Flow<R>& F
             gk[7] = Acc<S>::ld(G, G_W + 1, n);
             mutR = Acc<S>::ld(T, 0, n);
             F1R = Acc<S>::ld(T, 1, n);
+            kw[2] = Acc<S>::ld(W, W_K, n);
+            kw[3] = Acc<S>::ld(W, W_W, n);
         }
         Flux6<S> out = face_flux_sst(F, L, Rn, interior, tag, g, gL, gR, gk, gk + 4, phL, phR, Acc<S>::ld(T, 0, o),
-                                     mutR, Acc<S>::ld(T, 1, o), F1R);
+                                     mutR, Acc<S>::ld(T, 1, o), F1R, kw, kw + 2);
 #pragma unroll
         for (int c = 0; c < 6; ++c) Acc<S>::st(FA, c, f, out.f[c]);
         return;

@@ -250,10 +250,14 @@ struct cfdg_solver {
             F.w_inf = ww;
         }
         F.Pr_t = 0.9;
+        // correctly rounded reciprocals (host IEEE division) for the kernels' shared-reciprocal quotients
+        F.inv_Pr = 1.0 / F.Pr;
+        F.inv_Prt = 1.0 / F.Pr_t;
         Ff.gam = (float)F.gam; Ff.Rgas = (float)F.Rgas; Ff.Pr = (float)F.Pr; Ff.nu = (float)F.nu;
         Ff.Minf = (float)F.Minf; Ff.P0 = (float)F.P0; Ff.T0 = (float)F.T0; Ff.Pexit = (float)F.Pexit;
         for (int k = 0; k < 4; ++k) { Ff.fs[k] = (float)F.fs[k]; Ff.shock[k] = (float)F.shock[k]; }
         Ff.k_inf = (float)F.k_inf; Ff.w_inf = (float)F.w_inf; Ff.Pr_t = (float)F.Pr_t;
+        Ff.inv_Pr = (float)F.inv_Pr; Ff.inv_Prt = (float)F.inv_Prt;
         Ff.bcset = F.bcset; Ff.flux = F.flux; Ff.spatial = F.spatial; Ff.viscous = F.viscous; Ff.sst = F.sst;
     }
 
@@ -1115,8 +1119,9 @@ struct cfdg_solver {
     // Same arithmetic and decisions as one step at a time, so the trace is the same for
     // any k.  A step after convergence or a non-finite residual changes nothing (its solve
     // is empty, its update skipped) and is not reported.  recs gets the steps taken
-    // (*n_done); *converged when the last of them found the residual below tol.
-    cfdg_status newton_chain(double tol, int k, cfdg_step* recs, int* n_done, int* converged) {
+    // (*n_done); *converged when the last of them found the residual below tol (or, with
+    // tol_rho > 0, the density residual at or below tol_rho after step 5).
+    cfdg_status newton_chain(double tol, int k, cfdg_step* recs, int* n_done, int* converged, double tol_rho = 0.0) {
         *converged = 0;
         *n_done = 0;
         if (k < 1) return CFDG_OK;
@@ -1146,7 +1151,7 @@ struct cfdg_solver {
                 chain_ev.push_back(e);
             }
         NewtonCtl c{chain_ctl, scal + 12, chain_rec, gd.gi, cfg.limiter_freeze_step, cfg.limiter_freeze_cfl,
-                    cfg.cfl_max, limited ? 1 : 0};
+                    cfg.cfl_max, limited ? 1 : 0, tol_rho};
         const double wmin = F.w_inf * SstConst::w_min_frac;
         for (int j = 0; j < k; ++j) {
             if (timing) CK(cudaEventRecord(chain_ev[4 * j], st));
@@ -1158,7 +1163,8 @@ struct cfdg_solver {
             if (timing) CK(cudaEventRecord(chain_ev[4 * j + 1], st));
             CK(cudaGraphLaunch(gexec, st));
             if (timing) CK(cudaEventRecord(chain_ev[4 * j + 2], st));
-            launch_newton_update_chain(nv, nc, U, x, scal + 8, tol, cfg.gamma, wmin, chain_ctl + 4 + j, c, j, st);
+            launch_newton_update_chain(nv, nc, U, x, scal + 8, tol, cfg.gamma, wmin, chain_ctl + 4 + j, c, j, step + j,
+                                       st);
             ++launches;
             if (timing) CK(cudaEventRecord(chain_ev[4 * j + 3], st));
         }
@@ -2014,8 +2020,9 @@ cfdg_status cfdg_newton_step(cfdg_solver* s, double tol, cfdg_step* info, int* c
     return st;
 }
 
-cfdg_status cfdg_newton_steps(cfdg_solver* s, double tol, int k, cfdg_step* trace, int* n_done, int* converged) {
-    if (!s || k < 0) return fail(CFDG_ERR_ARG, "bad arguments");
+cfdg_status cfdg_newton_steps(cfdg_solver* s, double tol, double tol_rho, int k, cfdg_step* trace, int* n_done,
+                              int* converged) {
+    if (!s || k < 0 || tol_rho < 0) return fail(CFDG_ERR_ARG, "bad arguments");
     int n = 0, cv = 0;
     if (n_done) *n_done = 0;
     if (converged) *converged = 0;
@@ -2023,12 +2030,17 @@ cfdg_status cfdg_newton_steps(cfdg_solver* s, double tol, int k, cfdg_step* trac
         int done = 0;
         cfdg_status st;
         if (s->cfg.krylov == CFDG_KRYLOV_GRAPH) {
-            st = s->newton_chain(tol, std::min(k - n, (int)cfdg_solver::CHAIN_MAX), trace ? trace + n : nullptr, &done, &cv);
+            st = s->newton_chain(tol, std::min(k - n, (int)cfdg_solver::CHAIN_MAX), trace ? trace + n : nullptr, &done, &cv,
+                                 tol_rho);
         } else {
             cfdg_step rec;
+            const int step0 = s->step;
             st = s->newton_step(tol, &rec, &cv);
             if (trace) trace[n] = rec;
             done = 1;
+            // the density test on the host driver: this step's residual was already low (the
+            // update it made is kept)
+            if (st == CFDG_OK && !cv && tol_rho > 0.0 && step0 > 5 && rec.res_rho <= tol_rho) cv = 1;
         }
         n += done;
         if (n_done) *n_done = n;

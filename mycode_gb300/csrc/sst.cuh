@@ -93,16 +93,18 @@ CFD_HD void sst_face_flux(const Flow<R>& F, S mdotA, S kL, S wL, S kR, S wR, S r
     if (wall) {
         R d2 = dxL * dxL + dyL * dyL;
         R dn = dxL * nx + dyL * ny;
+        const R id2 = R(1) / d2;  // FP64: the two quotients through one reciprocal (div_shared)
         // (phi_face - phi_c) (d . n) / |d|^2, phi_face = 0 for k and w_face for w
-        dkn = (S(R(0)) - kL) * dn / d2;
-        dwn = (R(0.5) * (wL + wR) - wL) * dn / d2;
+        dkn = div_shared((S(R(0)) - kL) * dn, d2, id2);
+        dwn = div_shared((R(0.5) * (wL + wR) - wL) * dn, d2, id2);
     } else {
         S kx = R(0.5) * (gkL[0] + gkR[0]), ky = R(0.5) * (gkL[1] + gkR[1]);
         S wx = R(0.5) * (gkL[2] + gkR[2]), wy = R(0.5) * (gkL[3] + gkR[3]);
         R d2 = dxlr * dxlr + dylr * dylr;
         if (d2 > R(1e-14)) {
-            S ck = (kx * dxlr + ky * dylr - (kR - kL)) / d2;
-            S cw = (wx * dxlr + wy * dylr - (wR - wL)) / d2;
+            const R id2 = R(1) / d2;  // the viscous flux's reciprocal of the same d2
+            S ck = div_shared(kx * dxlr + ky * dylr - (kR - kL), d2, id2);
+            S cw = div_shared(wx * dxlr + wy * dylr - (wR - wL), d2, id2);
             kx = kx - ck * dxlr;
             ky = ky - ck * dylr;
             wx = wx - cw * dxlr;

@@ -13,6 +13,7 @@ Flow<double> flow(const double* p, const int* fl) {
     F.gam = p[0]; F.Rgas = p[1]; F.Pr = p[2]; F.nu = p[3]; F.Minf = p[4]; F.P0 = p[5]; F.T0 = p[6]; F.Pexit = p[7];
     for (int k = 0; k < 4; ++k) { F.fs[k] = p[8 + k]; F.shock[k] = p[12 + k]; }
     F.k_inf = 0; F.w_inf = 0; F.Pr_t = 0.9;
+    F.inv_Pr = 1.0 / F.Pr; F.inv_Prt = 1.0 / F.Pr_t;
     F.bcset = fl[0]; F.flux = fl[1]; F.spatial = fl[2]; F.viscous = fl[3];
     return F;
 }
@@ -67,8 +68,9 @@ void sst_face_eval(const double* p, const int* fl, const double* g, const double
                    const double* t, double* out) {
     Flow<double> F = flow(p, fl);
     F.sst = 1; F.k_inf = p[16]; F.w_inf = p[17];
+    const double kw[4] = {UL[4] / UL[0], UL[5] / UL[0], UR[4] / UR[0], UR[5] / UR[0]};
     Flux6<double> o = face_flux_sst(F, cs(F, UL), cs(F, UR), fl[4] != 0, fl[5], geo(g), gL, gR, gkL, gkR, phL, phR,
-                                    t[0], t[1], t[2], t[3]);
+                                    t[0], t[1], t[2], t[3], kw, kw + 2);
     for (int c = 0; c < 6; ++c) out[c] = o.f[c];
 }
 

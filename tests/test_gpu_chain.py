@@ -58,6 +58,19 @@ def test_chained_solve_stops_at_convergence_in_mid_chain(cuda_lib):
     _same(a, b)
 
 
+def test_chained_steps_stop_at_the_density_tolerance(cuda_lib):
+    ref = _solver(cuda_lib, "supersonic", "mixed", "exact", "HLLC", 1)
+    tr = ref.solveImplicit(0.0, 20)
+    tol_rho = float(tr["res_rho"][12]) * (1.0 + 1e-12)
+    first = 6 + int(np.flatnonzero(tr["res_rho"][6:] <= tol_rho)[0])
+    s = _solver(cuda_lib, "supersonic", "mixed", "exact", "HLLC", 1)
+    s.reset_newton()
+    recs, cv = s.newton_steps(40, 0.0, tol_rho)
+    assert cv and len(recs) == first + 1
+    np.testing.assert_array_equal([r.res_vm for r in recs], tr["res_vm"][: first + 1])
+    np.testing.assert_array_equal([r.cfl for r in recs], tr["cfl"][: first + 1])
+
+
 def test_newton_steps_continue_the_solve(cuda_lib):
     whole = _solver(cuda_lib, "supersonic", "mixed", "exact", "HLLC", 1)
     w = whole.solveImplicit(0.0, 25)
