@@ -143,6 +143,13 @@ void cfdg_config_default(cfdg_config* cfg);
  * slot for a triangle; bedges[3*n_bedges] = (node a, node b, physical tag). */
 cfdg_status cfdg_mesh_create(int n_nodes, const double* xy, int n_cells, const int* cells,
                              int n_bedges, const int* bedges, int renumber, cfdg_mesh** out);
+/* The same mesh (bit for bit: faces, owners, geometry, renumbering, the device layout) built
+ * by kernels on `device` instead of the host (Mesh::buildConnectivity and
+ * Mesh::computeGeometry, src/Mesh.cpp:102-201, with the Hilbert renumbering); reverse
+ * Cuthill-McKee runs on the host from the GPU's connectivity.  For large meshes: the host
+ * build of a 4M-cell mesh takes seconds. */
+cfdg_status cfdg_mesh_create_gpu(int n_nodes, const double* xy, int n_cells, const int* cells,
+                                 int n_bedges, const int* bedges, int renumber, int device, cfdg_mesh** out);
 /* Mesh::load (src/Mesh.cpp:10-26) on a Gmsh 2.2 ASCII file; LF and CRLF both accepted */
 cfdg_status cfdg_mesh_load_gmsh(const char* path, int renumber, cfdg_mesh** out);
 /* Mesh::getNumCells / getNumFaces (include/Mesh.hpp:25-27) */

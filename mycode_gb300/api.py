@@ -74,6 +74,7 @@ SIGNATURES = {
     "cfdg_config_default": (None, [C.POINTER(Config)]),
     "cfdg_mesh_create": (C.c_int, [C.c_int, _dp, C.c_int, _ip, C.c_int, _vp, C.c_int, C.POINTER(_vp)]),
     "cfdg_mesh_load_gmsh": (C.c_int, [C.c_char_p, C.c_int, C.POINTER(_vp)]),
+    "cfdg_mesh_create_gpu": (C.c_int, [C.c_int, _dp, C.c_int, _ip, C.c_int, _vp, C.c_int, C.c_int, C.POINTER(_vp)]),
     "cfdg_mesh_sizes": (C.c_int, [_vp, C.POINTER(C.c_int), C.POINTER(C.c_int), C.POINTER(C.c_int)]),
     "cfdg_mesh_faces": (C.c_int, [_vp, _ip, _dp]),
     "cfdg_mesh_cells": (C.c_int, [_vp, _dp]),
@@ -202,15 +203,21 @@ class Mesh:
         self.n_cells, self.n_faces, self.n_boundary_faces = nc.value, nf.value, nb.value
 
     @classmethod
-    def from_spec(cls, spec, renumber="hilbert") -> "Mesh":
+    def from_spec(cls, spec, renumber="hilbert", gpu=None) -> "Mesh":
+        """The mesh of a spec; gpu = a device ordinal builds it with kernels on that GPU
+        (cfdg_mesh_create_gpu, the same mesh bit for bit), None on the host."""
         xy = np.ascontiguousarray(spec.nodes, dtype=np.float64).ravel()
         cells = np.ascontiguousarray(spec.cells, dtype=np.int32).ravel()
         bed = np.ascontiguousarray(spec.bedges, dtype=np.int32).ravel()
         h = _vp()
-        _check(lib().cfdg_mesh_create(spec.n_nodes, xy, spec.n_cells, cells, spec.bedges.shape[0],
-                                      bed.ctypes.data_as(_vp) if bed.size else None,
-                                      RENUMBER[renumber] if isinstance(renumber, str) else int(renumber),
-                                      C.byref(h)))
+        ren = RENUMBER[renumber] if isinstance(renumber, str) else int(renumber)
+        bptr = bed.ctypes.data_as(_vp) if bed.size else None
+        if gpu is None:
+            _check(lib().cfdg_mesh_create(spec.n_nodes, xy, spec.n_cells, cells, spec.bedges.shape[0], bptr, ren,
+                                          C.byref(h)))
+        else:
+            _check(lib().cfdg_mesh_create_gpu(spec.n_nodes, xy, spec.n_cells, cells, spec.bedges.shape[0], bptr, ren,
+                                              int(gpu), C.byref(h)))
         m = cls(h)
         m._keep = (xy, cells, bed)
         return m

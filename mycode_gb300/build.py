@@ -9,6 +9,7 @@ Translation units and their floating-point contracts:
   noalloc.cu   nvcc --fmad=false  (residual norm with static scratch, no allocation)
   kern_adj.cu  nvcc               (adjoint / VJP of the FP64 residual)
   kern_qoi.cu  nvcc --fmad=false  (wall distance, Cp/Cf, drag, entropy error)
+  mesh_gpu.cu  nvcc --fmad=false  (mesh connectivity, geometry and renumbering on the GPU)
   mesh.cpp     g++ -ffp-contract=off (host geometry bit-exact on x86 and Arm)
 Compiles in parallel, links with nvcc (static cudart).
 """
@@ -33,6 +34,7 @@ CU = {
     "noalloc.cu": ["--fmad=false"],
     "kern_adj.cu": [],
     "kern_qoi.cu": ["--fmad=false"],
+    "mesh_gpu.cu": ["--fmad=false"],
 }
 CPP = ["mesh.cpp"]
 

@@ -10,11 +10,13 @@ static void residual_nv(const ResArgs<double>& a) {
     if (a.ev) cudaEventRecord(a.ev[0], a.stream);
     k_prim<double, NV><<<blocks_for(nc), tpb_for(nc), 0, a.stream>>>((int)nc, a.F, a.U, a.W);
     if (a.ev) cudaEventRecord(a.ev[1], a.stream);
-    k_grad<double, NV><<<blocks_for(nc), tpb_for(nc), 0, a.stream>>>(a.m, a.F, a.U, a.W, a.G, a.phi, a.do_limiter, nullptr,
-                                                                    a.lim_dev);
+    k_grad64<NV><<<blocks_for(nc), tpb_for(nc), 0, a.stream>>>(a.m, a.F, a.U, a.W, a.G, a.phi, a.do_limiter, a.lim_dev);
     if (NV == 6) k_sst_cell<double, NV><<<blocks_for(nc), tpb_for(nc), 0, a.stream>>>(a.m, a.F, a.W, a.G, a.dwall, a.T, nullptr);
     if (a.ev) cudaEventRecord(a.ev[2], a.stream);
-    k_flux<double, NV><<<blocks_for(nf), tpb_for(nf), 0, a.stream>>>(a.m, a.F, a.U, a.W, a.G, a.phi, a.FA, a.T, nullptr);
+    {
+        const unsigned t = tpb_for(nf) < FLUX64_THREADS ? tpb_for(nf) : FLUX64_THREADS;
+        k_flux64<NV><<<grid_for(nf, (int)t), t, 0, a.stream>>>(a.m, a.F, a.U, a.W, a.G, a.phi, a.FA, a.T);
+    }
     if (a.ev) cudaEventRecord(a.ev[3], a.stream);
     if (a.norms_out)
         k_gather_norms<NV><<<red_grid(nc), RED_THREADS, 0, a.stream>>>(a.m, a.FA.v, a.FA.n, a.out,

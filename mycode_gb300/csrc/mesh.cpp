@@ -103,6 +103,8 @@ void order_rcm(const HostMesh& m, std::vector<int>& perm) {
 
 }  // namespace
 
+void order_rcm_host(const HostMesh& m, std::vector<int>& perm) { order_rcm(m, perm); }
+
 std::string build_mesh(HostMesh& m, int n_nodes, const double* xy, int n_cells, const int* cells,
                        int n_bedges, const int* bedges, int renumber) {
     if (n_nodes <= 0 || n_cells <= 0) return "mesh has no nodes or no cells";

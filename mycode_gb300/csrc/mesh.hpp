@@ -32,6 +32,12 @@ struct HostMesh {
 std::string build_mesh(HostMesh& m, int n_nodes, const double* xy, int n_cells, const int* cells,
                        int n_bedges, const int* bedges, int renumber);
 
+// The same mesh built by kernels on `device` (mesh_gpu.cu): connectivity, geometry, the
+// Hilbert renumbering and the device layout; the same HostMesh bit for bit.  *seconds (may
+// be null) gets the device time of the build.
+std::string build_mesh_gpu(HostMesh& m, int n_nodes, const double* xy, int n_cells, const int* cells,
+                           int n_bedges, const int* bedges, int renumber, int device, double* seconds);
+
 // Gmsh 2.2 ASCII reader (LF or CRLF line ends).
 std::string read_gmsh(const std::string& path, std::vector<double>& xy, std::vector<int>& cells,
                       std::vector<int>& bedges);

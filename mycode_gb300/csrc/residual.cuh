@@ -384,6 +384,36 @@ __global__ void __launch_bounds__(256) k_flux(MeshView<R> m, Flow<R> F, Field<R>
     flux_item<S, NV>(m, F, U, W, G, phi, FA, T, f, done);
 }
 
+// The FP64 residual's gradient and face-flux kernels: grad_item / flux_item under launch
+// bounds that keep more warps resident than the shared templates' 256-thread bound (which
+// lets the compiler take 149 / 181 registers: one block, eight warps per SM).  Both kernels
+// are bound by GB300's FP64 pipe, whose long instruction latencies need more warps per
+// sub-partition.  Measured on the 4M-cell SST bump: gradients 4.81 -> 4.51 ms with at
+// least two 256-thread blocks per SM (128 registers), face fluxes 6.32 -> 5.86 ms with at
+// least three 128-thread blocks (170 registers); 128-thread blocks x 3 for the gradients
+// 4.55 ms, 64-thread blocks x 5-6 the same as x 3.
+template <int NV>
+__global__ void __launch_bounds__(256, 2) k_grad64(MeshView<double> m, Flow<double> F, Field<double> U,
+                                                   Field<double> W, Field<double> G, double* phi, int do_limiter,
+                                                   const int* lim_dev) {
+    long i = (long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= m.nc) return;
+    if (lim_dev && !*lim_dev) do_limiter = 0;
+    grad_item<double, NV>(m, F, U, W, G, phi, do_limiter, i, nullptr);
+}
+
+constexpr unsigned FLUX64_THREADS = 128;
+
+template <int NV>
+__global__ void __launch_bounds__(FLUX64_THREADS, 3) k_flux64(MeshView<double> m, Flow<double> F, Field<double> U,
+                                                              Field<double> W, Field<double> G,
+                                                              const double* __restrict__ phi, Field<double> FA,
+                                                              Field<double> T) {
+    long f = (long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (f >= m.nf) return;
+    flux_item<double, NV>(m, F, U, W, G, phi, FA, T, f, nullptr);
+}
+
 // ---------------------------------------------------------------- k_gather
 // R_i = sum over the cell's faces, in reference face order, of +F*A (owner) or -F*A
 // (neighbour) (src/Solver.cpp:795-799).  Optionally adds diag_v * vol/(dt + 1e-30)

@@ -1542,6 +1542,25 @@ cfdg_status cfdg_mesh_create(int n_nodes, const double* xy, int n_cells, const i
     return CFDG_OK;
 }
 
+cfdg_status cfdg_mesh_create_gpu(int n_nodes, const double* xy, int n_cells, const int* cells, int n_bedges,
+                                 const int* bedges, int renumber, int device, cfdg_mesh** out) {
+    if (!out || !xy || !cells || (n_bedges > 0 && !bedges) || n_nodes <= 0 || n_cells <= 0 || n_bedges < 0)
+        return fail(CFDG_ERR_ARG, "cfdg_mesh_create_gpu: bad arguments");
+    int ndev = 0;
+    if (cudaGetDeviceCount(&ndev) != cudaSuccess || device < 0 || device >= ndev) {
+        cudaGetLastError();
+        return fail(CFDG_ERR_CUDA, "cfdg_mesh_create_gpu: no such CUDA device");
+    }
+    cfdg_mesh* m = new cfdg_mesh();
+    std::string e = build_mesh_gpu(m->h, n_nodes, xy, n_cells, cells, n_bedges, bedges, renumber, device, nullptr);
+    if (!e.empty()) {
+        delete m;
+        return fail(e.rfind("GPU mesh build:", 0) == 0 ? CFDG_ERR_CUDA : CFDG_ERR_MESH, e);
+    }
+    *out = m;
+    return CFDG_OK;
+}
+
 cfdg_status cfdg_mesh_load_gmsh(const char* path, int renumber, cfdg_mesh** out) {
     if (!path || !out) return fail(CFDG_ERR_ARG, "cfdg_mesh_load_gmsh: null argument");
     std::vector<double> xy;
