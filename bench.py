@@ -348,8 +348,8 @@ def fp64_roofline_row(cls, avg_ms, nc, nf, peak_gbs, pipe_peak_warp, pipe_prof):
     units = nf if kind == "flux" else nc
     row = {"avg_us": round(avg_ms * 1e3, 2), "algorithmic_bytes": int(b),
            "hbm_gbs": round(b / (avg_ms * 1e-3) / 1e9, 1), "hbm_frac": round(b / (avg_ms * 1e-3) / 1e9 / peak_gbs, 4),
-           # the gather only adds face fluxes: memory-bound, the other classes FP64-pipe-bound
-           "bound": "hbm" if kind == "gather" else "fp64_pipe"}
+           # every class of the FP64 residual is bound by the FP64 pipe (ncu: 79-89 % busy)
+           "bound": "fp64_pipe"}
     p = pipe_prof.get(cls)
     if p:
         inst = p["fp64_warp_inst_per_unit"] * units

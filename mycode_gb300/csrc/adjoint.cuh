@@ -321,13 +321,17 @@ template <class R>
 CFD_HD void flux_hllc_b(const Flow<R>& F, const CS<R>& L, const CS<R>& Rt, R nx, R ny, const R* Fb, CSb<R>& Lb,
                         CSb<R>& Rb) {
     const R gm = F.gam - R(1.0);
+    // one reciprocal per divisor (the forward's quotients by rho, by sL + sR and the star
+    // state's, and every reverse quotient by the same values)
+    const R irL = R(1) / L.r, irR = R(1) / Rt.r;
     R unL = L.u * nx + L.v * ny, unR = Rt.u * nx + Rt.v * ny;
-    R cL = sqrt(F.gam * L.p / L.r), cR = sqrt(F.gam * Rt.p / Rt.r);
-    R hL = (L.rE + L.p) / L.r, hR = (Rt.rE + Rt.p) / Rt.r;
+    R cL = sqrt(F.gam * L.p * irL), cR = sqrt(F.gam * Rt.p * irR);
+    R hL = (L.rE + L.p) * irL, hR = (Rt.rE + Rt.p) * irR;
     R sL = sqrt(L.r), sR = sqrt(Rt.r);
     R S = sL + sR;
+    const R iS = R(1) / S;
     R nu_ = sL * L.u + sR * Rt.u, nv_ = sL * L.v + sR * Rt.v, nh_ = sL * hL + sR * hR;
-    R ut = nu_ / S, vt = nv_ / S, ht = nh_ / S;
+    R ut = nu_ * iS, vt = nv_ * iS, ht = nh_ * iS;
     R unt = ut * nx + vt * ny;
     R c2t = gm * (ht - R(0.5) * (ut * ut + vt * vt));
     R ct = sqrt(c2t);
@@ -349,14 +353,18 @@ CFD_HD void flux_hllc_b(const Flow<R>& F, const CS<R>& L, const CS<R>& Rt, R nx,
     const bool left = Ss >= R(0.0);
     const CS<R>& K = left ? L : Rt;
     CSb<R>& Kb = left ? Lb : Rb;
+    const R iK = left ? irL : irR;
+    const R iden = R(1) / den;
     R SK = left ? SL : SR;
     R unK = left ? unL : unR;
     R A = K.r * (SK - unK);
     R B = SK - Ss;
-    R coef = A / B;
+    const R iA = R(1) / A, iB = R(1) / B;
+    R coef = A * iB;
     R t = Ss - unK;
-    R q = K.p / A;
-    R e = K.rE / K.r + t * (Ss + q);
+    R q = K.p * iA;
+    const R eK = K.rE * iK;
+    R e = eK + t * (Ss + q);
     R Us[6] = {coef, coef * (K.u + t * nx), coef * (K.v + t * ny), coef * e, R(0), R(0)};
     R UK[6] = {K.r, K.ru, K.rv, K.rE, K.rk, K.rw};
     normal_flux_b(K, nx, ny, Fb, Kb);
@@ -369,13 +377,13 @@ CFD_HD void flux_hllc_b(const Flow<R>& F, const CS<R>& L, const CS<R>& Rt, R nx,
     // Us3 = coef e
     coefb += Usb[3] * e;
     R eb = Usb[3] * coef;
-    Kb.rE += eb / K.r;
-    Kb.r -= eb * K.rE / (K.r * K.r);
+    Kb.rE += eb * iK;
+    Kb.r -= eb * eK * iK;
     tb += eb * (Ss + q);
     Ssb += eb * t;
     R qb = eb * t;
-    Kb.p += qb / A;
-    Ab -= qb * q / A;
+    Kb.p += qb * iA;
+    Ab -= qb * q * iA;
     // Us2, Us1
     coefb += Usb[2] * (K.v + t * ny) + Usb[1] * (K.u + t * nx);
     Kb.v += Usb[2] * coef;
@@ -385,8 +393,8 @@ CFD_HD void flux_hllc_b(const Flow<R>& F, const CS<R>& L, const CS<R>& Rt, R nx,
     Ssb += tb;
     unKb -= tb;
     // coef = A / B, B = SK - Ss
-    Ab += coefb / B;
-    R Bb = -coefb * coef / B;
+    Ab += coefb * iB;
+    R Bb = -coefb * coef * iB;
     SKb += Bb;
     Ssb -= Bb;
     // A = K.r (SK - unK)
@@ -396,7 +404,7 @@ CFD_HD void flux_hllc_b(const Flow<R>& F, const CS<R>& L, const CS<R>& Rt, R nx,
     R SLb = left ? SKb : R(0), SRb = left ? R(0) : SKb;
     R unLb = left ? unKb : R(0), unRb = left ? R(0) : unKb;
     // Ss = num / den
-    R numb = Ssb / den, denb = -Ssb * Ss / den;
+    R numb = Ssb * iden, denb = -Ssb * Ss * iden;
     Rb.p += numb;
     Lb.p -= numb;
     Lb.r += numb * unL * (SL - unL) + denb * (SL - unL);
@@ -420,8 +428,8 @@ CFD_HD void flux_hllc_b(const Flow<R>& F, const CS<R>& L, const CS<R>& Rt, R nx,
     R utb = -gm * c2tb * ut + untb * nx;
     R vtb = -gm * c2tb * vt + untb * ny;
     // ut = nu_ / S
-    R nub = utb / S, nvb = vtb / S, nhb = htb / S;
-    R Sb = -(utb * ut + vtb * vt + htb * ht) / S;
+    R nub = utb * iS, nvb = vtb * iS, nhb = htb * iS;
+    R Sb = -(utb * ut + vtb * vt + htb * ht) * iS;
     R sLb = Sb + nub * L.u + nvb * L.v + nhb * hL;
     R sRb = Sb + nub * Rt.u + nvb * Rt.v + nhb * hR;
     Lb.u += nub * sL; Rb.u += nub * sR;
@@ -429,8 +437,8 @@ CFD_HD void flux_hllc_b(const Flow<R>& F, const CS<R>& L, const CS<R>& Rt, R nx,
     R hLb = nhb * sL, hRb = nhb * sR;
     Lb.r += sLb / (sL + sL);
     Rb.r += sRb / (sR + sR);
-    Lb.rE += hLb / L.r; Lb.p += hLb / L.r; Lb.r -= hLb * hL / L.r;
-    Rb.rE += hRb / Rt.r; Rb.p += hRb / Rt.r; Rb.r -= hRb * hR / Rt.r;
+    Lb.rE += hLb * irL; Lb.p += hLb * irL; Lb.r -= hLb * hL * irL;
+    Rb.rE += hRb * irR; Rb.p += hRb * irR; Rb.r -= hRb * hR * irR;
     sound_b(F, L, cL, cLb, Lb);
     sound_b(F, Rt, cR, cRb, Rb);
     Lb.u += unLb * nx; Lb.v += unLb * ny;
@@ -659,10 +667,11 @@ CFD_HD void face_flux_b(const Flow<R>& F, const CS<R>& L, const CS<R>& Rn, bool 
             }
         }
         R Cp = F.gam * F.Rgas / (F.gam - R(1.0));
+        const R CpPr = Cp * F.inv_Pr, CpPrt = Cp * F.inv_Prt;
         R mu = rf * F.nu;
-        R kc = mu * Cp / F.Pr;
+        R kc = mu * CpPr;
         if (F.sst) {
-            kc = kc + mutf * Cp / F.Pr_t;
+            kc = kc + mutf * CpPrt;
             mu = mu + mutf;
         }
         R div = dudx + dvdy;
@@ -683,8 +692,8 @@ CFD_HD void face_flux_b(const Flow<R>& F, const CS<R>& L, const CS<R>& Rn, bool 
         // mu (and kc) of the stresses include mu_t with SST; the laminar part is rf nu
         R mufb = txxb * (R(2.0) * dudx - (R(2.0) / R(3.0)) * div) + tyyb * (R(2.0) * dvdy - (R(2.0) / R(3.0)) * div) +
                  txyb * (dudy + dvdx);
-        R mub = kcb * Cp / F.Pr + mufb;
-        if (F.sst && mutfb) *mutfb += mufb + kcb * Cp / F.Pr_t;
+        R mub = kcb * CpPr + mufb;
+        if (F.sst && mutfb) *mutfb += mufb + kcb * CpPrt;
         R divb = -(R(2.0) / R(3.0)) * mu * (txxb + tyyb);
         R dudxb = R(2.0) * mu * txxb + divb;
         R dvdyb = R(2.0) * mu * tyyb + divb;

@@ -231,9 +231,10 @@ __global__ void __launch_bounds__(128) k_adj_cell1(MeshView<double> m, Flow<doub
         if (win >= 0 && win_ratio) {
             double ab = phb;
             double den = win_d2 > 0.0 ? win_d2 + eps : win_d2 - eps;
-            double extb = ab / den;  // adjoint of pmax (or pmin)
-            double pcb = -ab / den;
-            double d2b = -ab * win_a / den;
+            const double iden = 1.0 / den;
+            double extb = ab * iden;  // adjoint of pmax (or pmin)
+            double pcb = -ab * iden;
+            double d2b = -ab * win_a * iden;
             double Pfb = d2b;
             pcb -= d2b;
             wb[W_R] += Pfb * F.Rgas * (Tc + 1.0 * (gTx * win_dx + gTy * win_dy));

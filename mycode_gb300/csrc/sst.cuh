@@ -51,12 +51,15 @@ CFD_HD SstCell<S> sst_cell(const Flow<R>& F, S r, S k, S w, S ux, S uy, S vx, S 
     S Smag = sqrt(S2 + S(R(1e-30)));
     S nu = S(F.nu);
     R dd = d > R(1e-30) ? d : R(1e-30);
+    // one reciprocal per divisor (w, d, CD_kw, the eddy viscosity's denominator)
+    const S iwp = R(1) / wp;
+    const R idd = R(1) / dd;
     S gkgw = kx * wx + ky * wy;
-    S CDkw = smax(R(2) * r * R(C::sw2) * gkgw / wp, S(R(1e-10)));
+    S CDkw = smax(R(2) * r * R(C::sw2) * gkgw * iwp, S(R(1e-10)));
     S sk = sqrt(kp + S(R(1e-30)));
-    S t1 = sk / (bs * wp * dd);
-    S t2 = R(500) * nu / (dd * dd * wp);
-    S arg1 = smin(smax(t1, t2), R(4) * r * R(C::sw2) * kp / (CDkw * dd * dd));
+    S t1 = sk * iwp * (idd / bs);
+    S t2 = R(500) * nu * iwp * (idd * idd);
+    S arg1 = smin(smax(t1, t2), R(4) * r * R(C::sw2) * kp / CDkw * (idd * idd));
     // tanh(x) is 1 to double precision for x > 20: capping the arguments there changes no
     // value and keeps arg^4 (up to 1e45 next to a wall) inside FP32 range
     arg1 = smin(arg1, S(R(10)));
@@ -72,7 +75,7 @@ CFD_HD SstCell<S> sst_cell(const Flow<R>& F, S r, S k, S w, S ux, S uy, S vx, S 
     o.mut = mut;
     o.F1 = F1;
     o.Sk = P - bs * r * wp * kp;
-    o.Sw = gam * r / (mut + S(R(1e-30))) * P - beta * r * wp * wp + R(2) * (R(1) - F1) * r * R(C::sw2) * gkgw / wp;
+    o.Sw = gam * r / (mut + S(R(1e-30))) * P - beta * r * wp * wp + R(2) * (R(1) - F1) * r * R(C::sw2) * gkgw * iwp;
     return o;
 }
 
@@ -138,15 +141,17 @@ CFD_HD void sst_cell_b(const Flow<R>& F, R r, R k, R w, R ux, R uy, R vx, R vy, 
     R nu = F.nu;
     R dd = d > R(1e-30) ? d : R(1e-30);
     R gkgw = kx * wx + ky * wy;
-    R CDa = R(2) * r * sw2 * gkgw / wp;
+    const R iwp = R(1) / wp, idd = R(1) / dd;  // the forward's reciprocals (sst_cell)
+    R CDa = R(2) * r * sw2 * gkgw * iwp;
     bool cdclip = CDa < R(1e-10);
     R CDkw = cdclip ? R(1e-10) : CDa;
+    const R iCD = R(1) / CDkw;
     R sk = sqrt(kp + R(1e-30));
-    R t1 = sk / (bs * wp * dd);
-    R t2 = R(500) * nu / (dd * dd * wp);
+    R t1 = sk * iwp * (idd / bs);
+    R t2 = R(500) * nu * iwp * (idd * idd);
     bool m1t2 = t1 < t2;
     R m1 = m1t2 ? t2 : t1;
-    R t3 = R(4) * r * sw2 * kp / (CDkw * dd * dd);
+    R t3 = R(4) * r * sw2 * kp * iCD * (idd * idd);
     bool a1t3 = t3 < m1;
     R arg1u = a1t3 ? t3 : m1;
     bool a1cap = R(10) < arg1u;
@@ -161,27 +166,29 @@ CFD_HD void sst_cell_b(const Flow<R>& F, R r, R k, R w, R ux, R uy, R vx, R vy, 
     R da = a1 * wp, ds = Smag * F2;
     bool dens = da < ds;
     R den = dens ? ds : da;
-    R mut = r * a1 * kp / den;
+    const R iden = R(1) / den;
+    R mut = r * a1 * kp * iden;
     R beta = F1 * R(C::b1) + (R(1) - F1) * R(C::b2);
     R gam = F1 * R(C::g1) + (R(1) - F1) * R(C::g2);
     R Pu = mut * S2, Pl = R(10) * bs * r * kp * wp;
     bool plim = Pl < Pu;
     R P = plim ? Pl : Pu;
     R me = mut + R(1e-30);
+    const R ime = R(1) / me;
     // reverse
     R rb_ = 0, kpb = 0, wpb = 0, Pb = 0, gamb = 0, betab = 0, gkgwb = 0;
     R mutb_ = mutb, F1b_ = F1b;
-    gamb += Swb * r / me * P;
-    rb_ += Swb * gam / me * P;
-    mutb_ -= Swb * gam * r * P / (me * me);
-    Pb += Swb * gam * r / me;
+    gamb += Swb * r * ime * P;
+    rb_ += Swb * gam * ime * P;
+    mutb_ -= Swb * gam * r * P * ime * ime;
+    Pb += Swb * gam * r * ime;
     betab -= Swb * r * wp * wp;
     rb_ -= Swb * beta * wp * wp;
     wpb -= Swb * R(2) * beta * r * wp;
-    F1b_ -= Swb * R(2) * r * sw2 * gkgw / wp;
-    rb_ += Swb * R(2) * (R(1) - F1) * sw2 * gkgw / wp;
-    gkgwb += Swb * R(2) * (R(1) - F1) * r * sw2 / wp;
-    wpb -= Swb * R(2) * (R(1) - F1) * r * sw2 * gkgw / (wp * wp);
+    F1b_ -= Swb * R(2) * r * sw2 * gkgw * iwp;
+    rb_ += Swb * R(2) * (R(1) - F1) * sw2 * gkgw * iwp;
+    gkgwb += Swb * R(2) * (R(1) - F1) * r * sw2 * iwp;
+    wpb -= Swb * R(2) * (R(1) - F1) * r * sw2 * gkgw * iwp * iwp;
     Pb += Skb;
     rb_ -= Skb * bs * wp * kp;
     wpb -= Skb * bs * r * kp;
@@ -196,9 +203,9 @@ CFD_HD void sst_cell_b(const Flow<R>& F, R r, R k, R w, R ux, R uy, R vx, R vy, 
         S2b += Pb * mut;
     }
     F1b_ += betab * (R(C::b1) - R(C::b2)) + gamb * (R(C::g1) - R(C::g2));
-    rb_ += mutb_ * a1 * kp / den;
-    kpb += mutb_ * r * a1 / den;
-    R denb = -mutb_ * mut / den;
+    rb_ += mutb_ * a1 * kp * iden;
+    kpb += mutb_ * r * a1 * iden;
+    R denb = -mutb_ * mut * iden;
     R Smagb = 0, F2b = 0;
     if (dens) {
         Smagb += denb * F2;
@@ -216,19 +223,19 @@ CFD_HD void sst_cell_b(const Flow<R>& F, R r, R k, R w, R ux, R uy, R vx, R vy, 
     if (a1t3) t3b += arg1b;
     else m1b += arg1b;
     R CDkwb = 0;
-    rb_ += t3b * R(4) * sw2 * kp / (CDkw * dd * dd);
-    kpb += t3b * R(4) * r * sw2 / (CDkw * dd * dd);
-    CDkwb -= t3b * t3 / CDkw;
+    rb_ += t3b * R(4) * sw2 * kp * iCD * (idd * idd);
+    kpb += t3b * R(4) * r * sw2 * iCD * (idd * idd);
+    CDkwb -= t3b * t3 * iCD;
     if (m1t2) t2b += m1b;
     else t1b += m1b;
-    wpb -= t2b * t2 / wp;
-    R skb = t1b / (bs * wp * dd);
-    wpb -= t1b * t1 / wp;
+    wpb -= t2b * t2 * iwp;
+    R skb = t1b * iwp * (idd / bs);
+    wpb -= t1b * t1 * iwp;
     kpb += skb / (sk + sk);
     if (!cdclip) {
-        rb_ += CDkwb * R(2) * sw2 * gkgw / wp;
-        gkgwb += CDkwb * R(2) * r * sw2 / wp;
-        wpb -= CDkwb * CDa / wp;
+        rb_ += CDkwb * R(2) * sw2 * gkgw * iwp;
+        gkgwb += CDkwb * R(2) * r * sw2 * iwp;
+        wpb -= CDkwb * CDa * iwp;
     }
     kxb += gkgwb * wx;
     wxb += gkgwb * kx;
@@ -263,9 +270,10 @@ CFD_HD void sst_face_flux_b(const Flow<R>& F, R mdotA, R kL, R wL, R kR, R wR, R
     R d2w = dxL * dxL + dyL * dyL, dnw = dxL * nx + dyL * ny;
     R kx = 0, ky = 0, wx = 0, wy = 0, d2 = dxlr * dxlr + dylr * dylr;
     bool corr = !wall && d2 > R(1e-14);
+    const R id2w = wall ? R(1) / d2w : R(0), id2 = corr ? R(1) / d2 : R(0);
     if (wall) {
-        dkn = (R(0) - kL) * dnw / d2w;
-        dwn = (R(0.5) * (wL + wR) - wL) * dnw / d2w;
+        dkn = (R(0) - kL) * dnw * id2w;
+        dwn = (R(0.5) * (wL + wR) - wL) * dnw * id2w;
     } else {
         kx = R(0.5) * (gkL[0] + gkR[0]);
         ky = R(0.5) * (gkL[1] + gkR[1]);
@@ -273,8 +281,8 @@ CFD_HD void sst_face_flux_b(const Flow<R>& F, R mdotA, R kL, R wL, R kR, R wR, R
         wy = R(0.5) * (gkL[3] + gkR[3]);
         R kxc = kx, kyc = ky, wxc = wx, wyc = wy;
         if (corr) {
-            R ck = (kx * dxlr + ky * dylr - (kR - kL)) / d2;
-            R cw = (wx * dxlr + wy * dylr - (wR - wL)) / d2;
+            R ck = (kx * dxlr + ky * dylr - (kR - kL)) * id2;
+            R cw = (wx * dxlr + wy * dylr - (wR - wL)) * id2;
             kxc = kx - ck * dxlr;
             kyc = ky - ck * dylr;
             wxc = wx - cw * dxlr;
@@ -299,22 +307,23 @@ CFD_HD void sst_face_flux_b(const Flow<R>& F, R mdotA, R kL, R wL, R kR, R wR, R
     if (!mneg) mdotAb += mpb;
     if (!mpos) mdotAb += mmb;
     if (wall) {
-        kLb -= dknb * dnw / d2w;
-        R t = dwnb * dnw / d2w;
+        kLb -= dknb * dnw * id2w;
+        R t = dwnb * dnw * id2w;
         wLb += t * (R(0.5) - R(1));
         wRb += t * R(0.5);
     } else {
         R kxb = dknb * nx, kyb = dknb * ny, wxb = dwnb * nx, wyb = dwnb * ny;
         if (corr) {
             R ckb = -(kxb * dxlr + kyb * dylr), cwb = -(wxb * dxlr + wyb * dylr);
-            kxb += ckb * dxlr / d2;
-            kyb += ckb * dylr / d2;
-            kRb -= ckb / d2;
-            kLb += ckb / d2;
-            wxb += cwb * dxlr / d2;
-            wyb += cwb * dylr / d2;
-            wRb -= cwb / d2;
-            wLb += cwb / d2;
+            const R ckd = ckb * id2, cwd = cwb * id2;
+            kxb += ckd * dxlr;
+            kyb += ckd * dylr;
+            kRb -= ckd;
+            kLb += ckd;
+            wxb += cwd * dxlr;
+            wyb += cwd * dylr;
+            wRb -= cwd;
+            wLb += cwd;
         }
         gkLb[0] += R(0.5) * kxb;
         gkRb[0] += R(0.5) * kxb;
