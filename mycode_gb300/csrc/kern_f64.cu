@@ -78,6 +78,13 @@ void launch_soa_to_aos<double>(long nc, int np, int stride, const double* soa, c
     k_soa_to_aos<double><<<blocks_for(nc), tpb_for(nc), 0, s>>>(nc, np, stride, soa, perm, aos);
 }
 
+void launch_aos_rows_to_soa(long nc, int np, int stride, const double* aos, const int* inv, double* soa, cudaStream_t s) {
+    k_aos_rows_to_soa<double><<<blocks_for(nc), tpb_for(nc), 0, s>>>(nc, np, stride, aos, inv, soa);
+}
+void launch_soa_to_aos_rows(long nc, int np, int stride, const double* soa, const int* inv, double* aos, cudaStream_t s) {
+    k_soa_to_aos_rows<double><<<blocks_for(nc), tpb_for(nc), 0, s>>>(nc, np, stride, soa, inv, aos);
+}
+
 void launch_fd_perturb(long n, const double* U, const double* v, const double* u_sq, const double* v_sq, double* Up,
                        double* eps, cudaStream_t s) {
     k_fd_perturb<<<red_grid(n), RED_THREADS, 0, s>>>(n, U, v, u_sq, v_sq, Up, eps);

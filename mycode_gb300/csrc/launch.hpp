@@ -80,6 +80,10 @@ template <class T> void launch_aos_to_soa(long nc, int np, int stride, const dou
 template <class T> void launch_soa_to_aos(long nc, int np, int stride, const T* soa, const int* perm, double* aos,
                                           cudaStream_t s);
 template <class T> void launch_convert(long n, const double* in, T* out, cudaStream_t s);
+// the renumberings one thread per caller's row (inv: new index of each row), for an AoS
+// array the device reads or writes in place
+void launch_aos_rows_to_soa(long nc, int np, int stride, const double* aos, const int* inv, double* soa, cudaStream_t s);
+void launch_soa_to_aos_rows(long nc, int np, int stride, const double* soa, const int* inv, double* aos, cudaStream_t s);
 
 // ---- FP64 only (kern_f64.cu)
 void launch_prim64(int nv, long nc, const Flow<double>& F, Field<double> U, Field<double> W, cudaStream_t s);

@@ -740,4 +740,25 @@ __global__ void k_soa_to_aos(long nc, int np, int stride, const T* __restrict__ 
     for (int c = 0; c < stride; ++c) aos[dst + c] = c < np ? (double)soa[c * nc + i] : 0.0;
 }
 
+// The same two renumberings one thread per row of the AoS array (the caller's cell order,
+// inv = the new index of each): the AoS side is read or written in order, which is what
+// a kernel needs that works on the caller's pinned host buffer in place (over the
+// CPU-GPU link, without a staging copy); the SoA side takes the scattered accesses.
+template <class T>
+__global__ void k_aos_rows_to_soa(long nc, int np, int stride, const double* __restrict__ aos,
+                                  const int* __restrict__ inv, T* __restrict__ soa) {
+    long j = (long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (j >= nc) return;
+    const long i = inv[j];
+    for (int c = 0; c < np; ++c) soa[c * nc + i] = (T)aos[j * stride + c];
+}
+template <class T>
+__global__ void k_soa_to_aos_rows(long nc, int np, int stride, const T* __restrict__ soa,
+                                  const int* __restrict__ inv, double* __restrict__ aos) {
+    long j = (long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (j >= nc) return;
+    const long i = inv[j];
+    for (int c = 0; c < stride; ++c) aos[j * stride + c] = c < np ? (double)soa[c * nc + i] : 0.0;
+}
+
 }  // namespace cfdg

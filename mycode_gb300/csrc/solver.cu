@@ -102,7 +102,7 @@ struct cfdg_solver {
     Flow<double> F;
     Flow<float> Ff;
     // device mesh
-    int *cf = nullptr, *fo = nullptr, *fn = nullptr, *ftag = nullptr, *perm = nullptr;
+    int *cf = nullptr, *fo = nullptr, *fn = nullptr, *ftag = nullptr, *perm = nullptr, *pinv = nullptr;
     GeoBuf<double> g64;
     GeoBuf<float> g32;
     MeshView<double> mv;
@@ -330,20 +330,50 @@ struct cfdg_solver {
         return CFDG_OK;
     }
 
+    // The device's view of a caller's host buffer when it is pinned (page-locked and mapped:
+    // cudaHostAlloc / cudaHostRegister memory, which the GPU reads and writes over the
+    // CPU-GPU link at its own address), else null: pageable memory goes through the
+    // staging buffer and the copy engines.
+    static const double* mapped_view(const double* host) {
+        cudaPointerAttributes a;
+        if (cudaPointerGetAttributes(&a, host) != cudaSuccess) {
+            cudaGetLastError();
+            return nullptr;
+        }
+        return a.type == cudaMemoryTypeHost && a.devicePointer ? static_cast<const double*>(a.devicePointer) : nullptr;
+    }
+
+    // A caller's AoS array (reference numbering, 6 per cell) into np SoA planes (new
+    // numbering).  A pinned buffer is read in place by the renumbering kernel, in row
+    // order (one transfer over the link, no staging copy); otherwise it is copied to the
+    // staging buffer first.  Either way the call only enqueues: the caller's entry point
+    // synchronises before it returns.
     cfdg_status upload_aos(const double* host, double* dev_soa, int np = -1) {
         if (np < 0) np = nv;
-        CK(cudaMemcpyAsync(stage, host, sizeof(double) * 6 * (size_t)nc, cudaMemcpyHostToDevice, st));
-        launch_aos_to_soa<double>(nc, np, 6, stage, perm, dev_soa, st);
+        if (const double* dv = mapped_view(host)) {
+            launch_aos_rows_to_soa(nc, np, 6, dv, pinv, dev_soa, st);
+        } else {
+            CK(cudaMemcpyAsync(stage, host, sizeof(double) * 6 * (size_t)nc, cudaMemcpyHostToDevice, st));
+            launch_aos_to_soa<double>(nc, np, 6, stage, perm, dev_soa, st);
+        }
         ++launches;
         CK(cudaGetLastError());
         return CFDG_OK;
     }
 
+    // np SoA planes into a caller's AoS array (stride doubles per cell, zeros past np): a
+    // pinned buffer is written in place by the renumbering kernel, in row order
     cfdg_status download_aos(const double* dev_soa, double* host, int np, int stride) {
-        launch_soa_to_aos<double>(nc, np, stride, dev_soa, perm, stage, st);
-        ++launches;
-        CK(cudaGetLastError());
-        CK(cudaMemcpyAsync(host, stage, sizeof(double) * stride * (size_t)nc, cudaMemcpyDeviceToHost, st));
+        if (double* dv = const_cast<double*>(mapped_view(host))) {
+            launch_soa_to_aos_rows(nc, np, stride, dev_soa, pinv, dv, st);
+            ++launches;
+            CK(cudaGetLastError());
+        } else {
+            launch_soa_to_aos<double>(nc, np, stride, dev_soa, perm, stage, st);
+            ++launches;
+            CK(cudaGetLastError());
+            CK(cudaMemcpyAsync(host, stage, sizeof(double) * stride * (size_t)nc, cudaMemcpyDeviceToHost, st));
+        }
         CK(cudaStreamSynchronize(st));
         collect();
         return CFDG_OK;
@@ -1454,7 +1484,7 @@ struct cfdg_solver {
         cudaFree(dinv64);
         void* pt[] = {Tt, Tj, Tjd, dwall, T32, T32d, dwall32};
         for (void* p : pt) cudaFree(p);
-        void* ps[] = {cf, fo, fn, ftag, perm, U, W, G, phi, FA, R, dt, D, stage, Ub, Rb, Up, Rp, vtmp, x, rhs,
+        void* ps[] = {cf, fo, fn, ftag, perm, pinv, U, W, G, phi, FA, R, dt, D, stage, Ub, Rb, Up, Rp, vtmp, x, rhs,
                       Wj, Wjd, Gj, Gjd, FAjd, U32, W32, W32d, G32, G32d, FA32d, phi32, dt32, V32, z32, V, z,
                       rs.partial, rs.counter, scal, bad};
         for (void* p : ps) cudaFree(p);
@@ -1660,11 +1690,13 @@ cfdg_status cfdg_solver_create(const cfdg_mesh* m, const cfdg_config* cfg, cfdg_
     TRYS(dalloc(&s->fn, nf));
     TRYS(dalloc(&s->ftag, nf));
     TRYS(dalloc(&s->perm, nc));
+    TRYS(dalloc(&s->pinv, nc));
     if (cudaMemcpy(s->cf, h.cf.data(), sizeof(int) * 4 * (size_t)nc, cudaMemcpyHostToDevice) != cudaSuccess ||
         cudaMemcpy(s->fo, h.fo.data(), sizeof(int) * nf, cudaMemcpyHostToDevice) != cudaSuccess ||
         cudaMemcpy(s->fn, h.fn.data(), sizeof(int) * nf, cudaMemcpyHostToDevice) != cudaSuccess ||
         cudaMemcpy(s->ftag, h.ftag.data(), sizeof(int) * nf, cudaMemcpyHostToDevice) != cudaSuccess ||
-        cudaMemcpy(s->perm, h.cell_perm.data(), sizeof(int) * nc, cudaMemcpyHostToDevice) != cudaSuccess)
+        cudaMemcpy(s->perm, h.cell_perm.data(), sizeof(int) * nc, cudaMemcpyHostToDevice) != cudaSuccess ||
+        cudaMemcpy(s->pinv, h.cell_inv.data(), sizeof(int) * nc, cudaMemcpyHostToDevice) != cudaSuccess)
         return bail(fail(CFDG_ERR_CUDA, "mesh upload failed"));
     TRYS(upload_geo(s->g64, h));
     TRYS(upload_geo(s->g32, h));
