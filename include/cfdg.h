@@ -108,6 +108,15 @@ typedef struct cfdg_config {
      * host synchronisation per chain (the CFL control on the device between the steps;
      * the same trace for any value); 1 = one synchronisation per step.  Default 8. */
     int newton_chain;
+    /* Start-up aids for stiff cases, no reference counterpart, off (0) by default so the
+     * reference's algorithm is untouched.  Graph driver only.
+     * startup_first_order: the first this many Newton steps of a solve use the first-order
+     *   scheme, then the configured one.
+     * update_limit: each cell's Newton update is scaled so that its density and (to first
+     *   order) pressure change by at most this fraction, and with SST rho k and rho w fall
+     *   by at most this fraction (e.g. 0.2). */
+    int startup_first_order;
+    double update_limit;
 } cfdg_config;
 
 /* CFDG_KRYLOV_STREAM launches the graph driver's kernels one iteration at a time from a

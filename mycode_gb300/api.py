@@ -47,7 +47,8 @@ class Config(C.Structure):
         ("limiter_freeze_step", C.c_int), ("limiter_freeze_cfl", C.c_double),
         ("turb_intensity", C.c_double), ("mut_ratio", C.c_double), ("shock_deflection_deg", C.c_double),
         ("renumber", C.c_int), ("device", C.c_int), ("krylov", C.c_int), ("persistent", C.c_int), ("pdl", C.c_int),
-        ("barrier_poll_limit", C.c_int), ("newton_chain", C.c_int),
+        ("barrier_poll_limit", C.c_int), ("newton_chain", C.c_int), ("startup_first_order", C.c_int),
+        ("update_limit", C.c_double),
     ]
 
 

@@ -78,13 +78,6 @@ void launch_soa_to_aos<double>(long nc, int np, int stride, const double* soa, c
     k_soa_to_aos<double><<<blocks_for(nc), tpb_for(nc), 0, s>>>(nc, np, stride, soa, perm, aos);
 }
 
-void launch_aos_rows_to_soa(long nc, int np, int stride, const double* aos, const int* inv, double* soa, cudaStream_t s) {
-    k_aos_rows_to_soa<double><<<blocks_for(nc), tpb_for(nc), 0, s>>>(nc, np, stride, aos, inv, soa);
-}
-void launch_soa_to_aos_rows(long nc, int np, int stride, const double* soa, const int* inv, double* aos, cudaStream_t s) {
-    k_soa_to_aos_rows<double><<<blocks_for(nc), tpb_for(nc), 0, s>>>(nc, np, stride, soa, inv, aos);
-}
-
 void launch_fd_perturb(long n, const double* U, const double* v, const double* u_sq, const double* v_sq, double* Up,
                        double* eps, cudaStream_t s) {
     k_fd_perturb<<<red_grid(n), RED_THREADS, 0, s>>>(n, U, v, u_sq, v_sq, Up, eps);
@@ -105,9 +98,10 @@ void launch_local_dt(int nv, const MeshView<double>& m, const Flow<double>& F, c
     NV_SWITCH(nv, (k_local_dt<NVC><<<blocks_for(m.nc), tpb_for(m.nc), 0, s>>>(m, F, U, W, cfl, dt, cfl_dev)));
 }
 void launch_newton_update_chain(int nv, long nc, double* U, const double* dU, const double* norms, double tol,
-                                double gam, double wmin, int* bad, const NewtonCtl& c, int k, int step, cudaStream_t s) {
+                                double gam, double wmin, int* bad, const NewtonCtl& c, int k, int step, double ulim,
+                                cudaStream_t s) {
     NV_SWITCH(nv, (k_newton_update_chain<NVC><<<blocks_for(nc), tpb_for(nc), 0, s>>>(nc, U, dU, norms, tol, gam, wmin,
-                                                                                     bad, c, k, step)));
+                                                                                     bad, c, k, step, ulim)));
 }
 void launch_precond(int nv, const MeshView<double>& m, const Flow<double>& F, const double* U, const double* W,
                     const double* dt, double* D, const double* mut, cudaStream_t s) {

@@ -80,10 +80,6 @@ template <class T> void launch_aos_to_soa(long nc, int np, int stride, const dou
 template <class T> void launch_soa_to_aos(long nc, int np, int stride, const T* soa, const int* perm, double* aos,
                                           cudaStream_t s);
 template <class T> void launch_convert(long n, const double* in, T* out, cudaStream_t s);
-// the renumberings one thread per caller's row (inv: new index of each row), for an AoS
-// array the device reads or writes in place
-void launch_aos_rows_to_soa(long nc, int np, int stride, const double* aos, const int* inv, double* soa, cudaStream_t s);
-void launch_soa_to_aos_rows(long nc, int np, int stride, const double* soa, const int* inv, double* aos, cudaStream_t s);
 
 // ---- FP64 only (kern_f64.cu)
 void launch_prim64(int nv, long nc, const Flow<double>& F, Field<double> U, Field<double> W, cudaStream_t s);
@@ -113,7 +109,7 @@ void launch_newton_update_dev(int nv, long nc, double* U, const double* dU, cons
                               double wmin, int* bad, cudaStream_t s);
 // the same update plus the step's scalar control on the device (step k of a chain)
 void launch_newton_update_chain(int nv, long nc, double* U, const double* dU, const double* norms, double tol,
-                                double gam, double wmin, int* bad, const NewtonCtl& c, int k, int step,
+                                double gam, double wmin, int* bad, const NewtonCtl& c, int k, int step, double ulim,
                                 cudaStream_t s);
 // time stepping: timeStepExplicit's update, solveUnsteady's right-hand side and update
 void launch_explicit_update(int nv, long nc, double* U, const double* R, const double* vol, double dt, int* bad,

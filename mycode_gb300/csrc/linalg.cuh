@@ -610,6 +610,28 @@ __device__ __forceinline__ void newton_control(const NewtonCtl& c, const double*
     c.ctl[2] = (c.limited && !((step + 1) > c.freeze_step || cf > c.freeze_cfl)) ? 1 : 0;
 }
 
+// Optional local limit of a Newton update (no reference counterpart; off unless the
+// caller asks, cfdg_config.update_limit): the cell's update du is scaled by the largest
+// a <= 1 with |a d rho| <= lim rho, |a dp| <= lim p (dp the update's pressure change to
+// first order) and, with SST, neither rho k nor rho w falling by more than lim of itself.
+template <int NV>
+__device__ __forceinline__ double update_scale(const double* u0, const double* du, double gam, double lim) {
+    if (!(lim > 0.0)) return 1.0;
+    double a = 1.0;
+    const double r = u0[0];
+    if (!(r > 0.0)) return 1.0;
+    const double ir = 1.0 / r, uu = u0[1] * ir, vv = u0[2] * ir;
+    const double p = (gam - 1.0) * (u0[3] - 0.5 * (u0[1] * uu + u0[2] * vv));
+    const double dp = (gam - 1.0) * (du[3] - uu * du[1] - vv * du[2] + 0.5 * (uu * uu + vv * vv) * du[0]);
+    if (fabs(du[0]) * a > lim * r) a = lim * r / fabs(du[0]);
+    if (p > 0.0 && fabs(dp) * a > lim * p) a = lim * p / fabs(dp);
+    if constexpr (NV == 6) {
+        for (int c = 4; c < 6; ++c)
+            if (u0[c] > 0.0 && du[c] < 0.0 && -du[c] * a > lim * u0[c]) a = lim * u0[c] / (-du[c]);
+    }
+    return a;
+}
+
 // k_newton_update_dev's update plus the scalar control in thread 0 of block 0 (chain
 // step k, the solve's step `step` when no earlier step of the chain stopped).  The other
 // threads take their converged / non-finite / relaxation decisions from the same norms,
@@ -617,7 +639,7 @@ __device__ __forceinline__ void newton_control(const NewtonCtl& c, const double*
 template <int NV>
 __global__ void k_newton_update_chain(long nc, double* __restrict__ U, const double* __restrict__ dU,
                                       const double* __restrict__ norms, double tol, double gam, double wmin, int* bad,
-                                      NewtonCtl c, int k, int step) {
+                                      NewtonCtl c, int k, int step, double ulim) {
     long i = (long)blockIdx.x * blockDim.x + threadIdx.x;
     if (i == 0) newton_control(c, norms, tol, k);
     if (i >= nc) return;
@@ -627,9 +649,15 @@ __global__ void k_newton_update_chain(long nc, double* __restrict__ U, const dou
     double relax = 1.0;
     if (resVM > 1e6) relax = 0.5;
     else if (resVM > 2e3 && resVM < 1e2) relax = 0.9;
-    double u[NV];
+    double u[NV], u0[NV], du[NV];
 #pragma unroll
-    for (int cc = 0; cc < NV; ++cc) u[cc] = U[cc * nc + i] + dU[cc * nc + i] * relax;
+    for (int cc = 0; cc < NV; ++cc) {
+        u0[cc] = U[cc * nc + i];
+        du[cc] = dU[cc * nc + i] * relax;
+    }
+    const double a = update_scale<NV>(u0, du, gam, ulim);
+#pragma unroll
+    for (int cc = 0; cc < NV; ++cc) u[cc] = ulim > 0.0 ? u0[cc] + du[cc] * a : u0[cc] + du[cc];
     double ke = 0.5 * (u[1] * u[1] + u[2] * u[2]) / (u[0] + 1e-12);
     double pn = (gam - 1.0) * (u[3] - ke);
     if (u[0] < 1e-5) u[0] = 1e-5;
@@ -738,27 +766,6 @@ __global__ void k_soa_to_aos(long nc, int np, int stride, const T* __restrict__ 
     if (i >= nc) return;
     long dst = (long)perm[i] * stride;
     for (int c = 0; c < stride; ++c) aos[dst + c] = c < np ? (double)soa[c * nc + i] : 0.0;
-}
-
-// The same two renumberings one thread per row of the AoS array (the caller's cell order,
-// inv = the new index of each): the AoS side is read or written in order, which is what
-// a kernel needs that works on the caller's pinned host buffer in place (over the
-// CPU-GPU link, without a staging copy); the SoA side takes the scattered accesses.
-template <class T>
-__global__ void k_aos_rows_to_soa(long nc, int np, int stride, const double* __restrict__ aos,
-                                  const int* __restrict__ inv, T* __restrict__ soa) {
-    long j = (long)blockIdx.x * blockDim.x + threadIdx.x;
-    if (j >= nc) return;
-    const long i = inv[j];
-    for (int c = 0; c < np; ++c) soa[c * nc + i] = (T)aos[j * stride + c];
-}
-template <class T>
-__global__ void k_soa_to_aos_rows(long nc, int np, int stride, const T* __restrict__ soa,
-                                  const int* __restrict__ inv, double* __restrict__ aos) {
-    long j = (long)blockIdx.x * blockDim.x + threadIdx.x;
-    if (j >= nc) return;
-    const long i = inv[j];
-    for (int c = 0; c < stride; ++c) aos[j * stride + c] = c < np ? (double)soa[c * nc + i] : 0.0;
 }
 
 }  // namespace cfdg

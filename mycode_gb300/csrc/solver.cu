@@ -102,7 +102,7 @@ struct cfdg_solver {
     Flow<double> F;
     Flow<float> Ff;
     // device mesh
-    int *cf = nullptr, *fo = nullptr, *fn = nullptr, *ftag = nullptr, *perm = nullptr, *pinv = nullptr;
+    int *cf = nullptr, *fo = nullptr, *fn = nullptr, *ftag = nullptr, *perm = nullptr;
     GeoBuf<double> g64;
     GeoBuf<float> g32;
     MeshView<double> mv;
@@ -330,50 +330,61 @@ struct cfdg_solver {
         return CFDG_OK;
     }
 
-    // The device's view of a caller's host buffer when it is pinned (page-locked and mapped:
-    // cudaHostAlloc / cudaHostRegister memory, which the GPU reads and writes over the
-    // CPU-GPU link at its own address), else null: pageable memory goes through the
-    // staging buffer and the copy engines.
-    static const double* mapped_view(const double* host) {
+    // Host <-> staging copies.  A large pinned buffer is split over COPY_PARTS streams, so
+    // that several copy engines share the transfer; a pageable one is one copy (staged by
+    // the driver).  The copies are ordered after the work enqueued on st and st waits for
+    // them.
+    static constexpr int COPY_PARTS = 4;
+    cudaStream_t cst[COPY_PARTS] = {};
+    cudaEvent_t cev[COPY_PARTS + 1] = {};
+    static bool pinned(const void* host) {
         cudaPointerAttributes a;
         if (cudaPointerGetAttributes(&a, host) != cudaSuccess) {
             cudaGetLastError();
-            return nullptr;
+            return false;
         }
-        return a.type == cudaMemoryTypeHost && a.devicePointer ? static_cast<const double*>(a.devicePointer) : nullptr;
+        return a.type == cudaMemoryTypeHost;
+    }
+    cfdg_status copy_parts(void* dst, const void* src, size_t bytes, cudaMemcpyKind kind, const void* host) {
+        if (bytes < (16u << 20) || !pinned(host)) {
+            CK(cudaMemcpyAsync(dst, src, bytes, kind, st));
+            return CFDG_OK;
+        }
+        if (!cst[0]) {
+            for (int k = 0; k < COPY_PARTS; ++k) CK(cudaStreamCreateWithFlags(&cst[k], cudaStreamNonBlocking));
+            for (int k = 0; k <= COPY_PARTS; ++k) CK(cudaEventCreateWithFlags(&cev[k], cudaEventDisableTiming));
+        }
+        CK(cudaEventRecord(cev[COPY_PARTS], st));
+        const size_t part = (bytes / COPY_PARTS + 255) & ~size_t(255);
+        for (int k = 0; k < COPY_PARTS; ++k) {
+            const size_t off = part * k;
+            const size_t len = off >= bytes ? 0 : std::min(part, bytes - off);
+            CK(cudaStreamWaitEvent(cst[k], cev[COPY_PARTS], 0));
+            if (len) CK(cudaMemcpyAsync(static_cast<char*>(dst) + off, static_cast<const char*>(src) + off, len, kind, cst[k]));
+            CK(cudaEventRecord(cev[k], cst[k]));
+            CK(cudaStreamWaitEvent(st, cev[k], 0));
+        }
+        return CFDG_OK;
     }
 
     // A caller's AoS array (reference numbering, 6 per cell) into np SoA planes (new
-    // numbering).  A pinned buffer is read in place by the renumbering kernel, in row
-    // order (one transfer over the link, no staging copy); otherwise it is copied to the
-    // staging buffer first.  Either way the call only enqueues: the caller's entry point
-    // synchronises before it returns.
+    // numbering), through the staging buffer; only enqueues (the entry point synchronises
+    // before it returns)
     cfdg_status upload_aos(const double* host, double* dev_soa, int np = -1) {
         if (np < 0) np = nv;
-        if (const double* dv = mapped_view(host)) {
-            launch_aos_rows_to_soa(nc, np, 6, dv, pinv, dev_soa, st);
-        } else {
-            CK(cudaMemcpyAsync(stage, host, sizeof(double) * 6 * (size_t)nc, cudaMemcpyHostToDevice, st));
-            launch_aos_to_soa<double>(nc, np, 6, stage, perm, dev_soa, st);
-        }
+        TRY(copy_parts(stage, host, sizeof(double) * 6 * (size_t)nc, cudaMemcpyHostToDevice, host));
+        launch_aos_to_soa<double>(nc, np, 6, stage, perm, dev_soa, st);
         ++launches;
         CK(cudaGetLastError());
         return CFDG_OK;
     }
 
-    // np SoA planes into a caller's AoS array (stride doubles per cell, zeros past np): a
-    // pinned buffer is written in place by the renumbering kernel, in row order
+    // np SoA planes into a caller's AoS array (stride doubles per cell, zeros past np)
     cfdg_status download_aos(const double* dev_soa, double* host, int np, int stride) {
-        if (double* dv = const_cast<double*>(mapped_view(host))) {
-            launch_soa_to_aos_rows(nc, np, stride, dev_soa, pinv, dv, st);
-            ++launches;
-            CK(cudaGetLastError());
-        } else {
-            launch_soa_to_aos<double>(nc, np, stride, dev_soa, perm, stage, st);
-            ++launches;
-            CK(cudaGetLastError());
-            CK(cudaMemcpyAsync(host, stage, sizeof(double) * stride * (size_t)nc, cudaMemcpyDeviceToHost, st));
-        }
+        launch_soa_to_aos<double>(nc, np, stride, dev_soa, perm, stage, st);
+        ++launches;
+        CK(cudaGetLastError());
+        TRY(copy_parts(host, stage, sizeof(double) * stride * (size_t)nc, cudaMemcpyDeviceToHost, host));
         CK(cudaStreamSynchronize(st));
         collect();
         return CFDG_OK;
@@ -1156,6 +1167,15 @@ struct cfdg_solver {
         *n_done = 0;
         if (k < 1) return CFDG_OK;
         if (k > CHAIN_MAX) k = CHAIN_MAX;
+        // optional start-up (off by default): the first startup_first_order steps of a solve
+        // run the first-order scheme, the chain stops where the configured scheme takes over
+        const int want = step < cfg.startup_first_order ? CFDG_FIRST_ORDER : cfg.spatial;
+        if (F.spatial != want) {
+            F.spatial = want;
+            Ff.spatial = want;
+            ++flow_version;
+        }
+        if (step < cfg.startup_first_order) k = std::min(k, cfg.startup_first_order - step);
         double t0 = now_s();
         TRY(ensure_krylov());
         if (!gexec || graph_version != flow_version || gkey[0] != U || gkey[1] != R || gkey[2] != rhs || gkey[3] != x ||
@@ -1164,7 +1184,7 @@ struct cfdg_solver {
             TRY(build_gmres_graph(U, R, rhs, x, true));
         }
         const bool mixed = cfg.precision == CFDG_MIXED;
-        const bool limited = cfg.spatial == CFDG_SECOND_ORDER_LIMITED;
+        const bool limited = want == CFDG_SECOND_ORDER_LIMITED;
         double* hcfl = chain_h + NEWTON_REC * CHAIN_MAX;
         int* hc = reinterpret_cast<int*>(hcfl + 1);
         hc[0] = step;
@@ -1194,7 +1214,7 @@ struct cfdg_solver {
             CK(cudaGraphLaunch(gexec, st));
             if (timing) CK(cudaEventRecord(chain_ev[4 * j + 2], st));
             launch_newton_update_chain(nv, nc, U, x, scal + 8, tol, cfg.gamma, wmin, chain_ctl + 4 + j, c, j, step + j,
-                                       st);
+                                       cfg.update_limit, st);
             ++launches;
             if (timing) CK(cudaEventRecord(chain_ev[4 * j + 3], st));
         }
@@ -1484,7 +1504,7 @@ struct cfdg_solver {
         cudaFree(dinv64);
         void* pt[] = {Tt, Tj, Tjd, dwall, T32, T32d, dwall32};
         for (void* p : pt) cudaFree(p);
-        void* ps[] = {cf, fo, fn, ftag, perm, pinv, U, W, G, phi, FA, R, dt, D, stage, Ub, Rb, Up, Rp, vtmp, x, rhs,
+        void* ps[] = {cf, fo, fn, ftag, perm, U, W, G, phi, FA, R, dt, D, stage, Ub, Rb, Up, Rp, vtmp, x, rhs,
                       Wj, Wjd, Gj, Gjd, FAjd, U32, W32, W32d, G32, G32d, FA32d, phi32, dt32, V32, z32, V, z,
                       rs.partial, rs.counter, scal, bad};
         for (void* p : ps) cudaFree(p);
@@ -1501,6 +1521,8 @@ struct cfdg_solver {
         if (gexec) cudaGraphExecDestroy(gexec);
         for (auto& e : pool) cudaEventDestroy(e);
         for (auto& e : step_ev) if (e) cudaEventDestroy(e);
+        for (auto& e : cst) if (e) cudaStreamDestroy(e);
+        for (auto& e : cev) if (e) cudaEventDestroy(e);
         if (st) cudaStreamDestroy(st);
     }
 };
@@ -1556,6 +1578,8 @@ void cfdg_config_default(cfdg_config* c) {
     c->pdl = 1;
     c->barrier_poll_limit = 0;
     c->newton_chain = 8;
+    c->startup_first_order = 0;
+    c->update_limit = 0.0;
 }
 
 cfdg_status cfdg_mesh_create(int n_nodes, const double* xy, int n_cells, const int* cells, int n_bedges,
@@ -1690,13 +1714,11 @@ cfdg_status cfdg_solver_create(const cfdg_mesh* m, const cfdg_config* cfg, cfdg_
     TRYS(dalloc(&s->fn, nf));
     TRYS(dalloc(&s->ftag, nf));
     TRYS(dalloc(&s->perm, nc));
-    TRYS(dalloc(&s->pinv, nc));
     if (cudaMemcpy(s->cf, h.cf.data(), sizeof(int) * 4 * (size_t)nc, cudaMemcpyHostToDevice) != cudaSuccess ||
         cudaMemcpy(s->fo, h.fo.data(), sizeof(int) * nf, cudaMemcpyHostToDevice) != cudaSuccess ||
         cudaMemcpy(s->fn, h.fn.data(), sizeof(int) * nf, cudaMemcpyHostToDevice) != cudaSuccess ||
         cudaMemcpy(s->ftag, h.ftag.data(), sizeof(int) * nf, cudaMemcpyHostToDevice) != cudaSuccess ||
-        cudaMemcpy(s->perm, h.cell_perm.data(), sizeof(int) * nc, cudaMemcpyHostToDevice) != cudaSuccess ||
-        cudaMemcpy(s->pinv, h.cell_inv.data(), sizeof(int) * nc, cudaMemcpyHostToDevice) != cudaSuccess)
+        cudaMemcpy(s->perm, h.cell_perm.data(), sizeof(int) * nc, cudaMemcpyHostToDevice) != cudaSuccess)
         return bail(fail(CFDG_ERR_CUDA, "mesh upload failed"));
     TRYS(upload_geo(s->g64, h));
     TRYS(upload_geo(s->g32, h));
