@@ -209,14 +209,19 @@ __global__ void __launch_bounds__(128) k_adj_cell1(MeshView<double> m, Flow<doub
             double d2 = Pf - pc;
             double a = 1.0;
             bool ratio = false;
+            // as the forward: the divide only where the ratio can be below one
             if (d2 > 0.0) {
-                double r = (pmax - pc) / (d2 + eps);
-                ratio = r < 1.0;
-                a = ratio ? r : 1.0;
+                if (!(pmax - pc >= d2 + eps)) {
+                    double r = (pmax - pc) / (d2 + eps);
+                    ratio = r < 1.0;
+                    a = ratio ? r : 1.0;
+                }
             } else if (d2 < 0.0) {
-                double r = (pmin - pc) / (d2 - eps);
-                ratio = r < 1.0;
-                a = ratio ? r : 1.0;
+                if (!(pmin - pc <= d2 - eps)) {
+                    double r = (pmin - pc) / (d2 - eps);
+                    ratio = r < 1.0;
+                    a = ratio ? r : 1.0;
+                }
             }
             if (a < lim) {
                 lim = a;

@@ -243,12 +243,14 @@ __device__ __forceinline__ void grad_item(const MeshView<R>& m, const Flow<R>& F
         R Pf = rho * F.Rgas * Tf;
         R d2 = Pf - pc;
         R a = R(1.0);
+        // a = min(1, x / y): when x / y >= 1 exactly (x >= y > 0, or x <= y < 0) the rounded
+        // quotient is >= 1 too and a is 1: the divide runs only for the faces that limit
         if (d2 > R(0.0)) {
-            a = (pmax - pc) / (d2 + eps);
-            a = smin(R(1.0), a);
+            const R x = pmax - pc, y = d2 + eps;
+            if (!(x >= y)) a = smin(R(1.0), x / y);
         } else if (d2 < R(0.0)) {
-            a = (pmin - pc) / (d2 - eps);
-            a = smin(R(1.0), a);
+            const R x = pmin - pc, y = d2 - eps;
+            if (!(x <= y)) a = smin(R(1.0), x / y);
         }
         lim = smin(lim, a);
     }
