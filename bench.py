@@ -669,7 +669,71 @@ def other_configs(api, steps=20, warmup=3):
             # a diverging start-up (no start-up strategy beyond the reference's CFL control)
             out[name] = {"n_cells": mesh.n_cells, "n_faces": mesh.n_faces, "error": str(e)}
         s.close()
+        if name == "turbulent_plate_sst":
+            out[name].update(converged_plate_vjp(api, mesh, method, mach, re))
     return out
+
+
+def vjp_fd_check(s, U, kind, x0=-1e300, x1=1e300, seed=29, directions=16):
+    """The VJP of a wall objective at state U against central differences: lambda = dJ/dU
+    (itself checked against differences of J), then lambda^T (dR/dU) v by the VJP against
+    central differences of lambda^T R along seeded directions v scaled per component.  A
+    direction whose two step sizes (1e-7, 1e-8) disagree crossed a branch (a min / max /
+    clip of the scheme) and is counted, not compared."""
+    import numpy as np
+    J, lam = s.objective(kind, x0, x1)
+    gU = s.vjp(lam, U)
+    rng = np.random.default_rng(seed)
+    scale = np.abs(U).mean(axis=0)
+    worst, worst_dj, switched = 0.0, 0.0, 0
+    for _ in range(directions):
+        v = rng.standard_normal(U.shape) * scale
+        s.set_state(U + 1e-6 * v)
+        jp = s.objective(kind, x0, x1, gradient=False)
+        s.set_state(U - 1e-6 * v)
+        jm = s.objective(kind, x0, x1, gradient=False)
+        lv = float(np.sum(lam * v))
+        worst_dj = max(worst_dj, abs((jp - jm) / 2e-6 - lv) / max(abs(lv), 1e-300))
+        fd = {h: float(np.sum(lam * (s.computeResiduals(U + h * v) - s.computeResiduals(U - h * v)))) / (2 * h)
+              for h in (1e-7, 1e-8)}
+        a = float(np.sum(gU * v))
+        err = abs(fd[1e-7] - a) / abs(a)
+        if err > 1e-6 and abs(fd[1e-7] - fd[1e-8]) > 1e-7 * abs(a):
+            switched += 1
+        else:
+            worst = max(worst, err)
+    s.set_state(U)
+    return {"objective": kind, "J": J, "directions": directions, "worst_rel_err": worst,
+            "dJdU_worst_rel_err": worst_dj, "branch_switches": switched, "seed": seed}
+
+
+def converged_plate_vjp(api, mesh, method, mach, re, orders=6.0, max_steps=8000):
+    """The turbulent flat plate from the free stream to `orders` orders of volume-weighted
+    residual reduction under the reference's CFL control (mixed precision, chains of 64
+    steps), then the skin-friction-drag VJP at that state against central differences along
+    16 seeded directions."""
+    s = api.Solver(mesh, bcset="plate", viscous=1, init="freestream", turbulence="sst", precision="mixed",
+                   jv="exact", **method)
+    s.setFreestreamStatic(mach, 101325.0, 300.0)
+    s.setKinematicViscosity(re, 1.0)
+    s.initialize()
+    s.reset_newton()
+    s.synchronize()
+    t0 = time.perf_counter()
+    recs = []
+    while len(recs) < max_steps:
+        r, _ = s.newton_steps(64)
+        recs += r
+        if recs[-1].res_vm <= 10.0 ** -orders * recs[0].res_vm:
+            break
+    s.synchronize()
+    t = time.perf_counter() - t0
+    conv = {"newton_steps": len(recs), "seconds": round(t, 3), "res_vm_first_last": [recs[0].res_vm, recs[-1].res_vm],
+            "orders": math.log10(recs[0].res_vm / recs[-1].res_vm),
+            "gmres_iters": int(sum(x.gmres_iters for x in recs))}
+    chk = vjp_fd_check(s, s.getSolution(), "skin_friction_drag")
+    s.close()
+    return {"converged": conv, "skin_friction_drag_vjp": chk}
 
 
 def _golden(name):
