@@ -27,6 +27,20 @@ void launch_residual<float>(const ResArgs<float>& a) {
     else residual_nv<4>(a);
 }
 
+template <int NV>
+static void values_nv(const ResArgs<float>& a) {
+    long nc = a.m.nc;
+    k_prim<float, NV><<<blocks_for(nc), tpb_for(nc), 0, a.stream>>>((int)nc, a.F, a.U, a.W);
+    k_grad<float, NV><<<blocks_for(nc), tpb_for(nc), 0, a.stream>>>(a.m, a.F, a.U, a.W, a.G, a.phi, 0, nullptr, nullptr);
+    if (NV == 6) k_sst_cell<float, NV><<<blocks_for(nc), tpb_for(nc), 0, a.stream>>>(a.m, a.F, a.W, a.G, a.dwall, a.T, nullptr);
+}
+
+template <>
+void launch_values<float>(const ResArgs<float>& a) {
+    if (a.nv == 6) values_nv<6>(a);
+    else values_nv<4>(a);
+}
+
 
 template <>
 void launch_dot<float>(int nv, long nc, const float* a, const float* b, RedScratch rs, double* out, cudaStream_t s) {

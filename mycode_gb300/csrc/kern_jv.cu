@@ -29,12 +29,15 @@ template <class R, int NV>
 static void jv_mid_nv(const ResArgs<R>& a) {
     typedef Dual<R> S;
     long nc = a.m.nc, nf = a.m.nf;
+    // write views: derivative planes only when the value planes are current (a.tangent)
+    Field<R> Gw = a.G, Tw = a.T;
+    if (a.tangent) Gw.v = Tw.v = nullptr;
     if (a.ev) cudaEventRecord(a.ev[0], a.stream);
-    launch_k(a.pdl, k_grad<S, NV, R>, dim3(blocks_for(nc)), dim3(tpb_for(nc)), a.stream, a.m, a.F, a.U, a.W, a.G,
+    launch_k(a.pdl, k_grad<S, NV, R>, dim3(blocks_for(nc)), dim3(tpb_for(nc)), a.stream, a.m, a.F, a.U, a.W, Gw,
              a.phi, 0, a.done, (const int*)nullptr);
     if (NV == 6)
         launch_k(a.pdl, k_sst_cell<S, NV, R>, dim3(blocks_for(nc)), dim3(tpb_for(nc)), a.stream, a.m, a.F, a.W, a.G,
-                 a.dwall, a.T, a.done);
+                 a.dwall, Tw, a.done);
     if (a.ev) cudaEventRecord(a.ev[1], a.stream);
     launch_k(a.pdl, k_flux<S, NV, R>, dim3(blocks_for(nf)), dim3(tpb_for(nf)), a.stream, a.m, a.F, a.U, a.W, a.G,
              (const R*)a.phi, a.FA, a.T, a.done);

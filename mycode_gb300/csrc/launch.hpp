@@ -27,6 +27,11 @@ struct ResArgs {
     const R* dwall = nullptr;         // wall distance per cell; nv = 6 only
     bool pdl = false;                 // launch_jv_mid: programmatic dependent launch (pdl.cuh)
     const int* done = nullptr;        // launch_jv_mid: skip when *done (a finished Krylov solve)
+    // launch_jv_mid: the value planes of W, G and T are current (launch_values at the start
+    // of the solve: the linearisation point does not move within it), so the gradient and
+    // SST kernels write derivative planes only and the gradient kernel reads only the
+    // derivative planes of its neighbours
+    bool tangent = false;
     const int* lim_dev = nullptr;     // launch_residual<double>: the limiter also needs *lim_dev
     // launch_residual<double> of a Newton step: the gather fused with the step's reductions
     // (k_gather_norms) when norms_out is set
@@ -64,6 +69,9 @@ template <class R> void launch_residual(const ResArgs<R>& a);
 template <class R> void launch_jv(const ResArgs<R>& a);
 // the middle of it (gradients, SST terms, face fluxes) for the fused Arnoldi body
 template <class R> void launch_jv_mid(const ResArgs<R>& a);
+// the value planes of the linearisation point: primitives, gradients (no limiter) and, with
+// SST, the cell terms of a.U.v into a.W.v, a.G.v, a.T.v
+template <class R> void launch_values(const ResArgs<R>& a);
 
 // ---- vectors (T = double in kern_f64.cu, T = float in kern_f32.cu)
 template <class T> void launch_dot(int nv, long nc, const T* a, const T* b, RedScratch rs, double* out, cudaStream_t s);

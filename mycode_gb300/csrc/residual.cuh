@@ -14,6 +14,7 @@
 // frozen), where every array has a value plane and a derivative plane.
 #pragma once
 #include <cuda_runtime.h>
+#include <type_traits>
 #include "face.cuh"
 #include "pdl.cuh"
 #include "sst.cuh"
@@ -52,16 +53,21 @@ struct Field {
 template <class S> struct Acc;
 template <> struct Acc<double> {
     template <class R> static CFD_HD double ld(const Field<R>& f, int p, long i) { return f.v[p * f.n + i]; }
+    template <class R> static CFD_HD double ld_tangent(const Field<R>& f, int p, long i) { return f.v[p * f.n + i]; }
     template <class R> static CFD_HD void st(const Field<R>& f, int p, long i, double x) { f.v[p * f.n + i] = x; }
 };
 template <> struct Acc<float> {
     template <class R> static CFD_HD float ld(const Field<R>& f, int p, long i) { return f.v[p * f.n + i]; }
+    template <class R> static CFD_HD float ld_tangent(const Field<R>& f, int p, long i) { return f.v[p * f.n + i]; }
     template <class R> static CFD_HD void st(const Field<R>& f, int p, long i, float x) { f.v[p * f.n + i] = x; }
 };
 template <class R> struct Acc<Dual<R>> {
     static CFD_HD Dual<R> ld(const Field<R>& f, int p, long i) {
         return Dual<R>(f.v[p * f.n + i], f.d ? f.d[p * f.n + i] : R(0));
     }
+    // the derivative plane alone (value 0): for sums whose derivative does not depend on
+    // the values
+    static CFD_HD Dual<R> ld_tangent(const Field<R>& f, int p, long i) { return Dual<R>(R(0), f.d[p * f.n + i]); }
     static CFD_HD void st(const Field<R>& f, int p, long i, Dual<R> x) {
         if (f.v) f.v[p * f.n + i] = x.v;
         f.d[p * f.n + i] = x.d;
@@ -141,6 +147,10 @@ __device__ __forceinline__ void grad_item(const MeshView<R>& m, const Flow<R>& F
     // done: a finished Krylov solve (krylov.cuh); read with the mesh loads, tested after
     const int skip = done ? *done : 0;
     constexpr int NQ = NV == 6 ? 7 : 5;
+    // a dual gradient with no value planes to write (J v about a fixed point whose value
+    // planes are current): the face sums' derivatives need only the neighbours' derivative
+    // planes (the ghost states read the cell's own values)
+    const bool tangent = !std::is_same<S, R>::value && G.v == nullptr && !do_limiter;
     // Mesh data first (face entries, then each face's normal, area and neighbour, and for
     // a boundary face its distance and tag): no kernel writes it, so it is loaded before
     // the wait for the predecessor's primitives (pdl.cuh) and only the primitive loads
@@ -185,8 +195,13 @@ __device__ __forceinline__ void grad_item(const MeshView<R>& m, const Flow<R>& F
         S wj[NQ];
         int j = nbr[k];
         if (j >= 0) {
+            if (tangent) {
 #pragma unroll
-            for (int q = 0; q < NQ; ++q) wj[q] = Acc<S>::ld(W, q, j);
+                for (int q = 0; q < NQ; ++q) wj[q] = Acc<S>::ld_tangent(W, q, j);
+            } else {
+#pragma unroll
+                for (int q = 0; q < NQ; ++q) wj[q] = Acc<S>::ld(W, q, j);
+            }
         } else {
             CS<S> Ui = load_cs<S, NV>(U, W, i);
             R dn = fdn[k];
@@ -257,10 +272,21 @@ __device__ __forceinline__ void grad_item(const MeshView<R>& m, const Flow<R>& F
     phi[i] = lim;
 }
 
+// Resident 256-thread blocks per SM asked of the compiler for the shared gradient and
+// face-flux templates (the register cap is 65536 / (256 x blocks)).
+#ifndef GRAD_DUAL_MINB
+#define GRAD_DUAL_MINB 2
+#endif
+#ifndef FLUX_DUAL_MINB
+#define FLUX_DUAL_MINB 2
+#endif
+template <class S> struct MinBlocks { static constexpr int grad = 1, flux = 1; };
+template <> struct MinBlocks<Dual<float>> { static constexpr int grad = GRAD_DUAL_MINB, flux = FLUX_DUAL_MINB; };
+
 // lim_dev (optional): the limiter is recomputed only when *lim_dev is also set (a Newton
 // step whose limiter-freeze decision was taken on the device)
 template <class S, int NV, class R>
-__global__ void __launch_bounds__(256) k_grad(MeshView<R> m, Flow<R> F, Field<R> U, Field<R> W, Field<R> G,
+__global__ void __launch_bounds__(256, MinBlocks<S>::grad) k_grad(MeshView<R> m, Flow<R> F, Field<R> U, Field<R> W, Field<R> G,
                                               R* phi, int do_limiter, const int* done, const int* lim_dev) {
     long i = (long)blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= m.nc) return;
@@ -379,7 +405,7 @@ __device__ __forceinline__ void flux_item(const MeshView<R>& m, const Flow<R>& F
 }
 
 template <class S, int NV, class R>
-__global__ void __launch_bounds__(256) k_flux(MeshView<R> m, Flow<R> F, Field<R> U, Field<R> W, Field<R> G,
+__global__ void __launch_bounds__(256, MinBlocks<S>::flux) k_flux(MeshView<R> m, Flow<R> F, Field<R> U, Field<R> W, Field<R> G,
                                               const R* __restrict__ phi, Field<R> FA, Field<R> T, const int* done) {
     long f = (long)blockIdx.x * blockDim.x + threadIdx.x;
     if (f >= m.nf) return;

@@ -633,7 +633,21 @@ struct cfdg_solver {
         if (mixed) {
             launch_mixed_pre(nv, mvf, Ff, U, Ubase, W, phi, nv == 6 ? Tt : nullptr, newton ? scal + 12 : nullptr, dt,
                              U32, phi32, dt32, D, dinv32, st);
-            ++launches;
+            // the value planes of the FP32 linearisation point, once per solve: the Arnoldi
+            // body's dual kernels then form and write derivative planes only
+            ResArgs<float> a;
+            a.m = mvf;
+            a.F = Ff;
+            a.nv = nv;
+            a.U = f32(U32);
+            a.W = f32(W32);
+            a.G = f32(G32);
+            a.T = f32(T32);
+            a.dwall = dwall32;
+            a.phi = phi32;
+            a.stream = st;
+            launch_values<float>(a);
+            launches += nv == 6 ? 3 : 2;
         } else {
             launch_precond(nv, mv, F, U, W, dt, D, Tt, st);
             launch_gmres_dinv<double>(nv, nc, D, dinv64, st);
@@ -703,7 +717,7 @@ struct cfdg_solver {
         const bool mixed = cfg.precision == CFDG_MIXED;
         if (ev) CK(cudaEventRecord(ev[0], st));
         if (mixed) {
-            launch_gmres_prim_z<float>(nv, nc, Ff, U32, V32, L, dinv32, z32, f32(W32, W32d), w32, gd, h, st);
+            launch_gmres_prim_z<float>(nv, nc, Ff, U32, V32, L, dinv32, z32, f32(nullptr, W32d), w32, gd, h, st);
             ResArgs<float> a;
             a.m = mvf;
             a.F = Ff;
@@ -719,6 +733,7 @@ struct cfdg_solver {
             a.ev = ev ? ev + 1 : nullptr;
             a.pdl = pdl;
             a.done = gd.gi + 2;
+            a.tangent = true;
             launch_jv_mid<float>(a);
             launch_gmres_gather_dot<float>(nv, mvf, FA32d, w32, z32, dt32, nv == 6 ? T32d + 2 * nc : nullptr, V32, L, gd,
                                            st, pdl);

@@ -20,7 +20,10 @@ Recipes (cells, faces):
   turb_plate    480x240 quads, x in [-0.4, 2], y in [0, 1], first spacing for
                 y+ < 1 at Re 5e6/m, growth ratio 1.12 capped to fill the height.
   swbli         800x640 stretched quads, the outer half of the rows split into
-                triangles, jitter 5 %.
+                triangles, jitter 5 % of the smaller local spacing in both
+                directions (isotropic: a per-direction jitter of the streamwise
+                spacing would tilt the y+ < 1 wall cells, aspect ratio ~10^3, to
+                slivers).
   bump          3x1 channel with a Gaussian bump (height 0.05, width 0.2),
                 n_y = round(sqrt(N/6)), n_x = 3 n_y, every quad split in two.
 """
@@ -85,14 +88,14 @@ def _capped_geometric(n: int, total: float, first: float, ratio: float) -> np.nd
 
 
 def _structured(name: str, X: np.ndarray, Y: np.ndarray, split_row, tag_of_edge,
-                jitter: float = 0.0, seed: int = 0) -> MeshSpec:
+                jitter: float = 0.0, seed: int = 0, isotropic: bool = False) -> MeshSpec:
     """Mesh of the (ny+1) x (nx+1) node grid X, Y.
 
     Cells are emitted row by row (j outer, i inner).  A quad (a,b,c,d) =
     ((i,j),(i+1,j),(i+1,j+1),(i,j+1)) is either kept or split along a-c into
     (a,b,c) and (a,c,d) when ``split_row(j)`` is true.  Interior nodes move by a
     seeded uniform +-``jitter`` fraction of the smaller adjacent spacing in each
-    direction.
+    direction (``isotropic``: of the smaller of the two directions' spacings, in both).
     """
     ny, nx = X.shape[0] - 1, X.shape[1] - 1
     X = X.astype(np.float64).copy()
@@ -103,6 +106,8 @@ def _structured(name: str, X: np.ndarray, Y: np.ndarray, split_row, tag_of_edge,
         dyl = np.minimum(Y[2:, 1:-1] - Y[1:-1, 1:-1], Y[1:-1, 1:-1] - Y[:-2, 1:-1])
         ux = rng.uniform(-1.0, 1.0, size=dxl.shape)
         uy = rng.uniform(-1.0, 1.0, size=dyl.shape)
+        if isotropic:
+            dxl = dyl = np.minimum(dxl, dyl)
         X[1:-1, 1:-1] += jitter * dxl * ux
         Y[1:-1, 1:-1] += jitter * dyl * uy
     nodes = np.stack([X.ravel(), Y.ravel()], axis=1)
@@ -204,7 +209,8 @@ def swbli(nx: int = 800, ny: int = 640, length: float = 1.0, height: float = 0.4
           reynolds_per_m: float = 1e7, jitter: float = 0.05, seed: int = 0) -> MeshSpec:
     """Shock/boundary-layer interaction box: no-slip wall from x=0.1 (slip lead-in),
     free-stream inlet (1), extrapolation outlet (2), the top boundary carries the
-    post-shock state of an 8 degree deflection (6).  Rows in the outer half are split."""
+    post-shock state of an 8 degree deflection (6).  Rows in the outer half are split.
+    Interior nodes move by +-``jitter`` of the smaller local spacing in both directions."""
     cf = 0.0576 * reynolds_per_m ** -0.2
     first = 0.5 / (reynolds_per_m * math.sqrt(0.5 * cf))
     xs = np.linspace(0.0, length, nx + 1)
@@ -216,7 +222,7 @@ def swbli(nx: int = 800, ny: int = 640, length: float = 1.0, height: float = 0.4
             return TAG_NOSLIP if s > 0.1 * length else TAG_SLIP
         return {"left": TAG_INLET, "right": TAG_OUTLET, "top": TAG_SHOCK_INFLOW}[side]
 
-    return _structured(f"swbli_{nx}x{ny}", X, Y, lambda j: j >= ny // 2, tag, jitter, seed)
+    return _structured(f"swbli_{nx}x{ny}", X, Y, lambda j: j >= ny // 2, tag, jitter, seed, isotropic=True)
 
 
 def bump(n_target: int = 64_000, jitter: float = 0.10, seed: int = 0,
