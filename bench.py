@@ -134,18 +134,31 @@ def algorithmic_bytes(kind: str, nc: int, nf: int, nv: int, s: int, spatial: str
     raise ValueError(kind)
 
 
-def krylov_bytes(stage: str, nc: int, nf: int, nv: int, s: int, jbar: float) -> float:
+def krylov_bytes(stage: str, nc: int, nf: int, nv: int, s: int, jbar: float,
+                 spatial: str = "SECOND_ORDER_CENTRAL") -> float:
     """Compulsory bytes of one fused Arnoldi stage (FP32 basis: s = 4) at the mean number
-    of basis vectors jbar + 1 that the iterations read."""
+    of basis vectors jbar + 1 that the iterations read.  The value planes of the
+    linearisation point (primitives, gradients, SST cell terms) are formed once per solve,
+    so the body writes derivative planes only."""
     L = nv * nc
     nb = jbar + 1.0
+    nq = 7 if nv == 6 else 5
+    ng = 2 * nq
     if stage == "prim_z":
         # second pass of the pending vector and first pass of the last product (the pending
         # vector, the product and j basis vectors in; the finished basis vector and the new
-        # pending vector out), then U and 1/D in, z and the dual primitives out
-        return nc * (nv * s + s + nv * s + 2 * (7 if nv == 6 else 5) * s) + L * s * (jbar + 4)
-    if stage in ("grad", "flux"):
-        return algorithmic_bytes(stage, nc, nf, nv, s, "SECOND_ORDER_CENTRAL", True, True)
+        # pending vector out), then U and 1/D in, z and the primitives' derivatives out
+        return nc * (nv * s + s + nv * s + nq * s) + L * s * (jbar + 4)
+    if stage == "grad":
+        # the primitives' derivatives in, the gradients' derivatives out, the face list; the
+        # SST cell kernel: primitives and gradients (value + derivative) and d in, the cell
+        # terms' derivatives out
+        b = nc * (nq * s + ng * s + 16)
+        if nv == 6:
+            b += nc * (2 * nq * s + 2 * ng * s + s + 4 * s)
+        return b
+    if stage == "flux":
+        return algorithmic_bytes(stage, nc, nf, nv, s, spatial, True, True)
     if stage == "gather_dot":
         return nc * 16 + nf * nv * s + nc * (nv * s + 2 * s + nv * s) + nb * L * s
     if stage in ("update_dot", "update_final"):  # FD J v body only
@@ -641,7 +654,9 @@ def other_configs(api, steps=20, warmup=3):
     free stream, CUDA events around each step (secondary measurements, not the headline):
     the turbulent flat plate 480 x 240 (115,200 cells, Roe, central) and the shock/boundary-
     layer interaction box 800 x 640 with its outer half split (768,000 cells, HLLC + BJ
-    limiter, 8-degree shock inflow)."""
+    limiter, 8-degree shock inflow).  Then the plate converged and its skin-friction-drag
+    VJP; the interaction's wall-pressure VJP (x in [0.3, 0.7]) at the state the timed steps
+    reached, and its 200 x 160 mesh (48,000 cells) converged."""
     from mycode_gb300 import meshgen
     out = {}
     cases = (
@@ -665,21 +680,27 @@ def other_configs(api, steps=20, warmup=3):
             out[name] = {"n_cells": mesh.n_cells, "n_faces": mesh.n_faces, "value": evals * mesh.n_cells / t,
                          "unit": UNIT, "ms_per_step": 1e3 * t / steps, "steps": steps, "warmup": warmup,
                          "gmres_iters": [r[1] for r in recs], "res_vm_first_last": [recs[0][0], recs[-1][0]]}
+            if name == "swbli_sst":
+                s.set_timing(False)
+                out[name]["wall_pressure_vjp"] = vjp_fd_check(s, s.getSolution(), "wall_pressure", 0.3, 0.7, seed=37,
+                                                              steps=(1e-9, 1e-8))
+                out[name]["wall_pressure_vjp"]["state"] = f"after {warmup + steps} Newton steps from the free stream"
         except api.CfdgError as e:
-            # a diverging start-up (no start-up strategy beyond the reference's CFL control)
             out[name] = {"n_cells": mesh.n_cells, "n_faces": mesh.n_faces, "error": str(e)}
         s.close()
         if name == "turbulent_plate_sst":
             out[name].update(converged_plate_vjp(api, mesh, method, mach, re))
+        if name == "swbli_sst":
+            out[name]["converged_200x160"] = converged_run(api, meshgen.swbli(200, 160), method, mach, re, extra)
     return out
 
 
-def vjp_fd_check(s, U, kind, x0=-1e300, x1=1e300, seed=29, directions=16):
+def vjp_fd_check(s, U, kind, x0=-1e300, x1=1e300, seed=29, directions=16, steps=(1e-7, 1e-8)):
     """The VJP of a wall objective at state U against central differences: lambda = dJ/dU
     (itself checked against differences of J), then lambda^T (dR/dU) v by the VJP against
     central differences of lambda^T R along seeded directions v scaled per component.  A
-    direction whose two step sizes (1e-7, 1e-8) disagree crossed a branch (a min / max /
-    clip of the scheme) and is counted, not compared."""
+    direction whose two step sizes disagree crossed a branch (a min / max / clip of the
+    scheme, a limiter switch) and is counted, not compared."""
     import numpy as np
     J, lam = s.objective(kind, x0, x1)
     gU = s.vjp(lam, U)
@@ -694,26 +715,26 @@ def vjp_fd_check(s, U, kind, x0=-1e300, x1=1e300, seed=29, directions=16):
         jm = s.objective(kind, x0, x1, gradient=False)
         lv = float(np.sum(lam * v))
         worst_dj = max(worst_dj, abs((jp - jm) / 2e-6 - lv) / max(abs(lv), 1e-300))
-        fd = {h: float(np.sum(lam * (s.computeResiduals(U + h * v) - s.computeResiduals(U - h * v)))) / (2 * h)
-              for h in (1e-7, 1e-8)}
+        fd = [float(np.sum(lam * (s.computeResiduals(U + h * v) - s.computeResiduals(U - h * v)))) / (2 * h)
+              for h in steps]
         a = float(np.sum(gU * v))
-        err = abs(fd[1e-7] - a) / abs(a)
-        if err > 1e-6 and abs(fd[1e-7] - fd[1e-8]) > 1e-7 * abs(a):
+        err = abs(fd[0] - a) / abs(a)
+        if err > 1e-6 and abs(fd[0] - fd[1]) > 1e-7 * abs(a):
             switched += 1
         else:
             worst = max(worst, err)
     s.set_state(U)
-    return {"objective": kind, "J": J, "directions": directions, "worst_rel_err": worst,
-            "dJdU_worst_rel_err": worst_dj, "branch_switches": switched, "seed": seed}
+    return {"objective": kind, "range": [x0, x1] if x0 > -1e300 else None, "J": J, "directions": directions,
+            "steps": list(steps), "worst_rel_err": worst, "dJdU_worst_rel_err": worst_dj,
+            "branch_switches": switched, "seed": seed}
 
 
-def converged_plate_vjp(api, mesh, method, mach, re, orders=6.0, max_steps=8000):
-    """The turbulent flat plate from the free stream to `orders` orders of volume-weighted
-    residual reduction under the reference's CFL control (mixed precision, chains of 64
-    steps), then the skin-friction-drag VJP at that state against central differences along
-    16 seeded directions."""
+def _converge(api, mesh, method, mach, re, extra, orders, max_steps):
+    """A mixed-precision solver on `mesh` from the free stream to `orders` orders of
+    volume-weighted residual reduction under the reference's CFL control (chains of 64
+    Newton steps): the solver and the run's record."""
     s = api.Solver(mesh, bcset="plate", viscous=1, init="freestream", turbulence="sst", precision="mixed",
-                   jv="exact", **method)
+                   jv="exact", **method, **extra)
     s.setFreestreamStatic(mach, 101325.0, 300.0)
     s.setKinematicViscosity(re, 1.0)
     s.initialize()
@@ -728,12 +749,26 @@ def converged_plate_vjp(api, mesh, method, mach, re, orders=6.0, max_steps=8000)
             break
     s.synchronize()
     t = time.perf_counter() - t0
-    conv = {"newton_steps": len(recs), "seconds": round(t, 3), "res_vm_first_last": [recs[0].res_vm, recs[-1].res_vm],
-            "orders": math.log10(recs[0].res_vm / recs[-1].res_vm),
-            "gmres_iters": int(sum(x.gmres_iters for x in recs))}
+    return s, {"n_cells": mesh.n_cells, "newton_steps": len(recs), "seconds": round(t, 3),
+               "res_vm_first_last": [recs[0].res_vm, recs[-1].res_vm],
+               "res_rho_first_last": [recs[0].res_rho, recs[-1].res_rho],
+               "orders": math.log10(recs[0].res_vm / recs[-1].res_vm),
+               "gmres_iters": int(sum(x.gmres_iters for x in recs))}
+
+
+def converged_plate_vjp(api, mesh, method, mach, re, orders=6.0, max_steps=8000):
+    """The turbulent flat plate converged `orders` orders, then the skin-friction-drag VJP at
+    that state against central differences along 16 seeded directions."""
+    s, conv = _converge(api, mesh, method, mach, re, {}, orders, max_steps)
     chk = vjp_fd_check(s, s.getSolution(), "skin_friction_drag")
     s.close()
     return {"converged": conv, "skin_friction_drag_vjp": chk}
+
+
+def converged_run(api, spec, method, mach, re, extra, orders=6.0, max_steps=14000):
+    s, conv = _converge(api, api.Mesh.from_spec(spec, gpu=0), method, mach, re, extra, orders, max_steps)
+    s.close()
+    return conv
 
 
 def _golden(name):
@@ -1033,6 +1068,15 @@ def profile_case(args):
         line["gmres_iters"] = iters
         line["mean_j"] = sum(i * (i - 1) / 2 for i in iters) / max(1, sum(iters))
         line["launches"] = {k: v[1] for k, v in st.items() if k.startswith(prefix) and v[1]}
+        # algorithmic bytes of each stage at the mean j, per launch, and the bandwidth
+        nv = 4 if args.profile_workload == "laminar_plate" or args.no_sst else 6
+        spatial = "SECOND_ORDER_CENTRAL" if args.profile_workload == "laminar_plate" else "SECOND_ORDER_LIMITED"
+        peak, _ = measured_peak()
+        line["algorithmic"] = {}
+        for k, ms in line["ms_per_launch"].items():
+            b = krylov_bytes(k.split(".")[1], m.n_cells, m.n_faces, nv, 4, line["mean_j"], spatial)
+            line["algorithmic"][k] = {"MB": round(b / 1e6, 1), "GBs": round(b / (ms * 1e-3) / 1e9, 1),
+                                      "hbm_frac": round(b / (ms * 1e-3) / 1e9 / peak, 3)}
     print(json.dumps(line))
 
 
