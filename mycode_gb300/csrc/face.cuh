@@ -29,7 +29,7 @@ CFD_HD CS<S> face_right(const Flow<R>& F, const CS<S>& L, const CS<S>& Rn, bool 
 template <class R>
 CFD_HD R wall_normal_distance(const FaceGeo<R>& g) {
     R d = g.dxL * g.nx + g.dyL * g.ny;
-    return d < R(0) ? -d : d;
+    return lt0(d) ? -d : d;
 }
 
 // Second-order reconstruction of one side (src/Solver.cpp:596-623)
@@ -39,8 +39,8 @@ CFD_HD CS<S> reconstruct(const Flow<R>& F, const CS<S>& C, const S* g, S ph, R d
     S pf = C.p + ph * (g[FG_P] * dx + g[FG_P + 1] * dy);
     S uf = C.u + ph * (g[FG_U] * dx + g[FG_U + 1] * dy);
     S vf = C.v + ph * (g[FG_V] * dx + g[FG_V + 1] * dy);
-    if (val(rf) < R(1e-4)) rf = C.r;
-    if (val(pf) < R(1e-4)) pf = C.p;
+    if (lt(rf, R(1e-4))) rf = C.r;
+    if (lt(pf, R(1e-4))) pf = C.p;
     return p2c(F, rf, uf, vf, pf, S(R(0)), S(R(0)));
 }
 
@@ -74,9 +74,9 @@ CFD_HD Flux6<S> face_flux(const Flow<R>& F, const CS<S>& L, const CS<S>& Rn, boo
     }
     if (F.viscous) {
         const S* gRv = interior ? gR : gL;
-        S rf = R(0.5) * (L.r + Rt.r);
-        S uf = R(0.5) * (L.u + Rt.u);
-        S vf = R(0.5) * (L.v + Rt.v);
+        S rf = half(L.r + Rt.r);
+        S uf = half(L.u + Rt.u);
+        S vf = half(L.v + Rt.v);
         S dudx, dudy, dvdx, dvdy, dTdx, dTdy;
         if (!interior && tag == 4) {
             R dx = g.dxL, dy = g.dyL;
@@ -90,14 +90,14 @@ CFD_HD Flux6<S> face_flux(const Flow<R>& F, const CS<S>& L, const CS<S>& Rn, boo
             dTdx = S(R(0.0));
             dTdy = S(R(0.0));
         } else {
-            dudx = R(0.5) * (gL[FG_U] + gRv[FG_U]);
-            dudy = R(0.5) * (gL[FG_U + 1] + gRv[FG_U + 1]);
-            dvdx = R(0.5) * (gL[FG_V] + gRv[FG_V]);
-            dvdy = R(0.5) * (gL[FG_V + 1] + gRv[FG_V + 1]);
-            dTdx = R(0.5) * (gL[FG_T] + gRv[FG_T]);
-            dTdy = R(0.5) * (gL[FG_T + 1] + gRv[FG_T + 1]);
+            dudx = half(gL[FG_U] + gRv[FG_U]);
+            dudy = half(gL[FG_U + 1] + gRv[FG_U + 1]);
+            dvdx = half(gL[FG_V] + gRv[FG_V]);
+            dvdy = half(gL[FG_V + 1] + gRv[FG_V + 1]);
+            dTdx = half(gL[FG_T] + gRv[FG_T]);
+            dTdy = half(gL[FG_T + 1] + gRv[FG_T + 1]);
             R d2 = g.dxlr * g.dxlr + g.dylr * g.dylr;
-            if (d2 > R(1e-14)) {
+            if (lt(R(1e-14), d2)) {
                 const R id2 = R(1.0) / d2;  // FP64: four quotients by one reciprocal (div_shared)
                 S du = Rt.u - L.u;
                 S dv = Rt.v - L.v;
@@ -108,8 +108,7 @@ CFD_HD Flux6<S> face_flux(const Flow<R>& F, const CS<S>& L, const CS<S>& Rn, boo
                 dvdy = e0 - div_shared((c0 * g.dxlr + e0 * g.dylr - dv) * g.dylr, d2, id2);
             }
         }
-        const R gm1 = F.gam - R(1.0);
-        R Cp = div_shared(F.gam * F.Rgas, gm1, recip_for(gm1));  // 1/(gamma-1) shared with the reconstruction
+        const R Cp = F.Cp;
         S mu = rf * F.nu;
         S kc = div_shared(mu * Cp, F.Pr, F.inv_Pr);  // FP64: by the reciprocal of Pr, the same bits
         if (F.sst) {
@@ -117,8 +116,8 @@ CFD_HD Flux6<S> face_flux(const Flow<R>& F, const CS<S>& L, const CS<S>& Rn, boo
             mu = mu + mutf;
         }
         S div = dudx + dvdy;
-        S txx = mu * (R(2.0) * dudx - (R(2.0) / R(3.0)) * div);
-        S tyy = mu * (R(2.0) * dvdy - (R(2.0) / R(3.0)) * div);
+        S txx = mu * (twice(dudx) - (R(2.0) / R(3.0)) * div);
+        S tyy = mu * (twice(dvdy) - (R(2.0) / R(3.0)) * div);
         S txy = mu * (dudy + dvdx);
         S qx = -kc * dTdx, qy = -kc * dTdy;
         S wx = uf * txx + vf * txy - qx;
@@ -150,8 +149,8 @@ CFD_HD Flux6<S> face_flux_sst(const Flow<R>& F, const CS<S>& L, const CS<S>& Rn,
         mutR = mutL;
         F1R = F1L;
     }
-    S mutf = wall ? S(R(0)) : R(0.5) * (mutL + mutR);
-    S F1f = R(0.5) * (F1L + F1R);
+    S mutf = wall ? S(R(0)) : half(mutL + mutR);
+    S F1f = half(F1L + F1R);
     Flux6<S> out = face_flux(F, L, Rn, interior, tag, g, gL, gR, phL, phR, mutf);
     CS<S> Rt = face_right(F, L, Rn, interior, tag, g.nx, g.ny, wall_normal_distance(g));
     const S* gkRv = interior ? gkR : gkL;
@@ -165,7 +164,7 @@ CFD_HD Flux6<S> face_flux_sst(const Flow<R>& F, const CS<S>& L, const CS<S>& Rn,
         kR = quot_shared(Rt.rk, Rt.r, ig);
         wR = quot_shared(Rt.rw, Rt.r, ig);
     }
-    sst_face_flux(F, out.f[0], kwL[0], kwL[1], kR, wR, R(0.5) * (L.r + Rt.r), mutf, F1f, gkL, gkRv, wall, g.nx, g.ny,
+    sst_face_flux(F, out.f[0], kwL[0], kwL[1], kR, wR, half(L.r + Rt.r), mutf, F1f, gkL, gkRv, wall, g.nx, g.ny,
                   g.A, g.dxL, g.dyL, g.dxlr, g.dylr, Fk, Fw);
     out.f[4] = Fk;
     out.f[5] = Fw;

@@ -7,6 +7,7 @@
 // reference's CPU arithmetic bit for bit.  Citations are to AmberMond/mycode.
 #pragma once
 #include "dual.cuh"
+#include "exact64.cuh"
 
 namespace cfdg {
 
@@ -42,9 +43,12 @@ CFD_HD double recip_for(double b) { return 1.0 / b; }
 template <class S> CFD_HD S quot_shared(S a, S b, S) { return a / b; }
 CFD_HD double quot_shared(double a, double b, double y) { return quot_by_recip(a, b, y); }
 
-// libstdc++'s std::max / std::min selection rule (NaN behaviour included)
+// libstdc++'s std::max / std::min selection rule (NaN behaviour included; FP64: the
+// comparison on the integer pipes, exact64.cuh, the same selection for non-NaN operands)
 template <class S> CFD_HD S smax(S a, S b) { return (val(a) < val(b)) ? b : a; }
 template <class S> CFD_HD S smin(S a, S b) { return (val(b) < val(a)) ? b : a; }
+CFD_HD double smax(double a, double b) { return lt_exact(a, b) ? b : a; }
+CFD_HD double smin(double a, double b) { return lt_exact(b, a) ? b : a; }
 
 // Flow constants seen by the kernels (set on the host from the Solver setters).
 template <class R>
@@ -59,9 +63,23 @@ struct Flow {
     // SST (no reference counterpart; parity unpinned)
     R k_inf, w_inf, Pr_t;
     R inv_Pr, inv_Prt;  // RN(1 / Pr), RN(1 / Pr_t): quotients by them through quot_by_recip
+    // per-flow constants the face and cell functions would otherwise form per call (FP64:
+    // each the same bits as the expression it replaces): gamma - 1, RN(1 / (gamma - 1)),
+    // Cp = RN(gamma Rgas / (gamma - 1))
+    R gm1, igm1, Cp;
     int bcset, flux, spatial, viscous;
     int sst;    // 1: the state carries rhok, rhow (SST)
 };
+
+// The derived constants of F from gam, Rgas, Pr and Pr_t (correctly rounded divisions).
+template <class R>
+inline void flow_derived(Flow<R>& F) {
+    F.inv_Pr = R(1) / F.Pr;
+    F.inv_Prt = R(1) / F.Pr_t;
+    F.gm1 = F.gam - R(1);
+    F.igm1 = R(1) / F.gm1;
+    F.Cp = F.gam * F.Rgas / F.gm1;
+}
 
 // Conservative state with its derived primitives u, v, p (reference formulas).
 template <class S>
@@ -74,7 +92,7 @@ struct CS {
 template <class S, class R>
 CFD_HD S pressure(const Flow<R>& F, S r, S ru, S rv, S rE) {
     S V2 = (ru * ru + rv * rv) / (r * r);
-    return (F.gam - R(1.0)) * (rE - R(0.5) * r * V2);
+    return F.gm1 * (rE - half(r) * V2);
 }
 
 template <class S, class R>
@@ -91,8 +109,7 @@ CFD_HD CS<S> make_cs(const Flow<R>& F, S r, S ru, S rv, S rE, S rk, S rw) {
 // primitiveToConservative (src/Solver.cpp:498-501)
 template <class S, class R>
 CFD_HD CS<S> p2c(const Flow<R>& F, S r, S u, S v, S p, S k, S w) {
-    const R gm1 = F.gam - R(1.0);
-    S rE = div_shared(p, gm1, recip_for(gm1)) + R(0.5) * r * (u * u + v * v);  // 1/(gamma-1) shared
+    S rE = div_shared(p, F.gm1, F.igm1) + half(r) * (u * u + v * v);
     return make_cs(F, r, r * u, r * v, rE, r * k, r * w);
 }
 
@@ -122,12 +139,12 @@ CFD_HD Flux6<S> flux_llf(const Flow<R>& F, const CS<S>& L, const CS<S>& Rt, R nx
     S unR = Rt.u * nx + Rt.v * ny;
     S cR = sqrt(quot_shared(F.gam * Rt.p, Rt.r, recip_for(Rt.r)));
     S a = smax(fabs(unL) + cL, fabs(unR) + cR);
-    S ha = R(0.5) * a;
+    S ha = half(a);
     S UL[6] = {L.r, L.ru, L.rv, L.rE, L.rk, L.rw};
     S UR[6] = {Rt.r, Rt.ru, Rt.rv, Rt.rE, Rt.rk, Rt.rw};
     Flux6<S> o;
 #pragma unroll
-    for (int c = 0; c < 6; ++c) o.f[c] = (FL.f[c] + FR.f[c]) * R(0.5) - (UR[c] - UL[c]) * ha;
+    for (int c = 0; c < 6; ++c) o.f[c] = half(FL.f[c] + FR.f[c]) - (UR[c] - UL[c]) * ha;
     return o;
 }
 
@@ -142,7 +159,7 @@ CFD_HD Flux6<S> flux_roe(const Flow<R>& F, const CS<S>& L, const CS<S>& Rt, R nx
     S vt = (sL * L.v + sR * Rt.v) * inv;
     S ht = (sL * hL + sR * hR) * inv;
     S V2 = ut * ut + vt * vt;
-    S c2 = (F.gam - R(1.0)) * (ht - R(0.5) * V2);
+    S c2 = F.gm1 * (ht - half(V2));
     S ct = sqrt(smax(c2, S(R(1e-8))));
     S unt = ut * nx + vt * ny;
     S utt = -ut * ny + vt * nx;
@@ -150,7 +167,7 @@ CFD_HD Flux6<S> flux_roe(const Flow<R>& F, const CS<S>& L, const CS<S>& Rt, R nx
     S eps = R(0.1) * ct;
 #pragma unroll
     for (int i = 0; i < 4; ++i) {
-        if (val(fabs(lam[i])) < val(eps)) lam[i] = R(0.5) * (lam[i] * lam[i] / eps + eps);
+        if (lt(fabs(lam[i]), eps)) lam[i] = half(lam[i] * lam[i] / eps + eps);
         lam[i] = fabs(lam[i]);
     }
     S dr = Rt.r - L.r, du = Rt.u - L.u, dv = Rt.v - L.v, dp = Rt.p - L.p;
@@ -166,13 +183,13 @@ CFD_HD Flux6<S> flux_roe(const Flow<R>& F, const CS<S>& L, const CS<S>& Rt, R nx
     D[0] = w1 * R(1.0) + w2 * R(1.0) + w3 * R(0.0) + w4 * R(1.0);
     D[1] = w1 * (ut - ct * nx) + w2 * ut + w3 * (-ny) + w4 * (ut + ct * nx);
     D[2] = w1 * (vt - ct * ny) + w2 * vt + w3 * nx + w4 * (vt + ct * ny);
-    D[3] = w1 * (ht - unt * ct) + w2 * (R(0.5) * V2) + w3 * utt + w4 * (ht + unt * ct);
+    D[3] = w1 * (ht - unt * ct) + w2 * half(V2) + w3 * utt + w4 * (ht + unt * ct);
     D[4] = fabs(unt) * (quot_shared(Rt.rk, Rt.r, recip_for(Rt.r)) - quot_shared(L.rk, L.r, recip_for(L.r))) * rt;
     D[5] = fabs(unt) * (quot_shared(Rt.rw, Rt.r, recip_for(Rt.r)) - quot_shared(L.rw, L.r, recip_for(L.r))) * rt;
     Flux6<S> FL = normal_flux(L, nx, ny), FR = normal_flux(Rt, nx, ny);
     Flux6<S> o;
 #pragma unroll
-    for (int c = 0; c < 6; ++c) o.f[c] = (FL.f[c] + FR.f[c]) * R(0.5) - D[c] * R(0.5);
+    for (int c = 0; c < 6; ++c) o.f[c] = half(FL.f[c] + FR.f[c]) - half(D[c]);
     return o;
 }
 
@@ -189,17 +206,18 @@ CFD_HD Flux6<S> flux_hllc(const Flow<R>& F, const CS<S>& L, const CS<S>& Rt, R n
     S vt = quot_shared(sL * L.v + sR * Rt.v, sL + sR, iLR);
     S ht = quot_shared(sL * hL + sR * hR, sL + sR, iLR);
     S unt = ut * nx + vt * ny;
-    S ct = sqrt((F.gam - R(1.0)) * (ht - R(0.5) * (ut * ut + vt * vt)));
+    S ct = sqrt(F.gm1 * (ht - half(ut * ut + vt * vt)));
     S SL = smin(unL - cL, unt - ct);
     S SR = smax(unR + cR, unt + ct);
     S Ss = (Rt.p - L.p + L.r * unL * (SL - unL) - Rt.r * unR * (SR - unR)) /
            (L.r * (SL - unL) - Rt.r * (SR - unR));
-    if (val(SL) >= R(0.0)) return normal_flux(L, nx, ny);
-    if (val(SR) <= R(0.0)) return normal_flux(Rt, nx, ny);
-    const CS<S>& K = (val(Ss) >= R(0.0)) ? L : Rt;
-    S SK = (val(Ss) >= R(0.0)) ? SL : SR;
-    S unK = (val(Ss) >= R(0.0)) ? unL : unR;
-    const S iK = (val(Ss) >= R(0.0)) ? recip_for(L.r) : recip_for(Rt.r);  // the sound speeds' reciprocals
+    if (ge0(SL)) return normal_flux(L, nx, ny);
+    if (le0(SR)) return normal_flux(Rt, nx, ny);
+    const bool left = ge0(Ss);
+    const CS<S>& K = left ? L : Rt;
+    S SK = left ? SL : SR;
+    S unK = left ? unL : unR;
+    const S iK = left ? recip_for(L.r) : recip_for(Rt.r);  // the sound speeds' reciprocals
     S coef = K.r * (SK - unK) / (SK - Ss);
     S Us[6];
     Us[0] = coef;
@@ -274,7 +292,7 @@ CFD_HD CS<S> ghost_state(const Flow<R>& F, const CS<S>& U, int tag, R nx, R ny, 
             S rg = pu / (F.Rgas * Tg);
             R Cp = g * F.Rgas / (g - R(1.0));
             S V2 = R(2.0) * Cp * (F.T0 - Tg);
-            S V = (val(V2) > R(0)) ? sqrt(V2) : S(R(0.0));
+            S V = gt0(V2) ? sqrt(V2) : S(R(0.0));
             return sst_ghost(F, p2c(F, rg, V, S(R(0.0)), pu, S(R(0)), S(R(0))), U, 0, dwall);
         } else if (tag == 2) {
             return sst_ghost(F, p2c(F, U.r, U.u, U.v, S(F.Pexit), S(R(0)), S(R(0))), U, 1, dwall);
@@ -305,7 +323,7 @@ CFD_HD CS<S> ghost_state(const Flow<R>& F, const CS<S>& U, int tag, R nx, R ny, 
         if (tag == 3) return slip_ghost(F, U, nx, ny);
         if (tag == 4) {
             S ug = -(U.ru / U.r), vg = -(U.rv / U.r);
-            S ek = R(0.5) * (U.ru * U.ru + U.rv * U.rv) / U.r;
+            S ek = half(U.ru * U.ru + U.rv * U.rv) / U.r;
             S pin = (g - R(1.0)) * (U.rE - ek);
             S Tin = pin / (U.r * F.Rgas);
             S rg = pin / (F.Rgas * Tin);

@@ -220,7 +220,7 @@ __device__ __forceinline__ void grad_item(const MeshView<R>& m, const Flow<R>& F
         pmin = smin(pmin, val(wj[W_P]));
 #pragma unroll
         for (int q = 0; q < NQ; ++q) {
-            S ph = R(0.5) * (wi[q] + wj[q]);
+            S ph = half(wi[q] + wj[q]);
             S tx = ph * nx * A, ty = ph * ny * A;
             if (side) {
                 acc[2 * q] = acc[2 * q] - tx;
@@ -260,12 +260,12 @@ __device__ __forceinline__ void grad_item(const MeshView<R>& m, const Flow<R>& F
         R a = R(1.0);
         // a = min(1, x / y): when x / y >= 1 exactly (x >= y > 0, or x <= y < 0) the rounded
         // quotient is >= 1 too and a is 1: the divide runs only for the faces that limit
-        if (d2 > R(0.0)) {
+        if (gt0(d2)) {
             const R x = pmax - pc, y = d2 + eps;
-            if (!(x >= y)) a = smin(R(1.0), x / y);
-        } else if (d2 < R(0.0)) {
+            if (lt(x, y)) a = smin(R(1.0), x / y);
+        } else if (lt0(d2)) {
             const R x = pmin - pc, y = d2 - eps;
-            if (!(x <= y)) a = smin(R(1.0), x / y);
+            if (lt(y, x)) a = smin(R(1.0), x / y);
         }
         lim = smin(lim, a);
     }

@@ -250,14 +250,13 @@ struct cfdg_solver {
             F.w_inf = ww;
         }
         F.Pr_t = 0.9;
-        // correctly rounded reciprocals (host IEEE division) for the kernels' shared-reciprocal quotients
-        F.inv_Pr = 1.0 / F.Pr;
-        F.inv_Prt = 1.0 / F.Pr_t;
+        // correctly rounded reciprocals and quotients (host IEEE division) for the kernels
+        flow_derived(F);
         Ff.gam = (float)F.gam; Ff.Rgas = (float)F.Rgas; Ff.Pr = (float)F.Pr; Ff.nu = (float)F.nu;
         Ff.Minf = (float)F.Minf; Ff.P0 = (float)F.P0; Ff.T0 = (float)F.T0; Ff.Pexit = (float)F.Pexit;
         for (int k = 0; k < 4; ++k) { Ff.fs[k] = (float)F.fs[k]; Ff.shock[k] = (float)F.shock[k]; }
         Ff.k_inf = (float)F.k_inf; Ff.w_inf = (float)F.w_inf; Ff.Pr_t = (float)F.Pr_t;
-        Ff.inv_Pr = (float)F.inv_Pr; Ff.inv_Prt = (float)F.inv_Prt;
+        flow_derived(Ff);
         Ff.bcset = F.bcset; Ff.flux = F.flux; Ff.spatial = F.spatial; Ff.viscous = F.viscous; Ff.sst = F.sst;
     }
 

@@ -46,16 +46,16 @@ CFD_HD SstCell<S> sst_cell(const Flow<R>& F, S r, S k, S w, S ux, S uy, S vx, S 
     const R bs = R(C::beta_s), a1 = R(C::a1);
     S kp = smax(k, S(R(0)));
     S wp = smax(w, S(F.w_inf * R(C::w_min_frac)));
-    S Sxy = R(0.5) * (uy + vx);
-    S S2 = R(2) * (ux * ux + vy * vy + R(2) * Sxy * Sxy);
+    S Sxy = half(uy + vx);
+    S S2 = twice(ux * ux + vy * vy + twice(Sxy) * Sxy);
     S Smag = sqrt(S2 + S(R(1e-30)));
     S nu = S(F.nu);
-    R dd = d > R(1e-30) ? d : R(1e-30);
+    R dd = lt(R(1e-30), d) ? d : R(1e-30);
     // one reciprocal per divisor (w, d, CD_kw, the eddy viscosity's denominator)
     const S iwp = R(1) / wp;
     const R idd = R(1) / dd;
     S gkgw = kx * wx + ky * wy;
-    S CDkw = smax(R(2) * r * R(C::sw2) * gkgw * iwp, S(R(1e-10)));
+    S CDkw = smax(twice(r) * R(C::sw2) * gkgw * iwp, S(R(1e-10)));
     S sk = sqrt(kp + S(R(1e-30)));
     S t1 = sk * iwp * (idd / bs);
     S t2 = R(500) * nu * iwp * (idd * idd);
@@ -65,7 +65,7 @@ CFD_HD SstCell<S> sst_cell(const Flow<R>& F, S r, S k, S w, S ux, S uy, S vx, S 
     arg1 = smin(arg1, S(R(10)));
     S a14 = arg1 * arg1 * arg1 * arg1;
     S F1 = tanh_(a14);
-    S arg2 = smin(smax(R(2) * t1, t2), S(R(100)));
+    S arg2 = smin(smax(twice(t1), t2), S(R(100)));
     S F2 = tanh_(arg2 * arg2);
     S mut = r * a1 * kp / smax(a1 * wp, Smag * F2);
     S beta = F1 * R(C::b1) + (R(1) - F1) * R(C::b2);
@@ -99,12 +99,12 @@ CFD_HD void sst_face_flux(const Flow<R>& F, S mdotA, S kL, S wL, S kR, S wR, S r
         const R id2 = R(1) / d2;  // FP64: the two quotients through one reciprocal (div_shared)
         // (phi_face - phi_c) (d . n) / |d|^2, phi_face = 0 for k and w_face for w
         dkn = div_shared((S(R(0)) - kL) * dn, d2, id2);
-        dwn = div_shared((R(0.5) * (wL + wR) - wL) * dn, d2, id2);
+        dwn = div_shared((half(wL + wR) - wL) * dn, d2, id2);
     } else {
-        S kx = R(0.5) * (gkL[0] + gkR[0]), ky = R(0.5) * (gkL[1] + gkR[1]);
-        S wx = R(0.5) * (gkL[2] + gkR[2]), wy = R(0.5) * (gkL[3] + gkR[3]);
+        S kx = half(gkL[0] + gkR[0]), ky = half(gkL[1] + gkR[1]);
+        S wx = half(gkL[2] + gkR[2]), wy = half(gkL[3] + gkR[3]);
         R d2 = dxlr * dxlr + dylr * dylr;
-        if (d2 > R(1e-14)) {
+        if (lt(R(1e-14), d2)) {
             const R id2 = R(1) / d2;  // the viscous flux's reciprocal of the same d2
             S ck = div_shared(kx * dxlr + ky * dylr - (kR - kL), d2, id2);
             S cw = div_shared(wx * dxlr + wy * dylr - (wR - wL), d2, id2);

@@ -13,7 +13,7 @@ Flow<double> flow(const double* p, const int* fl) {
     F.gam = p[0]; F.Rgas = p[1]; F.Pr = p[2]; F.nu = p[3]; F.Minf = p[4]; F.P0 = p[5]; F.T0 = p[6]; F.Pexit = p[7];
     for (int k = 0; k < 4; ++k) { F.fs[k] = p[8 + k]; F.shock[k] = p[12 + k]; }
     F.k_inf = 0; F.w_inf = 0; F.Pr_t = 0.9;
-    F.inv_Pr = 1.0 / F.Pr; F.inv_Prt = 1.0 / F.Pr_t;
+    flow_derived(F);
     F.bcset = fl[0]; F.flux = fl[1]; F.spatial = fl[2]; F.viscous = fl[3];
     return F;
 }
