@@ -79,6 +79,11 @@ void launch_soa_to_aos<float>(long nc, int np, int stride, const float* soa, con
                                  cudaStream_t s) {
     k_soa_to_aos<float><<<blocks_for(nc), tpb_for(nc), 0, s>>>(nc, np, stride, soa, perm, aos);
 }
+template <>
+void launch_soa_to_rows<float>(long nc, int np, int stride, const float* soa, const int* iperm, double* aos,
+                               cudaStream_t s) {
+    k_soa_to_rows<float><<<grid_for(nc, ROW_BLOCK), ROW_BLOCK, 0, s>>>(nc, np, stride, soa, iperm, aos);
+}
 
 __global__ void k_convert_f32(long n, const double* __restrict__ in, float* __restrict__ out) {
     for (long q = (long)blockIdx.x * blockDim.x + threadIdx.x; q < n; q += (long)gridDim.x * blockDim.x) out[q] = (float)in[q];

@@ -8,7 +8,7 @@ template <int NV>
 static void residual_nv(const ResArgs<double>& a) {
     long nc = a.m.nc, nf = a.m.nf;
     if (a.ev) cudaEventRecord(a.ev[0], a.stream);
-    k_prim<double, NV><<<blocks_for(nc), tpb_for(nc), 0, a.stream>>>((int)nc, a.F, a.U, a.W);
+    if (!a.prim_done) k_prim<double, NV><<<blocks_for(nc), tpb_for(nc), 0, a.stream>>>((int)nc, a.F, a.U, a.W);
     if (a.ev) cudaEventRecord(a.ev[1], a.stream);
     k_grad64<NV><<<blocks_for(nc), tpb_for(nc), 0, a.stream>>>(a.m, a.F, a.U, a.W, a.G, a.phi, a.do_limiter, a.lim_dev);
     if (NV == 6) k_sst_cell<double, NV><<<blocks_for(nc), tpb_for(nc), 0, a.stream>>>(a.m, a.F, a.W, a.G, a.dwall, a.T, nullptr);
@@ -18,7 +18,11 @@ static void residual_nv(const ResArgs<double>& a) {
         k_flux64<NV><<<grid_for(nf, (int)t), t, 0, a.stream>>>(a.m, a.F, a.U, a.W, a.G, a.phi, a.FA, a.T);
     }
     if (a.ev) cudaEventRecord(a.ev[3], a.stream);
-    if (a.norms_out)
+    if (a.rows_out)
+        k_gather_rows<NV><<<grid_for(nc, ROW_BLOCK), ROW_BLOCK, 0, a.stream>>>(a.m, a.FA.v, a.FA.n,
+                                                                               NV == 6 ? a.T.v + 2 * nc : nullptr,
+                                                                               a.iperm, a.rows_out);
+    else if (a.norms_out)
         k_gather_norms<NV><<<red_grid(nc), RED_THREADS, 0, a.stream>>>(a.m, a.FA.v, a.FA.n, a.out,
                                                                         NV == 6 ? a.T.v + 2 * nc : nullptr, a.rhs_out,
                                                                         a.rs, a.norms_out, a.flag);
@@ -37,6 +41,21 @@ void launch_residual<double>(const ResArgs<double>& a) {
 void launch_prim64(int nv, long nc, const Flow<double>& F, Field<double> U, Field<double> W, cudaStream_t s) {
     if (nv == 6) k_prim<double, 6><<<blocks_for(nc), tpb_for(nc), 0, s>>>((int)nc, F, U, W);
     else k_prim<double, 4><<<blocks_for(nc), tpb_for(nc), 0, s>>>((int)nc, F, U, W);
+}
+
+void launch_rows_prim(int nv, long nc, const Flow<double>& F, const double* aos, const int* iperm, Field<double> U,
+                      Field<double> W, cudaStream_t s) {
+    if (nv == 6) k_rows_prim<6><<<grid_for(nc, ROW_BLOCK), ROW_BLOCK, 0, s>>>((int)nc, F, aos, iperm, U, W);
+    else k_rows_prim<4><<<grid_for(nc, ROW_BLOCK), ROW_BLOCK, 0, s>>>((int)nc, F, aos, iperm, U, W);
+}
+
+void launch_rows_to_soa(long nc, int np, int stride, const double* aos, const int* iperm, double* soa, cudaStream_t s) {
+    k_rows_to_soa<<<grid_for(nc, ROW_BLOCK), ROW_BLOCK, 0, s>>>(nc, np, stride, aos, iperm, soa);
+}
+template <>
+void launch_soa_to_rows<double>(long nc, int np, int stride, const double* soa, const int* iperm, double* aos,
+                                cudaStream_t s) {
+    k_soa_to_rows<double><<<grid_for(nc, ROW_BLOCK), ROW_BLOCK, 0, s>>>(nc, np, stride, soa, iperm, aos);
 }
 
 

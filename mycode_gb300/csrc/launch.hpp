@@ -39,6 +39,12 @@ struct ResArgs {
     double* norms_out = nullptr;
     int* flag = nullptr;
     RedScratch rs{nullptr, nullptr};
+    // launch_residual<double> of a caller's pinned rows: the primitives are current
+    // (launch_rows_prim formed them with U), and the gather writes the caller's rows of
+    // 6 doubles in place (rows_out, device-visible address) through iperm instead of out
+    bool prim_done = false;
+    double* rows_out = nullptr;
+    const int* iperm = nullptr;
 };
 
 // A kernel launch, with the programmatic stream-serialisation attribute when pdl: the
@@ -88,9 +94,17 @@ template <class T> void launch_aos_to_soa(long nc, int np, int stride, const dou
 template <class T> void launch_soa_to_aos(long nc, int np, int stride, const T* soa, const int* perm, double* aos,
                                           cudaStream_t s);
 template <class T> void launch_convert(long n, const double* in, T* out, cudaStream_t s);
+// a caller's pinned rows (stride doubles, caller numbering; device-visible address) in place:
+// np planes of soa at the rows' internal indices iperm[row] (stride <= ROW_MAX_STRIDE)
+template <class T> void launch_soa_to_rows(long nc, int np, int stride, const T* soa, const int* iperm, double* aos,
+                                           cudaStream_t s);
+void launch_rows_to_soa(long nc, int np, int stride, const double* aos, const int* iperm, double* soa, cudaStream_t s);
 
 // ---- FP64 only (kern_f64.cu)
 void launch_prim64(int nv, long nc, const Flow<double>& F, Field<double> U, Field<double> W, cudaStream_t s);
+// k_prim of a caller's pinned rows (6 doubles each): U and W planes at iperm[row]
+void launch_rows_prim(int nv, long nc, const Flow<double>& F, const double* aos, const int* iperm, Field<double> U,
+                      Field<double> W, cudaStream_t s);
 void launch_fd_perturb(long n, const double* U, const double* v, const double* u_sq, const double* v_sq, double* Up,
                        double* eps, cudaStream_t s);
 void launch_fd_combine(int nv, long nc, const double* Rp, const double* Rb, const double* v, const double* eps,

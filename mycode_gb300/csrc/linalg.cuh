@@ -768,4 +768,32 @@ __global__ void k_soa_to_aos(long nc, int np, int stride, const T* __restrict__ 
     for (int c = 0; c < stride; ++c) aos[dst + c] = c < np ? (double)soa[c * nc + i] : 0.0;
 }
 
+// ---- a caller's pinned AoS array read or written in place over the CPU-GPU link
+// (row staging: residual.cuh rows_load / rows_store)
+// np planes of soa (internal numbering) from a caller's rows of `stride` doubles
+static __global__ void __launch_bounds__(ROW_BLOCK) k_rows_to_soa(long nc, int np, int stride, const double* __restrict__ aos,
+                                                         const int* __restrict__ iperm, double* __restrict__ soa) {
+    __shared__ __align__(16) double sm[ROW_BLOCK * ROW_MAX_STRIDE];
+    long r0;
+    const int rows = rows_load(aos, nc, stride, sm, r0);
+    if ((int)threadIdx.x >= rows) return;
+    const long c = iperm[r0 + threadIdx.x];
+    for (int k = 0; k < np; ++k) soa[k * nc + c] = sm[threadIdx.x * stride + k];
+}
+
+// a caller's rows of `stride` doubles from np planes of soa (slots np..stride-1 zero)
+template <class T>
+__global__ void __launch_bounds__(ROW_BLOCK) k_soa_to_rows(long nc, int np, int stride, const T* __restrict__ soa,
+                                                         const int* __restrict__ iperm, double* __restrict__ aos) {
+    __shared__ __align__(16) double sm[ROW_BLOCK * ROW_MAX_STRIDE];
+    const long r0 = (long)blockIdx.x * ROW_BLOCK;
+    const long left = nc - r0;
+    const int rows = left < ROW_BLOCK ? (int)left : ROW_BLOCK;
+    if ((int)threadIdx.x < rows) {
+        const long c = iperm[r0 + threadIdx.x];
+        for (int k = 0; k < stride; ++k) sm[threadIdx.x * stride + k] = k < np ? (double)soa[k * nc + c] : 0.0;
+    }
+    rows_store(aos, r0, rows, stride, sm);
+}
+
 }  // namespace cfdg

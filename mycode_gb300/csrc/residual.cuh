@@ -496,4 +496,94 @@ __global__ void __launch_bounds__(256) k_gather(MeshView<R> m, const R* __restri
     for (int c = 0; c < NV; ++c) Rout[c * r_stride + i] = acc[c];
 }
 
+// ---------------------------------------------------------------- caller rows in place
+// Caller rows (stride doubles each, the caller's numbering) are moved by the kernels
+// themselves, with no staging buffer or copy engine.  A block owns ROW_BLOCK consecutive
+// rows: it moves them as one contiguous span (consecutive threads, consecutive addresses:
+// every link transaction carries whole lines) through shared memory, and each thread
+// exchanges its row with the SoA planes at the row's internal index iperm[row].  (One
+// thread per row, reading its row's doubles one by one, moved every line of the span
+// `stride` times: a quarter of the copy engines' rate.)  Launched with ROW_BLOCK threads.
+constexpr int ROW_BLOCK = 256;
+constexpr int ROW_MAX_STRIDE = 14;
+
+// rows [r0, r0 + rows) of aos into sm (rows * stride doubles); returns rows
+__device__ __forceinline__ int rows_load(const double* __restrict__ aos, long nrows, int stride, double* sm, long& r0) {
+    r0 = (long)blockIdx.x * ROW_BLOCK;
+    const long left = nrows - r0;
+    const int rows = left < ROW_BLOCK ? (int)left : ROW_BLOCK;
+    const long n = (long)rows * stride;
+    const double* src = aos + r0 * stride;
+    if ((stride & 1) == 0 && (reinterpret_cast<size_t>(src) & 15) == 0) {
+        const double2* s2 = reinterpret_cast<const double2*>(src);
+        double2* d2 = reinterpret_cast<double2*>(sm);
+        for (long q = threadIdx.x; q < n / 2; q += ROW_BLOCK) d2[q] = s2[q];
+    } else {
+        for (long q = threadIdx.x; q < n; q += ROW_BLOCK) sm[q] = src[q];
+    }
+    __syncthreads();
+    return rows;
+}
+
+__device__ __forceinline__ void rows_store(double* __restrict__ aos, long r0, int rows, int stride, const double* sm) {
+    __syncthreads();
+    const long n = (long)rows * stride;
+    double* dst = aos + r0 * stride;
+    if ((stride & 1) == 0 && (reinterpret_cast<size_t>(dst) & 15) == 0) {
+        const double2* s2 = reinterpret_cast<const double2*>(sm);
+        double2* d2 = reinterpret_cast<double2*>(dst);
+        for (long q = threadIdx.x; q < n / 2; q += ROW_BLOCK) d2[q] = s2[q];
+    } else {
+        for (long q = threadIdx.x; q < n; q += ROW_BLOCK) dst[q] = sm[q];
+    }
+}
+
+// The first and last stage of a residual evaluation whose state and residual live in a
+// caller's pinned AoS arrays (6 doubles per cell, the caller's numbering): the rows cross
+// the CPU-GPU link inside these kernels (staged in shared memory by rows_load /
+// rows_store), so the link transfer overlaps the primitives' and the gather's arithmetic
+// instead of preceding and following it.  Same arithmetic as k_prim and k_gather.
+
+// k_prim of the caller's rows: U planes and W planes at each row's internal index
+template <int NV>
+__global__ void __launch_bounds__(ROW_BLOCK) k_rows_prim(int nc, Flow<double> F, const double* __restrict__ aos,
+                                                       const int* __restrict__ iperm, Field<double> U, Field<double> W) {
+    __shared__ __align__(16) double sm[ROW_BLOCK * 6];
+    long r0;
+    const int rows = rows_load(aos, nc, 6, sm, r0);
+    if ((int)threadIdx.x >= rows) return;
+    const double* row = sm + threadIdx.x * 6;
+    const long c = iperm[r0 + threadIdx.x];
+    const double r = row[0], ru = row[1], rv = row[2], rE = row[3];
+    const double rk = NV == 6 ? row[4] : 0.0, rw = NV == 6 ? row[5] : 0.0;
+    U.v[c] = r;
+    U.v[U.n + c] = ru;
+    U.v[2 * U.n + c] = rv;
+    U.v[3 * U.n + c] = rE;
+    if (NV == 6) {
+        U.v[4 * U.n + c] = rk;
+        U.v[5 * U.n + c] = rw;
+    }
+    prim_cell<double, NV>(F, r, ru, rv, rE, rk, rw, W, c);
+}
+
+// k_gather into the caller's rows (slots NV..5 zero)
+template <int NV>
+__global__ void __launch_bounds__(ROW_BLOCK) k_gather_rows(MeshView<double> m, const double* __restrict__ FA,
+                                                         long fa_stride, const double* __restrict__ src,
+                                                         const int* __restrict__ iperm, double* __restrict__ aos) {
+    __shared__ __align__(16) double sm[ROW_BLOCK * 6];
+    const long r0 = (long)blockIdx.x * ROW_BLOCK;
+    const long left = (long)m.nc - r0;
+    const int rows = left < ROW_BLOCK ? (int)left : ROW_BLOCK;
+    if ((int)threadIdx.x < rows) {
+        const long c = iperm[r0 + threadIdx.x];
+        double acc[NV];
+        gather_cell<double, NV>(m, FA, fa_stride, src, m.nc, c, acc);
+#pragma unroll
+        for (int k = 0; k < 6; ++k) sm[threadIdx.x * 6 + k] = k < NV ? acc[k] : 0.0;
+    }
+    rows_store(aos, r0, rows, 6, sm);
+}
+
 }  // namespace cfdg

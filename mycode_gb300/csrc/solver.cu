@@ -103,6 +103,7 @@ struct cfdg_solver {
     Flow<float> Ff;
     // device mesh
     int *cf = nullptr, *fo = nullptr, *fn = nullptr, *ftag = nullptr, *perm = nullptr;
+    int* iperm = nullptr;  // [nc] caller cell -> internal cell (the inverse of perm)
     GeoBuf<double> g64;
     GeoBuf<float> g32;
     MeshView<double> mv;
@@ -310,8 +311,10 @@ struct cfdg_solver {
     // scal[8..11] and clears the update's non-finite flag (k_gather_norms; `flag`, default
     // bad).  lim_dev: the limiter is recomputed only where *lim_dev is also set (a chained
     // Newton step, whose limiter-freeze decision is taken on the device).
+    // prim_done: W already holds Uin's primitives (launch_rows_prim); rows_out: the gather
+    // writes the residual into a caller's pinned rows in place (device-visible address)
     cfdg_status residual_dev(double* Uin, double* out, int update_limiters, bool norms = false, int* flag = nullptr,
-                             const int* lim_dev = nullptr) {
+                             const int* lim_dev = nullptr, bool prim_done = false, double* rows_out = nullptr) {
         int do_lim = (cfg.spatial == CFDG_SECOND_ORDER_LIMITED && update_limiters) ? 1 : 0;
         ResArgs<double> a = res64(Uin, out, do_lim);
         if (norms) {
@@ -321,58 +324,41 @@ struct cfdg_solver {
             a.rs = rs;
         }
         a.lim_dev = lim_dev;
+        a.prim_done = prim_done;
+        a.rows_out = rows_out;
+        a.iperm = iperm;
         a.ev = take_events(0);
         launch_residual<double>(a);
-        launches += nv == 6 ? 5 : 4;
+        launches += (nv == 6 ? 5 : 4) - (prim_done ? 1 : 0);
         if (do_lim) limiter_valid = true;
         CK(cudaGetLastError());
         return CFDG_OK;
     }
 
-    // Host <-> staging copies.  A large pinned buffer is split over COPY_PARTS streams, so
-    // that several copy engines share the transfer; a pageable one is one copy (staged by
-    // the driver).  The copies are ordered after the work enqueued on st and st waits for
-    // them.
-    static constexpr int COPY_PARTS = 4;
-    cudaStream_t cst[COPY_PARTS] = {};
-    cudaEvent_t cev[COPY_PARTS + 1] = {};
-    static bool pinned(const void* host) {
+    // Device-visible address of a caller's page-locked host buffer, nullptr when it is
+    // pageable.  Pinned buffers are read and written in place by the row kernels
+    // (residual.cuh rows_load / rows_store) over the CPU-GPU link; pageable ones go through
+    // the device staging buffer and a copy.
+    static double* mapped(const void* host) {
         cudaPointerAttributes a;
         if (cudaPointerGetAttributes(&a, host) != cudaSuccess) {
             cudaGetLastError();
-            return false;
+            return nullptr;
         }
-        return a.type == cudaMemoryTypeHost;
-    }
-    cfdg_status copy_parts(void* dst, const void* src, size_t bytes, cudaMemcpyKind kind, const void* host) {
-        if (bytes < (16u << 20) || !pinned(host)) {
-            CK(cudaMemcpyAsync(dst, src, bytes, kind, st));
-            return CFDG_OK;
-        }
-        if (!cst[0]) {
-            for (int k = 0; k < COPY_PARTS; ++k) CK(cudaStreamCreateWithFlags(&cst[k], cudaStreamNonBlocking));
-            for (int k = 0; k <= COPY_PARTS; ++k) CK(cudaEventCreateWithFlags(&cev[k], cudaEventDisableTiming));
-        }
-        CK(cudaEventRecord(cev[COPY_PARTS], st));
-        const size_t part = (bytes / COPY_PARTS + 255) & ~size_t(255);
-        for (int k = 0; k < COPY_PARTS; ++k) {
-            const size_t off = part * k;
-            const size_t len = off >= bytes ? 0 : std::min(part, bytes - off);
-            CK(cudaStreamWaitEvent(cst[k], cev[COPY_PARTS], 0));
-            if (len) CK(cudaMemcpyAsync(static_cast<char*>(dst) + off, static_cast<const char*>(src) + off, len, kind, cst[k]));
-            CK(cudaEventRecord(cev[k], cst[k]));
-            CK(cudaStreamWaitEvent(st, cev[k], 0));
-        }
-        return CFDG_OK;
+        if (a.type != cudaMemoryTypeHost || !a.devicePointer) return nullptr;
+        return static_cast<double*>(a.devicePointer);
     }
 
     // A caller's AoS array (reference numbering, 6 per cell) into np SoA planes (new
-    // numbering), through the staging buffer; only enqueues (the entry point synchronises
-    // before it returns)
+    // numbering); only enqueues (the entry point synchronises before it returns)
     cfdg_status upload_aos(const double* host, double* dev_soa, int np = -1) {
         if (np < 0) np = nv;
-        TRY(copy_parts(stage, host, sizeof(double) * 6 * (size_t)nc, cudaMemcpyHostToDevice, host));
-        launch_aos_to_soa<double>(nc, np, 6, stage, perm, dev_soa, st);
+        if (double* hp = mapped(host)) {
+            launch_rows_to_soa(nc, np, 6, hp, iperm, dev_soa, st);
+        } else {
+            CK(cudaMemcpyAsync(stage, host, sizeof(double) * 6 * (size_t)nc, cudaMemcpyHostToDevice, st));
+            launch_aos_to_soa<double>(nc, np, 6, stage, perm, dev_soa, st);
+        }
         ++launches;
         CK(cudaGetLastError());
         return CFDG_OK;
@@ -380,20 +366,29 @@ struct cfdg_solver {
 
     // np SoA planes into a caller's AoS array (stride doubles per cell, zeros past np)
     cfdg_status download_aos(const double* dev_soa, double* host, int np, int stride) {
-        launch_soa_to_aos<double>(nc, np, stride, dev_soa, perm, stage, st);
+        double* hp = stride <= ROW_MAX_STRIDE ? mapped(host) : nullptr;
+        if (hp) {
+            launch_soa_to_rows<double>(nc, np, stride, dev_soa, iperm, hp, st);
+        } else {
+            launch_soa_to_aos<double>(nc, np, stride, dev_soa, perm, stage, st);
+            CK(cudaMemcpyAsync(host, stage, sizeof(double) * stride * (size_t)nc, cudaMemcpyDeviceToHost, st));
+        }
         ++launches;
         CK(cudaGetLastError());
-        TRY(copy_parts(host, stage, sizeof(double) * stride * (size_t)nc, cudaMemcpyDeviceToHost, host));
         CK(cudaStreamSynchronize(st));
         collect();
         return CFDG_OK;
     }
 
     cfdg_status download_aos32(const float* dev_soa, double* host) {
-        launch_soa_to_aos<float>(nc, nv, 6, dev_soa, perm, stage, st);
+        if (double* hp = mapped(host)) {
+            launch_soa_to_rows<float>(nc, nv, 6, dev_soa, iperm, hp, st);
+        } else {
+            launch_soa_to_aos<float>(nc, nv, 6, dev_soa, perm, stage, st);
+            CK(cudaMemcpyAsync(host, stage, sizeof(double) * 6 * (size_t)nc, cudaMemcpyDeviceToHost, st));
+        }
         ++launches;
         CK(cudaGetLastError());
-        CK(cudaMemcpyAsync(host, stage, sizeof(double) * 6 * (size_t)nc, cudaMemcpyDeviceToHost, st));
         CK(cudaStreamSynchronize(st));
         collect();
         return CFDG_OK;
@@ -1518,7 +1513,7 @@ struct cfdg_solver {
         cudaFree(dinv64);
         void* pt[] = {Tt, Tj, Tjd, dwall, T32, T32d, dwall32};
         for (void* p : pt) cudaFree(p);
-        void* ps[] = {cf, fo, fn, ftag, perm, U, W, G, phi, FA, R, dt, D, stage, Ub, Rb, Up, Rp, vtmp, x, rhs,
+        void* ps[] = {cf, fo, fn, ftag, perm, iperm, U, W, G, phi, FA, R, dt, D, stage, Ub, Rb, Up, Rp, vtmp, x, rhs,
                       Wj, Wjd, Gj, Gjd, FAjd, U32, W32, W32d, G32, G32d, FA32d, phi32, dt32, V32, z32, V, z,
                       rs.partial, rs.counter, scal, bad};
         for (void* p : ps) cudaFree(p);
@@ -1535,8 +1530,6 @@ struct cfdg_solver {
         if (gexec) cudaGraphExecDestroy(gexec);
         for (auto& e : pool) cudaEventDestroy(e);
         for (auto& e : step_ev) if (e) cudaEventDestroy(e);
-        for (auto& e : cst) if (e) cudaStreamDestroy(e);
-        for (auto& e : cev) if (e) cudaEventDestroy(e);
         if (st) cudaStreamDestroy(st);
     }
 };
@@ -1734,6 +1727,13 @@ cfdg_status cfdg_solver_create(const cfdg_mesh* m, const cfdg_config* cfg, cfdg_
         cudaMemcpy(s->ftag, h.ftag.data(), sizeof(int) * nf, cudaMemcpyHostToDevice) != cudaSuccess ||
         cudaMemcpy(s->perm, h.cell_perm.data(), sizeof(int) * nc, cudaMemcpyHostToDevice) != cudaSuccess)
         return bail(fail(CFDG_ERR_CUDA, "mesh upload failed"));
+    {
+        std::vector<int> ip((size_t)nc);
+        for (int i = 0; i < nc; ++i) ip[(size_t)h.cell_perm[i]] = i;
+        TRYS(dalloc(&s->iperm, nc));
+        if (cudaMemcpy(s->iperm, ip.data(), sizeof(int) * nc, cudaMemcpyHostToDevice) != cudaSuccess)
+            return bail(fail(CFDG_ERR_CUDA, "mesh upload failed"));
+    }
     TRYS(upload_geo(s->g64, h));
     TRYS(upload_geo(s->g32, h));
     auto view = [&](auto& g, auto& mvx) {
@@ -1905,6 +1905,23 @@ cfdg_status cfdg_get_state(cfdg_solver* s, double* U) {
 
 cfdg_status cfdg_residual(cfdg_solver* s, const double* U, double* R, int update_limiters) {
     if (!s || !R) return fail(CFDG_ERR_ARG, "null argument");
+    double* hR = s->mapped(R);
+    double* hU = U ? s->mapped(U) : nullptr;
+    if (hR && (!U || hU)) {
+        // pinned state and residual: the primitives are formed as U's rows arrive over the
+        // link, and the gather writes R's rows back in place (the transfers overlap the
+        // first and the last stage)
+        double* Uin = s->U;
+        if (U) {
+            launch_rows_prim(s->nv, s->nc, s->F, hU, s->iperm, s->f64(s->Ub), s->f64(s->W), s->st);
+            ++s->launches;
+            Uin = s->Ub;
+        }
+        TRY(s->residual_dev(Uin, s->R, update_limiters, false, nullptr, nullptr, U != nullptr, hR));
+        CK(cudaStreamSynchronize(s->st));
+        s->collect();
+        return CFDG_OK;
+    }
     double* Uin = s->U;
     if (U) {
         TRY(s->upload_aos(U, s->Ub));

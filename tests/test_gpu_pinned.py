@@ -1,6 +1,8 @@
 """Pinned host buffers: the library reads and writes the caller's page-locked AoS arrays in
-place (the renumbering kernel works over the CPU-GPU link, no staging copy).  The results
-must be the same bits as through pageable buffers (the copy-engine path)."""
+place over the CPU-GPU link (row kernels staging whole blocks of rows in shared memory; the
+residual's primitive and gather stages take and give the rows themselves), with no staging
+copy.  The results must be the same bits as through pageable buffers (the copy-engine
+path)."""
 import numpy as np
 import pytest
 
