@@ -150,10 +150,10 @@ def krylov_bytes(stage: str, nc: int, nf: int, nv: int, s: int, jbar: float,
         # pending vector out), then U and 1/D in, z and the primitives' derivatives out
         return nc * (nv * s + s + nv * s + nq * s) + L * s * (jbar + 4)
     if stage == "grad":
-        # the primitives' derivatives in, the gradients' derivatives out, the face list; the
-        # SST cell kernel: primitives and gradients (value + derivative) and d in, the cell
-        # terms' derivatives out
-        b = nc * (nq * s + ng * s + 16)
+        # the primitives' derivatives in, the gradients' derivatives out, the face list, each
+        # face's two cells, normal and area once; the SST cell kernel: primitives and
+        # gradients (value + derivative) and d in, the cell terms' derivatives out
+        b = nc * (nq * s + ng * s + 16) + nf * (8 + 3 * s)
         if nv == 6:
             b += nc * (2 * nq * s + 2 * ng * s + s + 4 * s)
         return b

@@ -33,8 +33,12 @@ static void jv_mid_nv(const ResArgs<R>& a) {
     Field<R> Gw = a.G, Tw = a.T;
     if (a.tangent) Gw.v = Tw.v = nullptr;
     if (a.ev) cudaEventRecord(a.ev[0], a.stream);
-    launch_k(a.pdl, k_grad<S, NV, R>, dim3(blocks_for(nc)), dim3(tpb_for(nc)), a.stream, a.m, a.F, a.U, a.W, Gw,
-             a.phi, 0, a.done, (const int*)nullptr);
+    if (a.cfx.nbr)
+        launch_k(a.pdl, k_grad_cf<S, NV, R>, dim3(blocks_for(nc)), dim3(tpb_for(nc)), a.stream, a.m, a.cfx, a.F, a.U,
+                 a.W, Gw, a.phi, 0, a.done);
+    else
+        launch_k(a.pdl, k_grad<S, NV, R>, dim3(blocks_for(nc)), dim3(tpb_for(nc)), a.stream, a.m, a.F, a.U, a.W, Gw,
+                 a.phi, 0, a.done, (const int*)nullptr);
     if (NV == 6)
         launch_k(a.pdl, k_sst_cell<S, NV, R>, dim3(blocks_for(nc)), dim3(tpb_for(nc)), a.stream, a.m, a.F, a.W, a.G,
                  a.dwall, Tw, a.done);

@@ -45,6 +45,9 @@ struct ResArgs {
     bool prim_done = false;
     double* rows_out = nullptr;
     const int* iperm = nullptr;
+    // launch_jv_mid: per-cell neighbours and face geometry for the gradient kernel
+    // (k_grad_cf) when cfx.nbr is set
+    CellFaces<R> cfx{nullptr, nullptr, nullptr, nullptr};
 };
 
 // A kernel launch, with the programmatic stream-serialisation attribute when pdl: the

@@ -41,6 +41,19 @@ struct MeshView {
     const R* vol;      // [nc]
 };
 
+// Per-cell copies of each face entry's neighbour cell and face geometry, [4][nc] planes
+// beside cf (the neighbour -1 for boundary entries and pads, the geometry 0 for pads): a
+// gradient kernel given them reads them with the cell's own coalesced loads, so its only
+// dependent loads are the neighbours' primitives (through the face index, the neighbour
+// and the geometry are a second dependent level).  The values are the face arrays' own.
+template <class R>
+struct CellFaces {
+    const int* nbr;
+    const R* nx;
+    const R* ny;
+    const R* A;
+};
+
 // A field of `planes` SoA planes of length n: value planes v and, for Dual kernels,
 // derivative planes d (nullptr for real-valued kernels).
 template <class R>
@@ -140,17 +153,20 @@ __global__ void __launch_bounds__(256) k_prim(int nc, Flow<R> F, Field<R> U, Fie
 // computeGradients (src/Solver.cpp:81-149) as a per-cell gather over the cell's faces
 // in reference face order, then (limited scheme, limiter not frozen) computeLimiters
 // (src/Solver.cpp:152-253) for the same cell from its own fresh gradient.
-template <class S, int NV, class R>
+// CF: the tangent-only gradient of a Krylov body (S a dual number, derivative planes
+// written, no limiter), with the neighbours and face geometry from cx (CellFaces) instead
+// of through the faces; everything else as the generic kernel computes it
+template <class S, int NV, class R, bool CF = false>
 __device__ __forceinline__ void grad_item(const MeshView<R>& m, const Flow<R>& F, const Field<R>& U,
                                           const Field<R>& W, const Field<R>& G, R* phi, int do_limiter, long i,
-                                          const int* done = nullptr) {
+                                          const int* done = nullptr, CellFaces<R> cx = {}) {
     // done: a finished Krylov solve (krylov.cuh); read with the mesh loads, tested after
     const int skip = done ? *done : 0;
     constexpr int NQ = NV == 6 ? 7 : 5;
     // a dual gradient with no value planes to write (J v about a fixed point whose value
     // planes are current): the face sums' derivatives need only the neighbours' derivative
     // planes (the ghost states read the cell's own values)
-    const bool tangent = !std::is_same<S, R>::value && G.v == nullptr && !do_limiter;
+    const bool tangent = CF || (!std::is_same<S, R>::value && G.v == nullptr && !do_limiter);
     // Mesh data first (face entries, then each face's normal, area and neighbour, and for
     // a boundary face its distance and tag): no kernel writes it, so it is loaded before
     // the wait for the predecessor's primitives (pdl.cuh) and only the primitive loads
@@ -159,19 +175,34 @@ __device__ __forceinline__ void grad_item(const MeshView<R>& m, const Flow<R>& F
     R fnx[4], fny[4], fA[4], fdn[4];
 #pragma unroll
     for (int k = 0; k < 4; ++k) ek[k] = m.cf[(long)k * m.nc + i];
+    if constexpr (CF) {
+#pragma unroll
+        for (int k = 0; k < 4; ++k) {
+            const long q = (long)k * m.nc + i;
+            nbr[k] = cx.nbr[q];
+            fnx[k] = cx.nx[q];
+            fny[k] = cx.ny[q];
+            fA[k] = cx.A[q];
+        }
+    }
     if (skip) return;  // tested with the first loads in flight, before the dependent ones
 #pragma unroll
     for (int k = 0; k < 4; ++k) {
         const int e = ek[k];
-        nbr[k] = -1;
+        if constexpr (!CF) {
+            nbr[k] = -1;
+            fnx[k] = fny[k] = fA[k] = R(0);
+        }
         ftg[k] = 0;
-        fnx[k] = fny[k] = fA[k] = fdn[k] = R(0);
+        fdn[k] = R(0);
         if (e < 0) continue;
         const int f = e >> 1;
-        fnx[k] = m.nx[f];
-        fny[k] = m.ny[f];
-        fA[k] = m.area[f];
-        nbr[k] = (e & 1) ? m.fo[f] : m.fn[f];
+        if constexpr (!CF) {
+            fnx[k] = m.nx[f];
+            fny[k] = m.ny[f];
+            fA[k] = m.area[f];
+            nbr[k] = (e & 1) ? m.fo[f] : m.fn[f];
+        }
         if (nbr[k] < 0) {
             fdn[k] = m.dxo[f] * fnx[k] + m.dyo[f] * fny[k];
             ftg[k] = m.ftag[f];
@@ -237,9 +268,10 @@ __device__ __forceinline__ void grad_item(const MeshView<R>& m, const Flow<R>& F
 #pragma unroll
     for (int q = 0; q < 2 * NQ; ++q) {
         acc[q] = div_shared(acc[q], vol, ivol);
-        Acc<S>::st(G, q, i, acc[q]);
+        if constexpr (CF) G.d[q * G.n + i] = acc[q].d;
+        else Acc<S>::st(G, q, i, acc[q]);
     }
-    if (!do_limiter) return;
+    if (CF || !do_limiter) return;
     // Barth-Jespersen on pressure reconstructed through T; one phi per cell
     const R eps = R(1e-12);
     R pc = val(wi[W_P]);
@@ -292,6 +324,19 @@ __global__ void __launch_bounds__(256, MinBlocks<S>::grad) k_grad(MeshView<R> m,
     if (i >= m.nc) return;
     if (lim_dev && !*lim_dev) do_limiter = 0;
     grad_item<S, NV>(m, F, U, W, G, phi, do_limiter, i, done);  // waits for its predecessor (pdl.cuh)
+}
+
+// k_grad with the neighbours and face geometry from per-cell copies (CellFaces), tangent
+// only.  Four resident 256-thread blocks per SM (three with SST: 64 / 80 registers, no
+// spills), where the generic template's 128 registers keep two: the neighbour loads are
+// its latency, and more warps keep more of them in flight.
+template <class S, int NV, class R>
+__global__ void __launch_bounds__(256, NV == 6 ? 3 : 4) k_grad_cf(MeshView<R> m, CellFaces<R> cx, Flow<R> F,
+                                                                   Field<R> U, Field<R> W, Field<R> G, R* phi,
+                                                                   int do_limiter, const int* done) {
+    long i = (long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= m.nc) return;
+    grad_item<S, NV, R, true>(m, F, U, W, G, phi, do_limiter, i, done, cx);  // waits for its predecessor (pdl.cuh)
 }
 
 // ---------------------------------------------------------------- k_flux

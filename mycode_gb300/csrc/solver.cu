@@ -106,6 +106,11 @@ struct cfdg_solver {
     int* iperm = nullptr;  // [nc] caller cell -> internal cell (the inverse of perm)
     GeoBuf<double> g64;
     GeoBuf<float> g32;
+    // per-cell neighbours and FP32 face geometry for the mixed solve's dual gradient
+    // (CellFaces, residual.cuh); mixed precision only
+    int* cfx_nbr = nullptr;
+    float* cfx_geo = nullptr;  // [3][4][nc]: nx, ny, area
+    CellFaces<float> cfx32{nullptr, nullptr, nullptr, nullptr};
     MeshView<double> mv;
     MeshView<float> mvf;
     // FP64 state and work
@@ -728,6 +733,7 @@ struct cfdg_solver {
             a.pdl = pdl;
             a.done = gd.gi + 2;
             a.tangent = true;
+            a.cfx = cfx32;
             launch_jv_mid<float>(a);
             launch_gmres_gather_dot<float>(nv, mvf, FA32d, w32, z32, dt32, nv == 6 ? T32d + 2 * nc : nullptr, V32, L, gd,
                                            st, pdl);
@@ -1519,6 +1525,8 @@ struct cfdg_solver {
         for (void* p : ps) cudaFree(p);
         g64.release();
         g32.release();
+        cudaFree(cfx_nbr);
+        cudaFree(cfx_geo);
         cudaFree(l2buf);
         cudaFree(gdi);
         cudaFree(gdd);
@@ -1744,6 +1752,29 @@ cfdg_status cfdg_solver_create(const cfdg_mesh* m, const cfdg_config* cfg, cfdg_
     };
     view(s->g64, s->mv);
     view(s->g32, s->mvf);
+    if (c.precision == CFDG_MIXED) {
+        // CellFaces of the FP32 view: the same float values as g32's face arrays
+        std::vector<int> nb(4 * (size_t)nc, -1);
+        std::vector<float> geo(12 * (size_t)nc, 0.0f);
+        for (int k = 0; k < 4; ++k) {
+            for (int i = 0; i < nc; ++i) {
+                const size_t q = (size_t)k * nc + i;
+                const int e = h.cf[q];
+                if (e < 0) continue;
+                const int f = e >> 1;
+                nb[q] = (e & 1) ? h.fo[f] : h.fn[f];
+                geo[q] = (float)h.nx[f];
+                geo[4 * (size_t)nc + q] = (float)h.ny[f];
+                geo[8 * (size_t)nc + q] = (float)h.area[f];
+            }
+        }
+        TRYS(dalloc(&s->cfx_nbr, nb.size()));
+        TRYS(dalloc(&s->cfx_geo, geo.size()));
+        if (cudaMemcpy(s->cfx_nbr, nb.data(), sizeof(int) * nb.size(), cudaMemcpyHostToDevice) != cudaSuccess ||
+            cudaMemcpy(s->cfx_geo, geo.data(), sizeof(float) * geo.size(), cudaMemcpyHostToDevice) != cudaSuccess)
+            return bail(fail(CFDG_ERR_CUDA, "mesh upload failed"));
+        s->cfx32 = CellFaces<float>{s->cfx_nbr, s->cfx_geo, s->cfx_geo + 4 * (size_t)nc, s->cfx_geo + 8 * (size_t)nc};
+    }
     int NW = nv == 6 ? 7 : 5, NG = nv == 6 ? 14 : 10;
     TRYS(dalloc(&s->U, L)); TRYS(dalloc(&s->W, (size_t)NW * nc)); TRYS(dalloc(&s->G, (size_t)NG * nc));
     TRYS(dalloc(&s->phi, nc)); TRYS(dalloc(&s->FA, (size_t)nv * nf)); TRYS(dalloc(&s->R, L));
