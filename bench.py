@@ -218,16 +218,6 @@ def profile_fp64_pipe() -> dict:
     return out
 
 
-def profile_traffic(kernel_class: str, jbar: float = 0.0):
-    """DRAM bytes per launch of a kernel class from ncu (profiles/traffic.txt: bytes at
-    Arnoldi iteration 0 and per further basis vector), evaluated at the mean iteration
-    jbar; None when the class is not listed."""
-    v = _profile_table("traffic.txt").get(kernel_class)
-    if not v:
-        return None
-    return round(v[0] + (v[1] if len(v) > 1 else 0.0) * jbar)
-
-
 # ---------------------------------------------------------------- clocks
 
 class ClockSampler:
@@ -1080,6 +1070,54 @@ def profile_case(args):
     print(json.dumps(line))
 
 
+def profile_krylov_iteration(args):
+    """Time of one Arnoldi iteration of the graph GMRES (the WHILE body, mixed precision,
+    exact J v) on a small mesh: Newton steps at GMRES tolerance 0 with Krylov dimensions
+    10 and 30 (every solve runs all of them); the slope of the step time over the
+    iterations is the iteration time.  Workloads: the limited supersonic wedge of
+    time_to_1e-10 (the FP64 oracle's frozen limiter) and the 240 x 120 laminar plate."""
+    import numpy as np
+    from mycode_gb300 import api, meshgen
+    if args.profile_workload == "laminar_plate":
+        mesh = api.Mesh.from_spec(meshgen.laminar_plate(240, 120, ratio=1.08))
+
+        def make(m, prec):
+            s = api.Solver(mesh, bcset="plate", init="freestream", viscous=1, flux="ROE",
+                           spatial="SECOND_ORDER_CENTRAL", precision=prec, jv="exact", gmres_m=m, gmres_tol=0.0)
+            s.setFreestreamStatic(0.2, 101325.0, 300.0)
+            s.setKinematicViscosity(1e5, 1.0)
+            s.initialize()
+            return s
+    else:
+        dw, spec = _golden("wedge_converged.npz")
+        mesh = api.Mesh.from_spec(spec)
+
+        def make(m, prec):
+            s = api.Solver(mesh, bcset="supersonic", init="freestream", viscous=0, precision=prec, jv="exact",
+                           gmres_m=m, gmres_tol=0.0, cfl0=10.0, flux="HLLC", spatial="SECOND_ORDER_LIMITED",
+                           limiter_freeze_step=-1)
+            s.setFlowConditions(2.5, 101325.0, 300.0)
+            s.initialize()
+            s.set_limiters(dw["phi"])
+            return s
+    line = {"path": "krylov_iteration", "workload": args.profile_workload, "cells": mesh.n_cells}
+    for prec in ("mixed", "fp64"):
+        t = {}
+        for m in (10, 30):
+            s = make(m, prec)
+            for _ in range(3):
+                s.newton_step(0.0)
+            s.synchronize()
+            t0 = time.perf_counter()
+            its = [s.newton_step(0.0)[0].gmres_iters for _ in range(args.reps)]
+            s.synchronize()
+            t[m] = ((time.perf_counter() - t0) / args.reps, float(np.mean(its)))
+            s.close()
+        line[prec] = {"ms_per_step": {m: round(v[0] * 1e3, 4) for m, v in t.items()},
+                      "us_per_iteration": round((t[30][0] - t[10][0]) / (t[30][1] - t[10][1]) * 1e6, 2)}
+    print(json.dumps(line))
+
+
 def main():
     ap = argparse.ArgumentParser(description=__doc__.split("\n")[0])
     ap.add_argument("--gpus", type=int, default=1)
@@ -1094,9 +1132,10 @@ def main():
     ap.add_argument("--sweep-sizes", default="", help="comma-separated target cell counts")
     ap.add_argument("--sweep-reps", type=int, default=10)
     ap.add_argument("--profile-case", default=None,
-                    choices=["residual64", "residual32", "jv64", "jv32", "vjp64", "krylov_stream"],
+                    choices=["residual64", "residual32", "jv64", "jv32", "vjp64", "krylov_stream",
+                             "krylov_iteration"],
                     help="run one kernel path --reps times (ncu workload) instead")
-    ap.add_argument("--profile-workload", default="bump", choices=["bump", "laminar_plate"])
+    ap.add_argument("--profile-workload", default="bump", choices=["bump", "laminar_plate", "wedge"])
     ap.add_argument("--no-sst", action="store_true", help="profile case: the bump without SST")
     ap.add_argument("--reps", type=int, default=3)
     ap.add_argument("--gmres-m", type=int, default=None, help="profile case: Krylov dimension")
@@ -1104,7 +1143,11 @@ def main():
     args = ap.parse_args()
     if args.warmup < 3 and not args.profile_case:
         ap.error("--warmup must be at least 3")
-    if args.profile_case:
+    if args.profile_workload == "wedge" and args.profile_case != "krylov_iteration":
+        ap.error("--profile-workload wedge is for --profile-case krylov_iteration")
+    if args.profile_case == "krylov_iteration":
+        profile_krylov_iteration(args)
+    elif args.profile_case:
         profile_case(args)
     elif args.sweep:
         sweep(args)
