@@ -10,7 +10,10 @@ static void residual_nv(const ResArgs<double>& a) {
     if (a.ev) cudaEventRecord(a.ev[0], a.stream);
     if (!a.prim_done) k_prim<double, NV><<<blocks_for(nc), tpb_for(nc), 0, a.stream>>>((int)nc, a.F, a.U, a.W);
     if (a.ev) cudaEventRecord(a.ev[1], a.stream);
-    k_grad64<NV><<<blocks_for(nc), tpb_for(nc), 0, a.stream>>>(a.m, a.F, a.U, a.W, a.G, a.phi, a.do_limiter, a.lim_dev);
+    {
+        const unsigned t = tpb_for(nc) < GRAD64_THREADS ? tpb_for(nc) : GRAD64_THREADS;
+        k_grad64<NV><<<grid_for(nc, (int)t), t, 0, a.stream>>>(a.m, a.F, a.U, a.W, a.G, a.phi, a.do_limiter, a.lim_dev);
+    }
     if (NV == 6) k_sst_cell<double, NV><<<blocks_for(nc), tpb_for(nc), 0, a.stream>>>(a.m, a.F, a.W, a.G, a.dwall, a.T, nullptr);
     if (a.ev) cudaEventRecord(a.ev[2], a.stream);
     {

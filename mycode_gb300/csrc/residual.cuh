@@ -465,8 +465,10 @@ __global__ void __launch_bounds__(256, MinBlocks<S>::flux) k_flux(MeshView<R> m,
 // least two 256-thread blocks per SM (128 registers), face fluxes 6.32 -> 5.86 ms with at
 // least three 128-thread blocks (170 registers); 128-thread blocks x 3 for the gradients
 // 4.55 ms, 64-thread blocks x 5-6 the same as x 3.
+constexpr unsigned GRAD64_THREADS = 256;
+
 template <int NV>
-__global__ void __launch_bounds__(256, 2) k_grad64(MeshView<double> m, Flow<double> F, Field<double> U,
+__global__ void __launch_bounds__(GRAD64_THREADS, 2) k_grad64(MeshView<double> m, Flow<double> F, Field<double> U,
                                                    Field<double> W, Field<double> G, double* phi, int do_limiter,
                                                    const int* lim_dev) {
     long i = (long)blockIdx.x * blockDim.x + threadIdx.x;
