@@ -262,6 +262,12 @@ cfdg_status cfdg_reset_newton(cfdg_solver* s);
  * the state (cfdg_get_state) and these two can replay the same Newton steps later. */
 cfdg_status cfdg_get_newton_state(cfdg_solver* s, double* cfl, int* step);
 cfdg_status cfdg_set_newton_state(cfdg_solver* s, double cfl, int step);
+/* The CFL cap of the pseudo-transient control (cfdg_config.cfl_max; the reference's
+ * hard-coded 1e4, src/Solver.cpp:1790), changed between Newton steps: a continuation
+ * schedule can hold the CFL number low through a stiff start-up transient and lift the
+ * cap once the flow has settled.  Takes effect from the next step or chain; a current CFL
+ * above the new cap is lowered to it. */
+cfdg_status cfdg_set_cfl_max(cfdg_solver* s, double cfl_max);
 
 /* Adjoint: gU = (dR/dU)^T lambda for the full residual at U, gradients and limiter
  * recomputed and differentiated along the branches the forward pass took (no

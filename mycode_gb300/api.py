@@ -109,6 +109,7 @@ SIGNATURES = {
     "cfdg_reset_newton": (C.c_int, [_vp]),
     "cfdg_get_newton_state": (C.c_int, [_vp, C.POINTER(C.c_double), C.POINTER(C.c_int)]),
     "cfdg_set_newton_state": (C.c_int, [_vp, C.c_double, C.c_int]),
+    "cfdg_set_cfl_max": (C.c_int, [_vp, C.c_double]),
     "cfdg_fp64_pipe_rate": (C.c_int, [C.c_int, C.POINTER(C.c_double)]),
     "cfdg_set_krylov": (C.c_int, [_vp, C.c_int]),
     "cfdg_vjp": (C.c_int, [_vp, C.c_void_p, _dp, _dp]),
@@ -469,6 +470,10 @@ class Solver:
 
     def set_newton_state(self, cfl, step):
         _check(lib().cfdg_set_newton_state(self._h, float(cfl), int(step)))
+
+    def set_cfl_max(self, cfl_max):
+        """The pseudo-transient control's CFL cap, from the next Newton step on."""
+        _check(lib().cfdg_set_cfl_max(self._h, float(cfl_max)))
 
     def vjp(self, lam, U=None):
         g = np.zeros(6 * self.n_cells)

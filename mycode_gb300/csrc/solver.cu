@@ -2147,6 +2147,13 @@ cfdg_status cfdg_set_newton_state(cfdg_solver* s, double cfl, int step) {
     return CFDG_OK;
 }
 
+cfdg_status cfdg_set_cfl_max(cfdg_solver* s, double cfl_max) {
+    if (!s || !(cfl_max > 0.0)) return fail(CFDG_ERR_ARG, "bad CFL cap");
+    s->cfg.cfl_max = cfl_max;
+    if (s->cfl > cfl_max) s->cfl = cfl_max;
+    return CFDG_OK;
+}
+
 cfdg_status cfdg_newton_step(cfdg_solver* s, double tol, cfdg_step* info, int* converged) {
     if (!s) return fail(CFDG_ERR_ARG, "null solver");
     int cv = 0;
