@@ -12,7 +12,14 @@ static void residual_nv(const ResArgs<double>& a) {
     if (a.ev) cudaEventRecord(a.ev[1], a.stream);
     {
         const unsigned t = tpb_for(nc) < GRAD64_THREADS ? tpb_for(nc) : GRAD64_THREADS;
-        k_grad64<NV><<<grid_for(nc, (int)t), t, 0, a.stream>>>(a.m, a.F, a.U, a.W, a.G, a.phi, a.do_limiter, a.lim_dev);
+        if (a.gft && a.m.nfi > 0) {
+            k_grad_faces64<NV><<<grid_for(a.m.nfi, 256), 256, 0, a.stream>>>(a.m, a.W, a.gft);
+            k_grad64<NV, true><<<grid_for(nc, (int)t), t, 0, a.stream>>>(a.m, a.F, a.U, a.W, a.G, a.phi, a.do_limiter,
+                                                                         a.lim_dev, a.gft);
+        } else {
+            k_grad64<NV, false><<<grid_for(nc, (int)t), t, 0, a.stream>>>(a.m, a.F, a.U, a.W, a.G, a.phi, a.do_limiter,
+                                                                          a.lim_dev, nullptr);
+        }
     }
     if (NV == 6) k_sst_cell<double, NV><<<blocks_for(nc), tpb_for(nc), 0, a.stream>>>(a.m, a.F, a.W, a.G, a.dwall, a.T, nullptr);
     if (a.ev) cudaEventRecord(a.ev[2], a.stream);

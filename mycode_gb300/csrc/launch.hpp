@@ -48,6 +48,9 @@ struct ResArgs {
     // launch_jv_mid: per-cell neighbours and face geometry for the gradient kernel
     // (k_grad_cf) when cfx.nbr is set
     CellFaces<R> cfx{nullptr, nullptr, nullptr, nullptr};
+    // launch_residual<double>: the interior faces' Green-Gauss terms (2 x primitives planes of
+    // m.nfi), formed once per face by k_grad_faces64 when set
+    double* gft = nullptr;
 };
 
 // A kernel launch, with the programmatic stream-serialisation attribute when pdl: the

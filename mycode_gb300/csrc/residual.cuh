@@ -155,11 +155,16 @@ __global__ void __launch_bounds__(256) k_prim(int nc, Flow<R> F, Field<R> U, Fie
 // (src/Solver.cpp:152-253) for the same cell from its own fresh gradient.
 // CF: the tangent-only gradient of a Krylov body (S a dual number, derivative planes
 // written, no limiter), with the neighbours and face geometry from cx (CellFaces) instead
-// of through the faces; everything else as the generic kernel computes it
-template <class S, int NV, class R, bool CF = false>
+// of through the faces; everything else as the generic kernel computes it.
+// FT (FP64 residual): each interior face's Green-Gauss terms (ph n_x A, ph n_y A per
+// primitive) read from ft, where k_grad_faces64 formed them once per face (planes of
+// ftn = nfi entries), instead of formed again by each of the face's two cells; the
+// neighbour's pressure is still read for the limiter's bounds.
+template <class S, int NV, class R, bool CF = false, bool FT = false>
 __device__ __forceinline__ void grad_item(const MeshView<R>& m, const Flow<R>& F, const Field<R>& U,
                                           const Field<R>& W, const Field<R>& G, R* phi, int do_limiter, long i,
-                                          const int* done = nullptr, CellFaces<R> cx = {}) {
+                                          const int* done = nullptr, CellFaces<R> cx = {}, const R* ft = nullptr,
+                                          long ftn = 0) {
     // done: a finished Krylov solve (krylov.cuh); read with the mesh loads, tested after
     const int skip = done ? *done : 0;
     constexpr int NQ = NV == 6 ? 7 : 5;
@@ -225,6 +230,28 @@ __device__ __forceinline__ void grad_item(const MeshView<R>& m, const Flow<R>& F
         R nx = fnx[k], ny = fny[k], A = fA[k];
         S wj[NQ];
         int j = nbr[k];
+        if constexpr (FT) {
+            if (j >= 0) {
+                // the face's terms, formed once for its two cells (the same bits: the half
+                // sum is commutative, the products the same expressions)
+                const long f = e >> 1;
+                const R pj = W.v[W_P * W.n + j];
+                pmax = smax(pmax, pj);
+                pmin = smin(pmin, pj);
+#pragma unroll
+                for (int q = 0; q < NQ; ++q) {
+                    const R tx = ft[(2 * q) * ftn + f], ty = ft[(2 * q + 1) * ftn + f];
+                    if (side) {
+                        acc[2 * q] = acc[2 * q] - tx;
+                        acc[2 * q + 1] = acc[2 * q + 1] - ty;
+                    } else {
+                        acc[2 * q] = acc[2 * q] + tx;
+                        acc[2 * q + 1] = acc[2 * q + 1] + ty;
+                    }
+                }
+                continue;
+            }
+        }
         if (j >= 0) {
             if (tangent) {
 #pragma unroll
@@ -467,14 +494,35 @@ __global__ void __launch_bounds__(256, MinBlocks<S>::flux) k_flux(MeshView<R> m,
 // 4.55 ms, 64-thread blocks x 5-6 the same as x 3.
 constexpr unsigned GRAD64_THREADS = 256;
 
-template <int NV>
+// FT: the interior faces' Green-Gauss terms from ft (k_grad_faces64), planes of m.nfi
+template <int NV, bool FT>
 __global__ void __launch_bounds__(GRAD64_THREADS, 2) k_grad64(MeshView<double> m, Flow<double> F, Field<double> U,
                                                    Field<double> W, Field<double> G, double* phi, int do_limiter,
-                                                   const int* lim_dev) {
+                                                   const int* lim_dev, const double* __restrict__ ft) {
     long i = (long)blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= m.nc) return;
     if (lim_dev && !*lim_dev) do_limiter = 0;
-    grad_item<double, NV>(m, F, U, W, G, phi, do_limiter, i, nullptr);
+    grad_item<double, NV, double, false, FT>(m, F, U, W, G, phi, do_limiter, i, nullptr, {}, ft, m.nfi);
+}
+
+// The Green-Gauss terms of each interior face, once: ph = (w_owner + w_neighbour) / 2 and
+// ph n_x A, ph n_y A for every primitive, the expressions the per-cell gather forms on each
+// side of the face (src/Solver.cpp:104-147), into planes 2q (x) and 2q + 1 (y) of nfi
+// entries.  Half of the gradient's FP64 work on the faces is forming these terms; the
+// gradient kernel adds them in each cell's face order.
+template <int NV>
+__global__ void __launch_bounds__(256) k_grad_faces64(MeshView<double> m, Field<double> W, double* __restrict__ ft) {
+    const long f = (long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (f >= m.nfi) return;
+    constexpr int NQ = NV == 6 ? 7 : 5;
+    const long o = m.fo[f], n = m.fn[f];
+    const double nx = m.nx[f], ny = m.ny[f], A = m.area[f];
+#pragma unroll
+    for (int q = 0; q < NQ; ++q) {
+        const double ph = half(W.v[q * W.n + o] + W.v[q * W.n + n]);
+        ft[(2 * q) * (long)m.nfi + f] = ph * nx * A;
+        ft[(2 * q + 1) * (long)m.nfi + f] = ph * ny * A;
+    }
 }
 
 constexpr unsigned FLUX64_THREADS = 128;

@@ -104,6 +104,7 @@ struct cfdg_solver {
     // device mesh
     int *cf = nullptr, *fo = nullptr, *fn = nullptr, *ftag = nullptr, *perm = nullptr;
     int* iperm = nullptr;  // [nc] caller cell -> internal cell (the inverse of perm)
+    double* gft = nullptr; // [2 x primitives][nfi] the FP64 gradient's per-face terms (k_grad_faces64)
     GeoBuf<double> g64;
     GeoBuf<float> g32;
     // per-cell neighbours and FP32 face geometry for the mixed solve's dual gradient
@@ -309,8 +310,12 @@ struct cfdg_solver {
         a.dt = nullptr;
         a.stream = st;
         a.ev = nullptr;
+        a.gft = gft;
         return a;
     }
+
+    // kernels of one FP64 residual (launch_residual<double>)
+    int res64_kernels() const { return (nv == 6 ? 5 : 4) + (gft && mv.nfi > 0 ? 1 : 0); }
 
     // norms (a Newton step): the gather also writes rhs = -R, the norm pieces and |R|^2 into
     // scal[8..11] and clears the update's non-finite flag (k_gather_norms; `flag`, default
@@ -334,7 +339,7 @@ struct cfdg_solver {
         a.iperm = iperm;
         a.ev = take_events(0);
         launch_residual<double>(a);
-        launches += (nv == 6 ? 5 : 4) - (prim_done ? 1 : 0);
+        launches += res64_kernels() - (prim_done ? 1 : 0);
         if (do_lim) limiter_valid = true;
         CK(cudaGetLastError());
         return CFDG_OK;
@@ -1519,7 +1524,7 @@ struct cfdg_solver {
         cudaFree(dinv64);
         void* pt[] = {Tt, Tj, Tjd, dwall, T32, T32d, dwall32};
         for (void* p : pt) cudaFree(p);
-        void* ps[] = {cf, fo, fn, ftag, perm, iperm, U, W, G, phi, FA, R, dt, D, stage, Ub, Rb, Up, Rp, vtmp, x, rhs,
+        void* ps[] = {cf, fo, fn, ftag, perm, iperm, gft, U, W, G, phi, FA, R, dt, D, stage, Ub, Rb, Up, Rp, vtmp, x, rhs,
                       Wj, Wjd, Gj, Gjd, FAjd, U32, W32, W32d, G32, G32d, FA32d, phi32, dt32, V32, z32, V, z,
                       rs.partial, rs.counter, scal, bad};
         for (void* p : ps) cudaFree(p);
@@ -1784,6 +1789,7 @@ cfdg_status cfdg_solver_create(const cfdg_mesh* m, const cfdg_config* cfg, cfdg_
     TRYS(dalloc(&s->Wj, (size_t)NW * nc)); TRYS(dalloc(&s->Wjd, (size_t)NW * nc));
     TRYS(dalloc(&s->Gj, (size_t)NG * nc)); TRYS(dalloc(&s->Gjd, (size_t)NG * nc));
     TRYS(dalloc(&s->FAjd, (size_t)nv * nf));
+    if (h.n_interior > 0) TRYS(dalloc(&s->gft, (size_t)2 * NW * h.n_interior));
     if (nv == 6) {
         TRYS(dalloc(&s->Tt, 4 * (size_t)nc)); TRYS(dalloc(&s->Tj, 4 * (size_t)nc)); TRYS(dalloc(&s->Tjd, 4 * (size_t)nc));
         TRYS(dalloc(&s->dwall, (size_t)nc)); TRYS(dalloc(&s->dwall32, (size_t)nc));
@@ -1982,7 +1988,7 @@ cfdg_status cfdg_gradients(cfdg_solver* s, const double* U, double* g10) {
     // the residual's gradient stage (no limiter update) leaves the gradients in G
     ResArgs<double> a = s->res64(Uin, s->R, 0);
     launch_residual<double>(a);
-    s->launches += s->nv == 6 ? 5 : 4;
+    s->launches += s->res64_kernels();
     CK(cudaGetLastError());
     return s->download_aos(s->G, g10, 10, 10);
 }
@@ -1996,7 +2002,7 @@ cfdg_status cfdg_limiters(cfdg_solver* s, const double* U, double* phi) {
     }
     ResArgs<double> a = s->res64(Uin, s->R, 1);
     launch_residual<double>(a);
-    s->launches += s->nv == 6 ? 5 : 4;
+    s->launches += s->res64_kernels();
     s->limiter_valid = true;
     CK(cudaGetLastError());
     return s->download_aos(s->phi, phi, 1, 1);
