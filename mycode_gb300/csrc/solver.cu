@@ -87,6 +87,9 @@ double now_s() {
 }  // namespace
 
 namespace cfdg {
+// interior faces from which the FP64 residual forms the gradient's face terms once per face
+// (k_grad_faces64); below, the per-cell gradient forms them on each side
+constexpr int GRAD_FACE_TERMS_MIN_FACES = 100000;
 // lets other translation units of the library report through cfdg_last_error()
 void set_error_message(const std::string& msg) { g_err = msg; }
 }  // namespace cfdg
@@ -1789,7 +1792,10 @@ cfdg_status cfdg_solver_create(const cfdg_mesh* m, const cfdg_config* cfg, cfdg_
     TRYS(dalloc(&s->Wj, (size_t)NW * nc)); TRYS(dalloc(&s->Wjd, (size_t)NW * nc));
     TRYS(dalloc(&s->Gj, (size_t)NG * nc)); TRYS(dalloc(&s->Gjd, (size_t)NG * nc));
     TRYS(dalloc(&s->FAjd, (size_t)nv * nf));
-    if (h.n_interior > 0) TRYS(dalloc(&s->gft, (size_t)2 * NW * h.n_interior));
+    // the FP64 gradient's per-face terms on meshes large enough for the FP64 pipe to bound
+    // the gradient; on small meshes the residual is latency-bound and the face kernel would
+    // be one launch more
+    if (h.n_interior >= GRAD_FACE_TERMS_MIN_FACES) TRYS(dalloc(&s->gft, (size_t)2 * NW * h.n_interior));
     if (nv == 6) {
         TRYS(dalloc(&s->Tt, 4 * (size_t)nc)); TRYS(dalloc(&s->Tj, 4 * (size_t)nc)); TRYS(dalloc(&s->Tjd, 4 * (size_t)nc));
         TRYS(dalloc(&s->dwall, (size_t)nc)); TRYS(dalloc(&s->dwall32, (size_t)nc));

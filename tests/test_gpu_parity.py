@@ -11,6 +11,7 @@ import numpy as np
 import pytest
 
 import cases as C
+from mycode_gb300 import meshgen as mg
 from oracle.oracle import OracleSolver
 
 pytestmark = pytest.mark.gpu
@@ -60,6 +61,24 @@ def test_residual_all_schemes(cuda_lib, name, renumber):
             _assert_match(s.computeResiduals(U), o.residual(U), exact, f"R {fl} {sp}")
             # frozen limiter: both keep the values of the last update
             _assert_match(s.computeResiduals(U, False), o.residual(U, False), exact, f"R frozen {fl} {sp}")
+
+
+@pytest.mark.parametrize("name,spec", [("supersonic", lambda: mg.wedge(260, 200, jitter=0.1, seed=4)),
+                                       ("plate_visc", lambda: mg.laminar_plate(300, 180, ratio=1.02))])
+def test_residual_bit_exact_with_per_face_gradient_terms(cuda_lib, name, spec):
+    """Meshes with more than 100,000 interior faces, where the FP64 residual forms each
+    interior face's Green-Gauss terms once (k_grad_faces64) and the gradient kernel adds
+    them: the gradients, limiter and residual still equal the oracle's bit for bit."""
+    case, s, o = _make(cuda_lib, name, spec=spec())
+    assert s.mesh.n_faces - s.mesh.n_boundary_faces >= 100_000
+    U = C.perturbed_state(o.get_state(), o.cells(), seed=7, amplitude=0.08)
+    _assert_match(s.gradients(U), o.gradients(U), True, "gradients")
+    _assert_match(s.limiters(U), o.limiters(U), True, "limiters")
+    for fl in C.FLUXES:
+        for sp in ("SECOND_ORDER_CENTRAL", "SECOND_ORDER_LIMITED"):
+            s.setNumericalMethod(fl, sp)
+            o.setNumericalMethod(fl, sp)
+            _assert_match(s.computeResiduals(U), o.residual(U), True, f"R {fl} {sp}")
 
 
 @pytest.mark.parametrize("name", list(C.CASES))
