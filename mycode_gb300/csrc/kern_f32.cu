@@ -10,8 +10,12 @@ static void residual_nv(const ResArgs<float>& a) {
     if (a.ev) cudaEventRecord(a.ev[0], a.stream);
     k_prim<float, NV><<<blocks_for(nc), tpb_for(nc), 0, a.stream>>>((int)nc, a.F, a.U, a.W);
     if (a.ev) cudaEventRecord(a.ev[1], a.stream);
-    k_grad<float, NV><<<blocks_for(nc), tpb_for(nc), 0, a.stream>>>(a.m, a.F, a.U, a.W, a.G, a.phi, a.do_limiter, nullptr,
-                                                                   nullptr);
+    if (a.cfx.nbr)
+        k_grad_cf<float, NV, float, false><<<blocks_for(nc), tpb_for(nc), 0, a.stream>>>(a.m, a.cfx, a.F, a.U, a.W, a.G,
+                                                                                         a.phi, a.do_limiter, nullptr);
+    else
+        k_grad<float, NV><<<blocks_for(nc), tpb_for(nc), 0, a.stream>>>(a.m, a.F, a.U, a.W, a.G, a.phi, a.do_limiter,
+                                                                       nullptr, nullptr);
     if (NV == 6) k_sst_cell<float, NV><<<blocks_for(nc), tpb_for(nc), 0, a.stream>>>(a.m, a.F, a.W, a.G, a.dwall, a.T, nullptr);
     if (a.ev) cudaEventRecord(a.ev[2], a.stream);
     k_flux<float, NV><<<blocks_for(nf), tpb_for(nf), 0, a.stream>>>(a.m, a.F, a.U, a.W, a.G, a.phi, a.FA, a.T, nullptr);
@@ -31,7 +35,12 @@ template <int NV>
 static void values_nv(const ResArgs<float>& a) {
     long nc = a.m.nc;
     k_prim<float, NV><<<blocks_for(nc), tpb_for(nc), 0, a.stream>>>((int)nc, a.F, a.U, a.W);
-    k_grad<float, NV><<<blocks_for(nc), tpb_for(nc), 0, a.stream>>>(a.m, a.F, a.U, a.W, a.G, a.phi, 0, nullptr, nullptr);
+    if (a.cfx.nbr)
+        k_grad_cf<float, NV, float, false><<<blocks_for(nc), tpb_for(nc), 0, a.stream>>>(a.m, a.cfx, a.F, a.U, a.W, a.G,
+                                                                                         a.phi, 0, nullptr);
+    else
+        k_grad<float, NV><<<blocks_for(nc), tpb_for(nc), 0, a.stream>>>(a.m, a.F, a.U, a.W, a.G, a.phi, 0, nullptr,
+                                                                       nullptr);
     if (NV == 6) k_sst_cell<float, NV><<<blocks_for(nc), tpb_for(nc), 0, a.stream>>>(a.m, a.F, a.W, a.G, a.dwall, a.T, nullptr);
 }
 

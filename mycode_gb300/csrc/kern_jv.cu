@@ -14,7 +14,11 @@ static void jv_nv(const ResArgs<R>& a) {
     if (a.ev) cudaEventRecord(a.ev[0], a.stream);
     k_prim<S, NV><<<blocks_for(nc), tpb_for(nc), 0, a.stream>>>((int)nc, a.F, a.U, a.W);
     if (a.ev) cudaEventRecord(a.ev[1], a.stream);
-    k_grad<S, NV><<<blocks_for(nc), tpb_for(nc), 0, a.stream>>>(a.m, a.F, a.U, a.W, a.G, a.phi, 0, nullptr, nullptr);
+    if (a.cfx.nbr)
+        k_grad_cf<S, NV, R, false><<<blocks_for(nc), tpb_for(nc), 0, a.stream>>>(a.m, a.cfx, a.F, a.U, a.W, a.G, a.phi,
+                                                                                 0, nullptr);
+    else
+        k_grad<S, NV><<<blocks_for(nc), tpb_for(nc), 0, a.stream>>>(a.m, a.F, a.U, a.W, a.G, a.phi, 0, nullptr, nullptr);
     if (NV == 6) k_sst_cell<S, NV><<<blocks_for(nc), tpb_for(nc), 0, a.stream>>>(a.m, a.F, a.W, a.G, a.dwall, a.T, nullptr);
     if (a.ev) cudaEventRecord(a.ev[2], a.stream);
     k_flux<S, NV><<<blocks_for(nf), tpb_for(nf), 0, a.stream>>>(a.m, a.F, a.U, a.W, a.G, a.phi, a.FA, a.T, nullptr);
@@ -34,8 +38,8 @@ static void jv_mid_nv(const ResArgs<R>& a) {
     if (a.tangent) Gw.v = Tw.v = nullptr;
     if (a.ev) cudaEventRecord(a.ev[0], a.stream);
     if (a.cfx.nbr)
-        launch_k(a.pdl, k_grad_cf<S, NV, R>, dim3(blocks_for(nc)), dim3(tpb_for(nc)), a.stream, a.m, a.cfx, a.F, a.U,
-                 a.W, Gw, a.phi, 0, a.done);
+        launch_k(a.pdl, k_grad_cf<S, NV, R, true>, dim3(blocks_for(nc)), dim3(tpb_for(nc)), a.stream, a.m, a.cfx, a.F,
+                 a.U, a.W, Gw, a.phi, 0, a.done);
     else
         launch_k(a.pdl, k_grad<S, NV, R>, dim3(blocks_for(nc)), dim3(tpb_for(nc)), a.stream, a.m, a.F, a.U, a.W, Gw,
                  a.phi, 0, a.done, (const int*)nullptr);

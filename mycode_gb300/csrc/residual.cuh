@@ -153,14 +153,14 @@ __global__ void __launch_bounds__(256) k_prim(int nc, Flow<R> F, Field<R> U, Fie
 // computeGradients (src/Solver.cpp:81-149) as a per-cell gather over the cell's faces
 // in reference face order, then (limited scheme, limiter not frozen) computeLimiters
 // (src/Solver.cpp:152-253) for the same cell from its own fresh gradient.
-// CF: the tangent-only gradient of a Krylov body (S a dual number, derivative planes
-// written, no limiter), with the neighbours and face geometry from cx (CellFaces) instead
-// of through the faces; everything else as the generic kernel computes it.
+// CF: the neighbours and face geometry from cx (CellFaces) instead of through the faces.
+// TAN: the tangent-only gradient of a Krylov body (S a dual number, derivative planes
+// written, no limiter).  Everything else as the generic kernel computes it.
 // FT (FP64 residual): each interior face's Green-Gauss terms (ph n_x A, ph n_y A per
 // primitive) read from ft, where k_grad_faces64 formed them once per face (planes of
 // ftn = nfi entries), instead of formed again by each of the face's two cells; the
 // neighbour's pressure is still read for the limiter's bounds.
-template <class S, int NV, class R, bool CF = false, bool FT = false>
+template <class S, int NV, class R, bool CF = false, bool FT = false, bool TAN = false>
 __device__ __forceinline__ void grad_item(const MeshView<R>& m, const Flow<R>& F, const Field<R>& U,
                                           const Field<R>& W, const Field<R>& G, R* phi, int do_limiter, long i,
                                           const int* done = nullptr, CellFaces<R> cx = {}, const R* ft = nullptr,
@@ -171,7 +171,7 @@ __device__ __forceinline__ void grad_item(const MeshView<R>& m, const Flow<R>& F
     // a dual gradient with no value planes to write (J v about a fixed point whose value
     // planes are current): the face sums' derivatives need only the neighbours' derivative
     // planes (the ghost states read the cell's own values)
-    const bool tangent = CF || (!std::is_same<S, R>::value && G.v == nullptr && !do_limiter);
+    const bool tangent = TAN || (!std::is_same<S, R>::value && G.v == nullptr && !do_limiter);
     // Mesh data first (face entries, then each face's normal, area and neighbour, and for
     // a boundary face its distance and tag): no kernel writes it, so it is loaded before
     // the wait for the predecessor's primitives (pdl.cuh) and only the primitive loads
@@ -295,10 +295,10 @@ __device__ __forceinline__ void grad_item(const MeshView<R>& m, const Flow<R>& F
 #pragma unroll
     for (int q = 0; q < 2 * NQ; ++q) {
         acc[q] = div_shared(acc[q], vol, ivol);
-        if constexpr (CF) G.d[q * G.n + i] = acc[q].d;
+        if constexpr (TAN) G.d[q * G.n + i] = acc[q].d;
         else Acc<S>::st(G, q, i, acc[q]);
     }
-    if (CF || !do_limiter) return;
+    if (TAN || !do_limiter) return;
     // Barth-Jespersen on pressure reconstructed through T; one phi per cell
     const R eps = R(1e-12);
     R pc = val(wi[W_P]);
@@ -353,17 +353,22 @@ __global__ void __launch_bounds__(256, MinBlocks<S>::grad) k_grad(MeshView<R> m,
     grad_item<S, NV>(m, F, U, W, G, phi, do_limiter, i, done);  // waits for its predecessor (pdl.cuh)
 }
 
-// k_grad with the neighbours and face geometry from per-cell copies (CellFaces), tangent
-// only.  Four resident 256-thread blocks per SM (three with SST: 64 / 80 registers, no
-// spills), where the generic template's 128 registers keep two: the neighbour loads are
-// its latency, and more warps keep more of them in flight.
-template <class S, int NV, class R>
-__global__ void __launch_bounds__(256, NV == 6 ? 3 : 4) k_grad_cf(MeshView<R> m, CellFaces<R> cx, Flow<R> F,
-                                                                   Field<R> U, Field<R> W, Field<R> G, R* phi,
-                                                                   int do_limiter, const int* done) {
+// k_grad with the neighbours and face geometry from per-cell copies (CellFaces).  The
+// tangent-only dual gradient of a Krylov body (TAN) runs four resident 256-thread blocks per
+// SM (three with SST: 64 / 80 registers, no spills), where the generic template's 128
+// registers keep two: the neighbour loads are its latency, and more warps keep more of them
+// in flight.  The FP32 value gradient (with its limiter) and the full dual gradient run two.
+template <class S, int NV, bool TAN> struct GradCfBlocks { static constexpr int value = 2; };
+template <class S, int NV> struct GradCfBlocks<S, NV, true> { static constexpr int value = NV == 6 ? 3 : 4; };
+
+template <class S, int NV, class R, bool TAN>
+__global__ void __launch_bounds__(256, (GradCfBlocks<S, NV, TAN>::value)) k_grad_cf(MeshView<R> m, CellFaces<R> cx,
+                                                                                  Flow<R> F, Field<R> U, Field<R> W,
+                                                                                  Field<R> G, R* phi, int do_limiter,
+                                                                                  const int* done) {
     long i = (long)blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= m.nc) return;
-    grad_item<S, NV, R, true>(m, F, U, W, G, phi, do_limiter, i, done, cx);  // waits for its predecessor (pdl.cuh)
+    grad_item<S, NV, R, true, false, TAN>(m, F, U, W, G, phi, do_limiter, i, done, cx);  // waits for its predecessor
 }
 
 // ---------------------------------------------------------------- k_flux

@@ -426,6 +426,7 @@ struct cfdg_solver {
         launch_convert<float>(L, Ubase, U32, st);
         ResArgs<float> a;
         a.m = mvf;
+        a.cfx = cfx32;
         a.F = Ff;
         a.nv = nv;
         a.U = f32(U32);
@@ -457,6 +458,7 @@ struct cfdg_solver {
         launch_convert<float>(L, vdev, f32dir, st);
         ResArgs<float> a;
         a.m = mvf;
+        a.cfx = cfx32;
         a.F = Ff;
         a.nv = nv;
         a.U = f32(U32, f32dir);
@@ -644,6 +646,7 @@ struct cfdg_solver {
             // body's dual kernels then form and write derivative planes only
             ResArgs<float> a;
             a.m = mvf;
+            a.cfx = cfx32;
             a.F = Ff;
             a.nv = nv;
             a.U = f32(U32);
@@ -727,6 +730,7 @@ struct cfdg_solver {
             launch_gmres_prim_z<float>(nv, nc, Ff, U32, V32, L, dinv32, z32, f32(nullptr, W32d), w32, gd, h, st);
             ResArgs<float> a;
             a.m = mvf;
+            a.cfx = cfx32;
             a.F = Ff;
             a.nv = nv;
             a.U = f32(U32, z32);
@@ -741,7 +745,6 @@ struct cfdg_solver {
             a.pdl = pdl;
             a.done = gd.gi + 2;
             a.tangent = true;
-            a.cfx = cfx32;
             launch_jv_mid<float>(a);
             launch_gmres_gather_dot<float>(nv, mvf, FA32d, w32, z32, dt32, nv == 6 ? T32d + 2 * nc : nullptr, V32, L, gd,
                                            st, pdl);
@@ -990,6 +993,7 @@ struct cfdg_solver {
                 launch_precond_apply<float>(nv, nc, Vj, D, z32, rs, nullptr, st);
                 ResArgs<float> a;
                 a.m = mvf;
+                a.cfx = cfx32;
                 a.F = Ff;
                 a.nv = nv;
                 a.U = f32(U32, z32);
