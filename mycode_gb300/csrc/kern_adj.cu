@@ -12,9 +12,16 @@ static void vjp_nv(const ResArgs<double>& a, const double* lam, const AdjBufs& b
     int limited = a.F.spatial == SP_LIMITED ? 1 : 0;
     if (a.ev) cudaEventRecord(a.ev[0], a.stream);
     k_prim<double, NV><<<grid_for(nc), 256, 0, a.stream>>>((int)nc, a.F, a.U, a.W);
-    k_grad64<NV, false><<<grid_for(nc, (int)GRAD64_THREADS), GRAD64_THREADS, 0, a.stream>>>(a.m, a.F, a.U, a.W, a.G,
-                                                                                          a.phi, limited, nullptr,
-                                                                                          nullptr);
+    if (a.gft && a.m.nfi > 0) {  // the residual's split gradient (face terms once per face): the same G and phi
+        k_grad_faces64<NV><<<grid_for(a.m.nfi, 256), 256, 0, a.stream>>>(a.m, a.W, a.gft);
+        k_grad64<NV, true><<<grid_for(nc, (int)GRAD64_THREADS), GRAD64_THREADS, 0, a.stream>>>(a.m, a.F, a.U, a.W, a.G,
+                                                                                              a.phi, limited, nullptr,
+                                                                                              a.gft);
+    } else {
+        k_grad64<NV, false><<<grid_for(nc, (int)GRAD64_THREADS), GRAD64_THREADS, 0, a.stream>>>(a.m, a.F, a.U, a.W,
+                                                                                               a.G, a.phi, limited,
+                                                                                               nullptr, nullptr);
+    }
     if (NV == 6) k_sst_cell<double, NV><<<grid_for(nc), 256, 0, a.stream>>>(a.m, a.F, a.W, a.G, a.dwall, a.T, nullptr);
     if (a.ev) cudaEventRecord(a.ev[1], a.stream);
     k_flux_adj<NV><<<grid_for(nf, 128), 128, 0, a.stream>>>(a.m, a.F, a.U, a.W, a.G, a.phi, lam, b, a.T);

@@ -622,7 +622,7 @@ struct cfdg_solver {
         a.phi = phi_adj;
         a.ev = take_events(8);
         launch_vjp64(a, lam, ab, gout);
-        launches += nv == 6 ? 6 : 5;
+        launches += (nv == 6 ? 6 : 5) + (gft && mv.nfi > 0 ? 1 : 0);
         CK(cudaGetLastError());
         return CFDG_OK;
     }
