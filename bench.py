@@ -1068,6 +1068,7 @@ def profile_case(args):
         "vjp64": (lambda: s.vjp(lam, U), "vjp."),
         "krylov_stream": (lambda: s.newton_step(0.0), "krylov."),
     }[args.profile_case]
+    run()  # warm-up: every kernel of the path launched once (module loading) before the stats
     s.synchronize()
     s.kernel_stats(reset=True)
     t0 = time.perf_counter()
