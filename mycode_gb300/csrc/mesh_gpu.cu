@@ -389,15 +389,19 @@ __global__ void k_face_geo(int nf, const double* xy, const int* f_n1, const int*
 }
 
 // ---------------------------------------------------------------- renumbering
-__global__ void k_minmax(long n, const double* x, const double* y, double* out4) {
-    // one block: x min, x max, y min, y max (exact: selections only)
+// Bounding box of the cell centroids in two passes: each of the first pass's blocks reduces
+// a grid-stride share into part[4 * block + (x min, x max, y min, y max)], then one block
+// reduces the parts (nb of them, x and y read through the same planes: stride 4) into out4.
+// Selections only, so the result is exact in any order.
+__global__ void k_minmax(long n, const double* x, const double* y, long stride, double* out4) {
     __shared__ double s[4][MT];
     double a = 1e300, b = -1e300, c = 1e300, d = -1e300;
-    for (long i = threadIdx.x; i < n; i += MT) {
-        a = fmin(a, x[i]);
-        b = fmax(b, x[i]);
-        c = fmin(c, y[i]);
-        d = fmax(d, y[i]);
+    for (long i = (long)blockIdx.x * MT + threadIdx.x; i < n; i += (long)gridDim.x * MT) {
+        const double xi = x[i * stride], yi = y[i * stride];
+        a = fmin(a, xi);
+        b = fmax(b, stride == 1 ? xi : x[i * stride + 1]);
+        c = fmin(c, yi);
+        d = fmax(d, stride == 1 ? yi : y[i * stride + 1]);
     }
     s[0][threadIdx.x] = a;
     s[1][threadIdx.x] = b;
@@ -413,7 +417,7 @@ __global__ void k_minmax(long n, const double* x, const double* y, double* out4)
         }
         __syncthreads();
     }
-    if (threadIdx.x < 4) out4[threadIdx.x] = s[threadIdx.x][0];
+    if (threadIdx.x < 4) out4[4 * blockIdx.x + threadIdx.x] = s[threadIdx.x][0];
 }
 
 // Hilbert index of (x, y) on a 2^order grid (the quadrant walk of mesh.cpp's hilbert_index)
@@ -686,9 +690,12 @@ std::string build_mesh_gpu(HostMesh& m, int n_nodes, const double* xy, int n_cel
     if (renumber == RENUMBER_HILBERT) {
         DBuf<double> mm;
         DBuf<uint64_t> key;
-        MG_TRY(mm.alloc(4));
+        constexpr int MM_BLOCKS = 304;
+        MG_TRY(mm.alloc(4 * (MM_BLOCKS + 1)));
         MG_TRY(key.alloc(nc));
-        k_minmax<<<1, MT, 0, st>>>(nc, c_xc.p, c_yc.p, mm.p);
+        k_minmax<<<MM_BLOCKS, MT, 0, st>>>(nc, c_xc.p, c_yc.p, 1, mm.p + 4);
+        // the parts: x min / x max at 4 b + 0 / 1, y min / y max at 4 b + 2 / 3
+        k_minmax<<<1, MT, 0, st>>>(MM_BLOCKS, mm.p + 4, mm.p + 6, 4, mm.p);
         double h4[4];
         MG_TRY(cudaMemcpyAsync(h4, mm.p, sizeof(h4), cudaMemcpyDeviceToHost, st));
         MG_TRY(cudaStreamSynchronize(st));
