@@ -325,6 +325,19 @@ static st_t inviscid_flux(st_t L, st_t R, double nx, double ny, int scheme) {
     }
 }
 
+/* The inviscid face flux and the normal flux alone, for the known-answer tests of the
+ * flux library (consistency F(U, U) = F.n(U), rotational invariance); states AoS, 6 doubles */
+void om_inviscid_flux(const double* UL, const double* UR, double nx, double ny, int scheme, double* F) {
+    st_t L = st(UL[0], UL[1], UL[2], UL[3], UL[4], UL[5]), R = st(UR[0], UR[1], UR[2], UR[3], UR[4], UR[5]);
+    st_t o = inviscid_flux(L, R, nx, ny, scheme);
+    F[0] = o.r; F[1] = o.ru; F[2] = o.rv; F[3] = o.rE; F[4] = o.rk; F[5] = o.rw;
+}
+
+void om_normal_flux(const double* U, double nx, double ny, double* F) {
+    st_t o = normal_flux(st(U[0], U[1], U[2], U[3], U[4], U[5]), nx, ny);
+    F[0] = o.r; F[1] = o.ru; F[2] = o.rv; F[3] = o.rE; F[4] = o.rk; F[5] = o.rw;
+}
+
 /* ------------------------------------------------------------------ solver */
 
 typedef struct {

@@ -104,6 +104,8 @@ def _oracle_lib():
             "om_wall_coefficients": (C.c_int, [vp, C.c_int, C.c_void_p, C.c_void_p, C.c_void_p]),
             "om_wall_distance": (None, [vp, _dp]),
             "om_objective": (C.c_double, [vp, C.c_int, C.c_double, C.c_double, C.c_void_p]),
+            "om_inviscid_flux": (None, [_dp, _dp, C.c_double, C.c_double, C.c_int, _dp]),
+            "om_normal_flux": (None, [_dp, C.c_double, C.c_double, _dp]),
         }
         for name, (res, args) in sig.items():
             fn = getattr(lib, name)
@@ -133,6 +135,24 @@ class _Base:
         U[:, 2] = r * v
         U[:, 3] = p / (gamma - 1.0) + 0.5 * r * (u * u + v * v)
         return U
+
+
+FLUX_CODES = {"LLF": 0, "ROE": 1, "HLLC": 2}
+
+
+def inviscid_flux(UL, UR, nx, ny, scheme):
+    """computeInviscidFlux (include/Flux.hpp:216-227) of one face: 6 components."""
+    F = np.zeros(6)
+    _oracle_lib().om_inviscid_flux(np.ascontiguousarray(UL, np.float64), np.ascontiguousarray(UR, np.float64),
+                                   float(nx), float(ny), FLUX_CODES[scheme], F)
+    return F
+
+
+def normal_flux(U, nx, ny):
+    """computeNormalFlux (include/Flux.hpp:23-34): 6 components, k and w zero."""
+    F = np.zeros(6)
+    _oracle_lib().om_normal_flux(np.ascontiguousarray(U, np.float64), float(nx), float(ny), F)
+    return F
 
 
 class OracleSolver(_Base):

@@ -1,0 +1,154 @@
+"""Known-answer tests of the reference's discretisation on the CPU oracle: properties that
+hold whatever the floating-point operation order, so they pin the restatement (and, through
+the bit-exact parity tests, the GPU path) to the mathematics as well as to the reference.
+
+  consistency           F(U, U, n) = F.n(U) for LLF, Roe and HLLC (include/Flux.hpp:36-213)
+  rotational invariance rotating both states' velocities and the normal by one angle rotates
+                        the momentum flux by it and leaves mass and energy fluxes unchanged
+  free-stream           R(U_inf) = 0 on cells two layers or more from the boundary, every
+  preservation          scheme and order, inviscid and viscous (src/Solver.cpp:529-801)
+  Green-Gauss           exact gradients of linear rho, u, v, p on interior cells of a uniform
+                        quad grid (src/Solver.cpp:81-149)
+  Barth-Jespersen       phi in [0, 1] for any state, and phi = 1 on interior cells for a linear
+                        pressure field (src/Solver.cpp:152-253)
+"""
+import numpy as np
+import pytest
+
+import cases as C
+from mycode_gb300 import meshgen as mg
+from oracle.oracle import OracleSolver, inviscid_flux, normal_flux
+
+GAMMA = 1.4
+
+
+def _cons(r, u, v, p):
+    return np.array([r, r * u, r * v, p / (GAMMA - 1.0) + 0.5 * r * (u * u + v * v), 0.0, 0.0])
+
+
+def _random_states(rng, n, mach_max):
+    out = []
+    for _ in range(n):
+        r = rng.uniform(0.3, 3.0)
+        p = rng.uniform(2e4, 3e5)
+        c = np.sqrt(GAMMA * p / r)
+        speed = rng.uniform(0.0, mach_max) * c
+        th = rng.uniform(0.0, 2 * np.pi)
+        out.append(_cons(r, speed * np.cos(th), speed * np.sin(th), p))
+    return out
+
+
+@pytest.mark.parametrize("scheme", ["LLF", "ROE", "HLLC"])
+def test_flux_consistency(scheme):
+    rng = np.random.default_rng(11)
+    for U in _random_states(rng, 400, 3.0):
+        th = rng.uniform(0.0, 2 * np.pi)
+        nx, ny = np.cos(th), np.sin(th)
+        F = inviscid_flux(U, U, nx, ny, scheme)
+        Fn = normal_flux(U, nx, ny)
+        scale = np.abs(Fn).max()
+        assert np.abs(F[:4] - Fn[:4]).max() <= 1e-13 * scale, (scheme, U, F, Fn)
+
+
+def _rotate(U, a):
+    c, s = np.cos(a), np.sin(a)
+    R = U.copy()
+    R[1] = c * U[1] - s * U[2]
+    R[2] = s * U[1] + c * U[2]
+    return R
+
+
+@pytest.mark.parametrize("scheme", ["LLF", "ROE", "HLLC"])
+def test_flux_rotational_invariance(scheme):
+    rng = np.random.default_rng(12)
+    states = _random_states(rng, 600, 2.5)
+    for k in range(0, len(states), 2):
+        UL, UR = states[k], states[k + 1]
+        th = rng.uniform(0.0, 2 * np.pi)
+        nx, ny = np.cos(th), np.sin(th)
+        F = inviscid_flux(UL, UR, nx, ny, scheme)
+        a = rng.uniform(0.0, 2 * np.pi)
+        Fr = inviscid_flux(_rotate(UL, a), _rotate(UR, a), np.cos(th + a), np.sin(th + a), scheme)
+        scale = np.abs(F).max()
+        want = _rotate(F, a)
+        assert np.abs(Fr[:4] - want[:4]).max() <= 1e-11 * scale, (scheme, UL, UR, F, Fr)
+
+
+def _layers_from_boundary(spec, depth):
+    """Cells at least `depth` face-neighbour layers away from every boundary face."""
+    o = OracleSolver(spec, bcset="supersonic", viscous=False, init="freestream")
+    ints, _ = o.faces()
+    owner, nbr = ints[:, 2], ints[:, 3]
+    nc = spec.n_cells
+    near = np.zeros(nc, bool)
+    near[owner[nbr < 0]] = True
+    inner = nbr >= 0
+    for _ in range(depth - 1):
+        grow = near.copy()
+        a, b = owner[inner], nbr[inner]
+        grow[a[near[b]]] = True
+        grow[b[near[a]]] = True
+        near = grow
+    return ~near
+
+
+@pytest.mark.parametrize("name,spec", [("supersonic", lambda: mg.wedge(24, 16, jitter=0.1, seed=3)),
+                                       ("plate_visc", lambda: mg.laminar_plate(24, 16, ratio=1.1))])
+def test_free_stream_preservation(name, spec):
+    spec = spec()
+    case = C.CASES[name]
+    o = OracleSolver(spec, bcset=case["bcset"], viscous=case["viscous"], init=case["init"])
+    C.setup(o, case)
+    U = o.get_state()
+    assert np.ptp(U[:, :4], axis=0).max() == 0.0  # a uniform free stream
+    keep = _layers_from_boundary(spec, 2)
+    assert keep.sum() > 50
+    areas = o.faces()[1][:, 2]
+    scale = np.abs(normal_flux(U[0], 1.0, 0.0)).max() * areas.max()
+    for fl in C.FLUXES:
+        for sp in C.SPATIALS:
+            o.setNumericalMethod(fl, sp)
+            R = o.residual(U)
+            assert np.abs(R[keep, :4]).max() <= 1e-11 * scale, (name, fl, sp)
+
+
+def _linear_box(nx=10, ny=8):
+    spec = mg.box(nx, ny)
+    o = OracleSolver(spec, bcset="bump", viscous=False, init="bump")
+    o.setFlowConditions(0.3, 101325.0, 300.0)
+    o.initialize()
+    xc = o.cells()[:, 1:]
+    return spec, o, xc
+
+
+def test_green_gauss_exact_for_linear_fields():
+    spec, o, xc = _linear_box()
+    x, y = xc[:, 0], xc[:, 1]
+    coef = {"rho": (1.1, 0.2, -0.1), "u": (80.0, 30.0, -20.0), "v": (-10.0, 15.0, 25.0), "p": (1e5, 3e3, -2e3)}
+    prim = np.stack([a + b * x + c * y for a, b, c in coef.values()], axis=1)
+    U = o.state_from_primitives(prim)
+    G = o.gradients(U)
+    keep = _layers_from_boundary(spec, 1)
+    assert keep.sum() >= 40
+    for q, (a, b, c) in enumerate(coef.values()):
+        for d, want in enumerate((b, c)):
+            got = G[keep, 2 * q + d]
+            assert np.abs(got - want).max() <= 1e-10 * max(abs(b), abs(c)), (list(coef)[q], d)
+
+
+def test_limiter_bounds_and_linear_pressure():
+    # any state: 0 <= phi <= 1
+    o = OracleSolver(mg.wedge(24, 16, jitter=0.1, seed=5), bcset="supersonic", viscous=False, init="freestream")
+    o.setFlowConditions(2.5, 101325.0, 300.0)
+    o.initialize()
+    U = C.perturbed_state(o.get_state(), o.cells(), seed=9, amplitude=0.15)
+    phi = o.limiters(U)
+    assert (phi >= 0.0).all() and (phi <= 1.0).all() and (phi < 1.0).any()
+    # a linear pressure (constant density, linear temperature) on a uniform grid: every
+    # reconstructed face pressure lies between the cell's and its neighbour's, so phi = 1
+    spec, o, xc = _linear_box()
+    x, y = xc[:, 0], xc[:, 1]
+    prim = np.stack([np.full_like(x, 1.2), 50.0 + 10.0 * x, 5.0 - 3.0 * y, 1e5 * (1.0 + 0.05 * x - 0.03 * y)], axis=1)
+    phi = o.limiters(o.state_from_primitives(prim))
+    keep = _layers_from_boundary(spec, 2)
+    assert (phi[keep] == 1.0).all()
