@@ -1,6 +1,6 @@
 // Residual kernels R(U) = sum_f (+-) F_f A_f on the renumbered SoA mesh.
 //
-// One evaluation is four launches:
+// One evaluation is four launches (five with the SST cell terms, k_sst_cell):
 //   k_prim    per cell   W = (rho, u, v, p, T [, k, w])           reads U
 //   k_grad    per cell   Green-Gauss gradients + Barth-Jespersen   gathers W over the
 //                        limiter, no atomics                      cell's faces
@@ -8,6 +8,12 @@
 //                        flux
 //   k_gather  per cell   R_i = sum of +-F*A over the cell's faces in the reference's
 //                        face order (deterministic, bit-reproducible)
+// The FP64 residual on a mesh of 100,000 or more interior faces splits the gradient in
+// two (k_grad_faces64: each interior face's Green-Gauss terms once; k_grad64<NV, true>:
+// the per-cell sums in face order and the limiter), the same bits with fewer FP64
+// instructions; the FP32 views' gradients read the neighbours and face geometry from
+// per-cell copies (CellFaces, k_grad_cf).  Through cfdg_residual with pinned host buffers
+// the first and last launch are k_rows_prim and k_gather_rows (the caller's rows in place).
 //
 // The kernels are templated on the scalar S: double / float for the residual, and
 // Dual<double> / Dual<float> for the exact forward linearisation (J v with the limiter

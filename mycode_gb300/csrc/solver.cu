@@ -155,8 +155,9 @@ struct cfdg_solver {
     double cfl = 0.1;
     int step = 0;
     bool limiter_valid = false;
-    // instrumentation: CUDA events around the four kernels of every residual (stat
-    // classes 0-3) and exact J v (4-7) evaluation, resolved at the next stream sync
+    // instrumentation: CUDA events around the four stages of every residual (stat
+    // classes 0-3: primitives, gradients with their face terms and SST cell terms, face
+    // flux, gather) and exact J v (4-7) evaluation, resolved at the next stream sync
     int timing = 0;
     std::vector<cudaEvent_t> pool;
     size_t pool_used = 0;
