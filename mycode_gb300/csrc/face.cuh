@@ -13,7 +13,16 @@ struct FaceGeo {
     R nx, ny, A;
     R dxL, dyL, dxR, dyR;  // face midpoint minus owner / neighbour centroid
     R dxlr, dylr;          // neighbour minus owner centroid (0 on the boundary)
+    R d2lr, id2lr;         // dxlr^2 + dylr^2 and its reciprocal (0 on the boundary), formed
+                           // once per mesh with the expressions the viscous flux would use
 };
+
+// d2lr and id2lr of g from its dxlr, dylr (the mesh upload and host harnesses)
+template <class R>
+CFD_HD void geo_derived(FaceGeo<R>& g) {
+    g.d2lr = g.dxlr * g.dxlr + g.dylr * g.dylr;
+    g.id2lr = g.d2lr > R(0) ? R(1) / g.d2lr : R(0);
+}
 
 // gradient layout per cell: (x, y) pairs of rho, u, v, p, T
 enum { FG_R = 0, FG_U = 2, FG_V = 4, FG_P = 6, FG_T = 8 };
@@ -96,9 +105,9 @@ CFD_HD Flux6<S> face_flux(const Flow<R>& F, const CS<S>& L, const CS<S>& Rn, boo
             dvdy = half(gL[FG_V + 1] + gRv[FG_V + 1]);
             dTdx = half(gL[FG_T] + gRv[FG_T]);
             dTdy = half(gL[FG_T + 1] + gRv[FG_T + 1]);
-            R d2 = g.dxlr * g.dxlr + g.dylr * g.dylr;
+            const R d2 = g.d2lr;  // precomputed per mesh: the same bits as formed here
             if (lt(R(1e-14), d2)) {
-                const R id2 = R(1.0) / d2;  // FP64: four quotients by one reciprocal (div_shared)
+                const R id2 = g.id2lr;  // FP64: four quotients by one reciprocal (div_shared)
                 S du = Rt.u - L.u;
                 S dv = Rt.v - L.v;
                 S a0 = dudx, b0 = dudy, c0 = dvdx, e0 = dvdy;
@@ -165,7 +174,7 @@ CFD_HD Flux6<S> face_flux_sst(const Flow<R>& F, const CS<S>& L, const CS<S>& Rn,
         wR = quot_shared(Rt.rw, Rt.r, ig);
     }
     sst_face_flux(F, out.f[0], kwL[0], kwL[1], kR, wR, half(L.r + Rt.r), mutf, F1f, gkL, gkRv, wall, g.nx, g.ny,
-                  g.A, g.dxL, g.dyL, g.dxlr, g.dylr, Fk, Fw);
+                  g.A, g.dxL, g.dyL, g.dxlr, g.dylr, g.d2lr, g.id2lr, Fk, Fw);
     out.f[4] = Fk;
     out.f[5] = Fw;
     return out;

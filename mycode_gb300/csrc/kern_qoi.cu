@@ -39,7 +39,14 @@ __global__ void __launch_bounds__(256) k_wall_distance(long nc, const double* __
     if (i < nc) {
         double r = nw > 0 ? sqrt(best) : 1e10;
         d[i] = r;
-        if (d32) d32[i] = (float)r;
+        // planes 2: the reciprocal of max(d, 1e-30) that the SST cell terms use (sst_cell_id)
+        const double dd = 1e-30 < r ? r : 1e-30;
+        d[nc + i] = 1.0 / dd;
+        if (d32) {
+            const float rf = (float)r, ddf = 1e-30f < rf ? rf : 1e-30f;
+            d32[i] = rf;
+            d32[nc + i] = 1.0f / ddf;
+        }
     }
 }
 

@@ -278,7 +278,7 @@ __global__ void __launch_bounds__(RED_THREADS) k_gather_norms(MeshView<double> m
     for (long i = (long)blockIdx.x * blockDim.x + threadIdx.x; i < nc; i += (long)gridDim.x * blockDim.x) {
         double acc[NV];
         gather_cell<double, NV>(m, FA, fa_stride, src, nc, i, acc);
-        const double vv = m.vol[i], iv = 1.0 / vv;  // the quotients by one reciprocal (quot_by_recip)
+        const double vv = m.vol[i], iv = m.ivol[i];  // the quotients by 1 / vol (quot_by_recip)
         double s = 0.0, q = 0.0;
 #pragma unroll
         for (int c = 0; c < NV; ++c) {

@@ -45,6 +45,9 @@ struct MeshView {
     const R* dxlr;     // [nf] neighbour centroid minus owner centroid (0 on the boundary)
     const R* dylr;
     const R* vol;      // [nc]
+    const R* d2lr;     // [nf] dxlr^2 + dylr^2 (0 on the boundary), formed once per mesh
+    const R* id2lr;    // [nf] its reciprocal (0 on the boundary)
+    const R* ivol;     // [nc] 1 / vol
 };
 
 // Per-cell copies of each face entry's neighbour cell and face geometry, [4][nc] planes
@@ -296,7 +299,7 @@ __device__ __forceinline__ void grad_item(const MeshView<R>& m, const Flow<R>& F
         }
     }
     R vol = m.vol[i];
-    const R ivol = R(1.0) / vol;  // FP64: the ten quotients by one reciprocal (div_shared)
+    const R ivol = m.ivol[i];  // 1 / vol, once per mesh; FP64: the quotients by it (div_shared)
     // gradient planes are in CellGradient order rho, u, v, p, T (= primitive order)
 #pragma unroll
     for (int q = 0; q < 2 * NQ; ++q) {
@@ -399,17 +402,20 @@ __device__ __forceinline__ FaceGeo<R> load_geo(const MeshView<R>& m, long f) {
     g.dyR = m.dyn[f];
     g.dxlr = m.dxlr[f];
     g.dylr = m.dylr[f];
+    g.d2lr = m.d2lr[f];
+    g.id2lr = m.id2lr[f];
     return g;
 }
 
-// SST cell terms (sst.cuh): T planes 0 mu_t, 1 F1, 2 S_k vol, 3 S_w vol
+// SST cell terms (sst.cuh): T planes 0 mu_t, 1 F1, 2 S_k vol, 3 S_w vol; dwall holds the
+// wall distances and, from nc on, 1 / max(d, 1e-30) (k_wall_distance)
 template <class S, int NV, class R>
 __device__ __forceinline__ void sst_item(const MeshView<R>& m, const Flow<R>& F, const Field<R>& W,
                                          const Field<R>& G, const R* __restrict__ dwall, const Field<R>& T, long i) {
-    SstCell<S> c = sst_cell(F, Acc<S>::ld(W, W_R, i), Acc<S>::ld(W, W_K, i), Acc<S>::ld(W, W_W, i),
+    SstCell<S> c = sst_cell_id(F, Acc<S>::ld(W, W_R, i), Acc<S>::ld(W, W_K, i), Acc<S>::ld(W, W_W, i),
                             Acc<S>::ld(G, G_U, i), Acc<S>::ld(G, G_U + 1, i), Acc<S>::ld(G, G_V, i),
                             Acc<S>::ld(G, G_V + 1, i), Acc<S>::ld(G, G_K, i), Acc<S>::ld(G, G_K + 1, i),
-                            Acc<S>::ld(G, G_W, i), Acc<S>::ld(G, G_W + 1, i), dwall[i]);
+                            Acc<S>::ld(G, G_W, i), Acc<S>::ld(G, G_W + 1, i), dwall[(long)m.nc + i]);
     R vol = m.vol[i];
     Acc<S>::st(T, 0, i, c.mut);
     Acc<S>::st(T, 1, i, c.F1);

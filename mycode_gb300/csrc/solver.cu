@@ -61,9 +61,9 @@ cfdg_status dalloc(T** p, size_t n) {
 template <class R>
 struct GeoBuf {
     R *nx = nullptr, *ny = nullptr, *area = nullptr, *dxo = nullptr, *dyo = nullptr, *dxn = nullptr, *dyn = nullptr,
-      *dxlr = nullptr, *dylr = nullptr, *vol = nullptr;
+      *dxlr = nullptr, *dylr = nullptr, *vol = nullptr, *d2lr = nullptr, *id2lr = nullptr, *ivol = nullptr;
     void release() {
-        R* a[] = {nx, ny, area, dxo, dyo, dxn, dyn, dxlr, dylr, vol};
+        R* a[] = {nx, ny, area, dxo, dyo, dxn, dyn, dxlr, dylr, vol, d2lr, id2lr, ivol};
         for (R* p : a) cudaFree(p);
     }
 };
@@ -77,6 +77,27 @@ cfdg_status upload_geo(GeoBuf<R>& g, const HostMesh& h) {
         TRY(dalloc(dst[k], tmp.size()));
         CK(cudaMemcpy(*dst[k], tmp.data(), tmp.size() * sizeof(R), cudaMemcpyHostToDevice));
     }
+    // mesh invariants the kernels would otherwise form on every evaluation, with their
+    // expressions in R (host code without contraction: the FP64 values have the bits of the
+    // kernels' own FP64 arithmetic): |x_R - x_L|^2 and its reciprocal per face, 1 / vol per
+    // cell
+    const size_t nf = h.dxlr.size(), nc = h.vol.size();
+    std::vector<R> d2(nf), id2(nf), iv(nc);
+    for (size_t f = 0; f < nf; ++f) {
+        FaceGeo<R> g;
+        g.dxlr = (R)h.dxlr[f];
+        g.dylr = (R)h.dylr[f];
+        geo_derived(g);
+        d2[f] = g.d2lr;
+        id2[f] = g.id2lr;
+    }
+    for (size_t c = 0; c < nc; ++c) iv[c] = R(1) / (R)h.vol[c];
+    TRY(dalloc(&g.d2lr, nf));
+    TRY(dalloc(&g.id2lr, nf));
+    TRY(dalloc(&g.ivol, nc));
+    CK(cudaMemcpy(g.d2lr, d2.data(), nf * sizeof(R), cudaMemcpyHostToDevice));
+    CK(cudaMemcpy(g.id2lr, id2.data(), nf * sizeof(R), cudaMemcpyHostToDevice));
+    CK(cudaMemcpy(g.ivol, iv.data(), nc * sizeof(R), cudaMemcpyHostToDevice));
     return CFDG_OK;
 }
 
@@ -1393,10 +1414,11 @@ struct cfdg_solver {
 
     // distance from each cell centroid to the nearest no-slip wall face midpoint
     // (computeWallDistances, src/Solver.cpp:1981-2015), 1e10 without walls, into dwall
-    // (and dwall32 when allocated); dwall is allocated here when the model has none
+    // (and dwall32 when allocated), with 1 / max(d, 1e-30) in their second nc entries;
+    // dwall is allocated here when the model has none
     cfdg_status wall_distance() {
         const HostMesh& h = mesh->h;
-        if (!dwall) TRY(dalloc(&dwall, (size_t)nc));
+        if (!dwall) TRY(dalloc(&dwall, 2 * (size_t)nc));
         std::vector<double> wxy;
         for (int f = 0; f < h.n_faces; ++f)
             if (h.f_n[f] < 0 && h.f_tag[f] == 4) wxy.push_back(h.f_xm[f]);
@@ -1762,6 +1784,7 @@ cfdg_status cfdg_solver_create(const cfdg_mesh* m, const cfdg_config* cfg, cfdg_
         mvx.cf = s->cf; mvx.fo = s->fo; mvx.fn = s->fn; mvx.ftag = s->ftag;
         mvx.nx = g.nx; mvx.ny = g.ny; mvx.area = g.area; mvx.dxo = g.dxo; mvx.dyo = g.dyo;
         mvx.dxn = g.dxn; mvx.dyn = g.dyn; mvx.dxlr = g.dxlr; mvx.dylr = g.dylr; mvx.vol = g.vol;
+        mvx.d2lr = g.d2lr; mvx.id2lr = g.id2lr; mvx.ivol = g.ivol;
     };
     view(s->g64, s->mv);
     view(s->g32, s->mvf);
@@ -1803,7 +1826,7 @@ cfdg_status cfdg_solver_create(const cfdg_mesh* m, const cfdg_config* cfg, cfdg_
     if (h.n_interior >= GRAD_FACE_TERMS_MIN_FACES) TRYS(dalloc(&s->gft, (size_t)2 * NW * h.n_interior));
     if (nv == 6) {
         TRYS(dalloc(&s->Tt, 4 * (size_t)nc)); TRYS(dalloc(&s->Tj, 4 * (size_t)nc)); TRYS(dalloc(&s->Tjd, 4 * (size_t)nc));
-        TRYS(dalloc(&s->dwall, (size_t)nc)); TRYS(dalloc(&s->dwall32, (size_t)nc));
+        TRYS(dalloc(&s->dwall, 2 * (size_t)nc)); TRYS(dalloc(&s->dwall32, 2 * (size_t)nc));
         TRYS(dalloc(&s->T32, 4 * (size_t)nc)); TRYS(dalloc(&s->T32d, 4 * (size_t)nc));
         TRYS(s->wall_distance());
     }

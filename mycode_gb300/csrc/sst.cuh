@@ -39,9 +39,11 @@ struct SstCell {
 template <class S> CFD_HD S tanh_(S x) { return tanh(x); }
 
 // One cell.  r, k, w: density and specific k, w; ux..vy: velocity gradient; kx..wy: k
-// and w gradients; d: wall distance.
+// and w gradients; idd: 1 / max(d, 1e-30) of the wall distance d (a mesh invariant, formed
+// once with the wall distances).
 template <class S, class R>
-CFD_HD SstCell<S> sst_cell(const Flow<R>& F, S r, S k, S w, S ux, S uy, S vx, S vy, S kx, S ky, S wx, S wy, R d) {
+CFD_HD SstCell<S> sst_cell_id(const Flow<R>& F, S r, S k, S w, S ux, S uy, S vx, S vy, S kx, S ky, S wx, S wy,
+                              R idd) {
     typedef SstConst C;
     const R bs = R(C::beta_s), a1 = R(C::a1);
     S kp = smax(k, S(R(0)));
@@ -50,10 +52,8 @@ CFD_HD SstCell<S> sst_cell(const Flow<R>& F, S r, S k, S w, S ux, S uy, S vx, S 
     S S2 = twice(ux * ux + vy * vy + twice(Sxy) * Sxy);
     S Smag = sqrt(S2 + S(R(1e-30)));
     S nu = S(F.nu);
-    R dd = lt(R(1e-30), d) ? d : R(1e-30);
     // one reciprocal per divisor (w, d, CD_kw, the eddy viscosity's denominator)
     const S iwp = R(1) / wp;
-    const R idd = R(1) / dd;
     S gkgw = kx * wx + ky * wy;
     S CDkw = smax(twice(r) * R(C::sw2) * gkgw * iwp, S(R(1e-10)));
     S sk = sqrt(kp + S(R(1e-30)));
@@ -79,12 +79,20 @@ CFD_HD SstCell<S> sst_cell(const Flow<R>& F, S r, S k, S w, S ux, S uy, S vx, S 
     return o;
 }
 
+// the same from the wall distance d itself
+template <class S, class R>
+CFD_HD SstCell<S> sst_cell(const Flow<R>& F, S r, S k, S w, S ux, S uy, S vx, S vy, S kx, S ky, S wx, S wy, R d) {
+    const R dd = lt(R(1e-30), d) ? d : R(1e-30);
+    return sst_cell_id(F, r, k, w, ux, uy, vx, vy, kx, ky, wx, wy, R(1) / dd);
+}
+
 // k and w face fluxes times the face area: first-order upwind advection with the Riemann
 // mass flux (mdotA = mass flux times area), and diffusion (mu + sigma mu_t) grad(phi).n A
 // with averaged, corrected face gradients (one-sided at a no-slip wall).
 template <class S, class R>
 CFD_HD void sst_face_flux(const Flow<R>& F, S mdotA, S kL, S wL, S kR, S wR, S rf, S mutf, S F1f, const S* gkL,
-                          const S* gkR, bool wall, R nx, R ny, R A, R dxL, R dyL, R dxlr, R dylr, S& Fk, S& Fw) {
+                          const S* gkR, bool wall, R nx, R ny, R A, R dxL, R dyL, R dxlr, R dylr, R d2lr,
+                          R id2lr, S& Fk, S& Fw) {
     typedef SstConst C;
     S mp = smax(mdotA, S(R(0))), mm = smin(mdotA, S(R(0)));
     Fk = mp * kL + mm * kR;
@@ -103,9 +111,9 @@ CFD_HD void sst_face_flux(const Flow<R>& F, S mdotA, S kL, S wL, S kR, S wR, S r
     } else {
         S kx = half(gkL[0] + gkR[0]), ky = half(gkL[1] + gkR[1]);
         S wx = half(gkL[2] + gkR[2]), wy = half(gkL[3] + gkR[3]);
-        R d2 = dxlr * dxlr + dylr * dylr;
+        const R d2 = d2lr;  // dxlr^2 + dylr^2, precomputed per mesh
         if (lt(R(1e-14), d2)) {
-            const R id2 = R(1) / d2;  // the viscous flux's reciprocal of the same d2
+            const R id2 = id2lr;  // its reciprocal, precomputed (the viscous flux's too)
             S ck = div_shared(kx * dxlr + ky * dylr - (kR - kL), d2, id2);
             S cw = div_shared(wx * dxlr + wy * dylr - (wR - wL), d2, id2);
             kx = kx - ck * dxlr;

@@ -21,6 +21,7 @@ FaceGeo<double> geo(const double* g) {
     FaceGeo<double> G;
     G.nx = g[0]; G.ny = g[1]; G.A = g[2]; G.dxL = g[3]; G.dyL = g[4]; G.dxR = g[5]; G.dyR = g[6];
     G.dxlr = g[7]; G.dylr = g[8];
+    geo_derived(G);
     return G;
 }
 CS<double> cs(const Flow<double>& F, const double* U) { return make_cs(F, U[0], U[1], U[2], U[3], U[4], U[5]); }
