@@ -3,6 +3,7 @@
 // src/Solver.cpp:543-800).  Shared by the residual kernel (any scalar type) and by the
 // adjoint, which differentiates exactly this sequence of operations.
 #pragma once
+#include <type_traits>
 #include "physics.cuh"
 #include "sst.cuh"
 
@@ -105,9 +106,12 @@ CFD_HD Flux6<S> face_flux(const Flow<R>& F, const CS<S>& L, const CS<S>& Rn, boo
             dvdy = half(gL[FG_V + 1] + gRv[FG_V + 1]);
             dTdx = half(gL[FG_T] + gRv[FG_T]);
             dTdy = half(gL[FG_T + 1] + gRv[FG_T + 1]);
-            const R d2 = g.d2lr;  // precomputed per mesh: the same bits as formed here
+            // FP64: precomputed per mesh, the same bits as formed here; the FP32 views form
+            // them in the kernel (their FMA contraction and approximate divide)
+            constexpr bool pre = std::is_same<R, double>::value;
+            const R d2 = pre ? g.d2lr : g.dxlr * g.dxlr + g.dylr * g.dylr;
             if (lt(R(1e-14), d2)) {
-                const R id2 = g.id2lr;  // FP64: four quotients by one reciprocal (div_shared)
+                const R id2 = pre ? g.id2lr : R(1.0) / d2;  // FP64: four quotients by one reciprocal
                 S du = Rt.u - L.u;
                 S dv = Rt.v - L.v;
                 S a0 = dudx, b0 = dudy, c0 = dvdx, e0 = dvdy;

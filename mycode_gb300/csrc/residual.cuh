@@ -299,7 +299,9 @@ __device__ __forceinline__ void grad_item(const MeshView<R>& m, const Flow<R>& F
         }
     }
     R vol = m.vol[i];
-    const R ivol = m.ivol[i];  // 1 / vol, once per mesh; FP64: the quotients by it (div_shared)
+    // 1 / vol: FP64 once per mesh (the same bits), the FP32 views in the kernel; FP64: the
+    // quotients by it (div_shared)
+    const R ivol = std::is_same<R, double>::value ? m.ivol[i] : R(1.0) / vol;
     // gradient planes are in CellGradient order rho, u, v, p, T (= primitive order)
 #pragma unroll
     for (int q = 0; q < 2 * NQ; ++q) {
@@ -412,10 +414,13 @@ __device__ __forceinline__ FaceGeo<R> load_geo(const MeshView<R>& m, long f) {
 template <class S, int NV, class R>
 __device__ __forceinline__ void sst_item(const MeshView<R>& m, const Flow<R>& F, const Field<R>& W,
                                          const Field<R>& G, const R* __restrict__ dwall, const Field<R>& T, long i) {
+    // 1 / max(d, 1e-30): FP64 from k_wall_distance (the same bits), the FP32 views in the kernel
+    const R dwi = dwall[i];
+    const R idd = std::is_same<R, double>::value ? dwall[(long)m.nc + i] : R(1) / (lt(R(1e-30), dwi) ? dwi : R(1e-30));
     SstCell<S> c = sst_cell_id(F, Acc<S>::ld(W, W_R, i), Acc<S>::ld(W, W_K, i), Acc<S>::ld(W, W_W, i),
                             Acc<S>::ld(G, G_U, i), Acc<S>::ld(G, G_U + 1, i), Acc<S>::ld(G, G_V, i),
                             Acc<S>::ld(G, G_V + 1, i), Acc<S>::ld(G, G_K, i), Acc<S>::ld(G, G_K + 1, i),
-                            Acc<S>::ld(G, G_W, i), Acc<S>::ld(G, G_W + 1, i), dwall[(long)m.nc + i]);
+                            Acc<S>::ld(G, G_W, i), Acc<S>::ld(G, G_W + 1, i), idd);
     R vol = m.vol[i];
     Acc<S>::st(T, 0, i, c.mut);
     Acc<S>::st(T, 1, i, c.F1);

@@ -19,6 +19,7 @@
 // reference's constant-nu model, mu = rho nu.  The -2/3 rho k delta_ij part of the
 // Reynolds stress is neglected.
 #pragma once
+#include <type_traits>
 #include "physics.cuh"
 
 namespace cfdg {
@@ -111,9 +112,12 @@ CFD_HD void sst_face_flux(const Flow<R>& F, S mdotA, S kL, S wL, S kR, S wR, S r
     } else {
         S kx = half(gkL[0] + gkR[0]), ky = half(gkL[1] + gkR[1]);
         S wx = half(gkL[2] + gkR[2]), wy = half(gkL[3] + gkR[3]);
-        const R d2 = d2lr;  // dxlr^2 + dylr^2, precomputed per mesh
+        // dxlr^2 + dylr^2 and its reciprocal: precomputed per mesh for FP64 (the viscous
+        // flux's too), formed here for the FP32 views
+        constexpr bool pre = std::is_same<R, double>::value;
+        const R d2 = pre ? d2lr : dxlr * dxlr + dylr * dylr;
         if (lt(R(1e-14), d2)) {
-            const R id2 = id2lr;  // its reciprocal, precomputed (the viscous flux's too)
+            const R id2 = pre ? id2lr : R(1) / d2;
             S ck = div_shared(kx * dxlr + ky * dylr - (kR - kL), d2, id2);
             S cw = div_shared(wx * dxlr + wy * dylr - (wR - wL), d2, id2);
             kx = kx - ck * dxlr;

@@ -8,9 +8,10 @@ of lambda^T R along 16 seeded directions, and dJ/dU against differences of J: at
 of 24 Newton steps from the free stream (a developing boundary layer and shock), and at the
 converged state.  The full mesh converges six orders of the volume-weighted residual from
 the free stream under the reference's pseudo-transient control with a continuation
-schedule for the CFL cap: 2 through the start-up transient (the first 16,384 steps; with a
-cap of 2.5 or more the transient goes non-finite with the reference's scalar diagonal
-preconditioner), then 10 (cfdg_set_cfl_max).  The 200 x 160 mesh converges six orders
+schedule for the CFL cap: 1.5 through the start-up transient (the first 16,384 steps; with
+a cap of 2.5 or more the transient goes non-finite with the reference's scalar diagonal
+preconditioner, and at 2 it survives or not depending on the FP32 Krylov solutions'
+last bits), then 10 (cfdg_set_cfl_max).  The 200 x 160 mesh converges six orders
 with the reference's cap.  (No reference counterpart: the reference has no SST and no adjoint.)"""
 import numpy as np
 import pytest
@@ -92,7 +93,7 @@ def test_swbli_200x160_converges_six_orders(cuda_lib):
 
 
 def test_swbli_full_size_converges_six_orders_then_wall_pressure_vjp(cuda_lib):
-    m, s = _solver(cuda_lib, mg.swbli(), cfl_max=2.0)
+    m, s = _solver(cuda_lib, mg.swbli(), cfl_max=1.5)
     assert m.n_cells == 768_000
     recs = []
     while len(recs) < 40_000:
@@ -103,7 +104,7 @@ def test_swbli_full_size_converges_six_orders_then_wall_pressure_vjp(cuda_lib):
         if recs[-1].res_vm <= 1e-6 * recs[0].res_vm:
             break
     orders = np.log10(recs[0].res_vm / recs[-1].res_vm)
-    print(f"SWBLI 768,000 cells, CFL cap 2 then 10: {len(recs)} Newton steps, res_vm {recs[0].res_vm:.3e} -> "
+    print(f"SWBLI 768,000 cells, CFL cap 1.5 then 10: {len(recs)} Newton steps, res_vm {recs[0].res_vm:.3e} -> "
           f"{recs[-1].res_vm:.3e} ({orders:.2f} orders), res_rho {recs[0].res_rho:.3e} -> {recs[-1].res_rho:.3e}")
     assert orders >= 6.0
     U = s.getSolution()
