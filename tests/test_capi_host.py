@@ -86,3 +86,20 @@ def test_no_cpu_fallback_without_gpu():
     with pytest.raises(api.CfdgError) as e:
         api.Solver(m)
     assert e.value.status == 2 and "no CUDA device" in str(e.value)
+
+
+def test_solver_entry_points_reject_a_null_handle():
+    """Entry points taking a solver return CFDG_ERR_ARG (1) with a message for a null handle
+    (no GPU needed: the check comes before any device work)."""
+    lib = api.lib()
+    cfl, step = ctypes.c_double(), ctypes.c_int()
+    calls = {
+        "cfdg_set_cfl_max": (None, 2.0),
+        "cfdg_set_newton_state": (None, 1.0, 0),
+        "cfdg_get_newton_state": (None, ctypes.byref(cfl), ctypes.byref(step)),
+        "cfdg_reset_newton": (None,),
+        "cfdg_set_krylov": (None, 1),
+    }
+    for name, args in calls.items():
+        assert getattr(lib, name)(*args) == 1, name
+        assert lib.cfdg_last_error().decode(), name
