@@ -117,6 +117,11 @@ typedef struct cfdg_config {
      *   by at most this fraction (e.g. 0.2). */
     int startup_first_order;
     double update_limit;
+    /* exact J v Arnoldi body: from this many cells the gather of J v and the iteration's
+     * dots run as two kernels (the fused kernel's dependent face gathers hold back its
+     * streaming dots on large meshes); the same results bit for bit either way.
+     * 0 = the default, 262,144 cells; a negative value never splits. */
+    int gather_split_cells;
 } cfdg_config;
 
 /* CFDG_KRYLOV_STREAM launches the graph driver's kernels one iteration at a time from a

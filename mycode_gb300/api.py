@@ -48,7 +48,7 @@ class Config(C.Structure):
         ("turb_intensity", C.c_double), ("mut_ratio", C.c_double), ("shock_deflection_deg", C.c_double),
         ("renumber", C.c_int), ("device", C.c_int), ("krylov", C.c_int), ("persistent", C.c_int), ("pdl", C.c_int),
         ("barrier_poll_limit", C.c_int), ("newton_chain", C.c_int), ("startup_first_order", C.c_int),
-        ("update_limit", C.c_double),
+        ("update_limit", C.c_double), ("gather_split_cells", C.c_int),
     ]
 
 

@@ -143,7 +143,14 @@ void launch_gmres_prim_z<float>(int nv, long nc, const Flow<float>& F, const flo
 }
 template <>
 void launch_gmres_gather_dot<float>(int nv, const MeshView<float>& m, const float* FA, float* w, const float* z, const float* dt,
-                                 const float* src, const float* V, long L, const GmresDev& d, cudaStream_t s, bool pdl) {
+                                 const float* src, const float* V, long L, const GmresDev& d, cudaStream_t s, bool pdl, bool split) {
+    if (split) {  // the gather, then the dots streamed on their own
+        NV_SWITCH(nv, launch_k(pdl, k_gmres_gather_w<float, NVC>, dim3(grid_for(m.nc, 256)), dim3(256), s, m, FA,
+                               (long)m.nf, w, z, dt, src, d));
+        NV_SWITCH(nv, launch_k(pdl, k_gmres_gather_dot<float, NVC, true>, dim3(gather_grid(m.nc, 4)), dim3(RED_THREADS), s,
+                               m, FA, (long)m.nf, w, z, dt, src, V, L, d));
+        return;
+    }
     NV_SWITCH(nv, launch_k(pdl, k_gmres_gather_dot<float, NVC>, dim3(gather_grid(m.nc, 4)), dim3(RED_THREADS), s, m, FA,
                            (long)m.nf,
                            w, z, dt, src, V, L, d));

@@ -214,7 +214,14 @@ void launch_gmres_prim_z<double>(int nv, long nc, const Flow<double>& F, const d
 }
 template <>
 void launch_gmres_gather_dot<double>(int nv, const MeshView<double>& m, const double* FA, double* w, const double* z, const double* dt,
-                                 const double* src, const double* V, long L, const GmresDev& d, cudaStream_t s, bool pdl) {
+                                 const double* src, const double* V, long L, const GmresDev& d, cudaStream_t s, bool pdl, bool split) {
+    if (split) {  // the gather, then the dots streamed on their own
+        NV_SWITCH(nv, launch_k(pdl, k_gmres_gather_w<double, NVC>, dim3(grid_for(m.nc, 256)), dim3(256), s, m, FA,
+                               (long)m.nf, w, z, dt, src, d));
+        NV_SWITCH(nv, launch_k(pdl, k_gmres_gather_dot<double, NVC, true>, dim3(gather_grid(m.nc, 8)), dim3(RED_THREADS), s,
+                               m, FA, (long)m.nf, w, z, dt, src, V, L, d));
+        return;
+    }
     NV_SWITCH(nv, launch_k(pdl, k_gmres_gather_dot<double, NVC>, dim3(gather_grid(m.nc, 8)), dim3(RED_THREADS), s, m, FA,
                            (long)m.nf,
                            w, z, dt, src, V, L, d));

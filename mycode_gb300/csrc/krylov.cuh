@@ -48,6 +48,11 @@ constexpr int KRY_MAXM = 128;  // largest Krylov dimension of the device solver
 // 28,800-cell plate with the four-kernel body: 3, 4, 5, 6 give 783.5, 783, 780, 780 M
 // cell-residuals/s (the same GB300)
 constexpr int KRY_BODY_ITERS = 4;
+// Default cell count from which the gather and the dots of an Arnoldi iteration run as two
+// kernels (k_gmres_gather_w, then k_gmres_gather_dot<..., true>; cfdg_config
+// gather_split_cells): on large meshes the fused kernel's per-cell dependent face gathers
+// hold back its streaming dots; on small ones the kernel boundary costs more than it saves.
+constexpr long KRY_SPLIT_GATHER_CELLS = 262144;
 
 struct GmresDev {
     int* gi;          // [0] j (FD body), [1] k (last iteration), [2] done, [3] m, [4] this iteration
@@ -619,7 +624,11 @@ __global__ void __launch_bounds__(RED_THREADS) k_gmres_multidot(long L, const T*
 // Grid-stride over cells (gather_grid blocks).  With an FP32 basis the kernel fits 128
 // registers without spills, so two blocks share an SM (a streaming pass over a
 // million-cell basis needs the loads of more than one block in flight per SM).
-template <class T, int NV>
+// SPLIT (large meshes): w was gathered by k_gmres_gather_w (one thread per cell, the same
+// arithmetic), and this kernel only streams w, P_j and the basis for the dots, with no
+// dependent loads in its loop; the same grid and the same per-thread cells, so the block
+// partials are the fused kernel's bit for bit.
+template <class T, int NV, bool SPLIT = false>
 __global__ void __launch_bounds__(RED_THREADS, sizeof(T) == 4 ? 2 : 1)
     k_gmres_gather_dot(MeshView<T> m, const T* __restrict__ FA,
                                                                   long fa_stride, T* __restrict__ w,
@@ -641,6 +650,11 @@ __global__ void __launch_bounds__(RED_THREADS, sizeof(T) == 4 ? 2 : 1)
         T tc, zc[NV], pj[NV], s4, s5;
     };
     auto pre = [&](long i, Pre& p) {
+        if constexpr (SPLIT) {
+#pragma unroll
+            for (int c = 0; c < NV; ++c) p.pj[c] = Pj[c * nc + i];
+            return;
+        }
 #pragma unroll
         for (int k = 0; k < 4; ++k) p.ek[k] = m.cf[(long)k * nc + i];
         p.tc = m.vol[i] / (dt[i] + T(1e-30));
@@ -656,6 +670,14 @@ __global__ void __launch_bounds__(RED_THREADS, sizeof(T) == 4 ? 2 : 1)
     };
     A nw = A(0);  // |w|^2
     auto gather = [&](long i, const Pre& p, T (&acc)[NV]) {
+        if constexpr (SPLIT) {
+#pragma unroll
+            for (int c = 0; c < NV; ++c) {
+                acc[c] = w[c * nc + i];
+                nw += (A)acc[c] * (A)acc[c];
+            }
+            return;
+        }
 #pragma unroll
         for (int c = 0; c < NV; ++c) acc[c] = T(0);
 #pragma unroll
@@ -781,6 +803,29 @@ __global__ void __launch_bounds__(RED_THREADS, sizeof(T) == 4 ? 2 : 1)
     block_partials(reinterpret_cast<A*>(d.partial), j, wsp);
     block_partials(reinterpret_cast<A*>(d.partial) + (long)(j + 1) * RED_BLOCKS, j + 1, wsw);
     if (blockIdx.x == 0 && threadIdx.x == 0) d.gi[5] = j + 1;  // products reduced
+}
+
+// The gather of k_gmres_gather_dot alone (large meshes: its SPLIT form then takes the
+// dots), one thread per cell: w = the faces' F*A derivatives in reference face order, minus
+// the SST source derivatives, plus z vol / dt, with the fused kernel's arithmetic.
+template <class T, int NV>
+__global__ void __launch_bounds__(256) k_gmres_gather_w(MeshView<T> m, const T* __restrict__ FA, long fa_stride,
+                                                        T* __restrict__ w, const T* __restrict__ z,
+                                                        const T* __restrict__ dt, const T* __restrict__ src,
+                                                        GmresDev d) {
+    const long nc = m.nc;
+    const long i = (long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (d.gi[2] || i >= nc) return;  // the solve has ended
+    const T tc = m.vol[i] / (dt[i] + T(1e-30));
+    T zc[NV];
+#pragma unroll
+    for (int c = 0; c < NV; ++c) zc[c] = z[c * nc + i];
+    pdl_wait();  // the face fluxes are the predecessor's
+    pdl_trigger();
+    T acc[NV];
+    gather_cell<T, NV>(m, FA, fa_stride, src, nc, i, acc);
+#pragma unroll
+    for (int c = 0; c < NV; ++c) w[c * nc + i] = acc[c] + zc[c] * tc;
 }
 
 // w -= sum_{i<=j} h1[i] sc[i] V_i, fused with the second CGS pass h2 = V^T w (FD J v

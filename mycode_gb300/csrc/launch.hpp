@@ -220,9 +220,11 @@ template <class T> void launch_gmres_multidot(long L, const T* w, const T* V, co
 template <class T> void launch_gmres_prim_z(int nv, long nc, const Flow<T>& F, const T* U, T* V, long L,
                                             const T* Dinv, T* z, Field<T> W, const T* w, const GmresDev& d,
                                             cudaGraphConditionalHandle h, cudaStream_t s);
+// split: the gather (k_gmres_gather_w) and the dots (k_gmres_gather_dot<..., true>) as two
+// kernels, the same results bit for bit
 template <class T> void launch_gmres_gather_dot(int nv, const MeshView<T>& m, const T* FA, T* w, const T* z,
                                                 const T* dt, const T* src, const T* V, long L, const GmresDev& d,
-                                                cudaStream_t s, bool pdl = false);
+                                                cudaStream_t s, bool pdl = false, bool split = false);
 template <class T> void launch_gmres_update_dot(long L, T* w, const T* V, const GmresDev& d, cudaStream_t s);
 template <class T> void launch_gmres_update_final(long L, const T* w, T* V, const GmresDev& d,
                                                   cudaGraphConditionalHandle h, cudaStream_t s);

@@ -734,6 +734,11 @@ struct cfdg_solver {
     }
 
     int body_unroll() const { return KRY_BODY_ITERS; }
+    // the exact J v body's gather and dots as two kernels (cfdg_config.gather_split_cells)
+    bool gather_split() const {
+        const long t = cfg.gather_split_cells == 0 ? KRY_SPLIT_GATHER_CELLS : (long)cfg.gather_split_cells;
+        return t > 0 && (long)nc >= t;
+    }
     // WHILE-body executions of a graph solve of `iters` iterations
     long long body_runs(int iters) const {
         if (use_persistent() || !(cfg.precision == CFDG_MIXED || cfg.jv == CFDG_JV_EXACT)) return iters;
@@ -769,9 +774,9 @@ struct cfdg_solver {
             a.tangent = true;
             launch_jv_mid<float>(a);
             launch_gmres_gather_dot<float>(nv, mvf, FA32d, w32, z32, dt32, nv == 6 ? T32d + 2 * nc : nullptr, V32, L, gd,
-                                           st, pdl);
+                                           st, pdl, gather_split());
             if (ev) CK(cudaEventRecord(ev[4], st));
-            launches += nv == 6 ? 5 : 4;
+            launches += (nv == 6 ? 5 : 4) + (gather_split() ? 1 : 0);
         } else if (cfg.jv == CFDG_JV_EXACT) {
             launch_gmres_prim_z<double>(nv, nc, F, Ubase, V, L, dinv64, z, f64(Wj, Wjd), w64, gd, h, st);
             ResArgs<double> a;
@@ -791,9 +796,9 @@ struct cfdg_solver {
             a.done = gd.gi + 2;
             launch_jv_mid<double>(a);
             launch_gmres_gather_dot<double>(nv, mv, FAjd, w64, z, dt, nv == 6 ? Tjd + 2 * nc : nullptr, V, L, gd, st,
-                                            pdl);
+                                            pdl, gather_split());
             if (ev) CK(cudaEventRecord(ev[4], st));
-            launches += nv == 6 ? 5 : 4;
+            launches += (nv == 6 ? 5 : 4) + (gather_split() ? 1 : 0);
         } else {
             launch_gmres_z<double>(nv, nc, V, L, dinv64, z, gd, st);
             ++launches;
@@ -1630,6 +1635,7 @@ void cfdg_config_default(cfdg_config* c) {
     c->newton_chain = 8;
     c->startup_first_order = 0;
     c->update_limit = 0.0;
+    c->gather_split_cells = 0;
 }
 
 cfdg_status cfdg_mesh_create(int n_nodes, const double* xy, int n_cells, const int* cells, int n_bedges,
