@@ -140,8 +140,10 @@ __device__ __forceinline__ void prim_cell(const Flow<R>& F, S r, S ru, S rv, S r
     Acc<S>::st(W, W_P, i, p);
     Acc<S>::st(W, W_T, i, T);
     if (NV == 6) {
-        Acc<S>::st(W, W_K, i, rk / r);
-        Acc<S>::st(W, W_W, i, rw / r);
+        // the specific k and w through the same reciprocal of rho (FP64: RN(rk / r) for
+        // finite nonzero quotients; a zero rk gives +0)
+        Acc<S>::st(W, W_K, i, quot_shared(rk, r, ir));
+        Acc<S>::st(W, W_W, i, quot_shared(rw, r, ir));
     }
 }
 

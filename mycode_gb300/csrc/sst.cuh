@@ -37,7 +37,31 @@ struct SstCell {
     S mut, F1, Sk, Sw;  // eddy viscosity, blending, sources per unit volume
 };
 
+// tanh where its rounded value is settled without evaluating it.  1 - tanh x = 2 / (e^{2x}
+// + 1) is below half an ulp of 1 (2^-54 in FP64, 2^-25 in FP32) from x = 19.06 (8.66), so
+// from TANH_ONE on the rounded tanh is 1; tanh x = x (1 - x^2 / 3 + ...) rounds to x below
+// TANH_ID (x^2 / 3 under half an ulp).  In the SST model F1 = tanh(arg1^4) and F2 =
+// tanh(arg2^2) sit in those two ranges in most cells (near a wall and in the free stream), so
+// most calls cost a comparison.  Checked bit for bit against CUDA's tanh on both sides of
+// both thresholds (tests/test_gpu_exact64.py).
+template <class R> struct TanhSat;
+template <> struct TanhSat<double> { static constexpr double one = 19.5, id = 7.450580596923828e-09; };  // 2^-27
+template <> struct TanhSat<float> { static constexpr float one = 9.5f, id = 1.220703125e-04f; };        // 2^-13
+template <class R>
+CFD_HD R tanh_sat(R x) {
+    const R ax = x < R(0) ? -x : x;
+    if (ax < TanhSat<R>::id) return x;
+    if (x >= TanhSat<R>::one) return R(1);
+    return tanh(x);
+}
 template <class S> CFD_HD S tanh_(S x) { return tanh(x); }
+CFD_HD double tanh_(double x) { return tanh_sat(x); }
+CFD_HD float tanh_(float x) { return tanh_sat(x); }
+// the dual number's: the value as above, the derivative (1 - t^2) x' (0 where t is 1)
+template <class R> CFD_HD Dual<R> tanh_(Dual<R> a) {
+    const R t = tanh_sat(a.v);
+    return Dual<R>(t, (R(1) - t * t) * a.d);
+}
 
 // One cell.  r, k, w: density and specific k, w; ux..vy: velocity gradient; kx..wy: k
 // and w gradients; idd: 1 / max(d, 1e-30) of the wall distance d (a mesh invariant, formed
@@ -169,12 +193,12 @@ CFD_HD void sst_cell_b(const Flow<R>& F, R r, R k, R w, R ux, R uy, R vx, R vy, 
     bool a1cap = R(10) < arg1u;
     R arg1 = a1cap ? R(10) : arg1u;
     R a14 = arg1 * arg1 * arg1 * arg1;
-    R F1 = tanh(a14);
+    R F1 = tanh_sat(a14);
     bool a2t2 = R(2) * t1 < t2;
     R arg2u = a2t2 ? t2 : R(2) * t1;
     bool a2cap = R(100) < arg2u;
     R arg2 = a2cap ? R(100) : arg2u;
-    R F2 = tanh(arg2 * arg2);
+    R F2 = tanh_sat(arg2 * arg2);
     R da = a1 * wp, ds = Smag * F2;
     bool dens = da < ds;
     R den = dens ? ds : da;

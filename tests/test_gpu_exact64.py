@@ -48,3 +48,32 @@ def test_exact64_ops_equal_fp64_instructions(tmp_path):
     with np.errstate(over="ignore"):
         np.testing.assert_array_equal(o[:, 0], (v * 0.5).view(np.uint64))
         np.testing.assert_array_equal(o[:, 2], (v * 2.0).view(np.uint64))
+
+
+def test_tanh_saturation_equals_cuda_tanh(tmp_path):
+    """The SST model's tanh_sat (1 from 19.5 in FP64 / 9.5 in FP32 on, x below 2^-27 /
+    2^-13) against CUDA's tanh and tanhf bit for bit: dense samples on both sides of both
+    thresholds, every exponent above and below them, and the special values."""
+    nvcc = shutil.which("nvcc") or "/usr/local/cuda/bin/nvcc"
+    if not os.path.exists(nvcc):
+        pytest.skip("nvcc not found")
+    exe = tmp_path / "tanh_check"
+    subprocess.run([nvcc, "-gencode", "arch=compute_103a,code=sm_103a", "-O3", "-std=c++17", "-o", str(exe),
+                    os.path.join(HERE, "exact64", "tanh_check.cu")], check=True)
+    rng = np.random.default_rng(5)
+    v = np.concatenate([
+        np.linspace(0.0, 30.0, 600001),                 # through both upper thresholds
+        rng.uniform(8.0, 25.0, 400000),
+        np.exp(rng.uniform(np.log(25.0), np.log(1e300), 100000)),
+        np.exp(rng.uniform(np.log(1e-320), np.log(1e-2), 400000)),  # through both lower thresholds
+        [0.0, -0.0, 5e-324, np.inf, 2.0 ** -27, np.nextafter(2.0 ** -27, 0), 2.0 ** -13, 19.5, 9.5],
+    ])
+    v = np.concatenate([v, -v[: 200000]])
+    (tmp_path / "in.bin").write_bytes(v.astype(np.float64).tobytes())
+    subprocess.run([str(exe), str(tmp_path / "in.bin"), str(tmp_path / "out.bin")], check=True)
+    o = np.frombuffer((tmp_path / "out.bin").read_bytes(), dtype=np.uint64).reshape(-1, 4)
+    assert o.shape[0] == v.size
+    bad64 = np.nonzero(o[:, 0] != o[:, 1])[0]
+    bad32 = np.nonzero(o[:, 2] != o[:, 3])[0]
+    assert bad64.size == 0, v[bad64[:5]]
+    assert bad32.size == 0, v[bad32[:5]]
