@@ -638,9 +638,9 @@ CFD_HD void face_flux_b(const Flow<R>& F, const CS<R>& L, const CS<R>& Rn, bool 
         bool wall = !interior && tag == 4;
         R dx = g.dxL, dy = g.dyL, d2w = dx * dx + dy * dy;
         R a0, b0, c0, e0, dTdx, dTdy;
-        R d2 = g.dxlr * g.dxlr + g.dylr * g.dylr;
-        bool corr = !wall && d2 > R(1e-14);
-        const R id2w = wall ? R(1) / d2w : R(0), id2 = corr ? R(1) / d2 : R(0);
+        // |x_R - x_L|^2 and its reciprocal: formed once per mesh (FaceGeo d2lr, id2lr)
+        bool corr = !wall && g.d2lr > R(1e-14);
+        const R id2w = wall ? R(1) / d2w : R(0), id2 = corr ? g.id2lr : R(0);
         R du = Rt.u - L.u, dv = Rt.v - L.v;
         R dudx, dudy, dvdx, dvdy;
         if (wall) {
@@ -797,7 +797,7 @@ CFD_HD void face_flux_sst_b(const Flow<R>& F, const CS<R>& L, const CS<R>& Rn, b
     R kL = L.rk / L.r, wL = L.rw / L.r, kR = Rt.rk / Rt.r, wR = Rt.rw / Rt.r;
     R mdotAb = 0, kLb = 0, wLb = 0, kRb = 0, wRb = 0, rfb = 0, mutfb = 0, F1fb = 0;
     sst_face_flux_b(F, out.f[0], kL, wL, kR, wR, R(0.5) * (L.r + Rt.r), mutf, F1f, gkL, gkRv, wall, g.nx, g.ny, g.A,
-                    g.dxL, g.dyL, g.dxlr, g.dylr, FAb_in[4], FAb_in[5], mdotAb, kLb, wLb, kRb, wRb, rfb, mutfb, F1fb,
+                    g.dxL, g.dyL, g.dxlr, g.dylr, g.d2lr, g.id2lr, FAb_in[4], FAb_in[5], mdotAb, kLb, wLb, kRb, wRb, rfb, mutfb, F1fb,
                     gkLb, gkRvb);
     // the mean flow, with the k and w rows' mass-flux adjoint added to row 0
     R FAb[6] = {FAb_in[0] + mdotAb, FAb_in[1], FAb_in[2], FAb_in[3], R(0), R(0)};

@@ -171,7 +171,7 @@ __global__ void __launch_bounds__(128) k_adj_cell1(MeshView<double> m, Flow<doub
         const double* Gi = G.v;
         sst_cell_b(F, wi[W_R], wi[W_K], wi[W_W], Gi[G_U * nc + i], Gi[(G_U + 1) * nc + i], Gi[G_V * nc + i],
                    Gi[(G_V + 1) * nc + i], Gi[G_K * nc + i], Gi[(G_K + 1) * nc + i], Gi[G_W * nc + i],
-                   Gi[(G_W + 1) * nc + i], dwall[i], mutb, F1b, Skb, Swb, wb[W_R], wb[W_K], wb[W_W], gb[G_U],
+                   Gi[(G_W + 1) * nc + i], dwall[nc + i], mutb, F1b, Skb, Swb, wb[W_R], wb[W_K], wb[W_W], gb[G_U],
                    gb[G_U + 1], gb[G_V], gb[G_V + 1], gb[G_K], gb[G_K + 1], gb[G_W], gb[G_W + 1]);
     }
     double pmaxb = 0.0, pminb = 0.0;
@@ -267,7 +267,7 @@ __global__ void __launch_bounds__(128) k_adj_cell1(MeshView<double> m, Flow<doub
         }
     }
     // Green-Gauss reverse, own half of every face (G = acc / vol)
-    const double ivol = 1.0 / m.vol[i];
+    const double ivol = m.ivol[i];  // 1 / vol, formed once per mesh
     double accb[NG];
     for (int q = 0; q < NG; ++q) {
         accb[q] = gb[q] * ivol;

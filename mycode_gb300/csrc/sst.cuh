@@ -161,7 +161,7 @@ CFD_HD void sst_face_flux(const Flow<R>& F, S mdotA, S kL, S wL, S kR, S wR, S r
 // branches the forward takes at the same point (the same selections as the Dual forward,
 // so the VJP is the exact transpose of the J v).  Accumulates into the *b outputs.
 template <class R>
-CFD_HD void sst_cell_b(const Flow<R>& F, R r, R k, R w, R ux, R uy, R vx, R vy, R kx, R ky, R wx, R wy, R d,
+CFD_HD void sst_cell_b(const Flow<R>& F, R r, R k, R w, R ux, R uy, R vx, R vy, R kx, R ky, R wx, R wy, R idd,
                        R mutb, R F1b, R Skb, R Swb, R& rb, R& kb, R& wb, R& uxb, R& uyb, R& vxb, R& vyb, R& kxb,
                        R& kyb, R& wxb, R& wyb) {
     typedef SstConst C;
@@ -175,9 +175,8 @@ CFD_HD void sst_cell_b(const Flow<R>& F, R r, R k, R w, R ux, R uy, R vx, R vy, 
     R S2 = R(2) * (ux * ux + vy * vy + R(2) * Sxy * Sxy);
     R Smag = sqrt(S2 + R(1e-30));
     R nu = F.nu;
-    R dd = d > R(1e-30) ? d : R(1e-30);
     R gkgw = kx * wx + ky * wy;
-    const R iwp = R(1) / wp, idd = R(1) / dd;  // the forward's reciprocals (sst_cell)
+    const R iwp = R(1) / wp;  // the forward's reciprocal (sst_cell_id); idd = 1 / max(d, 1e-30)
     R CDa = R(2) * r * sw2 * gkgw * iwp;
     bool cdclip = CDa < R(1e-10);
     R CDkw = cdclip ? R(1e-10) : CDa;
@@ -291,7 +290,8 @@ CFD_HD void sst_cell_b(const Flow<R>& F, R r, R k, R w, R ux, R uy, R vx, R vy, 
 // Adjoints of sst_face_flux's inputs from (Fkb, Fwb).  gkLb / gkRb: k_x, k_y, w_x, w_y.
 template <class R>
 CFD_HD void sst_face_flux_b(const Flow<R>& F, R mdotA, R kL, R wL, R kR, R wR, R rf, R mutf, R F1f, const R* gkL,
-                            const R* gkR, bool wall, R nx, R ny, R A, R dxL, R dyL, R dxlr, R dylr, R Fkb, R Fwb,
+                            const R* gkR, bool wall, R nx, R ny, R A, R dxL, R dyL, R dxlr, R dylr, R d2lr,
+                            R id2lr, R Fkb, R Fwb,
                             R& mdotAb, R& kLb, R& wLb, R& kRb, R& wRb, R& rfb, R& mutfb, R& F1fb, R* gkLb,
                             R* gkRb) {
     typedef SstConst C;
@@ -304,9 +304,9 @@ CFD_HD void sst_face_flux_b(const Flow<R>& F, R mdotA, R kL, R wL, R kR, R wR, R
     R Dk = mu + sk * mutf, Dw = mu + sw * mutf;
     R dkn, dwn;
     R d2w = dxL * dxL + dyL * dyL, dnw = dxL * nx + dyL * ny;
-    R kx = 0, ky = 0, wx = 0, wy = 0, d2 = dxlr * dxlr + dylr * dylr;
-    bool corr = !wall && d2 > R(1e-14);
-    const R id2w = wall ? R(1) / d2w : R(0), id2 = corr ? R(1) / d2 : R(0);
+    R kx = 0, ky = 0, wx = 0, wy = 0;
+    bool corr = !wall && d2lr > R(1e-14);  // d2lr, id2lr: |x_R - x_L|^2 and its reciprocal
+    const R id2w = wall ? R(1) / d2w : R(0), id2 = corr ? id2lr : R(0);
     if (wall) {
         dkn = (R(0) - kL) * dnw * id2w;
         dwn = (R(0.5) * (wL + wR) - wL) * dnw * id2w;

@@ -107,7 +107,8 @@ void sst_cell_adj(const double* p, const double* x, const double* ob, double* xb
     Flow<double> F = flow(p, fl);
     F.sst = 1; F.k_inf = p[16]; F.w_inf = p[17];
     for (int q = 0; q < 11; ++q) xb[q] = 0;
-    sst_cell_b(F, x[0], x[1], x[2], x[3], x[4], x[5], x[6], x[7], x[8], x[9], x[10], x[11], ob[0], ob[1], ob[2],
+    const double idd = 1.0 / (x[11] > 1e-30 ? x[11] : 1e-30);
+    sst_cell_b(F, x[0], x[1], x[2], x[3], x[4], x[5], x[6], x[7], x[8], x[9], x[10], idd, ob[0], ob[1], ob[2],
                ob[3], xb[0], xb[1], xb[2], xb[3], xb[4], xb[5], xb[6], xb[7], xb[8], xb[9], xb[10]);
 }
 
