@@ -133,12 +133,12 @@ void launch_gmres_prim_z<float>(int nv, long nc, const Flow<float>& F, const flo
                              float* z, Field<float> W, const float* w, const GmresDev& d, cudaGraphConditionalHandle h,
                              cudaStream_t s) {
     // blocks of RED_THREADS (every block sums the gather kernel's partials: wide blocks keep
-    // that short, and at most RED_BLOCKS of them, grid-stride over the cells) and one block
-    // more for the Givens step; the partials it sums are the gather kernel's (gather_grid
-    // blocks with this basis precision)
+    // that short, and at most RED_BLOCKS of them and one wave, grid-stride over the cells:
+    // prim_z_grid) and one block more for the Givens step; the partials it sums are the
+    // gather kernel's (gather_grid blocks with this basis precision)
     GmresDev dd = d;
     dd.nb1 = (int)gather_grid(nc, 4);
-    NV_SWITCH(nv, (k_gmres_prim_z<float, NVC><<<red_grid(nc) + 1, RED_THREADS, 0, s>>>((int)nc, F, U, V, L, Dinv, z, W, w, dd,
+    NV_SWITCH(nv, (k_gmres_prim_z<float, NVC><<<prim_z_grid<float, NVC>(nc), RED_THREADS, 0, s>>>((int)nc, F, U, V, L, Dinv, z, W, w, dd,
                                                                                   h)));
 }
 template <>

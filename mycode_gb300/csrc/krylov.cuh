@@ -371,7 +371,7 @@ __device__ __forceinline__ void givens_column(const GmresDev& d, int j, int m, d
 // 1e-12 (src/Solver.cpp:1553-1558) keeps the scales finite; the Givens step then ends the
 // solve.  Iteration m + 1 runs only the Givens step of column m - 1.
 template <class T, int NV>
-__global__ void __launch_bounds__(256) k_gmres_prim_z(int nc, Flow<T> F, const T* __restrict__ U, T* V, long L,
+__global__ void __launch_bounds__(256, 4) k_gmres_prim_z(int nc, Flow<T> F, const T* __restrict__ U, T* V, long L,
                                                       const T* __restrict__ Dinv, T* __restrict__ z, Field<T> W,
                                                       const T* __restrict__ w, GmresDev d,
                                                       cudaGraphConditionalHandle hnd) {
@@ -710,9 +710,12 @@ __global__ void __launch_bounds__(RED_THREADS, sizeof(T) == 4 ? 2 : 1)
     pdl_wait();  // the face fluxes are the predecessor's
     pdl_trigger();
     // one pass over the cells when the dots fit the register tiles (two tiles per product
-    // with an FP32 basis, one with FP64)
+    // with an FP32 basis, one with FP64), compiled for 8, 16 and RC basis vectors: the
+    // early iterations' passes hold fewer accumulators, which leaves registers for loads in
+    // flight (the same sums, in the same order, whichever form runs)
     constexpr int RC = sizeof(T) == 4 ? KRY_RC : KRY_TILE;
-    if (j < RC) {
+    auto one_pass = [&](auto ntv) {
+        constexpr int NTV = decltype(ntv)::value;  // j < NTV
         A vw0[KRY_TILE], vw1[KRY_TILE], vp0[KRY_TILE], vp1[KRY_TILE];
 #pragma unroll
         for (int t = 0; t < KRY_TILE; ++t) vw0[t] = vw1[t] = vp0[t] = vp1[t] = A(0);
@@ -726,7 +729,7 @@ __global__ void __launch_bounds__(RED_THREADS, sizeof(T) == 4 ? 2 : 1)
             }
             gather(i, p, acc);
 #pragma unroll
-            for (int t = 0; t < RC; ++t)
+            for (int t = 0; t < NTV; ++t)
                 if (t <= j) {
                     const T* Vi = V + (long)t * L;
                     A sw = A(0), sp = A(0);
@@ -748,10 +751,17 @@ __global__ void __launch_bounds__(RED_THREADS, sizeof(T) == 4 ? 2 : 1)
         const int n0 = j + 1 < KRY_TILE ? j + 1 : KRY_TILE;
         tile_to_smem(vw0, 0, n0, wsw);
         tile_to_smem(vp0, 0, n0, wsp);
-        if (RC > KRY_TILE && j >= KRY_TILE) {
+        if (NTV > KRY_TILE && j >= KRY_TILE) {
             tile_to_smem(vw1, KRY_TILE, j + 1 - KRY_TILE, wsw);
             tile_to_smem(vp1, KRY_TILE, j + 1 - KRY_TILE, wsp);
         }
+    };
+    if (j < 8) {
+        one_pass(std::integral_constant<int, 8>());
+    } else if (j < KRY_TILE) {
+        one_pass(std::integral_constant<int, KRY_TILE>());
+    } else if (RC > KRY_TILE && j < RC) {
+        one_pass(std::integral_constant<int, RC>());
     } else {
         for (int i0 = 0; i0 <= j; i0 += KRY_TILE) {
             const int nt = (j + 1 - i0) < KRY_TILE ? (j + 1 - i0) : KRY_TILE;

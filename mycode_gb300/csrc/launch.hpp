@@ -205,6 +205,28 @@ void launch_objective(int nv, int kind, int n, const int* slots, const double* w
 // ---- device-resident GMRES (krylov.cuh); T = float in kern_f32.cu, double in kern_f64.cu
 #include "krylov.cuh"
 namespace cfdg {
+// Blocks of k_gmres_prim_z: its cell blocks (grid-stride, elementwise: the count changes no
+// result) and the Givens block, no more than are resident on the GPU at once at the
+// kernel's register count.  A second, partial wave of cell blocks runs at a fraction of the
+// SMs' memory parallelism and about doubles the kernel's time (the FP32 SST form: 77
+// registers, three blocks per SM, 609 blocks at 4M cells).
+template <class T, int NV>
+unsigned prim_z_grid(long nc) {
+    static int cap = 0;  // resident blocks on this GPU
+    if (cap == 0) {
+        int dev = 0, sms = 0, per = 0;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_gmres_prim_z<T, NV>, RED_THREADS, 0);
+        cap = sms * per > 2 ? sms * per : 2;
+    }
+    long b = (nc + RED_THREADS - 1) / RED_THREADS;
+    if (b > RED_BLOCKS) b = RED_BLOCKS;
+    if (b > cap - 1) b = cap - 1;
+    if (b < 1) b = 1;
+    return (unsigned)b + 1;
+}
+
 void launch_gmres_backsub(const GmresDev& d, cudaStream_t s);
 // solve state and V0 = rhs / |rhs| (|rhs|^2 from *bsq, or d.beta[2] when bsq is null)
 template <class T> void launch_gmres_start(long n, T* V0, const double* rhs, const GmresDev& d, int m, double tol,
