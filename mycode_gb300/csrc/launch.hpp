@@ -212,17 +212,21 @@ namespace cfdg {
 // registers, three blocks per SM, 609 blocks at 4M cells).
 template <class T, int NV>
 unsigned prim_z_grid(long nc) {
-    static int cap = 0;  // resident blocks on this GPU
+    static int cap = 0;  // resident blocks on this GPU (0: not known yet)
     if (cap == 0) {
         int dev = 0, sms = 0, per = 0;
-        cudaGetDevice(&dev);
-        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_gmres_prim_z<T, NV>, RED_THREADS, 0);
-        cap = sms * per > 2 ? sms * per : 2;
+        if (cudaGetDevice(&dev) == cudaSuccess &&
+            cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) == cudaSuccess &&
+            cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_gmres_prim_z<T, NV>, RED_THREADS, 0) == cudaSuccess &&
+            sms * per > 1)
+            cap = sms * per;
+        else
+            cudaGetLastError();  // a failed query leaves no error behind; the grid is then
+                                 // capped at RED_BLOCKS only, and the query runs again next time
     }
     long b = (nc + RED_THREADS - 1) / RED_THREADS;
     if (b > RED_BLOCKS) b = RED_BLOCKS;
-    if (b > cap - 1) b = cap - 1;
+    if (cap > 1 && b > cap - 1) b = cap - 1;
     if (b < 1) b = 1;
     return (unsigned)b + 1;
 }
