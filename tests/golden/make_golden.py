@@ -18,6 +18,10 @@ Writes
   bump_residual_history.csv  the reference's shipped trace results/residual_history.csv
   bump_sol_9999.npz        Mach, Pressure, Density of the reference's shipped
                            results/sol_9999.vtk
+  plate_nasa.msh.gz        the reference's mesh/new_laminar_flat_plate (its NASA laminar
+                           flat plate, 6,962 quads) with LF line ends
+  plate_cf_profile.csv     the reference's shipped skin-friction profile of that case
+                           (results/data/cf_profile.csv: x, Cf, Blasius Cf)
 """
 import gzip
 import os
@@ -117,6 +121,18 @@ def gen_bump():
                         cfl=tr["cfl"], gmres_iters=tr["gmres_iters"], U=U[:, :4])
 
 
+def gen_plate():
+    for name, out in (("new_laminar_flat_plate", "plate_nasa.msh.gz"),):
+        with open(os.path.join(REF_SRC, "mesh", name), "rb") as fh:
+            text = fh.read().replace(b"\r", b"")
+        with gzip.open(os.path.join(HERE, out), "wb", compresslevel=9) as fh:
+            fh.write(text)
+    with open(os.path.join(REF_SRC, "results", "data", "cf_profile.csv"), "rb") as fh:
+        csv = fh.read().replace(b"\r", b"")
+    with open(os.path.join(HERE, "plate_cf_profile.csv"), "wb") as fh:
+        fh.write(csv)
+
+
 def parse_vtk_cell_scalars(path):
     with open(path, "r", newline="") as fh:
         lines = [l.strip() for l in fh]
@@ -139,5 +155,6 @@ if __name__ == "__main__":
         raise SystemExit("no reference checkout: set CFD_REFERENCE (see oracle/build_ref.py)")
     gen_cases()
     gen_bump()
+    gen_plate()
     for f in sorted(os.listdir(HERE)):
         print(f, os.path.getsize(os.path.join(HERE, f)))

@@ -99,3 +99,36 @@ def test_objective_gradient_matches_central_differences(kind):
 def test_pressure_drag_objective_is_calculate_drag():
     o, r, _ = _pair("supersonic")
     assert o.objective("pressure_drag", gradient=False) == r.drag()
+
+
+def test_nasa_plate_fixture_wall_and_blasius_columns(tmp_path):
+    """The reference's NASA laminar flat plate (its mesh and shipped results/data/cf_profile.csv,
+    tests/golden/make_golden.py): the profile's x column is the tag-4 face midpoints of the
+    mesh as this project ingests it, and its Blasius column 0.664 / sqrt(Re_x) follows from
+    the flow set up as the reference's plate case does (setFlowConditions(0.1, 41368.5,
+    388.89), setKinematicViscosity(2e5, 0.3048); src/Solver.cpp:34-43, :1899-1979)."""
+    import gzip
+    import os
+
+    from mycode_gb300 import meshgen as mg
+
+    gold = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
+    p = tmp_path / "plate_nasa.msh"
+    with gzip.open(os.path.join(gold, "plate_nasa.msh.gz"), "rb") as fh:
+        p.write_bytes(fh.read())
+    spec = mg.read_gmsh(str(p))
+    assert spec.n_cells == 6962
+    prof = np.loadtxt(os.path.join(gold, "plate_cf_profile.csv"), delimiter=",", skiprows=1)
+    o = OracleSolver(spec, bcset="plate", viscous=True, init="freestream")
+    o.setFlowConditions(0.1, 41368.5, 388.89)
+    o.setKinematicViscosity(200000.0, 0.3048)
+    o.initialize()
+    x, cp, cf = o.wall_coefficients(4)
+    order = np.argsort(x, kind="stable")
+    assert len(x) == len(prof) == 79
+    np.testing.assert_allclose(x[order], prof[:, 0], rtol=5e-6)
+    par = o.params()
+    gam = 1.4
+    u_inf = par["M_inf"] * np.sqrt(gam * par["R_gas"] * par["T0"] / (1.0 + 0.5 * (gam - 1.0) * par["M_inf"] ** 2))
+    blasius = 0.664 / np.sqrt(u_inf * prof[:, 0] / par["nu"])
+    np.testing.assert_allclose(blasius, prof[:, 2], rtol=1e-5)
