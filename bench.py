@@ -1038,6 +1038,8 @@ def profile_case(args):
         gm["gmres_m"] = args.gmres_m
     if args.gmres_tol is not None:
         gm["gmres_tol"] = args.gmres_tol
+    if args.gather_split_cells is not None:
+        gm["gather_split_cells"] = args.gather_split_cells
     if args.profile_workload == "laminar_plate":
         m = api.Mesh.from_spec(meshgen.laminar_plate(240, 120, ratio=1.08))
         s = api.Solver(m, bcset="plate", init="freestream", viscous=1, flux="ROE", spatial="SECOND_ORDER_CENTRAL",
@@ -1170,6 +1172,8 @@ def main():
     ap.add_argument("--reps", type=int, default=3)
     ap.add_argument("--gmres-m", type=int, default=None, help="profile case: Krylov dimension")
     ap.add_argument("--gmres-tol", type=float, default=None, help="profile case: GMRES tolerance (0: m iterations)")
+    ap.add_argument("--gather-split-cells", type=int, default=None,
+                    help="profile case: cfdg_config.gather_split_cells (-1: the fused gather/dot kernel at any size)")
     args = ap.parse_args()
     if args.warmup < 3 and not args.profile_case:
         ap.error("--warmup must be at least 3")

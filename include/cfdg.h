@@ -120,7 +120,7 @@ typedef struct cfdg_config {
     /* exact J v Arnoldi body: from this many cells the gather of J v and the iteration's
      * dots run as two kernels (the fused kernel's dependent face gathers hold back its
      * streaming dots on large meshes); the same results bit for bit either way.
-     * 0 = the default, 262,144 cells; a negative value never splits. */
+     * 0 = the default, 150,000 cells; a negative value never splits. */
     int gather_split_cells;
 } cfdg_config;
 

@@ -51,8 +51,10 @@ constexpr int KRY_BODY_ITERS = 4;
 // Default cell count from which the gather and the dots of an Arnoldi iteration run as two
 // kernels (k_gmres_gather_w, then k_gmres_gather_dot<..., true>; cfdg_config
 // gather_split_cells): on large meshes the fused kernel's per-cell dependent face gathers
-// hold back its streaming dots; on small ones the kernel boundary costs more than it saves.
-constexpr long KRY_SPLIT_GATHER_CELLS = 262144;
+// hold back its streaming dots; on small ones the kernel boundary costs more than it saves
+// (stream-driver stage times, laminar bump, FP32 basis: fused / split 10.1 / 12.4 us at 60k
+// cells, 14.7 / 16.2 at 119k, 39.7 / 26.2 at 250k, 114 / 67 at 1M).
+constexpr long KRY_SPLIT_GATHER_CELLS = 150000;
 
 struct GmresDev {
     int* gi;          // [0] j (FD body), [1] k (last iteration), [2] done, [3] m, [4] this iteration
