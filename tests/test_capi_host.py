@@ -38,6 +38,17 @@ def test_config_defaults_follow_reference():
     assert c.cfl0 == 0.1 and c.cfl_max == 1e4 and c.limiter_freeze_step == 150 and c.limiter_freeze_cfl == 10.0
 
 
+def test_config_defaults_leave_the_reference_algorithm_untouched():
+    """Off by default: the start-up aids (no reference counterpart) and the persistent
+    Arnoldi kernel; automatic (0): the Krylov driver, the barrier poll limit and the size
+    from which the Arnoldi body splits its gather and dots (results the same either way)."""
+    c = api.default_config()
+    assert c.precision == 0 and c.jv == 0  # FP64 with the reference's FD J v
+    assert c.startup_first_order == 0 and c.update_limit == 0.0
+    assert c.persistent == 0 and c.barrier_poll_limit == 0 and c.gather_split_cells == 0
+    assert c.krylov == -1 and c.pdl == 1 and c.newton_chain == 8
+
+
 @pytest.mark.parametrize("spec_fn", [lambda: mg.mixed_box(8, 6), lambda: mg.wedge(12, 8),
                                      lambda: mg.laminar_plate(12, 8, ratio=1.2), lambda: mg.bump(3000, seed=1)])
 @pytest.mark.parametrize("renumber", ["none", "hilbert", "rcm"])
