@@ -22,6 +22,10 @@ Writes
                            flat plate, 6,962 quads) with LF line ends
   plate_cf_profile.csv     the reference's shipped skin-friction profile of that case
                            (results/data/cf_profile.csv: x, Cf, Blasius Cf)
+  plate_nasa_ref.npz       the reference's own run of that case (compiled from its current
+                           sources; src/main.cpp's settings, solveImplicit(1e-4, 50000)):
+                           Newton steps, last res_vm, and x, Cf of the tag-4 faces at full
+                           precision (about 45 minutes of one core)
 """
 import gzip
 import os
@@ -131,6 +135,30 @@ def gen_plate():
         csv = fh.read().replace(b"\r", b"")
     with open(os.path.join(HERE, "plate_cf_profile.csv"), "wb") as fh:
         fh.write(csv)
+    from oracle.oracle import OracleSolver
+    spec = mg.read_gmsh(os.path.join(REF_SRC, "mesh", "new_laminar_flat_plate"))
+    runs = []
+    for cls, kw in ((RefSolver, dict(variant="plate_visc")),
+                    (OracleSolver, dict(bcset="plate", viscous=True, init="freestream"))):
+        r = cls(spec, **kw)
+        r.setNumericalMethod("HLLC", "SECOND_ORDER_CENTRAL")
+        r.setFlowConditions(0.1, 41368.5, 388.89)
+        r.setKinematicViscosity(200000.0, 0.3048)
+        r.initialize()
+        tr = r.solveImplicit(1e-4, 50000)
+        runs.append((tr["res_vm"], r.get_state()))
+    (rv, U), (ov, Uo) = runs
+    assert len(rv) == len(ov) and np.array_equal(U, Uo), "oracle and reference disagree on the plate"
+    # the oracle's wall coefficients at the reference's final state (the same state bit for bit)
+    o = OracleSolver(spec, bcset="plate", viscous=True, init="freestream")
+    o.setFlowConditions(0.1, 41368.5, 388.89)
+    o.setKinematicViscosity(200000.0, 0.3048)
+    o.initialize()
+    o.set_state(U)
+    x, cp, cf = o.wall_coefficients(4)
+    order = np.argsort(x, kind="stable")
+    np.savez_compressed(os.path.join(HERE, "plate_nasa_ref.npz"), steps=len(rv), res_vm_last=rv[-1],
+                        x=x[order], cf=cf[order])
 
 
 def parse_vtk_cell_scalars(path):
