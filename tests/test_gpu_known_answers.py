@@ -1,7 +1,9 @@
 """The known-answer properties of tests/test_oracle_known_answers.py on the GPU path:
 free-stream preservation of the FP64 residual (every scheme and order, inviscid and
 viscous) and of the FP32 residual, Green-Gauss exactness for linear fields on a uniform
-grid, and the Barth-Jespersen limiter's bounds and its value 1 for a linear pressure."""
+grid, the Barth-Jespersen limiter's bounds and its value 1 for a linear pressure, and
+plane Couette flow (zero mass and momentum residual, the energy residual the viscous
+heating)."""
 import numpy as np
 import pytest
 
@@ -72,3 +74,11 @@ def test_limiter_bounds_and_linear_pressure(cuda_lib):
     s.initialize()
     phi = s.limiters(o.state_from_primitives(prim))
     assert (phi[K._layers_from_boundary(spec, 2)] == 1.0).all()
+
+
+def test_plane_couette_flow(cuda_lib):
+    spec = mg.box(10, 8)
+    _, U, keep, vol, tau, heat = K.couette(spec)
+    s = cuda_lib.Solver(cuda_lib.Mesh.from_spec(spec), bcset="plate", viscous=1, init="freestream")
+    K.couette_setup(s)
+    K.check_couette(s, U, keep, vol, tau, heat, s.computeResiduals)

@@ -11,6 +11,12 @@ the bit-exact parity tests, the GPU path) to the mathematics as well as to the r
                         quad grid (src/Solver.cpp:81-149)
   Barth-Jespersen       phi in [0, 1] for any state, and phi = 1 on interior cells for a linear
                         pressure field (src/Solver.cpp:152-253)
+  plane Couette flow    u = a y, v = 0, constant rho and p: the stress mu a is uniform, so the
+                        mass and momentum residuals vanish on interior cells for every scheme
+                        and order, and the energy residual is the viscous heating
+                        -mu a^2 vol wherever the scheme adds no dissipation of its own (HLLC,
+                        which resolves the shear wave, and every flux with the limited
+                        reconstruction, exact for a linear field) (src/Solver.cpp:543-800)
 """
 import numpy as np
 import pytest
@@ -152,3 +158,45 @@ def test_limiter_bounds_and_linear_pressure():
     phi = o.limiters(o.state_from_primitives(prim))
     keep = _layers_from_boundary(spec, 2)
     assert (phi[keep] == 1.0).all()
+
+
+def couette(spec):
+    """The plane Couette state on `spec` (cells in the spec's numbering), from an oracle set
+    up with the reference's setters: the oracle, the state, interior cells, cell volumes, the
+    stress scale mu a A and the heating mu a^2."""
+    o = OracleSolver(spec, bcset="plate", viscous=True, init="freestream")
+    couette_setup(o)
+    cells = o.cells()
+    y = cells[:, 2]
+    a, rho = 400.0, 1.2
+    U = np.stack([_cons(rho, 30.0 + a * yc, 0.0, 1e5) for yc in y])
+    mu = rho * o.params()["nu"]
+    keep = _layers_from_boundary(spec, 2)
+    return o, U, keep, cells[:, 0], mu * a * o.faces()[1][:, 2].max(), mu * a * a
+
+
+def couette_setup(s):
+    s.setFreestreamStatic(0.2, 101325.0, 300.0)
+    s.setKinematicViscosity(1e3, 1.0)
+    s.initialize()
+
+
+COUETTE_EXACT_ENERGY = [(fl, sp) for fl in C.FLUXES for sp in C.SPATIALS if fl == "HLLC" or sp == "SECOND_ORDER_LIMITED"]
+
+
+def check_couette(s, U, keep, vol, tau, heat, residual):
+    for fl in C.FLUXES:
+        for sp in C.SPATIALS:
+            s.setNumericalMethod(fl, sp)
+            R = residual(U)
+            assert np.abs(R[keep, 0]).max() <= 1e-11 * tau, (fl, sp)
+            assert np.abs(R[keep, 1:3]).max() <= 1e-11 * tau, (fl, sp)
+            if (fl, sp) in COUETTE_EXACT_ENERGY:
+                want = -heat * vol[keep]
+                assert np.abs(R[keep, 3] / want - 1.0).max() <= 1e-10, (fl, sp)
+
+
+def test_plane_couette_flow():
+    o, U, keep, vol, tau, heat = couette(mg.box(10, 8))
+    assert keep.sum() >= 20
+    check_couette(o, U, keep, vol, tau, heat, o.residual)
