@@ -3,7 +3,7 @@ free-stream preservation of the FP64 residual (every scheme and order, inviscid 
 viscous) and of the FP32 residual, Green-Gauss exactness for linear fields on a uniform
 grid, the Barth-Jespersen limiter's bounds and its value 1 for a linear pressure, and
 plane Couette flow (zero mass and momentum residual, the energy residual the viscous
-heating)."""
+heating) and plane Poiseuille flow (zero mass and momentum residual)."""
 import numpy as np
 import pytest
 
@@ -82,3 +82,11 @@ def test_plane_couette_flow(cuda_lib):
     s = cuda_lib.Solver(cuda_lib.Mesh.from_spec(spec), bcset="plate", viscous=1, init="freestream")
     K.couette_setup(s)
     K.check_couette(s, U, keep, vol, tau, heat, s.computeResiduals)
+
+
+def test_plane_poiseuille_flow(cuda_lib):
+    spec = mg.box(10, 8)
+    _, U, keep, scale = K.poiseuille(spec)
+    s = cuda_lib.Solver(cuda_lib.Mesh.from_spec(spec), bcset="plate", viscous=1, init="freestream")
+    K.couette_setup(s)
+    K.check_poiseuille(s, U, keep, scale, s.computeResiduals)

@@ -17,6 +17,11 @@ the bit-exact parity tests, the GPU path) to the mathematics as well as to the r
                         -mu a^2 vol wherever the scheme adds no dissipation of its own (HLLC,
                         which resolves the shear wave, and every flux with the limited
                         reconstruction, exact for a linear field) (src/Solver.cpp:543-800)
+  plane Poiseuille flow u = u0 + b y (y - 1) with mu u'' = dp/dx, p linear in x, constant rho:
+                        with the limited reconstruction (exact at the faces for the linear p and
+                        the quadratic u, phi = 1) the interior mass and momentum residuals
+                        vanish for every flux: the Green-Gauss gradients, their face average
+                        and its correction are exact for quadratics on a uniform grid
 """
 import numpy as np
 import pytest
@@ -200,3 +205,28 @@ def test_plane_couette_flow():
     o, U, keep, vol, tau, heat = couette(mg.box(10, 8))
     assert keep.sum() >= 20
     check_couette(o, U, keep, vol, tau, heat, o.residual)
+
+
+def poiseuille(spec):
+    """The plane Poiseuille state on `spec` (u from 37 to 60 m/s, dp/dx = -20 Pa/m): the
+    oracle, the state, interior cells and the scale |dp/dx| vol."""
+    o = OracleSolver(spec, bcset="plate", viscous=True, init="freestream")
+    couette_setup(o)
+    cells = o.cells()
+    x, y = cells[:, 1], cells[:, 2]
+    rho, dpdx = 1.2, -20.0
+    b = dpdx / (2.0 * rho * o.params()["nu"])
+    U = np.stack([_cons(rho, 30.0 + b * yc * (yc - 1.0), 0.0, 1e5 + dpdx * xc) for xc, yc in zip(x, y)])
+    return o, U, _layers_from_boundary(spec, 2), abs(dpdx) * cells[:, 0].max()
+
+
+def check_poiseuille(s, U, keep, scale, residual):
+    for fl in C.FLUXES:
+        s.setNumericalMethod(fl, "SECOND_ORDER_LIMITED")
+        R = residual(U)
+        assert np.abs(R[keep, :3]).max() <= 1e-10 * scale, fl
+
+
+def test_plane_poiseuille_flow():
+    o, U, keep, scale = poiseuille(mg.box(10, 8))
+    check_poiseuille(o, U, keep, scale, o.residual)
