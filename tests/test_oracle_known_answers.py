@@ -17,6 +17,10 @@ the bit-exact parity tests, the GPU path) to the mathematics as well as to the r
                         -mu a^2 vol wherever the scheme adds no dissipation of its own (HLLC,
                         which resolves the shear wave, and every flux with the limited
                         reconstruction, exact for a linear field) (src/Solver.cpp:543-800)
+  oblique shock        the converged supersonic wedge (M 2.5, 15 degree ramp from x = 0.5,
+                        tests/golden/wedge_converged.npz, the oracle's solution, bit for bit
+                        the compiled reference's): wall Cp 0 upstream of the ramp and, past the
+                        shock foot, the theta-beta-M relation's weak-shock value
   plane Poiseuille flow u = u0 + b y (y - 1) with mu u'' = dp/dx, p linear in x, constant rho:
                         with the limited reconstruction (exact at the faces for the linear p and
                         the quadratic u, phi = 1) the interior mass and momentum residuals
@@ -230,3 +234,31 @@ def check_poiseuille(s, U, keep, scale, residual):
 def test_plane_poiseuille_flow():
     o, U, keep, scale = poiseuille(mg.box(10, 8))
     check_poiseuille(o, U, keep, scale, o.residual)
+
+
+def oblique_shock_cp(mach, theta_deg, gamma=GAMMA):
+    """Wall Cp behind the weak attached oblique shock of a wedge (the theta-beta-M relation
+    tan theta = 2 cot beta (M^2 sin^2 beta - 1) / (M^2 (gamma + cos 2 beta) + 2), then the
+    normal-shock pressure ratio of M sin beta)."""
+    from scipy.optimize import brentq
+    th = np.radians(theta_deg)
+
+    def f(b):
+        m2s = mach * mach * np.sin(b) ** 2
+        return np.tan(th) - 2.0 / np.tan(b) * (m2s - 1.0) / (mach * mach * (gamma + np.cos(2.0 * b)) + 2.0)
+
+    beta = brentq(f, np.arcsin(1.0 / mach) + 1e-9, np.radians(64.0))  # the weak root
+    p21 = 1.0 + 2.0 * gamma / (gamma + 1.0) * (mach * mach * np.sin(beta) ** 2 - 1.0)
+    return (p21 - 1.0) / (0.5 * gamma * mach * mach), np.degrees(beta)
+
+
+def test_wedge_ramp_pressure_is_the_oblique_shock_value():
+    import os
+    d = np.load(os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden", "wedge_converged.npz"))
+    x, cp = d["x_wall"], d["cp_wall"]
+    cp_th, beta = oblique_shock_cp(2.5, 15.0)
+    assert abs(beta - 36.945) < 1e-2 and abs(cp_th - 0.33543) < 1e-4
+    assert np.abs(cp[x < 0.45]).max() <= 1e-12
+    ramp = x > 0.65
+    assert ramp.sum() >= 10
+    assert np.abs(cp[ramp] / cp_th - 1.0).max() <= 1e-2
