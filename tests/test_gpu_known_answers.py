@@ -3,7 +3,8 @@ free-stream preservation of the FP64 residual (every scheme and order, inviscid 
 viscous) and of the FP32 residual, Green-Gauss exactness for linear fields on a uniform
 grid, the Barth-Jespersen limiter's bounds and its value 1 for a linear pressure, and
 plane Couette flow (zero mass and momentum residual, the energy residual the viscous
-heating) and plane Poiseuille flow (zero mass and momentum residual)."""
+heating), plane Poiseuille flow (zero mass and momentum residual) and discrete
+conservation in a box closed by slip walls."""
 import numpy as np
 import pytest
 
@@ -90,3 +91,10 @@ def test_plane_poiseuille_flow(cuda_lib):
     s = cuda_lib.Solver(cuda_lib.Mesh.from_spec(spec), bcset="plate", viscous=1, init="freestream")
     K.couette_setup(s)
     K.check_poiseuille(s, U, keep, scale, s.computeResiduals)
+
+
+def test_discrete_conservation_in_a_closed_box(cuda_lib):
+    for spec, bc, visc, _, U, scale in K.closed_box_cases():
+        s = cuda_lib.Solver(cuda_lib.Mesh.from_spec(spec), bcset=bc, viscous=int(visc), init="freestream")
+        K.closed_box_setup(s)
+        K.check_closed_box(s, U, visc, scale, s.computeResiduals)

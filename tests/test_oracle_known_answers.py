@@ -17,6 +17,9 @@ the bit-exact parity tests, the GPU path) to the mathematics as well as to the r
                         -mu a^2 vol wherever the scheme adds no dissipation of its own (HLLC,
                         which resolves the shear wave, and every flux with the limited
                         reconstruction, exact for a linear field) (src/Solver.cpp:543-800)
+  discrete             in a box closed by slip walls the interior face fluxes telescope: the
+  conservation         cells' mass residuals sum to zero (and, inviscid, their energy
+                        residuals) for any state, scheme, order and BC set
   oblique shock        the converged supersonic wedge (M 2.5, 15 degree ramp from x = 0.5,
                         tests/golden/wedge_converged.npz, the oracle's solution, bit for bit
                         the compiled reference's): wall Cp 0 upstream of the ramp and, past the
@@ -262,3 +265,40 @@ def test_wedge_ramp_pressure_is_the_oblique_shock_value():
     ramp = x > 0.65
     assert ramp.sum() >= 10
     assert np.abs(cp[ramp] / cp_th - 1.0).max() <= 1e-2
+
+
+def closed_box_cases():
+    """(solver arguments, perturbed state, mass scale) for a jittered triangulated box
+    closed by slip walls, every BC set, inviscid and viscous."""
+    ts = mg.TAG_SLIP
+    spec = mg.box(12, 9, split=True, jitter=0.15, seed=4, tags=(ts, ts, ts, ts))
+    out = []
+    for bc in ("bump", "plate", "supersonic"):
+        for visc in (False, True):
+            o = OracleSolver(spec, bcset=bc, viscous=visc, init="freestream")
+            closed_box_setup(o)
+            U = C.perturbed_state(o.get_state(), o.cells(), seed=3, amplitude=0.1)
+            scale = np.abs(U[:, 0]).max() * 100.0 * o.faces()[1][:, 2].max()
+            out.append((spec, bc, visc, o, U, scale))
+    return out
+
+
+def closed_box_setup(s):
+    s.setFreestreamStatic(0.3, 101325.0, 300.0)
+    s.setKinematicViscosity(1e3, 1.0)
+    s.initialize()
+
+
+def check_closed_box(s, U, visc, scale, residual):
+    for fl in C.FLUXES:
+        for sp in C.SPATIALS:
+            s.setNumericalMethod(fl, sp)
+            R = residual(U)
+            assert abs(R[:, 0].sum()) <= 1e-13 * scale, (fl, sp, visc)
+            if not visc:  # slip walls do no pressure work; the viscous wall terms do
+                assert abs(R[:, 3].sum()) <= 1e-13 * scale * 3e5, (fl, sp)
+
+
+def test_discrete_conservation_in_a_closed_box():
+    for spec, bc, visc, o, U, scale in closed_box_cases():
+        check_closed_box(o, U, visc, scale, o.residual)
