@@ -3,8 +3,8 @@ free-stream preservation of the FP64 residual (every scheme and order, inviscid 
 viscous) and of the FP32 residual, Green-Gauss exactness for linear fields on a uniform
 grid, the Barth-Jespersen limiter's bounds and its value 1 for a linear pressure, and
 plane Couette flow (zero mass and momentum residual, the energy residual the viscous
-heating), plane Poiseuille flow (zero mass and momentum residual) and discrete
-conservation in a box closed by slip walls."""
+heating), plane Poiseuille flow (zero mass and momentum residual), discrete
+conservation in a box closed by slip walls and the residual's rotation with the mesh."""
 import numpy as np
 import pytest
 
@@ -98,3 +98,12 @@ def test_discrete_conservation_in_a_closed_box(cuda_lib):
         s = cuda_lib.Solver(cuda_lib.Mesh.from_spec(spec), bcset=bc, viscous=int(visc), init="freestream")
         K.closed_box_setup(s)
         K.check_closed_box(s, U, visc, scale, s.computeResiduals)
+
+
+def test_residual_rotates_with_the_mesh(cuda_lib):
+    for spec, rspec, visc, U, Ur, keep, cs in K.rotated_cases():
+        a = cuda_lib.Solver(cuda_lib.Mesh.from_spec(spec), bcset="plate", viscous=int(visc), init="freestream")
+        b = cuda_lib.Solver(cuda_lib.Mesh.from_spec(rspec), bcset="plate", viscous=int(visc), init="freestream")
+        for x in (a, b):
+            K.closed_box_setup(x)
+        K.check_rotated(a, b, U, Ur, keep, cs, a.computeResiduals, b.computeResiduals)

@@ -17,6 +17,10 @@ the bit-exact parity tests, the GPU path) to the mathematics as well as to the r
                         -mu a^2 vol wherever the scheme adds no dissipation of its own (HLLC,
                         which resolves the shear wave, and every flux with the limited
                         reconstruction, exact for a linear field) (src/Solver.cpp:543-800)
+  rotated residual     rotating the mesh and every cell's velocity by one angle rotates the
+                        momentum rows of the whole residual (reconstruction, limiter, Riemann
+                        and viscous fluxes) on cells three layers from the boundary and leaves
+                        mass and energy unchanged, every scheme and order
   discrete             in a box closed by slip walls the interior face fluxes telescope: the
   conservation         cells' mass residuals sum to zero (and, inviscid, their energy
                         residuals) for any state, scheme, order and BC set
@@ -302,3 +306,47 @@ def check_closed_box(s, U, visc, scale, residual):
 def test_discrete_conservation_in_a_closed_box():
     for spec, bc, visc, o, U, scale in closed_box_cases():
         check_closed_box(o, U, visc, scale, o.residual)
+
+
+def rotated_cases(angle=0.7):
+    """(mesh, rotated mesh, viscous, state, rotated state, interior cells, rotation) for a
+    jittered triangulated box, inviscid and viscous."""
+    import copy
+    spec = mg.box(14, 10, split=True, jitter=0.15, seed=7)
+    c, s = np.cos(angle), np.sin(angle)
+    rspec = copy.deepcopy(spec)
+    rspec.nodes = spec.nodes @ np.array([[c, s], [-s, c]])
+    keep = _layers_from_boundary(spec, 3)
+    out = []
+    for visc in (False, True):
+        o = OracleSolver(spec, bcset="plate", viscous=visc, init="freestream")
+        closed_box_setup(o)
+        U = C.perturbed_state(o.get_state(), o.cells(), seed=3, amplitude=0.1)
+        Ur = U.copy()
+        Ur[:, 1] = c * U[:, 1] - s * U[:, 2]
+        Ur[:, 2] = s * U[:, 1] + c * U[:, 2]
+        out.append((spec, rspec, visc, U, Ur, keep, (c, s)))
+    return out
+
+
+def check_rotated(a, b, U, Ur, keep, cs, residual_a, residual_b):
+    c, s = cs
+    for fl in C.FLUXES:
+        for sp in C.SPATIALS:
+            a.setNumericalMethod(fl, sp)
+            b.setNumericalMethod(fl, sp)
+            R, Rr = residual_a(U), residual_b(Ur)
+            back = Rr.copy()
+            back[:, 1] = c * Rr[:, 1] + s * Rr[:, 2]
+            back[:, 2] = -s * Rr[:, 1] + c * Rr[:, 2]
+            scale = np.abs(R[keep, :4]).max(axis=0)
+            assert (np.abs(back[keep, :4] - R[keep, :4]).max(axis=0) <= 1e-12 * scale).all(), (fl, sp)
+
+
+def test_residual_rotates_with_the_mesh():
+    for spec, rspec, visc, U, Ur, keep, cs in rotated_cases():
+        a = OracleSolver(spec, bcset="plate", viscous=visc, init="freestream")
+        b = OracleSolver(rspec, bcset="plate", viscous=visc, init="freestream")
+        for x in (a, b):
+            closed_box_setup(x)
+        check_rotated(a, b, U, Ur, keep, cs, a.residual, b.residual)
