@@ -80,6 +80,26 @@ def test_gmsh_loader_accepts_crlf_and_lf(tmp_path):
         np.testing.assert_array_equal(m.faces()[1], ms.faces()[1])
 
 
+@pytest.mark.parametrize("renumber", ["none", "hilbert"])
+def test_reference_plate_mesh_file_ingest_bit_exact_with_oracle(tmp_path, renumber):
+    """The reference's own NASA laminar plate mesh (Gmsh 2.2, 6,962 quads) through the
+    library's C++ reader and host connectivity against the oracle's ingest of the same file."""
+    import gzip
+
+    gold = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
+    p = tmp_path / "plate_nasa.msh"
+    with gzip.open(os.path.join(gold, "plate_nasa.msh.gz"), "rb") as fh:
+        p.write_bytes(fh.read())
+    m = api.Mesh.load(str(p), renumber=renumber)
+    o = OracleSolver(mg.read_gmsh(str(p)))
+    assert (m.n_cells, m.n_faces) == (o.n_cells, o.n_faces) and m.n_cells == 6962
+    mi, md = m.faces()
+    oi, od = o.faces()
+    np.testing.assert_array_equal(mi, oi)
+    np.testing.assert_array_equal(md, od)
+    np.testing.assert_array_equal(m.cells(), o.cells())
+
+
 def test_mesh_errors_are_reported(tmp_path):
     with pytest.raises(api.CfdgError) as e:
         api.Mesh.load(str(tmp_path / "missing.msh"))
